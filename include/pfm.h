@@ -1,0 +1,189 @@
+/*
+ * pfm.h -- C ABI of libpfm.so, the sm_103a (GB300) implementation of the particle-flow-map time
+ * step of the impulse-based Eulerian-Lagrangian fluid solver (zjw49246/particle-flow-maps).
+ *
+ * Every entry point replaces one Taichi kernel (or kernel group) that the reference's step loop
+ * calls; each declaration cites the reference interface it replaces (path:line within the
+ * reference project).  Conventions:
+ *
+ *  - All array arguments are caller-owned DEVICE pointers (e.g. torch tensor data_ptr()).
+ *  - Grid fields are f32, C-order with the last index fastest, face grids padded by one along
+ *    their own axis: u_x [nx+1][ny][nz], u_y [nx][ny+1][nz], u_z [nx][ny][nz+1]
+ *    (2D: u_x [nx+1][ny], u_y [nx][ny+1]); cell fields [nx][ny][nz].
+ *  - Particle fields are structure-of-arrays: a field of n-vectors is n contiguous runs of P
+ *    floats ([n][P]).  A per-particle set of d vectors of size d (T_x/T_y/T_z, init_C_x/..)
+ *    is [d][d][P]: vector v, component c of particle q sits at (v*d + c)*P + q.
+ *    (The reference's Taichi layout is AoS [P][n]; the Python layer converts for the oracle.)
+ *  - Every call takes the CUDA stream to run on (cudaStream_t passed as void*) and is
+ *    asynchronous, except where a function is documented as a synchronization point because it
+ *    returns a host value.
+ *  - Every function returns a pfm_status; pfm_last_error() gives the message of the last error
+ *    on that handle.  A handle is used by one host thread at a time.
+ */
+#ifndef PFM_H_
+#define PFM_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum pfm_status {
+  PFM_OK = 0,
+  PFM_ERR_NULL = 1,           /* a required pointer is NULL */
+  PFM_ERR_SHAPE = 2,          /* configuration / size mismatch */
+  PFM_ERR_WORKSPACE = 3,      /* no workspace bound, or too small */
+  PFM_ERR_NOT_CONVERGED = 4,  /* MGPCG reached max_iters (results are still written) */
+  PFM_ERR_NONFINITE = 5,      /* NaN/Inf met in a reduction */
+  PFM_ERR_CUDA = 6,           /* a CUDA runtime call failed */
+  PFM_ERR_ARG = 7             /* an argument is out of range */
+} pfm_status;
+
+/* Solver configuration.  Mirrors MGPCG_3(boundary_types, N, base_level) (3D/mgpcg.py:350-357,
+ * 17-60) and the step constants of hyperparameters.py. */
+typedef struct pfm_config {
+  int dim;                   /* 2 or 3 */
+  int res[3];                /* res_x, res_y, res_z (res_z ignored in 2D) */
+  double dx;                 /* cell size; the reference uses dx = 1/res_y (3D/run_3D.py:16) */
+  int64_t particles;         /* particle count P */
+  int base_level;            /* level formula int(log2(min N)) - base_level + 1 (3D/mgpcg.py:28) */
+  int mg_levels;             /* > 0 overrides the formula */
+  int pre_post_smoothing;    /* 2 (3D/mgpcg.py:29) */
+  int bottom_smoothing;      /* 50 (3D/mgpcg.py:30) */
+  int boundary[3][2];        /* 1 = Dirichlet, 2 = Neumann, per axis low/high (3D/run_3D.py:28) */
+  int use_apic;              /* hyperparameters.use_APIC */
+} pfm_config;
+
+typedef struct pfm_handle pfm_handle;
+
+/* Options and statistics of one MGPCG solve: MGPCG.solve(max_iters, eps, tol)
+ * (3D/mgpcg.py:202-280).  tol_mode 0 stops when r.r < tol (the reference's absolute rule);
+ * tol_mode 1 stops when sqrt(r.r / r0.r0) < tol (relative). */
+typedef struct pfm_solve_opts {
+  int max_iters;   /* 400 in Poisson() (3D/mgpcg.py:422); -1 = unlimited */
+  double eps;      /* 1e-12, added to the denominators of alpha and beta */
+  double tol;      /* 1e-12 in Poisson() */
+  int tol_mode;    /* 0 absolute r.r, 1 relative norm */
+  int check_every; /* host convergence check cadence in iterations (>= 1); iterations after
+                      convergence inside a cadence block are skipped on the device */
+} pfm_solve_opts;
+
+typedef struct pfm_solve_stats {
+  int iterations;      /* the `it` the reference prints on convergence */
+  int converged;       /* 1 if the stopping rule was met */
+  double rTr;          /* final r.r */
+  double rTr0;         /* r.r after the first residual update of iteration 0 (before any stop) */
+} pfm_solve_stats;
+
+/* ---- handle, workspace, errors ------------------------------------------------------------- */
+
+/* Creates a handle for one scene.  No device memory is allocated by the library. */
+int pfm_create(const pfm_config* cfg, pfm_handle** out);
+int pfm_destroy(pfm_handle* h);
+/* Bytes of device scratch the handle needs (sort buffers, P2G payload, MGPCG hierarchy). */
+int pfm_workspace_size(const pfm_handle* h, size_t* bytes);
+/* Binds caller-allocated device scratch (>= pfm_workspace_size bytes, 256-byte aligned). */
+int pfm_set_workspace(pfm_handle* h, void* dptr, size_t bytes);
+const char* pfm_last_error(const pfm_handle* h);
+const char* pfm_status_string(int status);
+/* Number of MGPCG levels the handle uses. */
+int pfm_mg_levels(const pfm_handle* h, int* levels);
+
+/* ---- 3D step phases ------------------------------------------------------------------------ */
+
+/* calc_max_speed (3D/run_3D.py:95-103): max over cells of the centre-averaged speed, floor 1e-3.
+ * Writes the f32 result to *max_dev (device pointer).  Asynchronous. */
+int pfm3_calc_max_speed(pfm_handle* h, const float* u_x, const float* u_y, const float* u_z,
+                        float* max_dev, void* stream);
+
+/* init_particles_imp / init_particles_imp_grad_m (3D/init_conditions.py:254-273): G2P of the
+ * grid velocity (imp_out [3][P], may be NULL) and its gradient (C_out [3][3][P] = init_C_x/y/z,
+ * may be NULL) at the particle positions pos [3][P]. */
+int pfm3_g2p(pfm_handle* h, const float* pos, const float* u_x, const float* u_y, const float* u_z,
+             float* imp_out, float* C_out, void* stream);
+
+/* update_T (3D/run_3D.py:430-439): T_init <- cols(T_gm) @ cols(T_init); then, when reset_gm is
+ * nonzero, reset_T_to_identity(T_gm) (3D/run_3D.py:133-140).  Both [3][3][P]. */
+int pfm3_update_T(pfm_handle* h, float* T_init, float* T_gm, int reset_gm, void* stream);
+
+/* reset_T_to_identity (3D/run_3D.py:133-140) on a [3][3][P] field. */
+int pfm3_reset_T(pfm_handle* h, float* T, void* stream);
+
+/* RK4_T_forward (3D/run_3D.py:175-219): forward RK4 of positions pos [3][P] and of the three
+ * rows of T [3][3][P] (dT/dt = -(grad u)^T T) in the velocity field u over dt.  In place. */
+int pfm3_rk4_T_forward(pfm_handle* h, float* pos, float* T, const float* u_x, const float* u_y,
+                       const float* u_z, float dt, void* stream);
+
+/* Midpoint velocity (3D/run_3D.py:779-788 before the projection): reset_to_identity_grid,
+ * RK4_grid over -dt_half for every face family, then advect_u: u1 = T . u0(psi).
+ * u0 and u1 must not alias.  psi_out/T_out ([F][3] per family, AoS like the reference grids)
+ * may be NULL; when given they receive psi_{x,y,z}_grid / T_{x,y,z}_grid. */
+int pfm3_midpoint(pfm_handle* h, const float* u0_x, const float* u0_y, const float* u0_z,
+                  float* u1_x, float* u1_y, float* u1_z, float dt_half, float* psi_out[3],
+                  float* T_out[3], void* stream);
+
+/* get_particles_id_in_every_cell (3D/run_3D.py:342-351) as a deterministic counting sort: bins
+ * the particles by int(pos/dx) (clamped to the grid) and orders each bin by particle index.
+ * Results stay in the workspace; cell_count (may be NULL, [C] int32) and order (may be NULL,
+ * [P] int32, the stable permutation) are copied out when given. */
+int pfm3_sort_particles(pfm_handle* h, const float* pos, int* cell_count, int* order, void* stream);
+
+/* P2G (3D/run_3D.py:441-552): APIC transfer of impulse m = T_gm^T T_init^T-composed init_imp
+ * with affine term (T_gm^T init_C T_gm) to the faces, normalised by the weight sums.
+ * Deterministic: sort + per-face gather in (cell, particle-index) order, no float atomics.
+ * Writes u_x/u_y/u_z and the weight grids w_x/w_y/w_z. */
+int pfm3_p2g(pfm_handle* h, const float* init_imp, const float* pos, const float* T_gm,
+             const float* T_init, const float* init_C, float* u_x, float* u_y, float* u_z,
+             float* w_x, float* w_y, float* w_z, void* stream);
+
+/* MGPCG_3.Poisson (3D/mgpcg.py:425-430): apply_bc, divergence, MGPCG solve of the pressure,
+ * subtract_grad_p, apply_bc.  In place on u.  p_out [nx][ny][nz] (may be NULL) receives the
+ * pressure.  SYNCHRONIZATION POINT: returns after the solve finished; stats may be NULL. */
+int pfm3_poisson(pfm_handle* h, float* u_x, float* u_y, float* u_z, float* p_out,
+                 const pfm_solve_opts* opts, pfm_solve_stats* stats, void* stream);
+
+/* ---- 2D step phases ------------------------------------------------------------------------ */
+
+int pfm2_calc_max_speed(pfm_handle* h, const float* u_x, const float* u_y, float* max_dev,
+                        void* stream); /* 2D/run_2D.py:101-108 */
+/* init_particles_imp / _grad_m (2D/init_conditions.py:184-210): imp_out [2][P], C_out [2][2][P] */
+int pfm2_g2p(pfm_handle* h, const float* pos, const float* u_x, const float* u_y, float* imp_out,
+             float* C_out, void* stream);
+/* RK4_T_forward (2D/run_2D.py:304-341), advect_psi as in the reference */
+int pfm2_rk4_T_forward(pfm_handle* h, float* pos, float* T, const float* u_x, const float* u_y,
+                       float dt, int advect_psi, void* stream);
+/* update_particles_grad_m (2D/run_2D.py:526-536): C = T^T-sandwich of init_C */
+int pfm2_update_grad_m(pfm_handle* h, float* C, const float* init_C, const float* T_gm, void* stream);
+/* update_T (2D/run_2D.py:538-546): T = cols(T_gm) @ cols(T_init) */
+int pfm2_update_T(pfm_handle* h, float* T, const float* T_init, const float* T_gm, void* stream);
+/* update_particles_imp (2D/run_2D.py:517-524): imp = cols(T) @ init_imp */
+int pfm2_update_imp(pfm_handle* h, float* imp, const float* init_imp, const float* T, void* stream);
+/* reset_T_to_identity (2D/run_2D.py:141-146) */
+int pfm2_reset_T(pfm_handle* h, float* T, void* stream);
+/* midpoint (2D/run_2D.py:866-871 before the projection) */
+int pfm2_midpoint(pfm_handle* h, const float* u0_x, const float* u0_y, float* u1_x, float* u1_y,
+                  float dt_half, float* psi_out[2], float* T_out[2], void* stream);
+int pfm2_sort_particles(pfm_handle* h, const float* pos, int* cell_count, int* order, void* stream);
+/* P2G (2D/run_2D.py:548-611): impulse with APIC C [2][2][P] and the reference map psi [2][P]
+ * (psi_x/psi_y grids [F][2] may be NULL). */
+int pfm2_p2g(pfm_handle* h, const float* imp, const float* pos, const float* C, const float* psi,
+             float* u_x, float* u_y, float* psi_x, float* psi_y, float* w_x, float* w_y, void* stream);
+/* MGPCG_2.Poisson (2D/mgpcg.py:342-347). SYNCHRONIZATION POINT. */
+int pfm2_poisson(pfm_handle* h, float* u_x, float* u_y, float* p_out, const pfm_solve_opts* opts,
+                 pfm_solve_stats* stats, void* stream);
+
+/* ---- the MGPCG solver alone ----------------------------------------------------------------- */
+
+/* MGPCG.init(r, -1) + solve() + get_result (3D/mgpcg.py:71-90, 202-280) on a caller-given
+ * divergence field div [cells] (the right-hand side is -div, as in Poisson()).  x_out [cells]
+ * receives the pressure.  SYNCHRONIZATION POINT. */
+int pfm_mgpcg_solve(pfm_handle* h, const float* div, float* x_out, const pfm_solve_opts* opts,
+                    pfm_solve_stats* stats, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PFM_H_ */

@@ -1,0 +1,171 @@
+// Handle, workspace layout and error reporting of libpfm.so.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "pfm_internal.cuh"
+
+namespace pfm {
+
+int set_error(pfm_handle* h, int status, const std::string& msg) {
+  if (h) h->err = msg;
+  return status;
+}
+
+int check_cuda(pfm_handle* h, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return PFM_OK;
+  return set_error(h, PFM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int launch_check(pfm_handle* h, const char* what) { return check_cuda(h, cudaGetLastError(), what); }
+
+int require_ws(pfm_handle* h) {
+  if (!h->ws) return set_error(h, PFM_ERR_WORKSPACE, "no workspace bound (pfm_set_workspace)");
+  if (h->ws_bytes < h->ws_need) return set_error(h, PFM_ERR_WORKSPACE, "workspace too small");
+  return PFM_OK;
+}
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace pfm
+
+using namespace pfm;
+
+extern "C" {
+
+const char* pfm_status_string(int s) {
+  switch (s) {
+    case PFM_OK: return "ok";
+    case PFM_ERR_NULL: return "null pointer";
+    case PFM_ERR_SHAPE: return "shape mismatch";
+    case PFM_ERR_WORKSPACE: return "workspace missing or too small";
+    case PFM_ERR_NOT_CONVERGED: return "MGPCG did not converge";
+    case PFM_ERR_NONFINITE: return "non-finite value";
+    case PFM_ERR_CUDA: return "CUDA error";
+    case PFM_ERR_ARG: return "invalid argument";
+    default: return "unknown status";
+  }
+}
+
+const char* pfm_last_error(const pfm_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+int pfm_create(const pfm_config* cfg, pfm_handle** out) {
+  if (!cfg || !out) return PFM_ERR_NULL;
+  *out = nullptr;
+  if (cfg->dim != 2 && cfg->dim != 3) return PFM_ERR_ARG;
+  const int D = cfg->dim;
+  for (int d = 0; d < D; ++d)
+    if (cfg->res[d] < 4 || cfg->res[d] > (1 << 14)) return PFM_ERR_SHAPE;
+  if (!(cfg->dx > 0.0)) return PFM_ERR_ARG;
+  if (cfg->particles < 0) return PFM_ERR_ARG;
+  pfm_handle* h = new (std::nothrow) pfm_handle();
+  if (!h) return PFM_ERR_ARG;
+  h->cfg = *cfg;
+  if (D == 2) h->cfg.res[2] = 1;
+  h->P = cfg->particles;
+  MacGeom& g = h->geom;
+  g.dim = D;
+  for (int a = 0; a < 3; ++a) g.N[a] = (a < D) ? h->cfg.res[a] : 1;
+  for (int c = 0; c < 3; ++c)
+    for (int a = 0; a < 3; ++a) {
+      g.n[c][a] = g.N[a] + ((a == c && c < D) ? 1 : 0);
+      // u_dim - 2 - eps formed in double, rounded to f32 (3D/taichi_utils.py:282-284)
+      g.hi[c][a] = (float)((double)g.n[c][a] - 2.0 - 1e-6);
+    }
+  g.dx = (float)cfg->dx;
+  g.inv_dx = (float)(1.0 / cfg->dx);
+  h->cells = (int64_t)g.N[0] * g.N[1] * g.N[2];
+
+  // MGPCG hierarchy (3D/mgpcg.py:28): int(log2(min N)) - base_level + 1 levels
+  int mn = g.N[0];
+  for (int d = 1; d < D; ++d) mn = mn < g.N[d] ? mn : g.N[d];
+  int L = (int)std::log2((double)mn) - cfg->base_level + 1;
+  if (cfg->mg_levels > 0) L = cfg->mg_levels;
+  if (L < 1 || L > kMaxLevels) {
+    delete h;
+    return PFM_ERR_ARG;
+  }
+  h->L = L;
+  for (int l = 0; l < L; ++l) {
+    int64_t cnt = 1;
+    for (int a = 0; a < 3; ++a) {
+      h->lv[l].n[a] = (a < D) ? (g.N[a] >> l) : 1;
+      if (h->lv[l].n[a] < 1) {
+        delete h;
+        return PFM_ERR_SHAPE;
+      }
+      cnt *= h->lv[l].n[a];
+    }
+    h->lv[l].count = cnt;
+  }
+  if (h->cfg.pre_post_smoothing <= 0) h->cfg.pre_post_smoothing = 2;
+  if (h->cfg.bottom_smoothing <= 0) h->cfg.bottom_smoothing = 50;
+
+  // workspace layout
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off = align256(off + bytes);
+    return o;
+  };
+  const size_t P = (size_t)h->P, C = (size_t)h->cells;
+  h->o_key = take(P * 4);
+  h->o_slot = take(P * 4);
+  h->o_order = take(P * 4);
+  h->o_count = take(C * 4);
+  h->o_start = take((C + 1) * 4);
+  size_t per_block = (size_t)kScanItems * kScanThreads;
+  h->o_blocksums = take(((C + per_block - 1) / per_block + 1) * 4);
+  h->o_payload = take(P * 16 * (D == 3 ? 4 : 3));
+  for (int l = 0; l < L; ++l) {
+    h->o_r[l] = take((size_t)h->lv[l].count * 4);
+    h->o_z[l] = take((size_t)h->lv[l].count * 4);
+  }
+  h->o_x = take(C * 4);
+  h->o_p = take(C * 4);
+  h->o_Ap = take(C * 4);
+  h->o_partials = take(kReduceBlocks * sizeof(double));
+  h->o_state = take(sizeof(SolveState));
+  h->o_maxpart = take(kReduceBlocks * sizeof(float) + 256);
+  h->ws_need = off;
+  if (cudaHostAlloc((void**)&h->h_state, sizeof(SolveState), cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    delete h;
+    return PFM_ERR_CUDA;
+  }
+  std::memset(h->h_state, 0, sizeof(SolveState));
+  *out = h;
+  return PFM_OK;
+}
+
+int pfm_destroy(pfm_handle* h) {
+  if (!h) return PFM_ERR_NULL;
+  if (h->h_state) cudaFreeHost(h->h_state);
+  delete h;
+  return PFM_OK;
+}
+
+int pfm_workspace_size(const pfm_handle* h, size_t* bytes) {
+  if (!h || !bytes) return PFM_ERR_NULL;
+  *bytes = h->ws_need;
+  return PFM_OK;
+}
+
+int pfm_set_workspace(pfm_handle* h, void* dptr, size_t bytes) {
+  if (!h) return PFM_ERR_NULL;
+  if (!dptr) return set_error(h, PFM_ERR_NULL, "workspace pointer is NULL");
+  if (((uintptr_t)dptr) & 255) return set_error(h, PFM_ERR_ARG, "workspace must be 256-byte aligned");
+  if (bytes < h->ws_need) return set_error(h, PFM_ERR_WORKSPACE, "workspace smaller than pfm_workspace_size");
+  h->ws = (char*)dptr;
+  h->ws_bytes = bytes;
+  return PFM_OK;
+}
+
+int pfm_mg_levels(const pfm_handle* h, int* levels) {
+  if (!h || !levels) return PFM_ERR_NULL;
+  *levels = h->L;
+  return PFM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,279 @@
+// Grid kernels of the step: CFL max speed and the midpoint velocity (backward RK4 of the face
+// positions and Jacobians, then the advection u1 = T . u0(psi)).
+#include "pfm_internal.cuh"
+
+namespace pfm {
+
+constexpr int kGThreads = 128;
+
+// calc_max_speed (3D/run_3D.py:95-103; 2D/run_2D.py:101-108).  Max is order independent, so the
+// per-block maxima are combined by the last block without atomics on floats.
+template <int D>
+__global__ void __launch_bounds__(256) k_max_speed(const float* __restrict__ ux, const float* __restrict__ uy,
+                                                   const float* __restrict__ uz, MacGeom g,
+                                                   float* __restrict__ partial, unsigned* ticket,
+                                                   float* __restrict__ out) {
+  const int64_t C = (int64_t)g.N[0] * g.N[1] * g.N[2];
+  float m = 1.e-3f;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < C; e += (int64_t)gridDim.x * blockDim.x) {
+    int k = (int)(e % g.N[2]);
+    int64_t t = e / g.N[2];
+    int j = (int)(t % g.N[1]);
+    int i = (int)(t / g.N[1]);
+    float u, v, sp;
+    if (D == 3) {
+      float w;
+      u = 0.5f * (ux[((int64_t)i * g.N[1] + j) * g.N[2] + k] + ux[((int64_t)(i + 1) * g.N[1] + j) * g.N[2] + k]);
+      v = 0.5f * (uy[((int64_t)i * (g.N[1] + 1) + j) * g.N[2] + k] +
+                  uy[((int64_t)i * (g.N[1] + 1) + j + 1) * g.N[2] + k]);
+      w = 0.5f * (uz[((int64_t)i * g.N[1] + j) * (g.N[2] + 1) + k] +
+                  uz[((int64_t)i * g.N[1] + j) * (g.N[2] + 1) + k + 1]);
+      sp = sqrtf(u * u + v * v + w * w);
+    } else {
+      u = 0.5f * (ux[(int64_t)i * g.N[1] + j] + ux[(int64_t)(i + 1) * g.N[1] + j]);
+      v = 0.5f * (uy[(int64_t)i * (g.N[1] + 1) + j] + uy[(int64_t)i * (g.N[1] + 1) + j + 1]);
+      sp = sqrtf(u * u + v * v);
+    }
+    m = fmaxf(m, sp);
+  }
+  __shared__ float sm[256];
+  sm[threadIdx.x] = m;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sm[threadIdx.x] = fmaxf(sm[threadIdx.x], sm[threadIdx.x + s]);
+    __syncthreads();
+  }
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    partial[blockIdx.x] = sm[0];
+    __threadfence();
+    unsigned t = atomicAdd(ticket, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  float mm = 1.e-3f;
+  for (int b = threadIdx.x; b < gridDim.x; b += blockDim.x) mm = fmaxf(mm, ((volatile float*)partial)[b]);
+  sm[threadIdx.x] = mm;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sm[threadIdx.x] = fmaxf(sm[threadIdx.x], sm[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    *out = sm[0];
+    *ticket = 0u;
+  }
+}
+
+// Midpoint for face family `fam` (3D/run_3D.py:106-120, 144-173, 296-312): psi starts at the face
+// centre X_fam (taichi_utils.py:33-46), T at the unit vector e_fam; RK4 over -dt_half with the
+// rows-form gradient (dT/dt = grad u . T); then u1 = T . u0(psi).
+template <int fam>
+__global__ void __launch_bounds__(kGThreads) k_midpoint3(MacFields3 F, MacGeom g, float dt_half,
+                                                        float* __restrict__ u1, float* __restrict__ psi_out,
+                                                        float* __restrict__ T_out) {
+  const int n0 = g.n[fam][0], n1 = g.n[fam][1], n2 = g.n[fam][2];
+  const int64_t nf = (int64_t)n0 * n1 * n2;
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nf) return;
+  int k = (int)(e % n2);
+  int64_t t = e / n2;
+  int j = (int)(t % n1);
+  int i = (int)(t / n1);
+  float X[3] = {(float)i, (float)j, (float)k};
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+    if (d != fam) X[d] = X[d] + 0.5f;
+  float p0[3] = {X[0] * g.dx, X[1] * g.dx, X[2] * g.dx};
+  float T0[3] = {fam == 0 ? 1.f : 0.f, fam == 1 ? 1.f : 0.f, fam == 2 ? 1.f : 0.f};
+  const float neg_dt = -1.f * dt_half;
+  const float half = 0.5f * neg_dt;
+  float pk[3] = {p0[0], p0[1], p0[2]}, Tk[3] = {T0[0], T0[1], T0[2]};
+  float su[3], sT[3];
+#pragma unroll 1
+  for (int s = 0; s < 4; ++s) {
+    float u[3], G[3][3];
+    interp_mac3(F, g, pk, u, G, true);
+    float dT[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) dT[c] = G[c][0] * Tk[0] + G[c][1] * Tk[1] + G[c][2] * Tk[2];
+    const float wgt = (s == 0 || s == 3) ? 1.f : 2.f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      su[c] = (s == 0) ? u[c] : su[c] + wgt * u[c];
+      sT[c] = (s == 0) ? dT[c] : sT[c] + wgt * dT[c];
+    }
+    if (s < 3) {
+      const float cdt = (s < 2) ? half : neg_dt;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        pk[c] = p0[c] + cdt * u[c];
+        Tk[c] = T0[c] + cdt * dT[c];
+      }
+    }
+  }
+  const float coef = neg_dt / 6.f;
+  float pf[3], Tf[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    pf[c] = p0[c] + coef * su[c];
+    Tf[c] = T0[c] + coef * sT[c];
+  }
+  if (psi_out) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) psi_out[e * 3 + c] = pf[c];
+  }
+  if (T_out) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) T_out[e * 3 + c] = Tf[c];
+  }
+  float ua[3], G[3][3];
+  interp_mac3(F, g, pf, ua, G, false);
+  u1[e] = Tf[0] * ua[0] + Tf[1] * ua[1] + Tf[2] * ua[2];
+}
+
+// 2D midpoint (2D/run_2D.py:120-129, 233-261, 429-441)
+template <int fam>
+__global__ void __launch_bounds__(kGThreads) k_midpoint2(MacFields2 F, MacGeom g, float dt_half,
+                                                        float* __restrict__ u1, float* __restrict__ psi_out,
+                                                        float* __restrict__ T_out) {
+  const int n0 = g.n[fam][0], n1 = g.n[fam][1];
+  const int64_t nf = (int64_t)n0 * n1;
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nf) return;
+  int j = (int)(e % n1);
+  int i = (int)(e / n1);
+  float X[2] = {(float)i, (float)j};
+  X[1 - fam] = X[1 - fam] + 0.5f;
+  float p0[2] = {X[0] * g.dx, X[1] * g.dx};
+  float T0[2] = {fam == 0 ? 1.f : 0.f, fam == 1 ? 1.f : 0.f};
+  const float neg_dt = -1.f * dt_half;
+  const float half = 0.5f * neg_dt;
+  float pk[2] = {p0[0], p0[1]}, Tk[2] = {T0[0], T0[1]};
+  float su[2], sT[2];
+#pragma unroll 1
+  for (int s = 0; s < 4; ++s) {
+    float u[2], G[2][2];
+    interp_mac2(F, g, pk, u, G);
+    float dT[2];
+#pragma unroll
+    for (int c = 0; c < 2; ++c) dT[c] = G[c][0] * Tk[0] + G[c][1] * Tk[1];
+    const float wgt = (s == 0 || s == 3) ? 1.f : 2.f;
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      su[c] = (s == 0) ? u[c] : su[c] + wgt * u[c];
+      sT[c] = (s == 0) ? dT[c] : sT[c] + wgt * dT[c];
+    }
+    if (s < 3) {
+      const float cdt = (s < 2) ? half : neg_dt;
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        pk[c] = p0[c] + cdt * u[c];
+        Tk[c] = T0[c] + cdt * dT[c];
+      }
+    }
+  }
+  const float coef = neg_dt / 6.f;
+  float pf[2] = {p0[0] + coef * su[0], p0[1] + coef * su[1]};
+  float Tf[2] = {T0[0] + coef * sT[0], T0[1] + coef * sT[1]};
+  if (psi_out) {
+    psi_out[e * 2] = pf[0];
+    psi_out[e * 2 + 1] = pf[1];
+  }
+  if (T_out) {
+    T_out[e * 2] = Tf[0];
+    T_out[e * 2 + 1] = Tf[1];
+  }
+  float ua[2], G[2][2];
+  interp_mac2(F, g, pf, ua, G);
+  u1[e] = Tf[0] * ua[0] + Tf[1] * ua[1];
+}
+
+int max_speed_async(pfm_handle* h, const float* ux, const float* uy, const float* uz, float* out,
+                    cudaStream_t st) {
+  int s = require_ws(h);
+  if (s) return s;
+  float* part = ws_ptr<float>(h, h->o_maxpart);
+  unsigned* ticket = reinterpret_cast<unsigned*>(part + kReduceBlocks);
+  unsigned blocks = grid_for(h->cells, 256);
+  if (blocks > (unsigned)kReduceBlocks) blocks = kReduceBlocks;
+  s = check_cuda(h, cudaMemsetAsync(ticket, 0, sizeof(unsigned), st), "memset ticket");
+  if (s) return s;
+  if (h->cfg.dim == 3)
+    k_max_speed<3><<<blocks, 256, 0, st>>>(ux, uy, uz, h->geom, part, ticket, out);
+  else
+    k_max_speed<2><<<blocks, 256, 0, st>>>(ux, uy, uz, h->geom, part, ticket, out);
+  return launch_check(h, "k_max_speed");
+}
+
+}  // namespace pfm
+
+using namespace pfm;
+
+extern "C" {
+
+int pfm3_calc_max_speed(pfm_handle* h, const float* u_x, const float* u_y, const float* u_z, float* max_dev,
+                        void* stream) {
+  if (!h) return PFM_ERR_NULL;
+  if (h->cfg.dim != 3) return set_error(h, PFM_ERR_SHAPE, "pfm3_calc_max_speed on a 2D handle");
+  if (!u_x || !u_y || !u_z || !max_dev) return set_error(h, PFM_ERR_NULL, "pfm3_calc_max_speed: null input");
+  return max_speed_async(h, u_x, u_y, u_z, max_dev, (cudaStream_t)stream);
+}
+
+int pfm2_calc_max_speed(pfm_handle* h, const float* u_x, const float* u_y, float* max_dev, void* stream) {
+  if (!h) return PFM_ERR_NULL;
+  if (h->cfg.dim != 2) return set_error(h, PFM_ERR_SHAPE, "pfm2_calc_max_speed on a 3D handle");
+  if (!u_x || !u_y || !max_dev) return set_error(h, PFM_ERR_NULL, "pfm2_calc_max_speed: null input");
+  return max_speed_async(h, u_x, u_y, nullptr, max_dev, (cudaStream_t)stream);
+}
+
+int pfm3_midpoint(pfm_handle* h, const float* u0_x, const float* u0_y, const float* u0_z, float* u1_x,
+                  float* u1_y, float* u1_z, float dt_half, float* psi_out[3], float* T_out[3], void* stream) {
+  if (!h) return PFM_ERR_NULL;
+  if (h->cfg.dim != 3) return set_error(h, PFM_ERR_SHAPE, "pfm3_midpoint on a 2D handle");
+  if (!u0_x || !u0_y || !u0_z || !u1_x || !u1_y || !u1_z)
+    return set_error(h, PFM_ERR_NULL, "pfm3_midpoint: null input");
+  if (u0_x == u1_x || u0_y == u1_y || u0_z == u1_z)
+    return set_error(h, PFM_ERR_ARG, "pfm3_midpoint: u0 and u1 must not alias");
+  MacFields3 F{{u0_x, u0_y, u0_z}};
+  float* outs[3] = {u1_x, u1_y, u1_z};
+  for (int fam = 0; fam < 3; ++fam) {
+    int64_t nf = (int64_t)h->geom.n[fam][0] * h->geom.n[fam][1] * h->geom.n[fam][2];
+    float* po = psi_out ? psi_out[fam] : nullptr;
+    float* to = T_out ? T_out[fam] : nullptr;
+    dim3 gr(grid_for(nf, kGThreads));
+    cudaStream_t st = (cudaStream_t)stream;
+    if (fam == 0) k_midpoint3<0><<<gr, kGThreads, 0, st>>>(F, h->geom, dt_half, outs[fam], po, to);
+    if (fam == 1) k_midpoint3<1><<<gr, kGThreads, 0, st>>>(F, h->geom, dt_half, outs[fam], po, to);
+    if (fam == 2) k_midpoint3<2><<<gr, kGThreads, 0, st>>>(F, h->geom, dt_half, outs[fam], po, to);
+    int s = launch_check(h, "k_midpoint3");
+    if (s) return s;
+  }
+  return PFM_OK;
+}
+
+int pfm2_midpoint(pfm_handle* h, const float* u0_x, const float* u0_y, float* u1_x, float* u1_y, float dt_half,
+                  float* psi_out[2], float* T_out[2], void* stream) {
+  if (!h) return PFM_ERR_NULL;
+  if (h->cfg.dim != 2) return set_error(h, PFM_ERR_SHAPE, "pfm2_midpoint on a 3D handle");
+  if (!u0_x || !u0_y || !u1_x || !u1_y) return set_error(h, PFM_ERR_NULL, "pfm2_midpoint: null input");
+  if (u0_x == u1_x || u0_y == u1_y) return set_error(h, PFM_ERR_ARG, "pfm2_midpoint: u0 and u1 must not alias");
+  MacFields2 F{{u0_x, u0_y}};
+  float* outs[2] = {u1_x, u1_y};
+  for (int fam = 0; fam < 2; ++fam) {
+    int64_t nf = (int64_t)h->geom.n[fam][0] * h->geom.n[fam][1];
+    float* po = psi_out ? psi_out[fam] : nullptr;
+    float* to = T_out ? T_out[fam] : nullptr;
+    dim3 gr(grid_for(nf, kGThreads));
+    cudaStream_t st = (cudaStream_t)stream;
+    if (fam == 0) k_midpoint2<0><<<gr, kGThreads, 0, st>>>(F, h->geom, dt_half, outs[fam], po, to);
+    if (fam == 1) k_midpoint2<1><<<gr, kGThreads, 0, st>>>(F, h->geom, dt_half, outs[fam], po, to);
+    int s = launch_check(h, "k_midpoint2");
+    if (s) return s;
+  }
+  return PFM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,272 @@
+// Internal definitions shared by the libpfm.so translation units: the handle, the workspace
+// layout, grid geometry and the quadratic-B-spline interpolation device code.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/pfm.h"
+
+namespace pfm {
+
+constexpr int kMaxLevels = 16;
+constexpr int kReduceBlocks = 1024;  // fixed partition of every deterministic reduction
+constexpr int kReduceThreads = 256;
+constexpr int kScanItems = 8;        // items per thread in the cell-count scan
+constexpr int kScanThreads = 1024;
+
+// Device-resident state of one MGPCG solve (3D/mgpcg.py:202-280).  Scalars that the reference
+// keeps as Python floats (zTr, pAp, rTr) are doubles; alpha/beta are stored to f32 fields in the
+// reference (self.alpha[None] = ...), so they are f32 here too.
+struct SolveState {
+  double zTr_old;
+  double pAp;
+  double rTr;
+  double rTr0;
+  double sum;      // scratch result of the last reduction
+  float alpha;
+  float beta;
+  float mean;      // recenter mean
+  int it;          // completed iterations
+  int done;        // 1 converged, 2 iteration limit, 3 non-finite
+  int conv_it;     // iteration index at convergence
+  unsigned ticket; // last-block counter of the reductions
+  unsigned pad;
+};
+
+struct LevelDims {
+  int n[3];
+  int64_t count;
+};
+
+// Face-grid geometry (3D/run_3D.py:73-75) and the f32 clamp constants of interp_grad_2
+// (3D/taichi_utils.py:282-284): hi[c][a] = f32(dim_a(field c) - 2 - 1e-6), formed in double.
+struct MacGeom {
+  int dim;
+  int N[3];        // res
+  int n[3][3];     // n[c][a]: extent of face field c along axis a
+  float hi[3][3];  // interpolation clamp constants
+  float dx;        // f32(dx)
+  float inv_dx;    // f32(1/dx)
+};
+
+}  // namespace pfm
+
+struct pfm_handle {
+  pfm_config cfg;
+  pfm::MacGeom geom;
+  int64_t P;
+  int64_t cells;
+  int L;
+  pfm::LevelDims lv[pfm::kMaxLevels];
+  // workspace
+  char* ws;
+  size_t ws_bytes;
+  size_t ws_need;
+  // workspace offsets
+  size_t o_key, o_slot, o_order, o_count, o_start, o_blocksums, o_payload;
+  size_t o_r[pfm::kMaxLevels], o_z[pfm::kMaxLevels];
+  size_t o_x, o_p, o_Ap, o_partials, o_state, o_maxpart;
+  // pinned host mirror of the solve state
+  pfm::SolveState* h_state;
+  std::string err;
+};
+
+namespace pfm {
+
+int set_error(pfm_handle* h, int status, const std::string& msg);
+int check_cuda(pfm_handle* h, cudaError_t e, const char* what);
+int require_ws(pfm_handle* h);
+
+template <class T>
+inline T* ws_ptr(pfm_handle* h, size_t off) {
+  return reinterpret_cast<T*>(h->ws + off);
+}
+
+inline unsigned grid_for(int64_t n, int threads) {
+  int64_t b = (n + threads - 1) / threads;
+  return (unsigned)(b < 1 ? 1 : b);
+}
+
+// ------------------------------------------------------------------------------------------
+// Quadratic B-spline (3D/taichi_utils.py:252-272).  Branch structure as in the reference.
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ float N2(float x) {
+  float ax = fabsf(x);
+  float r = 0.f;
+  if (ax < 0.5f)
+    r = 0.75f - ax * ax;
+  else if (ax < 1.5f)
+    r = 0.5f * ((1.5f - ax) * (1.5f - ax));
+  return r;
+}
+
+__device__ __forceinline__ float dN2(float x) {
+  float ax = fabsf(x);
+  float r = 0.f;
+  if (ax < 0.5f)
+    r = -2.f * ax;
+  else if (ax < 1.5f)
+    r = 0.5f * (2.f * ax - 3.f);
+  if (x < 0.f) r = -r;
+  return r;
+}
+
+// One axis of the interp_grad_2 stencil (3D/taichi_utils.py:278-305).  The reference visits
+// the four taps iu-1..iu+2 of the clamped sample position s; exactly one of the outer two has
+// |x| >= 1.5, where N_2 and dN_2 are exactly zero, so only the three taps starting at `first`
+// are kept.  Indices are clamped like sample() (3D/taichi_utils.py:48-54).
+struct Axis3 {
+  int idx[3];
+  float w[3];
+  float dw[3];
+};
+
+__device__ __forceinline__ void axis_taps(float u, float hi, int n, Axis3& a) {
+  float s = fmaxf(1.f, fminf(u, hi));
+  float iu = floorf(s);
+  float frac = s - iu;
+  int first = frac < 0.5f ? -1 : 0;
+  int ib = __float2int_rz(iu);
+#pragma unroll
+  for (int t = 0; t < 3; ++t) {
+    float x = s - (iu + (float)(first + t));
+    a.w[t] = N2(x);
+    a.dw[t] = dN2(x);
+    int id = ib + first + t;
+    id = id < 0 ? 0 : (id > n - 1 ? n - 1 : id);
+    a.idx[t] = id;
+  }
+}
+
+// Value and gradient of one MAC component at a position, from precomputed axis taps.
+__device__ __forceinline__ void interp3_component(const float* __restrict__ f, int n1, int n2,
+                                                  const Axis3& X, const Axis3& Y, const Axis3& Z,
+                                                  float inv_dx, float& val, float& gx, float& gy,
+                                                  float& gz) {
+  float v_ = 0.f, x_ = 0.f, y_ = 0.f, z_ = 0.f;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      const float* row = f + ((size_t)X.idx[a] * n1 + Y.idx[b]) * n2;
+      float v0 = __ldg(row + Z.idx[0]), v1 = __ldg(row + Z.idx[1]), v2 = __ldg(row + Z.idx[2]);
+      float tn = v0 * Z.w[0] + v1 * Z.w[1] + v2 * Z.w[2];
+      float td = v0 * Z.dw[0] + v1 * Z.dw[1] + v2 * Z.dw[2];
+      float wxy = X.w[a] * Y.w[b];
+      v_ += wxy * tn;
+      x_ += (X.dw[a] * Y.w[b]) * tn;
+      y_ += (X.w[a] * Y.dw[b]) * tn;
+      z_ += wxy * td;
+    }
+  }
+  val = v_;
+  gx = x_ * inv_dx;
+  gy = y_ * inv_dx;
+  gz = z_ * inv_dx;
+}
+
+__device__ __forceinline__ float interp3_value(const float* __restrict__ f, int n1, int n2,
+                                               const Axis3& X, const Axis3& Y, const Axis3& Z) {
+  float v_ = 0.f;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      const float* row = f + ((size_t)X.idx[a] * n1 + Y.idx[b]) * n2;
+      float tn = __ldg(row + Z.idx[0]) * Z.w[0] + __ldg(row + Z.idx[1]) * Z.w[1] +
+                 __ldg(row + Z.idx[2]) * Z.w[2];
+      v_ += (X.w[a] * Y.w[b]) * tn;
+    }
+  }
+  return v_;
+}
+
+// interp_u_MAC_grad (3D/taichi_utils.py:312-317): u at p and G[c][r] = d u_c / d x_r.
+// The two distinct tap sets per axis are shared: component c uses the BL = 0 set on axis c
+// and the BL = 0.5 set on the others.
+struct MacFields3 {
+  const float* u[3];
+};
+
+__device__ __forceinline__ void interp_mac3(const MacFields3& F, const MacGeom& g, const float p[3],
+                                            float uo[3], float G[3][3], bool want_grad) {
+  Axis3 A0[3], A1[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    float u = p[a] / g.dx;
+    axis_taps(u - 0.0f, g.hi[a][a], g.n[a][a], A0[a]);               // the component along a
+    axis_taps(u - 0.5f, g.hi[(a + 1) % 3][a], g.n[(a + 1) % 3][a], A1[a]);  // the others
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const Axis3& X = (c == 0) ? A0[0] : A1[0];
+    const Axis3& Y = (c == 1) ? A0[1] : A1[1];
+    const Axis3& Z = (c == 2) ? A0[2] : A1[2];
+    if (want_grad) {
+      interp3_component(F.u[c], g.n[c][1], g.n[c][2], X, Y, Z, g.inv_dx, uo[c], G[c][0], G[c][1], G[c][2]);
+    } else {
+      uo[c] = interp3_value(F.u[c], g.n[c][1], g.n[c][2], X, Y, Z);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// 2D (2D/taichi_utils.py:214-261)
+// ------------------------------------------------------------------------------------------
+struct MacFields2 {
+  const float* u[2];
+};
+
+__device__ __forceinline__ void interp2_component(const float* __restrict__ f, int n1, const Axis3& X,
+                                                  const Axis3& Y, float inv_dx, float& val, float& gx,
+                                                  float& gy) {
+  float v_ = 0.f, x_ = 0.f, y_ = 0.f;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float* row = f + (size_t)X.idx[a] * n1;
+    float v0 = __ldg(row + Y.idx[0]), v1 = __ldg(row + Y.idx[1]), v2 = __ldg(row + Y.idx[2]);
+    float tn = v0 * Y.w[0] + v1 * Y.w[1] + v2 * Y.w[2];
+    float td = v0 * Y.dw[0] + v1 * Y.dw[1] + v2 * Y.dw[2];
+    v_ += X.w[a] * tn;
+    x_ += X.dw[a] * tn;
+    y_ += X.w[a] * td;
+  }
+  val = v_;
+  gx = x_ * inv_dx;
+  gy = y_ * inv_dx;
+}
+
+__device__ __forceinline__ void interp_mac2(const MacFields2& F, const MacGeom& g, const float p[2],
+                                            float uo[2], float G[2][2]) {
+  Axis3 A0[2], A1[2];
+#pragma unroll
+  for (int a = 0; a < 2; ++a) {
+    float u = p[a] / g.dx;
+    axis_taps(u - 0.0f, g.hi[a][a], g.n[a][a], A0[a]);
+    axis_taps(u - 0.5f, g.hi[1 - a][a], g.n[1 - a][a], A1[a]);
+  }
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    const Axis3& X = (c == 0) ? A0[0] : A1[0];
+    const Axis3& Y = (c == 1) ? A0[1] : A1[1];
+    interp2_component(F.u[c], g.n[c][1], X, Y, g.inv_dx, uo[c], G[c][0], G[c][1]);
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// host-side launch helpers (defined in the .cu files)
+// ------------------------------------------------------------------------------------------
+int launch_check(pfm_handle* h, const char* what);
+
+// MGPCG entry used by the Poisson wrappers (pfm_mgpcg.cu): solves A x = -div where div is in
+// r_0 of the workspace (already written).  x may be a caller buffer.
+int mgpcg_solve_in_place(pfm_handle* h, float* x, const pfm_solve_opts* opts, pfm_solve_stats* stats,
+                         cudaStream_t st);
+
+// Counting sort of the particle cells (pfm_p2g.cu).
+int sort_particles(pfm_handle* h, const float* pos, cudaStream_t st);
+
+}  // namespace pfm

@@ -1,0 +1,597 @@
+// MGPCG pressure projection on the MAC grid (3D/mgpcg.py, 2D/mgpcg.py).
+//
+// Structure follows MGPCG.solve (3D/mgpcg.py:202-280) exactly, with these GB300 choices:
+//  * alpha/beta/convergence live in a device SolveState; the host reads it every
+//    `check_every` iterations instead of three times per iteration, and kernels enqueued past
+//    convergence return immediately, so the stopping iteration is the reference's;
+//  * every reduction is deterministic: a fixed block partition, per-thread f32 partials,
+//    f64 block and grid combination in block order (no float atomics);
+//  * the restriction scatter (r_{l+1}[I//2] += res/(dim-1), 3D/mgpcg.py:152-158) is a gather
+//    over the 8 (4 in 2D) children, so it needs no atomics either.
+#include <cmath>
+
+#include "pfm_internal.cuh"
+
+namespace pfm {
+
+struct Lvl {
+  int n0, n1, n2;
+  int64_t count;
+};
+
+struct BC {
+  int lo[3], hi[3];  // 2 = Neumann
+};
+
+static inline Lvl lvl_of(const pfm_handle* h, int l) {
+  return Lvl{h->lv[l].n[0], h->lv[l].n[1], h->lv[l].n[2], h->lv[l].count};
+}
+
+// neighbor_sum / num_fluid_neighbors (3D/mgpcg.py:92-115)
+template <int D>
+__device__ __forceinline__ void stencil(const float* __restrict__ f, const Lvl& L, const BC& bc, int i, int j,
+                                        int k, int64_t e, float& nb, float& mult) {
+  float ret = 0.f;
+  float num = 2.f * D;
+  const int64_t sx = (int64_t)L.n1 * L.n2, sy = L.n2;
+  if (i < L.n0 - 1) ret += f[e + sx];
+  if (i > 0) ret += f[e - sx];
+  if (D == 3) {
+    if (j < L.n1 - 1) ret += f[e + sy];
+    if (j > 0) ret += f[e - sy];
+    if (k < L.n2 - 1) ret += f[e + 1];
+    if (k > 0) ret += f[e - 1];
+  } else {
+    if (j < L.n1 - 1) ret += f[e + sy];
+    if (j > 0) ret += f[e - sy];
+  }
+  if (i <= 0 && bc.lo[0] == 2) num -= 1.f;
+  if (i >= L.n0 - 1 && bc.hi[0] == 2) num -= 1.f;
+  if (j <= 0 && bc.lo[1] == 2) num -= 1.f;
+  if (j >= L.n1 - 1 && bc.hi[1] == 2) num -= 1.f;
+  if (D == 3) {
+    if (k <= 0 && bc.lo[2] == 2) num -= 1.f;
+    if (k >= L.n2 - 1 && bc.hi[2] == 2) num -= 1.f;
+  }
+  nb = ret;
+  mult = num;
+}
+
+__device__ __forceinline__ void decode(const Lvl& L, int64_t e, int& i, int& j, int& k) {
+  k = (int)(e % L.n2);
+  int64_t t = e / L.n2;
+  j = (int)(t % L.n1);
+  i = (int)(t / L.n1);
+}
+
+// ---------------------------------------------------------------------------------------------
+// deterministic block/grid reduction
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sums `v` over the grid.  Returns true in the last block to finish, where *total holds the
+// grid sum (combined in block order).  Fixed partition => bitwise reproducible.
+__device__ bool grid_sum(double v, double* partials, unsigned* ticket, double* total) {
+  __shared__ double ws[32];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  v = warp_sum(v);
+  if (lane == 0) ws[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    double b = lane < (int)(blockDim.x >> 5) ? ws[lane] : 0.0;
+    b = warp_sum(b);
+    if (lane == 0) {
+      partials[blockIdx.x] = b;
+      __threadfence();
+      unsigned t = atomicAdd(ticket, 1u);
+      last = (t == gridDim.x - 1);
+    }
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  double s = 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s += ((volatile double*)partials)[b];
+  s = warp_sum(s);
+  if (lane == 0) ws[wid] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += ws[w];
+    *total = t;
+    *ticket = 0u;
+  }
+  __syncthreads();
+  return true;
+}
+
+struct RedBuf {
+  double* partials;
+  SolveState* st;
+};
+
+// ---------------------------------------------------------------------------------------------
+// Poisson pieces: apply_bc, divergence, subtract_grad_p (3D/mgpcg.py:359-418; 2D 293-335)
+// ---------------------------------------------------------------------------------------------
+template <int D>
+__global__ void k_apply_bc(float* __restrict__ u, int fam, MacGeom g, int lo_neu, int hi_neu) {
+  // faces with index 0 or n along `fam`
+  const int n0 = g.n[fam][0], n1 = g.n[fam][1], n2 = g.n[fam][2];
+  int a1 = (fam == 0) ? 1 : 0, a2 = (fam == 2) ? 1 : 2;
+  if (D == 2) a2 = 2;
+  const int m1 = g.n[fam][a1], m2 = (D == 3) ? g.n[fam][a2] : 1;
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t plane = (int64_t)m1 * m2;
+  if (e >= 2 * plane) return;
+  int side = (int)(e / plane);
+  int64_t r = e % plane;
+  int c1 = (int)(r / m2), c2 = (int)(r % m2);
+  int idx[3] = {0, 0, 0};
+  idx[fam] = side ? g.n[fam][fam] - 1 : 0;
+  idx[a1] = c1;
+  if (D == 3) idx[a2] = c2;
+  if ((side == 0 && lo_neu) || (side == 1 && hi_neu)) u[((int64_t)idx[0] * n1 + idx[1]) * n2 + idx[2]] = 0.f;
+  (void)n0;
+}
+
+// divergence then init(u_div, -1): r0 = -(vr - vl + vt - vb + vc - va)
+template <int D>
+__global__ void k_divergence(const float* __restrict__ ux, const float* __restrict__ uy,
+                             const float* __restrict__ uz, MacGeom g, float* __restrict__ r0) {
+  const Lvl L{g.N[0], g.N[1], g.N[2], (int64_t)g.N[0] * g.N[1] * g.N[2]};
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= L.count) return;
+  int i, j, k;
+  decode(L, e, i, j, k);
+  float div;
+  if (D == 3) {
+    float vl = ux[((int64_t)i * L.n1 + j) * L.n2 + k], vr = ux[((int64_t)(i + 1) * L.n1 + j) * L.n2 + k];
+    float vb = uy[((int64_t)i * (L.n1 + 1) + j) * L.n2 + k], vt = uy[((int64_t)i * (L.n1 + 1) + j + 1) * L.n2 + k];
+    float va = uz[((int64_t)i * L.n1 + j) * (L.n2 + 1) + k], vc = uz[((int64_t)i * L.n1 + j) * (L.n2 + 1) + k + 1];
+    div = vr - vl + vt - vb + vc - va;
+  } else {
+    float vl = ux[(int64_t)i * L.n1 + j], vr = ux[(int64_t)(i + 1) * L.n1 + j];
+    float vb = uy[(int64_t)i * (L.n1 + 1) + j], vt = uy[(int64_t)i * (L.n1 + 1) + j + 1];
+    div = vr - vl + vt - vb;
+  }
+  r0[e] = div * -1.f;
+}
+
+// subtract_grad_p for family `fam`, followed by apply_bc on that family's boundary faces.
+template <int D>
+__global__ void k_subtract_grad_p(float* __restrict__ u, int fam, const float* __restrict__ p, MacGeom g,
+                                  int lo_neu, int hi_neu) {
+  const int n0 = g.n[fam][0], n1 = g.n[fam][1], n2 = g.n[fam][2];
+  const int64_t nf = (int64_t)n0 * n1 * n2;
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nf) return;
+  int idx[3];
+  idx[2] = (int)(e % n2);
+  int64_t t = e / n2;
+  idx[1] = (int)(t % n1);
+  idx[0] = (int)(t / n1);
+  const int N[3] = {g.N[0], g.N[1], g.N[2]};
+  // sample(p, I) and sample(p, I - e_fam): clamped indices, then the explicit zeros
+  int hiI[3] = {idx[0], idx[1], idx[2]}, loI[3] = {idx[0], idx[1], idx[2]};
+  loI[fam] -= 1;
+  int a = idx[fam];
+  auto clampi = [](int v, int n) { return v < 0 ? 0 : (v > n - 1 ? n - 1 : v); };
+  hiI[fam] = clampi(hiI[fam], N[fam]);
+  loI[fam] = clampi(loI[fam], N[fam]);
+  float pr = p[((int64_t)hiI[0] * N[1] + hiI[1]) * N[2] + hiI[2]];
+  float pl = p[((int64_t)loI[0] * N[1] + loI[1]) * N[2] + loI[2]];
+  if (a - 1 < 0) pl = 0.f;
+  if (a >= N[fam]) pr = 0.f;
+  float v = u[e] - (pr - pl);
+  if ((a == 0 && lo_neu) || (a == N[fam] && hi_neu)) v = 0.f;
+  u[e] = v;
+}
+
+// ---------------------------------------------------------------------------------------------
+// multigrid V-cycle kernels (3D/mgpcg.py:152-200)
+// ---------------------------------------------------------------------------------------------
+
+// smooth(l, phase): z = (r + nbsum(z)) / mult on cells with (i+j+k)&1 == phase.  One thread per
+// pair of cells along the last axis; the thread updates the member of the right colour.
+template <int D>
+__global__ void __launch_bounds__(256) k_smooth(float* __restrict__ z, const float* __restrict__ r, Lvl L,
+                                                BC bc, int phase, const SolveState* st) {
+  if (st && st->done) return;
+  const int nl = (D == 3) ? L.n2 : L.n1;
+  const int half = (nl + 1) >> 1;
+  const int64_t npairs = (D == 3) ? (int64_t)L.n0 * L.n1 * half : (int64_t)L.n0 * half;
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= npairs) return;
+  int i, j, k;
+  if (D == 3) {
+    int m = (int)(e % half);
+    int64_t t = e / half;
+    j = (int)(t % L.n1);
+    i = (int)(t / L.n1);
+    k = 2 * m + ((i + j + phase) & 1);
+    if (k >= L.n2) return;
+  } else {
+    int m = (int)(e % half);
+    i = (int)(e / half);
+    j = 2 * m + ((i + phase) & 1);
+    k = 0;
+    if (j >= L.n1) return;
+  }
+  const int64_t c = ((int64_t)i * L.n1 + j) * L.n2 + k;
+  float nb, mult;
+  stencil<D>(z, L, bc, i, j, k, c, nb, mult);
+  z[c] = (r[c] + nb) / mult;
+}
+
+// restrict(l) as a gather: rc[I] = sum over children (fine-index order) of res/(dim-1),
+// res = r - (mult z - nbsum(z)).
+template <int D>
+__global__ void __launch_bounds__(256) k_restrict(const float* __restrict__ zf, const float* __restrict__ rf,
+                                                  Lvl Lf, float* __restrict__ rc, Lvl Lc, BC bc,
+                                                  const SolveState* st) {
+  if (st && st->done) return;
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= Lc.count) return;
+  int I, J, K;
+  decode(Lc, e, I, J, K);
+  float acc = 0.f;
+  const float den = (float)D - 1.0f;
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int b = 0; b < 2; ++b)
+#pragma unroll
+      for (int cc = 0; cc < (D == 3 ? 2 : 1); ++cc) {
+        int i = 2 * I + a, j = 2 * J + b, k = (D == 3) ? 2 * K + cc : 0;
+        if (i >= Lf.n0 || j >= Lf.n1 || k >= Lf.n2) continue;
+        const int64_t c = ((int64_t)i * Lf.n1 + j) * Lf.n2 + k;
+        float nb, mult;
+        stencil<D>(zf, Lf, bc, i, j, k, c, nb, mult);
+        float res = rf[c] - (mult * zf[c] - nb);
+        acc += res * 1.0f / den;
+      }
+  rc[e] = acc;
+}
+
+// prolongate(l): z_l[I] += z_{l+1}[I//2]
+template <int D>
+__global__ void __launch_bounds__(256) k_prolong(float* __restrict__ zf, Lvl Lf, const float* __restrict__ zc,
+                                                 Lvl Lc, const SolveState* st) {
+  if (st && st->done) return;
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= Lf.count) return;
+  int i, j, k;
+  decode(Lf, e, i, j, k);
+  int64_t ce = (D == 3) ? ((int64_t)(i >> 1) * Lc.n1 + (j >> 1)) * Lc.n2 + (k >> 1)
+                        : (int64_t)(i >> 1) * Lc.n1 + (j >> 1);
+  zf[e] += zc[ce];
+}
+
+__global__ void __launch_bounds__(256) k_negate(float* __restrict__ out, const float* __restrict__ in, int64_t n) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    out[e] = in[e] * -1.f;
+}
+
+__global__ void __launch_bounds__(256) k_zero(float* __restrict__ a, int64_t n, const SolveState* st) {
+  if (st && st->done) return;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    a[e] = 0.f;
+}
+
+// ---------------------------------------------------------------------------------------------
+// PCG kernels with fused reductions and device-side scalar updates
+// ---------------------------------------------------------------------------------------------
+enum RedKind { RED_ZTR_INIT = 0, RED_ZTR = 1, RED_RTR0 = 2, RED_MEAN = 3 };
+
+// sum(a*b) (or sum(a) for RED_MEAN) with a finalizer that updates the solve state.
+__global__ void __launch_bounds__(kReduceThreads) k_dot(const float* __restrict__ a, const float* __restrict__ b,
+                                                        int64_t n, RedBuf rb, int kind, double eps, double inv_n) {
+  SolveState* st = rb.st;
+  if (st->done) return;
+  float acc = 0.f;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    acc += (kind == RED_MEAN) ? a[e] : a[e] * b[e];
+  double total;
+  if (!grid_sum((double)acc, rb.partials, &st->ticket, &total)) return;
+  if (threadIdx.x != 0) return;
+  if (kind == RED_ZTR_INIT) {
+    st->zTr_old = total;
+  } else if (kind == RED_ZTR) {
+    // beta = new_zTr / (old_zTr + eps); p update follows (3D/mgpcg.py:268-275)
+    st->beta = (float)(total / (st->zTr_old + eps));
+    st->zTr_old = total;
+    st->it += 1;
+  } else if (kind == RED_RTR0) {
+    st->rTr0 = total;
+  } else {
+    st->mean = (float)(total * inv_n);
+  }
+}
+
+// recenter (3D/mgpcg.py:174-180): r -= mean
+__global__ void __launch_bounds__(256) k_sub_mean(float* __restrict__ r, int64_t n, const SolveState* st) {
+  if (st->done) return;
+  const float m = st->mean;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    r[e] -= m;
+}
+
+// compute_Ap + reduce(p, Ap) + alpha = zTr / (pAp + eps)   (3D/mgpcg.py:237-240)
+template <int D>
+__global__ void __launch_bounds__(kReduceThreads) k_Ap_dot(const float* __restrict__ p, float* __restrict__ Ap,
+                                                           Lvl L, BC bc, RedBuf rb, double eps) {
+  SolveState* st = rb.st;
+  if (st->done) return;
+  float acc = 0.f;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < L.count; e += (int64_t)gridDim.x * blockDim.x) {
+    int i, j, k;
+    decode(L, e, i, j, k);
+    float nb, mult;
+    stencil<D>(p, L, bc, i, j, k, e, nb, mult);
+    float pe = p[e];
+    float ap = mult * pe - nb;
+    Ap[e] = ap;
+    acc += pe * ap;
+  }
+  double total;
+  if (!grid_sum((double)acc, rb.partials, &st->ticket, &total)) return;
+  if (threadIdx.x == 0) {
+    st->pAp = total;
+    st->alpha = (float)(st->zTr_old / (total + eps));
+  }
+}
+
+// update_x, update_r, reduce(r, r) and the convergence test (3D/mgpcg.py:243-258).
+__global__ void __launch_bounds__(kReduceThreads) k_update_xr(float* __restrict__ x, const float* __restrict__ p,
+                                                              float* __restrict__ r, const float* __restrict__ Ap,
+                                                              int64_t n, RedBuf rb, double tol, int tol_mode) {
+  SolveState* st = rb.st;
+  if (st->done) return;
+  const float alpha = st->alpha;
+  float acc = 0.f;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    x[e] += alpha * p[e];
+    float re = r[e] - alpha * Ap[e];
+    r[e] = re;
+    acc += re * re;
+  }
+  double total;
+  if (!grid_sum((double)acc, rb.partials, &st->ticket, &total)) return;
+  if (threadIdx.x == 0) {
+    st->rTr = total;
+    bool stop = (tol_mode == 0) ? (total < tol) : (sqrt(total) < tol * sqrt(st->rTr0));
+    if (!isfinite(total)) {
+      st->done = 3;
+      st->conv_it = st->it;
+    } else if (stop) {
+      st->done = 1;
+      st->conv_it = st->it;
+    }
+  }
+}
+
+// update_p: p = z + beta p (3D/mgpcg.py:147-150)
+__global__ void __launch_bounds__(256) k_update_p(float* __restrict__ p, const float* __restrict__ z, int64_t n,
+                                                  const SolveState* st) {
+  if (st->done) return;
+  const float beta = st->beta;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    p[e] = z[e] + beta * p[e];
+}
+
+// ---------------------------------------------------------------------------------------------
+// host orchestration
+// ---------------------------------------------------------------------------------------------
+static BC bc_of(const pfm_handle* h) {
+  BC b;
+  for (int d = 0; d < 3; ++d) {
+    b.lo[d] = (d < h->cfg.dim) ? h->cfg.boundary[d][0] : 2;
+    b.hi[d] = (d < h->cfg.dim) ? h->cfg.boundary[d][1] : 2;
+  }
+  return b;
+}
+
+static unsigned red_blocks(int64_t n) {
+  unsigned b = grid_for(n, kReduceThreads);
+  return b > (unsigned)kReduceBlocks ? (unsigned)kReduceBlocks : b;
+}
+
+static unsigned stream_blocks(int64_t n) {
+  unsigned b = grid_for(n, 256);
+  return b > 152u * 16u ? 152u * 16u : b;
+}
+
+template <int D>
+static void smooth_launch(pfm_handle* h, int l, int phase, const SolveState* st, cudaStream_t s) {
+  Lvl L = lvl_of(h, l);
+  const int nl = (D == 3) ? L.n2 : L.n1;
+  int64_t npairs = (D == 3) ? (int64_t)L.n0 * L.n1 * ((nl + 1) / 2) : (int64_t)L.n0 * ((nl + 1) / 2);
+  k_smooth<D><<<grid_for(npairs, 256), 256, 0, s>>>(ws_ptr<float>(h, h->o_z[l]), ws_ptr<float>(h, h->o_r[l]), L,
+                                                   bc_of(h), phase, st);
+}
+
+// apply_preconditioner (3D/mgpcg.py:182-200)
+template <int D>
+static void vcycle(pfm_handle* h, const SolveState* st, cudaStream_t s) {
+  const int L = h->L;
+  const BC bc = bc_of(h);
+  k_zero<<<stream_blocks(h->lv[0].count), 256, 0, s>>>(ws_ptr<float>(h, h->o_z[0]), h->lv[0].count, st);
+  for (int l = 0; l < L - 1; ++l) {
+    for (int i = 0; i < h->cfg.pre_post_smoothing; ++i) {
+      smooth_launch<D>(h, l, 0, st, s);
+      smooth_launch<D>(h, l, 1, st, s);
+    }
+    k_zero<<<stream_blocks(h->lv[l + 1].count), 256, 0, s>>>(ws_ptr<float>(h, h->o_z[l + 1]), h->lv[l + 1].count, st);
+    Lvl Lf = lvl_of(h, l), Lc = lvl_of(h, l + 1);
+    k_restrict<D><<<grid_for(Lc.count, 256), 256, 0, s>>>(ws_ptr<float>(h, h->o_z[l]), ws_ptr<float>(h, h->o_r[l]),
+                                                          Lf, ws_ptr<float>(h, h->o_r[l + 1]), Lc, bc, st);
+  }
+  for (int i = 0; i < h->cfg.bottom_smoothing; ++i) {
+    smooth_launch<D>(h, L - 1, 0, st, s);
+    smooth_launch<D>(h, L - 1, 1, st, s);
+  }
+  for (int l = L - 2; l >= 0; --l) {
+    Lvl Lf = lvl_of(h, l), Lc = lvl_of(h, l + 1);
+    k_prolong<D><<<grid_for(Lf.count, 256), 256, 0, s>>>(ws_ptr<float>(h, h->o_z[l]), Lf,
+                                                         ws_ptr<float>(h, h->o_z[l + 1]), Lc, st);
+    for (int i = 0; i < h->cfg.pre_post_smoothing; ++i) {
+      smooth_launch<D>(h, l, 1, st, s);
+      smooth_launch<D>(h, l, 0, st, s);
+    }
+  }
+}
+
+static bool all_neumann(const pfm_handle* h) {
+  for (int d = 0; d < h->cfg.dim; ++d)
+    if (h->cfg.boundary[d][0] != 2 || h->cfg.boundary[d][1] != 2) return false;
+  return true;
+}
+
+template <int D>
+static int solve_impl(pfm_handle* h, float* x, const pfm_solve_opts* opts, pfm_solve_stats* stats, cudaStream_t s) {
+  pfm_solve_opts o{400, 1e-12, 1e-12, 0, 4};
+  if (opts) o = *opts;
+  if (o.check_every < 1) o.check_every = 1;
+  const int64_t n = h->cells;
+  SolveState* st = ws_ptr<SolveState>(h, h->o_state);
+  RedBuf rb{ws_ptr<double>(h, h->o_partials), st};
+  float* r0 = ws_ptr<float>(h, h->o_r[0]);
+  float* z0 = ws_ptr<float>(h, h->o_z[0]);
+  float* p = ws_ptr<float>(h, h->o_p);
+  float* Ap = ws_ptr<float>(h, h->o_Ap);
+  const Lvl L0 = lvl_of(h, 0);
+  const BC bc = bc_of(h);
+  const double inv_n = 1.0 / (double)n;
+  int rc = check_cuda(h, cudaMemsetAsync(st, 0, sizeof(SolveState), s), "memset state");
+  if (rc) return rc;
+  // init(): x = p = Ap = z0 = 0 (3D/mgpcg.py:63-79)
+  cudaMemsetAsync(x, 0, n * 4, s);
+  cudaMemsetAsync(p, 0, n * 4, s);
+  cudaMemsetAsync(Ap, 0, n * 4, s);
+  const bool neu = all_neumann(h);
+  if (neu) {
+    k_dot<<<red_blocks(n), kReduceThreads, 0, s>>>(r0, nullptr, n, rb, RED_MEAN, o.eps, inv_n);
+    k_sub_mean<<<stream_blocks(n), 256, 0, s>>>(r0, n, st);
+  }
+  k_dot<<<red_blocks(n), kReduceThreads, 0, s>>>(r0, r0, n, rb, RED_RTR0, o.eps, inv_n);
+  vcycle<D>(h, st, s);
+  k_update_p<<<stream_blocks(n), 256, 0, s>>>(p, z0, n, st);  // beta = 0 in the state
+  k_dot<<<red_blocks(n), kReduceThreads, 0, s>>>(z0, r0, n, rb, RED_ZTR_INIT, o.eps, inv_n);
+  rc = launch_check(h, "mgpcg setup");
+  if (rc) return rc;
+  int enq = 0;
+  SolveState* hs = h->h_state;
+  while (true) {
+    int chunk = o.check_every;
+    if (o.max_iters >= 0 && enq + chunk > o.max_iters) chunk = o.max_iters - enq;
+    for (int c = 0; c < chunk; ++c) {
+      k_Ap_dot<D><<<red_blocks(n), kReduceThreads, 0, s>>>(p, Ap, L0, bc, rb, o.eps);
+      k_update_xr<<<red_blocks(n), kReduceThreads, 0, s>>>(x, p, r0, Ap, n, rb, o.tol, o.tol_mode);
+      if (neu) {
+        k_dot<<<red_blocks(n), kReduceThreads, 0, s>>>(r0, nullptr, n, rb, RED_MEAN, o.eps, inv_n);
+        k_sub_mean<<<stream_blocks(n), 256, 0, s>>>(r0, n, st);
+      }
+      vcycle<D>(h, st, s);
+      k_dot<<<red_blocks(n), kReduceThreads, 0, s>>>(z0, r0, n, rb, RED_ZTR, o.eps, inv_n);
+      k_update_p<<<stream_blocks(n), 256, 0, s>>>(p, z0, n, st);
+    }
+    enq += chunk;
+    rc = launch_check(h, "mgpcg iteration");
+    if (rc) return rc;
+    rc = check_cuda(h, cudaMemcpyAsync(hs, st, sizeof(SolveState), cudaMemcpyDeviceToHost, s), "state readback");
+    if (rc) return rc;
+    rc = check_cuda(h, cudaStreamSynchronize(s), "mgpcg sync");
+    if (rc) return rc;
+    if (hs->done) break;
+    if (o.max_iters >= 0 && enq >= o.max_iters) break;
+  }
+  if (stats) {
+    stats->converged = hs->done == 1;
+    stats->iterations = hs->done ? hs->conv_it : hs->it;
+    stats->rTr = hs->rTr;
+    stats->rTr0 = hs->rTr0;
+  }
+  if (hs->done == 3) return set_error(h, PFM_ERR_NONFINITE, "MGPCG: non-finite residual");
+  if (hs->done != 1) return set_error(h, PFM_ERR_NOT_CONVERGED, "MGPCG: iteration limit reached");
+  return PFM_OK;
+}
+
+int mgpcg_solve_in_place(pfm_handle* h, float* x, const pfm_solve_opts* opts, pfm_solve_stats* stats,
+                         cudaStream_t s) {
+  return h->cfg.dim == 3 ? solve_impl<3>(h, x, opts, stats, s) : solve_impl<2>(h, x, opts, stats, s);
+}
+
+template <int D>
+static int poisson_impl(pfm_handle* h, float* const* u, float* p_out, const pfm_solve_opts* opts,
+                        pfm_solve_stats* stats, cudaStream_t s) {
+  int rc = require_ws(h);
+  if (rc) return rc;
+  const MacGeom& g = h->geom;
+  for (int f = 0; f < D; ++f) {
+    int a1 = (f == 0) ? 1 : 0, a2 = (f == 2) ? 1 : 2;
+    int64_t plane = (int64_t)g.n[f][a1] * (D == 3 ? g.n[f][a2] : 1);
+    k_apply_bc<D><<<grid_for(2 * plane, 256), 256, 0, s>>>(u[f], f, g, h->cfg.boundary[f][0] == 2,
+                                                          h->cfg.boundary[f][1] == 2);
+  }
+  float* r0 = ws_ptr<float>(h, h->o_r[0]);
+  k_divergence<D><<<grid_for(h->cells, 256), 256, 0, s>>>(u[0], u[1], D == 3 ? u[2] : nullptr, g, r0);
+  rc = launch_check(h, "divergence");
+  if (rc) return rc;
+  float* x = p_out ? p_out : ws_ptr<float>(h, h->o_x);
+  int solve_rc = solve_impl<D>(h, x, opts, stats, s);
+  if (solve_rc != PFM_OK && solve_rc != PFM_ERR_NOT_CONVERGED) return solve_rc;
+  for (int f = 0; f < D; ++f) {
+    int64_t nf = (int64_t)g.n[f][0] * g.n[f][1] * g.n[f][2];
+    k_subtract_grad_p<D><<<grid_for(nf, 256), 256, 0, s>>>(u[f], f, x, g, h->cfg.boundary[f][0] == 2,
+                                                          h->cfg.boundary[f][1] == 2);
+  }
+  rc = launch_check(h, "subtract_grad_p");
+  if (rc) return rc;
+  return solve_rc;
+}
+
+}  // namespace pfm
+
+using namespace pfm;
+
+extern "C" {
+
+int pfm3_poisson(pfm_handle* h, float* u_x, float* u_y, float* u_z, float* p_out, const pfm_solve_opts* opts,
+                 pfm_solve_stats* stats, void* stream) {
+  if (!h) return PFM_ERR_NULL;
+  if (h->cfg.dim != 3) return set_error(h, PFM_ERR_SHAPE, "pfm3_poisson on a 2D handle");
+  if (!u_x || !u_y || !u_z) return set_error(h, PFM_ERR_NULL, "pfm3_poisson: null velocity");
+  float* u[3] = {u_x, u_y, u_z};
+  return poisson_impl<3>(h, u, p_out, opts, stats, (cudaStream_t)stream);
+}
+
+int pfm2_poisson(pfm_handle* h, float* u_x, float* u_y, float* p_out, const pfm_solve_opts* opts,
+                 pfm_solve_stats* stats, void* stream) {
+  if (!h) return PFM_ERR_NULL;
+  if (h->cfg.dim != 2) return set_error(h, PFM_ERR_SHAPE, "pfm2_poisson on a 3D handle");
+  if (!u_x || !u_y) return set_error(h, PFM_ERR_NULL, "pfm2_poisson: null velocity");
+  float* u[2] = {u_x, u_y};
+  return poisson_impl<2>(h, u, p_out, opts, stats, (cudaStream_t)stream);
+}
+
+int pfm_mgpcg_solve(pfm_handle* h, const float* div, float* x_out, const pfm_solve_opts* opts,
+                    pfm_solve_stats* stats, void* stream) {
+  if (!h) return PFM_ERR_NULL;
+  if (!div || !x_out) return set_error(h, PFM_ERR_NULL, "pfm_mgpcg_solve: null input");
+  int rc = require_ws(h);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  float* r0 = ws_ptr<float>(h, h->o_r[0]);
+  // init(div, -1): r0 = -div (3D/mgpcg.py:71-79)
+  k_negate<<<stream_blocks(h->cells), 256, 0, s>>>(r0, div, h->cells);
+  rc = launch_check(h, "k_negate");
+  if (rc) return rc;
+  return mgpcg_solve_in_place(h, x_out, opts, stats, s);
+}
+
+}  // extern "C"

@@ -1,0 +1,106 @@
+"""ctypes binding of libpfm.so (declarations in include/pfm.h).
+
+The library is the only compute path: if it is missing or CUDA is unavailable, loading raises
+:class:`PfmError` -- there is no CPU fallback.
+"""
+import ctypes
+import os
+
+from . import build as _build
+
+PFM_OK = 0
+PFM_ERR_NOT_CONVERGED = 4
+STATUS_NAMES = {0: "PFM_OK", 1: "PFM_ERR_NULL", 2: "PFM_ERR_SHAPE", 3: "PFM_ERR_WORKSPACE",
+                4: "PFM_ERR_NOT_CONVERGED", 5: "PFM_ERR_NONFINITE", 6: "PFM_ERR_CUDA", 7: "PFM_ERR_ARG"}
+
+
+class PfmError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("dim", ctypes.c_int), ("res", ctypes.c_int * 3), ("dx", ctypes.c_double),
+                ("particles", ctypes.c_int64), ("base_level", ctypes.c_int), ("mg_levels", ctypes.c_int),
+                ("pre_post_smoothing", ctypes.c_int), ("bottom_smoothing", ctypes.c_int),
+                ("boundary", (ctypes.c_int * 2) * 3), ("use_apic", ctypes.c_int)]
+
+
+class SolveOpts(ctypes.Structure):
+    _fields_ = [("max_iters", ctypes.c_int), ("eps", ctypes.c_double), ("tol", ctypes.c_double),
+                ("tol_mode", ctypes.c_int), ("check_every", ctypes.c_int)]
+
+
+class SolveStats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("converged", ctypes.c_int), ("rTr", ctypes.c_double),
+                ("rTr0", ctypes.c_double)]
+
+
+# name -> argument types (all return int status unless listed in _RESTYPE)
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_F = ctypes.c_float
+SIGNATURES = {
+    "pfm_create": [ctypes.POINTER(Config), ctypes.POINTER(_P)],
+    "pfm_destroy": [_P],
+    "pfm_workspace_size": [_P, ctypes.POINTER(ctypes.c_size_t)],
+    "pfm_set_workspace": [_P, _P, ctypes.c_size_t],
+    "pfm_last_error": [_P],
+    "pfm_status_string": [_I],
+    "pfm_mg_levels": [_P, ctypes.POINTER(_I)],
+    "pfm3_calc_max_speed": [_P, _P, _P, _P, _P, _P],
+    "pfm3_g2p": [_P, _P, _P, _P, _P, _P, _P, _P],
+    "pfm3_update_T": [_P, _P, _P, _I, _P],
+    "pfm3_reset_T": [_P, _P, _P],
+    "pfm3_rk4_T_forward": [_P, _P, _P, _P, _P, _P, _F, _P],
+    "pfm3_midpoint": [_P, _P, _P, _P, _P, _P, _P, _F, _P, _P, _P],
+    "pfm3_sort_particles": [_P, _P, _P, _P, _P],
+    "pfm3_p2g": [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
+    "pfm3_poisson": [_P, _P, _P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats), _P],
+    "pfm2_calc_max_speed": [_P, _P, _P, _P, _P],
+    "pfm2_g2p": [_P, _P, _P, _P, _P, _P, _P],
+    "pfm2_rk4_T_forward": [_P, _P, _P, _P, _P, _F, _I, _P],
+    "pfm2_update_grad_m": [_P, _P, _P, _P, _P],
+    "pfm2_update_T": [_P, _P, _P, _P, _P],
+    "pfm2_update_imp": [_P, _P, _P, _P, _P],
+    "pfm2_reset_T": [_P, _P, _P],
+    "pfm2_midpoint": [_P, _P, _P, _P, _P, _F, _P, _P, _P],
+    "pfm2_sort_particles": [_P, _P, _P, _P, _P],
+    "pfm2_p2g": [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
+    "pfm2_poisson": [_P, _P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats), _P],
+    "pfm_mgpcg_solve": [_P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats), _P],
+}
+_RESTYPE = {"pfm_last_error": ctypes.c_char_p, "pfm_status_string": ctypes.c_char_p}
+
+_lib = None
+
+
+def lib_path():
+    return _build.LIB_PATH
+
+
+def load(build_if_missing=True):
+    """Load libpfm.so (building it first when absent).  Raises PfmError if that fails."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise PfmError(6, f"libpfm.so not built at {path}")
+        try:
+            _build.build()
+        except Exception as e:  # noqa: BLE001
+            raise PfmError(6, f"cannot build libpfm.so: {e}") from e
+    L = ctypes.CDLL(path)
+    for name, args in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = _RESTYPE.get(name, ctypes.c_int)
+    _lib = L
+    return L
+
+
+def exported_symbols():
+    return list(SIGNATURES)

@@ -1,0 +1,302 @@
+"""Host side of the GB300 particle-flow-map step: one :class:`Scene` per simulated domain.
+
+A Scene owns a libpfm handle and its device workspace (a torch uint8 buffer); torch tensors are
+used only as device buffers.  Each method launches the sm_103a kernels of one reference phase on
+the current torch CUDA stream.  Particle fields are SoA tensors ``[n, P]`` (``[d, d, P]`` for the
+per-particle vector triples T_x/T_y/T_z and init_C_x/..); grids have the reference's shapes.
+"""
+import ctypes
+
+import torch
+
+from . import _lib
+from ._lib import PfmError, SolveOpts, SolveStats
+
+__all__ = ["Scene", "PfmError", "SolveInfo"]
+
+
+class SolveInfo:
+    """Result of one MGPCG solve (what the reference prints: iteration and final residual)."""
+
+    def __init__(self, stats, status):
+        self.iterations = int(stats.iterations)
+        self.converged = bool(stats.converged)
+        self.rTr = float(stats.rTr)
+        self.rTr0 = float(stats.rTr0)
+        self.status = status
+
+    def __repr__(self):
+        return (f"SolveInfo(iterations={self.iterations}, converged={self.converged}, "
+                f"rTr={self.rTr:.3e})")
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+class Scene:
+    """One scene: grid resolution, cell size, particle count and MGPCG configuration.
+
+    Mirrors the module-level state the reference's kernels read (``dx``, ``res_x/y/z`` from
+    hyperparameters.py, ``MGPCG_3(boundary_types, N, base_level)`` in 3D/run_3D.py:28-29).
+    """
+
+    def __init__(self, dim, res, dx, particles, base_level=3, mg_levels=0, boundary=None,
+                 use_apic=True, pre_post_smoothing=2, bottom_smoothing=50, device=None):
+        if not torch.cuda.is_available():
+            raise PfmError(6, "CUDA is not available: the particle-flow-map step runs only on the GPU")
+        self.lib = _lib.load()
+        self.dim = int(dim)
+        res = tuple(int(r) for r in res)
+        self.res = res[:self.dim]
+        self.dx = float(dx)
+        self.P = int(particles)
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        cfg = _lib.Config()
+        cfg.dim = self.dim
+        for a in range(3):
+            cfg.res[a] = res[a] if a < len(res) else 1
+        cfg.dx = self.dx
+        cfg.particles = self.P
+        cfg.base_level = int(base_level)
+        cfg.mg_levels = int(mg_levels)
+        cfg.pre_post_smoothing = int(pre_post_smoothing)
+        cfg.bottom_smoothing = int(bottom_smoothing)
+        bt = boundary if boundary is not None else [[2, 2]] * 3
+        for a in range(3):
+            row = bt[a] if a < len(bt) else (2, 2)
+            cfg.boundary[a][0], cfg.boundary[a][1] = int(row[0]), int(row[1])
+        cfg.use_apic = int(bool(use_apic))
+        self.cfg = cfg
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            st = self.lib.pfm_create(ctypes.byref(cfg), ctypes.byref(h))
+            if st != 0:
+                raise PfmError(st, "pfm_create failed (check res, dx, particle count, MG levels)")
+            self.h = h
+            size = ctypes.c_size_t()
+            self._check(self.lib.pfm_workspace_size(h, ctypes.byref(size)))
+            self.workspace = torch.empty(max(int(size.value), 256), dtype=torch.uint8, device=self.device)
+            self._check(self.lib.pfm_set_workspace(h, _ptr(self.workspace), ctypes.c_size_t(self.workspace.numel())))
+            self.max_dev = torch.zeros(1, dtype=torch.float32, device=self.device)
+        lv = ctypes.c_int()
+        self._check(self.lib.pfm_mg_levels(h, ctypes.byref(lv)))
+        self.mg_levels = lv.value
+
+    # ------------------------------------------------------------------------------------------
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h is not None and getattr(self, "lib", None) is not None:
+            self.lib.pfm_destroy(h)
+            self.h = None
+
+    def _check(self, status, allow=()):
+        if status != 0 and status not in allow:
+            msg = self.lib.pfm_last_error(self.h) if getattr(self, "h", None) else b""
+            raise PfmError(status, (msg or b"").decode())
+        return status
+
+    def _stream(self):
+        return ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+
+    @property
+    def face_shapes(self):
+        if self.dim == 3:
+            nx, ny, nz = self.res
+            return [(nx + 1, ny, nz), (nx, ny + 1, nz), (nx, ny, nz + 1)]
+        nx, ny = self.res
+        return [(nx + 1, ny), (nx, ny + 1)]
+
+    @property
+    def cell_shape(self):
+        return tuple(self.res)
+
+    def _grid(self, t, fam, name):
+        self._dev(t, name)
+        if tuple(t.shape) != self.face_shapes[fam]:
+            raise PfmError(2, f"{name}: shape {tuple(t.shape)} != {self.face_shapes[fam]}")
+        return t
+
+    def _dev(self, t, name, dtype=torch.float32):
+        if not isinstance(t, torch.Tensor):
+            raise PfmError(1, f"{name} must be a torch tensor")
+        if t.device.type != "cuda":
+            raise PfmError(7, f"{name} must be a CUDA tensor")
+        if t.dtype != dtype:
+            raise PfmError(7, f"{name} must be {dtype}")
+        if not t.is_contiguous():
+            raise PfmError(7, f"{name} must be contiguous")
+        return t
+
+    def _part(self, t, n, name, vec=None):
+        self._dev(t, name)
+        want = (n, self.P) if vec is None else (vec, n, self.P)
+        if tuple(t.shape) != want:
+            raise PfmError(2, f"{name}: shape {tuple(t.shape)} != {want}")
+        return t
+
+    def _grids(self, u, name="u"):
+        if len(u) != self.dim:
+            raise PfmError(2, f"{name} needs {self.dim} face grids")
+        return [self._grid(t, f, f"{name}[{f}]") for f, t in enumerate(u)]
+
+    def alloc_faces(self, fill=0.0):
+        return [torch.full(s, fill, dtype=torch.float32, device=self.device) for s in self.face_shapes]
+
+    # ------------------------------------------------------------------------------------------
+    # phases
+    # ------------------------------------------------------------------------------------------
+    def calc_max_speed_async(self, u):
+        """calc_max_speed: result stays on the device in ``self.max_dev``."""
+        u = self._grids(u)
+        if self.dim == 3:
+            self._check(self.lib.pfm3_calc_max_speed(self.h, *map(_ptr, u), _ptr(self.max_dev), self._stream()))
+        else:
+            self._check(self.lib.pfm2_calc_max_speed(self.h, *map(_ptr, u), _ptr(self.max_dev), self._stream()))
+        return self.max_dev
+
+    def calc_max_speed(self, u):
+        """calc_max_speed + the ``max_speed[None]`` read (a host sync, as in the reference)."""
+        return float(self.calc_max_speed_async(u).item())
+
+    def g2p(self, pos, u, imp_out=None, C_out=None):
+        """init_particles_imp (imp_out) / init_particles_imp_grad_m (C_out) G2P."""
+        d = self.dim
+        self._part(pos, d, "pos")
+        u = self._grids(u)
+        if imp_out is not None:
+            self._part(imp_out, d, "imp_out")
+        if C_out is not None:
+            self._part(C_out, d, "C_out", vec=d)
+        fn = self.lib.pfm3_g2p if d == 3 else self.lib.pfm2_g2p
+        self._check(fn(self.h, _ptr(pos), *map(_ptr, u), _ptr(imp_out), _ptr(C_out), self._stream()))
+
+    def update_T(self, T_init, T_gm, reset_gm=True):
+        """3D update_T + reset_T_to_identity(T_gm)."""
+        self._part(T_init, 3, "T_init", vec=3)
+        self._part(T_gm, 3, "T_gm", vec=3)
+        self._check(self.lib.pfm3_update_T(self.h, _ptr(T_init), _ptr(T_gm), int(bool(reset_gm)), self._stream()))
+
+    def reset_T(self, T):
+        d = self.dim
+        self._part(T, d, "T", vec=d)
+        fn = self.lib.pfm3_reset_T if d == 3 else self.lib.pfm2_reset_T
+        self._check(fn(self.h, _ptr(T), self._stream()))
+
+    def rk4_T_forward(self, pos, T, u, dt, advect_psi=True):
+        d = self.dim
+        self._part(pos, d, "pos")
+        self._part(T, d, "T", vec=d)
+        u = self._grids(u)
+        if d == 3:
+            self._check(self.lib.pfm3_rk4_T_forward(self.h, _ptr(pos), _ptr(T), *map(_ptr, u), ctypes.c_float(dt),
+                                                    self._stream()))
+        else:
+            self._check(self.lib.pfm2_rk4_T_forward(self.h, _ptr(pos), _ptr(T), *map(_ptr, u), ctypes.c_float(dt),
+                                                    int(bool(advect_psi)), self._stream()))
+
+    def midpoint(self, u0, u1, dt_half, psi_out=None, T_out=None):
+        d = self.dim
+        u0 = self._grids(u0, "u0")
+        u1 = self._grids(u1, "u1")
+        arr = ctypes.c_void_p * d
+        ps = arr(*[t.data_ptr() for t in psi_out]) if psi_out is not None else None
+        ts = arr(*[t.data_ptr() for t in T_out]) if T_out is not None else None
+        if d == 3:
+            self._check(self.lib.pfm3_midpoint(self.h, *map(_ptr, u0), *map(_ptr, u1), ctypes.c_float(dt_half),
+                                               ps, ts, self._stream()))
+        else:
+            self._check(self.lib.pfm2_midpoint(self.h, *map(_ptr, u0), *map(_ptr, u1), ctypes.c_float(dt_half),
+                                               ps, ts, self._stream()))
+
+    def sort_particles(self, pos):
+        """get_particles_id_in_every_cell as a deterministic counting sort.
+
+        Returns (cell_count [cells] int32, order [P] int32 stable permutation)."""
+        d = self.dim
+        self._part(pos, d, "pos")
+        count = torch.empty(self.cell_shape, dtype=torch.int32, device=self.device)
+        order = torch.empty(max(self.P, 1), dtype=torch.int32, device=self.device)
+        fn = self.lib.pfm3_sort_particles if d == 3 else self.lib.pfm2_sort_particles
+        self._check(fn(self.h, _ptr(pos), _ptr(count), _ptr(order), self._stream()))
+        return count, order[:self.P]
+
+    def p2g3(self, init_imp, pos, T_gm, T_init, init_C, u_out, w_out):
+        """3D P2G (3D/run_3D.py:441-552)."""
+        self._part(init_imp, 3, "init_imp")
+        self._part(pos, 3, "pos")
+        self._part(T_gm, 3, "T_gm", vec=3)
+        self._part(T_init, 3, "T_init", vec=3)
+        self._part(init_C, 3, "init_C", vec=3)
+        u_out = self._grids(u_out, "u_out")
+        w_out = self._grids(w_out, "w_out")
+        self._check(self.lib.pfm3_p2g(self.h, _ptr(init_imp), _ptr(pos), _ptr(T_gm), _ptr(T_init), _ptr(init_C),
+                                      *map(_ptr, u_out), *map(_ptr, w_out), self._stream()))
+
+    def p2g2(self, imp, pos, C, psi, u_out, w_out, psi_out=None):
+        """2D P2G (2D/run_2D.py:548-611); psi_out = (psi_x_grid [F,2], psi_y_grid [F,2]) or None."""
+        self._part(imp, 2, "imp")
+        self._part(pos, 2, "pos")
+        self._part(C, 2, "C", vec=2)
+        if psi is not None:
+            self._part(psi, 2, "psi")
+        u_out = self._grids(u_out, "u_out")
+        w_out = self._grids(w_out, "w_out")
+        px = py = None
+        if psi_out is not None:
+            px, py = psi_out
+            for f, t in enumerate((px, py)):
+                self._dev(t, "psi_out")
+                if tuple(t.shape) != self.face_shapes[f] + (2,):
+                    raise PfmError(2, "psi_out shape")
+        self._check(self.lib.pfm2_p2g(self.h, _ptr(imp), _ptr(pos), _ptr(C), _ptr(psi), *map(_ptr, u_out),
+                                      _ptr(px), _ptr(py), *map(_ptr, w_out), self._stream()))
+
+    def update_grad_m2(self, C, init_C, T_gm):
+        for t, n in ((C, "C"), (init_C, "init_C"), (T_gm, "T_gm")):
+            self._part(t, 2, n, vec=2)
+        self._check(self.lib.pfm2_update_grad_m(self.h, _ptr(C), _ptr(init_C), _ptr(T_gm), self._stream()))
+
+    def update_T2(self, T, T_init, T_gm):
+        for t, n in ((T, "T"), (T_init, "T_init"), (T_gm, "T_gm")):
+            self._part(t, 2, n, vec=2)
+        self._check(self.lib.pfm2_update_T(self.h, _ptr(T), _ptr(T_init), _ptr(T_gm), self._stream()))
+
+    def update_imp2(self, imp, init_imp, T):
+        self._part(imp, 2, "imp")
+        self._part(init_imp, 2, "init_imp")
+        self._part(T, 2, "T", vec=2)
+        self._check(self.lib.pfm2_update_imp(self.h, _ptr(imp), _ptr(init_imp), _ptr(T), self._stream()))
+
+    @staticmethod
+    def _opts(max_iters, tol, tol_mode, check_every, eps=1e-12):
+        o = SolveOpts()
+        o.max_iters, o.eps, o.tol, o.tol_mode, o.check_every = int(max_iters), float(eps), float(tol), int(tol_mode), int(check_every)
+        return o
+
+    def poisson(self, u, p_out=None, max_iters=400, tol=1e-12, tol_mode=0, check_every=4, raise_on_limit=False):
+        """MGPCG_{2,3}.Poisson in place on u (a sync point).  Returns SolveInfo."""
+        u = self._grids(u)
+        if p_out is not None:
+            self._dev(p_out, "p_out")
+            if tuple(p_out.shape) != self.cell_shape:
+                raise PfmError(2, "p_out shape")
+        o = self._opts(max_iters, tol, tol_mode, check_every)
+        s = SolveStats()
+        fn = self.lib.pfm3_poisson if self.dim == 3 else self.lib.pfm2_poisson
+        allow = () if raise_on_limit else (_lib.PFM_ERR_NOT_CONVERGED,)
+        st = self._check(fn(self.h, *map(_ptr, u), _ptr(p_out), ctypes.byref(o), ctypes.byref(s), self._stream()),
+                         allow=allow)
+        return SolveInfo(s, st)
+
+    def mgpcg_solve(self, div, x_out, max_iters=400, tol=1e-12, tol_mode=0, check_every=4):
+        """MGPCG init(div, -1) + solve + get_result."""
+        self._dev(div, "div")
+        self._dev(x_out, "x_out")
+        if tuple(div.shape) != self.cell_shape or tuple(x_out.shape) != self.cell_shape:
+            raise PfmError(2, "div/x_out must have the cell shape")
+        o = self._opts(max_iters, tol, tol_mode, check_every)
+        s = SolveStats()
+        st = self._check(self.lib.pfm_mgpcg_solve(self.h, _ptr(div), _ptr(x_out), ctypes.byref(o), ctypes.byref(s),
+                                                  self._stream()), allow=(_lib.PFM_ERR_NOT_CONVERGED,))
+        return SolveInfo(s, st)

@@ -1,0 +1,235 @@
+"""The particle-flow-map step loops on the GPU: run_3D.main() / run_2D.main() loop bodies.
+
+Phase order, reinitialisation cadence and the CFL/frame clock follow 3D/run_3D.py:716-822 and
+2D/run_2D.py:772-909; every phase is one libpfm entry point (see core.Scene).
+"""
+import numpy as np
+import torch
+
+from .core import Scene
+
+__all__ = ["DtClock", "Sim3D", "Sim2D", "soa", "aos", "soa_T", "aos_T", "lattice3", "lattice2",
+           "jittered"]
+
+
+# ------------------------------------------------------------------------------------------------
+# layout helpers: the reference's Taichi AoS [P, n] / [P, nv, nc]  <->  device SoA [n, P] / [nv, nc, P]
+# ------------------------------------------------------------------------------------------------
+def soa(a, device="cuda"):
+    return torch.from_numpy(np.ascontiguousarray(np.asarray(a, np.float32).T)).to(device)
+
+
+def aos(t):
+    return t.detach().cpu().numpy().T.copy()
+
+
+def soa_T(a, device="cuda"):
+    return torch.from_numpy(np.ascontiguousarray(np.asarray(a, np.float32).transpose(1, 2, 0))).to(device)
+
+
+def aos_T(t):
+    return t.detach().cpu().numpy().transpose(2, 0, 1).copy()
+
+
+# ------------------------------------------------------------------------------------------------
+# particle seeding
+# ------------------------------------------------------------------------------------------------
+def lattice3(res, dx, ppc_axis=2):
+    """init_particles_pos_uniform (3D/init_conditions.py:238-252): the reference's x-fastest lattice."""
+    nx, ny, nz = res
+    P = nx * ny * nz * ppc_axis ** 3
+    i = np.arange(P, dtype=np.int64)
+    px, py = ppc_axis * nx, ppc_axis * ny
+    idx = np.stack([i % px, (i // px) % py, (i // px) // py], axis=1)
+    dist = np.float32(dx / ppc_axis)
+    return ((idx.astype(np.float32) + np.float32(0.5)) * dist).astype(np.float32)
+
+
+def lattice2(res, dx, ppc):
+    """init_particles_pos_uniform (2D/init_conditions.py:139-166)."""
+    nx, ny = res
+    axis = int(np.sqrt(ppc))
+    P = nx * ny * ppc
+    i = np.arange(P, dtype=np.int64)
+    px = axis * nx
+    idx = np.stack([i % px, i // px], axis=1)
+    dist = np.float32(dx / axis)
+    return ((idx.astype(np.float32) + np.float32(0.5)) * dist).astype(np.float32)
+
+
+def jittered(res, dx, ppc, seed=0):
+    """Stratified jitter: each cell holds ppc particles, one per sub-cell of a ppc_axis^d lattice,
+    placed uniformly inside its sub-cell by numpy.random.default_rng(seed).  Stored cell-major
+    with the last axis fastest, so consecutive particles share grid neighbourhoods."""
+    d = len(res)
+    axis = int(round(ppc ** (1.0 / d)))
+    if axis ** d != ppc:
+        raise ValueError("particles per cell must be a perfect square (2D) or cube (3D)")
+    rng = np.random.default_rng(seed)
+    cells = np.stack(np.meshgrid(*[np.arange(n) for n in res], indexing="ij"), axis=-1).reshape(-1, d)
+    sub = np.stack(np.meshgrid(*[np.arange(axis)] * d, indexing="ij"), axis=-1).reshape(-1, d)
+    lat = (cells[:, None, :] * axis + sub[None, :, :]).reshape(-1, d).astype(np.float64)
+    jit = rng.uniform(0.0, 1.0, size=lat.shape)
+    return ((lat + jit) * (dx / axis)).astype(np.float32)
+
+
+class DtClock:
+    """CFL step with the frame clamp of run_3D.py:725-743 / run_2D.py:782-799 (Python doubles)."""
+
+    def __init__(self, CFL, dx, visualize_dt, save_frame_each_step=False):
+        self.CFL, self.dx, self.visualize_dt = CFL, dx, visualize_dt
+        self.save_frame_each_step = save_frame_each_step
+        self.sub_t = 0.0
+        self.frame_idx = 0
+
+    def next(self, max_speed):
+        curr_dt = self.CFL * self.dx / max_speed
+        if self.save_frame_each_step:
+            self.frame_idx += 1
+            return curr_dt, True
+        if self.sub_t + curr_dt >= self.visualize_dt:
+            curr_dt = self.visualize_dt - self.sub_t
+            self.sub_t = 0.0
+            self.frame_idx += 1
+            return curr_dt, True
+        self.sub_t += curr_dt
+        return curr_dt, False
+
+
+class Sim3D:
+    """GPU state and step of the 3D solver (3D/run_3D.py:716-822)."""
+
+    def __init__(self, u, seeds, res, dx, CFL=0.5, visualize_dt=0.1, reinit_every=20,
+                 reinit_every_grad_m=1, use_midpoint_vel=True, reinit_particle_pos=True, use_apic=True,
+                 base_level=3, mg_levels=0, poisson_opts=None, device="cuda"):
+        seeds = np.asarray(seeds, np.float32)
+        self.P = seeds.shape[0]
+        self.scene = Scene(3, res, dx, self.P, base_level=base_level, mg_levels=mg_levels, use_apic=use_apic,
+                           device=device)
+        sc = self.scene
+        self.res, self.dx = tuple(res), dx
+        self.clock = DtClock(CFL, dx, visualize_dt)
+        self.reinit_every, self.grad_m = reinit_every, reinit_every_grad_m
+        self.use_midpoint_vel, self.reinit_particle_pos = use_midpoint_vel, reinit_particle_pos
+        self.poisson_opts = dict(poisson_opts or {})
+        self.u = [torch.as_tensor(np.asarray(a, np.float32)).to(sc.device).contiguous() for a in u]
+        self.u_mid = sc.alloc_faces()
+        self.w = sc.alloc_faces()
+        dev = sc.device
+        self.seeds = soa(seeds, dev)
+        P = self.P
+        self.pos = torch.zeros(3, P, device=dev)
+        self.init_imp = torch.zeros(3, P, device=dev)
+        self.T_init = torch.zeros(3, 3, P, device=dev)
+        self.T_gm = torch.zeros(3, 3, P, device=dev)
+        self.init_C = torch.zeros(3, 3, P, device=dev)
+        sc.reset_T(self.T_init)
+        sc.reset_T(self.T_gm)
+        self.p = torch.zeros(sc.cell_shape, device=dev)
+        self.i, self.ik = -1, 0
+        self.infos = []
+        self.last_dt = None
+
+    def step(self):
+        sc = self.scene
+        self.i += 1
+        i = self.i
+        j = i % self.reinit_every
+        max_speed = sc.calc_max_speed(self.u)
+        curr_dt, _ = self.clock.next(max_speed)
+        self.last_dt = curr_dt
+        if j == 0:
+            if self.reinit_particle_pos or i == 0:
+                self.pos.copy_(self.seeds)
+                self.ik = i
+            sc.g2p(self.pos, self.u, imp_out=self.init_imp)
+            sc.reset_T(self.T_init)
+            sc.reset_T(self.T_gm)
+        k = (i - self.ik) % self.grad_m
+        if k == 0:
+            sc.g2p(self.pos, self.u, C_out=self.init_C)
+            sc.update_T(self.T_init, self.T_gm, reset_gm=True)
+        adv = self.u
+        if self.use_midpoint_vel:
+            sc.midpoint(self.u, self.u_mid, float(np.float32(0.5 * curr_dt)))
+            self.infos.append(sc.poisson(self.u_mid, **self.poisson_opts))
+            adv = self.u_mid
+        sc.rk4_T_forward(self.pos, self.T_gm, adv, float(np.float32(curr_dt)))
+        sc.p2g3(self.init_imp, self.pos, self.T_gm, self.T_init, self.init_C, self.u, self.w)
+        self.infos.append(sc.poisson(self.u, self.p, **self.poisson_opts))
+        return curr_dt
+
+
+class Sim2D:
+    """GPU state and step of the 2D solver (2D/run_2D.py:772-909)."""
+
+    def __init__(self, u, seeds, res, dx, CFL=0.5, visualize_dt=0.1, reinit_every=12,
+                 reinit_every_grad_m=8, use_midpoint_vel=True, reinit_particle_pos=True, use_apic=True,
+                 base_level=3, mg_levels=0, poisson_opts=None, device="cuda"):
+        seeds = np.asarray(seeds, np.float32)
+        self.P = seeds.shape[0]
+        self.scene = Scene(2, res, dx, self.P, base_level=base_level, mg_levels=mg_levels, use_apic=use_apic,
+                           device=device)
+        sc = self.scene
+        self.res, self.dx = tuple(res), dx
+        self.clock = DtClock(CFL, dx, visualize_dt)
+        self.reinit_every, self.grad_m = reinit_every, reinit_every_grad_m
+        self.use_midpoint_vel, self.reinit_particle_pos = use_midpoint_vel, reinit_particle_pos
+        self.poisson_opts = dict(poisson_opts or {})
+        dev = sc.device
+        self.u = [torch.as_tensor(np.asarray(a, np.float32)).to(dev).contiguous() for a in u]
+        self.u_mid = sc.alloc_faces()
+        self.w = sc.alloc_faces()
+        self.psi_grid = [torch.zeros(s + (2,), device=dev) for s in sc.face_shapes]
+        self.seeds = soa(seeds, dev)
+        P = self.P
+        self.pos = self.seeds.clone()
+        self.imp = torch.zeros(2, P, device=dev)
+        self.init_imp = torch.zeros(2, P, device=dev)
+        self.psi = self.seeds.clone()
+        self.T = torch.zeros(2, 2, P, device=dev)
+        self.T_init = torch.zeros(2, 2, P, device=dev)
+        self.T_gm = torch.zeros(2, 2, P, device=dev)
+        for t in (self.T, self.T_init, self.T_gm):
+            sc.reset_T(t)
+        self.init_C = torch.zeros(2, 2, P, device=dev)
+        self.C = torch.zeros(2, 2, P, device=dev)
+        self.p = torch.zeros(sc.cell_shape, device=dev)
+        self.i, self.ik = -1, 0
+        self.infos = []
+        self.last_dt = None
+
+    def step(self):
+        sc = self.scene
+        self.i += 1
+        i = self.i
+        j = i % self.reinit_every
+        max_speed = sc.calc_max_speed(self.u)
+        curr_dt, _ = self.clock.next(max_speed)
+        self.last_dt = curr_dt
+        if j == 0:
+            if self.reinit_particle_pos or i == 0:
+                self.pos.copy_(self.seeds)
+            self.ik = i
+            sc.g2p(self.pos, self.u, imp_out=self.imp)
+            self.init_imp.copy_(self.imp)
+            self.psi.copy_(self.pos)
+            sc.reset_T(self.T)
+            sc.reset_T(self.T_init)
+        k = (i - self.ik) % self.grad_m
+        if k == 0:
+            sc.g2p(self.pos, self.u, C_out=self.init_C)
+            sc.reset_T(self.T_gm)
+            self.T_init.copy_(self.T)
+        adv = self.u
+        if self.use_midpoint_vel:
+            sc.midpoint(self.u, self.u_mid, float(np.float32(0.5 * curr_dt)))
+            self.infos.append(sc.poisson(self.u_mid, **self.poisson_opts))
+            adv = self.u_mid
+        sc.rk4_T_forward(self.pos, self.T_gm, adv, float(np.float32(curr_dt)), advect_psi=True)
+        sc.update_grad_m2(self.C, self.init_C, self.T_gm)
+        sc.update_T2(self.T, self.T_init, self.T_gm)
+        sc.update_imp2(self.imp, self.init_imp, self.T)
+        sc.p2g2(self.imp, self.pos, self.C, self.psi, self.u, self.w, psi_out=self.psi_grid)
+        self.infos.append(sc.poisson(self.u, self.p, **self.poisson_opts))
+        return curr_dt

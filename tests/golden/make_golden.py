@@ -1,0 +1,435 @@
+"""Generate the golden vectors by running the reference's own Python/Taichi source.
+
+Run in a container that has the reference checked out (it reads ``/root/reference``)::
+
+    python tests/golden/make_golden.py ref3d_kernels   # per-kernel cases, 3D
+    python tests/golden/make_golden.py ref2d_kernels   # per-kernel cases, 2D
+    python tests/golden/make_golden.py ref3d_steps     # run_3D.main(): 10 steps at 8^3
+    python tests/golden/make_golden.py ref2d_steps     # run_2D.main(): 20 steps at 32^2
+
+Taichi 1.5.0 is not installable here, so the reference modules are executed through
+``oracle/ref_shim`` (a restatement of the Taichi semantics the step uses: f32 arithmetic,
+truncating ``int()``, sequential struct-for, in-place atomics).  Every kernel, ``@ti.func`` and
+the ``main()`` driver that produces the numbers is the reference's unmodified source; only the
+``hyperparameters`` module (grid size, reinit cadence), the image/VTK writers (``io_utils``) and the
+2D driver's missing ``single_vortex`` import are replaced.  Each case writes one
+``tests/golden/<case>.npz``.
+"""
+import contextlib
+import io
+import os
+import re
+import shutil
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REF = "/root/reference"
+sys.path.insert(0, os.path.join(REPO, "oracle", "ref_shim"))
+import loader  # noqa: E402
+
+IO_STUB = dict(np=np, os=os, remove_everything_in=lambda d: None,
+               write_field=lambda *a, **k: None, write_image=lambda *a, **k: None,
+               write_w_and_smoke=lambda *a, **k: None, write_particles=lambda *a, **k: None)
+
+
+def hp3d(res, **over):
+    hp = dict(case=0, dim=3, use_midpoint_vel=True, forward_update_T=True, use_APIC=True,
+              use_APIC_smoke=True, save_particle_pos_numpy=False, save_particle_imp_numpy=False,
+              save_frame_each_step=False, reinit_particle_pos=True, min_res=(8, 8, 8), num_levels=4,
+              feat_dim=4, activate_threshold=0.032, N_iters=1, N_batch=1, success_threshold=2e-7,
+              res_x=res[0], res_y=res[1], res_z=res[2], visualize_dt=0.1, reinit_every=20,
+              reinit_every_grad_m=1, ckpt_every=1, CFL=0.5, from_frame=0, total_frames=10 ** 6,
+              use_total_steps=True, total_steps=1, exp_name="golden3d", particles_per_cell=8,
+              total_particles_num_ratio=1, cell_max_particle_num_ratio=1.6)
+    hp.update(over)
+    return hp
+
+
+def hp2d(res, **over):
+    hp = dict(dim=2, testing=False, use_neural=False, save_ckpt=True, save_frame_each_step=False,
+              use_BFECC=False, use_midpoint_vel=True, use_APIC=True, forward_update_T=True,
+              plot_particles=False, use_reseed_particles=False, reinit_particle_pos=True, dpi_vor=64,
+              min_res=(8, 8), num_levels=4, feat_dim=2, activate_threshold=0.03, N_iters=1, N_batch=1,
+              success_threshold=3e-8, res_x=res[0], res_y=res[1], visualize_dt=0.1, reinit_every=12,
+              reinit_every_grad_m=8, ckpt_every=1, CFL=0.5, from_frame=0, total_frames=10 ** 6,
+              use_total_steps=True, total_steps=1, exp_name="golden2d", particles_per_cell=4,
+              total_particles_num_ratio=1, cell_max_particle_num_ratio=2.0,
+              min_particles_per_cell_ratio=1, min_particles_per_cell=4,
+              max_particles_per_cell_ratio=1.6, max_particles_per_cell=6,
+              max_delete_particle_try_num=100000)
+    hp.update(over)
+    return hp
+
+
+def load3d(hp):
+    loader.install(os.path.join(REF, "3D"), ["taichi_utils", "mgpcg", "init_conditions", "run_3D"],
+                   hp, {"io_utils": IO_STUB})
+    import run_3D
+    return run_3D
+
+
+def load2d(hp):
+    sv = dict(vortex_vel_func_point=None, dvxdx=None, dvxdy=None, dvydx=None, dvydy=None)
+    loader.install(os.path.join(REF, "2D"), ["taichi_utils", "mgpcg", "init_conditions", "run_2D"],
+                   hp, {"io_utils": IO_STUB, "single_vortex": sv})
+    import run_2D
+    return run_2D
+
+
+def smooth_field(shape, rng, amp=1.0, dx=1.0):
+    """A smooth random grid field (sum of a few low sine modes) for kernel inputs."""
+    idx = np.meshgrid(*[np.arange(s, dtype=np.float64) for s in shape], indexing="ij")
+    out = np.zeros(shape)
+    for _ in range(4):
+        k = rng.uniform(0.5, 2.5, size=len(shape))
+        ph = rng.uniform(0, 2 * np.pi, size=len(shape))
+        term = rng.uniform(-1, 1)
+        for d in range(len(shape)):
+            term = term * np.sin(2 * np.pi * k[d] * idx[d] * dx + ph[d])
+        out += term
+    return (amp * out).astype(np.float32)
+
+
+def vec_field_np(f):
+    return f.to_numpy().astype(np.float32)
+
+
+def set_vec(f, arr):
+    f.from_numpy(np.asarray(arr, dtype=np.float32))
+
+
+# ------------------------------------------------------------------------------------------------
+# 3D per-kernel cases (16^3 grid, so MGPCG runs a 2-level V-cycle)
+# ------------------------------------------------------------------------------------------------
+def ref3d_kernels():
+    import taichi as ti
+    res = (16, 16, 16)
+    R = load3d(hp3d(res))
+    import init_conditions as IC
+    import mgpcg as MG
+    rng = np.random.default_rng(1234)
+    dx = R.dx
+    out = {"res": np.array(res), "dx": np.float32(dx)}
+    nx, ny, nz = res
+    ux = smooth_field((nx + 1, ny, nz), rng, 0.6, 1 / 16)
+    uy = smooth_field((nx, ny + 1, nz), rng, 0.6, 1 / 16)
+    uz = smooth_field((nx, ny, nz + 1), rng, 0.6, 1 / 16)
+    out.update(u_x=ux, u_y=uy, u_z=uz)
+    R.u_x.from_numpy(ux); R.u_y.from_numpy(uy); R.u_z.from_numpy(uz)
+
+    R.calc_max_speed(R.u_x, R.u_y, R.u_z)
+    out["max_speed"] = np.float32(R.max_speed[None])
+
+    n = 512
+    pos = rng.uniform(0.0, 1.0, size=(n, 3)).astype(np.float32)
+    pos[:8] = np.array([[0.001, 0.5, 0.5], [0.999, 0.5, 0.5], [0.5, 0.0005, 0.5], [0.5, 0.5, 0.9999],
+                        [-0.01, 0.3, 0.3], [1.004, 0.6, 0.7], [0.03, 0.97, 0.02], [0.5, 0.5, 0.5]],
+                       dtype=np.float32)
+    out["pos"] = pos
+    T = (np.eye(3)[None] + 0.05 * rng.standard_normal((n, 3, 3))).astype(np.float32)  # [p, vec, comp]
+    out["T_gm"] = T
+    T_init = (np.eye(3)[None] + 0.05 * rng.standard_normal((n, 3, 3))).astype(np.float32)
+    out["T_init"] = T_init
+    C = (0.5 * rng.standard_normal((n, 3, 3))).astype(np.float32)
+    out["init_C"] = C
+    imp0 = (0.5 * rng.standard_normal((n, 3))).astype(np.float32)
+    out["init_imp"] = imp0
+    dt = np.float32(0.4 * dx / out["max_speed"])
+    out["dt"] = dt
+
+    mk = lambda: ti.Vector.field(3, float, shape=n)  # noqa: E731
+    # G2P of impulse and its gradient (init_conditions.py:266-273)
+    p_f, imp_f, Cx, Cy, Cz = mk(), mk(), mk(), mk(), mk()
+    set_vec(p_f, pos)
+    IC.init_particles_imp_grad_m(imp_f, p_f, R.u_x, R.u_y, R.u_z, Cx, Cy, Cz, dx)
+    out["g2p_imp"] = vec_field_np(imp_f)
+    out["g2p_C"] = np.stack([vec_field_np(Cx), vec_field_np(Cy), vec_field_np(Cz)], axis=1)
+
+    # RK4_T_forward (run_3D.py:175-219)
+    p_f = mk(); set_vec(p_f, pos)
+    Tx, Ty, Tz = mk(), mk(), mk()
+    set_vec(Tx, T[:, 0]); set_vec(Ty, T[:, 1]); set_vec(Tz, T[:, 2])
+    R.RK4_T_forward(p_f, Tx, Ty, Tz, R.u_x, R.u_y, R.u_z, dt)
+    out["rk4_pos"] = vec_field_np(p_f)
+    out["rk4_T"] = np.stack([vec_field_np(Tx), vec_field_np(Ty), vec_field_np(Tz)], axis=1)
+
+    # update_T (run_3D.py:430-439)
+    Ti = [mk() for _ in range(3)]
+    Tg = [mk() for _ in range(3)]
+    for v in range(3):
+        set_vec(Ti[v], T_init[:, v]); set_vec(Tg[v], T[:, v])
+    R.update_T(*Ti, *Tg)
+    out["update_T"] = np.stack([vec_field_np(f) for f in Ti], axis=1)
+
+    # P2G (run_3D.py:441-552); init_C is read from the module globals init_C_[xyz]
+    for v, f in enumerate([R.init_C_x, R.init_C_y, R.init_C_z]):
+        a = f.to_numpy(); a[:n] = C[:, v]; f.from_numpy(a)
+    p_f = mk(); set_vec(p_f, pos)
+    imp_f = mk(); set_vec(imp_f, imp0)
+    Ti = [mk() for _ in range(3)]
+    Tg = [mk() for _ in range(3)]
+    for v in range(3):
+        set_vec(Ti[v], T_init[:, v]); set_vec(Tg[v], T[:, v])
+    ux_f = ti.field(float, shape=(nx + 1, ny, nz)); uy_f = ti.field(float, shape=(nx, ny + 1, nz))
+    uz_f = ti.field(float, shape=(nx, ny, nz + 1))
+    wx = ti.field(float, shape=(nx + 1, ny, nz)); wy = ti.field(float, shape=(nx, ny + 1, nz))
+    wz = ti.field(float, shape=(nx, ny, nz + 1))
+    R.P2G(imp_f, mk(), p_f, ux_f, uy_f, uz_f, wx, wy, wz, *Tg, *Ti, R.cell_particles_id,
+          R.cell_particle_num)
+    out.update(p2g_u_x=ux_f.to_numpy(), p2g_u_y=uy_f.to_numpy(), p2g_u_z=uz_f.to_numpy(),
+               p2g_w_x=wx.to_numpy(), p2g_w_y=wy.to_numpy(), p2g_w_z=wz.to_numpy())
+
+    # particle binning (run_3D.py:342-351) on the module's own particle field
+    allp = np.zeros((R.particle_num, 3), np.float32)
+    allp[:] = rng.uniform(0.0, 1.0, size=(R.particle_num, 3))
+    R.particles_pos.from_numpy(allp)
+    R.get_particles_id_in_every_cell(R.cell_particles_id, R.cell_particle_num, R.particles_pos)
+    out["bin_pos"] = allp
+    out["bin_count"] = R.cell_particle_num.to_numpy()
+
+    # midpoint grid step (run_3D.py:779-788 without the projection)
+    R.reset_to_identity_grid(R.psi_x_grid, R.psi_y_grid, R.psi_z_grid, R.T_x_grid, R.T_y_grid,
+                             R.T_z_grid)
+    R.RK4_grid(R.psi_x_grid, R.T_x_grid, R.u_x, R.u_y, R.u_z, 0.5 * float(dt))
+    R.RK4_grid(R.psi_y_grid, R.T_y_grid, R.u_x, R.u_y, R.u_z, 0.5 * float(dt))
+    R.RK4_grid(R.psi_z_grid, R.T_z_grid, R.u_x, R.u_y, R.u_z, 0.5 * float(dt))
+    R.copy_to(R.u_x, R.p2g_weight_x); R.copy_to(R.u_y, R.p2g_weight_y)
+    R.copy_to(R.u_z, R.p2g_weight_z)
+    R.advect_u(R.p2g_weight_x, R.p2g_weight_y, R.p2g_weight_z, R.u_x, R.u_y, R.u_z, R.T_x_grid,
+               R.T_y_grid, R.T_z_grid, R.psi_x_grid, R.psi_y_grid, R.psi_z_grid, dx)
+    out.update(mid_u_x=R.u_x.to_numpy(), mid_u_y=R.u_y.to_numpy(), mid_u_z=R.u_z.to_numpy(),
+               mid_psi_x=R.psi_x_grid.to_numpy(), mid_T_x=R.T_x_grid.to_numpy(),
+               mid_psi_z=R.psi_z_grid.to_numpy(), mid_T_z=R.T_z_grid.to_numpy())
+
+    # MGPCG_3.Poisson (mgpcg.py:425-430) on the midpoint field, 16^3 -> 2 levels
+    log = io.StringIO()
+    with contextlib.redirect_stdout(log):
+        R.solver.Poisson(R.u_x, R.u_y, R.u_z)
+    out.update(poisson_u_x=R.u_x.to_numpy(), poisson_u_y=R.u_y.to_numpy(),
+               poisson_u_z=R.u_z.to_numpy(), poisson_p=R.solver.p.to_numpy(),
+               poisson_iters=np.int32(parse_iters(log.getvalue())[-1]))
+
+    # a non-cubic grid: 32x16x16, 2 levels
+    N2 = [32, 16, 16]
+    s2 = MG.MGPCG_3(boundary_types=R.boundary_types, N=N2, base_level=3)
+    fx = ti.field(float, shape=(33, 16, 16)); fy = ti.field(float, shape=(32, 17, 16))
+    fz = ti.field(float, shape=(32, 16, 17))
+    a, b, c = (smooth_field(f.shape, rng, 0.3, 1 / 16) for f in (fx, fy, fz))
+    fx.from_numpy(a); fy.from_numpy(b); fz.from_numpy(c)
+    out.update(poisson2_in_x=a, poisson2_in_y=b, poisson2_in_z=c)
+    log = io.StringIO()
+    with contextlib.redirect_stdout(log):
+        s2.Poisson(fx, fy, fz)
+    out.update(poisson2_u_x=fx.to_numpy(), poisson2_u_y=fy.to_numpy(), poisson2_u_z=fz.to_numpy(),
+               poisson2_p=s2.p.to_numpy(), poisson2_iters=np.int32(parse_iters(log.getvalue())[-1]))
+    return out
+
+
+def parse_iters(text):
+    its = [int(m) for m in re.findall(r"Converged at iter:\s+(\d+)", text)]
+    its += [-int(m) for m in re.findall(r"without converging at iter:\s+(\d+)", text)]
+    return its or [-1]
+
+
+# ------------------------------------------------------------------------------------------------
+# 2D per-kernel cases (32^2 grid -> 3 MG levels)
+# ------------------------------------------------------------------------------------------------
+def ref2d_kernels():
+    import taichi as ti
+    res = (32, 32)
+    R = load2d(hp2d(res))
+    import init_conditions as IC
+    import mgpcg as MG
+    rng = np.random.default_rng(4321)
+    dx = R.dx
+    nx, ny = res
+    out = {"res": np.array(res), "dx": np.float32(dx)}
+    ux = smooth_field((nx + 1, ny), rng, 0.6, 1 / 32)
+    uy = smooth_field((nx, ny + 1), rng, 0.6, 1 / 32)
+    out.update(u_x=ux, u_y=uy)
+    R.u_x.from_numpy(ux); R.u_y.from_numpy(uy)
+    R.calc_max_speed(R.u_x, R.u_y)
+    out["max_speed"] = np.float32(R.max_speed[None])
+    dt = np.float32(0.4 * dx / out["max_speed"])
+    out["dt"] = dt
+
+    n = 512
+    pos = rng.uniform(0.0, 1.0, size=(n, 2)).astype(np.float32)
+    pos[:6] = np.array([[0.001, 0.5], [0.9995, 0.5], [0.5, 0.0004], [-0.01, 0.3], [1.006, 0.6],
+                        [0.5, 0.5]], dtype=np.float32)
+    out["pos"] = pos
+    T = (np.eye(2)[None] + 0.05 * rng.standard_normal((n, 2, 2))).astype(np.float32)
+    T_init = (np.eye(2)[None] + 0.05 * rng.standard_normal((n, 2, 2))).astype(np.float32)
+    C = (0.5 * rng.standard_normal((n, 2, 2))).astype(np.float32)
+    imp0 = (0.5 * rng.standard_normal((n, 2))).astype(np.float32)
+    psi = (pos + 0.01 * rng.standard_normal((n, 2))).astype(np.float32)
+    out.update(T_gm=T, T_init=T_init, init_C=C, init_imp=imp0, psi=psi)
+    mk = lambda: ti.Vector.field(2, float, shape=n)  # noqa: E731
+
+    # G2P (init_conditions.py:184-210)
+    p_f, imp_f, init_f, Cx, Cy = mk(), mk(), mk(), mk(), mk()
+    set_vec(p_f, pos)
+    IC.init_particles_imp(imp_f, init_f, p_f, R.u_x, R.u_y, Cx, Cy, dx)
+    out["g2p_imp"] = vec_field_np(init_f)
+    IC.init_particles_imp_grad_m(imp_f, p_f, R.u_x, R.u_y, Cx, Cy, dx)
+    out["g2p_C"] = np.stack([vec_field_np(Cx), vec_field_np(Cy)], axis=1)
+
+    # RK4_T_forward with advect_psi=1 (run_2D.py:304-341)
+    p_f = mk(); set_vec(p_f, pos)
+    Tx, Ty = mk(), mk(); set_vec(Tx, T[:, 0]); set_vec(Ty, T[:, 1])
+    R.RK4_T_forward(p_f, Tx, Ty, R.u_x, R.u_y, dt, 1)
+    out["rk4_pos"] = vec_field_np(p_f)
+    out["rk4_T"] = np.stack([vec_field_np(Tx), vec_field_np(Ty)], axis=1)
+
+    # update_particles_grad_m / update_T / update_particles_imp (run_2D.py:517-546)
+    Cx, Cy, iCx, iCy, Tgx, Tgy = mk(), mk(), mk(), mk(), mk(), mk()
+    set_vec(iCx, C[:, 0]); set_vec(iCy, C[:, 1]); set_vec(Tgx, T[:, 0]); set_vec(Tgy, T[:, 1])
+    R.update_particles_grad_m(Cx, Cy, iCx, iCy, Tgx, Tgy)
+    out["grad_m_C"] = np.stack([vec_field_np(Cx), vec_field_np(Cy)], axis=1)
+    Tx, Ty, Tix, Tiy = mk(), mk(), mk(), mk()
+    set_vec(Tix, T_init[:, 0]); set_vec(Tiy, T_init[:, 1])
+    R.update_T(Tx, Ty, Tix, Tiy, Tgx, Tgy)
+    out["update_T"] = np.stack([vec_field_np(Tx), vec_field_np(Ty)], axis=1)
+    imp_f, init_f = mk(), mk(); set_vec(init_f, imp0)
+    R.update_particles_imp(imp_f, init_f, Tx, Ty)
+    out["update_imp"] = vec_field_np(imp_f)
+
+    # P2G (run_2D.py:548-611): reads the module globals C_x, C_y
+    for v, f in enumerate([R.C_x, R.C_y]):
+        a = f.to_numpy(); a[:n] = C[:, v]; f.from_numpy(a)
+    p_f = mk(); set_vec(p_f, pos)
+    imp_f = mk(); set_vec(imp_f, imp0)
+    psi_f = mk(); set_vec(psi_f, psi)
+    fx = ti.field(float, shape=(nx + 1, ny)); fy = ti.field(float, shape=(nx, ny + 1))
+    wx = ti.field(float, shape=(nx + 1, ny)); wy = ti.field(float, shape=(nx, ny + 1))
+    gx = ti.Vector.field(2, float, shape=(nx + 1, ny)); gy = ti.Vector.field(2, float, shape=(nx, ny + 1))
+    R.P2G(imp_f, p_f, fx, fy, psi_f, gx, gy, wx, wy)
+    out.update(p2g_u_x=fx.to_numpy(), p2g_u_y=fy.to_numpy(), p2g_w_x=wx.to_numpy(),
+               p2g_w_y=wy.to_numpy(), p2g_psi_x=gx.to_numpy(), p2g_psi_y=gy.to_numpy())
+
+    # midpoint (run_2D.py:866-871 without the projection)
+    R.reset_to_identity_grid(R.psi_x_grid, R.psi_y_grid, R.T_x_grid, R.T_y_grid)
+    R.RK4_grid(R.psi_x_grid, R.T_x_grid, R.u_x, R.u_y, 0.5 * float(dt))
+    R.RK4_grid(R.psi_y_grid, R.T_y_grid, R.u_x, R.u_y, 0.5 * float(dt))
+    R.copy_to(R.u_x, R.tmp_u_x); R.copy_to(R.u_y, R.tmp_u_y)
+    R.advect_u(R.tmp_u_x, R.tmp_u_y, R.u_x, R.u_y, R.T_x_grid, R.T_y_grid, R.psi_x_grid,
+               R.psi_y_grid, dx)
+    out.update(mid_u_x=R.u_x.to_numpy(), mid_u_y=R.u_y.to_numpy(), mid_psi_x=R.psi_x_grid.to_numpy(),
+               mid_T_x=R.T_x_grid.to_numpy(), mid_psi_y=R.psi_y_grid.to_numpy(),
+               mid_T_y=R.T_y_grid.to_numpy())
+
+    # MGPCG_2.Poisson (mgpcg.py:342-347), 32^2 -> 3 levels
+    log = io.StringIO()
+    with contextlib.redirect_stdout(log):
+        R.solver.Poisson(R.u_x, R.u_y)
+    out.update(poisson_u_x=R.u_x.to_numpy(), poisson_u_y=R.u_y.to_numpy(),
+               poisson_p=R.solver.p.to_numpy(), poisson_iters=np.int32(parse_iters(log.getvalue())[-1]))
+
+    # 64x32 domain (the reference's 4:1 aspect, shrunk), 3 levels
+    s2 = MG.MGPCG_2(boundary_types=R.boundary_types, N=[64, 32], base_level=3)
+    fx = ti.field(float, shape=(65, 32)); fy = ti.field(float, shape=(64, 33))
+    a, b = smooth_field(fx.shape, rng, 0.3, 1 / 32), smooth_field(fy.shape, rng, 0.3, 1 / 32)
+    fx.from_numpy(a); fy.from_numpy(b)
+    out.update(poisson2_in_x=a, poisson2_in_y=b)
+    log = io.StringIO()
+    with contextlib.redirect_stdout(log):
+        s2.Poisson(fx, fy)
+    out.update(poisson2_u_x=fx.to_numpy(), poisson2_u_y=fy.to_numpy(), poisson2_p=s2.p.to_numpy(),
+               poisson2_iters=np.int32(parse_iters(log.getvalue())[-1]))
+    return out
+
+
+# ------------------------------------------------------------------------------------------------
+# whole-step runs through the reference's own main()
+# ------------------------------------------------------------------------------------------------
+def _run_main(R, nsteps, snap_particles_at, particle_fields, grid_fields, extra=None):
+    """Run ``R.main()`` and snapshot after every step's final projection."""
+    snaps = {}
+    state = {"calls": 0, "step": 0, "log": io.StringIO()}
+    solver = R.solver
+    orig = solver.Poisson
+    per_step = 2 if R.use_midpoint_vel else 1
+
+    def hooked(*args, **kw):
+        orig(*args, **kw)
+        state["calls"] += 1
+        c = state["calls"] - 1  # call 0 is the initial-condition projection
+        if c == 0:
+            for name in grid_fields:
+                snaps[f"init_{name}"] = getattr(R, name).to_numpy()
+            return
+        if (c - 1) % per_step == per_step - 1:
+            s = state["step"] + 1
+            state["step"] = s
+            for name in grid_fields:
+                snaps[f"s{s}_{name}"] = getattr(R, name).to_numpy()
+            snaps[f"s{s}_p"] = solver.p.to_numpy()
+            snaps[f"s{s}_max_speed"] = np.float32(R.max_speed[None])
+            if s in snap_particles_at:
+                for name in particle_fields:
+                    snaps[f"s{s}_{name}"] = getattr(R, name).to_numpy()
+            if extra:
+                extra(snaps, s)
+        else:
+            s = state["step"] + 1
+            for name in grid_fields:
+                snaps[f"s{s}_mid_{name}"] = getattr(R, name).to_numpy()
+
+    solver.Poisson = hooked
+    wd = tempfile.mkdtemp()
+    cwd = os.getcwd()
+    try:
+        os.chdir(wd)
+        open("hyperparameters.py", "w").write("# golden run\n")
+        with contextlib.redirect_stdout(state["log"]):
+            R.main(from_frame=0)
+    finally:
+        os.chdir(cwd)
+        shutil.rmtree(wd, ignore_errors=True)
+    its = parse_iters(state["log"].getvalue())
+    snaps["iters"] = np.array(its, dtype=np.int32)
+    dts = [float(m) for m in re.findall(r"Visualize time ([0-9.eE+-]+)/", state["log"].getvalue())]
+    snaps["log_sub_t"] = np.array(dts)
+    assert state["step"] == nsteps, (state["step"], nsteps)
+    return snaps
+
+
+def ref3d_steps():
+    nsteps = 10
+    hp = hp3d((8, 8, 8), reinit_every=5, reinit_every_grad_m=2, total_steps=nsteps)
+    R = load3d(hp)
+    pf = ["particles_pos", "particles_init_imp", "T_x_init", "T_y_init", "T_z_init", "T_x_grad_m",
+          "T_y_grad_m", "T_z_grad_m", "init_C_x", "init_C_y", "init_C_z"]
+    gf = ["u_x", "u_y", "u_z"]
+    snaps = _run_main(R, nsteps, {1, 2, 10}, pf, gf)
+    snaps["res"] = np.array([8, 8, 8])
+    snaps["hp"] = np.array([hp["reinit_every"], hp["reinit_every_grad_m"]])
+    return snaps
+
+
+def ref2d_steps():
+    nsteps = 20
+    hp = hp2d((32, 32), total_steps=nsteps)
+    R = load2d(hp)
+    pf = ["particles_pos", "particles_imp", "particles_init_imp", "T_x", "T_y", "T_x_init",
+          "T_y_init", "T_x_grad_m", "T_y_grad_m", "init_C_x", "init_C_y", "C_x", "C_y", "psi"]
+    gf = ["u_x", "u_y"]
+    snaps = _run_main(R, nsteps, {1, 2, 10, 20}, pf, gf)
+    snaps["res"] = np.array([32, 32])
+    snaps["hp"] = np.array([hp["reinit_every"], hp["reinit_every_grad_m"]])
+    return snaps
+
+
+CASES = dict(ref3d_kernels=ref3d_kernels, ref2d_kernels=ref2d_kernels, ref3d_steps=ref3d_steps,
+             ref2d_steps=ref2d_steps)
+
+if __name__ == "__main__":
+    name = sys.argv[1]
+    data = CASES[name]()
+    path = os.path.join(HERE, f"{name}.npz")
+    np.savez_compressed(path, **{k: np.asarray(v) for k, v in data.items()})
+    print("wrote", path, os.path.getsize(path), "bytes")
