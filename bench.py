@@ -1,0 +1,373 @@
+#!/usr/bin/env python3
+"""Throughput of the particle-flow-map time step on GB300.
+
+Workload: 3D two-ring leapfrog scene (rings on the x axis through (y, z) = (0.5, 0.5), radius
+0.15, core 0.025 with the reference's 1-exp(-(r/d)^3) mollifier, circulation 1.0, centres x = 0.25
+and 0.35), unit cube at res^3 (default 256^3), 8 jittered particles per cell (seed 0), reinit
+every 20 steps, gradient reinit every step, RK4, CFL 0.5, MGPCG (the reference's V-cycle) to a
+1e-6 relative residual.  One bench step = one full time step (run_3D.py:716-822 loop body).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line.  N > 1 (under torchrun) runs N independent replicas, one per GPU; value is
+the whole-job steps/s (N*K / max-over-ranks time).  --impl reference times the CPU oracle (the
+reference's kernels restated in C++/OpenMP) on the host cores.
+"""
+import argparse
+import contextlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(REPO, "particle-flow-maps_gb300"), os.path.join(REPO, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "3D 256³ steps/s: mixed-prec+warm-start vs plain FP32 at equal residual; %HBM peak"
+UNIT = "steps/s"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--res", type=int, default=256)
+    ap.add_argument("--ppc-axis", type=int, default=2)
+    ap.add_argument("--tol", type=float, default=1e-6)
+    ap.add_argument("--tol-mode", type=int, default=1, help="0: r.r < tol (reference); 1: relative norm")
+    ap.add_argument("--cpu-res", type=int, default=64, help="grid of the bounded CPU sample")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def ring_params():
+    """The two coaxial rings of the 3D workload (add_vortex_ring arguments)."""
+    common = dict(w=1.0, rad=0.15, delta=0.025, unit_x=(0.0, 0.0, -1.0), unit_y=(0.0, 1.0, 0.0), num_samples=2000)
+    return [dict(common, c=(0.25, 0.5, 0.5)), dict(common, c=(0.35, 0.5, 0.5))]
+
+
+# ------------------------------------------------------------------------------------------------
+# GPU scene set-up
+# ------------------------------------------------------------------------------------------------
+def make_sim(res, ppc_axis, poisson_opts, device="cuda"):
+    import torch
+    import pfm
+    n = res
+    dx = 1.0 / n
+    P = n ** 3 * ppc_axis ** 3
+    seeds = torch.empty(3, P, device=device)
+    zeros = [torch.zeros(s, device=device) for s in ((n + 1, n, n), (n, n + 1, n), (n, n, n + 1))]
+    sim = pfm.Sim3D(zeros, seeds, (n, n, n), dx, CFL=0.5, visualize_dt=0.1, reinit_every=20, reinit_every_grad_m=1,
+                    poisson_opts=poisson_opts, device=device)
+    sc = sim.scene
+    sc.seed_jittered(sim.seeds, 0, ppc_axis)
+    vc = torch.zeros((n, n, n, 3), device=device)
+    for r in ring_params():
+        sc.add_vortex_ring(vc, **r)
+    sc.split_central_vector(vc, sim.u)
+    del vc
+    sc.poisson(sim.u, **poisson_opts)  # split_central_vector + Poisson (run_3D.py:667-670)
+    torch.cuda.synchronize()
+    return sim
+
+
+class PhaseTimer:
+    """CUDA-event pairs around the step phases (on the launching stream)."""
+
+    def __init__(self):
+        self.records = {}
+
+    @contextlib.contextmanager
+    def __call__(self, name):
+        import torch
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        yield
+        b.record()
+        self.records.setdefault(name, []).append((a, b))
+
+    def summary(self):
+        return {k: [a.elapsed_time(b) for a, b in v] for k, v in self.records.items()}
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, ValueError, KeyError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+# ------------------------------------------------------------------------------------------------
+# CPU oracle sample (cpu_baseline and the reference arm)
+# ------------------------------------------------------------------------------------------------
+def cpu_ic(n):
+    """The same two-ring velocity at n^3, built on the host (numpy Biot-Savart of add_vortex_ring)."""
+    import numpy as np
+    dx = 1.0 / n
+    vc = np.zeros((n, n, n, 3), np.float64)
+    g = (np.arange(n) + 0.5) * dx
+    X = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1)
+    for r in ring_params():
+        c, ux, uy = map(np.array, (r["c"], r["unit_x"], r["unit_y"]))
+        ns, rad, dl, w = r["num_samples"], r["rad"], r["delta"], r["w"]
+        cl = 2 * np.pi * rad / ns
+        for l in range(0, ns, 8):  # every 8th sample with 8x the weight keeps the host set-up short
+            th = l / ns * 2 * np.pi
+            ps = rad * (np.cos(th) * ux + np.sin(th) * uy) + c
+            wv = w * (-np.sin(th) * ux + np.cos(th) * uy)
+            d = X - ps
+            rr = np.linalg.norm(d, axis=-1)
+            f = 8 * cl * (-1 / (4 * np.pi * rr ** 3) * (1 - np.exp(-(rr / dl) ** 3)))
+            vc += f[..., None] * np.cross(d, wv)
+    out = []
+    for fam in range(3):
+        a = vc[..., fam]
+        pad = [(0, 0)] * 3
+        pad[fam] = (1, 1)
+        e = np.pad(a, pad, mode="edge")
+        sl_hi = [slice(None)] * 3
+        sl_lo = [slice(None)] * 3
+        sl_hi[fam] = slice(1, None)
+        sl_lo[fam] = slice(0, -1)
+        out.append((0.5 * (e[tuple(sl_hi)] + e[tuple(sl_lo)])).astype(np.float32))
+    return out
+
+
+def cpu_sample(n, ppc_axis, steps=1, tol=1e-6, tol_mode=1):
+    """Seconds per oracle step at n^3 (all host threads)."""
+    import numpy as np
+    import oracle as O
+    from pfm.sim import jittered
+    dx = 1.0 / n
+    u = cpu_ic(n)
+    popts = dict(tol=tol, tol_mode=tol_mode)
+    u = list(O.poisson3(*u, **popts)[:3])
+    seeds = jittered((n, n, n), dx, ppc_axis ** 3, seed=0)
+    sim = O.Sim3D(u, seeds, (n, n, n), dx, CFL=0.5, visualize_dt=0.1, reinit_every=20, reinit_every_grad_m=1,
+                  p2g_threads=O.num_threads(), poisson_opts=popts)
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        sim.step()
+        times.append(time.perf_counter() - t0)
+    return times, O.num_threads(), int(np.int64(seeds.shape[0]))
+
+
+def cpu_baseline_entry(args, n_target):
+    times, cores, P = cpu_sample(args.cpu_res, args.ppc_axis, tol=args.tol, tol_mode=args.tol_mode)
+    scale = (n_target / args.cpu_res) ** 3
+    t = statistics.median(times) * scale
+    return {"value": 1.0 / t, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"one full oracle step at {args.cpu_res}^3 ({P} particles, same workload scaled), "
+                      f"{statistics.median(times):.2f} s, x{scale:.0f} work scale to {n_target}^3"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    n_target = args.res
+    scale = (n_target / args.cpu_res) ** 3
+    times, cores, P = cpu_sample(args.cpu_res, args.ppc_axis, steps=args.warmup + args.steps, tol=args.tol,
+                                 tol_mode=args.tol_mode)
+    timed = times[args.warmup:] if len(times) > args.warmup else times
+    per = statistics.mean(timed) * scale
+    value = 1.0 / per
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"3D {n_target}^3 two-ring leapfrog, {args.ppc_axis ** 3} ppc, plain FP32, "
+                                   f"MGPCG rel tol {args.tol:g}", "res": n_target},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"each step: one full CPU-oracle step at {args.cpu_res}^3 ({P} particles), "
+                                       f"x{scale:.0f} work scale to {n_target}^3"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------------------------------------
+# GPU arm
+# ------------------------------------------------------------------------------------------------
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    popts = dict(tol=args.tol, tol_mode=args.tol_mode, max_iters=400, check_every=4)
+    sim = make_sim(args.res, args.ppc_axis, popts)
+    for _ in range(args.warmup):
+        sim.step()
+    torch.cuda.synchronize()
+
+    timer = PhaseTimer()
+    sim.timer = timer
+    iters_before = len(sim.infos)
+    launches0 = sim.scene.launches
+    clocks = ClockSampler(local)
+    barrier()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    e0.record()
+    for _ in range(args.steps):
+        sim.step()
+    e1.record()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    barrier()
+    launches = sim.scene.launches - launches0
+    sim.timer = None
+    elapsed = e0.elapsed_time(e1) / 1e3
+    if dist is not None:
+        t = torch.tensor([elapsed], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    value = world * args.steps / elapsed
+    phases = timer.summary()
+    infos = sim.infos[iters_before:]
+    mg_iters = [i.iterations for i in infos]
+
+    # roofline of the dominant single-kernel phase: RK4_T_forward (one launch per step)
+    P = sim.P
+    n = args.res
+    F3 = 3 * (n + 1) * n * n
+    peak, peak_kind = measured_peak()
+    rk4_ms = statistics.mean(phases["rk4"])
+    rk4_bytes = P * 96 + F3 * 4  # pos + T read and written (48 B + 48 B / particle) + velocity grid once
+    achieved = rk4_bytes / (rk4_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "k_rk4_T_forward3", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                "bytes_per_launch": rk4_bytes, "ms_per_launch": rk4_ms}
+
+    e2e = None
+    if not args.no_e2e:
+        # through the same C-ABI calls, with the step's grid velocity uploaded from pinned host memory
+        # and the projected result read back every step
+        host_u = [t.cpu().pin_memory() for t in sim.u]
+        out_u = [torch.empty_like(h).pin_memory() for h in host_u]
+        barrier()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(args.steps):
+            for d, h in zip(sim.u, host_u):
+                d.copy_(h, non_blocking=True)
+            sim.step()
+            for h, d in zip(out_u, sim.u):
+                h.copy_(d, non_blocking=True)
+        b.record()
+        torch.cuda.synchronize()
+        e_el = a.elapsed_time(b) / 1e3
+        if dist is not None:
+            t = torch.tensor([e_el], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e_el = float(t.item())
+        gbytes = sum(h.numel() * 4 for h in host_u)
+        e2e = {"value": world * args.steps / e_el, "unit": UNIT, "h2d_bytes_per_step": gbytes,
+               "d2h_bytes_per_step": gbytes}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline_entry(args, n)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3, "wall_s": wall,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded two-ring initial condition and jittered particles)",
+                "config": {"workload": f"3D {n}^3 two-ring leapfrog, {args.ppc_axis ** 3} ppc ({P} particles), "
+                                       f"plain FP32 step, MGPCG tol {args.tol:g} "
+                                       f"({'relative' if args.tol_mode else 'absolute r.r'})",
+                           "res": n, "particles": P, "parallelism": f"replicas x{world}",
+                           "l2": "inputs larger than L2 (particle state %.1f GB)" % (P * 132 / 1e9)},
+                "particle_updates_per_s": value * P,
+                "mgpcg_iters": mg_iters,
+                "phase_ms": {k: statistics.mean(v) for k, v in phases.items()},
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches}
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

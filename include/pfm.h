@@ -90,6 +90,8 @@ const char* pfm_last_error(const pfm_handle* h);
 const char* pfm_status_string(int status);
 /* Number of MGPCG levels the handle uses. */
 int pfm_mg_levels(const pfm_handle* h, int* levels);
+/* Number of kernels launched through this handle since pfm_create (bookkeeping for benchmarks). */
+int pfm_launch_count(const pfm_handle* h, uint64_t* launches);
 
 /* ---- 3D step phases ------------------------------------------------------------------------ */
 
@@ -173,6 +175,27 @@ int pfm2_p2g(pfm_handle* h, const float* imp, const float* pos, const float* C, 
 /* MGPCG_2.Poisson (2D/mgpcg.py:342-347). SYNCHRONIZATION POINT. */
 int pfm2_poisson(pfm_handle* h, float* u_x, float* u_y, float* p_out, const pfm_solve_opts* opts,
                  pfm_solve_stats* stats, void* stream);
+
+/* ---- initial conditions --------------------------------------------------------------------- */
+
+/* add_vortex_ring (3D/init_conditions.py:10-22): adds the Biot-Savart velocity of a ring of
+ * strength w, radius rad and core delta (mollifier 1-exp(-(r/delta)^3)) centred at c in the plane
+ * spanned by unit_x/unit_y, sampled with num_samples points, to the cell-centred vector field
+ * vc [nx][ny][nz][3] (cell centres at (I + 0.5) dx).  c/unit_x/unit_y are host arrays. */
+int pfm3_add_vortex_ring(pfm_handle* h, float w, float rad, float delta, const float c[3],
+                         const float unit_x[3], const float unit_y[3], int num_samples, float* vc,
+                         void* stream);
+/* split_central_vector (3D/taichi_utils.py:87-100, 2D/taichi_utils.py:56-67): face velocity =
+ * average of the two adjacent cell-centred values (clamped at the walls).  vc [cells][dim]. */
+int pfm_split_central_vector(pfm_handle* h, const float* vc, float* u_x, float* u_y, float* u_z,
+                             void* stream);
+
+/* Jittered particle seeding (the BASELINE configs' "uniformly jittered from seed"): each cell
+ * holds ppc_axis^dim particles, one per sub-cell, at (sub-lattice index + U) * dx / ppc_axis with
+ * U from a counter-based splitmix64 hash of (seed, particle index, axis); cell-major order,
+ * last axis fastest.  P must equal ppc_axis^dim * cells.  pos [dim][P].  Bit-identical to
+ * pfm.sim.jittered() on the host. */
+int pfm_seed_jittered(pfm_handle* h, uint64_t seed, int ppc_axis, float* pos, void* stream);
 
 /* ---- the MGPCG solver alone ----------------------------------------------------------------- */
 

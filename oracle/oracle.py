@@ -108,7 +108,7 @@ def update_T3(T_init, T_gm):
 
 
 def p2g3(init_imp, pos, T_gm, T_init, init_C, res, dx, use_apic=True, nthreads=1):
-    nx, ny, nz = res
+    nx, ny, nz = (int(r) for r in res)
     ux = np.zeros((nx + 1, ny, nz), np.float32); uy = np.zeros((nx, ny + 1, nz), np.float32)
     uz = np.zeros((nx, ny, nz + 1), np.float32)
     wx, wy, wz = np.zeros_like(ux), np.zeros_like(uy), np.zeros_like(uz)
@@ -119,6 +119,7 @@ def p2g3(init_imp, pos, T_gm, T_init, init_C, res, dx, use_apic=True, nthreads=1
 
 
 def bin_count3(pos, res, dx):
+    res = tuple(int(r) for r in res)
     count = np.zeros(res, np.int32)
     lib().oracle3_bin_count(_p(f32(pos)), f32(pos).shape[0], res[0], res[1], res[2], _cd(dx),
                             _p(count, np.int32))
@@ -141,7 +142,7 @@ def midpoint3(ux, uy, uz, dx, dt_half):
 
 
 def poisson3(ux, uy, uz, base_level=3, boundary=(2, 2, 2, 2, 2, 2), levels=0, max_iters=400,
-             tol=1e-12, fp64=False):
+             tol=1e-12, fp64=False, tol_mode=0):
     """MGPCG_3.Poisson on copies of (ux, uy, uz). Returns (ux, uy, uz, p, iters, final_rTr)."""
     dt = np.float64 if fp64 else np.float32
     ux, uy, uz = (np.ascontiguousarray(a, dtype=dt).copy() for a in (ux, uy, uz))
@@ -151,7 +152,7 @@ def poisson3(ux, uy, uz, base_level=3, boundary=(2, 2, 2, 2, 2, 2), levels=0, ma
     rtr = ctypes.c_double(0)
     fn = lib().oracle3_poisson_f64 if fp64 else lib().oracle3_poisson_f32
     it = fn(_p(ux, dt), _p(uy, dt), _p(uz, dt), _p(p, dt), _p(N, np.int32), int(base_level),
-            _p(bt, np.int32), int(levels), int(max_iters), _cd(tol), ctypes.byref(rtr))
+            _p(bt, np.int32), int(levels), int(max_iters), _cd(tol), ctypes.byref(rtr), int(tol_mode))
     return ux, uy, uz, p, int(it), rtr.value
 
 
@@ -201,7 +202,7 @@ def update_imp2(imp0, T):
 
 
 def p2g2(imp, pos, C, psi, res, dx, use_apic=True, want_psi=True):
-    nx, ny = res
+    nx, ny = (int(r) for r in res)
     ux = np.zeros((nx + 1, ny), np.float32); uy = np.zeros((nx, ny + 1), np.float32)
     wx, wy = np.zeros_like(ux), np.zeros_like(uy)
     gx = np.zeros((nx + 1, ny, 2), np.float32) if want_psi else None
@@ -223,7 +224,7 @@ def midpoint_family2(fam, ux, uy, dx, dt_half):
 
 
 def poisson2(ux, uy, base_level=3, boundary=(2, 2, 2, 2), levels=0, max_iters=400, tol=1e-12,
-             fp64=False):
+             fp64=False, tol_mode=0):
     dt = np.float64 if fp64 else np.float32
     ux, uy = (np.ascontiguousarray(a, dtype=dt).copy() for a in (ux, uy))
     N = np.array([uy.shape[0], ux.shape[1]], np.int32)
@@ -232,7 +233,7 @@ def poisson2(ux, uy, base_level=3, boundary=(2, 2, 2, 2), levels=0, max_iters=40
     rtr = ctypes.c_double(0)
     fn = lib().oracle2_poisson_f64 if fp64 else lib().oracle2_poisson_f32
     it = fn(_p(ux, dt), _p(uy, dt), _p(p, dt), _p(N, np.int32), int(base_level), _p(bt, np.int32),
-            int(levels), int(max_iters), _cd(tol), ctypes.byref(rtr))
+            int(levels), int(max_iters), _cd(tol), ctypes.byref(rtr), int(tol_mode))
     return ux, uy, p, int(it), rtr.value
 
 
@@ -290,10 +291,11 @@ class Sim3D:
 
     def __init__(self, u, seeds, res, dx, CFL=0.5, visualize_dt=0.1, reinit_every=20,
                  reinit_every_grad_m=1, use_midpoint_vel=True, reinit_particle_pos=True,
-                 use_apic=True, base_level=3, p2g_threads=1):
+                 use_apic=True, base_level=3, p2g_threads=1, poisson_opts=None):
+        self.poisson_opts = dict(poisson_opts or {})
         self.u = [f32(a).copy() for a in u]
         self.seeds = f32(seeds)
-        self.res, self.dx = tuple(res), dx
+        self.res, self.dx = tuple(int(r) for r in res), float(dx)
         self.clock = DtClock(CFL, dx, visualize_dt)
         self.reinit_every, self.grad_m = reinit_every, reinit_every_grad_m
         self.use_midpoint_vel, self.reinit_particle_pos = use_midpoint_vel, reinit_particle_pos
@@ -333,13 +335,13 @@ class Sim3D:
         u_adv = self.u
         if self.use_midpoint_vel:
             mid = midpoint3(*self.u, self.dx, np.float32(0.5 * curr_dt))
-            ux, uy, uz, _, it, _ = poisson3(*mid, base_level=self.base_level)
+            ux, uy, uz, _, it, _ = poisson3(*mid, base_level=self.base_level, **self.poisson_opts)
             self.iters.append(it)
             u_adv = [ux, uy, uz]
         self.pos, self.T_gm = rk4_T_forward3(self.pos, self.T_gm, *u_adv, self.dx, np.float32(curr_dt))
         (ux, uy, uz), _ = p2g3(self.init_imp, self.pos, self.T_gm, self.T_init, self.init_C, self.res,
                                self.dx, self.use_apic, self.p2g_threads)
-        ux, uy, uz, p, it, _ = poisson3(ux, uy, uz, base_level=self.base_level)
+        ux, uy, uz, p, it, _ = poisson3(ux, uy, uz, base_level=self.base_level, **self.poisson_opts)
         self.iters.append(it)
         self.u = [ux, uy, uz]
         self.p = p
@@ -351,10 +353,11 @@ class Sim2D:
 
     def __init__(self, u, seeds, res, dx, CFL=0.5, visualize_dt=0.1, reinit_every=12,
                  reinit_every_grad_m=8, use_midpoint_vel=True, reinit_particle_pos=True,
-                 use_apic=True, base_level=3):
+                 use_apic=True, base_level=3, poisson_opts=None):
+        self.poisson_opts = dict(poisson_opts or {})
         self.u = [f32(a).copy() for a in u]
         self.seeds = f32(seeds)
-        self.res, self.dx = tuple(res), dx
+        self.res, self.dx = tuple(int(r) for r in res), float(dx)
         self.clock = DtClock(CFL, dx, visualize_dt)
         self.reinit_every, self.grad_m = reinit_every, reinit_every_grad_m
         self.use_midpoint_vel, self.reinit_particle_pos = use_midpoint_vel, reinit_particle_pos
@@ -399,7 +402,7 @@ class Sim2D:
         u_adv = self.u
         if self.use_midpoint_vel:
             mids = [midpoint_family2(f, *self.u, self.dx, np.float32(0.5 * curr_dt))[2] for f in range(2)]
-            ux, uy, _, it, _ = poisson2(*mids, base_level=self.base_level)
+            ux, uy, _, it, _ = poisson2(*mids, base_level=self.base_level, **self.poisson_opts)
             self.iters.append(it)
             u_adv = [ux, uy]
         self.pos, self.T_gm = rk4_T_forward2(self.pos, self.T_gm, *u_adv, self.dx, np.float32(curr_dt), 1)
@@ -408,7 +411,7 @@ class Sim2D:
         self.imp = update_imp2(self.init_imp, self.T)
         (ux, uy), _, self.psi_grid = p2g2(self.imp, self.pos, self.C, self.psi, self.res, self.dx,
                                           self.use_apic)
-        ux, uy, p, it, _ = poisson2(ux, uy, base_level=self.base_level)
+        ux, uy, p, it, _ = poisson2(ux, uy, base_level=self.base_level, **self.poisson_opts)
         self.iters.append(it)
         self.u = [ux, uy]
         self.p = p

@@ -422,12 +422,15 @@ struct MG {
 
   // solve(max_iters, eps, tol): mgpcg.py:202-280.  Returns the iteration reported by the
   // reference's print (it at convergence), or -max_iters when it returns without converging.
-  int solve(int max_iters, double eps, double tol, double* final_rTr, double beta_in = 0.0) {
+  // tol_mode 0: the reference's r.r < tol; 1: |r| < tol |r0| with r0 the recentred initial residual.
+  int solve(int max_iters, double eps, double tol, double* final_rTr, int tol_mode = 0, double beta_in = 0.0) {
     bool all_neumann = true;
     for (int d = 0; d < dim; ++d)
       for (int s = 0; s < 2; ++s) all_neumann &= (bt[d][s] == 2);
     R beta = R(beta_in);
     if (all_neumann) recenter(r[0].data());
+    double rTr0 = 0.0;
+    for (size_t q = 0; q < n0; ++q) rTr0 += (double)r[0][q] * (double)r[0][q];
     apply_preconditioner();
     for (size_t q = 0; q < n0; ++q) p[q] = z[0][q] + beta * p[q];  // update_p
     double old_zTr = (double)reduce(z[0].data(), r[0].data());
@@ -440,7 +443,8 @@ struct MG {
       for (size_t q = 0; q < n0; ++q) x[q] += alpha * p[q];
       for (size_t q = 0; q < n0; ++q) r[0][q] -= alpha * Ap[q];
       rTr = (double)reduce(r[0].data(), r[0].data());
-      if (rTr < tol) {
+      bool stop = tol_mode == 0 ? (rTr < tol) : (std::sqrt(rTr) < tol * std::sqrt(rTr0));
+      if (stop) {
         *final_rTr = rTr;
         return it;
       }
@@ -461,7 +465,7 @@ struct MG {
 // 3D: mgpcg.py:359-430.
 template <class R>
 int poisson3(R* ux, R* uy, R* uz, R* p_out, const int* N, int base_level, const int* bt,
-             int levels_override, int max_iters, double tol, double* final_rTr) {
+             int levels_override, int max_iters, double tol, double* final_rTr, int tol_mode) {
   const int nx = N[0], ny = N[1], nz = N[2];
   auto IX = [&](int i, int j, int k) { return ((size_t)i * ny + j) * nz + k; };
   auto IY = [&](int i, int j, int k) { return ((size_t)i * (ny + 1) + j) * nz + k; };
@@ -500,7 +504,7 @@ int poisson3(R* ux, R* uy, R* uz, R* p_out, const int* N, int base_level, const 
         R div = vr - vl + vt - vb + vc - va;
         mg.r[0][mg.idx(0, i, j, k)] = div * R(-1);
       }
-  int it = mg.solve(max_iters, 1e-12, tol, final_rTr);
+  int it = mg.solve(max_iters, 1e-12, tol, final_rTr, tol_mode);
   const R* P = mg.x.data();
   if (p_out) std::memcpy(p_out, P, sizeof(R) * mg.n0);
   auto PI = [&](int i, int j, int k) { return P[((size_t)i * ny + j) * nz + k]; };
@@ -539,7 +543,7 @@ int poisson3(R* ux, R* uy, R* uz, R* p_out, const int* N, int base_level, const 
 // 2D Poisson: 2D/mgpcg.py:293-347
 template <class R>
 int poisson2(R* ux, R* uy, R* p_out, const int* N, int base_level, const int* bt, int levels_override,
-             int max_iters, double tol, double* final_rTr) {
+             int max_iters, double tol, double* final_rTr, int tol_mode) {
   const int nx = N[0], ny = N[1];
   auto IX = [&](int i, int j) { return (size_t)i * ny + j; };
   auto IY = [&](int i, int j) { return (size_t)i * (ny + 1) + j; };
@@ -565,7 +569,7 @@ int poisson2(R* ux, R* uy, R* p_out, const int* N, int base_level, const int* bt
       R div = vr - vl + vt - vb;
       mg.r[0][mg.idx(0, i, j, 0)] = div * R(-1);
     }
-  int it = mg.solve(max_iters, 1e-12, tol, final_rTr);
+  int it = mg.solve(max_iters, 1e-12, tol, final_rTr, tol_mode);
   const R* P = mg.x.data();
   if (p_out) std::memcpy(p_out, P, sizeof(R) * mg.n0);
   auto PI = [&](int i, int j) { return P[(size_t)i * ny + j]; };
@@ -881,13 +885,13 @@ void oracle3_midpoint_family(int fam, const float* ux, const float* uy, const fl
 }
 
 int oracle3_poisson_f32(float* ux, float* uy, float* uz, float* p_out, const int* N, int base_level,
-                        const int* bt, int levels, int max_iters, double tol, double* final_rTr) {
-  return poisson3<float>(ux, uy, uz, p_out, N, base_level, bt, levels, max_iters, tol, final_rTr);
+                        const int* bt, int levels, int max_iters, double tol, double* final_rTr, int tol_mode) {
+  return poisson3<float>(ux, uy, uz, p_out, N, base_level, bt, levels, max_iters, tol, final_rTr, tol_mode);
 }
 
 int oracle3_poisson_f64(double* ux, double* uy, double* uz, double* p_out, const int* N, int base_level,
-                        const int* bt, int levels, int max_iters, double tol, double* final_rTr) {
-  return poisson3<double>(ux, uy, uz, p_out, N, base_level, bt, levels, max_iters, tol, final_rTr);
+                        const int* bt, int levels, int max_iters, double tol, double* final_rTr, int tol_mode) {
+  return poisson3<double>(ux, uy, uz, p_out, N, base_level, bt, levels, max_iters, tol, final_rTr, tol_mode);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -1108,13 +1112,13 @@ void oracle2_midpoint_family(int fam, const float* ux, const float* uy, int nx, 
 }
 
 int oracle2_poisson_f32(float* ux, float* uy, float* p_out, const int* N, int base_level, const int* bt,
-                        int levels, int max_iters, double tol, double* final_rTr) {
-  return poisson2<float>(ux, uy, p_out, N, base_level, bt, levels, max_iters, tol, final_rTr);
+                        int levels, int max_iters, double tol, double* final_rTr, int tol_mode) {
+  return poisson2<float>(ux, uy, p_out, N, base_level, bt, levels, max_iters, tol, final_rTr, tol_mode);
 }
 
 int oracle2_poisson_f64(double* ux, double* uy, double* p_out, const int* N, int base_level, const int* bt,
-                        int levels, int max_iters, double tol, double* final_rTr) {
-  return poisson2<double>(ux, uy, p_out, N, base_level, bt, levels, max_iters, tol, final_rTr);
+                        int levels, int max_iters, double tol, double* final_rTr, int tol_mode) {
+  return poisson2<double>(ux, uy, p_out, N, base_level, bt, levels, max_iters, tol, final_rTr, tol_mode);
 }
 
 }  // extern "C"

@@ -162,6 +162,12 @@ int pfm_set_workspace(pfm_handle* h, void* dptr, size_t bytes) {
   return PFM_OK;
 }
 
+int pfm_launch_count(const pfm_handle* h, uint64_t* launches) {
+  if (!h || !launches) return PFM_ERR_NULL;
+  *launches = h->launches;
+  return PFM_OK;
+}
+
 int pfm_mg_levels(const pfm_handle* h, int* levels) {
   if (!h || !levels) return PFM_ERR_NULL;
   *levels = h->L;

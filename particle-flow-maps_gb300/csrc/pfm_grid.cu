@@ -202,9 +202,9 @@ int max_speed_async(pfm_handle* h, const float* ux, const float* uy, const float
   s = check_cuda(h, cudaMemsetAsync(ticket, 0, sizeof(unsigned), st), "memset ticket");
   if (s) return s;
   if (h->cfg.dim == 3)
-    k_max_speed<3><<<blocks, 256, 0, st>>>(ux, uy, uz, h->geom, part, ticket, out);
+    launch(h, k_max_speed<3>, blocks, 256, 0, st, ux, uy, uz, h->geom, part, ticket, out);
   else
-    k_max_speed<2><<<blocks, 256, 0, st>>>(ux, uy, uz, h->geom, part, ticket, out);
+    launch(h, k_max_speed<2>, blocks, 256, 0, st, ux, uy, uz, h->geom, part, ticket, out);
   return launch_check(h, "k_max_speed");
 }
 
@@ -245,9 +245,9 @@ int pfm3_midpoint(pfm_handle* h, const float* u0_x, const float* u0_y, const flo
     float* to = T_out ? T_out[fam] : nullptr;
     dim3 gr(grid_for(nf, kGThreads));
     cudaStream_t st = (cudaStream_t)stream;
-    if (fam == 0) k_midpoint3<0><<<gr, kGThreads, 0, st>>>(F, h->geom, dt_half, outs[fam], po, to);
-    if (fam == 1) k_midpoint3<1><<<gr, kGThreads, 0, st>>>(F, h->geom, dt_half, outs[fam], po, to);
-    if (fam == 2) k_midpoint3<2><<<gr, kGThreads, 0, st>>>(F, h->geom, dt_half, outs[fam], po, to);
+    if (fam == 0) launch(h, k_midpoint3<0>, gr, kGThreads, 0, st, F, h->geom, dt_half, outs[fam], po, to);
+    if (fam == 1) launch(h, k_midpoint3<1>, gr, kGThreads, 0, st, F, h->geom, dt_half, outs[fam], po, to);
+    if (fam == 2) launch(h, k_midpoint3<2>, gr, kGThreads, 0, st, F, h->geom, dt_half, outs[fam], po, to);
     int s = launch_check(h, "k_midpoint3");
     if (s) return s;
   }
@@ -268,8 +268,8 @@ int pfm2_midpoint(pfm_handle* h, const float* u0_x, const float* u0_y, float* u1
     float* to = T_out ? T_out[fam] : nullptr;
     dim3 gr(grid_for(nf, kGThreads));
     cudaStream_t st = (cudaStream_t)stream;
-    if (fam == 0) k_midpoint2<0><<<gr, kGThreads, 0, st>>>(F, h->geom, dt_half, outs[fam], po, to);
-    if (fam == 1) k_midpoint2<1><<<gr, kGThreads, 0, st>>>(F, h->geom, dt_half, outs[fam], po, to);
+    if (fam == 0) launch(h, k_midpoint2<0>, gr, kGThreads, 0, st, F, h->geom, dt_half, outs[fam], po, to);
+    if (fam == 1) launch(h, k_midpoint2<1>, gr, kGThreads, 0, st, F, h->geom, dt_half, outs[fam], po, to);
     int s = launch_check(h, "k_midpoint2");
     if (s) return s;
   }

@@ -1,0 +1,160 @@
+// Initial-condition kernels used to set up large scenes on the device: the vortex-ring
+// Biot-Savart sum (add_vortex_ring, 3D/init_conditions.py:10-22) and the centre-to-face split
+// (split_central_vector, 3D/taichi_utils.py:87-100; 2D/taichi_utils.py:56-67).
+#include "pfm_internal.cuh"
+
+namespace pfm {
+
+// vf[i,j,k] += sum_l curve_length * (-1/(4 pi r^3) * (1 - exp(-(r/delta)^3))) * (p - p_l) x w_l
+// with p the cell centre (I + 0.5) * dx (center_coords_func, 3D/taichi_utils.py:28-31).
+__global__ void __launch_bounds__(256) k_vortex_ring(float* __restrict__ vc, MacGeom g, float w, float rad,
+                                                     float delta, float3 c, float3 ux, float3 uy, int num_samples) {
+  const int64_t C = (int64_t)g.N[0] * g.N[1] * g.N[2];
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= C) return;
+  int k = (int)(e % g.N[2]);
+  int64_t t = e / g.N[2];
+  int j = (int)(t % g.N[1]);
+  int i = (int)(t / g.N[1]);
+  const float px = ((float)i + 0.5f) * g.dx, py = ((float)j + 0.5f) * g.dx, pz = ((float)k + 0.5f) * g.dx;
+  const float pi = 3.14159265358979323846f;
+  const float curve_length = (2.f * pi * rad) / (float)num_samples;
+  float ax = 0.f, ay = 0.f, az = 0.f;
+  for (int l = 0; l < num_samples; ++l) {
+    float theta = (float)l / (float)num_samples * 2.f * pi;
+    float ct = cosf(theta), st = sinf(theta);
+    float sx = rad * (ct * ux.x + st * uy.x) + c.x;
+    float sy = rad * (ct * ux.y + st * uy.y) + c.y;
+    float sz = rad * (ct * ux.z + st * uy.z) + c.z;
+    float dx = px - sx, dy = py - sy, dz = pz - sz;
+    float r = sqrtf(dx * dx + dy * dy + dz * dz);
+    float wx = w * (-st * ux.x + ct * uy.x), wy = w * (-st * ux.y + ct * uy.y), wz = w * (-st * ux.z + ct * uy.z);
+    float rd = r / delta;
+    float f = curve_length * (-1.f / (4.f * pi * r * r * r) * (1.f - expf(-(rd * rd * rd))));
+    ax += f * (dy * wz - dz * wy);
+    ay += f * (dz * wx - dx * wz);
+    az += f * (dx * wy - dy * wx);
+  }
+  vc[e * 3 + 0] += ax;
+  vc[e * 3 + 1] += ay;
+  vc[e * 3 + 2] += az;
+}
+
+// split_central_vector: face = 0.5 * (sample(vc, I) + sample(vc, I - e_fam)) with clamped samples
+template <int D>
+__global__ void __launch_bounds__(256) k_split_central(const float* __restrict__ vc, MacGeom g, int fam,
+                                                       float* __restrict__ out) {
+  const int n0 = g.n[fam][0], n1 = g.n[fam][1], n2 = g.n[fam][2];
+  const int64_t nf = (int64_t)n0 * n1 * n2;
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nf) return;
+  int idx[3];
+  idx[2] = (int)(e % n2);
+  int64_t t = e / n2;
+  idx[1] = (int)(t % n1);
+  idx[0] = (int)(t / n1);
+  int a[3] = {idx[0], idx[1], idx[2]}, b[3] = {idx[0], idx[1], idx[2]};
+  b[fam] -= 1;
+  for (int d = 0; d < 3; ++d) {
+    a[d] = a[d] < 0 ? 0 : (a[d] > g.N[d] - 1 ? g.N[d] - 1 : a[d]);
+    b[d] = b[d] < 0 ? 0 : (b[d] > g.N[d] - 1 ? g.N[d] - 1 : b[d]);
+  }
+  const int64_t ea = ((int64_t)a[0] * g.N[1] + a[1]) * g.N[2] + a[2];
+  const int64_t eb = ((int64_t)b[0] * g.N[1] + b[1]) * g.N[2] + b[2];
+  out[e] = 0.5f * (vc[ea * D + fam] + vc[eb * D + fam]);
+}
+
+// Counter-based uniform in [0, 1) with 24 random bits (splitmix64 finaliser of seed and index).
+__device__ __forceinline__ float hash_uniform(uint64_t seed, uint64_t n) {
+  uint64_t z = seed * 0xD1B54A32D192ED03ull + n + 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z = z ^ (z >> 31);
+  return (float)(z >> 40) * (1.0f / 16777216.0f);
+}
+
+// Stratified jittered seeding: particle q of cell c (cell-major, last axis fastest) sits in
+// sub-cell s = q % ppc of a ppc_axis^D lattice, at (lattice index + U) * dx / ppc_axis.
+template <int D>
+__global__ void __launch_bounds__(256) k_seed_jittered(float* __restrict__ pos, int64_t P, MacGeom g, uint64_t seed,
+                                                       int axis, float h_sub) {
+  int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= P) return;
+  int ppc = axis * axis * (D == 3 ? axis : 1);
+  int64_t cell = q / ppc;
+  int sub = (int)(q % ppc);
+  int ci[3], si[3];
+  if (D == 3) {
+    ci[2] = (int)(cell % g.N[2]);
+    int64_t t = cell / g.N[2];
+    ci[1] = (int)(t % g.N[1]);
+    ci[0] = (int)(t / g.N[1]);
+    si[2] = sub % axis;
+    si[1] = (sub / axis) % axis;
+    si[0] = sub / (axis * axis);
+  } else {
+    ci[1] = (int)(cell % g.N[1]);
+    ci[0] = (int)(cell / g.N[1]);
+    si[1] = sub % axis;
+    si[0] = sub / axis;
+  }
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    float lat = (float)(ci[d] * axis + si[d]);
+    float u = hash_uniform(seed, (uint64_t)q * D + d);
+    pos[d * P + q] = __fmul_rn(__fadd_rn(lat, u), h_sub);
+  }
+}
+
+}  // namespace pfm
+
+using namespace pfm;
+
+extern "C" {
+
+int pfm3_add_vortex_ring(pfm_handle* h, float w, float rad, float delta, const float c[3], const float unit_x[3],
+                         const float unit_y[3], int num_samples, float* vc, void* stream) {
+  if (!h) return PFM_ERR_NULL;
+  if (h->cfg.dim != 3) return set_error(h, PFM_ERR_SHAPE, "pfm3_add_vortex_ring on a 2D handle");
+  if (!c || !unit_x || !unit_y || !vc) return set_error(h, PFM_ERR_NULL, "pfm3_add_vortex_ring: null input");
+  if (num_samples < 1) return set_error(h, PFM_ERR_ARG, "pfm3_add_vortex_ring: num_samples < 1");
+  launch(h, k_vortex_ring, grid_for(h->cells, 256), 256, 0, (cudaStream_t)stream, vc, h->geom, w, rad, delta,
+         make_float3(c[0], c[1], c[2]), make_float3(unit_x[0], unit_x[1], unit_x[2]),
+         make_float3(unit_y[0], unit_y[1], unit_y[2]), num_samples);
+  return launch_check(h, "k_vortex_ring");
+}
+
+int pfm_split_central_vector(pfm_handle* h, const float* vc, float* u_x, float* u_y, float* u_z, void* stream) {
+  if (!h) return PFM_ERR_NULL;
+  const int D = h->cfg.dim;
+  if (!vc || !u_x || !u_y || (D == 3 && !u_z)) return set_error(h, PFM_ERR_NULL, "pfm_split_central_vector: null");
+  float* outs[3] = {u_x, u_y, u_z};
+  for (int f = 0; f < D; ++f) {
+    int64_t nf = (int64_t)h->geom.n[f][0] * h->geom.n[f][1] * h->geom.n[f][2];
+    if (D == 3)
+      launch(h, k_split_central<3>, grid_for(nf, 256), 256, 0, (cudaStream_t)stream, vc, h->geom, f, outs[f]);
+    else
+      launch(h, k_split_central<2>, grid_for(nf, 256), 256, 0, (cudaStream_t)stream, vc, h->geom, f, outs[f]);
+  }
+  return launch_check(h, "k_split_central");
+}
+
+int pfm_seed_jittered(pfm_handle* h, uint64_t seed, int ppc_axis, float* pos, void* stream) {
+  if (!h) return PFM_ERR_NULL;
+  if (!pos && h->P > 0) return set_error(h, PFM_ERR_NULL, "pfm_seed_jittered: null pos");
+  if (ppc_axis < 1) return set_error(h, PFM_ERR_ARG, "pfm_seed_jittered: ppc_axis < 1");
+  const int D = h->cfg.dim;
+  int64_t ppc = (int64_t)ppc_axis * ppc_axis * (D == 3 ? ppc_axis : 1);
+  if (h->P != ppc * h->cells) return set_error(h, PFM_ERR_SHAPE, "pfm_seed_jittered: particles != ppc * cells");
+  if (h->P == 0) return PFM_OK;
+  const float h_sub = (float)(h->cfg.dx / ppc_axis);
+  if (D == 3)
+    launch(h, k_seed_jittered<3>, grid_for(h->P, 256), 256, 0, (cudaStream_t)stream, pos, h->P, h->geom, seed,
+           ppc_axis, h_sub);
+  else
+    launch(h, k_seed_jittered<2>, grid_for(h->P, 256), 256, 0, (cudaStream_t)stream, pos, h->P, h->geom, seed,
+           ppc_axis, h_sub);
+  return launch_check(h, "k_seed_jittered");
+}
+
+}  // extern "C"

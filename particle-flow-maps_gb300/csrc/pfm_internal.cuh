@@ -71,6 +71,8 @@ struct pfm_handle {
   size_t o_x, o_p, o_Ap, o_partials, o_state, o_maxpart;
   // pinned host mirror of the solve state
   pfm::SolveState* h_state;
+  // kernels launched through this handle (reported by pfm_launch_count)
+  uint64_t launches;
   std::string err;
 };
 
@@ -83,6 +85,14 @@ int require_ws(pfm_handle* h);
 template <class T>
 inline T* ws_ptr(pfm_handle* h, size_t off) {
   return reinterpret_cast<T*>(h->ws + off);
+}
+
+// Launches `kernel` and counts it on the handle.
+template <typename... KArgs, typename... Args>
+inline void launch(pfm_handle* h, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                   Args... args) {
+  kernel<<<grid, block, smem, st>>>(args...);
+  h->launches++;
 }
 
 inline unsigned grid_for(int64_t n, int threads) {

@@ -411,7 +411,7 @@ static void smooth_launch(pfm_handle* h, int l, int phase, const SolveState* st,
   Lvl L = lvl_of(h, l);
   const int nl = (D == 3) ? L.n2 : L.n1;
   int64_t npairs = (D == 3) ? (int64_t)L.n0 * L.n1 * ((nl + 1) / 2) : (int64_t)L.n0 * ((nl + 1) / 2);
-  k_smooth<D><<<grid_for(npairs, 256), 256, 0, s>>>(ws_ptr<float>(h, h->o_z[l]), ws_ptr<float>(h, h->o_r[l]), L,
+  launch(h, k_smooth<D>, grid_for(npairs, 256), 256, 0, s, ws_ptr<float>(h, h->o_z[l]), ws_ptr<float>(h, h->o_r[l]), L,
                                                    bc_of(h), phase, st);
 }
 
@@ -420,15 +420,15 @@ template <int D>
 static void vcycle(pfm_handle* h, const SolveState* st, cudaStream_t s) {
   const int L = h->L;
   const BC bc = bc_of(h);
-  k_zero<<<stream_blocks(h->lv[0].count), 256, 0, s>>>(ws_ptr<float>(h, h->o_z[0]), h->lv[0].count, st);
+  launch(h, k_zero, stream_blocks(h->lv[0].count), 256, 0, s, ws_ptr<float>(h, h->o_z[0]), h->lv[0].count, st);
   for (int l = 0; l < L - 1; ++l) {
     for (int i = 0; i < h->cfg.pre_post_smoothing; ++i) {
       smooth_launch<D>(h, l, 0, st, s);
       smooth_launch<D>(h, l, 1, st, s);
     }
-    k_zero<<<stream_blocks(h->lv[l + 1].count), 256, 0, s>>>(ws_ptr<float>(h, h->o_z[l + 1]), h->lv[l + 1].count, st);
+    launch(h, k_zero, stream_blocks(h->lv[l + 1].count), 256, 0, s, ws_ptr<float>(h, h->o_z[l + 1]), h->lv[l + 1].count, st);
     Lvl Lf = lvl_of(h, l), Lc = lvl_of(h, l + 1);
-    k_restrict<D><<<grid_for(Lc.count, 256), 256, 0, s>>>(ws_ptr<float>(h, h->o_z[l]), ws_ptr<float>(h, h->o_r[l]),
+    launch(h, k_restrict<D>, grid_for(Lc.count, 256), 256, 0, s, ws_ptr<float>(h, h->o_z[l]), ws_ptr<float>(h, h->o_r[l]),
                                                           Lf, ws_ptr<float>(h, h->o_r[l + 1]), Lc, bc, st);
   }
   for (int i = 0; i < h->cfg.bottom_smoothing; ++i) {
@@ -437,7 +437,7 @@ static void vcycle(pfm_handle* h, const SolveState* st, cudaStream_t s) {
   }
   for (int l = L - 2; l >= 0; --l) {
     Lvl Lf = lvl_of(h, l), Lc = lvl_of(h, l + 1);
-    k_prolong<D><<<grid_for(Lf.count, 256), 256, 0, s>>>(ws_ptr<float>(h, h->o_z[l]), Lf,
+    launch(h, k_prolong<D>, grid_for(Lf.count, 256), 256, 0, s, ws_ptr<float>(h, h->o_z[l]), Lf,
                                                          ws_ptr<float>(h, h->o_z[l + 1]), Lc, st);
     for (int i = 0; i < h->cfg.pre_post_smoothing; ++i) {
       smooth_launch<D>(h, l, 1, st, s);
@@ -475,13 +475,13 @@ static int solve_impl(pfm_handle* h, float* x, const pfm_solve_opts* opts, pfm_s
   cudaMemsetAsync(Ap, 0, n * 4, s);
   const bool neu = all_neumann(h);
   if (neu) {
-    k_dot<<<red_blocks(n), kReduceThreads, 0, s>>>(r0, nullptr, n, rb, RED_MEAN, o.eps, inv_n);
-    k_sub_mean<<<stream_blocks(n), 256, 0, s>>>(r0, n, st);
+    launch(h, k_dot, red_blocks(n), kReduceThreads, 0, s, r0, nullptr, n, rb, RED_MEAN, o.eps, inv_n);
+    launch(h, k_sub_mean, stream_blocks(n), 256, 0, s, r0, n, st);
   }
-  k_dot<<<red_blocks(n), kReduceThreads, 0, s>>>(r0, r0, n, rb, RED_RTR0, o.eps, inv_n);
+  launch(h, k_dot, red_blocks(n), kReduceThreads, 0, s, r0, r0, n, rb, RED_RTR0, o.eps, inv_n);
   vcycle<D>(h, st, s);
-  k_update_p<<<stream_blocks(n), 256, 0, s>>>(p, z0, n, st);  // beta = 0 in the state
-  k_dot<<<red_blocks(n), kReduceThreads, 0, s>>>(z0, r0, n, rb, RED_ZTR_INIT, o.eps, inv_n);
+  launch(h, k_update_p, stream_blocks(n), 256, 0, s, p, z0, n, st);  // beta = 0 in the state
+  launch(h, k_dot, red_blocks(n), kReduceThreads, 0, s, z0, r0, n, rb, RED_ZTR_INIT, o.eps, inv_n);
   rc = launch_check(h, "mgpcg setup");
   if (rc) return rc;
   int enq = 0;
@@ -490,15 +490,15 @@ static int solve_impl(pfm_handle* h, float* x, const pfm_solve_opts* opts, pfm_s
     int chunk = o.check_every;
     if (o.max_iters >= 0 && enq + chunk > o.max_iters) chunk = o.max_iters - enq;
     for (int c = 0; c < chunk; ++c) {
-      k_Ap_dot<D><<<red_blocks(n), kReduceThreads, 0, s>>>(p, Ap, L0, bc, rb, o.eps);
-      k_update_xr<<<red_blocks(n), kReduceThreads, 0, s>>>(x, p, r0, Ap, n, rb, o.tol, o.tol_mode);
+      launch(h, k_Ap_dot<D>, red_blocks(n), kReduceThreads, 0, s, p, Ap, L0, bc, rb, o.eps);
+      launch(h, k_update_xr, red_blocks(n), kReduceThreads, 0, s, x, p, r0, Ap, n, rb, o.tol, o.tol_mode);
       if (neu) {
-        k_dot<<<red_blocks(n), kReduceThreads, 0, s>>>(r0, nullptr, n, rb, RED_MEAN, o.eps, inv_n);
-        k_sub_mean<<<stream_blocks(n), 256, 0, s>>>(r0, n, st);
+        launch(h, k_dot, red_blocks(n), kReduceThreads, 0, s, r0, nullptr, n, rb, RED_MEAN, o.eps, inv_n);
+        launch(h, k_sub_mean, stream_blocks(n), 256, 0, s, r0, n, st);
       }
       vcycle<D>(h, st, s);
-      k_dot<<<red_blocks(n), kReduceThreads, 0, s>>>(z0, r0, n, rb, RED_ZTR, o.eps, inv_n);
-      k_update_p<<<stream_blocks(n), 256, 0, s>>>(p, z0, n, st);
+      launch(h, k_dot, red_blocks(n), kReduceThreads, 0, s, z0, r0, n, rb, RED_ZTR, o.eps, inv_n);
+      launch(h, k_update_p, stream_blocks(n), 256, 0, s, p, z0, n, st);
     }
     enq += chunk;
     rc = launch_check(h, "mgpcg iteration");
@@ -535,11 +535,11 @@ static int poisson_impl(pfm_handle* h, float* const* u, float* p_out, const pfm_
   for (int f = 0; f < D; ++f) {
     int a1 = (f == 0) ? 1 : 0, a2 = (f == 2) ? 1 : 2;
     int64_t plane = (int64_t)g.n[f][a1] * (D == 3 ? g.n[f][a2] : 1);
-    k_apply_bc<D><<<grid_for(2 * plane, 256), 256, 0, s>>>(u[f], f, g, h->cfg.boundary[f][0] == 2,
+    launch(h, k_apply_bc<D>, grid_for(2 * plane, 256), 256, 0, s, u[f], f, g, h->cfg.boundary[f][0] == 2,
                                                           h->cfg.boundary[f][1] == 2);
   }
   float* r0 = ws_ptr<float>(h, h->o_r[0]);
-  k_divergence<D><<<grid_for(h->cells, 256), 256, 0, s>>>(u[0], u[1], D == 3 ? u[2] : nullptr, g, r0);
+  launch(h, k_divergence<D>, grid_for(h->cells, 256), 256, 0, s, u[0], u[1], D == 3 ? u[2] : nullptr, g, r0);
   rc = launch_check(h, "divergence");
   if (rc) return rc;
   float* x = p_out ? p_out : ws_ptr<float>(h, h->o_x);
@@ -547,7 +547,7 @@ static int poisson_impl(pfm_handle* h, float* const* u, float* p_out, const pfm_
   if (solve_rc != PFM_OK && solve_rc != PFM_ERR_NOT_CONVERGED) return solve_rc;
   for (int f = 0; f < D; ++f) {
     int64_t nf = (int64_t)g.n[f][0] * g.n[f][1] * g.n[f][2];
-    k_subtract_grad_p<D><<<grid_for(nf, 256), 256, 0, s>>>(u[f], f, x, g, h->cfg.boundary[f][0] == 2,
+    launch(h, k_subtract_grad_p<D>, grid_for(nf, 256), 256, 0, s, u[f], f, x, g, h->cfg.boundary[f][0] == 2,
                                                           h->cfg.boundary[f][1] == 2);
   }
   rc = launch_check(h, "subtract_grad_p");
@@ -588,7 +588,7 @@ int pfm_mgpcg_solve(pfm_handle* h, const float* div, float* x_out, const pfm_sol
   cudaStream_t s = (cudaStream_t)stream;
   float* r0 = ws_ptr<float>(h, h->o_r[0]);
   // init(div, -1): r0 = -div (3D/mgpcg.py:71-79)
-  k_negate<<<stream_blocks(h->cells), 256, 0, s>>>(r0, div, h->cells);
+  launch(h, k_negate, stream_blocks(h->cells), 256, 0, s, r0, div, h->cells);
   rc = launch_check(h, "k_negate");
   if (rc) return rc;
   return mgpcg_solve_in_place(h, x_out, opts, stats, s);

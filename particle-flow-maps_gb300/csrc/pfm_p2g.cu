@@ -327,19 +327,19 @@ int sort_particles(pfm_handle* h, const float* pos, cudaStream_t st) {
   if (rc) return rc;
   if (P > 0) {
     if (h->cfg.dim == 3)
-      k_bin_keys<3><<<grid_for(P, kBinThreads), kBinThreads, 0, st>>>(pos, P, h->geom, key, slot, count);
+      launch(h, k_bin_keys<3>, grid_for(P, kBinThreads), kBinThreads, 0, st, pos, P, h->geom, key, slot, count);
     else
-      k_bin_keys<2><<<grid_for(P, kBinThreads), kBinThreads, 0, st>>>(pos, P, h->geom, key, slot, count);
+      launch(h, k_bin_keys<2>, grid_for(P, kBinThreads), kBinThreads, 0, st, pos, P, h->geom, key, slot, count);
   }
   const int64_t per_block = (int64_t)kScanThreads * kScanItems;
   const int nb = (int)((C + per_block - 1) / per_block);
   if (nb > kScanThreads * kScanItems) return set_error(h, PFM_ERR_SHAPE, "too many cells for the bin scan");
-  k_scan_blocksums<<<nb, kScanThreads, 0, st>>>(count, C, bsum);
-  k_scan_top<<<1, kScanThreads, 0, st>>>(bsum, nb);
-  k_scan_apply<<<nb, kScanThreads, 0, st>>>(count, C, bsum, start, (int)P);
+  launch(h, k_scan_blocksums, nb, kScanThreads, 0, st, count, C, bsum);
+  launch(h, k_scan_top, 1, kScanThreads, 0, st, bsum, nb);
+  launch(h, k_scan_apply, nb, kScanThreads, 0, st, count, C, bsum, start, (int)P);
   if (P > 0) {
-    k_scatter_order<<<grid_for(P, kBinThreads), kBinThreads, 0, st>>>(key, slot, start, P, order);
-    k_cell_sort<<<grid_for(C, kBinThreads), kBinThreads, 0, st>>>(start, C, order);
+    launch(h, k_scatter_order, grid_for(P, kBinThreads), kBinThreads, 0, st, key, slot, start, P, order);
+    launch(h, k_cell_sort, grid_for(C, kBinThreads), kBinThreads, 0, st, start, C, order);
   }
   return launch_check(h, "sort_particles");
 }
@@ -395,16 +395,16 @@ int pfm3_p2g(pfm_handle* h, const float* init_imp, const float* pos, const float
   if (rc) return rc;
   float4* pay = ws_ptr<float4>(h, h->o_payload);
   if (h->P > 0)
-    k_payload3<<<grid_for(h->P, kBinThreads), kBinThreads, 0, st>>>(ws_ptr<int>(h, h->o_order), h->P, h->geom, pos,
+    launch(h, k_payload3, grid_for(h->P, kBinThreads), kBinThreads, 0, st, ws_ptr<int>(h, h->o_order), h->P, h->geom, pos,
                                                                     init_imp, T_gm, T_init, init_C, pay);
   float* us[3] = {u_x, u_y, u_z};
   float* ws[3] = {w_x, w_y, w_z};
   for (int f = 0; f < 3; ++f) {
     int64_t nf = (int64_t)h->geom.n[f][0] * h->geom.n[f][1] * h->geom.n[f][2];
     const int* start = ws_ptr<int>(h, h->o_start);
-    if (f == 0) k_gather3<0><<<grid_for(nf, 128), 128, 0, st>>>(pay, start, h->geom, h->cfg.use_apic, us[f], ws[f]);
-    if (f == 1) k_gather3<1><<<grid_for(nf, 128), 128, 0, st>>>(pay, start, h->geom, h->cfg.use_apic, us[f], ws[f]);
-    if (f == 2) k_gather3<2><<<grid_for(nf, 128), 128, 0, st>>>(pay, start, h->geom, h->cfg.use_apic, us[f], ws[f]);
+    if (f == 0) launch(h, k_gather3<0>, grid_for(nf, 128), 128, 0, st, pay, start, h->geom, h->cfg.use_apic, us[f], ws[f]);
+    if (f == 1) launch(h, k_gather3<1>, grid_for(nf, 128), 128, 0, st, pay, start, h->geom, h->cfg.use_apic, us[f], ws[f]);
+    if (f == 2) launch(h, k_gather3<2>, grid_for(nf, 128), 128, 0, st, pay, start, h->geom, h->cfg.use_apic, us[f], ws[f]);
   }
   return launch_check(h, "pfm3_p2g");
 }
@@ -421,7 +421,7 @@ int pfm2_p2g(pfm_handle* h, const float* imp, const float* pos, const float* C, 
   if (rc) return rc;
   float4* pay = ws_ptr<float4>(h, h->o_payload);
   if (h->P > 0)
-    k_payload2<<<grid_for(h->P, kBinThreads), kBinThreads, 0, st>>>(ws_ptr<int>(h, h->o_order), h->P, h->geom, pos,
+    launch(h, k_payload2, grid_for(h->P, kBinThreads), kBinThreads, 0, st, ws_ptr<int>(h, h->o_order), h->P, h->geom, pos,
                                                                     imp, C, psi, pay);
   float* us[2] = {u_x, u_y};
   float* ws[2] = {w_x, w_y};
@@ -429,8 +429,8 @@ int pfm2_p2g(pfm_handle* h, const float* imp, const float* pos, const float* C, 
   for (int f = 0; f < 2; ++f) {
     int64_t nf = (int64_t)h->geom.n[f][0] * h->geom.n[f][1];
     const int* start = ws_ptr<int>(h, h->o_start);
-    if (f == 0) k_gather2<0><<<grid_for(nf, 128), 128, 0, st>>>(pay, start, h->geom, h->cfg.use_apic, us[f], ws[f], ps[f]);
-    if (f == 1) k_gather2<1><<<grid_for(nf, 128), 128, 0, st>>>(pay, start, h->geom, h->cfg.use_apic, us[f], ws[f], ps[f]);
+    if (f == 0) launch(h, k_gather2<0>, grid_for(nf, 128), 128, 0, st, pay, start, h->geom, h->cfg.use_apic, us[f], ws[f], ps[f]);
+    if (f == 1) launch(h, k_gather2<1>, grid_for(nf, 128), 128, 0, st, pay, start, h->geom, h->cfg.use_apic, us[f], ws[f], ps[f]);
   }
   return launch_check(h, "pfm2_p2g");
 }

@@ -276,7 +276,7 @@ int pfm3_g2p(pfm_handle* h, const float* pos, const float* u_x, const float* u_y
   if (!pos || !u_x || !u_y || !u_z) return set_error(h, PFM_ERR_NULL, "pfm3_g2p: null input");
   if (h->P == 0 || (!imp_out && !C_out)) return PFM_OK;
   MacFields3 F{{u_x, u_y, u_z}};
-  k_g2p3<<<grid_for(h->P, kPThreads), kPThreads, 0, (cudaStream_t)stream>>>(pos, h->P, F, h->geom, imp_out, C_out);
+  launch(h, k_g2p3, grid_for(h->P, kPThreads), kPThreads, 0, (cudaStream_t)stream, pos, h->P, F, h->geom, imp_out, C_out);
   return launch_check(h, "k_g2p3");
 }
 
@@ -285,7 +285,7 @@ int pfm3_update_T(pfm_handle* h, float* T_init, float* T_gm, int reset_gm, void*
   if (s) return s;
   if (!T_init || !T_gm) return set_error(h, PFM_ERR_NULL, "pfm3_update_T: null input");
   if (h->P == 0) return PFM_OK;
-  k_update_T3<<<grid_for(h->P, 256), 256, 0, (cudaStream_t)stream>>>(T_init, T_gm, h->P, reset_gm);
+  launch(h, k_update_T3, grid_for(h->P, 256), 256, 0, (cudaStream_t)stream, T_init, T_gm, h->P, reset_gm);
   return launch_check(h, "k_update_T3");
 }
 
@@ -294,7 +294,7 @@ int pfm3_reset_T(pfm_handle* h, float* T, void* stream) {
   if (s) return s;
   if (!T) return set_error(h, PFM_ERR_NULL, "pfm3_reset_T: null input");
   if (h->P == 0) return PFM_OK;
-  k_reset_T<3><<<grid_for(h->P, 256), 256, 0, (cudaStream_t)stream>>>(T, h->P);
+  launch(h, k_reset_T<3>, grid_for(h->P, 256), 256, 0, (cudaStream_t)stream, T, h->P);
   return launch_check(h, "k_reset_T<3>");
 }
 
@@ -305,7 +305,7 @@ int pfm3_rk4_T_forward(pfm_handle* h, float* pos, float* T, const float* u_x, co
   if (!pos || !T || !u_x || !u_y || !u_z) return set_error(h, PFM_ERR_NULL, "pfm3_rk4_T_forward: null input");
   if (h->P == 0) return PFM_OK;
   MacFields3 F{{u_x, u_y, u_z}};
-  k_rk4_T_forward3<<<grid_for(h->P, kPThreads), kPThreads, 0, (cudaStream_t)stream>>>(pos, T, h->P, F, h->geom, dt);
+  launch(h, k_rk4_T_forward3, grid_for(h->P, kPThreads), kPThreads, 0, (cudaStream_t)stream, pos, T, h->P, F, h->geom, dt);
   return launch_check(h, "k_rk4_T_forward3");
 }
 
@@ -316,7 +316,7 @@ int pfm2_g2p(pfm_handle* h, const float* pos, const float* u_x, const float* u_y
   if (!pos || !u_x || !u_y) return set_error(h, PFM_ERR_NULL, "pfm2_g2p: null input");
   if (h->P == 0 || (!imp_out && !C_out)) return PFM_OK;
   MacFields2 F{{u_x, u_y}};
-  k_g2p2<<<grid_for(h->P, kPThreads), kPThreads, 0, (cudaStream_t)stream>>>(pos, h->P, F, h->geom, imp_out, C_out);
+  launch(h, k_g2p2, grid_for(h->P, kPThreads), kPThreads, 0, (cudaStream_t)stream, pos, h->P, F, h->geom, imp_out, C_out);
   return launch_check(h, "k_g2p2");
 }
 
@@ -327,7 +327,7 @@ int pfm2_rk4_T_forward(pfm_handle* h, float* pos, float* T, const float* u_x, co
   if (!pos || !T || !u_x || !u_y) return set_error(h, PFM_ERR_NULL, "pfm2_rk4_T_forward: null input");
   if (h->P == 0) return PFM_OK;
   MacFields2 F{{u_x, u_y}};
-  k_rk4_T_forward2<<<grid_for(h->P, kPThreads), kPThreads, 0, (cudaStream_t)stream>>>(pos, T, h->P, F, h->geom,
+  launch(h, k_rk4_T_forward2, grid_for(h->P, kPThreads), kPThreads, 0, (cudaStream_t)stream, pos, T, h->P, F, h->geom,
                                                                                        dt, advect_psi);
   return launch_check(h, "k_rk4_T_forward2");
 }
@@ -337,7 +337,7 @@ int pfm2_update_grad_m(pfm_handle* h, float* C, const float* init_C, const float
   if (s) return s;
   if (!C || !init_C || !T_gm) return set_error(h, PFM_ERR_NULL, "pfm2_update_grad_m: null input");
   if (h->P == 0) return PFM_OK;
-  k_update_grad_m2<<<grid_for(h->P, 256), 256, 0, (cudaStream_t)stream>>>(C, init_C, T_gm, h->P);
+  launch(h, k_update_grad_m2, grid_for(h->P, 256), 256, 0, (cudaStream_t)stream, C, init_C, T_gm, h->P);
   return launch_check(h, "k_update_grad_m2");
 }
 
@@ -346,7 +346,7 @@ int pfm2_update_T(pfm_handle* h, float* T, const float* T_init, const float* T_g
   if (s) return s;
   if (!T || !T_init || !T_gm) return set_error(h, PFM_ERR_NULL, "pfm2_update_T: null input");
   if (h->P == 0) return PFM_OK;
-  k_update_T2<<<grid_for(h->P, 256), 256, 0, (cudaStream_t)stream>>>(T, T_init, T_gm, h->P);
+  launch(h, k_update_T2, grid_for(h->P, 256), 256, 0, (cudaStream_t)stream, T, T_init, T_gm, h->P);
   return launch_check(h, "k_update_T2");
 }
 
@@ -355,7 +355,7 @@ int pfm2_update_imp(pfm_handle* h, float* imp, const float* init_imp, const floa
   if (s) return s;
   if (!imp || !init_imp || !T) return set_error(h, PFM_ERR_NULL, "pfm2_update_imp: null input");
   if (h->P == 0) return PFM_OK;
-  k_update_imp2<<<grid_for(h->P, 256), 256, 0, (cudaStream_t)stream>>>(imp, init_imp, T, h->P);
+  launch(h, k_update_imp2, grid_for(h->P, 256), 256, 0, (cudaStream_t)stream, imp, init_imp, T, h->P);
   return launch_check(h, "k_update_imp2");
 }
 
@@ -364,7 +364,7 @@ int pfm2_reset_T(pfm_handle* h, float* T, void* stream) {
   if (s) return s;
   if (!T) return set_error(h, PFM_ERR_NULL, "pfm2_reset_T: null input");
   if (h->P == 0) return PFM_OK;
-  k_reset_T<2><<<grid_for(h->P, 256), 256, 0, (cudaStream_t)stream>>>(T, h->P);
+  launch(h, k_reset_T<2>, grid_for(h->P, 256), 256, 0, (cudaStream_t)stream, T, h->P);
   return launch_check(h, "k_reset_T<2>");
 }
 

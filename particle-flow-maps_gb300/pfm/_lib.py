@@ -49,6 +49,10 @@ SIGNATURES = {
     "pfm_last_error": [_P],
     "pfm_status_string": [_I],
     "pfm_mg_levels": [_P, ctypes.POINTER(_I)],
+    "pfm_launch_count": [_P, ctypes.POINTER(ctypes.c_uint64)],
+    "pfm3_add_vortex_ring": [_P, _F, _F, _F, ctypes.POINTER(_F), ctypes.POINTER(_F), ctypes.POINTER(_F), _I, _P, _P],
+    "pfm_split_central_vector": [_P, _P, _P, _P, _P, _P],
+    "pfm_seed_jittered": [_P, ctypes.c_uint64, _I, _P, _P],
     "pfm3_calc_max_speed": [_P, _P, _P, _P, _P, _P],
     "pfm3_g2p": [_P, _P, _P, _P, _P, _P, _P, _P],
     "pfm3_update_T": [_P, _P, _P, _I, _P],

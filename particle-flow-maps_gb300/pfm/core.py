@@ -289,6 +289,38 @@ class Scene:
                          allow=allow)
         return SolveInfo(s, st)
 
+    # ------------------------------------------------------------------------------------------
+    # set-up helpers (initial conditions, seeding) and bookkeeping
+    # ------------------------------------------------------------------------------------------
+    def add_vortex_ring(self, vc, w, rad, delta, c, unit_x, unit_y, num_samples):
+        """add_vortex_ring (3D/init_conditions.py:10-22) into the cell-centred field vc [*res, 3]."""
+        self._dev(vc, "vc")
+        if tuple(vc.shape) != self.cell_shape + (3,):
+            raise PfmError(2, "vc must be [nx, ny, nz, 3]")
+        f3 = ctypes.c_float * 3
+        self._check(self.lib.pfm3_add_vortex_ring(self.h, ctypes.c_float(w), ctypes.c_float(rad), ctypes.c_float(delta),
+                                                  f3(*c), f3(*unit_x), f3(*unit_y), int(num_samples), _ptr(vc),
+                                                  self._stream()))
+
+    def split_central_vector(self, vc, u):
+        """split_central_vector (3D/taichi_utils.py:87-100): cell-centred vc -> face grids u."""
+        self._dev(vc, "vc")
+        u = self._grids(u)
+        uz = u[2] if self.dim == 3 else None
+        self._check(self.lib.pfm_split_central_vector(self.h, _ptr(vc), _ptr(u[0]), _ptr(u[1]), _ptr(uz),
+                                                      self._stream()))
+
+    def seed_jittered(self, pos, seed, ppc_axis):
+        """Device twin of pfm.sim.jittered (bit-identical)."""
+        self._part(pos, self.dim, "pos")
+        self._check(self.lib.pfm_seed_jittered(self.h, ctypes.c_uint64(seed), int(ppc_axis), _ptr(pos), self._stream()))
+
+    @property
+    def launches(self):
+        n = ctypes.c_uint64()
+        self._check(self.lib.pfm_launch_count(self.h, ctypes.byref(n)))
+        return int(n.value)
+
     def mgpcg_solve(self, div, x_out, max_iters=400, tol=1e-12, tol_mode=0, check_every=4):
         """MGPCG init(div, -1) + solve + get_result."""
         self._dev(div, "div")

@@ -57,20 +57,36 @@ def lattice2(res, dx, ppc):
     return ((idx.astype(np.float32) + np.float32(0.5)) * dist).astype(np.float32)
 
 
+def _hash_uniform(seed, n):
+    """Counter-based uniform in [0, 1) (24 bits): splitmix64 finaliser of (seed, n)."""
+    with np.errstate(over="ignore"):
+        z = np.uint64(seed) * np.uint64(0xD1B54A32D192ED03) + n.astype(np.uint64) + np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return (z >> np.uint64(40)).astype(np.float32) * np.float32(1.0 / 16777216.0)
+
+
 def jittered(res, dx, ppc, seed=0):
-    """Stratified jitter: each cell holds ppc particles, one per sub-cell of a ppc_axis^d lattice,
-    placed uniformly inside its sub-cell by numpy.random.default_rng(seed).  Stored cell-major
-    with the last axis fastest, so consecutive particles share grid neighbourhoods."""
+    """Stratified jittered seeding, bit-identical to the device kernel pfm_seed_jittered.
+
+    Each cell holds ppc particles, one per sub-cell of a ppc_axis^d lattice, at
+    (sub-lattice index + U) * dx / ppc_axis, U a splitmix64 hash of (seed, particle, axis).
+    Cell-major order with the last axis fastest, so consecutive particles share grid
+    neighbourhoods."""
     d = len(res)
     axis = int(round(ppc ** (1.0 / d)))
     if axis ** d != ppc:
         raise ValueError("particles per cell must be a perfect square (2D) or cube (3D)")
-    rng = np.random.default_rng(seed)
-    cells = np.stack(np.meshgrid(*[np.arange(n) for n in res], indexing="ij"), axis=-1).reshape(-1, d)
-    sub = np.stack(np.meshgrid(*[np.arange(axis)] * d, indexing="ij"), axis=-1).reshape(-1, d)
-    lat = (cells[:, None, :] * axis + sub[None, :, :]).reshape(-1, d).astype(np.float64)
-    jit = rng.uniform(0.0, 1.0, size=lat.shape)
-    return ((lat + jit) * (dx / axis)).astype(np.float32)
+    cells = int(np.prod(res))
+    P = cells * ppc
+    q = np.arange(P, dtype=np.int64)
+    cell, sub = q // ppc, q % ppc
+    ci = np.stack(np.unravel_index(cell, res), axis=1)
+    si = np.stack(np.unravel_index(sub, (axis,) * d), axis=1)
+    lat = (ci * axis + si).astype(np.float32)
+    u = _hash_uniform(seed, (q[:, None] * d + np.arange(d)[None, :]))
+    return ((lat + u) * np.float32(dx / axis)).astype(np.float32)
 
 
 class DtClock:
@@ -97,13 +113,20 @@ class DtClock:
 
 
 class Sim3D:
-    """GPU state and step of the 3D solver (3D/run_3D.py:716-822)."""
+    """GPU state and step of the 3D solver (3D/run_3D.py:716-822).
+
+    ``u``: the three face grids (numpy arrays or CUDA tensors); ``seeds``: reinit positions, AoS
+    numpy [P, 3] or a device SoA tensor [3, P].  Pass ``timer`` (a callable taking a phase name and
+    returning a context manager) to bracket the phases with CUDA events."""
 
     def __init__(self, u, seeds, res, dx, CFL=0.5, visualize_dt=0.1, reinit_every=20,
                  reinit_every_grad_m=1, use_midpoint_vel=True, reinit_particle_pos=True, use_apic=True,
                  base_level=3, mg_levels=0, poisson_opts=None, device="cuda"):
-        seeds = np.asarray(seeds, np.float32)
-        self.P = seeds.shape[0]
+        if isinstance(seeds, torch.Tensor):
+            self.P = int(seeds.shape[1])
+        else:
+            seeds = np.asarray(seeds, np.float32)
+            self.P = seeds.shape[0]
         self.scene = Scene(3, res, dx, self.P, base_level=base_level, mg_levels=mg_levels, use_apic=use_apic,
                            device=device)
         sc = self.scene
@@ -112,11 +135,12 @@ class Sim3D:
         self.reinit_every, self.grad_m = reinit_every, reinit_every_grad_m
         self.use_midpoint_vel, self.reinit_particle_pos = use_midpoint_vel, reinit_particle_pos
         self.poisson_opts = dict(poisson_opts or {})
-        self.u = [torch.as_tensor(np.asarray(a, np.float32)).to(sc.device).contiguous() for a in u]
+        dev = sc.device
+        self.u = [(a.to(dev).contiguous() if isinstance(a, torch.Tensor)
+                   else torch.as_tensor(np.asarray(a, np.float32)).to(dev).contiguous()) for a in u]
         self.u_mid = sc.alloc_faces()
         self.w = sc.alloc_faces()
-        dev = sc.device
-        self.seeds = soa(seeds, dev)
+        self.seeds = seeds.to(dev).contiguous() if isinstance(seeds, torch.Tensor) else soa(seeds, dev)
         P = self.P
         self.pos = torch.zeros(3, P, device=dev)
         self.init_imp = torch.zeros(3, P, device=dev)
@@ -129,34 +153,48 @@ class Sim3D:
         self.i, self.ik = -1, 0
         self.infos = []
         self.last_dt = None
+        self.timer = None
+
+    def _t(self, name):
+        import contextlib
+        return self.timer(name) if self.timer is not None else contextlib.nullcontext()
 
     def step(self):
         sc = self.scene
         self.i += 1
         i = self.i
         j = i % self.reinit_every
-        max_speed = sc.calc_max_speed(self.u)
+        with self._t("max_speed"):
+            max_speed = sc.calc_max_speed(self.u)
         curr_dt, _ = self.clock.next(max_speed)
         self.last_dt = curr_dt
         if j == 0:
-            if self.reinit_particle_pos or i == 0:
-                self.pos.copy_(self.seeds)
-                self.ik = i
-            sc.g2p(self.pos, self.u, imp_out=self.init_imp)
-            sc.reset_T(self.T_init)
-            sc.reset_T(self.T_gm)
+            with self._t("reinit"):
+                if self.reinit_particle_pos or i == 0:
+                    self.pos.copy_(self.seeds)
+                    self.ik = i
+                sc.g2p(self.pos, self.u, imp_out=self.init_imp)
+                sc.reset_T(self.T_init)
+                sc.reset_T(self.T_gm)
         k = (i - self.ik) % self.grad_m
         if k == 0:
-            sc.g2p(self.pos, self.u, C_out=self.init_C)
-            sc.update_T(self.T_init, self.T_gm, reset_gm=True)
+            with self._t("g2p"):
+                sc.g2p(self.pos, self.u, C_out=self.init_C)
+            with self._t("update_T"):
+                sc.update_T(self.T_init, self.T_gm, reset_gm=True)
         adv = self.u
         if self.use_midpoint_vel:
-            sc.midpoint(self.u, self.u_mid, float(np.float32(0.5 * curr_dt)))
-            self.infos.append(sc.poisson(self.u_mid, **self.poisson_opts))
+            with self._t("midpoint"):
+                sc.midpoint(self.u, self.u_mid, float(np.float32(0.5 * curr_dt)))
+            with self._t("poisson_mid"):
+                self.infos.append(sc.poisson(self.u_mid, **self.poisson_opts))
             adv = self.u_mid
-        sc.rk4_T_forward(self.pos, self.T_gm, adv, float(np.float32(curr_dt)))
-        sc.p2g3(self.init_imp, self.pos, self.T_gm, self.T_init, self.init_C, self.u, self.w)
-        self.infos.append(sc.poisson(self.u, self.p, **self.poisson_opts))
+        with self._t("rk4"):
+            sc.rk4_T_forward(self.pos, self.T_gm, adv, float(np.float32(curr_dt)))
+        with self._t("p2g"):
+            sc.p2g3(self.init_imp, self.pos, self.T_gm, self.T_init, self.init_C, self.u, self.w)
+        with self._t("poisson"):
+            self.infos.append(sc.poisson(self.u, self.p, **self.poisson_opts))
         return curr_dt
 
 

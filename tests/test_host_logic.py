@@ -1,0 +1,84 @@
+"""Host-side logic of the drop-in: CFL/frame clock, reinit schedule, seeding and layouts (CPU)."""
+import numpy as np
+import pytest
+
+import oracle as O
+import pfm
+
+
+def test_clock_matches_reference_rule():
+    c = pfm.DtClock(CFL=0.5, dx=1 / 32, visualize_dt=0.1)
+    dts = []
+    for ms in (0.1, 0.1, 0.2, 5.0, 0.01):
+        dt, out = c.next(ms)
+        dts.append((dt, out))
+    # first: 0.5/32/0.1 = 0.15625 >= 0.1 -> clamped to the frame end
+    assert dts[0] == (pytest.approx(0.1), True)
+    assert dts[2][0] == pytest.approx(0.078125) and not dts[2][1]
+    assert dts[3][0] == pytest.approx(0.5 / 32 / 5.0) and not dts[3][1]
+    assert c.sub_t == pytest.approx(0.078125 + 0.5 / 32 / 5.0 + 0.0 if not dts[4][1] else 0.0) or dts[4][1]
+
+
+def test_clock_same_as_oracle():
+    a, b = pfm.DtClock(0.5, 1 / 64, 0.1), O.DtClock(0.5, 1 / 64, 0.1)
+    rng = np.random.default_rng(0)
+    for ms in rng.uniform(0.05, 3.0, 200):
+        assert a.next(ms) == b.next(ms)
+
+
+def test_lattice_is_the_reference_order():
+    p = pfm.lattice3((4, 3, 2), 0.25)
+    assert p.shape == (4 * 3 * 2 * 8, 3)
+    # x fastest: consecutive particles step by dx/2 in x (init_conditions.py:246-252)
+    assert np.allclose(p[1] - p[0], [0.125, 0, 0])
+    assert np.allclose(p[8], [0.0625, 0.1875, 0.0625])
+    assert np.array_equal(p, O.lattice3((4, 3, 2), 0.25))
+    assert np.array_equal(pfm.lattice2((8, 4), 0.25, 4), O.lattice2((8, 4), 0.25, 4))
+
+
+def test_jitter_is_seeded_stratified_and_cell_major():
+    a = pfm.jittered((4, 4, 4), 0.25, 8, seed=0)
+    b = pfm.jittered((4, 4, 4), 0.25, 8, seed=0)
+    c = pfm.jittered((4, 4, 4), 0.25, 8, seed=1)
+    assert np.array_equal(a, b) and not np.array_equal(a, c)
+    cells = np.floor(a / 0.25).astype(int)
+    lin = (cells[:, 0] * 4 + cells[:, 1]) * 4 + cells[:, 2]
+    assert np.array_equal(lin, np.repeat(np.arange(64), 8))  # 8 per cell, cell-major order
+    sub = np.floor(a / 0.125).astype(int) % 2
+    assert len({tuple(s) for s in sub[:8]}) == 8  # one per sub-cell
+    two = pfm.jittered((8, 8), 1 / 8, 4, seed=0)
+    assert two.shape == (256, 2)
+    with pytest.raises(ValueError):
+        pfm.jittered((4, 4), 0.25, 3)
+
+
+def test_soa_round_trip():
+    rng = np.random.default_rng(0)
+    a = rng.standard_normal((10, 3)).astype(np.float32)
+    T = rng.standard_normal((10, 3, 3)).astype(np.float32)
+    s = pfm.soa(a, "cpu")
+    assert tuple(s.shape) == (3, 10) and np.array_equal(pfm.aos(s), a)
+    t = pfm.soa_T(T, "cpu")
+    assert tuple(t.shape) == (3, 3, 10) and np.array_equal(pfm.aos_T(t), T)
+    # element (v, c, q) is T_v[c] of particle q
+    assert t[1, 2, 7] == T[7, 1, 2]
+
+
+def test_reinit_schedule_3d_vs_2d():
+    """3D resets ik only when particles are reseeded (run_3D.py:751-755); 2D always (run_2D.py:811-819)."""
+    def sched(n, every, gm, is3d, reseed=True):
+        out, ik = [], 0
+        for i in range(n):
+            j = i % every
+            if j == 0:
+                if is3d:
+                    if reseed or i == 0:
+                        ik = i
+                else:
+                    ik = i
+            out.append((j == 0, (i - ik) % gm == 0))
+        return out
+    s3 = sched(12, 5, 2, True, reseed=False)
+    assert [k for _, k in s3] == [(i % 2 == 0) for i in range(12)]
+    s2 = sched(12, 5, 2, False)
+    assert s2[5] == (True, True) and s2[6] == (False, False) and s2[7] == (False, True)

@@ -1,0 +1,131 @@
+"""Pins the CPU oracle to the reference: every golden vector in tests/golden/ was produced by the
+reference's own Taichi kernels and main() loop (tests/golden/make_golden.py)."""
+import numpy as np
+import pytest
+
+import oracle as O
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    d = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / (d if d > 0 else 1.0))
+
+
+def prel(a, b):
+    """Relative L2 of the pressure with its all-Neumann null-space constant removed."""
+    return rel(np.asarray(a) - np.mean(a), np.asarray(b) - np.mean(b))
+
+
+# The oracle evaluates each kernel in the reference's expression order; what remains is numpy's
+# own rounding in the shim (a few ulp), hence the tight tolerance.
+KTOL = 1e-7
+
+
+def test_oracle_kernels_3d(golden):
+    g = golden("ref3d_kernels")
+    dx = 1.0 / int(g["res"][1])
+    u = (g["u_x"], g["u_y"], g["u_z"])
+    assert O.calc_max_speed3(*u) == float(g["max_speed"])
+    imp, C = O.g2p3(g["pos"], *u, dx)
+    assert rel(imp, g["g2p_imp"]) < KTOL and rel(C, g["g2p_C"]) < KTOL
+    pos, T = O.rk4_T_forward3(g["pos"], g["T_gm"], *u, dx, g["dt"])
+    assert rel(pos, g["rk4_pos"]) < KTOL and rel(T, g["rk4_T"]) < KTOL
+    assert np.array_equal(O.update_T3(g["T_init"], g["T_gm"]), g["update_T"])
+    (ux, uy, uz), (wx, wy, wz) = O.p2g3(g["init_imp"], g["pos"], g["T_gm"], g["T_init"], g["init_C"],
+                                        tuple(g["res"]), dx)
+    for a, n in zip((ux, uy, uz, wx, wy, wz), ("u_x", "u_y", "u_z", "w_x", "w_y", "w_z")):
+        assert rel(a, g["p2g_" + n]) < KTOL, n
+    assert np.array_equal(O.bin_count3(g["bin_pos"], tuple(g["res"]), dx), g["bin_count"])
+    for fam, n in ((0, "x"), (2, "z")):
+        psi, T, um = O.midpoint_family3(fam, *u, dx, np.float32(0.5 * float(g["dt"])))
+        assert np.array_equal(psi, g[f"mid_psi_{n}"])
+        assert rel(T, g[f"mid_T_{n}"]) < KTOL and rel(um, g[f"mid_u_{n}"]) < KTOL
+
+
+@pytest.mark.parametrize("case", ["poisson", "poisson2"])
+def test_oracle_poisson_3d_bitexact(golden, case):
+    g = golden("ref3d_kernels")
+    ins = ([g["mid_u_x"], g["mid_u_y"], g["mid_u_z"]] if case == "poisson"
+           else [g["poisson2_in_x"], g["poisson2_in_y"], g["poisson2_in_z"]])
+    ux, uy, uz, p, it, _ = O.poisson3(*ins)
+    assert it == int(g[f"{case}_iters"])
+    for a, n in zip((ux, uy, uz), "xyz"):
+        assert np.array_equal(a, g[f"{case}_u_{n}"])
+    assert np.array_equal(p, g[f"{case}_p"])
+
+
+def test_oracle_kernels_2d(golden):
+    g = golden("ref2d_kernels")
+    dx = 1.0 / int(g["res"][1])
+    u = (g["u_x"], g["u_y"])
+    assert O.calc_max_speed2(*u) == float(g["max_speed"])
+    imp, C = O.g2p2(g["pos"], *u, dx)
+    assert rel(imp, g["g2p_imp"]) < KTOL and rel(C, g["g2p_C"]) < KTOL
+    pos, T = O.rk4_T_forward2(g["pos"], g["T_gm"], *u, dx, g["dt"], 1)
+    assert rel(pos, g["rk4_pos"]) < KTOL and rel(T, g["rk4_T"]) < KTOL
+    assert np.array_equal(O.update_grad_m2(g["init_C"], g["T_gm"]), g["grad_m_C"])
+    T2 = O.update_T2(g["T_init"], g["T_gm"])
+    assert np.array_equal(T2, g["update_T"])
+    assert np.array_equal(O.update_imp2(g["init_imp"], T2), g["update_imp"])
+    (ux, uy), (wx, wy), (gx, gy) = O.p2g2(g["init_imp"], g["pos"], g["init_C"], g["psi"], tuple(g["res"]), dx)
+    for a, n in zip((ux, uy, wx, wy, gx, gy), ("u_x", "u_y", "w_x", "w_y", "psi_x", "psi_y")):
+        assert rel(a, g["p2g_" + n]) < KTOL, n
+    for fam, n in ((0, "x"), (1, "y")):
+        psi, T, um = O.midpoint_family2(fam, *u, dx, np.float32(0.5 * float(g["dt"])))
+        assert np.array_equal(psi, g[f"mid_psi_{n}"])
+        assert rel(T, g[f"mid_T_{n}"]) < KTOL and rel(um, g[f"mid_u_{n}"]) < KTOL
+
+
+@pytest.mark.parametrize("case", ["poisson", "poisson2"])
+def test_oracle_poisson_2d_bitexact(golden, case):
+    g = golden("ref2d_kernels")
+    ins = [g["mid_u_x"], g["mid_u_y"]] if case == "poisson" else [g["poisson2_in_x"], g["poisson2_in_y"]]
+    ux, uy, p, it, _ = O.poisson2(*ins)
+    assert it == int(g[f"{case}_iters"])
+    assert np.array_equal(ux, g[f"{case}_u_x"]) and np.array_equal(uy, g[f"{case}_u_y"])
+    assert np.array_equal(p, g[f"{case}_p"])
+
+
+def test_oracle_steps_2d(golden):
+    """run_2D.main() of the reference, 20 steps at 32^2 (reinit 12, grad_m reinit 8)."""
+    g = golden("ref2d_steps")
+    res = tuple(int(r) for r in g["res"])
+    dx = 1.0 / res[1]
+    sim = O.Sim2D([g["init_u_x"], g["init_u_y"]], O.lattice2(res, dx, 4), res, dx, CFL=0.5, visualize_dt=0.1,
+                  reinit_every=int(g["hp"][0]), reinit_every_grad_m=int(g["hp"][1]))
+    for s in range(1, 21):
+        sim.step()
+        assert rel(sim.u[0], g[f"s{s}_u_x"]) < 1e-5 and rel(sim.u[1], g[f"s{s}_u_y"]) < 1e-5, s
+        assert prel(sim.p, g[f"s{s}_p"]) < 1e-5, s
+        if f"s{s}_particles_pos" in g:
+            assert rel(sim.pos, g[f"s{s}_particles_pos"]) < 1e-6
+            assert rel(sim.imp, g[f"s{s}_particles_imp"]) < 1e-5
+            assert rel(sim.T, np.stack([g[f"s{s}_T_x"], g[f"s{s}_T_y"]], 1)) < 1e-5
+    # iteration counts printed by the reference: IC projection, then (midpoint, final) per step
+    assert sim.iters == [int(i) for i in g["iters"][1:]]
+
+
+def test_oracle_steps_3d(golden):
+    """run_3D.main() of the reference, 10 steps at 8^3 (reinit 5, grad_m reinit 2)."""
+    import os
+    path = os.path.join(os.path.dirname(__file__), "golden", "ref3d_steps.npz")
+    if not os.path.exists(path):
+        pytest.skip("3D step golden not generated")
+    g = golden("ref3d_steps")
+    res = tuple(int(r) for r in g["res"])
+    dx = 1.0 / res[1]
+    sim = O.Sim3D([g["init_u_x"], g["init_u_y"], g["init_u_z"]], O.lattice3(res, dx), res, dx, CFL=0.5,
+                  visualize_dt=0.1, reinit_every=int(g["hp"][0]), reinit_every_grad_m=int(g["hp"][1]))
+    for s in range(1, 11):
+        sim.step()
+        for f, n in enumerate("xyz"):
+            assert rel(sim.u[f], g[f"s{s}_u_{n}"]) < 1e-5, (s, n)
+        assert prel(sim.p, g[f"s{s}_p"]) < 1e-5, s
+        if f"s{s}_particles_pos" in g:
+            assert rel(sim.pos, g[f"s{s}_particles_pos"]) < 1e-6
+            assert rel(sim.init_imp, g[f"s{s}_particles_init_imp"]) < 1e-5
+            T_init = np.stack([g[f"s{s}_T_{v}_init"] for v in "xyz"], 1)
+            assert rel(sim.T_init, T_init) < 1e-5
+    assert sim.iters == [int(i) for i in g["iters"][1:]]
