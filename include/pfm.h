@@ -134,8 +134,9 @@ int pfm3_sort_particles(pfm_handle* h, const float* pos, int* cell_count, int* o
 
 /* P2G (3D/run_3D.py:441-552): APIC transfer of impulse m = T_gm^T T_init^T-composed init_imp
  * with affine term (T_gm^T init_C T_gm) to the faces, normalised by the weight sums.
- * Deterministic: sort + per-face gather in (cell, particle-index) order, no float atomics.
- * Writes u_x/u_y/u_z and the weight grids w_x/w_y/w_z. */
+ * Deterministic, no float atomics: particles are counting-sorted into cell bins, then every face
+ * sums its neighbourhood's bins in a fixed order.  Writes u_x/u_y/u_z and the weight grids
+ * w_x/w_y/w_z. */
 int pfm3_p2g(pfm_handle* h, const float* init_imp, const float* pos, const float* T_gm,
              const float* T_init, const float* init_C, float* u_x, float* u_y, float* u_z,
              float* w_x, float* w_y, float* w_z, void* stream);

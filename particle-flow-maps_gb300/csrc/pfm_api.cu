@@ -128,6 +128,7 @@ int pfm_create(const pfm_config* cfg, pfm_handle** out) {
   h->o_partials = take(kReduceBlocks * sizeof(double));
   h->o_state = take(sizeof(SolveState));
   h->o_maxpart = take(kReduceBlocks * sizeof(float) + 256);
+
   h->ws_need = off;
   if (cudaHostAlloc((void**)&h->h_state, sizeof(SolveState), cudaHostAllocDefault) != cudaSuccess) {
     cudaGetLastError();
@@ -141,6 +142,9 @@ int pfm_create(const pfm_config* cfg, pfm_handle** out) {
 
 int pfm_destroy(pfm_handle* h) {
   if (!h) return PFM_ERR_NULL;
+  if (h->g_setup) cudaGraphExecDestroy(h->g_setup);
+  if (h->g_iter) cudaGraphExecDestroy(h->g_iter);
+  if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
   if (h->h_state) cudaFreeHost(h->h_state);
   delete h;
   return PFM_OK;

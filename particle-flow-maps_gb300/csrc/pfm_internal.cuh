@@ -69,10 +69,17 @@ struct pfm_handle {
   size_t o_key, o_slot, o_order, o_count, o_start, o_blocksums, o_payload;
   size_t o_r[pfm::kMaxLevels], o_z[pfm::kMaxLevels];
   size_t o_x, o_p, o_Ap, o_partials, o_state, o_maxpart;
+
   // pinned host mirror of the solve state
   pfm::SolveState* h_state;
   // kernels launched through this handle (reported by pfm_launch_count)
   uint64_t launches;
+  // CUDA graphs of the MGPCG setup and of one PCG iteration (captured on first use)
+  cudaStream_t cap_stream;
+  cudaGraphExec_t g_setup, g_iter;
+  int g_setup_nodes, g_iter_nodes;
+  double g_eps, g_tol;
+  int g_mode, g_valid;
   std::string err;
 };
 
@@ -126,8 +133,14 @@ __device__ __forceinline__ float dN2(float x) {
 
 // One axis of the interp_grad_2 stencil (3D/taichi_utils.py:278-305).  The reference visits
 // the four taps iu-1..iu+2 of the clamped sample position s; exactly one of the outer two has
-// |x| >= 1.5, where N_2 and dN_2 are exactly zero, so only the three taps starting at `first`
-// are kept.  Indices are clamped like sample() (3D/taichi_utils.py:48-54).
+// |x| >= 1.5, where N_2 and dN_2 are exactly zero, so only the three taps around the middle tap
+// m (|s - m| <= 0.5) are kept.  With t = s - m in [-0.5, 0.5) the three taps sit at x = t+1, t,
+// t-1, where the branches of N_2 / dN_2 reduce to
+//   N_2:  0.5 (0.5 - t)^2,  0.75 - t^2,  0.5 (0.5 + t)^2
+//   dN_2: t - 0.5,          -2 t,        t + 0.5
+// (the |x| = 0.5 and 1.5 boundary cases included).  For s >= 1 every subtraction involved is
+// exact, so the weights are bitwise those of the reference's per-tap evaluation.
+// Indices are clamped like sample() (3D/taichi_utils.py:48-54).
 struct Axis3 {
   int idx[3];
   float w[3];
@@ -135,19 +148,24 @@ struct Axis3 {
 };
 
 __device__ __forceinline__ void axis_taps(float u, float hi, int n, Axis3& a) {
-  float s = fmaxf(1.f, fminf(u, hi));
-  float iu = floorf(s);
-  float frac = s - iu;
-  int first = frac < 0.5f ? -1 : 0;
-  int ib = __float2int_rz(iu);
+  const float s = fmaxf(1.f, fminf(u, hi));
+  const float iu = floorf(s);
+  const float frac = s - iu;
+  const bool lo = frac < 0.5f;
+  const float t = lo ? frac : frac - 1.f;
+  const float l = 0.5f - t, r = 0.5f + t;
+  a.w[0] = 0.5f * (l * l);
+  a.w[1] = 0.75f - t * t;
+  a.w[2] = 0.5f * (r * r);
+  a.dw[0] = t - 0.5f;
+  a.dw[1] = -2.f * t;
+  a.dw[2] = t + 0.5f;
+  const int first = __float2int_rz(iu) + (lo ? -1 : 0);
 #pragma unroll
-  for (int t = 0; t < 3; ++t) {
-    float x = s - (iu + (float)(first + t));
-    a.w[t] = N2(x);
-    a.dw[t] = dN2(x);
-    int id = ib + first + t;
+  for (int q = 0; q < 3; ++q) {
+    int id = first + q;
     id = id < 0 ? 0 : (id > n - 1 ? n - 1 : id);
-    a.idx[t] = id;
+    a.idx[q] = id;
   }
 }
 

@@ -385,6 +385,110 @@ __global__ void __launch_bounds__(256) k_update_p(float* __restrict__ p, const f
 }
 
 // ---------------------------------------------------------------------------------------------
+// coarse-level V-cycle tail in one CTA
+// ---------------------------------------------------------------------------------------------
+// Levels whose cell count fits kTailMaxCells run the rest of the V-cycle (pre-smoothing,
+// restriction, the bottom sweeps, prolongation, post-smoothing; 3D/mgpcg.py:182-200) inside one
+// thread block, with the level vectors in shared memory and __syncthreads() between half-sweeps.
+// Each cell update is the same expression as in the grid-wide kernels, in the same sweep order.
+constexpr int kTailMaxCells = 4096;
+constexpr int kTailThreads = 1024;
+
+struct TailPlan {
+  int l0, L;           // levels l0 .. L-1 live in shared memory
+  Lvl lv[kMaxLevels];
+  int off[kMaxLevels]; // offset of level l in each of the z and r shared arrays
+  int total;           // floats per array
+};
+
+template <int D>
+__device__ void tail_smooth(float* z, const float* r, const Lvl& L, const BC& bc, int phase) {
+  for (int e = threadIdx.x; e < (int)L.count; e += blockDim.x) {
+    int i, j, k;
+    decode(L, e, i, j, k);
+    if (((i + j + k) & 1) == phase) {
+      float nb, mult;
+      stencil<D>(z, L, bc, i, j, k, e, nb, mult);
+      z[e] = (r[e] + nb) / mult;
+    }
+  }
+  __syncthreads();
+}
+
+template <int D>
+__global__ void __launch_bounds__(kTailThreads) k_vcycle_tail(float* __restrict__ zg, const float* __restrict__ rg,
+                                                              TailPlan T, BC bc, int pre_post, int bottom,
+                                                              const SolveState* st) {
+  if (st && st->done) return;
+  extern __shared__ float sh[];
+  float* Z = sh;
+  float* R = sh + T.total;
+  const int l0 = T.l0;
+  for (int e = threadIdx.x; e < (int)T.lv[l0].count; e += blockDim.x) {
+    R[T.off[l0] + e] = rg[e];
+    Z[T.off[l0] + e] = 0.f;
+  }
+  __syncthreads();
+  for (int l = l0; l < T.L - 1; ++l) {
+    float* z = Z + T.off[l];
+    const float* r = R + T.off[l];
+    for (int it = 0; it < pre_post; ++it) {
+      tail_smooth<D>(z, r, T.lv[l], bc, 0);
+      tail_smooth<D>(z, r, T.lv[l], bc, 1);
+    }
+    const Lvl Lf = T.lv[l], Lc = T.lv[l + 1];
+    float* zc = Z + T.off[l + 1];
+    float* rc = R + T.off[l + 1];
+    for (int e = threadIdx.x; e < (int)Lc.count; e += blockDim.x) {
+      int I, J, K;
+      decode(Lc, e, I, J, K);
+      float acc = 0.f;
+      for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2; ++b)
+          for (int cc = 0; cc < (D == 3 ? 2 : 1); ++cc) {
+            int i = 2 * I + a, j = 2 * J + b, k = (D == 3) ? 2 * K + cc : 0;
+            if (i >= Lf.n0 || j >= Lf.n1 || k >= Lf.n2) continue;
+            const int64_t c = ((int64_t)i * Lf.n1 + j) * Lf.n2 + k;
+            float nb, mult;
+            stencil<D>(z, Lf, bc, i, j, k, c, nb, mult);
+            float res = r[c] - (mult * z[c] - nb);
+            acc += res * 1.0f / ((float)D - 1.0f);
+          }
+      rc[e] = acc;
+      zc[e] = 0.f;
+    }
+    __syncthreads();
+  }
+  {
+    float* z = Z + T.off[T.L - 1];
+    const float* r = R + T.off[T.L - 1];
+    for (int it = 0; it < bottom; ++it) {
+      tail_smooth<D>(z, r, T.lv[T.L - 1], bc, 0);
+      tail_smooth<D>(z, r, T.lv[T.L - 1], bc, 1);
+    }
+  }
+  for (int l = T.L - 2; l >= l0; --l) {
+    float* z = Z + T.off[l];
+    const float* r = R + T.off[l];
+    const Lvl Lf = T.lv[l], Lc = T.lv[l + 1];
+    const float* zc = Z + T.off[l + 1];
+    for (int e = threadIdx.x; e < (int)Lf.count; e += blockDim.x) {
+      int i, j, k;
+      decode(Lf, e, i, j, k);
+      int64_t ce = (D == 3) ? ((int64_t)(i >> 1) * Lc.n1 + (j >> 1)) * Lc.n2 + (k >> 1)
+                            : (int64_t)(i >> 1) * Lc.n1 + (j >> 1);
+      z[e] += zc[ce];
+    }
+    __syncthreads();
+    for (int it = 0; it < pre_post; ++it) {
+      tail_smooth<D>(z, r, Lf, bc, 1);
+      tail_smooth<D>(z, r, Lf, bc, 0);
+    }
+  }
+  for (int e = threadIdx.x; e < (int)T.lv[l0].count; e += blockDim.x) zg[e] = Z[T.off[l0] + e];
+}
+
+// ---------------------------------------------------------------------------------------------
 // host orchestration
 // ---------------------------------------------------------------------------------------------
 static BC bc_of(const pfm_handle* h) {
@@ -415,30 +519,56 @@ static void smooth_launch(pfm_handle* h, int l, int phase, const SolveState* st,
                                                    bc_of(h), phase, st);
 }
 
+static int tail_level(const pfm_handle* h) {
+  for (int l = 0; l < h->L; ++l)
+    if (h->lv[l].count <= kTailMaxCells) return l;
+  return h->L;  // no level small enough: every level runs as grid-wide kernels
+}
+
 // apply_preconditioner (3D/mgpcg.py:182-200)
 template <int D>
 static void vcycle(pfm_handle* h, const SolveState* st, cudaStream_t s) {
   const int L = h->L;
   const BC bc = bc_of(h);
+  const int l0 = tail_level(h);
   launch(h, k_zero, stream_blocks(h->lv[0].count), 256, 0, s, ws_ptr<float>(h, h->o_z[0]), h->lv[0].count, st);
-  for (int l = 0; l < L - 1; ++l) {
+  const int down_end = l0 < L ? l0 : L - 1;  // grid-wide levels that restrict to a coarser one
+  for (int l = 0; l < down_end; ++l) {
     for (int i = 0; i < h->cfg.pre_post_smoothing; ++i) {
       smooth_launch<D>(h, l, 0, st, s);
       smooth_launch<D>(h, l, 1, st, s);
     }
-    launch(h, k_zero, stream_blocks(h->lv[l + 1].count), 256, 0, s, ws_ptr<float>(h, h->o_z[l + 1]), h->lv[l + 1].count, st);
+    if (l + 1 != l0)
+      launch(h, k_zero, stream_blocks(h->lv[l + 1].count), 256, 0, s, ws_ptr<float>(h, h->o_z[l + 1]),
+             h->lv[l + 1].count, st);
     Lvl Lf = lvl_of(h, l), Lc = lvl_of(h, l + 1);
     launch(h, k_restrict<D>, grid_for(Lc.count, 256), 256, 0, s, ws_ptr<float>(h, h->o_z[l]), ws_ptr<float>(h, h->o_r[l]),
-                                                          Lf, ws_ptr<float>(h, h->o_r[l + 1]), Lc, bc, st);
+           Lf, ws_ptr<float>(h, h->o_r[l + 1]), Lc, bc, st);
   }
-  for (int i = 0; i < h->cfg.bottom_smoothing; ++i) {
-    smooth_launch<D>(h, L - 1, 0, st, s);
-    smooth_launch<D>(h, L - 1, 1, st, s);
+  if (l0 < L) {
+    TailPlan T{};
+    T.l0 = l0;
+    T.L = L;
+    int off = 0;
+    for (int l = l0; l < L; ++l) {
+      T.lv[l] = lvl_of(h, l);
+      T.off[l] = off;
+      off += (int)h->lv[l].count;
+    }
+    T.total = off;
+    const size_t smem = (size_t)off * 2 * sizeof(float);
+    launch(h, k_vcycle_tail<D>, 1, kTailThreads, smem, s, ws_ptr<float>(h, h->o_z[l0]), ws_ptr<float>(h, h->o_r[l0]),
+           T, bc, h->cfg.pre_post_smoothing, h->cfg.bottom_smoothing, st);
+  } else {
+    for (int i = 0; i < h->cfg.bottom_smoothing; ++i) {
+      smooth_launch<D>(h, L - 1, 0, st, s);
+      smooth_launch<D>(h, L - 1, 1, st, s);
+    }
   }
-  for (int l = L - 2; l >= 0; --l) {
+  for (int l = down_end - 1; l >= 0; --l) {
     Lvl Lf = lvl_of(h, l), Lc = lvl_of(h, l + 1);
     launch(h, k_prolong<D>, grid_for(Lf.count, 256), 256, 0, s, ws_ptr<float>(h, h->o_z[l]), Lf,
-                                                         ws_ptr<float>(h, h->o_z[l + 1]), Lc, st);
+           ws_ptr<float>(h, h->o_z[l + 1]), Lc, st);
     for (int i = 0; i < h->cfg.pre_post_smoothing; ++i) {
       smooth_launch<D>(h, l, 1, st, s);
       smooth_launch<D>(h, l, 0, st, s);
@@ -452,8 +582,37 @@ static bool all_neumann(const pfm_handle* h) {
   return true;
 }
 
+// Captures `body` (kernels only) on the handle's capture stream into an executable graph.
+template <class F>
+static int capture(pfm_handle* h, F&& body, cudaGraphExec_t* exec, int* nodes) {
+  if (!h->cap_stream) {
+    int rc = check_cuda(h, cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking), "capture stream");
+    if (rc) return rc;
+  }
+  cudaGraph_t g = nullptr;
+  int rc = check_cuda(h, cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+  if (rc) return rc;
+  const uint64_t before = h->launches;
+  body(h->cap_stream);
+  *nodes = (int)(h->launches - before);
+  h->launches = before;
+  rc = check_cuda(h, cudaStreamEndCapture(h->cap_stream, &g), "end capture");
+  if (rc) return rc;
+  rc = check_cuda(h, cudaGraphInstantiate(exec, g, 0), "graph instantiate");
+  cudaGraphDestroy(g);
+  return rc;
+}
+
+static int run_graph(pfm_handle* h, cudaGraphExec_t exec, int nodes, cudaStream_t s) {
+  h->launches += (uint64_t)nodes;
+  return check_cuda(h, cudaGraphLaunch(exec, s), "graph launch");
+}
+
+// MGPCG.solve (3D/mgpcg.py:202-280) on r_0 (already -div); the solution is left in the
+// workspace vector x.  The setup (recenter, first V-cycle, p = z, z.r) and one PCG iteration are
+// each replayed from a CUDA graph; the host reads the device state every check_every iterations.
 template <int D>
-static int solve_impl(pfm_handle* h, float* x, const pfm_solve_opts* opts, pfm_solve_stats* stats, cudaStream_t s) {
+static int solve_impl(pfm_handle* h, const pfm_solve_opts* opts, pfm_solve_stats* stats, cudaStream_t s) {
   pfm_solve_opts o{400, 1e-12, 1e-12, 0, 4};
   if (opts) o = *opts;
   if (o.check_every < 1) o.check_every = 1;
@@ -462,27 +621,60 @@ static int solve_impl(pfm_handle* h, float* x, const pfm_solve_opts* opts, pfm_s
   RedBuf rb{ws_ptr<double>(h, h->o_partials), st};
   float* r0 = ws_ptr<float>(h, h->o_r[0]);
   float* z0 = ws_ptr<float>(h, h->o_z[0]);
+  float* x = ws_ptr<float>(h, h->o_x);
   float* p = ws_ptr<float>(h, h->o_p);
   float* Ap = ws_ptr<float>(h, h->o_Ap);
   const Lvl L0 = lvl_of(h, 0);
   const BC bc = bc_of(h);
   const double inv_n = 1.0 / (double)n;
+  const bool neu = all_neumann(h);
+  if (!h->g_valid || h->g_eps != o.eps || h->g_tol != o.tol || h->g_mode != o.tol_mode) {
+    if (h->g_setup) cudaGraphExecDestroy(h->g_setup);
+    if (h->g_iter) cudaGraphExecDestroy(h->g_iter);
+    h->g_setup = h->g_iter = nullptr;
+    h->g_valid = 0;
+    auto setup = [&](cudaStream_t q) {
+      if (neu) {
+        launch(h, k_dot, red_blocks(n), kReduceThreads, 0, q, r0, (const float*)nullptr, n, rb, (int)RED_MEAN, o.eps, inv_n);
+        launch(h, k_sub_mean, stream_blocks(n), 256, 0, q, r0, n, (const SolveState*)st);
+      }
+      launch(h, k_dot, red_blocks(n), kReduceThreads, 0, q, (const float*)r0, (const float*)r0, n, rb, (int)RED_RTR0,
+             o.eps, inv_n);
+      vcycle<D>(h, st, q);
+      launch(h, k_update_p, stream_blocks(n), 256, 0, q, p, (const float*)z0, n, (const SolveState*)st);
+      launch(h, k_dot, red_blocks(n), kReduceThreads, 0, q, (const float*)z0, (const float*)r0, n, rb,
+             (int)RED_ZTR_INIT, o.eps, inv_n);
+    };
+    auto iter = [&](cudaStream_t q) {
+      launch(h, k_Ap_dot<D>, red_blocks(n), kReduceThreads, 0, q, (const float*)p, Ap, L0, bc, rb, o.eps);
+      launch(h, k_update_xr, red_blocks(n), kReduceThreads, 0, q, x, (const float*)p, r0, (const float*)Ap, n, rb, o.tol,
+             o.tol_mode);
+      if (neu) {
+        launch(h, k_dot, red_blocks(n), kReduceThreads, 0, q, (const float*)r0, (const float*)nullptr, n, rb,
+               (int)RED_MEAN, o.eps, inv_n);
+        launch(h, k_sub_mean, stream_blocks(n), 256, 0, q, r0, n, (const SolveState*)st);
+      }
+      vcycle<D>(h, st, q);
+      launch(h, k_dot, red_blocks(n), kReduceThreads, 0, q, (const float*)z0, (const float*)r0, n, rb, (int)RED_ZTR,
+             o.eps, inv_n);
+      launch(h, k_update_p, stream_blocks(n), 256, 0, q, p, (const float*)z0, n, (const SolveState*)st);
+    };
+    int rc = capture(h, setup, &h->g_setup, &h->g_setup_nodes);
+    if (rc) return rc;
+    rc = capture(h, iter, &h->g_iter, &h->g_iter_nodes);
+    if (rc) return rc;
+    h->g_eps = o.eps;
+    h->g_tol = o.tol;
+    h->g_mode = o.tol_mode;
+    h->g_valid = 1;
+  }
   int rc = check_cuda(h, cudaMemsetAsync(st, 0, sizeof(SolveState), s), "memset state");
   if (rc) return rc;
-  // init(): x = p = Ap = z0 = 0 (3D/mgpcg.py:63-79)
+  // init(): x = p = Ap = 0 (3D/mgpcg.py:63-79); z0 is zeroed by the V-cycle
   cudaMemsetAsync(x, 0, n * 4, s);
   cudaMemsetAsync(p, 0, n * 4, s);
   cudaMemsetAsync(Ap, 0, n * 4, s);
-  const bool neu = all_neumann(h);
-  if (neu) {
-    launch(h, k_dot, red_blocks(n), kReduceThreads, 0, s, r0, nullptr, n, rb, RED_MEAN, o.eps, inv_n);
-    launch(h, k_sub_mean, stream_blocks(n), 256, 0, s, r0, n, st);
-  }
-  launch(h, k_dot, red_blocks(n), kReduceThreads, 0, s, r0, r0, n, rb, RED_RTR0, o.eps, inv_n);
-  vcycle<D>(h, st, s);
-  launch(h, k_update_p, stream_blocks(n), 256, 0, s, p, z0, n, st);  // beta = 0 in the state
-  launch(h, k_dot, red_blocks(n), kReduceThreads, 0, s, z0, r0, n, rb, RED_ZTR_INIT, o.eps, inv_n);
-  rc = launch_check(h, "mgpcg setup");
+  rc = run_graph(h, h->g_setup, h->g_setup_nodes, s);
   if (rc) return rc;
   int enq = 0;
   SolveState* hs = h->h_state;
@@ -490,19 +682,10 @@ static int solve_impl(pfm_handle* h, float* x, const pfm_solve_opts* opts, pfm_s
     int chunk = o.check_every;
     if (o.max_iters >= 0 && enq + chunk > o.max_iters) chunk = o.max_iters - enq;
     for (int c = 0; c < chunk; ++c) {
-      launch(h, k_Ap_dot<D>, red_blocks(n), kReduceThreads, 0, s, p, Ap, L0, bc, rb, o.eps);
-      launch(h, k_update_xr, red_blocks(n), kReduceThreads, 0, s, x, p, r0, Ap, n, rb, o.tol, o.tol_mode);
-      if (neu) {
-        launch(h, k_dot, red_blocks(n), kReduceThreads, 0, s, r0, nullptr, n, rb, RED_MEAN, o.eps, inv_n);
-        launch(h, k_sub_mean, stream_blocks(n), 256, 0, s, r0, n, st);
-      }
-      vcycle<D>(h, st, s);
-      launch(h, k_dot, red_blocks(n), kReduceThreads, 0, s, z0, r0, n, rb, RED_ZTR, o.eps, inv_n);
-      launch(h, k_update_p, stream_blocks(n), 256, 0, s, p, z0, n, st);
+      rc = run_graph(h, h->g_iter, h->g_iter_nodes, s);
+      if (rc) return rc;
     }
     enq += chunk;
-    rc = launch_check(h, "mgpcg iteration");
-    if (rc) return rc;
     rc = check_cuda(h, cudaMemcpyAsync(hs, st, sizeof(SolveState), cudaMemcpyDeviceToHost, s), "state readback");
     if (rc) return rc;
     rc = check_cuda(h, cudaStreamSynchronize(s), "mgpcg sync");
@@ -521,9 +704,16 @@ static int solve_impl(pfm_handle* h, float* x, const pfm_solve_opts* opts, pfm_s
   return PFM_OK;
 }
 
-int mgpcg_solve_in_place(pfm_handle* h, float* x, const pfm_solve_opts* opts, pfm_solve_stats* stats,
+int mgpcg_solve_in_place(pfm_handle* h, float* x_out, const pfm_solve_opts* opts, pfm_solve_stats* stats,
                          cudaStream_t s) {
-  return h->cfg.dim == 3 ? solve_impl<3>(h, x, opts, stats, s) : solve_impl<2>(h, x, opts, stats, s);
+  int rc = h->cfg.dim == 3 ? solve_impl<3>(h, opts, stats, s) : solve_impl<2>(h, opts, stats, s);
+  if (rc != PFM_OK && rc != PFM_ERR_NOT_CONVERGED) return rc;
+  if (x_out) {
+    int c = check_cuda(h, cudaMemcpyAsync(x_out, ws_ptr<float>(h, h->o_x), h->cells * 4, cudaMemcpyDeviceToDevice, s),
+                       "copy pressure");
+    if (c) return c;
+  }
+  return rc;
 }
 
 template <int D>
@@ -542,8 +732,8 @@ static int poisson_impl(pfm_handle* h, float* const* u, float* p_out, const pfm_
   launch(h, k_divergence<D>, grid_for(h->cells, 256), 256, 0, s, u[0], u[1], D == 3 ? u[2] : nullptr, g, r0);
   rc = launch_check(h, "divergence");
   if (rc) return rc;
-  float* x = p_out ? p_out : ws_ptr<float>(h, h->o_x);
-  int solve_rc = solve_impl<D>(h, x, opts, stats, s);
+  int solve_rc = mgpcg_solve_in_place(h, p_out, opts, stats, s);
+  const float* x = ws_ptr<float>(h, h->o_x);
   if (solve_rc != PFM_OK && solve_rc != PFM_ERR_NOT_CONVERGED) return solve_rc;
   for (int f = 0; f < D; ++f) {
     int64_t nf = (int64_t)g.n[f][0] * g.n[f][1] * g.n[f][2];

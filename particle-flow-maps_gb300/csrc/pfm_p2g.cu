@@ -17,6 +17,7 @@
 namespace pfm {
 
 constexpr int kBinThreads = 256;
+constexpr int kColumn2 = 8;   // faces per thread along j (2D column gather)
 
 // cell key + slot in the bin (slot order is arbitrary here; fixed by k_cell_sort)
 template <int D>
@@ -151,166 +152,287 @@ __global__ void __launch_bounds__(kBinThreads) k_cell_sort(const int* __restrict
   }
 }
 
-// Payload (3D): per sorted slot s, record 0 = pos/dx, records 1..3 = (m_c, (T C T)_c row) for the
-// three face families (3D/run_3D.py:462-479).
+// Payload (3D), structure of float4 arrays in sorted order s:
+//   pos4[s]      = (pos/dx, 0)                         -- read by every visit
+//   famrec[f][s] = (m_f, (T C T)_f row)  f = x, y, z   -- read when the particle reaches the face
+// m = T_gm^T-composed init_imp and T C T = T_gm^T init_C T_gm as in 3D/run_3D.py:462-479.
 __global__ void __launch_bounds__(kBinThreads) k_payload3(const int* __restrict__ order, int64_t P, MacGeom g,
                                                           const float* __restrict__ pos, const float* __restrict__ imp0,
                                                           const float* __restrict__ Tg, const float* __restrict__ Ti,
-                                                          const float* __restrict__ C, float4* __restrict__ pay) {
-  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= P) return;
-  const int64_t q = order[s];
-  float A[3][3], Cm[3][3], N[3][3];
+                                                          const float* __restrict__ C, float4* __restrict__ pos4,
+                                                          float4* __restrict__ famrec) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < P) {
+    const int64_t q = order[s];
+    float A[3][3], Cm[3][3], N[3][3];
 #pragma unroll
-  for (int r = 0; r < 3; ++r)
+    for (int r = 0; r < 3; ++r)
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      A[r][c] = Tg[(r * 3 + c) * P + q];   // rows(T_gm): A[r][c] = T_gm_r[c]
-      Cm[r][c] = C[(r * 3 + c) * P + q];   // rows(init_C)
-      N[c][r] = Ti[(r * 3 + c) * P + q];   // cols(T_init): N[k][c'] = T_init_c'[k]
-    }
-  // TCT = A^T (C A); T_transpose = A^T N; m = T_transpose init_imp
-  float CA[3][3], TCT[3][3], TT[3][3];
+      for (int c = 0; c < 3; ++c) {
+        A[r][c] = Tg[(r * 3 + c) * P + q];   // rows(T_gm): A[r][c] = T_gm_r[c]
+        Cm[r][c] = C[(r * 3 + c) * P + q];   // rows(init_C)
+        N[c][r] = Ti[(r * 3 + c) * P + q];   // cols(T_init): N[k][c'] = T_init_c'[k]
+      }
+    // TCT = A^T (C A); T_transpose = A^T N; m = T_transpose init_imp
+    float CA[3][3], TCT[3][3], TT[3][3];
 #pragma unroll
-  for (int r = 0; r < 3; ++r)
+    for (int r = 0; r < 3; ++r)
 #pragma unroll
-    for (int c = 0; c < 3; ++c) CA[r][c] = Cm[r][0] * A[0][c] + Cm[r][1] * A[1][c] + Cm[r][2] * A[2][c];
+      for (int c = 0; c < 3; ++c) CA[r][c] = Cm[r][0] * A[0][c] + Cm[r][1] * A[1][c] + Cm[r][2] * A[2][c];
 #pragma unroll
-  for (int r = 0; r < 3; ++r)
+    for (int r = 0; r < 3; ++r)
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      TCT[r][c] = A[0][r] * CA[0][c] + A[1][r] * CA[1][c] + A[2][r] * CA[2][c];
-      TT[r][c] = A[0][r] * N[0][c] + A[1][r] * N[1][c] + A[2][r] * N[2][c];
-    }
-  float m0[3] = {imp0[q], imp0[P + q], imp0[2 * P + q]};
-  float m[3];
+      for (int c = 0; c < 3; ++c) {
+        TCT[r][c] = A[0][r] * CA[0][c] + A[1][r] * CA[1][c] + A[2][r] * CA[2][c];
+        TT[r][c] = A[0][r] * N[0][c] + A[1][r] * N[1][c] + A[2][r] * N[2][c];
+      }
+    float m0[3] = {imp0[q], imp0[P + q], imp0[2 * P + q]};
+    float m[3];
 #pragma unroll
-  for (int r = 0; r < 3; ++r) m[r] = TT[r][0] * m0[0] + TT[r][1] * m0[1] + TT[r][2] * m0[2];
-  float4* o = pay + s * 4;
-  o[0] = make_float4(pos[q] / g.dx, pos[P + q] / g.dx, pos[2 * P + q] / g.dx, 0.f);
+    for (int r = 0; r < 3; ++r) m[r] = TT[r][0] * m0[0] + TT[r][1] * m0[1] + TT[r][2] * m0[2];
+    pos4[s] = make_float4(pos[q] / g.dx, pos[P + q] / g.dx, pos[2 * P + q] / g.dx, 0.f);
 #pragma unroll
-  for (int f = 0; f < 3; ++f) o[1 + f] = make_float4(m[f], TCT[f][0], TCT[f][1], TCT[f][2]);
+    for (int f = 0; f < 3; ++f) famrec[f * P + s] = make_float4(m[f], TCT[f][0], TCT[f][1], TCT[f][2]);
+  }
 }
 
-// Payload (2D): record 0 = (pos/dx, psi), records 1..2 = (imp_c, C_c row, 0)
+// Payload (2D): pos4 = (pos/dx, psi), famrec[f] = (imp_f, C_f row, 0)
 __global__ void __launch_bounds__(kBinThreads) k_payload2(const int* __restrict__ order, int64_t P, MacGeom g,
                                                           const float* __restrict__ pos, const float* __restrict__ imp,
                                                           const float* __restrict__ C, const float* __restrict__ psi,
-                                                          float4* __restrict__ pay) {
+                                                          float4* __restrict__ pos4, float4* __restrict__ famrec) {
   int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= P) return;
   const int64_t q = order[s];
-  float4* o = pay + s * 3;
-  o[0] = make_float4(pos[q] / g.dx, pos[P + q] / g.dx, psi ? psi[q] : 0.f, psi ? psi[P + q] : 0.f);
-  o[1] = make_float4(imp[q], C[q], C[P + q], 0.f);
-  o[2] = make_float4(imp[P + q], C[2 * P + q], C[3 * P + q], 0.f);
+  pos4[s] = make_float4(pos[q] / g.dx, pos[P + q] / g.dx, psi ? psi[q] : 0.f, psi ? psi[P + q] : 0.f);
+  famrec[s] = make_float4(imp[q], C[q], C[P + q], 0.f);
+  famrec[P + s] = make_float4(imp[P + q], C[2 * P + q], C[3 * P + q], 0.f);
 }
 
-// per-face gather (3D), one face family per launch
+// Column gather (3D).  One thread owns the faces (i, j, k0 .. k0+K-1) of family `fam` and walks
+// the cell layers ck in increasing order; a particle of layer ck reaches the faces ck-1..ck+1
+// along k (ck-1..ck+2 when k is the family's own axis), so the open faces live in a rolling
+// register window and a face is final once the walk has passed it.  Per face the sum runs over
+// layers ck, then the neighbourhood cells (ci, cj) in lexicographic order (family axis
+// idx-2..idx+1, offset axes idx-1..idx+1), then particles in index order.
+constexpr int kColumn3 = 32;  // faces per thread along k
+
 template <int fam>
-__global__ void __launch_bounds__(128) k_gather3(const float4* __restrict__ pay, const int* __restrict__ start,
-                                                 MacGeom g, int use_apic, float* __restrict__ u,
-                                                 float* __restrict__ w) {
+__device__ __forceinline__ void window_weights(float pz, int ck, int kb, float dx, float* wk, float* dk) {
+  constexpr int WIN = (fam == 2) ? 4 : 3;
+  const float fz = pz - (float)ck;
+  if (fz >= 0.f && fz < 1.f) {  // closed form of the N_2 branches about the particle's layer
+    if (fam == 2) {  // faces ck-1 .. ck+2 at x = fz+1, fz, fz-1, fz-2
+      const bool lo = fz < 0.5f;
+      const float t = lo ? fz : fz - 1.f;
+      const float l = 0.5f - t, r = 0.5f + t;
+      const float w0 = 0.5f * (l * l), w1 = 0.75f - t * t, w2 = 0.5f * (r * r);
+      wk[0] = lo ? w0 : 0.f;
+      wk[1] = lo ? w1 : w0;
+      wk[2] = lo ? w2 : w1;
+      wk[WIN - 1] = lo ? 0.f : w2;
+    } else {  // faces ck-1 .. ck+1 at (x - 1/2) = t+1, t, t-1 with t = fz - 1/2
+      const float t = fz - 0.5f;
+      const float l = 0.5f - t, r = 0.5f + t;
+      wk[0] = 0.5f * (l * l);
+      wk[1] = 0.75f - t * t;
+      wk[2] = 0.5f * (r * r);
+    }
+  } else {  // outside the grid along k: per-face N_2
+#pragma unroll
+    for (int q = 0; q < WIN; ++q) {
+      const float fk = (float)(kb + q);
+      wk[q] = (fam == 2) ? N2(pz - fk) : N2((pz - fk) - 0.5f);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < WIN; ++q) {
+    const float fk = (float)(kb + q);
+    dk[q] = ((fam == 2) ? (fk - pz) : ((fk + 0.5f) - pz)) * dx;
+  }
+}
+
+template <int fam>
+__global__ void __launch_bounds__(128, 6) k_gather3(const float4* __restrict__ pos4, const float4* __restrict__ famrec,
+                                                 const int* __restrict__ start, MacGeom g, int K, int use_apic,
+                                                 int64_t P, float* __restrict__ u, float* __restrict__ w) {
+  constexpr int WIN = (fam == 2) ? 4 : 3;
   const int n0 = g.n[fam][0], n1 = g.n[fam][1], n2 = g.n[fam][2];
-  const int64_t nf = (int64_t)n0 * n1 * n2;
-  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= nf) return;
-  int f[3];
-  f[2] = (int)(e % n2);
-  int64_t t = e / n2;
-  f[1] = (int)(t % n1);
-  f[0] = (int)(t / n1);
-  int lo[3], hi[3];
-
+  const int nseg = (n2 + K - 1) / K;
+  const int64_t ncol = (int64_t)n0 * n1 * nseg;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncol) return;
+  const int j = (int)(t % n1);  // neighbouring threads run along j and share cells
+  const int64_t r = t / n1;
+  const int i = (int)(r % n0);
+  const int seg = (int)(r / n0);
+  const int k0 = seg * K, k1 = min(k0 + K, n2);
+  const int G0 = g.N[0], G1 = g.N[1], G2 = g.N[2];
+  const int ci_lo = max(i - (fam == 0 ? 2 : 1), 0), ci_hi = min(i + 1, G0 - 1);
+  const int cj_lo = max(j - (fam == 1 ? 2 : 1), 0), cj_hi = min(j + 1, G1 - 1);
+  const int ck_lo = max(k0 - (fam == 2 ? 2 : 1), 0), ck_hi = min(k1, G2 - 1);
+  const float fi = (float)i, fj = (float)j;
+  const float dx = g.dx;
+  const float4* fam_rec = famrec + (int64_t)fam * P;
+  float num[WIN], den[WIN];
 #pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    lo[a] = f[a] - (a == fam ? 2 : 1);
-    hi[a] = f[a] + 1;
-    lo[a] = lo[a] < 0 ? 0 : lo[a];
-    hi[a] = hi[a] > g.N[a] - 1 ? g.N[a] - 1 : hi[a];
-
-  }
-  const float ff[3] = {(float)f[0], (float)f[1], (float)f[2]};
-  float num = 0.f, den = 0.f;
-  for (int ci = lo[0]; ci <= hi[0]; ++ci)
-    for (int cj = lo[1]; cj <= hi[1]; ++cj) {
-      const int rowc = (ci * g.N[1] + cj) * g.N[2];
-      const int sb = __ldg(start + rowc + lo[2]), se = __ldg(start + rowc + hi[2] + 1);
-      for (int s = sb; s < se; ++s) {  // the cells of a (ci, cj) row are contiguous in sorted order
-        const float4 p0 = __ldg(pay + (int64_t)s * 4);
-        const float pp[3] = {p0.x, p0.y, p0.z};
-        float wgt = 1.f;
-        float dp[3];
+  for (int q = 0; q < WIN; ++q) num[q] = den[q] = 0.f;
+  int kb = ck_lo - 1;  // window slot q holds face kb + q
+  auto store = [&](int kf, float a, float b) {
+    if (kf >= k0 && kf < k1) {
+      const int64_t e = ((int64_t)i * n1 + j) * n2 + kf;
+      w[e] = b;
+      u[e] = b > 0.f ? a / b : a;  // 3D normalises by division (run_3D.py:530-552)
+    }
+  };
+  for (int ck = ck_lo; ck <= ck_hi; ++ck) {
+    while (kb < ck - 1) {
+      store(kb, num[0], den[0]);
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          float arg = (a == fam) ? (pp[a] - ff[a]) : ((pp[a] - ff[a]) - 0.5f);
-          wgt *= N2(arg);
-          dp[a] = ((a == fam) ? (ff[a] - pp[a]) : ((ff[a] + 0.5f) - pp[a])) * g.dx;
+      for (int q = 0; q < WIN - 1; ++q) {
+        num[q] = num[q + 1];
+        den[q] = den[q + 1];
+      }
+      num[WIN - 1] = den[WIN - 1] = 0.f;
+      ++kb;
+    }
+    for (int ci = ci_lo; ci <= ci_hi; ++ci) {
+      for (int cj = cj_lo; cj <= cj_hi; ++cj) {
+        const int c = (ci * G1 + cj) * G2 + ck;
+        const int sb = __ldg(start + c), se = __ldg(start + c + 1);
+        for (int s = sb; s < se; ++s) {
+          const float4 p = __ldg(pos4 + s);
+          // weights and offsets along i and j (3D/run_3D.py:486-487 and the twins for y, z)
+          float wi, wj, di, dj;
+          if (fam == 0) {
+            wi = N2(p.x - fi);
+            di = (fi - p.x) * dx;
+          } else {
+            wi = N2((p.x - fi) - 0.5f);
+            di = ((fi + 0.5f) - p.x) * dx;
+          }
+          if (fam == 1) {
+            wj = N2(p.y - fj);
+            dj = (fj - p.y) * dx;
+          } else {
+            wj = N2((p.y - fj) - 0.5f);
+            dj = ((fj + 0.5f) - p.y) * dx;
+          }
+          const float wij = wi * wj;
+          if (wij == 0.f) continue;
+          const float4 fr = __ldg(fam_rec + s);
+          const float d01 = fr.y * di + fr.z * dj;
+          float wk[WIN], dk[WIN];
+          window_weights<fam>(p.z, ck, kb, dx, wk, dk);
+#pragma unroll
+          for (int q = 0; q < WIN; ++q) {
+            const float wt = wij * wk[q];
+            const float delta = d01 + fr.w * dk[q];
+            num[q] += (use_apic ? (fr.x + delta) : fr.x) * wt;
+            den[q] += wt;
+          }
         }
-        if (wgt == 0.f) continue;
-        const float4 pf = __ldg(pay + (int64_t)s * 4 + 1 + fam);
-        float delta = pf.y * dp[0] + pf.z * dp[1] + pf.w * dp[2];
-        den += wgt;
-        num += (use_apic ? (pf.x + delta) : pf.x) * wgt;
       }
     }
-  w[e] = den;
-  u[e] = den > 0.f ? num / den : num;  // 3D normalises by division (run_3D.py:530-552)
+  }
+#pragma unroll
+  for (int q = 0; q < WIN; ++q) store(kb + q, num[q], den[q]);
 }
 
+// Column gather (2D): columns along j; 2D normalises with scale = 1/w (run_2D.py:599-611) and
+// also carries the reference map psi.
 template <int fam>
-__global__ void __launch_bounds__(128) k_gather2(const float4* __restrict__ pay, const int* __restrict__ start,
-                                                 MacGeom g, int use_apic, float* __restrict__ u,
-                                                 float* __restrict__ w, float* __restrict__ psig) {
+__global__ void __launch_bounds__(128) k_gather2(const float4* __restrict__ pos4, const float4* __restrict__ famrec,
+                                                 const int* __restrict__ start, MacGeom g, int K, int use_apic,
+                                                 int64_t P, float* __restrict__ u, float* __restrict__ w,
+                                                 float* __restrict__ psig) {
+  constexpr int WIN = (fam == 1) ? 4 : 3;
   const int n0 = g.n[fam][0], n1 = g.n[fam][1];
-  const int64_t nf = (int64_t)n0 * n1;
-  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= nf) return;
-  int f[2] = {(int)(e / n1), (int)(e % n1)};
-  int lo[2], hi[2];
+  const int nseg = (n1 + K - 1) / K;
+  const int64_t ncol = (int64_t)n0 * nseg;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncol) return;
+  const int i = (int)(t % n0);
+  const int seg = (int)(t / n0);
+  const int j0 = seg * K, j1 = min(j0 + K, n1);
+  const int G0 = g.N[0], G1 = g.N[1];
+  const int ci_lo = max(i - (fam == 0 ? 2 : 1), 0), ci_hi = min(i + 1, G0 - 1);
+  const int cj_lo = max(j0 - (fam == 1 ? 2 : 1), 0), cj_hi = min(j1, G1 - 1);
+  const float fi = (float)i, dx = g.dx;
+  float num[WIN], den[WIN], s0[WIN], s1[WIN];
 #pragma unroll
-  for (int a = 0; a < 2; ++a) {
-    lo[a] = f[a] - (a == fam ? 2 : 1);
-    hi[a] = f[a] + 1;
-    lo[a] = lo[a] < 0 ? 0 : lo[a];
-    hi[a] = hi[a] > g.N[a] - 1 ? g.N[a] - 1 : hi[a];
-  }
-  const float ff[2] = {(float)f[0], (float)f[1]};
-  float num = 0.f, den = 0.f, s0 = 0.f, s1 = 0.f;
-  for (int ci = lo[0]; ci <= hi[0]; ++ci) {
-    const int rowc = ci * g.N[1];
-    const int sb = __ldg(start + rowc + lo[1]), se = __ldg(start + rowc + hi[1] + 1);
-    for (int s = sb; s < se; ++s) {
-      const float4 p0 = __ldg(pay + (int64_t)s * 3);
-      const float pp[2] = {p0.x, p0.y};
-      float wgt = 1.f, dp[2];
-#pragma unroll
-      for (int a = 0; a < 2; ++a) {
-        float arg = (a == fam) ? (pp[a] - ff[a]) : ((pp[a] - ff[a]) - 0.5f);
-        wgt *= N2(arg);
-        dp[a] = ((a == fam) ? (ff[a] - pp[a]) : ((ff[a] + 0.5f) - pp[a])) * g.dx;
+  for (int q = 0; q < WIN; ++q) num[q] = den[q] = s0[q] = s1[q] = 0.f;
+  auto flush = [&](int jf, int q) {
+    if (jf >= j0 && jf < j1) {
+      const int64_t e = (int64_t)i * n1 + jf;
+      float a = num[q], b0 = s0[q], b1 = s1[q];
+      if (den[q] > 0.f) {
+        float scale = 1.f / den[q];
+        a *= scale;
+        b0 *= scale;
+        b1 *= scale;
       }
-      if (wgt == 0.f) continue;
-      const float4 pf = __ldg(pay + (int64_t)s * 3 + 1 + fam);
-      float delta = pf.y * dp[0] + pf.z * dp[1];
-      den += wgt;
-      num += (use_apic ? (pf.x + delta) : pf.x) * wgt;
-      s0 += p0.z * wgt;
-      s1 += p0.w * wgt;
+      w[e] = den[q];
+      u[e] = a;
+      if (psig) {
+        psig[e * 2] = b0;
+        psig[e * 2 + 1] = b1;
+      }
+    }
+  };
+  int jb = cj_lo - 1;
+  for (int cj = cj_lo; cj <= cj_hi; ++cj) {
+    while (jb < cj - 1) {
+      flush(jb, 0);
+#pragma unroll
+      for (int q = 0; q < WIN - 1; ++q) {
+        num[q] = num[q + 1];
+        den[q] = den[q + 1];
+        s0[q] = s0[q + 1];
+        s1[q] = s1[q + 1];
+      }
+      num[WIN - 1] = den[WIN - 1] = s0[WIN - 1] = s1[WIN - 1] = 0.f;
+      ++jb;
+    }
+    const float fj0 = (float)(cj - 1);
+    for (int ci = ci_lo; ci <= ci_hi; ++ci) {
+      const int c = ci * G1 + cj;
+      const int sb = __ldg(start + c), se = __ldg(start + c + 1);
+      for (int s = sb; s < se; ++s) {
+        const float4 p = __ldg(pos4 + s);
+        float wi, di;
+        if (fam == 0) {
+          wi = N2(p.x - fi);
+          di = (fi - p.x) * dx;
+        } else {
+          wi = N2((p.x - fi) - 0.5f);
+          di = ((fi + 0.5f) - p.x) * dx;
+        }
+        if (wi == 0.f) continue;
+        const float4 fr = __ldg(famrec + (int64_t)fam * P + s);
+#pragma unroll
+        for (int q = 0; q < WIN; ++q) {
+          const float fj = fj0 + (float)q;
+          float wj, dj;
+          if (fam == 1) {
+            wj = N2(p.y - fj);
+            dj = (fj - p.y) * dx;
+          } else {
+            wj = N2((p.y - fj) - 0.5f);
+            dj = ((fj + 0.5f) - p.y) * dx;
+          }
+          const float wt = wi * wj;
+          const float delta = fr.y * di + fr.z * dj;
+          num[q] += (use_apic ? (fr.x + delta) : fr.x) * wt;
+          den[q] += wt;
+          s0[q] += p.z * wt;
+          s1[q] += p.w * wt;
+        }
+      }
     }
   }
-  w[e] = den;
-  if (den > 0.f) {  // 2D normalises with scale = 1/w (run_2D.py:599-611)
-    float scale = 1.f / den;
-    num *= scale;
-    s0 *= scale;
-    s1 *= scale;
-  }
-  u[e] = num;
-  if (psig) {
-    psig[e * 2] = s0;
-    psig[e * 2 + 1] = s1;
-  }
+#pragma unroll
+  for (int q = 0; q < WIN; ++q) flush(jb + q, q);
 }
 
 int sort_particles(pfm_handle* h, const float* pos, cudaStream_t st) {
@@ -393,18 +515,24 @@ int pfm3_p2g(pfm_handle* h, const float* init_imp, const float* pos, const float
   cudaStream_t st = (cudaStream_t)stream;
   int rc = sort_particles(h, pos, st);
   if (rc) return rc;
-  float4* pay = ws_ptr<float4>(h, h->o_payload);
-  if (h->P > 0)
-    launch(h, k_payload3, grid_for(h->P, kBinThreads), kBinThreads, 0, st, ws_ptr<int>(h, h->o_order), h->P, h->geom, pos,
-                                                                    init_imp, T_gm, T_init, init_C, pay);
+  float4* pos4 = ws_ptr<float4>(h, h->o_payload);
+  float4* famrec = pos4 + h->P;
   float* us[3] = {u_x, u_y, u_z};
   float* ws[3] = {w_x, w_y, w_z};
+  const int* start = ws_ptr<int>(h, h->o_start);
+  if (h->P > 0)
+    launch(h, k_payload3, grid_for(h->P, kBinThreads), kBinThreads, 0, st, ws_ptr<int>(h, h->o_order), h->P, h->geom,
+           pos, init_imp, T_gm, T_init, init_C, pos4, famrec);
   for (int f = 0; f < 3; ++f) {
-    int64_t nf = (int64_t)h->geom.n[f][0] * h->geom.n[f][1] * h->geom.n[f][2];
-    const int* start = ws_ptr<int>(h, h->o_start);
-    if (f == 0) launch(h, k_gather3<0>, grid_for(nf, 128), 128, 0, st, pay, start, h->geom, h->cfg.use_apic, us[f], ws[f]);
-    if (f == 1) launch(h, k_gather3<1>, grid_for(nf, 128), 128, 0, st, pay, start, h->geom, h->cfg.use_apic, us[f], ws[f]);
-    if (f == 2) launch(h, k_gather3<2>, grid_for(nf, 128), 128, 0, st, pay, start, h->geom, h->cfg.use_apic, us[f], ws[f]);
+    const int n2 = h->geom.n[f][2];
+    const int K = n2 < kColumn3 ? n2 : kColumn3;
+    const int64_t ncol = (int64_t)h->geom.n[f][0] * h->geom.n[f][1] * ((n2 + K - 1) / K);
+    if (f == 0) launch(h, k_gather3<0>, grid_for(ncol, 128), 128, 0, st, pos4, famrec, start, h->geom, K,
+                       h->cfg.use_apic, h->P, us[f], ws[f]);
+    if (f == 1) launch(h, k_gather3<1>, grid_for(ncol, 128), 128, 0, st, pos4, famrec, start, h->geom, K,
+                       h->cfg.use_apic, h->P, us[f], ws[f]);
+    if (f == 2) launch(h, k_gather3<2>, grid_for(ncol, 128), 128, 0, st, pos4, famrec, start, h->geom, K,
+                       h->cfg.use_apic, h->P, us[f], ws[f]);
   }
   return launch_check(h, "pfm3_p2g");
 }
@@ -419,18 +547,23 @@ int pfm2_p2g(pfm_handle* h, const float* imp, const float* pos, const float* C, 
   cudaStream_t st = (cudaStream_t)stream;
   int rc = sort_particles(h, pos, st);
   if (rc) return rc;
-  float4* pay = ws_ptr<float4>(h, h->o_payload);
+  float4* pos4 = ws_ptr<float4>(h, h->o_payload);
+  float4* famrec = pos4 + h->P;
   if (h->P > 0)
-    launch(h, k_payload2, grid_for(h->P, kBinThreads), kBinThreads, 0, st, ws_ptr<int>(h, h->o_order), h->P, h->geom, pos,
-                                                                    imp, C, psi, pay);
+    launch(h, k_payload2, grid_for(h->P, kBinThreads), kBinThreads, 0, st, ws_ptr<int>(h, h->o_order), h->P, h->geom,
+           pos, imp, C, psi, pos4, famrec);
   float* us[2] = {u_x, u_y};
   float* ws[2] = {w_x, w_y};
   float* ps[2] = {psi_x, psi_y};
+  const int* start = ws_ptr<int>(h, h->o_start);
   for (int f = 0; f < 2; ++f) {
-    int64_t nf = (int64_t)h->geom.n[f][0] * h->geom.n[f][1];
-    const int* start = ws_ptr<int>(h, h->o_start);
-    if (f == 0) launch(h, k_gather2<0>, grid_for(nf, 128), 128, 0, st, pay, start, h->geom, h->cfg.use_apic, us[f], ws[f], ps[f]);
-    if (f == 1) launch(h, k_gather2<1>, grid_for(nf, 128), 128, 0, st, pay, start, h->geom, h->cfg.use_apic, us[f], ws[f], ps[f]);
+    const int n1 = h->geom.n[f][1];
+    const int K = n1 < kColumn2 ? n1 : kColumn2;
+    const int64_t ncol = (int64_t)h->geom.n[f][0] * ((n1 + K - 1) / K);
+    if (f == 0) launch(h, k_gather2<0>, grid_for(ncol, 128), 128, 0, st, pos4, famrec, start, h->geom, K,
+                       h->cfg.use_apic, h->P, us[f], ws[f], ps[f]);
+    if (f == 1) launch(h, k_gather2<1>, grid_for(ncol, 128), 128, 0, st, pos4, famrec, start, h->geom, K,
+                       h->cfg.use_apic, h->P, us[f], ws[f], ps[f]);
   }
   return launch_check(h, "pfm2_p2g");
 }

@@ -1,0 +1,144 @@
+"""Whole-step parity on the GPU: pfm.Sim3D / pfm.Sim2D against the reference's own main() runs
+(tests/golden/ref*_steps.npz) and against the oracle's step loop at larger sizes.
+
+Bar: grid velocity and particle impulse agree within 1e-5 relative L2 after 1 and 10 steps,
+positions within 1e-6.  Pressure (all-Neumann null-space constant removed) is held to 1e-5 per
+solve (tests/test_gpu_phases.py) and to 2e-5 along multi-step runs: the reference stops MGPCG at
+the absolute residual r.r < 1e-12 (3D/mgpcg.py:255, 422), which pins the pressure only to about
+1e-5 relative at these sizes (the oracle itself differs from the reference by up to 7e-6)."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import oracle as O  # noqa: E402
+import pfm  # noqa: E402
+
+TOL = 1e-5
+PTOL = 2e-5
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    d = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / (d if d > 0 else 1.0))
+
+
+def prel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return rel(a - a.mean(), b - b.mean())
+
+
+def host(t):
+    return t.detach().cpu().numpy()
+
+
+def test_step3d_vs_reference_main(golden):
+    g = golden("ref3d_steps")
+    res = tuple(int(r) for r in g["res"])
+    dx = 1.0 / res[1]
+    sim = pfm.Sim3D([g["init_u_x"], g["init_u_y"], g["init_u_z"]], pfm.lattice3(res, dx), res, dx, CFL=0.5,
+                    visualize_dt=0.1, reinit_every=int(g["hp"][0]), reinit_every_grad_m=int(g["hp"][1]))
+    for s in range(1, 11):
+        sim.step()
+        for f, n in enumerate("xyz"):
+            assert rel(host(sim.u[f]), g[f"s{s}_u_{n}"]) < TOL, (s, n)
+        assert prel(host(sim.p), g[f"s{s}_p"]) < PTOL, s
+        if f"s{s}_particles_pos" in g:
+            assert rel(pfm.aos(sim.pos), g[f"s{s}_particles_pos"]) < 1e-6
+            assert rel(pfm.aos(sim.init_imp), g[f"s{s}_particles_init_imp"]) < TOL
+            T_init = np.stack([g[f"s{s}_T_{v}_init"] for v in "xyz"], 1)
+            assert rel(pfm.aos_T(sim.T_init), T_init) < TOL
+    assert [i.iterations for i in sim.infos] == [int(i) for i in g["iters"][1:]]
+
+
+def test_step2d_vs_reference_main(golden):
+    g = golden("ref2d_steps")
+    res = tuple(int(r) for r in g["res"])
+    dx = 1.0 / res[1]
+    sim = pfm.Sim2D([g["init_u_x"], g["init_u_y"]], pfm.lattice2(res, dx, 4), res, dx, CFL=0.5, visualize_dt=0.1,
+                    reinit_every=int(g["hp"][0]), reinit_every_grad_m=int(g["hp"][1]))
+    for s in range(1, 21):
+        sim.step()
+        assert rel(host(sim.u[0]), g[f"s{s}_u_x"]) < TOL and rel(host(sim.u[1]), g[f"s{s}_u_y"]) < TOL, s
+        assert prel(host(sim.p), g[f"s{s}_p"]) < PTOL, s
+        if f"s{s}_particles_pos" in g:
+            assert rel(pfm.aos(sim.pos), g[f"s{s}_particles_pos"]) < 1e-6
+            assert rel(pfm.aos(sim.imp), g[f"s{s}_particles_imp"]) < TOL
+            assert rel(pfm.aos_T(sim.C), np.stack([g[f"s{s}_C_x"], g[f"s{s}_C_y"]], 1)) < TOL
+    assert [i.iterations for i in sim.infos] == [int(i) for i in g["iters"][1:]]
+
+
+def _ring_u(res, dx):
+    import __graft_entry__ as G
+    return G._ring_velocity(res, dx)
+
+
+@pytest.mark.parametrize("res", [(32, 32, 32), (48, 32, 32)])
+def test_step3d_vs_oracle_10_steps(res):
+    dx = 1.0 / res[1]
+    u0 = _ring_u(res, dx)
+    seeds = pfm.jittered(res, dx, 8, seed=0)
+    kw = dict(CFL=0.5, visualize_dt=0.1, reinit_every=6, reinit_every_grad_m=2)
+    gpu = pfm.Sim3D(u0, seeds, res, dx, **kw)
+    ref = O.Sim3D(u0, seeds, res, dx, **kw)
+    for s in range(1, 11):
+        gpu.step()
+        ref.step()
+        if s in (1, 10):
+            for f in range(3):
+                assert rel(host(gpu.u[f]), ref.u[f]) < TOL, (s, f)
+            assert prel(host(gpu.p), ref.p) < PTOL, s
+            assert rel(pfm.aos(gpu.pos), ref.pos) < 1e-6
+            assert rel(pfm.aos(gpu.init_imp), ref.init_imp) < TOL
+            assert rel(pfm.aos_T(gpu.T_gm), ref.T_gm) < TOL
+    assert all(abs(a.iterations - b) <= 1 for a, b in zip(gpu.infos, ref.iters))
+
+
+def test_step2d_vs_oracle_10_steps():
+    res = (128, 64)
+    dx = 1.0 / res[1]
+    rng = np.random.default_rng(5)
+    u0 = []
+    for fam in range(2):
+        shp = (res[0] + (fam == 0), res[1] + (fam == 1))
+        x, y = np.meshgrid(np.arange(shp[0]) / shp[0], np.arange(shp[1]) / shp[1], indexing="ij")
+        u0.append((0.3 * np.sin(2 * np.pi * (x + rng.uniform())) * np.cos(2 * np.pi * (y + rng.uniform()))).astype(np.float32))
+    ux, uy, _, _, _ = O.poisson2(*u0)
+    seeds = pfm.jittered(res, dx, 4, seed=0)
+    kw = dict(CFL=0.5, visualize_dt=0.1, reinit_every=12, reinit_every_grad_m=8)
+    gpu = pfm.Sim2D([ux, uy], seeds, res, dx, **kw)
+    ref = O.Sim2D([ux, uy], seeds, res, dx, **kw)
+    for s in range(1, 11):
+        gpu.step()
+        ref.step()
+        if s in (1, 10):
+            for f in range(2):
+                assert rel(host(gpu.u[f]), ref.u[f]) < TOL, (s, f)
+            assert prel(host(gpu.p), ref.p) < PTOL
+            assert rel(pfm.aos(gpu.imp), ref.imp) < TOL
+            assert rel(pfm.aos(gpu.pos), ref.pos) < 1e-6
+
+
+def test_step3d_divergence_free_and_deterministic():
+    """Size-independent properties at a bench-like size: the projected velocity is discretely
+    divergence free to the solver tolerance, and the step is bitwise reproducible."""
+    res = (64, 64, 64)
+    dx = 1.0 / 64
+    u0 = _ring_u(res, dx)
+    seeds = pfm.jittered(res, dx, 8, seed=0)
+    outs = []
+    for _ in range(2):
+        sim = pfm.Sim3D(u0, seeds, res, dx, poisson_opts=dict(tol=1e-6, tol_mode=1))
+        sim.step()
+        sim.step()
+        outs.append([host(t) for t in sim.u] + [host(sim.p), pfm.aos(sim.pos)])
+        ux, uy, uz = (np.float64(host(t)) for t in sim.u)
+        div = (ux[1:] - ux[:-1]) + (uy[:, 1:] - uy[:, :-1]) + (uz[:, :, 1:] - uz[:, :, :-1])
+        ref_div = np.abs(np.diff(np.float64(u0[0]), axis=0)).max()
+        assert np.abs(div).max() < 1e-3 * max(ref_div, 1e-6)
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
