@@ -169,6 +169,27 @@ int pfm2_reset_T(pfm_handle* h, float* T, void* stream);
 int pfm2_midpoint(pfm_handle* h, const float* u0_x, const float* u0_y, float* u1_x, float* u1_y,
                   float dt_half, float* psi_out[2], float* T_out[2], void* stream);
 int pfm2_sort_particles(pfm_handle* h, const float* pos, int* cell_count, int* order, void* stream);
+
+/* Particle binning that allocates nothing (no counterpart in the reference, which sorts inside a
+ * Taichi kernel on fields it allocated itself).  For callers that must not allocate device memory
+ * at all: code running inside a host allocator's or framework's own memory callbacks, embedders
+ * whose pools own every byte of the device, or anyone without a pfm_handle (pfm_create and the
+ * workspace both allocate).  Same result as pfm3_sort_particles / pfm2_sort_particles, bit for
+ * bit: cell_count [C] int32 (C = product of res[0..dim)) and order [P] int32, the stable
+ * permutation by int(pos/dx) clamped to the grid.  pos [dim][P] f32.
+ *
+ * Scratch is one fixed array inside the library's device image, so the sizes are bounded:
+ * particles <= PFM_NOALLOC_MAX_PARTICLES and C <= PFM_NOALLOC_MAX_CELLS, else PFM_ERR_SHAPE
+ * (nothing launched).  Every call on a device shares that array and leaves its last contents
+ * there; calls that overlap in time (two streams, two host threads) race on it and must be
+ * serialised by the caller.  The first call on each device (that device current) looks up the
+ * array's address; make that first call before any stream capture.
+ * Returns PFM_ERR_ARG (dim not 2/3, dx <= 0, particles < 0), PFM_ERR_NULL, PFM_ERR_SHAPE or
+ * PFM_ERR_CUDA (launch error). */
+#define PFM_NOALLOC_MAX_PARTICLES (1 << 21)
+#define PFM_NOALLOC_MAX_CELLS (1 << 18)
+int pfm_sort_particles_noalloc(int dim, const int res[3], double dx, int64_t particles, const float* pos,
+                               int* cell_count, int* order, void* stream);
 /* P2G (2D/run_2D.py:548-611): impulse with APIC C [2][2][P] and the reference map psi [2][P]
  * (psi_x/psi_y grids [F][2] may be NULL). */
 int pfm2_p2g(pfm_handle* h, const float* imp, const float* pos, const float* C, const float* psi,

@@ -5,8 +5,9 @@ Host-side mirror of the reference solver's step phases (zjw49246/particle-flow-m
 ctypes; torch tensors are only device buffers.  There is no CPU fallback.
 """
 from ._lib import PfmError, exported_symbols, lib_path, load
-from .core import Scene, SolveInfo
+from .core import Scene, SolveInfo, sort_particles_noalloc
 from .sim import (DtClock, Sim2D, Sim3D, aos, aos_T, jittered, lattice2, lattice3, soa, soa_T)
 
 __all__ = ["PfmError", "Scene", "SolveInfo", "Sim2D", "Sim3D", "DtClock", "soa", "aos", "soa_T", "aos_T",
-           "lattice2", "lattice3", "jittered", "load", "lib_path", "exported_symbols"]
+           "lattice2", "lattice3", "jittered", "load", "lib_path", "exported_symbols",
+           "sort_particles_noalloc"]

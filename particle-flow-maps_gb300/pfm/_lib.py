@@ -74,7 +74,11 @@ SIGNATURES = {
     "pfm2_p2g": [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "pfm2_poisson": [_P, _P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats), _P],
     "pfm_mgpcg_solve": [_P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats), _P],
+    "pfm_sort_particles_noalloc": [_I, ctypes.POINTER(_I), ctypes.c_double, ctypes.c_int64, _P, _P, _P, _P],
 }
+# scratch limits of pfm_sort_particles_noalloc (include/pfm.h)
+NOALLOC_MAX_PARTICLES = 1 << 21
+NOALLOC_MAX_CELLS = 1 << 18
 _RESTYPE = {"pfm_last_error": ctypes.c_char_p, "pfm_status_string": ctypes.c_char_p}
 
 _lib = None

@@ -12,7 +12,7 @@ import torch
 from . import _lib
 from ._lib import PfmError, SolveOpts, SolveStats
 
-__all__ = ["Scene", "PfmError", "SolveInfo"]
+__all__ = ["Scene", "PfmError", "SolveInfo", "sort_particles_noalloc"]
 
 
 class SolveInfo:
@@ -332,3 +332,32 @@ class Scene:
         st = self._check(self.lib.pfm_mgpcg_solve(self.h, _ptr(div), _ptr(x_out), ctypes.byref(o), ctypes.byref(s),
                                                   self._stream()), allow=(_lib.PFM_ERR_NOT_CONVERGED,))
         return SolveInfo(s, st)
+
+
+def sort_particles_noalloc(pos, res, dx, cell_count, order):
+    """Particle binning through ``pfm_sort_particles_noalloc``: the library allocates nothing
+    (no handle, no workspace) and writes into the caller's ``cell_count`` (int32, ``prod(res)``
+    entries) and ``order`` (int32, ``P`` entries).  Same result as :meth:`Scene.sort_particles`.
+
+    Bounded by the library's fixed scratch: ``P <= NOALLOC_MAX_PARTICLES`` and
+    ``prod(res) <= NOALLOC_MAX_CELLS``.  Calls share that scratch: do not run two at once."""
+    dim = len(res)
+    P = int(pos.shape[1]) if pos.dim() == 2 else -1
+    if dim not in (2, 3) or pos.dim() != 2 or pos.shape[0] != dim:
+        raise PfmError(7, f"pos must be [{dim}, P] for a {dim}D grid, got {tuple(pos.shape)}")
+    cells = 1
+    for r in res:
+        cells *= int(r)
+    if P > _lib.NOALLOC_MAX_PARTICLES or cells > _lib.NOALLOC_MAX_CELLS:
+        raise PfmError(2, f"no-alloc binning holds at most {_lib.NOALLOC_MAX_PARTICLES} particles and "
+                          f"{_lib.NOALLOC_MAX_CELLS} cells, got {P} particles and {cells} cells")
+    for name, t, n, dt in (("pos", pos, None, torch.float32), ("cell_count", cell_count, cells, torch.int32),
+                           ("order", order, P, torch.int32)):
+        if t.dtype != dt or not t.is_cuda or not t.is_contiguous() or (n is not None and t.numel() < n):
+            raise PfmError(2, f"{name} must be a contiguous CUDA {dt} tensor"
+                              + (f" with at least {n} entries" if n is not None else ""))
+    r = (ctypes.c_int * 3)(*(list(int(x) for x in res) + [1] * (3 - dim)))
+    st = _lib.load().pfm_sort_particles_noalloc(dim, r, float(dx), P, _ptr(pos), _ptr(cell_count), _ptr(order),
+                                                 ctypes.c_void_p(torch.cuda.current_stream(pos.device).cuda_stream))
+    if st != 0:
+        raise PfmError(st, "pfm_sort_particles_noalloc failed")
