@@ -6,12 +6,13 @@
 //     sort with one digit of radix = number of cells bins the particles; each bin is then put in
 //     particle-index order, so the permutation equals a stable CPU sort of the same keys;
 //  2. a payload pass evaluates each particle's impulse m = T_gm^T-composed init_imp and affine
-//     matrix T_gm^T C T_gm once, in sorted order (AoS float4 records);
-//  3. one thread per face gathers, in (cell, particle-index) order, every particle of the cells
-//     that can reach the face: for the face's own axis the cells idx-2..idx+1, for the others
-//     idx-1..idx+1 (|x| < 1.5 support of N_2).  Particles outside the grid keep a clamped key,
-//     which stays inside every neighbourhood they can reach, and their weights come from their
-//     real positions, exactly as the reference's bounds-checked scatter.
+//     matrix T_gm^T C T_gm once, in sorted order (float4 records);
+//  3. 3D: one thread per cell sums its particles into the window of faces they reach and cell
+//     tiles merge the windows in shared memory in a fixed order (k_tile3); 2D: one thread per
+//     face column gathers the particles of the cells that reach it (k_gather2).
+//     Particles outside the grid keep a clamped key, which stays inside every neighbourhood they
+//     can reach, and their weights come from their real positions, exactly as the reference's
+//     bounds-checked scatter.
 #include "pfm_internal.cuh"
 
 namespace pfm {
@@ -209,134 +210,167 @@ __global__ void __launch_bounds__(kBinThreads) k_payload2(const int* __restrict_
   famrec[P + s] = make_float4(imp[P + q], C[2 * P + q], C[3 * P + q], 0.f);
 }
 
-// Column gather (3D).  One thread owns the faces (i, j, k0 .. k0+K-1) of family `fam` and walks
-// the cell layers ck in increasing order; a particle of layer ck reaches the faces ck-1..ck+1
-// along k (ck-1..ck+2 when k is the family's own axis), so the open faces live in a rolling
-// register window and a face is final once the walk has passed it.  Per face the sum runs over
-// layers ck, then the neighbourhood cells (ci, cj) in lexicographic order (family axis
-// idx-2..idx+1, offset axes idx-1..idx+1), then particles in index order.
-constexpr int kColumn3 = 32;  // faces per thread along k
+// Tiled P2G (3D).  Cells are grouped in kTX x kTY x kTZ tiles, one thread per cell.  For each
+// face family the thread sums its cell's particles (particle-index order) into a register window
+// of the 4 x 3 x 3 faces they can reach (4 along the family's own axis: faces c-1 .. c+2; 3 along
+// the others: c-1 .. c+1), the tile adds the windows into a shared copy of the faces around it in
+// 36 passes (one window offset per pass, a barrier between passes), and then adds that region into
+// the face grids.  Tiles run in 8 launches by the parity of their tile coordinates: tiles of one
+// parity are a tile apart and their face regions (one face below, two above) never overlap, so no
+// atomics are needed.  Each face sums in a fixed order (launch, pass, particle index): the result
+// is bitwise reproducible.  Particles outside the grid sit in the clamped edge cell, whose window
+// still holds every in-grid face they reach; their weights come from their real positions.
+constexpr int kTX = 8, kTY = 8, kTZ = 8;
+constexpr int kTileThreads = kTX * kTY * kTZ;
+constexpr int kTileExtMax = (kTX + 3) * (kTY + 2) * (kTZ + 2);
 
-template <int fam>
-__device__ __forceinline__ void window_weights(float pz, int ck, int kb, float dx, float* wk, float* dk) {
-  constexpr int WIN = (fam == 2) ? 4 : 3;
-  const float fz = pz - (float)ck;
-  if (fz >= 0.f && fz < 1.f) {  // closed form of the N_2 branches about the particle's layer
-    if (fam == 2) {  // faces ck-1 .. ck+2 at x = fz+1, fz, fz-1, fz-2
+struct FaceOut3 {
+  float* u[3];
+  float* w[3];
+};
+
+// Weights and offsets of the window faces c-1 .. c-1+W-1 along one axis (N_2 of 3D/run_3D.py:486)
+template <bool OWN>
+__device__ __forceinline__ void tile_axis(float p, int c, float dx, float* w, float* d) {
+  constexpr int W = OWN ? 4 : 3;
+  const float fz = p - (float)c;
+  if (c >= 1 && fz >= 0.f && fz < 1.f) {  // closed form of the branches (exact subtractions)
+    if (OWN) {  // faces c-1 .. c+2 at x = fz+1, fz, fz-1, fz-2
       const bool lo = fz < 0.5f;
       const float t = lo ? fz : fz - 1.f;
       const float l = 0.5f - t, r = 0.5f + t;
       const float w0 = 0.5f * (l * l), w1 = 0.75f - t * t, w2 = 0.5f * (r * r);
-      wk[0] = lo ? w0 : 0.f;
-      wk[1] = lo ? w1 : w0;
-      wk[2] = lo ? w2 : w1;
-      wk[WIN - 1] = lo ? 0.f : w2;
-    } else {  // faces ck-1 .. ck+1 at (x - 1/2) = t+1, t, t-1 with t = fz - 1/2
+      w[0] = lo ? w0 : 0.f;
+      w[1] = lo ? w1 : w0;
+      w[2] = lo ? w2 : w1;
+      w[W - 1] = lo ? 0.f : w2;
+    } else {  // faces c-1 .. c+1 at (x - 1/2) = t+1, t, t-1 with t = fz - 1/2
       const float t = fz - 0.5f;
       const float l = 0.5f - t, r = 0.5f + t;
-      wk[0] = 0.5f * (l * l);
-      wk[1] = 0.75f - t * t;
-      wk[2] = 0.5f * (r * r);
+      w[0] = 0.5f * (l * l);
+      w[1] = 0.75f - t * t;
+      w[2] = 0.5f * (r * r);
     }
-  } else {  // outside the grid along k: per-face N_2
+  } else {  // first cell or outside the grid: per-face N_2 as the reference
 #pragma unroll
-    for (int q = 0; q < WIN; ++q) {
-      const float fk = (float)(kb + q);
-      wk[q] = (fam == 2) ? N2(pz - fk) : N2((pz - fk) - 0.5f);
+    for (int o = 0; o < W; ++o) {
+      const float t = (float)(c - 1 + o);
+      w[o] = OWN ? N2(p - t) : N2((p - t) - 0.5f);
     }
   }
 #pragma unroll
-  for (int q = 0; q < WIN; ++q) {
-    const float fk = (float)(kb + q);
-    dk[q] = ((fam == 2) ? (fk - pz) : ((fk + 0.5f) - pz)) * dx;
+  for (int o = 0; o < W; ++o) {
+    const float t = (float)(c - 1 + o);
+    d[o] = (OWN ? (t - p) : ((t + 0.5f) - p)) * dx;
   }
 }
 
-template <int fam>
-__global__ void __launch_bounds__(128, 6) k_gather3(const float4* __restrict__ pos4, const float4* __restrict__ famrec,
-                                                 const int* __restrict__ start, MacGeom g, int K, int use_apic,
-                                                 int64_t P, float* __restrict__ u, float* __restrict__ w) {
-  constexpr int WIN = (fam == 2) ? 4 : 3;
-  const int n0 = g.n[fam][0], n1 = g.n[fam][1], n2 = g.n[fam][2];
-  const int nseg = (n2 + K - 1) / K;
-  const int64_t ncol = (int64_t)n0 * n1 * nseg;
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ncol) return;
-  const int j = (int)(t % n1);  // neighbouring threads run along j and share cells
-  const int64_t r = t / n1;
-  const int i = (int)(r % n0);
-  const int seg = (int)(r / n0);
-  const int k0 = seg * K, k1 = min(k0 + K, n2);
-  const int G0 = g.N[0], G1 = g.N[1], G2 = g.N[2];
-  const int ci_lo = max(i - (fam == 0 ? 2 : 1), 0), ci_hi = min(i + 1, G0 - 1);
-  const int cj_lo = max(j - (fam == 1 ? 2 : 1), 0), cj_hi = min(j + 1, G1 - 1);
-  const int ck_lo = max(k0 - (fam == 2 ? 2 : 1), 0), ck_hi = min(k1, G2 - 1);
-  const float fi = (float)i, fj = (float)j;
+template <int FAM>
+__device__ __forceinline__ void tile_family(float2* __restrict__ acc, const float4* __restrict__ pos4,
+                                            const float4* __restrict__ rec, int sb, int se, int ci, int cj, int ck,
+                                            int lx, int ly, int lz, int x0, int y0, int z0, const MacGeom& g,
+                                            int use_apic, float* __restrict__ u, float* __restrict__ w) {
+  constexpr int W0 = FAM == 0 ? 4 : 3, W1 = FAM == 1 ? 4 : 3, W2 = FAM == 2 ? 4 : 3;
+  constexpr int E0 = kTX + W0 - 1, E1 = kTY + W1 - 1, E2 = kTZ + W2 - 1, NE = E0 * E1 * E2;
+  for (int e = threadIdx.x; e < NE; e += kTileThreads) acc[e] = make_float2(0.f, 0.f);
+  float num[W0][W1][W2], den[W0][W1][W2];
+#pragma unroll
+  for (int a = 0; a < W0; ++a)
+#pragma unroll
+    for (int b = 0; b < W1; ++b)
+#pragma unroll
+      for (int k = 0; k < W2; ++k) num[a][b][k] = den[a][b][k] = 0.f;
   const float dx = g.dx;
-  const float4* fam_rec = famrec + (int64_t)fam * P;
-  float num[WIN], den[WIN];
+  for (int s = sb; s < se; ++s) {
+    const float4 p = __ldg(pos4 + s);
+    const float4 fr = __ldg(rec + s);
+    float w0[W0], d0[W0], w1[W1], d1[W1], w2[W2], d2[W2];
+    tile_axis<FAM == 0>(p.x, ci, dx, w0, d0);
+    tile_axis<FAM == 1>(p.y, cj, dx, w1, d1);
+    tile_axis<FAM == 2>(p.z, ck, dx, w2, d2);
 #pragma unroll
-  for (int q = 0; q < WIN; ++q) num[q] = den[q] = 0.f;
-  int kb = ck_lo - 1;  // window slot q holds face kb + q
-  auto store = [&](int kf, float a, float b) {
-    if (kf >= k0 && kf < k1) {
-      const int64_t e = ((int64_t)i * n1 + j) * n2 + kf;
-      w[e] = b;
-      u[e] = b > 0.f ? a / b : a;  // 3D normalises by division (run_3D.py:530-552)
-    }
-  };
-  for (int ck = ck_lo; ck <= ck_hi; ++ck) {
-    while (kb < ck - 1) {
-      store(kb, num[0], den[0]);
+    for (int a = 0; a < W0; ++a)
 #pragma unroll
-      for (int q = 0; q < WIN - 1; ++q) {
-        num[q] = num[q + 1];
-        den[q] = den[q + 1];
-      }
-      num[WIN - 1] = den[WIN - 1] = 0.f;
-      ++kb;
-    }
-    for (int ci = ci_lo; ci <= ci_hi; ++ci) {
-      for (int cj = cj_lo; cj <= cj_hi; ++cj) {
-        const int c = (ci * G1 + cj) * G2 + ck;
-        const int sb = __ldg(start + c), se = __ldg(start + c + 1);
-        for (int s = sb; s < se; ++s) {
-          const float4 p = __ldg(pos4 + s);
-          // weights and offsets along i and j (3D/run_3D.py:486-487 and the twins for y, z)
-          float wi, wj, di, dj;
-          if (fam == 0) {
-            wi = N2(p.x - fi);
-            di = (fi - p.x) * dx;
-          } else {
-            wi = N2((p.x - fi) - 0.5f);
-            di = ((fi + 0.5f) - p.x) * dx;
-          }
-          if (fam == 1) {
-            wj = N2(p.y - fj);
-            dj = (fj - p.y) * dx;
-          } else {
-            wj = N2((p.y - fj) - 0.5f);
-            dj = ((fj + 0.5f) - p.y) * dx;
-          }
-          const float wij = wi * wj;
-          if (wij == 0.f) continue;
-          const float4 fr = __ldg(fam_rec + s);
-          const float d01 = fr.y * di + fr.z * dj;
-          float wk[WIN], dk[WIN];
-          window_weights<fam>(p.z, ck, kb, dx, wk, dk);
+      for (int b = 0; b < W1; ++b) {
+        const float w01 = w0[a] * w1[b];
+        const float d01 = fr.y * d0[a] + fr.z * d1[b];
 #pragma unroll
-          for (int q = 0; q < WIN; ++q) {
-            const float wt = wij * wk[q];
-            const float delta = d01 + fr.w * dk[q];
-            num[q] += (use_apic ? (fr.x + delta) : fr.x) * wt;
-            den[q] += wt;
-          }
+        for (int k = 0; k < W2; ++k) {
+          const float wt = w01 * w2[k];
+          const float delta = d01 + fr.w * d2[k];
+          num[a][b][k] += (use_apic ? (fr.x + delta) : fr.x) * wt;
+          den[a][b][k] += wt;
         }
       }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int a = 0; a < W0; ++a)
+#pragma unroll
+    for (int b = 0; b < W1; ++b)
+#pragma unroll
+      for (int k = 0; k < W2; ++k) {
+        float2* cell = acc + ((lx + a) * E1 + (ly + b)) * E2 + (lz + k);
+        float2 v = *cell;
+        v.x += num[a][b][k];
+        v.y += den[a][b][k];
+        *cell = v;
+        __syncthreads();
+      }
+  const int n0 = g.n[FAM][0], n1 = g.n[FAM][1], n2 = g.n[FAM][2];
+  for (int e = threadIdx.x; e < NE; e += kTileThreads) {
+    const int ez = e % E2, r = e / E2, ey = r % E1, ex = r / E1;
+    const int gi = x0 - 1 + ex, gj = y0 - 1 + ey, gk = z0 - 1 + ez;
+    if (gi >= 0 && gi < n0 && gj >= 0 && gj < n1 && gk >= 0 && gk < n2) {
+      const float2 v = acc[e];
+      const int64_t q = ((int64_t)gi * n1 + gj) * n2 + gk;
+      u[q] += v.x;
+      w[q] += v.y;
     }
   }
-#pragma unroll
-  for (int q = 0; q < WIN; ++q) store(kb + q, num[q], den[q]);
+  __syncthreads();
+}
+
+// One parity class (px, py, pz) of tiles; grid = (tiles along z, y, x of that parity).
+__global__ void __launch_bounds__(kTileThreads, 1) k_tile3(const float4* __restrict__ pos4,
+                                                           const float4* __restrict__ famrec,
+                                                           const int* __restrict__ start, MacGeom g, int use_apic,
+                                                           int64_t P, int px, int py, int pz, FaceOut3 out) {
+  __shared__ float2 acc[kTileExtMax];
+  const int x0 = (2 * (int)blockIdx.z + px) * kTX, y0 = (2 * (int)blockIdx.y + py) * kTY;
+  const int z0 = (2 * (int)blockIdx.x + pz) * kTZ;
+  const int lz = threadIdx.x % kTZ, ly = (threadIdx.x / kTZ) % kTY, lx = threadIdx.x / (kTZ * kTY);
+  const int ci = x0 + lx, cj = y0 + ly, ck = z0 + lz;
+  int sb = 0, se = 0;
+  if (ci < g.N[0] && cj < g.N[1] && ck < g.N[2]) {
+    const int c = (ci * g.N[1] + cj) * g.N[2] + ck;
+    sb = __ldg(start + c);
+    se = __ldg(start + c + 1);
+  }
+  tile_family<0>(acc, pos4, famrec, sb, se, ci, cj, ck, lx, ly, lz, x0, y0, z0, g, use_apic, out.u[0], out.w[0]);
+  tile_family<1>(acc, pos4, famrec + P, sb, se, ci, cj, ck, lx, ly, lz, x0, y0, z0, g, use_apic, out.u[1],
+                 out.w[1]);
+  tile_family<2>(acc, pos4, famrec + 2 * P, sb, se, ci, cj, ck, lx, ly, lz, x0, y0, z0, g, use_apic, out.u[2],
+                 out.w[2]);
+}
+
+// u = u / w where w > 0 (3D/run_3D.py:530-552), all three families in one pass
+__global__ void __launch_bounds__(kBinThreads) k_normalize3(FaceOut3 out, int64_t F0, int64_t F1, int64_t F2) {
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int f = 0;
+  if (e >= F0) {
+    e -= F0;
+    f = 1;
+    if (e >= F1) {
+      e -= F1;
+      f = 2;
+      if (e >= F2) return;
+    }
+  }
+  float* u = f == 0 ? out.u[0] : (f == 1 ? out.u[1] : out.u[2]);
+  const float* w = f == 0 ? out.w[0] : (f == 1 ? out.w[1] : out.w[2]);
+  const float wv = w[e];
+  if (wv > 0.f) u[e] = u[e] / wv;
 }
 
 // Column gather (2D): columns along j; 2D normalises with scale = 1/w (run_2D.py:599-611) and
@@ -523,16 +557,25 @@ int pfm3_p2g(pfm_handle* h, const float* init_imp, const float* pos, const float
   if (h->P > 0)
     launch(h, k_payload3, grid_for(h->P, kBinThreads), kBinThreads, 0, st, ws_ptr<int>(h, h->o_order), h->P, h->geom,
            pos, init_imp, T_gm, T_init, init_C, pos4, famrec);
+  FaceOut3 out{{u_x, u_y, u_z}, {w_x, w_y, w_z}};
+  int64_t F[3];
   for (int f = 0; f < 3; ++f) {
-    const int n2 = h->geom.n[f][2];
-    const int K = n2 < kColumn3 ? n2 : kColumn3;
-    const int64_t ncol = (int64_t)h->geom.n[f][0] * h->geom.n[f][1] * ((n2 + K - 1) / K);
-    if (f == 0) launch(h, k_gather3<0>, grid_for(ncol, 128), 128, 0, st, pos4, famrec, start, h->geom, K,
-                       h->cfg.use_apic, h->P, us[f], ws[f]);
-    if (f == 1) launch(h, k_gather3<1>, grid_for(ncol, 128), 128, 0, st, pos4, famrec, start, h->geom, K,
-                       h->cfg.use_apic, h->P, us[f], ws[f]);
-    if (f == 2) launch(h, k_gather3<2>, grid_for(ncol, 128), 128, 0, st, pos4, famrec, start, h->geom, K,
-                       h->cfg.use_apic, h->P, us[f], ws[f]);
+    F[f] = (int64_t)h->geom.n[f][0] * h->geom.n[f][1] * h->geom.n[f][2];
+    rc = check_cuda(h, cudaMemsetAsync(us[f], 0, F[f] * 4, st), "zero u");
+    if (!rc) rc = check_cuda(h, cudaMemsetAsync(ws[f], 0, F[f] * 4, st), "zero w");
+    if (rc) return rc;
+  }
+  if (h->P > 0) {
+    const int nt[3] = {(h->geom.N[0] + kTX - 1) / kTX, (h->geom.N[1] + kTY - 1) / kTY, (h->geom.N[2] + kTZ - 1) / kTZ};
+    for (int px = 0; px < 2; ++px)
+      for (int py = 0; py < 2; ++py)
+        for (int pz = 0; pz < 2; ++pz) {
+          const unsigned bx = (nt[0] - px + 1) / 2, by = (nt[1] - py + 1) / 2, bz = (nt[2] - pz + 1) / 2;
+          if (!bx || !by || !bz) continue;
+          launch(h, k_tile3, dim3(bz, by, bx), kTileThreads, 0, st, (const float4*)pos4, (const float4*)famrec,
+                 start, h->geom, h->cfg.use_apic, h->P, px, py, pz, out);
+        }
+    launch(h, k_normalize3, grid_for(F[0] + F[1] + F[2], kBinThreads), kBinThreads, 0, st, out, F[0], F[1], F[2]);
   }
   return launch_check(h, "pfm3_p2g");
 }
