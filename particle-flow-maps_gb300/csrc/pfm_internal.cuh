@@ -219,6 +219,16 @@ struct MacFields3 {
   const float* u[3];
 };
 
+// The 27-tap sums are evaluated axis by axis (z taps, then y, then x): per component
+//   tn_ab = sum_k wz_k f_abk,  td_ab = sum_k dwz_k f_abk,
+//   A_a = sum_b wy_b tn_ab,  B_a = sum_b dwy_b tn_ab,  C_a = sum_b wy_b td_ab,
+//   u = sum_a wx_a A_a,  du/dx = sum_a dwx_a A_a / dx,  du/dy = sum_a wx_a B_a / dx,
+//   du/dz = sum_a wx_a C_a / dx,
+// the same terms as the reference's triple loop in a different association (rounding-level
+// differences only).  Components x and y share the z tap set (BL = 0.5 along z) and their
+// x/y weights form natural pairs, so they run together on packed f32x2 FMAs; z runs scalar.
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+
 __device__ __forceinline__ void interp_mac3(const MacFields3& F, const MacGeom& g, const float p[3],
                                             float uo[3], float G[3][3], bool want_grad) {
   Axis3 A0[3], A1[3];
@@ -228,15 +238,91 @@ __device__ __forceinline__ void interp_mac3(const MacFields3& F, const MacGeom& 
     axis_taps(u - 0.0f, g.hi[a][a], g.n[a][a], A0[a]);               // the component along a
     axis_taps(u - 0.5f, g.hi[(a + 1) % 3][a], g.n[(a + 1) % 3][a], A1[a]);  // the others
   }
+  const float inv_dx = g.inv_dx;
+  // ---- components x and y together: x uses (A0x, A1y, A1z), y uses (A1x, A0y, A1z)
+  {
+    const float* __restrict__ f0 = F.u[0];
+    const float* __restrict__ f1 = F.u[1];
+    const int m01 = g.n[0][1], m02 = g.n[0][2], m11 = g.n[1][1], m12 = g.n[1][2];
+    const Axis3& Z = A1[2];
+    const float2 zw0 = f2(Z.w[0], Z.w[0]), zw1 = f2(Z.w[1], Z.w[1]), zw2 = f2(Z.w[2], Z.w[2]);
+    float2 V = f2(0.f, 0.f), GX = V, GY = V, GZ = V;
 #pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    const Axis3& X = (c == 0) ? A0[0] : A1[0];
-    const Axis3& Y = (c == 1) ? A0[1] : A1[1];
-    const Axis3& Z = (c == 2) ? A0[2] : A1[2];
+    for (int a = 0; a < 3; ++a) {
+      float2 Aa = f2(0.f, 0.f), Ba = Aa, Ca = Aa;
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        const int r0 = (A0[0].idx[a] * m01 + A1[1].idx[b]) * m02;
+        const int r1 = (A1[0].idx[a] * m11 + A0[1].idx[b]) * m12;
+        const float2 v0 = f2(__ldg(f0 + r0 + Z.idx[0]), __ldg(f1 + r1 + Z.idx[0]));
+        const float2 v1 = f2(__ldg(f0 + r0 + Z.idx[1]), __ldg(f1 + r1 + Z.idx[1]));
+        const float2 v2 = f2(__ldg(f0 + r0 + Z.idx[2]), __ldg(f1 + r1 + Z.idx[2]));
+        float2 tn = __fmul2_rn(v0, zw0);
+        tn = __ffma2_rn(v1, zw1, tn);
+        tn = __ffma2_rn(v2, zw2, tn);
+        const float2 wy = f2(A1[1].w[b], A0[1].w[b]);
+        Aa = __ffma2_rn(wy, tn, Aa);
+        if (want_grad) {
+          const float2 zd0 = f2(Z.dw[0], Z.dw[0]), zd1 = f2(Z.dw[1], Z.dw[1]), zd2 = f2(Z.dw[2], Z.dw[2]);
+          float2 td = __fmul2_rn(v0, zd0);
+          td = __ffma2_rn(v1, zd1, td);
+          td = __ffma2_rn(v2, zd2, td);
+          Ba = __ffma2_rn(f2(A1[1].dw[b], A0[1].dw[b]), tn, Ba);
+          Ca = __ffma2_rn(wy, td, Ca);
+        }
+      }
+      const float2 wx = f2(A0[0].w[a], A1[0].w[a]);
+      V = __ffma2_rn(wx, Aa, V);
+      if (want_grad) {
+        GX = __ffma2_rn(f2(A0[0].dw[a], A1[0].dw[a]), Aa, GX);
+        GY = __ffma2_rn(wx, Ba, GY);
+        GZ = __ffma2_rn(wx, Ca, GZ);
+      }
+    }
+    uo[0] = V.x;
+    uo[1] = V.y;
     if (want_grad) {
-      interp3_component(F.u[c], g.n[c][1], g.n[c][2], X, Y, Z, g.inv_dx, uo[c], G[c][0], G[c][1], G[c][2]);
-    } else {
-      uo[c] = interp3_value(F.u[c], g.n[c][1], g.n[c][2], X, Y, Z);
+      G[0][0] = GX.x * inv_dx;
+      G[1][0] = GX.y * inv_dx;
+      G[0][1] = GY.x * inv_dx;
+      G[1][1] = GY.y * inv_dx;
+      G[0][2] = GZ.x * inv_dx;
+      G[1][2] = GZ.y * inv_dx;
+    }
+  }
+  // ---- component z: (A1x, A1y, A0z)
+  {
+    const float* __restrict__ f = F.u[2];
+    const int m1 = g.n[2][1], m2 = g.n[2][2];
+    const Axis3 &X = A1[0], &Y = A1[1], &Z = A0[2];
+    float v_ = 0.f, x_ = 0.f, y_ = 0.f, z_ = 0.f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      float Aa = 0.f, Ba = 0.f, Ca = 0.f;
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        const float* row = f + (X.idx[a] * m1 + Y.idx[b]) * m2;
+        const float v0 = __ldg(row + Z.idx[0]), v1 = __ldg(row + Z.idx[1]), v2 = __ldg(row + Z.idx[2]);
+        const float tn = fmaf(v2, Z.w[2], fmaf(v1, Z.w[1], v0 * Z.w[0]));
+        Aa = fmaf(Y.w[b], tn, Aa);
+        if (want_grad) {
+          const float td = fmaf(v2, Z.dw[2], fmaf(v1, Z.dw[1], v0 * Z.dw[0]));
+          Ba = fmaf(Y.dw[b], tn, Ba);
+          Ca = fmaf(Y.w[b], td, Ca);
+        }
+      }
+      v_ = fmaf(X.w[a], Aa, v_);
+      if (want_grad) {
+        x_ = fmaf(X.dw[a], Aa, x_);
+        y_ = fmaf(X.w[a], Ba, y_);
+        z_ = fmaf(X.w[a], Ca, z_);
+      }
+    }
+    uo[2] = v_;
+    if (want_grad) {
+      G[2][0] = x_ * inv_dx;
+      G[2][1] = y_ * inv_dx;
+      G[2][2] = z_ * inv_dx;
     }
   }
 }

@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(256) k_reset_T(float* __restrict__ T, int64_t 
 // RK4_T_forward (3D/run_3D.py:175-219): the gradient is taken in the transpose form
 // (interp_u_MAC_grad_transpose, 3D/taichi_utils.py:319-324), so dT_v/dt[r] = sum_c du_c/dx_r T_v[c].
 // The stage sums (k1 + 2 k2 + 2 k3 + k4) accumulate in the reference's left-to-right order.
-__global__ void __launch_bounds__(kPThreads) k_rk4_T_forward3(float* __restrict__ pos, float* __restrict__ T,
+__global__ void __launch_bounds__(kPThreads, 4) k_rk4_T_forward3(float* __restrict__ pos, float* __restrict__ T,
                                                              int64_t P, MacFields3 F, MacGeom g, float dt) {
   int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= P) return;
