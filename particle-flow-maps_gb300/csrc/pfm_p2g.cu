@@ -222,7 +222,10 @@ __global__ void __launch_bounds__(kBinThreads) k_payload2(const int* __restrict_
 // still holds every in-grid face they reach; their weights come from their real positions.
 constexpr int kTX = 8, kTY = 8, kTZ = 8;
 constexpr int kTileThreads = kTX * kTY * kTZ;
-constexpr int kTileExtMax = (kTX + 3) * (kTY + 2) * (kTZ + 2);
+constexpr int kExt0 = (kTX + 3) * (kTY + 2) * (kTZ + 2);  // face region of family x
+constexpr int kExt1 = (kTX + 2) * (kTY + 3) * (kTZ + 2);  // family y
+constexpr int kExt2 = (kTX + 2) * (kTY + 2) * (kTZ + 3);  // family z
+constexpr int kTileExtMax = kExt0 > kExt1 ? (kExt0 > kExt2 ? kExt0 : kExt2) : (kExt1 > kExt2 ? kExt1 : kExt2);
 
 struct FaceOut3 {
   float* u[3];
@@ -272,6 +275,7 @@ __device__ __forceinline__ void tile_family(float2* __restrict__ acc, const floa
                                             int use_apic, float* __restrict__ u, float* __restrict__ w) {
   constexpr int W0 = FAM == 0 ? 4 : 3, W1 = FAM == 1 ? 4 : 3, W2 = FAM == 2 ? 4 : 3;
   constexpr int E0 = kTX + W0 - 1, E1 = kTY + W1 - 1, E2 = kTZ + W2 - 1, NE = E0 * E1 * E2;
+  static_assert(NE <= kTileExtMax, "tile face region exceeds the shared buffer");
   for (int e = threadIdx.x; e < NE; e += kTileThreads) acc[e] = make_float2(0.f, 0.f);
   float num[W0][W1][W2], den[W0][W1][W2];
 #pragma unroll
