@@ -76,6 +76,16 @@ int pfm_create(const pfm_config* cfg, pfm_handle** out) {
   g.dx = (float)cfg->dx;
   g.inv_dx = (float)(1.0 / cfg->dx);
   h->cells = (int64_t)g.N[0] * g.N[1] * g.N[2];
+  // grid kernels index cells and faces with 32-bit integers
+  for (int c = 0; c < D; ++c)
+    if ((int64_t)g.n[c][0] * g.n[c][1] * g.n[c][2] >= (int64_t(1) << 31)) {
+      delete h;
+      return PFM_ERR_SHAPE;
+    }
+  for (int a = 0; a < 3; ++a) {
+    g.dN[a] = make_div32((unsigned)g.N[a]);
+    for (int c = 0; c < 3; ++c) g.dn[c][a] = make_div32((unsigned)g.n[c][a]);
+  }
 
   // MGPCG hierarchy (3D/mgpcg.py:28): int(log2(min N)) - base_level + 1 levels
   int mn = g.N[0];
@@ -143,7 +153,7 @@ int pfm_create(const pfm_config* cfg, pfm_handle** out) {
 int pfm_destroy(pfm_handle* h) {
   if (!h) return PFM_ERR_NULL;
   if (h->g_setup) cudaGraphExecDestroy(h->g_setup);
-  if (h->g_iter) cudaGraphExecDestroy(h->g_iter);
+  if (h->g_loop) cudaGraphExecDestroy(h->g_loop);
   if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
   if (h->h_state) cudaFreeHost(h->h_state);
   delete h;

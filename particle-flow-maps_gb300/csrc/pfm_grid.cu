@@ -16,10 +16,8 @@ __global__ void __launch_bounds__(256) k_max_speed(const float* __restrict__ ux,
   const int64_t C = (int64_t)g.N[0] * g.N[1] * g.N[2];
   float m = 1.e-3f;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < C; e += (int64_t)gridDim.x * blockDim.x) {
-    int k = (int)(e % g.N[2]);
-    int64_t t = e / g.N[2];
-    int j = (int)(t % g.N[1]);
-    int i = (int)(t / g.N[1]);
+    int i, j, k;
+    split3((unsigned)e, g.dN[1], g.dN[2], i, j, k);
     float u, v, sp;
     if (D == 3) {
       float w;
@@ -78,10 +76,8 @@ __global__ void __launch_bounds__(kGThreads) k_midpoint3(MacFields3 F, MacGeom g
   const int64_t nf = (int64_t)n0 * n1 * n2;
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= nf) return;
-  int k = (int)(e % n2);
-  int64_t t = e / n2;
-  int j = (int)(t % n1);
-  int i = (int)(t / n1);
+  int i, j, k;
+  split3((unsigned)e, g.dn[fam][1], g.dn[fam][2], i, j, k);
   float X[3] = {(float)i, (float)j, (float)k};
 #pragma unroll
   for (int d = 0; d < 3; ++d)
@@ -143,8 +139,8 @@ __global__ void __launch_bounds__(kGThreads) k_midpoint2(MacFields2 F, MacGeom g
   const int64_t nf = (int64_t)n0 * n1;
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= nf) return;
-  int j = (int)(e % n1);
-  int i = (int)(e / n1);
+  const int i = (int)udiv((unsigned)e, g.dn[fam][1]);
+  const int j = (int)((unsigned)e - (unsigned)i * (unsigned)n1);
   float X[2] = {(float)i, (float)j};
   X[1 - fam] = X[1 - fam] + 0.5f;
   float p0[2] = {X[0] * g.dx, X[1] * g.dx};

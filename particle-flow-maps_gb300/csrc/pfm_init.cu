@@ -12,10 +12,8 @@ __global__ void __launch_bounds__(256) k_vortex_ring(float* __restrict__ vc, Mac
   const int64_t C = (int64_t)g.N[0] * g.N[1] * g.N[2];
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= C) return;
-  int k = (int)(e % g.N[2]);
-  int64_t t = e / g.N[2];
-  int j = (int)(t % g.N[1]);
-  int i = (int)(t / g.N[1]);
+  int i, j, k;
+  split3((unsigned)e, g.dN[1], g.dN[2], i, j, k);
   const float px = ((float)i + 0.5f) * g.dx, py = ((float)j + 0.5f) * g.dx, pz = ((float)k + 0.5f) * g.dx;
   const float pi = 3.14159265358979323846f;
   const float curve_length = (2.f * pi * rad) / (float)num_samples;
@@ -49,10 +47,7 @@ __global__ void __launch_bounds__(256) k_split_central(const float* __restrict__
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= nf) return;
   int idx[3];
-  idx[2] = (int)(e % n2);
-  int64_t t = e / n2;
-  idx[1] = (int)(t % n1);
-  idx[0] = (int)(t / n1);
+  split3((unsigned)e, g.dn[fam][1], g.dn[fam][2], idx[0], idx[1], idx[2]);
   int a[3] = {idx[0], idx[1], idx[2]}, b[3] = {idx[0], idx[1], idx[2]};
   b[fam] -= 1;
   for (int d = 0; d < 3; ++d) {
@@ -85,10 +80,7 @@ __global__ void __launch_bounds__(256) k_seed_jittered(float* __restrict__ pos, 
   int sub = (int)(q % ppc);
   int ci[3], si[3];
   if (D == 3) {
-    ci[2] = (int)(cell % g.N[2]);
-    int64_t t = cell / g.N[2];
-    ci[1] = (int)(t % g.N[1]);
-    ci[0] = (int)(t / g.N[1]);
+    split3((unsigned)cell, g.dN[1], g.dN[2], ci[0], ci[1], ci[2]);
     si[2] = sub % axis;
     si[1] = (sub / axis) % axis;
     si[0] = sub / (axis * axis);

@@ -33,8 +33,34 @@ struct SolveState {
   int done;        // 1 converged, 2 iteration limit, 3 non-finite
   int conv_it;     // iteration index at convergence
   unsigned ticket; // last-block counter of the reductions
-  unsigned pad;
+  int it_stop;     // the device loop pauses when `it` reaches this count
 };
+
+// Unsigned division by a divisor that is fixed for a launch, with one multiply-high (Granlund and
+// Montgomery, "Division by invariant integers using multiplication", PLDI 1994): with
+// s = ceil(log2 d) and m = floor(2^32 (2^s - d) / d) + 1, n / d = (umulhi(n, m) + n) >> s for
+// every 0 <= n < 2^31.  Grid and level indices stay below 2^31 (pfm_create rejects larger grids).
+struct Div32 {
+  unsigned d, m, s;
+};
+
+inline Div32 make_div32(unsigned d) {
+  unsigned s = 0;
+  while ((1ull << s) < d) ++s;
+  const unsigned long long m = ((1ull << 32) * ((1ull << s) - d)) / d + 1;
+  return Div32{d, (unsigned)m, s};
+}
+
+__device__ __forceinline__ unsigned udiv(unsigned n, const Div32& D) { return (__umulhi(n, D.m) + n) >> D.s; }
+
+// e = (i * n1 + j) * n2 + k  ->  (i, j, k), with d1 / d2 the divisors n1 / n2
+__device__ __forceinline__ void split3(unsigned e, const Div32& d1, const Div32& d2, int& i, int& j, int& k) {
+  const unsigned t = udiv(e, d2);
+  k = (int)(e - t * d2.d);
+  const unsigned u = udiv(t, d1);
+  j = (int)(t - u * d1.d);
+  i = (int)u;
+}
 
 struct LevelDims {
   int n[3];
@@ -50,6 +76,8 @@ struct MacGeom {
   float hi[3][3];  // interpolation clamp constants
   float dx;        // f32(dx)
   float inv_dx;    // f32(1/dx)
+  Div32 dN[3];     // divisors N[a]
+  Div32 dn[3][3];  // divisors n[c][a]
 };
 
 }  // namespace pfm
@@ -76,10 +104,10 @@ struct pfm_handle {
   uint64_t launches;
   // CUDA graphs of the MGPCG setup and of one PCG iteration (captured on first use)
   cudaStream_t cap_stream;
-  cudaGraphExec_t g_setup, g_iter;
-  int g_setup_nodes, g_iter_nodes;
+  cudaGraphExec_t g_setup, g_loop;  // setup + first half-iteration; device-side PCG loop
+  int g_setup_nodes, g_body_nodes;
   double g_eps, g_tol;
-  int g_mode, g_valid;
+  int g_mode, g_valid, g_max_iters, g_chunk;
   std::string err;
 };
 

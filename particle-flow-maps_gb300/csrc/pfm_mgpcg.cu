@@ -1,9 +1,10 @@
 // MGPCG pressure projection on the MAC grid (3D/mgpcg.py, 2D/mgpcg.py).
 //
 // Structure follows MGPCG.solve (3D/mgpcg.py:202-280) exactly, with these GB300 choices:
-//  * alpha/beta/convergence live in a device SolveState; the host reads it every
-//    `check_every` iterations instead of three times per iteration, and kernels enqueued past
-//    convergence return immediately, so the stopping iteration is the reference's;
+//  * alpha/beta/convergence live in a device SolveState, and the iteration loop runs on the
+//    device: a CUDA graph WHILE node repeats the iteration until the convergence test (or the
+//    iteration limit) clears its condition, so the host waits once per solve and the stopping
+//    iteration is the reference's;
 //  * every reduction is deterministic: a fixed block partition, per-thread f32 partials,
 //    f64 block and grid combination in block order (no float atomics);
 //  * the restriction scatter (r_{l+1}[I//2] += res/(dim-1), 3D/mgpcg.py:152-158) is a gather
@@ -17,14 +18,22 @@ namespace pfm {
 struct Lvl {
   int n0, n1, n2;
   int64_t count;
+  Div32 d1, d2;  // divisors n1, n2
+  Div32 dh;      // divisor (last extent + 1) / 2: the cell pairs of a smoothing sweep
 };
+
+static inline Lvl make_lvl(int n0, int n1, int n2, int D) {
+  const int last = (D == 3) ? n2 : n1;
+  return Lvl{n0, n1, n2, (int64_t)n0 * n1 * n2, make_div32((unsigned)n1), make_div32((unsigned)n2),
+             make_div32((unsigned)((last + 1) >> 1))};
+}
 
 struct BC {
   int lo[3], hi[3];  // 2 = Neumann
 };
 
 static inline Lvl lvl_of(const pfm_handle* h, int l) {
-  return Lvl{h->lv[l].n[0], h->lv[l].n[1], h->lv[l].n[2], h->lv[l].count};
+  return make_lvl(h->lv[l].n[0], h->lv[l].n[1], h->lv[l].n[2], h->cfg.dim);
 }
 
 // neighbor_sum / num_fluid_neighbors (3D/mgpcg.py:92-115)
@@ -58,10 +67,7 @@ __device__ __forceinline__ void stencil(const float* __restrict__ f, const Lvl& 
 }
 
 __device__ __forceinline__ void decode(const Lvl& L, int64_t e, int& i, int& j, int& k) {
-  k = (int)(e % L.n2);
-  int64_t t = e / L.n2;
-  j = (int)(t % L.n1);
-  i = (int)(t / L.n1);
+  split3((unsigned)e, L.d1, L.d2, i, j, k);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -125,12 +131,12 @@ __global__ void k_apply_bc(float* __restrict__ u, int fam, MacGeom g, int lo_neu
   int a1 = (fam == 0) ? 1 : 0, a2 = (fam == 2) ? 1 : 2;
   if (D == 2) a2 = 2;
   const int m1 = g.n[fam][a1], m2 = (D == 3) ? g.n[fam][a2] : 1;
-  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  int64_t plane = (int64_t)m1 * m2;
+  const unsigned e = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned plane = (unsigned)m1 * (unsigned)m2;
   if (e >= 2 * plane) return;
-  int side = (int)(e / plane);
-  int64_t r = e % plane;
-  int c1 = (int)(r / m2), c2 = (int)(r % m2);
+  const int side = (int)(e / plane);
+  const unsigned r = e - (unsigned)side * plane;
+  const int c1 = (int)(r / (unsigned)m2), c2 = (int)(r % (unsigned)m2);
   int idx[3] = {0, 0, 0};
   idx[fam] = side ? g.n[fam][fam] - 1 : 0;
   idx[a1] = c1;
@@ -142,8 +148,7 @@ __global__ void k_apply_bc(float* __restrict__ u, int fam, MacGeom g, int lo_neu
 // divergence then init(u_div, -1): r0 = -(vr - vl + vt - vb + vc - va)
 template <int D>
 __global__ void k_divergence(const float* __restrict__ ux, const float* __restrict__ uy,
-                             const float* __restrict__ uz, MacGeom g, float* __restrict__ r0) {
-  const Lvl L{g.N[0], g.N[1], g.N[2], (int64_t)g.N[0] * g.N[1] * g.N[2]};
+                             const float* __restrict__ uz, Lvl L, float* __restrict__ r0) {
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= L.count) return;
   int i, j, k;
@@ -163,18 +168,14 @@ __global__ void k_divergence(const float* __restrict__ ux, const float* __restri
 }
 
 // subtract_grad_p for family `fam`, followed by apply_bc on that family's boundary faces.
-template <int D>
-__global__ void k_subtract_grad_p(float* __restrict__ u, int fam, const float* __restrict__ p, MacGeom g,
-                                  int lo_neu, int hi_neu) {
-  const int n0 = g.n[fam][0], n1 = g.n[fam][1], n2 = g.n[fam][2];
-  const int64_t nf = (int64_t)n0 * n1 * n2;
-  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+template <int D, int fam>
+__global__ void __launch_bounds__(256) k_subtract_grad_p(float* __restrict__ u, const float* __restrict__ p, MacGeom g,
+                                                         int lo_neu, int hi_neu) {
+  const unsigned nf = (unsigned)g.n[fam][0] * g.n[fam][1] * g.n[fam][2];
+  const unsigned e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= nf) return;
   int idx[3];
-  idx[2] = (int)(e % n2);
-  int64_t t = e / n2;
-  idx[1] = (int)(t % n1);
-  idx[0] = (int)(t / n1);
+  split3(e, g.dn[fam][1], g.dn[fam][2], idx[0], idx[1], idx[2]);
   const int N[3] = {g.N[0], g.N[1], g.N[2]};
   // sample(p, I) and sample(p, I - e_fam): clamped indices, then the explicit zeros
   int hiI[3] = {idx[0], idx[1], idx[2]}, loI[3] = {idx[0], idx[1], idx[2]};
@@ -205,19 +206,19 @@ __global__ void __launch_bounds__(256) k_smooth(float* __restrict__ z, const flo
   const int nl = (D == 3) ? L.n2 : L.n1;
   const int half = (nl + 1) >> 1;
   const int64_t npairs = (D == 3) ? (int64_t)L.n0 * L.n1 * half : (int64_t)L.n0 * half;
-  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= npairs) return;
+  const unsigned e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (unsigned)npairs) return;
   int i, j, k;
+  const unsigned t = udiv(e, L.dh);
+  const int m = (int)(e - t * (unsigned)half);
   if (D == 3) {
-    int m = (int)(e % half);
-    int64_t t = e / half;
-    j = (int)(t % L.n1);
-    i = (int)(t / L.n1);
+    const unsigned q = udiv(t, L.d1);
+    j = (int)(t - q * (unsigned)L.n1);
+    i = (int)q;
     k = 2 * m + ((i + j + phase) & 1);
     if (k >= L.n2) return;
   } else {
-    int m = (int)(e % half);
-    i = (int)(e / half);
+    i = (int)t;
     j = 2 * m + ((i + phase) & 1);
     k = 0;
     if (j >= L.n1) return;
@@ -290,7 +291,8 @@ enum RedKind { RED_ZTR_INIT = 0, RED_ZTR = 1, RED_RTR0 = 2, RED_MEAN = 3 };
 
 // sum(a*b) (or sum(a) for RED_MEAN) with a finalizer that updates the solve state.
 __global__ void __launch_bounds__(kReduceThreads) k_dot(const float* __restrict__ a, const float* __restrict__ b,
-                                                        int64_t n, RedBuf rb, int kind, double eps, double inv_n) {
+                                                        int64_t n, RedBuf rb, int kind, double eps, double inv_n,
+                                                        int max_iters) {
   SolveState* st = rb.st;
   if (st->done) return;
   float acc = 0.f;
@@ -301,11 +303,19 @@ __global__ void __launch_bounds__(kReduceThreads) k_dot(const float* __restrict_
   if (threadIdx.x != 0) return;
   if (kind == RED_ZTR_INIT) {
     st->zTr_old = total;
+    if (max_iters == 0) {  // for i in range(0): no iteration at all
+      st->done = 2;
+      st->conv_it = 0;
+    }
   } else if (kind == RED_ZTR) {
     // beta = new_zTr / (old_zTr + eps); p update follows (3D/mgpcg.py:268-275)
     st->beta = (float)(total / (st->zTr_old + eps));
     st->zTr_old = total;
     st->it += 1;
+    if (max_iters >= 0 && st->it >= max_iters) {  // the reference's loop ends here (limit)
+      st->done = 2;
+      st->conv_it = st->it;
+    }
   } else if (kind == RED_RTR0) {
     st->rTr0 = total;
   } else {
@@ -382,6 +392,19 @@ __global__ void __launch_bounds__(256) k_update_p(float* __restrict__ p, const f
   const float beta = st->beta;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
     p[e] = z[e] + beta * p[e];
+}
+
+// Device loop control.  The loop body is the second half of iteration k (recenter, V-cycle, beta,
+// p update) followed by the first half of iteration k+1 (Ap, alpha, x/r update, convergence
+// test), so the WHILE condition is evaluated exactly where the reference breaks.  One launch of
+// the loop runs at most `chunk` bodies.
+__global__ void k_loop_begin(SolveState* st, int chunk, cudaGraphConditionalHandle cond) {
+  st->it_stop = st->it + chunk;
+  cudaGraphSetConditional(cond, (st->done == 0 && chunk > 0) ? 1u : 0u);
+}
+
+__global__ void k_loop_cond(const SolveState* st, cudaGraphConditionalHandle cond) {
+  cudaGraphSetConditional(cond, (st->done == 0 && st->it < st->it_stop) ? 1u : 0u);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -609,13 +632,19 @@ static int run_graph(pfm_handle* h, cudaGraphExec_t exec, int nodes, cudaStream_
 }
 
 // MGPCG.solve (3D/mgpcg.py:202-280) on r_0 (already -div); the solution is left in the
-// workspace vector x.  The setup (recenter, first V-cycle, p = z, z.r) and one PCG iteration are
-// each replayed from a CUDA graph; the host reads the device state every check_every iterations.
+// workspace vector x.  Two graphs per handle, captured once per option set:
+//   setup: x = p = Ap = 0, recenter, r0.r0, first V-cycle, p = z, z.r, and the first half of
+//          iteration 1 (Ap, alpha, x/r update, convergence test);
+//   loop:  WHILE(not done and it < it_stop) { second half of iteration k, first half of k+1 },
+//          then the device state is copied to pinned host memory.
+// With a finite max_iters one loop launch finishes the solve; with max_iters = -1 the host
+// relaunches the loop every check_every iterations until the state reports convergence.
 template <int D>
 static int solve_impl(pfm_handle* h, const pfm_solve_opts* opts, pfm_solve_stats* stats, cudaStream_t s) {
   pfm_solve_opts o{400, 1e-12, 1e-12, 0, 4};
   if (opts) o = *opts;
   if (o.check_every < 1) o.check_every = 1;
+  const int chunk = o.max_iters >= 0 ? o.max_iters + 1 : o.check_every;
   const int64_t n = h->cells;
   SolveState* st = ws_ptr<SolveState>(h, h->o_state);
   RedBuf rb{ws_ptr<double>(h, h->o_partials), st};
@@ -624,74 +653,122 @@ static int solve_impl(pfm_handle* h, const pfm_solve_opts* opts, pfm_solve_stats
   float* x = ws_ptr<float>(h, h->o_x);
   float* p = ws_ptr<float>(h, h->o_p);
   float* Ap = ws_ptr<float>(h, h->o_Ap);
+  SolveState* hs = h->h_state;
   const Lvl L0 = lvl_of(h, 0);
   const BC bc = bc_of(h);
   const double inv_n = 1.0 / (double)n;
   const bool neu = all_neumann(h);
-  if (!h->g_valid || h->g_eps != o.eps || h->g_tol != o.tol || h->g_mode != o.tol_mode) {
+  const int mi = o.max_iters;
+  if (!h->g_valid || h->g_eps != o.eps || h->g_tol != o.tol || h->g_mode != o.tol_mode || h->g_max_iters != mi ||
+      h->g_chunk != chunk) {
     if (h->g_setup) cudaGraphExecDestroy(h->g_setup);
-    if (h->g_iter) cudaGraphExecDestroy(h->g_iter);
-    h->g_setup = h->g_iter = nullptr;
+    if (h->g_loop) cudaGraphExecDestroy(h->g_loop);
+    h->g_setup = h->g_loop = nullptr;
     h->g_valid = 0;
-    auto setup = [&](cudaStream_t q) {
-      if (neu) {
-        launch(h, k_dot, red_blocks(n), kReduceThreads, 0, q, r0, (const float*)nullptr, n, rb, (int)RED_MEAN, o.eps, inv_n);
-        launch(h, k_sub_mean, stream_blocks(n), 256, 0, q, r0, n, (const SolveState*)st);
-      }
-      launch(h, k_dot, red_blocks(n), kReduceThreads, 0, q, (const float*)r0, (const float*)r0, n, rb, (int)RED_RTR0,
-             o.eps, inv_n);
-      vcycle<D>(h, st, q);
-      launch(h, k_update_p, stream_blocks(n), 256, 0, q, p, (const float*)z0, n, (const SolveState*)st);
-      launch(h, k_dot, red_blocks(n), kReduceThreads, 0, q, (const float*)z0, (const float*)r0, n, rb,
-             (int)RED_ZTR_INIT, o.eps, inv_n);
+    auto recenter = [&](cudaStream_t q) {
+      if (!neu) return;
+      launch(h, k_dot, red_blocks(n), kReduceThreads, 0, q, (const float*)r0, (const float*)nullptr, n, rb,
+             (int)RED_MEAN, o.eps, inv_n, mi);
+      launch(h, k_sub_mean, stream_blocks(n), 256, 0, q, r0, n, (const SolveState*)st);
     };
-    auto iter = [&](cudaStream_t q) {
+    auto first_half = [&](cudaStream_t q) {
       launch(h, k_Ap_dot<D>, red_blocks(n), kReduceThreads, 0, q, (const float*)p, Ap, L0, bc, rb, o.eps);
       launch(h, k_update_xr, red_blocks(n), kReduceThreads, 0, q, x, (const float*)p, r0, (const float*)Ap, n, rb, o.tol,
              o.tol_mode);
-      if (neu) {
-        launch(h, k_dot, red_blocks(n), kReduceThreads, 0, q, (const float*)r0, (const float*)nullptr, n, rb,
-               (int)RED_MEAN, o.eps, inv_n);
-        launch(h, k_sub_mean, stream_blocks(n), 256, 0, q, r0, n, (const SolveState*)st);
-      }
+    };
+    auto setup = [&](cudaStream_t q) {
+      // init(): x = p = Ap = 0 (3D/mgpcg.py:63-79); z0 is zeroed by the V-cycle
+      cudaMemsetAsync(st, 0, sizeof(SolveState), q);
+      cudaMemsetAsync(x, 0, n * 4, q);
+      cudaMemsetAsync(p, 0, n * 4, q);
+      cudaMemsetAsync(Ap, 0, n * 4, q);
+      recenter(q);
+      launch(h, k_dot, red_blocks(n), kReduceThreads, 0, q, (const float*)r0, (const float*)r0, n, rb, (int)RED_RTR0,
+             o.eps, inv_n, mi);
       vcycle<D>(h, st, q);
-      launch(h, k_dot, red_blocks(n), kReduceThreads, 0, q, (const float*)z0, (const float*)r0, n, rb, (int)RED_ZTR,
-             o.eps, inv_n);
       launch(h, k_update_p, stream_blocks(n), 256, 0, q, p, (const float*)z0, n, (const SolveState*)st);
+      launch(h, k_dot, red_blocks(n), kReduceThreads, 0, q, (const float*)z0, (const float*)r0, n, rb,
+             (int)RED_ZTR_INIT, o.eps, inv_n, mi);
+      first_half(q);
     };
     int rc = capture(h, setup, &h->g_setup, &h->g_setup_nodes);
     if (rc) return rc;
-    rc = capture(h, iter, &h->g_iter, &h->g_iter_nodes);
+    // loop graph: k_loop_begin -> WHILE(cond) { body } -> state readback
+    cudaStream_t cs = h->cap_stream;
+    rc = check_cuda(h, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "begin capture");
+    if (rc) return rc;
+    cudaStreamCaptureStatus cst;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    cudaGraphConditionalHandle cond;
+    cudaGraph_t body = nullptr;
+    cudaGraphNode_t cnode;
+    const uint64_t before = h->launches;
+    rc = check_cuda(h, cudaStreamGetCaptureInfo(cs, &cst, nullptr, &g, nullptr, nullptr, nullptr), "capture info");
+    if (!rc) rc = check_cuda(h, cudaGraphConditionalHandleCreate(&cond, g, 0, 0), "conditional handle");
+    if (!rc) {
+      launch(h, k_loop_begin, 1, 1, 0, cs, st, chunk, cond);
+      rc = check_cuda(h, cudaStreamGetCaptureInfo(cs, &cst, nullptr, &g, &deps, nullptr, &ndeps), "capture info");
+    }
+    if (!rc) {
+      cudaGraphNodeParams cp{};
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = cond;
+      cp.conditional.type = cudaGraphCondTypeWhile;
+      cp.conditional.size = 1;
+      rc = check_cuda(h, cudaGraphAddNode(&cnode, g, deps, nullptr, ndeps, &cp), "while node");
+      if (!rc) body = cp.conditional.phGraph_out[0];
+    }
+    if (!rc)
+      rc = check_cuda(h, cudaStreamUpdateCaptureDependencies(cs, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies),
+                      "capture dependencies");
+    if (!rc) cudaMemcpyAsync(hs, st, sizeof(SolveState), cudaMemcpyDeviceToHost, cs);
+    cudaGraph_t top = nullptr;
+    int rc_end = check_cuda(h, cudaStreamEndCapture(cs, &top), "end capture");
+    if (rc || rc_end) {
+      if (top) cudaGraphDestroy(top);
+      h->launches = before;
+      return rc ? rc : rc_end;
+    }
+    rc = check_cuda(h, cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+                    "begin body capture");
+    if (!rc) {
+      const uint64_t b0 = h->launches;
+      recenter(cs);
+      vcycle<D>(h, st, cs);
+      launch(h, k_dot, red_blocks(n), kReduceThreads, 0, cs, (const float*)z0, (const float*)r0, n, rb, (int)RED_ZTR,
+             o.eps, inv_n, mi);
+      launch(h, k_update_p, stream_blocks(n), 256, 0, cs, p, (const float*)z0, n, (const SolveState*)st);
+      first_half(cs);
+      launch(h, k_loop_cond, 1, 1, 0, cs, (const SolveState*)st, cond);
+      h->g_body_nodes = (int)(h->launches - b0);
+      cudaGraph_t b2 = nullptr;
+      rc = check_cuda(h, cudaStreamEndCapture(cs, &b2), "end body capture");
+    }
+    h->launches = before;
+    if (!rc) rc = check_cuda(h, cudaGraphInstantiate(&h->g_loop, top, 0), "loop graph instantiate");
+    cudaGraphDestroy(top);
     if (rc) return rc;
     h->g_eps = o.eps;
     h->g_tol = o.tol;
     h->g_mode = o.tol_mode;
+    h->g_max_iters = mi;
+    h->g_chunk = chunk;
     h->g_valid = 1;
   }
-  int rc = check_cuda(h, cudaMemsetAsync(st, 0, sizeof(SolveState), s), "memset state");
+  int rc = run_graph(h, h->g_setup, h->g_setup_nodes, s);
   if (rc) return rc;
-  // init(): x = p = Ap = 0 (3D/mgpcg.py:63-79); z0 is zeroed by the V-cycle
-  cudaMemsetAsync(x, 0, n * 4, s);
-  cudaMemsetAsync(p, 0, n * 4, s);
-  cudaMemsetAsync(Ap, 0, n * 4, s);
-  rc = run_graph(h, h->g_setup, h->g_setup_nodes, s);
-  if (rc) return rc;
-  int enq = 0;
-  SolveState* hs = h->h_state;
+  int it_before = 0;
   while (true) {
-    int chunk = o.check_every;
-    if (o.max_iters >= 0 && enq + chunk > o.max_iters) chunk = o.max_iters - enq;
-    for (int c = 0; c < chunk; ++c) {
-      rc = run_graph(h, h->g_iter, h->g_iter_nodes, s);
-      if (rc) return rc;
-    }
-    enq += chunk;
-    rc = check_cuda(h, cudaMemcpyAsync(hs, st, sizeof(SolveState), cudaMemcpyDeviceToHost, s), "state readback");
+    rc = check_cuda(h, cudaGraphLaunch(h->g_loop, s), "loop graph launch");
     if (rc) return rc;
     rc = check_cuda(h, cudaStreamSynchronize(s), "mgpcg sync");
     if (rc) return rc;
-    if (hs->done) break;
-    if (o.max_iters >= 0 && enq >= o.max_iters) break;
+    // kernels launched: k_loop_begin, one body per completed iteration, k_loop_cond inside
+    h->launches += 1 + (uint64_t)h->g_body_nodes * (uint64_t)(hs->it - it_before);
+    it_before = hs->it;
+    if (hs->done || mi >= 0) break;
   }
   if (stats) {
     stats->converged = hs->done == 1;
@@ -729,7 +806,8 @@ static int poisson_impl(pfm_handle* h, float* const* u, float* p_out, const pfm_
                                                           h->cfg.boundary[f][1] == 2);
   }
   float* r0 = ws_ptr<float>(h, h->o_r[0]);
-  launch(h, k_divergence<D>, grid_for(h->cells, 256), 256, 0, s, u[0], u[1], D == 3 ? u[2] : nullptr, g, r0);
+  launch(h, k_divergence<D>, grid_for(h->cells, 256), 256, 0, s, u[0], u[1], D == 3 ? u[2] : nullptr, lvl_of(h, 0),
+         r0);
   rc = launch_check(h, "divergence");
   if (rc) return rc;
   int solve_rc = mgpcg_solve_in_place(h, p_out, opts, stats, s);
@@ -737,8 +815,10 @@ static int poisson_impl(pfm_handle* h, float* const* u, float* p_out, const pfm_
   if (solve_rc != PFM_OK && solve_rc != PFM_ERR_NOT_CONVERGED) return solve_rc;
   for (int f = 0; f < D; ++f) {
     int64_t nf = (int64_t)g.n[f][0] * g.n[f][1] * g.n[f][2];
-    launch(h, k_subtract_grad_p<D>, grid_for(nf, 256), 256, 0, s, u[f], f, x, g, h->cfg.boundary[f][0] == 2,
-                                                          h->cfg.boundary[f][1] == 2);
+    const int lo = h->cfg.boundary[f][0] == 2, hi = h->cfg.boundary[f][1] == 2;
+    if (f == 0) launch(h, k_subtract_grad_p<D, 0>, grid_for(nf, 256), 256, 0, s, u[f], x, g, lo, hi);
+    if (f == 1) launch(h, k_subtract_grad_p<D, 1>, grid_for(nf, 256), 256, 0, s, u[f], x, g, lo, hi);
+    if (f == 2) launch(h, k_subtract_grad_p<D, 2>, grid_for(nf, 256), 256, 0, s, u[f], x, g, lo, hi);
   }
   rc = launch_check(h, "subtract_grad_p");
   if (rc) return rc;

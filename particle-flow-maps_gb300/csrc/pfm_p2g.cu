@@ -322,14 +322,26 @@ __device__ __forceinline__ void tile_family(float2* __restrict__ acc, const floa
         __syncthreads();
       }
   const int n0 = g.n[FAM][0], n1 = g.n[FAM][1], n2 = g.n[FAM][2];
-  for (int e = threadIdx.x; e < NE; e += kTileThreads) {
+  constexpr int NPT = (NE + kTileThreads - 1) / kTileThreads;
+  int64_t qs[NPT];
+  float2 vs[NPT];
+#pragma unroll
+  for (int j = 0; j < NPT; ++j) {  // all reads first: one memory latency for the whole add-back
+    const int e = threadIdx.x + j * kTileThreads;
     const int ez = e % E2, r = e / E2, ey = r % E1, ex = r / E1;
     const int gi = x0 - 1 + ex, gj = y0 - 1 + ey, gk = z0 - 1 + ez;
-    if (gi >= 0 && gi < n0 && gj >= 0 && gj < n1 && gk >= 0 && gk < n2) {
+    qs[j] = -1;
+    if (e < NE && gi >= 0 && gi < n0 && gj >= 0 && gj < n1 && gk >= 0 && gk < n2) {
+      qs[j] = ((int64_t)gi * n1 + gj) * n2 + gk;
       const float2 v = acc[e];
-      const int64_t q = ((int64_t)gi * n1 + gj) * n2 + gk;
-      u[q] += v.x;
-      w[q] += v.y;
+      vs[j] = make_float2(v.x + u[qs[j]], v.y + w[qs[j]]);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < NPT; ++j) {
+    if (qs[j] >= 0) {
+      u[qs[j]] = vs[j].x;
+      w[qs[j]] = vs[j].y;
     }
   }
   __syncthreads();
