@@ -66,8 +66,9 @@ typedef struct pfm_solve_opts {
   double eps;      /* 1e-12, added to the denominators of alpha and beta */
   double tol;      /* 1e-12 in Poisson() */
   int tol_mode;    /* 0 absolute r.r, 1 relative norm */
-  int check_every; /* host convergence check cadence in iterations (>= 1); iterations after
-                      convergence inside a cadence block are skipped on the device */
+  int check_every; /* the iteration loop runs on the device (a CUDA graph WHILE node) and the
+                      host waits once per solve; with max_iters = -1 the host relaunches the
+                      loop every check_every iterations (>= 1) until it converges */
 } pfm_solve_opts;
 
 typedef struct pfm_solve_stats {
@@ -79,7 +80,9 @@ typedef struct pfm_solve_stats {
 
 /* ---- handle, workspace, errors ------------------------------------------------------------- */
 
-/* Creates a handle for one scene.  No device memory is allocated by the library. */
+/* Creates a handle for one scene.  No device memory is allocated by the library.  Grids whose
+ * cell or face fields hold 2^31 or more entries are rejected (PFM_ERR_SHAPE): the grid kernels
+ * index with 32-bit integers. */
 int pfm_create(const pfm_config* cfg, pfm_handle** out);
 int pfm_destroy(pfm_handle* h);
 /* Bytes of device scratch the handle needs (sort buffers, P2G payload, MGPCG hierarchy). */
