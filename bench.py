@@ -289,8 +289,10 @@ def main():
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t0 = time.perf_counter()
     e0.record()
+    torch.cuda.nvtx.range_push("pfm_timed_steps")  # lets ncu --nvtx-include select the timed steps
     for _ in range(args.steps):
         sim.step()
+    torch.cuda.nvtx.range_pop()
     e1.record()
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
@@ -316,8 +318,13 @@ def main():
     rk4_ms = statistics.mean(phases["rk4"])
     rk4_bytes = P * 96 + F3 * 4  # pos + T read and written (48 B + 48 B / particle) + velocity grid once
     achieved = rk4_bytes / (rk4_ms / 1e3) / 1e9
+    # DRAM bytes of one launch: dram__bytes_read.sum + dram__bytes_write.sum of the ncu capture at
+    # 128^3 (830,966,528 + 744,071,424 B for 16,777,216 particles, profiles/k_rk4_T_forward3_128.md),
+    # scaled by the particle count (the grid scales with it at a fixed particle density)
+    traffic = (830966528 + 744071424) / 16777216 * P
     roofline = {"bound": "hbm", "kernel": "k_rk4_T_forward3", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                "traffic_source": "ncu capture at 128^3 scaled by the particle count",
                 "bytes_per_launch": rk4_bytes, "ms_per_launch": rk4_ms}
 
     e2e = None
