@@ -168,14 +168,18 @@ __device__ __forceinline__ float dN2(float x) {
 //   dN_2: t - 0.5,          -2 t,        t + 0.5
 // (the |x| = 0.5 and 1.5 boundary cases included).  For s >= 1 every subtraction involved is
 // exact, so the weights are bitwise those of the reference's per-tap evaluation.
-// Indices are clamped like sample() (3D/taichi_utils.py:48-54).
+// sample() clamps every tap index to [0, n-1] (3D/taichi_utils.py:48-54), but the position is
+// first clamped to [1, n - 2 - eps], so floor(s) lies in [1, n-3] and the three taps
+// first .. first+2 always lie in [0, n-1] (n >= 4 is enforced when the handle is created; a NaN
+// or infinite position clamps to an end of the range too).  The clamp never changes an index, so
+// only the first tap is stored and the taps of a row are three consecutive floats.
 struct Axis3 {
-  int idx[3];
+  int first;
   float w[3];
   float dw[3];
 };
 
-__device__ __forceinline__ void axis_taps(float u, float hi, int n, Axis3& a) {
+__device__ __forceinline__ void axis_taps(float u, float hi, Axis3& a) {
   const float s = fmaxf(1.f, fminf(u, hi));
   const float iu = floorf(s);
   const float frac = s - iu;
@@ -188,56 +192,7 @@ __device__ __forceinline__ void axis_taps(float u, float hi, int n, Axis3& a) {
   a.dw[0] = t - 0.5f;
   a.dw[1] = -2.f * t;
   a.dw[2] = t + 0.5f;
-  const int first = __float2int_rz(iu) + (lo ? -1 : 0);
-#pragma unroll
-  for (int q = 0; q < 3; ++q) {
-    int id = first + q;
-    id = id < 0 ? 0 : (id > n - 1 ? n - 1 : id);
-    a.idx[q] = id;
-  }
-}
-
-// Value and gradient of one MAC component at a position, from precomputed axis taps.
-__device__ __forceinline__ void interp3_component(const float* __restrict__ f, int n1, int n2,
-                                                  const Axis3& X, const Axis3& Y, const Axis3& Z,
-                                                  float inv_dx, float& val, float& gx, float& gy,
-                                                  float& gz) {
-  float v_ = 0.f, x_ = 0.f, y_ = 0.f, z_ = 0.f;
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-#pragma unroll
-    for (int b = 0; b < 3; ++b) {
-      const float* row = f + ((size_t)X.idx[a] * n1 + Y.idx[b]) * n2;
-      float v0 = __ldg(row + Z.idx[0]), v1 = __ldg(row + Z.idx[1]), v2 = __ldg(row + Z.idx[2]);
-      float tn = v0 * Z.w[0] + v1 * Z.w[1] + v2 * Z.w[2];
-      float td = v0 * Z.dw[0] + v1 * Z.dw[1] + v2 * Z.dw[2];
-      float wxy = X.w[a] * Y.w[b];
-      v_ += wxy * tn;
-      x_ += (X.dw[a] * Y.w[b]) * tn;
-      y_ += (X.w[a] * Y.dw[b]) * tn;
-      z_ += wxy * td;
-    }
-  }
-  val = v_;
-  gx = x_ * inv_dx;
-  gy = y_ * inv_dx;
-  gz = z_ * inv_dx;
-}
-
-__device__ __forceinline__ float interp3_value(const float* __restrict__ f, int n1, int n2,
-                                               const Axis3& X, const Axis3& Y, const Axis3& Z) {
-  float v_ = 0.f;
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-#pragma unroll
-    for (int b = 0; b < 3; ++b) {
-      const float* row = f + ((size_t)X.idx[a] * n1 + Y.idx[b]) * n2;
-      float tn = __ldg(row + Z.idx[0]) * Z.w[0] + __ldg(row + Z.idx[1]) * Z.w[1] +
-                 __ldg(row + Z.idx[2]) * Z.w[2];
-      v_ += (X.w[a] * Y.w[b]) * tn;
-    }
-  }
-  return v_;
+  a.first = __float2int_rz(iu) + (lo ? -1 : 0);
 }
 
 // interp_u_MAC_grad (3D/taichi_utils.py:312-317): u at p and G[c][r] = d u_c / d x_r.
@@ -263,8 +218,8 @@ __device__ __forceinline__ void interp_mac3(const MacFields3& F, const MacGeom& 
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     float u = p[a] / g.dx;
-    axis_taps(u - 0.0f, g.hi[a][a], g.n[a][a], A0[a]);               // the component along a
-    axis_taps(u - 0.5f, g.hi[(a + 1) % 3][a], g.n[(a + 1) % 3][a], A1[a]);  // the others
+    axis_taps(u - 0.0f, g.hi[a][a], A0[a]);            // the component along a
+    axis_taps(u - 0.5f, g.hi[(a + 1) % 3][a], A1[a]);  // the others
   }
   const float inv_dx = g.inv_dx;
   // ---- components x and y together: x uses (A0x, A1y, A1z), y uses (A1x, A0y, A1z)
@@ -273,6 +228,9 @@ __device__ __forceinline__ void interp_mac3(const MacFields3& F, const MacGeom& 
     const float* __restrict__ f1 = F.u[1];
     const int m01 = g.n[0][1], m02 = g.n[0][2], m11 = g.n[1][1], m12 = g.n[1][2];
     const Axis3& Z = A1[2];
+    const float* __restrict__ b0 = f0 + ((A0[0].first * m01 + A1[1].first) * m02 + Z.first);
+    const float* __restrict__ b1 = f1 + ((A1[0].first * m11 + A0[1].first) * m12 + Z.first);
+    const int sx0 = m01 * m02, sx1 = m11 * m12;
     const float2 zw0 = f2(Z.w[0], Z.w[0]), zw1 = f2(Z.w[1], Z.w[1]), zw2 = f2(Z.w[2], Z.w[2]);
     float2 V = f2(0.f, 0.f), GX = V, GY = V, GZ = V;
 #pragma unroll
@@ -280,11 +238,11 @@ __device__ __forceinline__ void interp_mac3(const MacFields3& F, const MacGeom& 
       float2 Aa = f2(0.f, 0.f), Ba = Aa, Ca = Aa;
 #pragma unroll
       for (int b = 0; b < 3; ++b) {
-        const int r0 = (A0[0].idx[a] * m01 + A1[1].idx[b]) * m02;
-        const int r1 = (A1[0].idx[a] * m11 + A0[1].idx[b]) * m12;
-        const float2 v0 = f2(__ldg(f0 + r0 + Z.idx[0]), __ldg(f1 + r1 + Z.idx[0]));
-        const float2 v1 = f2(__ldg(f0 + r0 + Z.idx[1]), __ldg(f1 + r1 + Z.idx[1]));
-        const float2 v2 = f2(__ldg(f0 + r0 + Z.idx[2]), __ldg(f1 + r1 + Z.idx[2]));
+        const float* __restrict__ r0 = b0 + (a * sx0 + b * m02);
+        const float* __restrict__ r1 = b1 + (a * sx1 + b * m12);
+        const float2 v0 = f2(__ldg(r0), __ldg(r1));
+        const float2 v1 = f2(__ldg(r0 + 1), __ldg(r1 + 1));
+        const float2 v2 = f2(__ldg(r0 + 2), __ldg(r1 + 2));
         float2 tn = __fmul2_rn(v0, zw0);
         tn = __ffma2_rn(v1, zw1, tn);
         tn = __ffma2_rn(v2, zw2, tn);
@@ -323,14 +281,16 @@ __device__ __forceinline__ void interp_mac3(const MacFields3& F, const MacGeom& 
     const float* __restrict__ f = F.u[2];
     const int m1 = g.n[2][1], m2 = g.n[2][2];
     const Axis3 &X = A1[0], &Y = A1[1], &Z = A0[2];
+    const float* __restrict__ base = f + ((X.first * m1 + Y.first) * m2 + Z.first);
+    const int sx = m1 * m2;
     float v_ = 0.f, x_ = 0.f, y_ = 0.f, z_ = 0.f;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
       float Aa = 0.f, Ba = 0.f, Ca = 0.f;
 #pragma unroll
       for (int b = 0; b < 3; ++b) {
-        const float* row = f + (X.idx[a] * m1 + Y.idx[b]) * m2;
-        const float v0 = __ldg(row + Z.idx[0]), v1 = __ldg(row + Z.idx[1]), v2 = __ldg(row + Z.idx[2]);
+        const float* __restrict__ row = base + (a * sx + b * m2);
+        const float v0 = __ldg(row), v1 = __ldg(row + 1), v2 = __ldg(row + 2);
         const float tn = fmaf(v2, Z.w[2], fmaf(v1, Z.w[1], v0 * Z.w[0]));
         Aa = fmaf(Y.w[b], tn, Aa);
         if (want_grad) {
@@ -368,8 +328,8 @@ __device__ __forceinline__ void interp2_component(const float* __restrict__ f, i
   float v_ = 0.f, x_ = 0.f, y_ = 0.f;
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    const float* row = f + (size_t)X.idx[a] * n1;
-    float v0 = __ldg(row + Y.idx[0]), v1 = __ldg(row + Y.idx[1]), v2 = __ldg(row + Y.idx[2]);
+    const float* __restrict__ row = f + ((X.first + a) * n1 + Y.first);
+    float v0 = __ldg(row), v1 = __ldg(row + 1), v2 = __ldg(row + 2);
     float tn = v0 * Y.w[0] + v1 * Y.w[1] + v2 * Y.w[2];
     float td = v0 * Y.dw[0] + v1 * Y.dw[1] + v2 * Y.dw[2];
     v_ += X.w[a] * tn;
@@ -387,8 +347,8 @@ __device__ __forceinline__ void interp_mac2(const MacFields2& F, const MacGeom& 
 #pragma unroll
   for (int a = 0; a < 2; ++a) {
     float u = p[a] / g.dx;
-    axis_taps(u - 0.0f, g.hi[a][a], g.n[a][a], A0[a]);
-    axis_taps(u - 0.5f, g.hi[1 - a][a], g.n[1 - a][a], A1[a]);
+    axis_taps(u - 0.0f, g.hi[a][a], A0[a]);
+    axis_taps(u - 0.5f, g.hi[1 - a][a], A1[a]);
   }
 #pragma unroll
   for (int c = 0; c < 2; ++c) {
