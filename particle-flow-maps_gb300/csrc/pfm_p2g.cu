@@ -153,48 +153,61 @@ __global__ void __launch_bounds__(kBinThreads) k_cell_sort(const int* __restrict
   }
 }
 
-// Payload (3D), structure of float4 arrays in sorted order s:
-//   pos4[s]      = (pos/dx, 0)                         -- read by every visit
-//   famrec[f][s] = (m_f, (T C T)_f row)  f = x, y, z   -- read when the particle reaches the face
-// m = T_gm^T-composed init_imp and T C T = T_gm^T init_C T_gm as in 3D/run_3D.py:462-479.
-__global__ void __launch_bounds__(kBinThreads) k_payload3(const int* __restrict__ order, int64_t P, MacGeom g,
-                                                          const float* __restrict__ pos, const float* __restrict__ imp0,
-                                                          const float* __restrict__ Tg, const float* __restrict__ Ti,
-                                                          const float* __restrict__ C, float4* __restrict__ pos4,
-                                                          float4* __restrict__ famrec) {
-  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < P) {
-    const int64_t q = order[s];
-    float A[3][3], Cm[3][3], N[3][3];
+// Payload and cell keys (3D), one pass in particle order q (coalesced reads and writes):
+//   pos4[q]      = (pos/dx, 0)                         -- read by every window update
+//   famrec[f][q] = (m_f, (T C T)_f row)  f = x, y, z   -- read for face family f
+//   key[q]       = linear cell of int(pos/dx) (clamped), slot[q] = arrival in its bin
+// m = T_gm^T-composed init_imp and T C T = T_gm^T init_C T_gm as in 3D/run_3D.py:462-479; the
+// key is get_particles_id_in_every_cell's int(particles_pos[i] / dx) (3D/run_3D.py:348).
+__global__ void __launch_bounds__(kBinThreads) k_payload_keys3(int64_t P, MacGeom g, const float* __restrict__ pos,
+                                                               const float* __restrict__ imp0,
+                                                               const float* __restrict__ Tg,
+                                                               const float* __restrict__ Ti,
+                                                               const float* __restrict__ C, float4* __restrict__ pos4,
+                                                               float4* __restrict__ famrec, int* __restrict__ key,
+                                                               int* __restrict__ slot, int* __restrict__ count) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= P) return;
+  const float px = pos[q] / g.dx, py = pos[P + q] / g.dx, pz = pos[2 * P + q] / g.dx;
+  int c[3];
+  const float pv[3] = {px, py, pz};
 #pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        A[r][c] = Tg[(r * 3 + c) * P + q];   // rows(T_gm): A[r][c] = T_gm_r[c]
-        Cm[r][c] = C[(r * 3 + c) * P + q];   // rows(init_C)
-        N[c][r] = Ti[(r * 3 + c) * P + q];   // cols(T_init): N[k][c'] = T_init_c'[k]
-      }
-    // TCT = A^T (C A); T_transpose = A^T N; m = T_transpose init_imp
-    float CA[3][3], TCT[3][3], TT[3][3];
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-      for (int c = 0; c < 3; ++c) CA[r][c] = Cm[r][0] * A[0][c] + Cm[r][1] * A[1][c] + Cm[r][2] * A[2][c];
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        TCT[r][c] = A[0][r] * CA[0][c] + A[1][r] * CA[1][c] + A[2][r] * CA[2][c];
-        TT[r][c] = A[0][r] * N[0][c] + A[1][r] * N[1][c] + A[2][r] * N[2][c];
-      }
-    float m0[3] = {imp0[q], imp0[P + q], imp0[2 * P + q]};
-    float m[3];
-#pragma unroll
-    for (int r = 0; r < 3; ++r) m[r] = TT[r][0] * m0[0] + TT[r][1] * m0[1] + TT[r][2] * m0[2];
-    pos4[s] = make_float4(pos[q] / g.dx, pos[P + q] / g.dx, pos[2 * P + q] / g.dx, 0.f);
-#pragma unroll
-    for (int f = 0; f < 3; ++f) famrec[f * P + s] = make_float4(m[f], TCT[f][0], TCT[f][1], TCT[f][2]);
+  for (int a = 0; a < 3; ++a) {
+    const int ci = __float2int_rz(pv[a]);
+    c[a] = ci < 0 ? 0 : (ci > g.N[a] - 1 ? g.N[a] - 1 : ci);
   }
+  const int k = (c[0] * g.N[1] + c[1]) * g.N[2] + c[2];
+  key[q] = k;
+  slot[q] = atomicAdd(&count[k], 1);
+  float A[3][3], Cm[3][3], N[3][3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc) {
+      A[r][cc] = Tg[(r * 3 + cc) * P + q];   // rows(T_gm): A[r][c] = T_gm_r[c]
+      Cm[r][cc] = C[(r * 3 + cc) * P + q];   // rows(init_C)
+      N[cc][r] = Ti[(r * 3 + cc) * P + q];   // cols(T_init): N[k][c'] = T_init_c'[k]
+    }
+  // TCT = A^T (C A); T_transpose = A^T N; m = T_transpose init_imp
+  float CA[3][3], TCT[3][3], TT[3][3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc) CA[r][cc] = Cm[r][0] * A[0][cc] + Cm[r][1] * A[1][cc] + Cm[r][2] * A[2][cc];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc) {
+      TCT[r][cc] = A[0][r] * CA[0][cc] + A[1][r] * CA[1][cc] + A[2][r] * CA[2][cc];
+      TT[r][cc] = A[0][r] * N[0][cc] + A[1][r] * N[1][cc] + A[2][r] * N[2][cc];
+    }
+  const float m0[3] = {imp0[q], imp0[P + q], imp0[2 * P + q]};
+  float m[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) m[r] = TT[r][0] * m0[0] + TT[r][1] * m0[1] + TT[r][2] * m0[2];
+  pos4[q] = make_float4(px, py, pz, 0.f);
+#pragma unroll
+  for (int f = 0; f < 3; ++f) famrec[f * P + q] = make_float4(m[f], TCT[f][0], TCT[f][1], TCT[f][2]);
 }
 
 // Payload (2D): pos4 = (pos/dx, psi), famrec[f] = (imp_f, C_f row, 0)
@@ -270,7 +283,8 @@ __device__ __forceinline__ void tile_axis(float p, int c, float dx, float* w, fl
 
 template <int FAM>
 __device__ __forceinline__ void tile_family(float2* __restrict__ acc, const float4* __restrict__ pos4,
-                                            const float4* __restrict__ rec, int sb, int se, int ci, int cj, int ck,
+                                            const float4* __restrict__ rec, const int* __restrict__ order, int sb,
+                                            int se, int ci, int cj, int ck,
                                             int lx, int ly, int lz, int x0, int y0, int z0, const MacGeom& g,
                                             int use_apic, float* __restrict__ u, float* __restrict__ w) {
   constexpr int W0 = FAM == 0 ? 4 : 3, W1 = FAM == 1 ? 4 : 3, W2 = FAM == 2 ? 4 : 3;
@@ -286,8 +300,9 @@ __device__ __forceinline__ void tile_family(float2* __restrict__ acc, const floa
       for (int k = 0; k < W2; ++k) num[a][b][k] = den[a][b][k] = 0.f;
   const float dx = g.dx;
   for (int s = sb; s < se; ++s) {
-    const float4 p = __ldg(pos4 + s);
-    const float4 fr = __ldg(rec + s);
+    const int q = __ldg(order + s);  // sorted slot -> particle
+    const float4 p = __ldg(pos4 + q);
+    const float4 fr = __ldg(rec + q);
     float w0[W0], d0[W0], w1[W1], d1[W1], w2[W2], d2[W2];
     tile_axis<FAM == 0>(p.x, ci, dx, w0, d0);
     tile_axis<FAM == 1>(p.y, cj, dx, w1, d1);
@@ -350,6 +365,7 @@ __device__ __forceinline__ void tile_family(float2* __restrict__ acc, const floa
 // One parity class (px, py, pz) of tiles; grid = (tiles along z, y, x of that parity).
 __global__ void __launch_bounds__(kTileThreads, 1) k_tile3(const float4* __restrict__ pos4,
                                                            const float4* __restrict__ famrec,
+                                                           const int* __restrict__ order,
                                                            const int* __restrict__ start, MacGeom g, int use_apic,
                                                            int64_t P, int px, int py, int pz, FaceOut3 out) {
   __shared__ float2 acc[kTileExtMax];
@@ -363,10 +379,10 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_tile3(const float4* __restr
     sb = __ldg(start + c);
     se = __ldg(start + c + 1);
   }
-  tile_family<0>(acc, pos4, famrec, sb, se, ci, cj, ck, lx, ly, lz, x0, y0, z0, g, use_apic, out.u[0], out.w[0]);
-  tile_family<1>(acc, pos4, famrec + P, sb, se, ci, cj, ck, lx, ly, lz, x0, y0, z0, g, use_apic, out.u[1],
+  tile_family<0>(acc, pos4, famrec, order, sb, se, ci, cj, ck, lx, ly, lz, x0, y0, z0, g, use_apic, out.u[0], out.w[0]);
+  tile_family<1>(acc, pos4, famrec + P, order, sb, se, ci, cj, ck, lx, ly, lz, x0, y0, z0, g, use_apic, out.u[1],
                  out.w[1]);
-  tile_family<2>(acc, pos4, famrec + 2 * P, sb, se, ci, cj, ck, lx, ly, lz, x0, y0, z0, g, use_apic, out.u[2],
+  tile_family<2>(acc, pos4, famrec + 2 * P, order, sb, se, ci, cj, ck, lx, ly, lz, x0, y0, z0, g, use_apic, out.u[2],
                  out.w[2]);
 }
 
@@ -485,17 +501,36 @@ __global__ void __launch_bounds__(128) k_gather2(const float4* __restrict__ pos4
   for (int q = 0; q < WIN; ++q) flush(jb + q, q);
 }
 
-int sort_particles(pfm_handle* h, const float* pos, cudaStream_t st) {
-  int rc = require_ws(h);
-  if (rc) return rc;
+// Bins with counted keys/slots -> bin starts and the stable order (scan, scatter, per-bin sort).
+static int sort_from_keys(pfm_handle* h, cudaStream_t st) {
   const int64_t P = h->P, C = h->cells;
-  int* key = ws_ptr<int>(h, h->o_key);
-  int* slot = ws_ptr<int>(h, h->o_slot);
+  const int* key = ws_ptr<int>(h, h->o_key);
+  const int* slot = ws_ptr<int>(h, h->o_slot);
   int* order = ws_ptr<int>(h, h->o_order);
   int* count = ws_ptr<int>(h, h->o_count);
   int* start = ws_ptr<int>(h, h->o_start);
   int* bsum = ws_ptr<int>(h, h->o_blocksums);
-  rc = check_cuda(h, cudaMemsetAsync(count, 0, C * 4, st), "memset counts");
+  const int64_t per_block = (int64_t)kScanThreads * kScanItems;
+  const int nb = (int)((C + per_block - 1) / per_block);
+  if (nb > kScanThreads * kScanItems) return set_error(h, PFM_ERR_SHAPE, "too many cells for the bin scan");
+  launch(h, k_scan_blocksums, nb, kScanThreads, 0, st, (const int*)count, C, bsum);
+  launch(h, k_scan_top, 1, kScanThreads, 0, st, bsum, nb);
+  launch(h, k_scan_apply, nb, kScanThreads, 0, st, (const int*)count, C, (const int*)bsum, start, (int)P);
+  if (P > 0) {
+    launch(h, k_scatter_order, grid_for(P, kBinThreads), kBinThreads, 0, st, key, slot, (const int*)start, P, order);
+    launch(h, k_cell_sort, grid_for(C, kBinThreads), kBinThreads, 0, st, (const int*)start, C, order);
+  }
+  return launch_check(h, "sort_particles");
+}
+
+int sort_particles(pfm_handle* h, const float* pos, cudaStream_t st) {
+  int rc = require_ws(h);
+  if (rc) return rc;
+  const int64_t P = h->P;
+  int* key = ws_ptr<int>(h, h->o_key);
+  int* slot = ws_ptr<int>(h, h->o_slot);
+  int* count = ws_ptr<int>(h, h->o_count);
+  rc = check_cuda(h, cudaMemsetAsync(count, 0, h->cells * 4, st), "memset counts");
   if (rc) return rc;
   if (P > 0) {
     if (h->cfg.dim == 3)
@@ -503,17 +538,7 @@ int sort_particles(pfm_handle* h, const float* pos, cudaStream_t st) {
     else
       launch(h, k_bin_keys<2>, grid_for(P, kBinThreads), kBinThreads, 0, st, pos, P, h->geom, key, slot, count);
   }
-  const int64_t per_block = (int64_t)kScanThreads * kScanItems;
-  const int nb = (int)((C + per_block - 1) / per_block);
-  if (nb > kScanThreads * kScanItems) return set_error(h, PFM_ERR_SHAPE, "too many cells for the bin scan");
-  launch(h, k_scan_blocksums, nb, kScanThreads, 0, st, count, C, bsum);
-  launch(h, k_scan_top, 1, kScanThreads, 0, st, bsum, nb);
-  launch(h, k_scan_apply, nb, kScanThreads, 0, st, count, C, bsum, start, (int)P);
-  if (P > 0) {
-    launch(h, k_scatter_order, grid_for(P, kBinThreads), kBinThreads, 0, st, key, slot, start, P, order);
-    launch(h, k_cell_sort, grid_for(C, kBinThreads), kBinThreads, 0, st, start, C, order);
-  }
-  return launch_check(h, "sort_particles");
+  return sort_from_keys(h, st);
 }
 
 static int copy_sort_out(pfm_handle* h, int* cell_count, int* order, cudaStream_t st) {
@@ -563,16 +588,21 @@ int pfm3_p2g(pfm_handle* h, const float* init_imp, const float* pos, const float
   if (h->P > 0 && (!init_imp || !pos || !T_gm || !T_init || !init_C))
     return set_error(h, PFM_ERR_NULL, "pfm3_p2g: null particle field");
   cudaStream_t st = (cudaStream_t)stream;
-  int rc = sort_particles(h, pos, st);
+  int rc = require_ws(h);
   if (rc) return rc;
   float4* pos4 = ws_ptr<float4>(h, h->o_payload);
   float4* famrec = pos4 + h->P;
   float* us[3] = {u_x, u_y, u_z};
   float* ws[3] = {w_x, w_y, w_z};
   const int* start = ws_ptr<int>(h, h->o_start);
+  const int* order = ws_ptr<int>(h, h->o_order);
+  rc = check_cuda(h, cudaMemsetAsync(ws_ptr<int>(h, h->o_count), 0, h->cells * 4, st), "memset counts");
+  if (rc) return rc;
   if (h->P > 0)
-    launch(h, k_payload3, grid_for(h->P, kBinThreads), kBinThreads, 0, st, ws_ptr<int>(h, h->o_order), h->P, h->geom,
-           pos, init_imp, T_gm, T_init, init_C, pos4, famrec);
+    launch(h, k_payload_keys3, grid_for(h->P, kBinThreads), kBinThreads, 0, st, h->P, h->geom, pos, init_imp, T_gm,
+           T_init, init_C, pos4, famrec, ws_ptr<int>(h, h->o_key), ws_ptr<int>(h, h->o_slot), ws_ptr<int>(h, h->o_count));
+  rc = sort_from_keys(h, st);
+  if (rc) return rc;
   FaceOut3 out{{u_x, u_y, u_z}, {w_x, w_y, w_z}};
   int64_t F[3];
   for (int f = 0; f < 3; ++f) {
@@ -589,7 +619,7 @@ int pfm3_p2g(pfm_handle* h, const float* init_imp, const float* pos, const float
           const unsigned bx = (nt[0] - px + 1) / 2, by = (nt[1] - py + 1) / 2, bz = (nt[2] - pz + 1) / 2;
           if (!bx || !by || !bz) continue;
           launch(h, k_tile3, dim3(bz, by, bx), kTileThreads, 0, st, (const float4*)pos4, (const float4*)famrec,
-                 start, h->geom, h->cfg.use_apic, h->P, px, py, pz, out);
+                 order, start, h->geom, h->cfg.use_apic, h->P, px, py, pz, out);
         }
     launch(h, k_normalize3, grid_for(F[0] + F[1] + F[2], kBinThreads), kBinThreads, 0, st, out, F[0], F[1], F[2]);
   }
