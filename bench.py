@@ -316,12 +316,15 @@ def main():
     F3 = 3 * (n + 1) * n * n
     peak, peak_kind = measured_peak()
     rk4_ms = statistics.mean(phases["rk4"])
-    rk4_bytes = P * 96 + F3 * 4  # pos + T read and written (48 B + 48 B / particle) + velocity grid once
+    # k_rk4_T_forward3 with the P2G records: pos + T_gm read and written (96 B), init_imp + T_init +
+    # init_C read (84 B), record (64 B) + key + slot (8 B) written per particle; the velocity grid once
+    rk4_bytes = P * (96 + 84 + 64 + 8) + F3 * 4
     achieved = rk4_bytes / (rk4_ms / 1e3) / 1e9
-    # DRAM bytes of one launch: dram__bytes_read.sum + dram__bytes_write.sum of the ncu capture at
-    # 128^3 (830,966,528 + 744,071,424 B for 16,777,216 particles, profiles/k_rk4_T_forward3_128.md),
-    # scaled by the particle count (the grid scales with it at a fixed particle density)
-    traffic = (830966528 + 744071424) / 16777216 * P
+    # DRAM bytes of one launch: dram__bytes_read.sum + dram__bytes_write.sum of the ncu capture of
+    # k_rk4_T_forward3<true> at 128^3 (2,248,936,960 + 1,970,354,944 B for 16,777,216 particles,
+    # profiles/k_rk4_T_forward3_128.md), scaled by the particle count (the grid scales with it at a
+    # fixed particle density)
+    traffic = (2248936960 + 1970354944) / 16777216 * P
     roofline = {"bound": "hbm", "kernel": "k_rk4_T_forward3", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                 "traffic_source": "ncu capture at 128^3 scaled by the particle count",

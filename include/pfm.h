@@ -137,12 +137,31 @@ int pfm3_sort_particles(pfm_handle* h, const float* pos, int* cell_count, int* o
 
 /* P2G (3D/run_3D.py:441-552): APIC transfer of impulse m = T_gm^T T_init^T-composed init_imp
  * with affine term (T_gm^T init_C T_gm) to the faces, normalised by the weight sums.
- * Deterministic, no float atomics: particles are counting-sorted into cell bins, then every face
- * sums its neighbourhood's bins in a fixed order.  Writes u_x/u_y/u_z and the weight grids
- * w_x/w_y/w_z. */
+ * Deterministic, no float atomics: particles are counting-sorted into cell bins, each cell's
+ * particles are summed into the window of faces they reach, and cell tiles merge the windows in
+ * a fixed order.  Writes u_x/u_y/u_z and the weight grids w_x/w_y/w_z. */
 int pfm3_p2g(pfm_handle* h, const float* init_imp, const float* pos, const float* T_gm,
              const float* T_init, const float* init_C, float* u_x, float* u_y, float* u_z,
              float* w_x, float* w_y, float* w_z, void* stream);
+
+/* RK4_T_forward followed by P2G, the pair the step loop calls back to back (3D/run_3D.py:795-812).
+ * pfm3_rk4_p2g_records advances pos/T_gm in the advecting velocity ua over dt (as
+ * pfm3_rk4_T_forward) and, in the same kernel, writes each advected particle's P2G record and
+ * cell key into the workspace, so the particle state is read once.  pfm3_p2g_from_records then
+ * runs the rest of P2G (bin sort, cell tiles, normalisation) from those records; it fails with
+ * PFM_ERR_ARG if no records are present (a sort or 2D P2G call on the handle in between
+ * overwrites them).  pfm3_rk4_p2g does both.  Results are bitwise those of
+ * pfm3_rk4_T_forward(pos, T_gm, ua, dt) followed by pfm3_p2g(init_imp, pos, T_gm, T_init,
+ * init_C, u, w).  ua may be the same grids as u. */
+int pfm3_rk4_p2g_records(pfm_handle* h, float* pos, float* T_gm, const float* ua_x,
+                         const float* ua_y, const float* ua_z, float dt, const float* init_imp,
+                         const float* T_init, const float* init_C, void* stream);
+int pfm3_p2g_from_records(pfm_handle* h, float* u_x, float* u_y, float* u_z, float* w_x,
+                          float* w_y, float* w_z, void* stream);
+int pfm3_rk4_p2g(pfm_handle* h, float* pos, float* T_gm, const float* ua_x, const float* ua_y,
+                 const float* ua_z, float dt, const float* init_imp, const float* T_init,
+                 const float* init_C, float* u_x, float* u_y, float* u_z, float* w_x, float* w_y,
+                 float* w_z, void* stream);
 
 /* MGPCG_3.Poisson (3D/mgpcg.py:425-430): apply_bc, divergence, MGPCG solve of the pressure,
  * subtract_grad_p, apply_bc.  In place on u.  p_out [nx][ny][nz] (may be NULL) receives the

@@ -173,6 +173,7 @@ int pfm_set_workspace(pfm_handle* h, void* dptr, size_t bytes) {
   if (bytes < h->ws_need) return set_error(h, PFM_ERR_WORKSPACE, "workspace smaller than pfm_workspace_size");
   h->ws = (char*)dptr;
   h->ws_bytes = bytes;
+  h->rec_valid = 0;
   return PFM_OK;
 }
 

@@ -102,6 +102,7 @@ struct pfm_handle {
   pfm::SolveState* h_state;
   // kernels launched through this handle (reported by pfm_launch_count)
   uint64_t launches;
+  int rec_valid;  // 3D P2G records and cell keys of the last RK4/payload pass are in the workspace
   // CUDA graphs of the MGPCG setup and of one PCG iteration (captured on first use)
   cudaStream_t cap_stream;
   cudaGraphExec_t g_setup, g_loop;  // setup + first half-iteration; device-side PCG loop
@@ -314,6 +315,70 @@ __device__ __forceinline__ void interp_mac3(const MacFields3& F, const MacGeom& 
     }
   }
 }
+
+// P2G particle record and cell key (3D), shared by the payload pass and the fused RK4 + P2G:
+//   pos4[q]      = (pos/dx, 0)
+//   famrec[f][q] = (m_f, (T C T)_f row), m = T_gm^T-composed init_imp, T C T = T_gm^T init_C T_gm
+//                  (3D/run_3D.py:462-479)
+//   key[q]       = linear cell of int(pos/dx) clamped to the grid (3D/run_3D.py:348),
+//   slot[q]      = arrival index in its bin (atomic on the bin count; fixed later by the sort).
+// A[r][c] = T_gm_r[c] (rows of T_gm); v = pos / dx.
+struct P2GRecords3 {
+  const float* imp0;  // init_imp [3][P]
+  const float* Ti;    // T_init [3][3][P]
+  const float* C;     // init_C [3][3][P]
+  float4* pos4;       // [P]
+  float4* famrec;     // [3][P]
+  int* key;
+  int* slot;
+  int* count;
+};
+
+__device__ __forceinline__ void write_p2g_record3(const P2GRecords3& R, int64_t q, int64_t P, const MacGeom& g,
+                                                  const float v[3], const float A[3][3]) {
+  int c[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const int ci = __float2int_rz(v[a]);
+    c[a] = ci < 0 ? 0 : (ci > g.N[a] - 1 ? g.N[a] - 1 : ci);
+  }
+  const int k = (c[0] * g.N[1] + c[1]) * g.N[2] + c[2];
+  R.key[q] = k;
+  R.slot[q] = atomicAdd(&R.count[k], 1);
+  float Cm[3][3], N[3][3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc) {
+      Cm[r][cc] = R.C[(r * 3 + cc) * P + q];   // rows(init_C)
+      N[cc][r] = R.Ti[(r * 3 + cc) * P + q];   // cols(T_init): N[k][c'] = T_init_c'[k]
+    }
+  // TCT = A^T (C A); T_transpose = A^T N; m = T_transpose init_imp
+  float CA[3][3], TCT[3][3], TT[3][3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc) CA[r][cc] = Cm[r][0] * A[0][cc] + Cm[r][1] * A[1][cc] + Cm[r][2] * A[2][cc];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc) {
+      TCT[r][cc] = A[0][r] * CA[0][cc] + A[1][r] * CA[1][cc] + A[2][r] * CA[2][cc];
+      TT[r][cc] = A[0][r] * N[0][cc] + A[1][r] * N[1][cc] + A[2][r] * N[2][cc];
+    }
+  const float m0[3] = {R.imp0[q], R.imp0[P + q], R.imp0[2 * P + q]};
+  float m[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) m[r] = TT[r][0] * m0[0] + TT[r][1] * m0[1] + TT[r][2] * m0[2];
+  R.pos4[q] = make_float4(v[0], v[1], v[2], 0.f);
+#pragma unroll
+  for (int f = 0; f < 3; ++f) R.famrec[f * P + q] = make_float4(m[f], TCT[f][0], TCT[f][1], TCT[f][2]);
+}
+
+// Launches RK4_T_forward (3D); with R non-null the kernel also writes the P2G records and keys
+// of the advected particles (defined in pfm_particles.cu).
+int launch_rk4_T_forward3(pfm_handle* h, float* pos, float* T, const MacFields3& F, float dt, const P2GRecords3* R,
+                          cudaStream_t st);
 
 // ------------------------------------------------------------------------------------------
 // 2D (2D/taichi_utils.py:214-261)

@@ -153,61 +153,19 @@ __global__ void __launch_bounds__(kBinThreads) k_cell_sort(const int* __restrict
   }
 }
 
-// Payload and cell keys (3D), one pass in particle order q (coalesced reads and writes):
-//   pos4[q]      = (pos/dx, 0)                         -- read by every window update
-//   famrec[f][q] = (m_f, (T C T)_f row)  f = x, y, z   -- read for face family f
-//   key[q]       = linear cell of int(pos/dx) (clamped), slot[q] = arrival in its bin
-// m = T_gm^T-composed init_imp and T C T = T_gm^T init_C T_gm as in 3D/run_3D.py:462-479; the
-// key is get_particles_id_in_every_cell's int(particles_pos[i] / dx) (3D/run_3D.py:348).
+// Payload and cell keys (3D), one pass in particle order q (coalesced reads and writes); the
+// record layout is write_p2g_record3's.
 __global__ void __launch_bounds__(kBinThreads) k_payload_keys3(int64_t P, MacGeom g, const float* __restrict__ pos,
-                                                               const float* __restrict__ imp0,
-                                                               const float* __restrict__ Tg,
-                                                               const float* __restrict__ Ti,
-                                                               const float* __restrict__ C, float4* __restrict__ pos4,
-                                                               float4* __restrict__ famrec, int* __restrict__ key,
-                                                               int* __restrict__ slot, int* __restrict__ count) {
+                                                               const float* __restrict__ Tg, P2GRecords3 R) {
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= P) return;
-  const float px = pos[q] / g.dx, py = pos[P + q] / g.dx, pz = pos[2 * P + q] / g.dx;
-  int c[3];
-  const float pv[3] = {px, py, pz};
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    const int ci = __float2int_rz(pv[a]);
-    c[a] = ci < 0 ? 0 : (ci > g.N[a] - 1 ? g.N[a] - 1 : ci);
-  }
-  const int k = (c[0] * g.N[1] + c[1]) * g.N[2] + c[2];
-  key[q] = k;
-  slot[q] = atomicAdd(&count[k], 1);
-  float A[3][3], Cm[3][3], N[3][3];
+  const float v[3] = {pos[q] / g.dx, pos[P + q] / g.dx, pos[2 * P + q] / g.dx};
+  float A[3][3];
 #pragma unroll
   for (int r = 0; r < 3; ++r)
 #pragma unroll
-    for (int cc = 0; cc < 3; ++cc) {
-      A[r][cc] = Tg[(r * 3 + cc) * P + q];   // rows(T_gm): A[r][c] = T_gm_r[c]
-      Cm[r][cc] = C[(r * 3 + cc) * P + q];   // rows(init_C)
-      N[cc][r] = Ti[(r * 3 + cc) * P + q];   // cols(T_init): N[k][c'] = T_init_c'[k]
-    }
-  // TCT = A^T (C A); T_transpose = A^T N; m = T_transpose init_imp
-  float CA[3][3], TCT[3][3], TT[3][3];
-#pragma unroll
-  for (int r = 0; r < 3; ++r)
-#pragma unroll
-    for (int cc = 0; cc < 3; ++cc) CA[r][cc] = Cm[r][0] * A[0][cc] + Cm[r][1] * A[1][cc] + Cm[r][2] * A[2][cc];
-#pragma unroll
-  for (int r = 0; r < 3; ++r)
-#pragma unroll
-    for (int cc = 0; cc < 3; ++cc) {
-      TCT[r][cc] = A[0][r] * CA[0][cc] + A[1][r] * CA[1][cc] + A[2][r] * CA[2][cc];
-      TT[r][cc] = A[0][r] * N[0][cc] + A[1][r] * N[1][cc] + A[2][r] * N[2][cc];
-    }
-  const float m0[3] = {imp0[q], imp0[P + q], imp0[2 * P + q]};
-  float m[3];
-#pragma unroll
-  for (int r = 0; r < 3; ++r) m[r] = TT[r][0] * m0[0] + TT[r][1] * m0[1] + TT[r][2] * m0[2];
-  pos4[q] = make_float4(px, py, pz, 0.f);
-#pragma unroll
-  for (int f = 0; f < 3; ++f) famrec[f * P + q] = make_float4(m[f], TCT[f][0], TCT[f][1], TCT[f][2]);
+    for (int c = 0; c < 3; ++c) A[r][c] = Tg[(r * 3 + c) * P + q];  // rows(T_gm)
+  write_p2g_record3(R, q, P, g, v, A);
 }
 
 // Payload (2D): pos4 = (pos/dx, psi), famrec[f] = (imp_f, C_f row, 0)
@@ -530,6 +488,7 @@ int sort_particles(pfm_handle* h, const float* pos, cudaStream_t st) {
   int* key = ws_ptr<int>(h, h->o_key);
   int* slot = ws_ptr<int>(h, h->o_slot);
   int* count = ws_ptr<int>(h, h->o_count);
+  h->rec_valid = 0;  // the keys of the P2G records are overwritten
   rc = check_cuda(h, cudaMemsetAsync(count, 0, h->cells * 4, st), "memset counts");
   if (rc) return rc;
   if (P > 0) {
@@ -553,6 +512,43 @@ static int copy_sort_out(pfm_handle* h, int* cell_count, int* order, cudaStream_
     if (rc) return rc;
   }
   return PFM_OK;
+}
+
+static P2GRecords3 records3(pfm_handle* h, const float* init_imp, const float* T_init, const float* init_C) {
+  float4* pos4 = ws_ptr<float4>(h, h->o_payload);
+  return P2GRecords3{init_imp, T_init, init_C, pos4, pos4 + h->P, ws_ptr<int>(h, h->o_key), ws_ptr<int>(h, h->o_slot),
+                     ws_ptr<int>(h, h->o_count)};
+}
+
+// P2G from records and keys already in the workspace: bin sort, tiles, normalisation.
+static int p2g3_from_records(pfm_handle* h, float* const* us, float* const* ws, cudaStream_t st) {
+  int rc = sort_from_keys(h, st);
+  if (rc) return rc;
+  const float4* pos4 = ws_ptr<float4>(h, h->o_payload);
+  const float4* famrec = pos4 + h->P;
+  const int* start = ws_ptr<int>(h, h->o_start);
+  const int* order = ws_ptr<int>(h, h->o_order);
+  FaceOut3 out{{us[0], us[1], us[2]}, {ws[0], ws[1], ws[2]}};
+  int64_t F[3];
+  for (int f = 0; f < 3; ++f) {
+    F[f] = (int64_t)h->geom.n[f][0] * h->geom.n[f][1] * h->geom.n[f][2];
+    rc = check_cuda(h, cudaMemsetAsync(us[f], 0, F[f] * 4, st), "zero u");
+    if (!rc) rc = check_cuda(h, cudaMemsetAsync(ws[f], 0, F[f] * 4, st), "zero w");
+    if (rc) return rc;
+  }
+  if (h->P > 0) {
+    const int nt[3] = {(h->geom.N[0] + kTX - 1) / kTX, (h->geom.N[1] + kTY - 1) / kTY, (h->geom.N[2] + kTZ - 1) / kTZ};
+    for (int px = 0; px < 2; ++px)
+      for (int py = 0; py < 2; ++py)
+        for (int pz = 0; pz < 2; ++pz) {
+          const unsigned bx = (nt[0] - px + 1) / 2, by = (nt[1] - py + 1) / 2, bz = (nt[2] - pz + 1) / 2;
+          if (!bx || !by || !bz) continue;
+          launch(h, k_tile3, dim3(bz, by, bx), kTileThreads, 0, st, pos4, famrec, order, start, h->geom,
+                 h->cfg.use_apic, h->P, px, py, pz, out);
+        }
+    launch(h, k_normalize3, grid_for(F[0] + F[1] + F[2], kBinThreads), kBinThreads, 0, st, out, F[0], F[1], F[2]);
+  }
+  return launch_check(h, "p2g3");
 }
 
 }  // namespace pfm
@@ -590,40 +586,61 @@ int pfm3_p2g(pfm_handle* h, const float* init_imp, const float* pos, const float
   cudaStream_t st = (cudaStream_t)stream;
   int rc = require_ws(h);
   if (rc) return rc;
-  float4* pos4 = ws_ptr<float4>(h, h->o_payload);
-  float4* famrec = pos4 + h->P;
-  float* us[3] = {u_x, u_y, u_z};
-  float* ws[3] = {w_x, w_y, w_z};
-  const int* start = ws_ptr<int>(h, h->o_start);
-  const int* order = ws_ptr<int>(h, h->o_order);
   rc = check_cuda(h, cudaMemsetAsync(ws_ptr<int>(h, h->o_count), 0, h->cells * 4, st), "memset counts");
   if (rc) return rc;
+  const P2GRecords3 R = records3(h, init_imp, T_init, init_C);
   if (h->P > 0)
-    launch(h, k_payload_keys3, grid_for(h->P, kBinThreads), kBinThreads, 0, st, h->P, h->geom, pos, init_imp, T_gm,
-           T_init, init_C, pos4, famrec, ws_ptr<int>(h, h->o_key), ws_ptr<int>(h, h->o_slot), ws_ptr<int>(h, h->o_count));
-  rc = sort_from_keys(h, st);
+    launch(h, k_payload_keys3, grid_for(h->P, kBinThreads), kBinThreads, 0, st, h->P, h->geom, pos, T_gm, R);
+  h->rec_valid = 1;
+  float* u[3] = {u_x, u_y, u_z};
+  float* w[3] = {w_x, w_y, w_z};
+  return p2g3_from_records(h, u, w, st);
+}
+
+int pfm3_rk4_p2g_records(pfm_handle* h, float* pos, float* T_gm, const float* ua_x, const float* ua_y,
+                         const float* ua_z, float dt, const float* init_imp, const float* T_init, const float* init_C,
+                         void* stream) {
+  if (!h) return PFM_ERR_NULL;
+  if (h->cfg.dim != 3) return set_error(h, PFM_ERR_SHAPE, "pfm3_rk4_p2g_records on a 2D handle");
+  if (!ua_x || !ua_y || !ua_z) return set_error(h, PFM_ERR_NULL, "pfm3_rk4_p2g_records: null grid");
+  if (h->P > 0 && (!init_imp || !pos || !T_gm || !T_init || !init_C))
+    return set_error(h, PFM_ERR_NULL, "pfm3_rk4_p2g_records: null particle field");
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = require_ws(h);
   if (rc) return rc;
-  FaceOut3 out{{u_x, u_y, u_z}, {w_x, w_y, w_z}};
-  int64_t F[3];
-  for (int f = 0; f < 3; ++f) {
-    F[f] = (int64_t)h->geom.n[f][0] * h->geom.n[f][1] * h->geom.n[f][2];
-    rc = check_cuda(h, cudaMemsetAsync(us[f], 0, F[f] * 4, st), "zero u");
-    if (!rc) rc = check_cuda(h, cudaMemsetAsync(ws[f], 0, F[f] * 4, st), "zero w");
-    if (rc) return rc;
-  }
-  if (h->P > 0) {
-    const int nt[3] = {(h->geom.N[0] + kTX - 1) / kTX, (h->geom.N[1] + kTY - 1) / kTY, (h->geom.N[2] + kTZ - 1) / kTZ};
-    for (int px = 0; px < 2; ++px)
-      for (int py = 0; py < 2; ++py)
-        for (int pz = 0; pz < 2; ++pz) {
-          const unsigned bx = (nt[0] - px + 1) / 2, by = (nt[1] - py + 1) / 2, bz = (nt[2] - pz + 1) / 2;
-          if (!bx || !by || !bz) continue;
-          launch(h, k_tile3, dim3(bz, by, bx), kTileThreads, 0, st, (const float4*)pos4, (const float4*)famrec,
-                 order, start, h->geom, h->cfg.use_apic, h->P, px, py, pz, out);
-        }
-    launch(h, k_normalize3, grid_for(F[0] + F[1] + F[2], kBinThreads), kBinThreads, 0, st, out, F[0], F[1], F[2]);
-  }
-  return launch_check(h, "pfm3_p2g");
+  rc = check_cuda(h, cudaMemsetAsync(ws_ptr<int>(h, h->o_count), 0, h->cells * 4, st), "memset counts");
+  if (rc) return rc;
+  const P2GRecords3 R = records3(h, init_imp, T_init, init_C);
+  const MacFields3 F{{ua_x, ua_y, ua_z}};
+  rc = launch_rk4_T_forward3(h, pos, T_gm, F, dt, &R, st);
+  if (rc) return rc;
+  h->rec_valid = 1;
+  return PFM_OK;
+}
+
+int pfm3_p2g_from_records(pfm_handle* h, float* u_x, float* u_y, float* u_z, float* w_x, float* w_y, float* w_z,
+                          void* stream) {
+  if (!h) return PFM_ERR_NULL;
+  if (h->cfg.dim != 3) return set_error(h, PFM_ERR_SHAPE, "pfm3_p2g_from_records on a 2D handle");
+  if (!u_x || !u_y || !u_z || !w_x || !w_y || !w_z) return set_error(h, PFM_ERR_NULL, "pfm3_p2g_from_records: null grid");
+  int rc = require_ws(h);
+  if (rc) return rc;
+  if (!h->rec_valid)
+    return set_error(h, PFM_ERR_ARG, "pfm3_p2g_from_records: no P2G records in the workspace (call "
+                                     "pfm3_rk4_p2g_records first; a sort or 2D P2G call overwrites them)");
+  float* u[3] = {u_x, u_y, u_z};
+  float* w[3] = {w_x, w_y, w_z};
+  return p2g3_from_records(h, u, w, (cudaStream_t)stream);
+}
+
+int pfm3_rk4_p2g(pfm_handle* h, float* pos, float* T_gm, const float* ua_x, const float* ua_y, const float* ua_z,
+                 float dt, const float* init_imp, const float* T_init, const float* init_C, float* u_x, float* u_y,
+                 float* u_z, float* w_x, float* w_y, float* w_z, void* stream) {
+  if (!h) return PFM_ERR_NULL;
+  if (!u_x || !u_y || !u_z || !w_x || !w_y || !w_z) return set_error(h, PFM_ERR_NULL, "pfm3_rk4_p2g: null grid");
+  int rc = pfm3_rk4_p2g_records(h, pos, T_gm, ua_x, ua_y, ua_z, dt, init_imp, T_init, init_C, stream);
+  if (rc) return rc;
+  return pfm3_p2g_from_records(h, u_x, u_y, u_z, w_x, w_y, w_z, stream);
 }
 
 int pfm2_p2g(pfm_handle* h, const float* imp, const float* pos, const float* C, const float* psi, float* u_x,
@@ -638,6 +655,7 @@ int pfm2_p2g(pfm_handle* h, const float* imp, const float* pos, const float* C, 
   if (rc) return rc;
   float4* pos4 = ws_ptr<float4>(h, h->o_payload);
   float4* famrec = pos4 + h->P;
+  h->rec_valid = 0;
   if (h->P > 0)
     launch(h, k_payload2, grid_for(h->P, kBinThreads), kBinThreads, 0, st, ws_ptr<int>(h, h->o_order), h->P, h->geom,
            pos, imp, C, psi, pos4, famrec);

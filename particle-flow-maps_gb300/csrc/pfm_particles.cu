@@ -74,8 +74,12 @@ __global__ void __launch_bounds__(256) k_reset_T(float* __restrict__ T, int64_t 
 // RK4_T_forward (3D/run_3D.py:175-219): the gradient is taken in the transpose form
 // (interp_u_MAC_grad_transpose, 3D/taichi_utils.py:319-324), so dT_v/dt[r] = sum_c du_c/dx_r T_v[c].
 // The stage sums (k1 + 2 k2 + 2 k3 + k4) accumulate in the reference's left-to-right order.
+// With PAY the kernel also writes the P2G record and cell key of the advected particle
+// (write_p2g_record3), the input of the P2G tiles that follow RK4_T_forward in the step.
+template <bool PAY>
 __global__ void __launch_bounds__(kPThreads, 4) k_rk4_T_forward3(float* __restrict__ pos, float* __restrict__ T,
-                                                             int64_t P, MacFields3 F, MacGeom g, float dt) {
+                                                             int64_t P, MacFields3 F, MacGeom g, float dt,
+                                                             P2GRecords3 R) {
   int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= P) return;
   float p0[3] = {pos[q], pos[P + q], pos[2 * P + q]};
@@ -123,12 +127,23 @@ __global__ void __launch_bounds__(kPThreads, 4) k_rk4_T_forward3(float* __restri
     }
   }
   const float coef = dt / 6.f;
+  float pn[3], Tn[3][3];
 #pragma unroll
-  for (int c = 0; c < 3; ++c) pos[c * P + q] = p0[c] + coef * su[c];
+  for (int c = 0; c < 3; ++c) {
+    pn[c] = p0[c] + coef * su[c];
+    pos[c * P + q] = pn[c];
+  }
 #pragma unroll
   for (int v = 0; v < 3; ++v)
 #pragma unroll
-    for (int c = 0; c < 3; ++c) T[(v * 3 + c) * P + q] = T0[v][c] - coef * sT[v][c];
+    for (int c = 0; c < 3; ++c) {
+      Tn[v][c] = T0[v][c] - coef * sT[v][c];
+      T[(v * 3 + c) * P + q] = Tn[v][c];
+    }
+  if (PAY) {
+    const float v[3] = {pn[0] / g.dx, pn[1] / g.dx, pn[2] / g.dx};
+    write_p2g_record3(R, q, P, g, v, Tn);
+  }
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -267,6 +282,21 @@ static int check_dim(pfm_handle* h, int D) {
 
 using namespace pfm;
 
+namespace pfm {
+
+int launch_rk4_T_forward3(pfm_handle* h, float* pos, float* T, const MacFields3& F, float dt, const P2GRecords3* R,
+                          cudaStream_t st) {
+  if (h->P == 0) return PFM_OK;
+  if (R)
+    launch(h, k_rk4_T_forward3<true>, grid_for(h->P, kPThreads), kPThreads, 0, st, pos, T, h->P, F, h->geom, dt, *R);
+  else
+    launch(h, k_rk4_T_forward3<false>, grid_for(h->P, kPThreads), kPThreads, 0, st, pos, T, h->P, F, h->geom, dt,
+           P2GRecords3{});
+  return launch_check(h, "k_rk4_T_forward3");
+}
+
+}  // namespace pfm
+
 extern "C" {
 
 int pfm3_g2p(pfm_handle* h, const float* pos, const float* u_x, const float* u_y, const float* u_z,
@@ -305,8 +335,7 @@ int pfm3_rk4_T_forward(pfm_handle* h, float* pos, float* T, const float* u_x, co
   if (!pos || !T || !u_x || !u_y || !u_z) return set_error(h, PFM_ERR_NULL, "pfm3_rk4_T_forward: null input");
   if (h->P == 0) return PFM_OK;
   MacFields3 F{{u_x, u_y, u_z}};
-  launch(h, k_rk4_T_forward3, grid_for(h->P, kPThreads), kPThreads, 0, (cudaStream_t)stream, pos, T, h->P, F, h->geom, dt);
-  return launch_check(h, "k_rk4_T_forward3");
+  return launch_rk4_T_forward3(h, pos, T, F, dt, nullptr, (cudaStream_t)stream);
 }
 
 int pfm2_g2p(pfm_handle* h, const float* pos, const float* u_x, const float* u_y, float* imp_out,

@@ -233,6 +233,40 @@ class Scene:
         self._check(self.lib.pfm3_p2g(self.h, _ptr(init_imp), _ptr(pos), _ptr(T_gm), _ptr(T_init), _ptr(init_C),
                                       *map(_ptr, u_out), *map(_ptr, w_out), self._stream()))
 
+    def rk4_p2g3(self, pos, T_gm, u_adv, dt, init_imp, T_init, init_C, u_out, w_out):
+        """RK4_T_forward then P2G in one call (3D/run_3D.py:795-812): bitwise the same as
+        rk4_T_forward(pos, T_gm, u_adv, dt) followed by p2g3(...), with the particle state read once."""
+        self._part(pos, 3, "pos")
+        self._part(T_gm, 3, "T_gm", vec=3)
+        self._part(init_imp, 3, "init_imp")
+        self._part(T_init, 3, "T_init", vec=3)
+        self._part(init_C, 3, "init_C", vec=3)
+        u_adv = self._grids(u_adv, "u_adv")
+        u_out = self._grids(u_out, "u_out")
+        w_out = self._grids(w_out, "w_out")
+        self._check(self.lib.pfm3_rk4_p2g(self.h, _ptr(pos), _ptr(T_gm), *map(_ptr, u_adv), ctypes.c_float(dt),
+                                          _ptr(init_imp), _ptr(T_init), _ptr(init_C), *map(_ptr, u_out),
+                                          *map(_ptr, w_out), self._stream()))
+
+    def rk4_p2g_records3(self, pos, T_gm, u_adv, dt, init_imp, T_init, init_C):
+        """RK4_T_forward that also leaves the P2G records and cell keys of the advected particles in
+        the workspace (first half of rk4_p2g3)."""
+        self._part(pos, 3, "pos")
+        self._part(T_gm, 3, "T_gm", vec=3)
+        self._part(init_imp, 3, "init_imp")
+        self._part(T_init, 3, "T_init", vec=3)
+        self._part(init_C, 3, "init_C", vec=3)
+        u_adv = self._grids(u_adv, "u_adv")
+        self._check(self.lib.pfm3_rk4_p2g_records(self.h, _ptr(pos), _ptr(T_gm), *map(_ptr, u_adv), ctypes.c_float(dt),
+                                                  _ptr(init_imp), _ptr(T_init), _ptr(init_C), self._stream()))
+
+    def p2g_from_records3(self, u_out, w_out):
+        """The rest of P2G (bin sort, cell tiles, normalisation) from the records of
+        rk4_p2g_records3 (second half of rk4_p2g3)."""
+        u_out = self._grids(u_out, "u_out")
+        w_out = self._grids(w_out, "w_out")
+        self._check(self.lib.pfm3_p2g_from_records(self.h, *map(_ptr, u_out), *map(_ptr, w_out), self._stream()))
+
     def p2g2(self, imp, pos, C, psi, u_out, w_out, psi_out=None):
         """2D P2G (2D/run_2D.py:548-611); psi_out = (psi_x_grid [F,2], psi_y_grid [F,2]) or None."""
         self._part(imp, 2, "imp")

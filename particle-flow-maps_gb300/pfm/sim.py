@@ -117,11 +117,13 @@ class Sim3D:
 
     ``u``: the three face grids (numpy arrays or CUDA tensors); ``seeds``: reinit positions, AoS
     numpy [P, 3] or a device SoA tensor [3, P].  Pass ``timer`` (a callable taking a phase name and
-    returning a context manager) to bracket the phases with CUDA events."""
+    returning a context manager) to bracket the phases with CUDA events.  ``fused_rk4_p2g`` runs
+    RK4_T_forward and P2G as one library call (same results, particle state read once)."""
 
     def __init__(self, u, seeds, res, dx, CFL=0.5, visualize_dt=0.1, reinit_every=20,
                  reinit_every_grad_m=1, use_midpoint_vel=True, reinit_particle_pos=True, use_apic=True,
-                 base_level=3, mg_levels=0, poisson_opts=None, device="cuda"):
+                 base_level=3, mg_levels=0, poisson_opts=None, device="cuda", fused_rk4_p2g=True):
+        self.fused_rk4_p2g = bool(fused_rk4_p2g)  # RK4_T_forward + P2G through pfm3_rk4_p2g
         if isinstance(seeds, torch.Tensor):
             self.P = int(seeds.shape[1])
         else:
@@ -189,10 +191,17 @@ class Sim3D:
             with self._t("poisson_mid"):
                 self.infos.append(sc.poisson(self.u_mid, **self.poisson_opts))
             adv = self.u_mid
-        with self._t("rk4"):
-            sc.rk4_T_forward(self.pos, self.T_gm, adv, float(np.float32(curr_dt)))
-        with self._t("p2g"):
-            sc.p2g3(self.init_imp, self.pos, self.T_gm, self.T_init, self.init_C, self.u, self.w)
+        if self.fused_rk4_p2g:
+            with self._t("rk4"):
+                sc.rk4_p2g_records3(self.pos, self.T_gm, adv, float(np.float32(curr_dt)), self.init_imp, self.T_init,
+                                    self.init_C)
+            with self._t("p2g"):
+                sc.p2g_from_records3(self.u, self.w)
+        else:
+            with self._t("rk4"):
+                sc.rk4_T_forward(self.pos, self.T_gm, adv, float(np.float32(curr_dt)))
+            with self._t("p2g"):
+                sc.p2g3(self.init_imp, self.pos, self.T_gm, self.T_init, self.init_C, self.u, self.w)
         with self._t("poisson"):
             self.infos.append(sc.poisson(self.u, self.p, **self.poisson_opts))
         return curr_dt

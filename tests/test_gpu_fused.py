@@ -1,0 +1,64 @@
+"""The fused RK4_T_forward + P2G entry points (pfm3_rk4_p2g_records / pfm3_p2g_from_records /
+pfm3_rk4_p2g) against the separate calls pfm3_rk4_T_forward then pfm3_p2g: bitwise equal grids,
+weights, positions and T, including particles outside the grid."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import pfm  # noqa: E402
+
+
+def _scene(res=(24, 16, 20), ppc=8, seed=4):
+    dx = 1.0 / res[1]
+    rng = np.random.default_rng(seed)
+    pos = pfm.jittered(res, dx, ppc, seed=seed)
+    pos[:11] += np.float32(1.5 * dx)    # some particles leave the grid on the high side
+    pos[11:23] -= np.float32(1.2 * dx)  # and on the low side
+    P = pos.shape[0]
+    dev = torch.device("cuda:0")
+    sc = pfm.Scene(3, res, dx, P)
+    u = [torch.from_numpy((0.3 * rng.standard_normal(s)).astype(np.float32)).to(dev) for s in sc.face_shapes]
+    st = dict(pos=pfm.soa(pos, dev),
+              T_gm=torch.from_numpy((np.eye(3)[:, :, None] + 0.05 * rng.standard_normal((3, 3, P))).astype(np.float32)).to(dev),
+              init_imp=torch.from_numpy(rng.standard_normal((3, P)).astype(np.float32)).to(dev),
+              T_init=torch.from_numpy((np.eye(3)[:, :, None] + 0.05 * rng.standard_normal((3, 3, P))).astype(np.float32)).to(dev),
+              init_C=torch.from_numpy(rng.standard_normal((3, 3, P)).astype(np.float32)).to(dev))
+    return sc, u, st
+
+
+def _clone(st):
+    return {k: v.clone() for k, v in st.items()}
+
+
+@pytest.mark.parametrize("mode", ["two_calls", "one_call"])
+def test_rk4_p2g_matches_separate_calls(mode):
+    sc, u, st = _scene()
+    dt = 0.01
+    a, b = _clone(st), _clone(st)
+    ua, wa = sc.alloc_faces(), sc.alloc_faces()
+    sc.rk4_T_forward(a["pos"], a["T_gm"], u, dt)
+    sc.p2g3(a["init_imp"], a["pos"], a["T_gm"], a["T_init"], a["init_C"], ua, wa)
+    ub, wb = sc.alloc_faces(), sc.alloc_faces()
+    if mode == "two_calls":
+        sc.rk4_p2g_records3(b["pos"], b["T_gm"], u, dt, b["init_imp"], b["T_init"], b["init_C"])
+        sc.p2g_from_records3(ub, wb)
+    else:
+        sc.rk4_p2g3(b["pos"], b["T_gm"], u, dt, b["init_imp"], b["T_init"], b["init_C"], ub, wb)
+    torch.cuda.synchronize()
+    assert torch.equal(a["pos"], b["pos"]) and torch.equal(a["T_gm"], b["T_gm"])
+    for f in range(3):
+        assert torch.equal(ua[f], ub[f]), f
+        assert torch.equal(wa[f], wb[f]), f
+
+
+def test_p2g_from_records_needs_records():
+    sc, u, st = _scene(res=(8, 8, 8), ppc=1)
+    out, w = sc.alloc_faces(), sc.alloc_faces()
+    with pytest.raises(pfm.PfmError, match="no P2G records"):
+        sc.p2g_from_records3(out, w)
+    sc.rk4_p2g_records3(st["pos"], st["T_gm"], u, 0.01, st["init_imp"], st["T_init"], st["init_C"])
+    sc.sort_particles(st["pos"])  # overwrites the keys of the records
+    with pytest.raises(pfm.PfmError, match="no P2G records"):
+        sc.p2g_from_records3(out, w)
