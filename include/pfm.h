@@ -243,11 +243,22 @@ int pfm_seed_jittered(pfm_handle* h, uint64_t seed, int ppc_axis, float* pos, vo
 
 /* ---- the MGPCG solver alone ----------------------------------------------------------------- */
 
-/* MGPCG.init(r, -1) + solve() + get_result (3D/mgpcg.py:71-90, 202-280) on a caller-given
- * divergence field div [cells] (the right-hand side is -div, as in Poisson()).  x_out [cells]
- * receives the pressure.  SYNCHRONIZATION POINT. */
-int pfm_mgpcg_solve(pfm_handle* h, const float* div, float* x_out, const pfm_solve_opts* opts,
+/* MGPCG.init(r, k) + solve() + get_result(x) (3D/mgpcg.py:71-90, 202-280): solves the scaled
+ * Poisson problem lap(x) = k r for a caller-given cell field r [cells] (Poisson() uses the
+ * divergence with k = -1, 3D/mgpcg.py:420-423).  x_out [cells] receives the solution.
+ * SYNCHRONIZATION POINT. */
+int pfm_mgpcg_solve(pfm_handle* h, const float* r, float k, float* x_out, const pfm_solve_opts* opts,
                     pfm_solve_stats* stats, void* stream);
+
+/* The pieces of MGPCG_3/MGPCG_2.Poisson (3D/mgpcg.py:359-418, 2D/mgpcg.py:293-335); u_z is NULL
+ * in 2D.  apply_bc zeroes the normal velocity on Neumann walls; divergence writes
+ * div_out [cells] = sum of face differences (unit spacing); subtract_grad_p subtracts the
+ * pressure difference p [cells] from every face (zero pressure outside the grid), without the
+ * wall reset (Poisson calls apply_bc after it). */
+int pfm_apply_bc(pfm_handle* h, float* u_x, float* u_y, float* u_z, void* stream);
+int pfm_divergence(pfm_handle* h, const float* u_x, const float* u_y, const float* u_z, float* div_out,
+                   void* stream);
+int pfm_subtract_grad_p(pfm_handle* h, float* u_x, float* u_y, float* u_z, const float* p, void* stream);
 
 #ifdef __cplusplus
 }

@@ -145,10 +145,10 @@ __global__ void k_apply_bc(float* __restrict__ u, int fam, MacGeom g, int lo_neu
   (void)n0;
 }
 
-// divergence then init(u_div, -1): r0 = -(vr - vl + vt - vb + vc - va)
+// divergence (3D/mgpcg.py:380-390) times scale: scale = -1 fuses init(u_div, -1), r0 = -(vr - vl + ...)
 template <int D>
 __global__ void k_divergence(const float* __restrict__ ux, const float* __restrict__ uy,
-                             const float* __restrict__ uz, Lvl L, float* __restrict__ r0) {
+                             const float* __restrict__ uz, Lvl L, float* __restrict__ r0, float scale) {
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= L.count) return;
   int i, j, k;
@@ -164,7 +164,7 @@ __global__ void k_divergence(const float* __restrict__ ux, const float* __restri
     float vb = uy[(int64_t)i * (L.n1 + 1) + j], vt = uy[(int64_t)i * (L.n1 + 1) + j + 1];
     div = vr - vl + vt - vb;
   }
-  r0[e] = div * -1.f;
+  r0[e] = div * scale;
 }
 
 // subtract_grad_p for family `fam`, followed by apply_bc on that family's boundary faces.
@@ -273,9 +273,11 @@ __global__ void __launch_bounds__(256) k_prolong(float* __restrict__ zf, Lvl Lf,
   zf[e] += zc[ce];
 }
 
-__global__ void __launch_bounds__(256) k_negate(float* __restrict__ out, const float* __restrict__ in, int64_t n) {
+// init(r, k) (3D/mgpcg.py:71-79): r0 = r * k
+__global__ void __launch_bounds__(256) k_scale(float* __restrict__ out, const float* __restrict__ in, int64_t n,
+                                              float k) {
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
-    out[e] = in[e] * -1.f;
+    out[e] = in[e] * k;
 }
 
 __global__ void __launch_bounds__(256) k_zero(float* __restrict__ a, int64_t n, const SolveState* st) {
@@ -807,7 +809,7 @@ static int poisson_impl(pfm_handle* h, float* const* u, float* p_out, const pfm_
   }
   float* r0 = ws_ptr<float>(h, h->o_r[0]);
   launch(h, k_divergence<D>, grid_for(h->cells, 256), 256, 0, s, u[0], u[1], D == 3 ? u[2] : nullptr, lvl_of(h, 0),
-         r0);
+         r0, -1.f);
   rc = launch_check(h, "divergence");
   if (rc) return rc;
   int solve_rc = mgpcg_solve_in_place(h, p_out, opts, stats, s);
@@ -849,19 +851,69 @@ int pfm2_poisson(pfm_handle* h, float* u_x, float* u_y, float* p_out, const pfm_
   return poisson_impl<2>(h, u, p_out, opts, stats, (cudaStream_t)stream);
 }
 
-int pfm_mgpcg_solve(pfm_handle* h, const float* div, float* x_out, const pfm_solve_opts* opts,
+int pfm_mgpcg_solve(pfm_handle* h, const float* r, float k, float* x_out, const pfm_solve_opts* opts,
                     pfm_solve_stats* stats, void* stream) {
   if (!h) return PFM_ERR_NULL;
-  if (!div || !x_out) return set_error(h, PFM_ERR_NULL, "pfm_mgpcg_solve: null input");
+  if (!r || !x_out) return set_error(h, PFM_ERR_NULL, "pfm_mgpcg_solve: null input");
   int rc = require_ws(h);
   if (rc) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   float* r0 = ws_ptr<float>(h, h->o_r[0]);
-  // init(div, -1): r0 = -div (3D/mgpcg.py:71-79)
-  launch(h, k_negate, stream_blocks(h->cells), 256, 0, s, r0, div, h->cells);
-  rc = launch_check(h, "k_negate");
+  // init(r, k): r0 = k r (3D/mgpcg.py:71-79)
+  launch(h, k_scale, stream_blocks(h->cells), 256, 0, s, r0, r, h->cells, k);
+  rc = launch_check(h, "k_scale");
   if (rc) return rc;
   return mgpcg_solve_in_place(h, x_out, opts, stats, s);
+}
+
+int pfm_apply_bc(pfm_handle* h, float* u_x, float* u_y, float* u_z, void* stream) {
+  if (!h) return PFM_ERR_NULL;
+  const int D = h->cfg.dim;
+  if (!u_x || !u_y || (D == 3 && !u_z)) return set_error(h, PFM_ERR_NULL, "pfm_apply_bc: null velocity");
+  float* u[3] = {u_x, u_y, u_z};
+  const MacGeom& g = h->geom;
+  cudaStream_t s = (cudaStream_t)stream;
+  for (int f = 0; f < D; ++f) {
+    const int a1 = (f == 0) ? 1 : 0, a2 = (f == 2) ? 1 : 2;
+    const int64_t plane = (int64_t)g.n[f][a1] * (D == 3 ? g.n[f][a2] : 1);
+    const int lo = h->cfg.boundary[f][0] == 2, hi = h->cfg.boundary[f][1] == 2;
+    if (D == 3) launch(h, k_apply_bc<3>, grid_for(2 * plane, 256), 256, 0, s, u[f], f, g, lo, hi);
+    else launch(h, k_apply_bc<2>, grid_for(2 * plane, 256), 256, 0, s, u[f], f, g, lo, hi);
+  }
+  return launch_check(h, "pfm_apply_bc");
+}
+
+int pfm_divergence(pfm_handle* h, const float* u_x, const float* u_y, const float* u_z, float* div_out,
+                   void* stream) {
+  if (!h) return PFM_ERR_NULL;
+  const int D = h->cfg.dim;
+  if (!u_x || !u_y || (D == 3 && !u_z) || !div_out) return set_error(h, PFM_ERR_NULL, "pfm_divergence: null input");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (D == 3)
+    launch(h, k_divergence<3>, grid_for(h->cells, 256), 256, 0, s, u_x, u_y, u_z, lvl_of(h, 0), div_out, 1.f);
+  else
+    launch(h, k_divergence<2>, grid_for(h->cells, 256), 256, 0, s, u_x, u_y, (const float*)nullptr, lvl_of(h, 0),
+           div_out, 1.f);
+  return launch_check(h, "pfm_divergence");
+}
+
+int pfm_subtract_grad_p(pfm_handle* h, float* u_x, float* u_y, float* u_z, const float* p, void* stream) {
+  if (!h) return PFM_ERR_NULL;
+  const int D = h->cfg.dim;
+  if (!u_x || !u_y || (D == 3 && !u_z) || !p) return set_error(h, PFM_ERR_NULL, "pfm_subtract_grad_p: null input");
+  const MacGeom& g = h->geom;
+  cudaStream_t s = (cudaStream_t)stream;
+  float* u[3] = {u_x, u_y, u_z};
+  for (int f = 0; f < D; ++f) {
+    const unsigned nf = (unsigned)((int64_t)g.n[f][0] * g.n[f][1] * g.n[f][2]);
+    // lo/hi = 0: the gradient subtraction alone; the boundary faces are left to pfm_apply_bc
+    if (D == 3 && f == 0) launch(h, k_subtract_grad_p<3, 0>, grid_for(nf, 256), 256, 0, s, u[f], p, g, 0, 0);
+    if (D == 3 && f == 1) launch(h, k_subtract_grad_p<3, 1>, grid_for(nf, 256), 256, 0, s, u[f], p, g, 0, 0);
+    if (D == 3 && f == 2) launch(h, k_subtract_grad_p<3, 2>, grid_for(nf, 256), 256, 0, s, u[f], p, g, 0, 0);
+    if (D == 2 && f == 0) launch(h, k_subtract_grad_p<2, 0>, grid_for(nf, 256), 256, 0, s, u[f], p, g, 0, 0);
+    if (D == 2 && f == 1) launch(h, k_subtract_grad_p<2, 1>, grid_for(nf, 256), 256, 0, s, u[f], p, g, 0, 0);
+  }
+  return launch_check(h, "pfm_subtract_grad_p");
 }
 
 }  // extern "C"

@@ -76,7 +76,10 @@ SIGNATURES = {
     "pfm2_sort_particles": [_P, _P, _P, _P, _P],
     "pfm2_p2g": [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "pfm2_poisson": [_P, _P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats), _P],
-    "pfm_mgpcg_solve": [_P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats), _P],
+    "pfm_mgpcg_solve": [_P, _P, _F, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats), _P],
+    "pfm_apply_bc": [_P, _P, _P, _P, _P],
+    "pfm_divergence": [_P, _P, _P, _P, _P, _P],
+    "pfm_subtract_grad_p": [_P, _P, _P, _P, _P, _P],
     "pfm_sort_particles_noalloc": [_I, ctypes.POINTER(_I), ctypes.c_double, ctypes.c_int64, _P, _P, _P, _P],
 }
 # scratch limits of pfm_sort_particles_noalloc (include/pfm.h)

@@ -355,17 +355,43 @@ class Scene:
         self._check(self.lib.pfm_launch_count(self.h, ctypes.byref(n)))
         return int(n.value)
 
-    def mgpcg_solve(self, div, x_out, max_iters=400, tol=1e-12, tol_mode=0, check_every=4):
-        """MGPCG init(div, -1) + solve + get_result."""
-        self._dev(div, "div")
-        self._dev(x_out, "x_out")
-        if tuple(div.shape) != self.cell_shape or tuple(x_out.shape) != self.cell_shape:
-            raise PfmError(2, "div/x_out must have the cell shape")
+    def mgpcg_solve(self, r, x_out, k=-1.0, max_iters=400, tol=1e-12, tol_mode=0, check_every=4):
+        """MGPCG init(r, k) + solve + get_result: lap(x) = k r (k = -1 for the divergence)."""
+        self._cells(r, "r")
+        self._cells(x_out, "x_out")
         o = self._opts(max_iters, tol, tol_mode, check_every)
         s = SolveStats()
-        st = self._check(self.lib.pfm_mgpcg_solve(self.h, _ptr(div), _ptr(x_out), ctypes.byref(o), ctypes.byref(s),
-                                                  self._stream()), allow=(_lib.PFM_ERR_NOT_CONVERGED,))
+        st = self._check(self.lib.pfm_mgpcg_solve(self.h, _ptr(r), ctypes.c_float(k), _ptr(x_out), ctypes.byref(o),
+                                                  ctypes.byref(s), self._stream()),
+                         allow=(_lib.PFM_ERR_NOT_CONVERGED,))
         return SolveInfo(s, st)
+
+    def _cells(self, t, name):
+        self._dev(t, name)
+        if tuple(t.shape) != self.cell_shape:
+            raise PfmError(2, f"{name} must have the cell shape {self.cell_shape}, got {tuple(t.shape)}")
+
+    def _uz(self, u):
+        return _ptr(u[2]) if self.dim == 3 else None
+
+    def apply_bc(self, u):
+        """MGPCG apply_bc (3D/mgpcg.py:359-378): zero normal velocity on Neumann walls, in place."""
+        u = self._grids(u, "u")
+        self._check(self.lib.pfm_apply_bc(self.h, _ptr(u[0]), _ptr(u[1]), self._uz(u), self._stream()))
+
+    def divergence(self, u, div_out):
+        """MGPCG divergence (3D/mgpcg.py:380-390) into div_out (cell shape)."""
+        u = self._grids(u, "u")
+        self._cells(div_out, "div_out")
+        self._check(self.lib.pfm_divergence(self.h, _ptr(u[0]), _ptr(u[1]), self._uz(u), _ptr(div_out),
+                                            self._stream()))
+
+    def subtract_grad_p(self, u, p):
+        """MGPCG subtract_grad_p (3D/mgpcg.py:392-418): u -= grad p, in place."""
+        u = self._grids(u, "u")
+        self._cells(p, "p")
+        self._check(self.lib.pfm_subtract_grad_p(self.h, _ptr(u[0]), _ptr(u[1]), self._uz(u), _ptr(p),
+                                                 self._stream()))
 
 
 def sort_particles_noalloc(pos, res, dx, cell_count, order):

@@ -224,7 +224,8 @@ class Sim2D:
         self.use_midpoint_vel, self.reinit_particle_pos = use_midpoint_vel, reinit_particle_pos
         self.poisson_opts = dict(poisson_opts or {})
         dev = sc.device
-        self.u = [torch.as_tensor(np.asarray(a, np.float32)).to(dev).contiguous() for a in u]
+        self.u = [(a.to(dev).float().contiguous() if isinstance(a, torch.Tensor)
+                   else torch.as_tensor(np.asarray(a, np.float32)).to(dev).contiguous()) for a in u]
         self.u_mid = sc.alloc_faces()
         self.w = sc.alloc_faces()
         self.psi_grid = [torch.zeros(s + (2,), device=dev) for s in sc.face_shapes]

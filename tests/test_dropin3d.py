@@ -1,0 +1,185 @@
+"""The 3D drop-in modules (particle-flow-maps_gb300/3D: hyperparameters, init_conditions, mgpcg,
+run_3D) keep the reference's names and reproduce pfm.Sim3D / pfm.Scene results bit for bit."""
+import importlib
+import os
+import sys
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+DROPIN = os.path.join(ROOT, "particle-flow-maps_gb300", "3D")
+
+
+def _import_3d(**hp):
+    """Fresh imports of the drop-in modules with hyperparameters overridden (as a user edits
+    hyperparameters.py before running run_3D)."""
+    other = os.path.join(ROOT, "particle-flow-maps_gb300", "2D")
+    while other in sys.path:
+        sys.path.remove(other)
+    if DROPIN in sys.path:
+        sys.path.remove(DROPIN)
+    sys.path.insert(0, DROPIN)
+    for m in ("run_3D", "run_2D", "mgpcg", "init_conditions", "hyperparameters"):
+        sys.modules.pop(m, None)
+    h = importlib.import_module("hyperparameters")
+    for k, v in hp.items():
+        setattr(h, k, v)
+    return h, importlib.import_module("run_3D")
+
+
+def test_dropin_names_match_the_reference_surface():
+    h, r = _import_3d()
+    for name in ("res_x", "res_y", "res_z", "reinit_every", "reinit_every_grad_m", "CFL", "visualize_dt",
+                 "particles_per_cell", "use_midpoint_vel", "use_APIC", "exp_name", "total_steps"):
+        assert hasattr(h, name), name
+    for name in ("calc_max_speed", "reset_T_to_identity", "RK4_grid", "RK4_T_forward", "advect_u",
+                 "stretch_T_and_advect_particles", "get_particles_id_in_every_cell", "update_T", "P2G", "main"):
+        assert callable(getattr(r, name)), name
+    m = importlib.import_module("mgpcg")
+    for name in ("init", "solve", "get_result", "Poisson", "apply_bc", "divergence", "subtract_grad_p",
+                 "solve_pressure_MGPCG"):
+        assert hasattr(m.MGPCG_3, name), name
+    assert r.dx == 1.0 / h.res_y and r.particle_num == h.res_x * h.res_y * h.res_z * h.particles_per_cell
+
+
+@pytest.mark.gpu
+def test_mgpcg3_poisson_equals_its_pieces():
+    _, r = _import_3d(res_x=32, res_y=16, res_z=16)
+    m = sys.modules["mgpcg"]
+    rng = np.random.default_rng(2)
+    u = [torch.from_numpy(rng.standard_normal(s).astype(np.float32)).cuda() for s in r._face_shapes]
+    a = [t.clone() for t in u]
+    b = [t.clone() for t in u]
+    s1 = m.MGPCG_3(r.boundary_types, [32, 16, 16])
+    s1.Poisson(*a)
+    s2 = m.MGPCG_3(r.boundary_types, [32, 16, 16])
+    s2.apply_bc(*b)
+    s2.divergence(*b)
+    s2.init(s2.u_div, -1)
+    s2.solve(max_iters=400, tol=1e-12)
+    s2.get_result(s2.p)
+    s2.subtract_grad_p(*b)
+    s2.apply_bc(*b)
+    torch.cuda.synchronize()
+    assert torch.equal(s1.p, s2.p)
+    for x, y in zip(a, b):
+        assert torch.equal(x, y)
+    div = torch.zeros(32, 16, 16, device="cuda")
+    s2.scene.divergence(b, div)
+    assert float(div.abs().max()) < 1e-4 * float(torch.cat([t.abs().flatten() for t in u]).max())
+
+
+@pytest.mark.gpu
+def test_rk4_grid_and_advect_u_equal_the_fused_midpoint():
+    _, r = _import_3d(res_x=24, res_y=16, res_z=16)
+    rng = np.random.default_rng(3)
+    u0 = [torch.from_numpy((0.2 * rng.standard_normal(s)).astype(np.float32)).cuda() for s in r._face_shapes]
+    psi = [torch.zeros(s + (3,), device="cuda") for s in r._face_shapes]
+    T = [torch.zeros(s + (3,), device="cuda") for s in r._face_shapes]
+    r.reset_to_identity_grid(*psi, *T)
+    for f in range(3):
+        r.RK4_grid(psi[f], T[f], *u0, 0.01)
+    u1 = [torch.zeros(s, device="cuda") for s in r._face_shapes]
+    r.advect_u(*u0, *u1, *T, *psi, r.dx)
+    sc = r._scene()
+    ref = sc.alloc_faces()
+    ps2 = [torch.zeros_like(t) for t in psi]
+    T2 = [torch.zeros_like(t) for t in T]
+    sc.midpoint(u0, ref, 0.01, psi_out=ps2, T_out=T2)
+    torch.cuda.synchronize()
+    for f in range(3):
+        assert torch.equal(u1[f], ref[f]) and torch.equal(psi[f], ps2[f]) and torch.equal(T[f], T2[f])
+    # the backward map starts at the face position with T = e_f
+    assert float((psi[0] - psi[0].mean()).abs().max()) > 0
+
+
+@pytest.mark.gpu
+def test_get_particles_id_in_every_cell_matches_numpy():
+    _, r = _import_3d(res_x=8, res_y=8, res_z=8, particles_per_cell=8)
+    P = r.particle_num
+    rng = np.random.default_rng(4)
+    pos = (rng.random((3, P)) * np.array([[8.0], [8.0], [8.0]]) * r.dx).astype(np.float32)
+    pos_d = torch.from_numpy(pos).cuda()
+    r.get_particles_id_in_every_cell(r.cell_particles_id, r.cell_particle_num, pos_d)
+    c = np.clip(np.trunc(pos / np.float32(r.dx)).astype(np.int64), 0, 7)
+    key = (c[0] * 8 + c[1]) * 8 + c[2]
+    counts = np.bincount(key, minlength=512)
+    assert np.array_equal(r.cell_particle_num.cpu().numpy().reshape(-1), counts)
+    order = np.argsort(key, kind="stable")
+    start = np.concatenate([[0], np.cumsum(counts)[:-1]])
+    ids = r.cell_particles_id.cpu().numpy().reshape(512, -1)
+    cap = ids.shape[1]
+    for cell in range(512):
+        n = min(counts[cell], cap)
+        assert np.array_equal(ids[cell, :n], order[start[cell]:start[cell] + n])
+        assert np.all(ids[cell, n:] == -1)
+
+
+@pytest.mark.gpu
+def test_run_3d_main_matches_sim3d(tmp_path):
+    import pfm
+    h, r = _import_3d(res_x=32, res_y=16, res_z=16, use_total_steps=True, total_steps=5, reinit_every=3,
+                      reinit_every_grad_m=1, exp_name="t")
+    steps = r.main(logs_root=str(tmp_path))
+    assert steps == 5
+    ck = tmp_path / "t" / "ckpts"
+    assert (ck / "vel_x_numpy_0.npy").exists() and (tmp_path / "t" / "frame_time" / "frame_times.npy").exists()
+    # the same run through pfm.Sim3D from the drop-in's initial field
+    u0 = [torch.zeros(s, device="cuda") for s in r._face_shapes]
+    vc = torch.zeros((32, 16, 16, 3), device="cuda")
+    r.init_vorts_leapfrog(None, vc, None, None)
+    r.split_central_vector(vc, *u0)
+    r.solver.Poisson(*u0)
+    seeds = pfm.lattice3((32, 16, 16), r.dx)
+    sim = pfm.Sim3D(u0, seeds, (32, 16, 16), r.dx, CFL=h.CFL, visualize_dt=h.visualize_dt, reinit_every=3,
+                    reinit_every_grad_m=1)
+    for _ in range(5):
+        sim.step()
+    torch.cuda.synchronize()
+    for f, t in enumerate((r.u_x, r.u_y, r.u_z)):
+        assert torch.equal(t, sim.u[f]), f
+    assert torch.equal(r.particles_pos, sim.pos)
+
+
+@pytest.mark.gpu
+def test_poisson_pieces_match_numpy():
+    """pfm_divergence / pfm_apply_bc / pfm_subtract_grad_p against their numpy restatement
+    (3D/mgpcg.py:359-418), and lap(x) = k r for k = +1 is exactly the negation of k = -1."""
+    import pfm
+    res = (20, 16, 12)
+    sc = pfm.Scene(3, res, 1 / 16, 0)
+    rng = np.random.default_rng(8)
+    u = [rng.standard_normal(s).astype(np.float32) for s in sc.face_shapes]
+    ud = [torch.from_numpy(a).cuda() for a in u]
+    div = torch.zeros(res, device="cuda")
+    sc.divergence(ud, div)
+    want = (u[0][1:] - u[0][:-1]) + (u[1][:, 1:] - u[1][:, :-1]) + (u[2][:, :, 1:] - u[2][:, :, :-1])
+    assert np.allclose(div.cpu().numpy(), want, rtol=0, atol=2e-6)
+    sc.apply_bc(ud)
+    got = [t.cpu().numpy() for t in ud]
+    for f in range(3):
+        inner = [slice(None)] * 3
+        inner[f] = slice(1, -1)
+        assert np.array_equal(got[f][tuple(inner)], u[f][tuple(inner)])
+        lo = [slice(None)] * 3
+        lo[f] = 0
+        hi = [slice(None)] * 3
+        hi[f] = -1
+        assert not got[f][tuple(lo)].any() and not got[f][tuple(hi)].any()
+    p = rng.standard_normal(res).astype(np.float32)
+    ud = [torch.from_numpy(a).cuda() for a in u]
+    sc.subtract_grad_p(ud, torch.from_numpy(p).cuda())
+    pp = np.pad(p, 1)  # zero pressure outside the grid
+    grads = [pp[1:, 1:-1, 1:-1] - pp[:-1, 1:-1, 1:-1], pp[1:-1, 1:, 1:-1] - pp[1:-1, :-1, 1:-1],
+             pp[1:-1, 1:-1, 1:] - pp[1:-1, 1:-1, :-1]]
+    for f in range(3):
+        assert np.array_equal(ud[f].cpu().numpy(), (u[f] - grads[f]).astype(np.float32))
+    r = torch.from_numpy(rng.standard_normal(res).astype(np.float32)).cuda()
+    x1, x2 = torch.zeros(res, device="cuda"), torch.zeros(res, device="cuda")
+    i1 = sc.mgpcg_solve(r, x1, k=-1.0)
+    i2 = sc.mgpcg_solve(r, x2, k=1.0)
+    assert i1.iterations == i2.iterations and i1.converged
+    assert torch.equal(x1, -x2)
