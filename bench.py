@@ -250,6 +250,18 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def job_rate(local_seconds, steps, world, dist=None, device=None):
+    """Whole-job steps/s of N independent replicas: every rank ran `steps` steps of its own scene,
+    the job took the slowest rank's time (an all-reduce MAX; no data moves between replicas)."""
+    elapsed = float(local_seconds)
+    if dist is not None and world > 1:
+        import torch
+        t = torch.tensor([elapsed], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    return world * steps / elapsed, elapsed
+
+
 # ------------------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------------------
@@ -300,12 +312,7 @@ def main():
     barrier()
     launches = sim.scene.launches - launches0
     sim.timer = None
-    elapsed = e0.elapsed_time(e1) / 1e3
-    if dist is not None:
-        t = torch.tensor([elapsed], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
-    value = world * args.steps / elapsed
+    value, elapsed = job_rate(e0.elapsed_time(e1) / 1e3, args.steps, world, dist, "cuda")
     phases = timer.summary()
     infos = sim.infos[iters_before:]
     mg_iters = [i.iterations for i in infos]
@@ -347,13 +354,9 @@ def main():
                 h.copy_(d, non_blocking=True)
         b.record()
         torch.cuda.synchronize()
-        e_el = a.elapsed_time(b) / 1e3
-        if dist is not None:
-            t = torch.tensor([e_el], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e_el = float(t.item())
+        e_rate, _ = job_rate(a.elapsed_time(b) / 1e3, args.steps, world, dist, "cuda")
         gbytes = sum(h.numel() * 4 for h in host_u)
-        e2e = {"value": world * args.steps / e_el, "unit": UNIT, "h2d_bytes_per_step": gbytes,
+        e2e = {"value": e_rate, "unit": UNIT, "h2d_bytes_per_step": gbytes,
                "d2h_bytes_per_step": gbytes}
 
     cpu = None
