@@ -60,22 +60,38 @@ typedef struct pfm_handle pfm_handle;
 
 /* Options and statistics of one MGPCG solve: MGPCG.solve(max_iters, eps, tol)
  * (3D/mgpcg.py:202-280).  tol_mode 0 stops when r.r < tol (the reference's absolute rule);
- * tol_mode 1 stops when sqrt(r.r / r0.r0) < tol (relative). */
+ * tol_mode 1 stops when sqrt(r.r / r0.r0) < tol (relative to the first residual); tol_mode 2
+ * stops when sqrt(r.r / b.b) < tol (relative to the recentred right-hand side b; the same as mode
+ * 1 for a zero initial guess, and the rule to compare warm-started solves at equal residual).
+ *
+ * precision 0 is the reference's FP32 solve.  precision 1 / 2 is the mixed form: the multigrid
+ * levels (the V-cycle's z and r on every level) are stored in FP16 / BF16 and smoothed,
+ * restricted and prolonged with FP32 arithmetic; the PCG vectors x, r, p, Ap stay FP32; inner
+ * products and norms accumulate in FP64.
+ * warm_start 1 starts from the caller's current pressure (p_out of pfm3/pfm2_poisson, x_out of
+ * pfm_mgpcg_solve) instead of zero.
+ * true_residual_every K > 0 replaces the recursive residual by r = b - A x every K iterations, so
+ * rounding drift of the recursive update does not accumulate (the stopping rule stays the
+ * reference's, on the current residual). */
 typedef struct pfm_solve_opts {
   int max_iters;   /* 400 in Poisson() (3D/mgpcg.py:422); -1 = unlimited */
   double eps;      /* 1e-12, added to the denominators of alpha and beta */
   double tol;      /* 1e-12 in Poisson() */
-  int tol_mode;    /* 0 absolute r.r, 1 relative norm */
+  int tol_mode;    /* 0 absolute r.r, 1 relative to r0, 2 relative to b */
   int check_every; /* the iteration loop runs on the device (a CUDA graph WHILE node) and the
                       host waits once per solve; with max_iters = -1 the host relaunches the
                       loop every check_every iterations (>= 1) until it converges */
+  int precision;   /* 0 FP32 (reference), 1 FP16 multigrid levels, 2 BF16 multigrid levels */
+  int warm_start;  /* 1: initial guess = the caller's pressure buffer */
+  int true_residual_every; /* 0: never (reference) */
 } pfm_solve_opts;
 
 typedef struct pfm_solve_stats {
   int iterations;      /* the `it` the reference prints on convergence */
   int converged;       /* 1 if the stopping rule was met */
-  double rTr;          /* final r.r */
-  double rTr0;         /* r.r after the first residual update of iteration 0 (before any stop) */
+  double rTr;          /* final r.r (the true residual when true_residual_every > 0) */
+  double rTr0;         /* r.r of the initial residual */
+  double bTb;          /* b.b of the recentred right-hand side */
 } pfm_solve_stats;
 
 /* ---- handle, workspace, errors ------------------------------------------------------------- */

@@ -25,10 +25,12 @@ struct SolveState {
   double pAp;
   double rTr;
   double rTr0;
+  double bTb;      // b.b of the recentred right-hand side (mixed / warm-started solves)
   double sum;      // scratch result of the last reduction
   float alpha;
   float beta;
   float mean;      // recenter mean
+  float hscale;    // 16-bit level storage holds r * hscale (unit RMS), z is read back / hscale
   int it;          // completed iterations
   int done;        // 1 converged, 2 iteration limit, 3 non-finite
   int conv_it;     // iteration index at convergence
@@ -96,7 +98,7 @@ struct pfm_handle {
   // workspace offsets
   size_t o_key, o_slot, o_order, o_count, o_start, o_blocksums, o_payload;
   size_t o_r[pfm::kMaxLevels], o_z[pfm::kMaxLevels];
-  size_t o_x, o_p, o_Ap, o_partials, o_state, o_maxpart;
+  size_t o_x, o_p, o_Ap, o_b, o_partials, o_state, o_maxpart;
 
   // pinned host mirror of the solve state
   pfm::SolveState* h_state;
@@ -108,7 +110,7 @@ struct pfm_handle {
   cudaGraphExec_t g_setup, g_loop;  // setup + first half-iteration; device-side PCG loop
   int g_setup_nodes, g_body_nodes;
   double g_eps, g_tol;
-  int g_mode, g_valid, g_max_iters, g_chunk;
+  int g_mode, g_valid, g_max_iters, g_chunk, g_variant, g_true_every;
   std::string err;
 };
 

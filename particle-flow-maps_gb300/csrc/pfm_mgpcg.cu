@@ -9,6 +9,9 @@
 //    f64 block and grid combination in block order (no float atomics);
 //  * the restriction scatter (r_{l+1}[I//2] += res/(dim-1), 3D/mgpcg.py:152-158) is a gather
 //    over the 8 (4 in 2D) children, so it needs no atomics either.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
 #include <cmath>
 
 #include "pfm_internal.cuh"
@@ -36,23 +39,32 @@ static inline Lvl lvl_of(const pfm_handle* h, int l) {
   return make_lvl(h->lv[l].n[0], h->lv[l].n[1], h->lv[l].n[2], h->cfg.dim);
 }
 
+// Multigrid level storage: FP32 (the reference), or FP16 / BF16 in the mixed-precision solve;
+// values are widened to FP32 on load and rounded to nearest on store.
+__device__ __forceinline__ float ldv(const float* p) { return *p; }
+__device__ __forceinline__ float ldv(const __half* p) { return __half2float(*p); }
+__device__ __forceinline__ float ldv(const __nv_bfloat16* p) { return __bfloat162float(*p); }
+__device__ __forceinline__ void stv(float* p, float v) { *p = v; }
+__device__ __forceinline__ void stv(__half* p, float v) { *p = __float2half_rn(v); }
+__device__ __forceinline__ void stv(__nv_bfloat16* p, float v) { *p = __float2bfloat16_rn(v); }
+
 // neighbor_sum / num_fluid_neighbors (3D/mgpcg.py:92-115)
-template <int D>
-__device__ __forceinline__ void stencil(const float* __restrict__ f, const Lvl& L, const BC& bc, int i, int j,
+template <int D, typename S>
+__device__ __forceinline__ void stencil(const S* __restrict__ f, const Lvl& L, const BC& bc, int i, int j,
                                         int k, int64_t e, float& nb, float& mult) {
   float ret = 0.f;
   float num = 2.f * D;
   const int64_t sx = (int64_t)L.n1 * L.n2, sy = L.n2;
-  if (i < L.n0 - 1) ret += f[e + sx];
-  if (i > 0) ret += f[e - sx];
+  if (i < L.n0 - 1) ret += ldv(f + e + sx);
+  if (i > 0) ret += ldv(f + e - sx);
   if (D == 3) {
-    if (j < L.n1 - 1) ret += f[e + sy];
-    if (j > 0) ret += f[e - sy];
-    if (k < L.n2 - 1) ret += f[e + 1];
-    if (k > 0) ret += f[e - 1];
+    if (j < L.n1 - 1) ret += ldv(f + e + sy);
+    if (j > 0) ret += ldv(f + e - sy);
+    if (k < L.n2 - 1) ret += ldv(f + e + 1);
+    if (k > 0) ret += ldv(f + e - 1);
   } else {
-    if (j < L.n1 - 1) ret += f[e + sy];
-    if (j > 0) ret += f[e - sy];
+    if (j < L.n1 - 1) ret += ldv(f + e + sy);
+    if (j > 0) ret += ldv(f + e - sy);
   }
   if (i <= 0 && bc.lo[0] == 2) num -= 1.f;
   if (i >= L.n0 - 1 && bc.hi[0] == 2) num -= 1.f;
@@ -199,8 +211,8 @@ __global__ void __launch_bounds__(256) k_subtract_grad_p(float* __restrict__ u, 
 
 // smooth(l, phase): z = (r + nbsum(z)) / mult on cells with (i+j+k)&1 == phase.  One thread per
 // pair of cells along the last axis; the thread updates the member of the right colour.
-template <int D>
-__global__ void __launch_bounds__(256) k_smooth(float* __restrict__ z, const float* __restrict__ r, Lvl L,
+template <int D, typename S>
+__global__ void __launch_bounds__(256) k_smooth(S* __restrict__ z, const S* __restrict__ r, Lvl L,
                                                 BC bc, int phase, const SolveState* st) {
   if (st && st->done) return;
   const int nl = (D == 3) ? L.n2 : L.n1;
@@ -226,14 +238,14 @@ __global__ void __launch_bounds__(256) k_smooth(float* __restrict__ z, const flo
   const int64_t c = ((int64_t)i * L.n1 + j) * L.n2 + k;
   float nb, mult;
   stencil<D>(z, L, bc, i, j, k, c, nb, mult);
-  z[c] = (r[c] + nb) / mult;
+  stv(z + c, (ldv(r + c) + nb) / mult);
 }
 
 // restrict(l) as a gather: rc[I] = sum over children (fine-index order) of res/(dim-1),
 // res = r - (mult z - nbsum(z)).
-template <int D>
-__global__ void __launch_bounds__(256) k_restrict(const float* __restrict__ zf, const float* __restrict__ rf,
-                                                  Lvl Lf, float* __restrict__ rc, Lvl Lc, BC bc,
+template <int D, typename S>
+__global__ void __launch_bounds__(256) k_restrict(const S* __restrict__ zf, const S* __restrict__ rf,
+                                                  Lvl Lf, S* __restrict__ rc, Lvl Lc, BC bc,
                                                   const SolveState* st) {
   if (st && st->done) return;
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -253,15 +265,15 @@ __global__ void __launch_bounds__(256) k_restrict(const float* __restrict__ zf, 
         const int64_t c = ((int64_t)i * Lf.n1 + j) * Lf.n2 + k;
         float nb, mult;
         stencil<D>(zf, Lf, bc, i, j, k, c, nb, mult);
-        float res = rf[c] - (mult * zf[c] - nb);
+        float res = ldv(rf + c) - (mult * ldv(zf + c) - nb);
         acc += res * 1.0f / den;
       }
-  rc[e] = acc;
+  stv(rc + e, acc);
 }
 
 // prolongate(l): z_l[I] += z_{l+1}[I//2]
-template <int D>
-__global__ void __launch_bounds__(256) k_prolong(float* __restrict__ zf, Lvl Lf, const float* __restrict__ zc,
+template <int D, typename S>
+__global__ void __launch_bounds__(256) k_prolong(S* __restrict__ zf, Lvl Lf, const S* __restrict__ zc,
                                                  Lvl Lc, const SolveState* st) {
   if (st && st->done) return;
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -270,7 +282,7 @@ __global__ void __launch_bounds__(256) k_prolong(float* __restrict__ zf, Lvl Lf,
   decode(Lf, e, i, j, k);
   int64_t ce = (D == 3) ? ((int64_t)(i >> 1) * Lc.n1 + (j >> 1)) * Lc.n2 + (k >> 1)
                         : (int64_t)(i >> 1) * Lc.n1 + (j >> 1);
-  zf[e] += zc[ce];
+  stv(zf + e, ldv(zf + e) + ldv(zc + ce));
 }
 
 // init(r, k) (3D/mgpcg.py:71-79): r0 = r * k
@@ -280,28 +292,47 @@ __global__ void __launch_bounds__(256) k_scale(float* __restrict__ out, const fl
     out[e] = in[e] * k;
 }
 
-__global__ void __launch_bounds__(256) k_zero(float* __restrict__ a, int64_t n, const SolveState* st) {
+template <typename S>
+__global__ void __launch_bounds__(256) k_zero(S* __restrict__ a, int64_t n, const SolveState* st) {
   if (st && st->done) return;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
-    a[e] = 0.f;
+    stv(a + e, 0.f);
 }
 
 // ---------------------------------------------------------------------------------------------
 // PCG kernels with fused reductions and device-side scalar updates
 // ---------------------------------------------------------------------------------------------
-enum RedKind { RED_ZTR_INIT = 0, RED_ZTR = 1, RED_RTR0 = 2, RED_MEAN = 3 };
+enum RedKind { RED_ZTR_INIT = 0, RED_ZTR = 1, RED_RTR0 = 2, RED_MEAN = 3, RED_BTB = 4 };
 
-// sum(a*b) (or sum(a) for RED_MEAN) with a finalizer that updates the solve state.
-__global__ void __launch_bounds__(kReduceThreads) k_dot(const float* __restrict__ a, const float* __restrict__ b,
+// the stopping rule of k_update_xr / k_true_residual
+__device__ __forceinline__ bool converged(double rTr, const SolveState* st, double tol, int tol_mode) {
+  if (tol_mode == 0) return rTr < tol;
+  const double ref = (tol_mode == 1) ? st->rTr0 : st->bTb;
+  return sqrt(rTr) < tol * sqrt(ref);
+}
+
+// sum(a*b) (or sum(a) for RED_MEAN) with a finalizer that updates the solve state.  Per-thread
+// partials accumulate in f32 (the reference solve) or f64 (f64 != 0, the mixed solve).
+template <typename SA>
+__global__ void __launch_bounds__(kReduceThreads) k_dot(const SA* __restrict__ a, const float* __restrict__ b,
                                                         int64_t n, RedBuf rb, int kind, double eps, double inv_n,
-                                                        int max_iters) {
+                                                        int max_iters, int f64) {
   SolveState* st = rb.st;
   if (st->done) return;
-  float acc = 0.f;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
-    acc += (kind == RED_MEAN) ? a[e] : a[e] * b[e];
   double total;
-  if (!grid_sum((double)acc, rb.partials, &st->ticket, &total)) return;
+  if (f64) {
+    // a 16-bit level vector (z) holds the scaled values: undo the scale of the residual it answers
+    const double us = (sizeof(SA) == 2) ? 1.0 / (double)st->hscale : 1.0;
+    double acc = 0.0;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+      acc += (kind == RED_MEAN) ? (double)ldv(a + e) : (double)ldv(a + e) * (double)b[e];
+    if (!grid_sum(acc * us, rb.partials, &st->ticket, &total)) return;
+  } else {
+    float acc = 0.f;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+      acc += (kind == RED_MEAN) ? ldv(a + e) : ldv(a + e) * b[e];
+    if (!grid_sum((double)acc, rb.partials, &st->ticket, &total)) return;
+  }
   if (threadIdx.x != 0) return;
   if (kind == RED_ZTR_INIT) {
     st->zTr_old = total;
@@ -320,26 +351,48 @@ __global__ void __launch_bounds__(kReduceThreads) k_dot(const float* __restrict_
     }
   } else if (kind == RED_RTR0) {
     st->rTr0 = total;
+    st->rTr = total;
+    st->hscale = total > 0.0 ? (float)(1.0 / sqrt(total * inv_n)) : 1.f;
+  } else if (kind == RED_BTB) {
+    st->bTb = total;
   } else {
     st->mean = (float)(total * inv_n);
   }
 }
 
-// recenter (3D/mgpcg.py:174-180): r -= mean
-__global__ void __launch_bounds__(256) k_sub_mean(float* __restrict__ r, int64_t n, const SolveState* st) {
+// recenter (3D/mgpcg.py:174-180): r -= mean; with rh, also the level-storage copy of r that the
+// mixed-precision V-cycle smooths against
+template <typename S>
+__global__ void __launch_bounds__(256) k_sub_mean(float* __restrict__ r, S* __restrict__ rh, int64_t n,
+                                                  const SolveState* st) {
   if (st->done) return;
   const float m = st->mean;
+  const float hs = (sizeof(S) == 2) ? st->hscale : 1.f;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const float v = r[e] - m;
+    r[e] = v;
+    if (rh) stv(rh + e, v * hs);
+  }
+}
+
+// the level-storage copy of r (mixed solve without recentring)
+template <typename S>
+__global__ void __launch_bounds__(256) k_to_storage(S* __restrict__ out, const float* __restrict__ in, int64_t n,
+                                                    const SolveState* st) {
+  if (st->done) return;
+  const float hs = (sizeof(S) == 2) ? st->hscale : 1.f;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
-    r[e] -= m;
+    stv(out + e, in[e] * hs);
 }
 
 // compute_Ap + reduce(p, Ap) + alpha = zTr / (pAp + eps)   (3D/mgpcg.py:237-240)
 template <int D>
 __global__ void __launch_bounds__(kReduceThreads) k_Ap_dot(const float* __restrict__ p, float* __restrict__ Ap,
-                                                           Lvl L, BC bc, RedBuf rb, double eps) {
+                                                           Lvl L, BC bc, RedBuf rb, double eps, int f64) {
   SolveState* st = rb.st;
   if (st->done) return;
   float acc = 0.f;
+  double acc64 = 0.0;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < L.count; e += (int64_t)gridDim.x * blockDim.x) {
     int i, j, k;
     decode(L, e, i, j, k);
@@ -348,10 +401,11 @@ __global__ void __launch_bounds__(kReduceThreads) k_Ap_dot(const float* __restri
     float pe = p[e];
     float ap = mult * pe - nb;
     Ap[e] = ap;
-    acc += pe * ap;
+    if (f64) acc64 += (double)pe * (double)ap;
+    else acc += pe * ap;
   }
   double total;
-  if (!grid_sum((double)acc, rb.partials, &st->ticket, &total)) return;
+  if (!grid_sum(f64 ? acc64 : (double)acc, rb.partials, &st->ticket, &total)) return;
   if (threadIdx.x == 0) {
     st->pAp = total;
     st->alpha = (float)(st->zTr_old / (total + eps));
@@ -361,26 +415,78 @@ __global__ void __launch_bounds__(kReduceThreads) k_Ap_dot(const float* __restri
 // update_x, update_r, reduce(r, r) and the convergence test (3D/mgpcg.py:243-258).
 __global__ void __launch_bounds__(kReduceThreads) k_update_xr(float* __restrict__ x, const float* __restrict__ p,
                                                               float* __restrict__ r, const float* __restrict__ Ap,
-                                                              int64_t n, RedBuf rb, double tol, int tol_mode) {
+                                                              int64_t n, RedBuf rb, double tol, int tol_mode,
+                                                              int f64, double inv_n) {
   SolveState* st = rb.st;
   if (st->done) return;
   const float alpha = st->alpha;
   float acc = 0.f;
+  double acc64 = 0.0;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
     x[e] += alpha * p[e];
     float re = r[e] - alpha * Ap[e];
     r[e] = re;
-    acc += re * re;
+    if (f64) acc64 += (double)re * (double)re;
+    else acc += re * re;
   }
   double total;
-  if (!grid_sum((double)acc, rb.partials, &st->ticket, &total)) return;
+  if (!grid_sum(f64 ? acc64 : (double)acc, rb.partials, &st->ticket, &total)) return;
   if (threadIdx.x == 0) {
     st->rTr = total;
-    bool stop = (tol_mode == 0) ? (total < tol) : (sqrt(total) < tol * sqrt(st->rTr0));
+    if (total > 0.0) st->hscale = (float)(1.0 / sqrt(total * inv_n));
     if (!isfinite(total)) {
       st->done = 3;
       st->conv_it = st->it;
-    } else if (stop) {
+    } else if (converged(total, st, tol, tol_mode)) {
+      st->done = 1;
+      st->conv_it = st->it;
+    }
+  }
+}
+
+// r = b - A x: the initial residual of a warm-started solve
+template <int D>
+__global__ void __launch_bounds__(256) k_residual(float* __restrict__ r, const float* __restrict__ b,
+                                                  const float* __restrict__ x, Lvl L, BC bc) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < L.count; e += (int64_t)gridDim.x * blockDim.x) {
+    int i, j, k;
+    decode(L, e, i, j, k);
+    float nb, mult;
+    stencil<D>(x, L, bc, i, j, k, e, nb, mult);
+    r[e] = b[e] - (mult * x[e] - nb);
+  }
+}
+
+// The true residual r = b - A x replaces the recursive one every `every` iterations (f64 norm),
+// so rounding drift of the recursive update does not accumulate.  It does not gate convergence: x
+// is stored in f32, which puts a floor under the true residual (about 2e-5 relative at 64^3 for a
+// smooth pressure) that the reference's recursive 1e-6 rule never sees.
+template <int D>
+__global__ void __launch_bounds__(kReduceThreads) k_true_residual(float* __restrict__ r, const float* __restrict__ b,
+                                                                  const float* __restrict__ x, Lvl L, BC bc,
+                                                                  RedBuf rb, double tol, int tol_mode, int every,
+                                                                  double inv_n) {
+  SolveState* st = rb.st;
+  if (st->done != 0 || every <= 0 || (st->it + 1) % every != 0) return;
+  double acc = 0.0;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < L.count; e += (int64_t)gridDim.x * blockDim.x) {
+    int i, j, k;
+    decode(L, e, i, j, k);
+    float nb, mult;
+    stencil<D>(x, L, bc, i, j, k, e, nb, mult);
+    const float re = b[e] - (mult * x[e] - nb);
+    r[e] = re;
+    acc += (double)re * (double)re;
+  }
+  double total;
+  if (!grid_sum(acc, rb.partials, &st->ticket, &total)) return;
+  if (threadIdx.x == 0) {
+    st->rTr = total;
+    if (total > 0.0) st->hscale = (float)(1.0 / sqrt(total * inv_n));
+    if (!isfinite(total)) {
+      st->done = 3;
+      st->conv_it = st->it;
+    } else if (converged(total, st, tol, tol_mode)) {
       st->done = 1;
       st->conv_it = st->it;
     }
@@ -388,12 +494,19 @@ __global__ void __launch_bounds__(kReduceThreads) k_update_xr(float* __restrict_
 }
 
 // update_p: p = z + beta p (3D/mgpcg.py:147-150)
-__global__ void __launch_bounds__(256) k_update_p(float* __restrict__ p, const float* __restrict__ z, int64_t n,
+template <typename SZ>
+__global__ void __launch_bounds__(256) k_update_p(float* __restrict__ p, const SZ* __restrict__ z, int64_t n,
                                                   const SolveState* st) {
   if (st->done) return;
   const float beta = st->beta;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
-    p[e] = z[e] + beta * p[e];
+  if (sizeof(SZ) == 2) {  // z answers the scaled residual
+    const float us = 1.f / st->hscale;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+      p[e] = ldv(z + e) * us + beta * p[e];
+  } else {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+      p[e] = ldv(z + e) + beta * p[e];
+  }
 }
 
 // Device loop control.  The loop body is the second half of iteration k (recenter, V-cycle, beta,
@@ -440,8 +553,8 @@ __device__ void tail_smooth(float* z, const float* r, const Lvl& L, const BC& bc
   __syncthreads();
 }
 
-template <int D>
-__global__ void __launch_bounds__(kTailThreads) k_vcycle_tail(float* __restrict__ zg, const float* __restrict__ rg,
+template <int D, typename S>
+__global__ void __launch_bounds__(kTailThreads) k_vcycle_tail(S* __restrict__ zg, const S* __restrict__ rg,
                                                               TailPlan T, BC bc, int pre_post, int bottom,
                                                               const SolveState* st) {
   if (st && st->done) return;
@@ -450,7 +563,7 @@ __global__ void __launch_bounds__(kTailThreads) k_vcycle_tail(float* __restrict_
   float* R = sh + T.total;
   const int l0 = T.l0;
   for (int e = threadIdx.x; e < (int)T.lv[l0].count; e += blockDim.x) {
-    R[T.off[l0] + e] = rg[e];
+    R[T.off[l0] + e] = ldv(rg + e);
     Z[T.off[l0] + e] = 0.f;
   }
   __syncthreads();
@@ -510,7 +623,7 @@ __global__ void __launch_bounds__(kTailThreads) k_vcycle_tail(float* __restrict_
       tail_smooth<D>(z, r, Lf, bc, 0);
     }
   }
-  for (int e = threadIdx.x; e < (int)T.lv[l0].count; e += blockDim.x) zg[e] = Z[T.off[l0] + e];
+  for (int e = threadIdx.x; e < (int)T.lv[l0].count; e += blockDim.x) stv(zg + e, Z[T.off[l0] + e]);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -535,13 +648,27 @@ static unsigned stream_blocks(int64_t n) {
   return b > 152u * 16u ? 152u * 16u : b;
 }
 
-template <int D>
+// Level l's z and r in storage S.  Level 0's r is the PCG residual in the FP32 solve; the mixed
+// solve smooths against its level-storage copy, kept in the upper half of level 0's z buffer
+// (level-0 z uses the lower half).
+template <typename S>
+static S* level_z(pfm_handle* h, int l) {
+  return ws_ptr<S>(h, h->o_z[l]);
+}
+
+template <typename S>
+static S* level_r(pfm_handle* h, int l) {
+  if (l == 0 && sizeof(S) == 2) return ws_ptr<S>(h, h->o_z[0]) + h->lv[0].count;
+  return ws_ptr<S>(h, h->o_r[l]);
+}
+
+template <int D, typename S>
 static void smooth_launch(pfm_handle* h, int l, int phase, const SolveState* st, cudaStream_t s) {
   Lvl L = lvl_of(h, l);
   const int nl = (D == 3) ? L.n2 : L.n1;
   int64_t npairs = (D == 3) ? (int64_t)L.n0 * L.n1 * ((nl + 1) / 2) : (int64_t)L.n0 * ((nl + 1) / 2);
-  launch(h, k_smooth<D>, grid_for(npairs, 256), 256, 0, s, ws_ptr<float>(h, h->o_z[l]), ws_ptr<float>(h, h->o_r[l]), L,
-                                                   bc_of(h), phase, st);
+  launch(h, k_smooth<D, S>, grid_for(npairs, 256), 256, 0, s, level_z<S>(h, l), (const S*)level_r<S>(h, l), L,
+         bc_of(h), phase, st);
 }
 
 static int tail_level(const pfm_handle* h) {
@@ -550,25 +677,24 @@ static int tail_level(const pfm_handle* h) {
   return h->L;  // no level small enough: every level runs as grid-wide kernels
 }
 
-// apply_preconditioner (3D/mgpcg.py:182-200)
-template <int D>
+// apply_preconditioner (3D/mgpcg.py:182-200) with level storage S
+template <int D, typename S>
 static void vcycle(pfm_handle* h, const SolveState* st, cudaStream_t s) {
   const int L = h->L;
   const BC bc = bc_of(h);
   const int l0 = tail_level(h);
-  launch(h, k_zero, stream_blocks(h->lv[0].count), 256, 0, s, ws_ptr<float>(h, h->o_z[0]), h->lv[0].count, st);
+  launch(h, k_zero<S>, stream_blocks(h->lv[0].count), 256, 0, s, level_z<S>(h, 0), h->lv[0].count, st);
   const int down_end = l0 < L ? l0 : L - 1;  // grid-wide levels that restrict to a coarser one
   for (int l = 0; l < down_end; ++l) {
     for (int i = 0; i < h->cfg.pre_post_smoothing; ++i) {
-      smooth_launch<D>(h, l, 0, st, s);
-      smooth_launch<D>(h, l, 1, st, s);
+      smooth_launch<D, S>(h, l, 0, st, s);
+      smooth_launch<D, S>(h, l, 1, st, s);
     }
     if (l + 1 != l0)
-      launch(h, k_zero, stream_blocks(h->lv[l + 1].count), 256, 0, s, ws_ptr<float>(h, h->o_z[l + 1]),
-             h->lv[l + 1].count, st);
+      launch(h, k_zero<S>, stream_blocks(h->lv[l + 1].count), 256, 0, s, level_z<S>(h, l + 1), h->lv[l + 1].count, st);
     Lvl Lf = lvl_of(h, l), Lc = lvl_of(h, l + 1);
-    launch(h, k_restrict<D>, grid_for(Lc.count, 256), 256, 0, s, ws_ptr<float>(h, h->o_z[l]), ws_ptr<float>(h, h->o_r[l]),
-           Lf, ws_ptr<float>(h, h->o_r[l + 1]), Lc, bc, st);
+    launch(h, k_restrict<D, S>, grid_for(Lc.count, 256), 256, 0, s, (const S*)level_z<S>(h, l),
+           (const S*)level_r<S>(h, l), Lf, level_r<S>(h, l + 1), Lc, bc, st);
   }
   if (l0 < L) {
     TailPlan T{};
@@ -582,21 +708,21 @@ static void vcycle(pfm_handle* h, const SolveState* st, cudaStream_t s) {
     }
     T.total = off;
     const size_t smem = (size_t)off * 2 * sizeof(float);
-    launch(h, k_vcycle_tail<D>, 1, kTailThreads, smem, s, ws_ptr<float>(h, h->o_z[l0]), ws_ptr<float>(h, h->o_r[l0]),
-           T, bc, h->cfg.pre_post_smoothing, h->cfg.bottom_smoothing, st);
+    launch(h, k_vcycle_tail<D, S>, 1, kTailThreads, smem, s, level_z<S>(h, l0), (const S*)level_r<S>(h, l0), T, bc,
+           h->cfg.pre_post_smoothing, h->cfg.bottom_smoothing, st);
   } else {
     for (int i = 0; i < h->cfg.bottom_smoothing; ++i) {
-      smooth_launch<D>(h, L - 1, 0, st, s);
-      smooth_launch<D>(h, L - 1, 1, st, s);
+      smooth_launch<D, S>(h, L - 1, 0, st, s);
+      smooth_launch<D, S>(h, L - 1, 1, st, s);
     }
   }
   for (int l = down_end - 1; l >= 0; --l) {
     Lvl Lf = lvl_of(h, l), Lc = lvl_of(h, l + 1);
-    launch(h, k_prolong<D>, grid_for(Lf.count, 256), 256, 0, s, ws_ptr<float>(h, h->o_z[l]), Lf,
-           ws_ptr<float>(h, h->o_z[l + 1]), Lc, st);
+    launch(h, k_prolong<D, S>, grid_for(Lf.count, 256), 256, 0, s, level_z<S>(h, l), Lf, (const S*)level_z<S>(h, l + 1),
+           Lc, st);
     for (int i = 0; i < h->cfg.pre_post_smoothing; ++i) {
-      smooth_launch<D>(h, l, 1, st, s);
-      smooth_launch<D>(h, l, 0, st, s);
+      smooth_launch<D, S>(h, l, 1, st, s);
+      smooth_launch<D, S>(h, l, 0, st, s);
     }
   }
 }
@@ -633,64 +759,89 @@ static int run_graph(pfm_handle* h, cudaGraphExec_t exec, int nodes, cudaStream_
   return check_cuda(h, cudaGraphLaunch(exec, s), "graph launch");
 }
 
-// MGPCG.solve (3D/mgpcg.py:202-280) on r_0 (already -div); the solution is left in the
-// workspace vector x.  Two graphs per handle, captured once per option set:
-//   setup: x = p = Ap = 0, recenter, r0.r0, first V-cycle, p = z, z.r, and the first half of
-//          iteration 1 (Ap, alpha, x/r update, convergence test);
+// MGPCG.solve (3D/mgpcg.py:202-280) on r_0 (already k r); the solution is left in the workspace
+// vector x.  Two graphs per handle, captured once per option set:
+//   setup: x (unless warm-started) = p = Ap = 0, recenter, [b = r0, b.b, r0 = b - A x for a warm
+//          start], r0.r0, first V-cycle, p = z, z.r, and the first half of iteration 1 (Ap,
+//          alpha, x/r update, convergence test [, true residual]);
 //   loop:  WHILE(not done and it < it_stop) { second half of iteration k, first half of k+1 },
 //          then the device state is copied to pinned host memory.
-// With a finite max_iters one loop launch finishes the solve; with max_iters = -1 the host
-// relaunches the loop every check_every iterations until the state reports convergence.
-template <int D>
-static int solve_impl(pfm_handle* h, const pfm_solve_opts* opts, pfm_solve_stats* stats, cudaStream_t s) {
-  pfm_solve_opts o{400, 1e-12, 1e-12, 0, 4};
-  if (opts) o = *opts;
-  if (o.check_every < 1) o.check_every = 1;
+// S is the multigrid level storage (float: the reference solve; __half / __nv_bfloat16: the
+// mixed solve, which also accumulates every inner product in f64).  With a finite max_iters one
+// loop launch finishes the solve; with max_iters = -1 the host relaunches the loop every
+// check_every iterations until the state reports convergence.
+template <int D, typename S>
+static int solve_impl(pfm_handle* h, const pfm_solve_opts& o, pfm_solve_stats* stats, cudaStream_t s) {
+  const bool mixed = sizeof(S) == 2;
+  const int f64 = mixed ? 1 : 0;
+  const bool warm = o.warm_start != 0;
+  const bool true_res = o.true_residual_every > 0;
+  const bool keep_b = warm || true_res || o.tol_mode == 2;
   const int chunk = o.max_iters >= 0 ? o.max_iters + 1 : o.check_every;
   const int64_t n = h->cells;
   SolveState* st = ws_ptr<SolveState>(h, h->o_state);
   RedBuf rb{ws_ptr<double>(h, h->o_partials), st};
   float* r0 = ws_ptr<float>(h, h->o_r[0]);
-  float* z0 = ws_ptr<float>(h, h->o_z[0]);
+  S* z0 = level_z<S>(h, 0);
+  S* rh = mixed ? level_r<S>(h, 0) : nullptr;
   float* x = ws_ptr<float>(h, h->o_x);
   float* p = ws_ptr<float>(h, h->o_p);
   float* Ap = ws_ptr<float>(h, h->o_Ap);
+  float* bvec = ws_ptr<float>(h, h->o_b);
   SolveState* hs = h->h_state;
   const Lvl L0 = lvl_of(h, 0);
   const BC bc = bc_of(h);
   const double inv_n = 1.0 / (double)n;
   const bool neu = all_neumann(h);
   const int mi = o.max_iters;
+  const int key_mode = (o.precision & 3) | (warm ? 4 : 0);
   if (!h->g_valid || h->g_eps != o.eps || h->g_tol != o.tol || h->g_mode != o.tol_mode || h->g_max_iters != mi ||
-      h->g_chunk != chunk) {
+      h->g_chunk != chunk || h->g_variant != key_mode || h->g_true_every != o.true_residual_every) {
     if (h->g_setup) cudaGraphExecDestroy(h->g_setup);
     if (h->g_loop) cudaGraphExecDestroy(h->g_loop);
     h->g_setup = h->g_loop = nullptr;
     h->g_valid = 0;
-    auto recenter = [&](cudaStream_t q) {
-      if (!neu) return;
-      launch(h, k_dot, red_blocks(n), kReduceThreads, 0, q, (const float*)r0, (const float*)nullptr, n, rb,
-             (int)RED_MEAN, o.eps, inv_n, mi);
-      launch(h, k_sub_mean, stream_blocks(n), 256, 0, q, r0, n, (const SolveState*)st);
+    // recenter r0 (all-Neumann) and, in the mixed solve with `storage`, refresh its scaled
+    // level-storage copy
+    auto recenter = [&](cudaStream_t q, bool storage) {
+      S* out = (mixed && storage) ? rh : nullptr;
+      if (neu) {
+        launch(h, k_dot<float>, red_blocks(n), kReduceThreads, 0, q, (const float*)r0, (const float*)nullptr, n, rb,
+               (int)RED_MEAN, o.eps, inv_n, mi, f64);
+        launch(h, k_sub_mean<S>, stream_blocks(n), 256, 0, q, r0, out, n, (const SolveState*)st);
+      } else if (out) {
+        launch(h, k_to_storage<S>, stream_blocks(n), 256, 0, q, out, (const float*)r0, n, (const SolveState*)st);
+      }
     };
     auto first_half = [&](cudaStream_t q) {
-      launch(h, k_Ap_dot<D>, red_blocks(n), kReduceThreads, 0, q, (const float*)p, Ap, L0, bc, rb, o.eps);
+      launch(h, k_Ap_dot<D>, red_blocks(n), kReduceThreads, 0, q, (const float*)p, Ap, L0, bc, rb, o.eps, f64);
       launch(h, k_update_xr, red_blocks(n), kReduceThreads, 0, q, x, (const float*)p, r0, (const float*)Ap, n, rb, o.tol,
-             o.tol_mode);
+             o.tol_mode, f64, inv_n);
+      if (true_res)
+        launch(h, k_true_residual<D>, red_blocks(n), kReduceThreads, 0, q, r0, (const float*)bvec, (const float*)x, L0,
+               bc, rb, o.tol, o.tol_mode, o.true_residual_every, inv_n);
     };
     auto setup = [&](cudaStream_t q) {
       // init(): x = p = Ap = 0 (3D/mgpcg.py:63-79); z0 is zeroed by the V-cycle
       cudaMemsetAsync(st, 0, sizeof(SolveState), q);
-      cudaMemsetAsync(x, 0, n * 4, q);
+      if (!warm) cudaMemsetAsync(x, 0, n * 4, q);
       cudaMemsetAsync(p, 0, n * 4, q);
       cudaMemsetAsync(Ap, 0, n * 4, q);
-      recenter(q);
-      launch(h, k_dot, red_blocks(n), kReduceThreads, 0, q, (const float*)r0, (const float*)r0, n, rb, (int)RED_RTR0,
-             o.eps, inv_n, mi);
-      vcycle<D>(h, st, q);
-      launch(h, k_update_p, stream_blocks(n), 256, 0, q, p, (const float*)z0, n, (const SolveState*)st);
-      launch(h, k_dot, red_blocks(n), kReduceThreads, 0, q, (const float*)z0, (const float*)r0, n, rb,
-             (int)RED_ZTR_INIT, o.eps, inv_n, mi);
+      recenter(q, false);
+      if (keep_b) {
+        cudaMemcpyAsync(bvec, r0, n * 4, cudaMemcpyDeviceToDevice, q);
+        launch(h, k_dot<float>, red_blocks(n), kReduceThreads, 0, q, (const float*)bvec, (const float*)bvec, n, rb,
+               (int)RED_BTB, o.eps, inv_n, mi, 1);
+      }
+      if (warm) launch(h, k_residual<D>, stream_blocks(n), 256, 0, q, r0, (const float*)bvec, (const float*)x, L0, bc);
+      launch(h, k_dot<float>, red_blocks(n), kReduceThreads, 0, q, (const float*)r0, (const float*)r0, n, rb,
+             (int)RED_RTR0, o.eps, inv_n, mi, f64);
+      // the scaled level-storage copy of r0, once r0.r0 (and so the scale) is known
+      if (mixed) launch(h, k_to_storage<S>, stream_blocks(n), 256, 0, q, rh, (const float*)r0, n, (const SolveState*)st);
+      vcycle<D, S>(h, st, q);
+      launch(h, k_update_p<S>, stream_blocks(n), 256, 0, q, p, (const S*)z0, n, (const SolveState*)st);
+      launch(h, k_dot<S>, red_blocks(n), kReduceThreads, 0, q, (const S*)z0, (const float*)r0, n, rb,
+             (int)RED_ZTR_INIT, o.eps, inv_n, mi, f64);
       first_half(q);
     };
     int rc = capture(h, setup, &h->g_setup, &h->g_setup_nodes);
@@ -737,11 +888,11 @@ static int solve_impl(pfm_handle* h, const pfm_solve_opts* opts, pfm_solve_stats
                     "begin body capture");
     if (!rc) {
       const uint64_t b0 = h->launches;
-      recenter(cs);
-      vcycle<D>(h, st, cs);
-      launch(h, k_dot, red_blocks(n), kReduceThreads, 0, cs, (const float*)z0, (const float*)r0, n, rb, (int)RED_ZTR,
-             o.eps, inv_n, mi);
-      launch(h, k_update_p, stream_blocks(n), 256, 0, cs, p, (const float*)z0, n, (const SolveState*)st);
+      recenter(cs, true);
+      vcycle<D, S>(h, st, cs);
+      launch(h, k_dot<S>, red_blocks(n), kReduceThreads, 0, cs, (const S*)z0, (const float*)r0, n, rb, (int)RED_ZTR,
+             o.eps, inv_n, mi, f64);
+      launch(h, k_update_p<S>, stream_blocks(n), 256, 0, cs, p, (const S*)z0, n, (const SolveState*)st);
       first_half(cs);
       launch(h, k_loop_cond, 1, 1, 0, cs, (const SolveState*)st, cond);
       h->g_body_nodes = (int)(h->launches - b0);
@@ -757,6 +908,8 @@ static int solve_impl(pfm_handle* h, const pfm_solve_opts* opts, pfm_solve_stats
     h->g_mode = o.tol_mode;
     h->g_max_iters = mi;
     h->g_chunk = chunk;
+    h->g_variant = key_mode;
+    h->g_true_every = o.true_residual_every;
     h->g_valid = 1;
   }
   int rc = run_graph(h, h->g_setup, h->g_setup_nodes, s);
@@ -777,15 +930,34 @@ static int solve_impl(pfm_handle* h, const pfm_solve_opts* opts, pfm_solve_stats
     stats->iterations = hs->done ? hs->conv_it : hs->it;
     stats->rTr = hs->rTr;
     stats->rTr0 = hs->rTr0;
+    stats->bTb = hs->bTb;
   }
   if (hs->done == 3) return set_error(h, PFM_ERR_NONFINITE, "MGPCG: non-finite residual");
   if (hs->done != 1) return set_error(h, PFM_ERR_NOT_CONVERGED, "MGPCG: iteration limit reached");
   return PFM_OK;
 }
 
+template <int D>
+static int solve_dispatch(pfm_handle* h, const pfm_solve_opts* opts, pfm_solve_stats* stats, cudaStream_t s) {
+  pfm_solve_opts o{400, 1e-12, 1e-12, 0, 4, 0, 0, 0};
+  if (opts) o = *opts;
+  if (o.check_every < 1) o.check_every = 1;
+  if (o.tol_mode < 0 || o.tol_mode > 2) return set_error(h, PFM_ERR_ARG, "MGPCG: tol_mode must be 0, 1 or 2");
+  if (o.precision == 1) return solve_impl<D, __half>(h, o, stats, s);
+  if (o.precision == 2) return solve_impl<D, __nv_bfloat16>(h, o, stats, s);
+  if (o.precision != 0) return set_error(h, PFM_ERR_ARG, "MGPCG: precision must be 0 (FP32), 1 (FP16) or 2 (BF16)");
+  return solve_impl<D, float>(h, o, stats, s);
+}
+
 int mgpcg_solve_in_place(pfm_handle* h, float* x_out, const pfm_solve_opts* opts, pfm_solve_stats* stats,
                          cudaStream_t s) {
-  int rc = h->cfg.dim == 3 ? solve_impl<3>(h, opts, stats, s) : solve_impl<2>(h, opts, stats, s);
+  if (opts && opts->warm_start) {  // the initial guess is the caller's current x_out
+    if (!x_out) return set_error(h, PFM_ERR_NULL, "MGPCG: warm_start needs the pressure buffer");
+    int c = check_cuda(h, cudaMemcpyAsync(ws_ptr<float>(h, h->o_x), x_out, h->cells * 4, cudaMemcpyDeviceToDevice, s),
+                       "copy initial guess");
+    if (c) return c;
+  }
+  int rc = h->cfg.dim == 3 ? solve_dispatch<3>(h, opts, stats, s) : solve_dispatch<2>(h, opts, stats, s);
   if (rc != PFM_OK && rc != PFM_ERR_NOT_CONVERGED) return rc;
   if (x_out) {
     int c = check_cuda(h, cudaMemcpyAsync(x_out, ws_ptr<float>(h, h->o_x), h->cells * 4, cudaMemcpyDeviceToDevice, s),

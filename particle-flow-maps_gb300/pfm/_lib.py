@@ -29,12 +29,13 @@ class Config(ctypes.Structure):
 
 class SolveOpts(ctypes.Structure):
     _fields_ = [("max_iters", ctypes.c_int), ("eps", ctypes.c_double), ("tol", ctypes.c_double),
-                ("tol_mode", ctypes.c_int), ("check_every", ctypes.c_int)]
+                ("tol_mode", ctypes.c_int), ("check_every", ctypes.c_int), ("precision", ctypes.c_int),
+                ("warm_start", ctypes.c_int), ("true_residual_every", ctypes.c_int)]
 
 
 class SolveStats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("converged", ctypes.c_int), ("rTr", ctypes.c_double),
-                ("rTr0", ctypes.c_double)]
+                ("rTr0", ctypes.c_double), ("bTb", ctypes.c_double)]
 
 
 # name -> argument types (all return int status unless listed in _RESTYPE)

@@ -23,6 +23,7 @@ class SolveInfo:
         self.converged = bool(stats.converged)
         self.rTr = float(stats.rTr)
         self.rTr0 = float(stats.rTr0)
+        self.bTb = float(stats.bTb)
         self.status = status
 
     def __repr__(self):
@@ -303,19 +304,31 @@ class Scene:
         self._check(self.lib.pfm2_update_imp(self.h, _ptr(imp), _ptr(init_imp), _ptr(T), self._stream()))
 
     @staticmethod
-    def _opts(max_iters, tol, tol_mode, check_every, eps=1e-12):
+    def _opts(max_iters, tol, tol_mode, check_every, eps=1e-12, precision=0, warm_start=False, true_residual_every=0):
         o = SolveOpts()
         o.max_iters, o.eps, o.tol, o.tol_mode, o.check_every = int(max_iters), float(eps), float(tol), int(tol_mode), int(check_every)
+        o.precision = {"fp32": 0, "fp16": 1, "bf16": 2}.get(precision, precision)
+        o.precision = int(o.precision)
+        o.warm_start = int(bool(warm_start))
+        o.true_residual_every = int(true_residual_every)
         return o
 
-    def poisson(self, u, p_out=None, max_iters=400, tol=1e-12, tol_mode=0, check_every=4, raise_on_limit=False):
-        """MGPCG_{2,3}.Poisson in place on u (a sync point).  Returns SolveInfo."""
+    def poisson(self, u, p_out=None, max_iters=400, tol=1e-12, tol_mode=0, check_every=4, raise_on_limit=False,
+                precision=0, warm_start=False, true_residual_every=0):
+        """MGPCG_{2,3}.Poisson in place on u (a sync point).  Returns SolveInfo.
+
+        ``precision`` "fp32" (0, the reference), "fp16" (1) or "bf16" (2) multigrid level storage;
+        ``warm_start`` starts from p_out's current pressure; ``true_residual_every`` K > 0
+        recomputes r = b - A x every K iterations and before accepting convergence."""
         u = self._grids(u)
         if p_out is not None:
             self._dev(p_out, "p_out")
             if tuple(p_out.shape) != self.cell_shape:
                 raise PfmError(2, "p_out shape")
-        o = self._opts(max_iters, tol, tol_mode, check_every)
+        elif warm_start:
+            raise PfmError(1, "warm_start needs p_out (the previous pressure)")
+        o = self._opts(max_iters, tol, tol_mode, check_every, precision=precision, warm_start=warm_start,
+                       true_residual_every=true_residual_every)
         s = SolveStats()
         fn = self.lib.pfm3_poisson if self.dim == 3 else self.lib.pfm2_poisson
         allow = () if raise_on_limit else (_lib.PFM_ERR_NOT_CONVERGED,)
@@ -355,11 +368,14 @@ class Scene:
         self._check(self.lib.pfm_launch_count(self.h, ctypes.byref(n)))
         return int(n.value)
 
-    def mgpcg_solve(self, r, x_out, k=-1.0, max_iters=400, tol=1e-12, tol_mode=0, check_every=4):
-        """MGPCG init(r, k) + solve + get_result: lap(x) = k r (k = -1 for the divergence)."""
+    def mgpcg_solve(self, r, x_out, k=-1.0, max_iters=400, tol=1e-12, tol_mode=0, check_every=4, precision=0,
+                    warm_start=False, true_residual_every=0):
+        """MGPCG init(r, k) + solve + get_result: lap(x) = k r (k = -1 for the divergence);
+        with warm_start the solve starts from x_out's current values."""
         self._cells(r, "r")
         self._cells(x_out, "x_out")
-        o = self._opts(max_iters, tol, tol_mode, check_every)
+        o = self._opts(max_iters, tol, tol_mode, check_every, precision=precision, warm_start=warm_start,
+                       true_residual_every=true_residual_every)
         s = SolveStats()
         st = self._check(self.lib.pfm_mgpcg_solve(self.h, _ptr(r), ctypes.c_float(k), _ptr(x_out), ctypes.byref(o),
                                                   ctypes.byref(s), self._stream()),

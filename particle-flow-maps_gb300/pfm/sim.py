@@ -152,6 +152,7 @@ class Sim3D:
         sc.reset_T(self.T_init)
         sc.reset_T(self.T_gm)
         self.p = torch.zeros(sc.cell_shape, device=dev)
+        self.p_mid = torch.zeros(sc.cell_shape, device=dev)  # the midpoint solve's pressure (warm starts)
         self.i, self.ik = -1, 0
         self.infos = []
         self.last_dt = None
@@ -189,7 +190,7 @@ class Sim3D:
             with self._t("midpoint"):
                 sc.midpoint(self.u, self.u_mid, float(np.float32(0.5 * curr_dt)))
             with self._t("poisson_mid"):
-                self.infos.append(sc.poisson(self.u_mid, **self.poisson_opts))
+                self.infos.append(sc.poisson(self.u_mid, self.p_mid, **self.poisson_opts))
             adv = self.u_mid
         if self.fused_rk4_p2g:
             with self._t("rk4"):

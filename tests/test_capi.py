@@ -59,8 +59,9 @@ def _c_layout():
 int main(void) {
   printf("%zu %zu %zu %zu %zu\n", sizeof(pfm_config), offsetof(pfm_config, dx), offsetof(pfm_config, particles),
          offsetof(pfm_config, boundary), offsetof(pfm_config, use_apic));
-  printf("%zu %zu %zu\n", sizeof(pfm_solve_opts), offsetof(pfm_solve_opts, tol), offsetof(pfm_solve_opts, check_every));
-  printf("%zu %zu\n", sizeof(pfm_solve_stats), offsetof(pfm_solve_stats, rTr0));
+  printf("%zu %zu %zu %zu\n", sizeof(pfm_solve_opts), offsetof(pfm_solve_opts, tol), offsetof(pfm_solve_opts, check_every),
+         offsetof(pfm_solve_opts, true_residual_every));
+  printf("%zu %zu %zu\n", sizeof(pfm_solve_stats), offsetof(pfm_solve_stats, rTr0), offsetof(pfm_solve_stats, bTb));
   return 0;
 }
 """
@@ -80,9 +81,9 @@ def test_struct_layouts_match_header():
     C = _lib.Config
     assert c[:5] == [ctypes.sizeof(C), C.dx.offset, C.particles.offset, C.boundary.offset, C.use_apic.offset]
     O = _lib.SolveOpts
-    assert c[5:8] == [ctypes.sizeof(O), O.tol.offset, O.check_every.offset]
+    assert c[5:9] == [ctypes.sizeof(O), O.tol.offset, O.check_every.offset, O.true_residual_every.offset]
     S = _lib.SolveStats
-    assert c[8:10] == [ctypes.sizeof(S), S.rTr0.offset]
+    assert c[9:12] == [ctypes.sizeof(S), S.rTr0.offset, S.bTb.offset]
 
 
 def test_scene_fails_loudly_without_cuda():
