@@ -46,6 +46,10 @@ def parse():
     ap.add_argument("--cpu-res", type=int, default=64, help="grid of the bounded CPU sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--arms", default="both", choices=["both", "plain", "mixed"],
+                    help="plain FP32 MGPCG and/or the mixed-precision warm-started MGPCG (the headline)")
+    ap.add_argument("--precision", default="fp16", choices=["fp16", "bf16"],
+                    help="multigrid level storage of the mixed arm")
     return ap.parse_args()
 
 
@@ -75,7 +79,7 @@ def make_sim(res, ppc_axis, poisson_opts, device="cuda"):
         sc.add_vortex_ring(vc, **r)
     sc.split_central_vector(vc, sim.u)
     del vc
-    sc.poisson(sim.u, **poisson_opts)  # split_central_vector + Poisson (run_3D.py:667-670)
+    sc.poisson(sim.u, sim.p, **poisson_opts)  # split_central_vector + Poisson (run_3D.py:667-670); p starts at 0
     torch.cuda.synchronize()
     return sim
 
@@ -285,37 +289,52 @@ def main():
             dist.barrier()
         torch.cuda.synchronize()
 
-    popts = dict(tol=args.tol, tol_mode=args.tol_mode, max_iters=400, check_every=4)
-    sim = make_sim(args.res, args.ppc_axis, popts)
-    for _ in range(args.warmup):
-        sim.step()
-    torch.cuda.synchronize()
+    def timed_arm(popts):
+        """W warm-up steps, then K steps timed with CUDA events (max over ranks), phase events,
+        launch counts and the SM clocks sampled during the timed region."""
+        sim = make_sim(args.res, args.ppc_axis, popts)
+        for _ in range(args.warmup):
+            sim.step()
+        torch.cuda.synchronize()
+        timer = PhaseTimer()
+        sim.timer = timer
+        iters_before = len(sim.infos)
+        launches0 = sim.scene.launches
+        clocks = ClockSampler(local)
+        barrier()
+        clocks.start()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record()
+        torch.cuda.nvtx.range_push("pfm_timed_steps")  # lets ncu --nvtx-include select the timed steps
+        for _ in range(args.steps):
+            sim.step()
+        torch.cuda.nvtx.range_pop()
+        e1.record()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        clk = clocks.stop()
+        barrier()
+        sim.timer = None
+        value, elapsed = job_rate(e0.elapsed_time(e1) / 1e3, args.steps, world, dist, "cuda")
+        return dict(sim=sim, value=value, elapsed=elapsed, wall=wall, clocks=clk,
+                    launches=sim.scene.launches - launches0, phases=timer.summary(),
+                    mg_iters=[i.iterations for i in sim.infos[iters_before:]])
 
-    timer = PhaseTimer()
-    sim.timer = timer
-    iters_before = len(sim.infos)
-    launches0 = sim.scene.launches
-    clocks = ClockSampler(local)
-    barrier()
-    clocks.start()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    t0 = time.perf_counter()
-    e0.record()
-    torch.cuda.nvtx.range_push("pfm_timed_steps")  # lets ncu --nvtx-include select the timed steps
-    for _ in range(args.steps):
-        sim.step()
-    torch.cuda.nvtx.range_pop()
-    e1.record()
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - t0
-    clk = clocks.stop()
-    barrier()
-    launches = sim.scene.launches - launches0
-    sim.timer = None
-    value, elapsed = job_rate(e0.elapsed_time(e1) / 1e3, args.steps, world, dist, "cuda")
-    phases = timer.summary()
-    infos = sim.infos[iters_before:]
-    mg_iters = [i.iterations for i in infos]
+    # the two arms of the metric, at the same residual: MGPCG stops at |r| < tol |b| in both
+    plain_opts = dict(tol=args.tol, tol_mode=args.tol_mode, max_iters=400, check_every=4)
+    mixed_opts = dict(tol=args.tol, tol_mode=2, max_iters=400, check_every=4, precision=args.precision,
+                      warm_start=True, true_residual_every=5)
+    plain = None
+    if args.arms in ("both", "plain"):
+        plain = timed_arm(plain_opts)
+        if args.arms == "both":
+            del plain["sim"]
+            torch.cuda.empty_cache()
+    head = timed_arm(mixed_opts) if args.arms in ("both", "mixed") else plain
+    sim = head["sim"]
+    value, elapsed, wall, clk, launches = head["value"], head["elapsed"], head["wall"], head["clocks"], head["launches"]
+    phases, mg_iters = head["phases"], head["mg_iters"]
 
     # roofline of the dominant single-kernel phase: RK4_T_forward (one launch per step)
     P = sim.P
@@ -357,26 +376,35 @@ def main():
         e_rate, _ = job_rate(a.elapsed_time(b) / 1e3, args.steps, world, dist, "cuda")
         gbytes = sum(h.numel() * 4 for h in host_u)
         e2e = {"value": e_rate, "unit": UNIT, "h2d_bytes_per_step": gbytes,
-               "d2h_bytes_per_step": gbytes}
+               "d2h_bytes_per_step": gbytes, "mgpcg_iters": [i.iterations for i in sim.infos[-2 * args.steps:]]}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline_entry(args, n)
 
     if rank == 0:
+        mixed = args.arms != "plain"
+        arm = (f"mixed-precision MGPCG ({args.precision} multigrid levels, FP64 inner products, true residual "
+               f"every 5 iterations) warm-started from the previous step's pressure" if mixed else
+               "plain FP32 MGPCG from a zero initial guess")
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3, "wall_s": wall,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded two-ring initial condition and jittered particles)",
                 "config": {"workload": f"3D {n}^3 two-ring leapfrog, {args.ppc_axis ** 3} ppc ({P} particles), "
-                                       f"plain FP32 step, MGPCG tol {args.tol:g} "
-                                       f"({'relative' if args.tol_mode else 'absolute r.r'})",
+                                       f"FP32 particle/grid step; {arm}; MGPCG to |r| < {args.tol:g} |b|",
                            "res": n, "particles": P, "parallelism": f"replicas x{world}",
                            "l2": "inputs larger than L2 (particle state %.1f GB)" % (P * 132 / 1e9)},
                 "particle_updates_per_s": value * P,
                 "mgpcg_iters": mg_iters,
                 "phase_ms": {k: statistics.mean(v) for k, v in phases.items()},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches}
+        if plain is not None and mixed:
+            line["plain_fp32"] = {"value": plain["value"], "ms_per_step": plain["elapsed"] / args.steps * 1e3,
+                                  "mgpcg_iters": plain["mg_iters"],
+                                  "phase_ms": {k: statistics.mean(v) for k, v in plain["phases"].items()},
+                                  "clocks": plain["clocks"]}
+            line["speedup_vs_plain_fp32"] = value / plain["value"]
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

@@ -67,12 +67,13 @@ typedef struct pfm_handle pfm_handle;
  * precision 0 is the reference's FP32 solve.  precision 1 / 2 is the mixed form: the multigrid
  * levels (the V-cycle's z and r on every level) are stored in FP16 / BF16 and smoothed,
  * restricted and prolonged with FP32 arithmetic; the PCG vectors x, r, p, Ap stay FP32; inner
- * products and norms accumulate in FP64.
+ * products and norms are compensated FP32 sums per thread combined in FP64.
  * warm_start 1 starts from the caller's current pressure (p_out of pfm3/pfm2_poisson, x_out of
  * pfm_mgpcg_solve) instead of zero.
- * true_residual_every K > 0 replaces the recursive residual by r = b - A x every K iterations, so
- * rounding drift of the recursive update does not accumulate (the stopping rule stays the
- * reference's, on the current residual). */
+ * true_residual_every K > 0 recomputes the true residual |b - A x| every K iterations and after
+ * the last one and reports it (stats.rTr_true); the stopping rule stays the reference's, on the
+ * recursive residual (x is stored in f32, whose rounding alone leaves a true residual of about
+ * 2e-5 relative at 64^3, above a 1e-6 rule). */
 typedef struct pfm_solve_opts {
   int max_iters;   /* 400 in Poisson() (3D/mgpcg.py:422); -1 = unlimited */
   double eps;      /* 1e-12, added to the denominators of alpha and beta */
@@ -83,7 +84,7 @@ typedef struct pfm_solve_opts {
                       loop every check_every iterations (>= 1) until it converges */
   int precision;   /* 0 FP32 (reference), 1 FP16 multigrid levels, 2 BF16 multigrid levels */
   int warm_start;  /* 1: initial guess = the caller's pressure buffer */
-  int true_residual_every; /* 0: never (reference) */
+  int true_residual_every; /* 0: never (reference); K > 0: check every K iterations and at the end */
 } pfm_solve_opts;
 
 typedef struct pfm_solve_stats {
@@ -92,6 +93,7 @@ typedef struct pfm_solve_stats {
   double rTr;          /* final r.r (the true residual when true_residual_every > 0) */
   double rTr0;         /* r.r of the initial residual */
   double bTb;          /* b.b of the recentred right-hand side */
+  double rTr_true;     /* |b - A x|^2 after the solve (true_residual_every > 0), else -1 */
 } pfm_solve_stats;
 
 /* ---- handle, workspace, errors ------------------------------------------------------------- */

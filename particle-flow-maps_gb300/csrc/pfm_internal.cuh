@@ -26,6 +26,7 @@ struct SolveState {
   double rTr;
   double rTr0;
   double bTb;      // b.b of the recentred right-hand side (mixed / warm-started solves)
+  double rTr_true; // |b - A x|^2 at the last true-residual check
   double sum;      // scratch result of the last reduction
   float alpha;
   float beta;

@@ -304,6 +304,19 @@ __global__ void __launch_bounds__(256) k_zero(S* __restrict__ a, int64_t n, cons
 // ---------------------------------------------------------------------------------------------
 enum RedKind { RED_ZTR_INIT = 0, RED_ZTR = 1, RED_RTR0 = 2, RED_MEAN = 3, RED_BTB = 4 };
 
+// Per-thread partial sums of the mixed solve: Neumaier-compensated f32 (each thread adds at most a
+// few hundred terms; the block and grid sums are f64).  Per-element f64 arithmetic would run on
+// GB300's narrow FP64 pipe and cost about 0.1 ms per PCG iteration at 256^3.
+struct CompSum {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float t = s + x;
+    c += (fabsf(s) >= fabsf(x)) ? ((s - t) + x) : ((x - t) + s);
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
 // the stopping rule of k_update_xr / k_true_residual
 __device__ __forceinline__ bool converged(double rTr, const SolveState* st, double tol, int tol_mode) {
   if (tol_mode == 0) return rTr < tol;
@@ -323,10 +336,10 @@ __global__ void __launch_bounds__(kReduceThreads) k_dot(const SA* __restrict__ a
   if (f64) {
     // a 16-bit level vector (z) holds the scaled values: undo the scale of the residual it answers
     const double us = (sizeof(SA) == 2) ? 1.0 / (double)st->hscale : 1.0;
-    double acc = 0.0;
+    CompSum acc;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
-      acc += (kind == RED_MEAN) ? (double)ldv(a + e) : (double)ldv(a + e) * (double)b[e];
-    if (!grid_sum(acc * us, rb.partials, &st->ticket, &total)) return;
+      acc.add((kind == RED_MEAN) ? ldv(a + e) : ldv(a + e) * b[e]);
+    if (!grid_sum(acc.value() * us, rb.partials, &st->ticket, &total)) return;
   } else {
     float acc = 0.f;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
@@ -392,7 +405,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_Ap_dot(const float* __restri
   SolveState* st = rb.st;
   if (st->done) return;
   float acc = 0.f;
-  double acc64 = 0.0;
+  CompSum cacc;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < L.count; e += (int64_t)gridDim.x * blockDim.x) {
     int i, j, k;
     decode(L, e, i, j, k);
@@ -401,11 +414,11 @@ __global__ void __launch_bounds__(kReduceThreads) k_Ap_dot(const float* __restri
     float pe = p[e];
     float ap = mult * pe - nb;
     Ap[e] = ap;
-    if (f64) acc64 += (double)pe * (double)ap;
+    if (f64) cacc.add(pe * ap);
     else acc += pe * ap;
   }
   double total;
-  if (!grid_sum(f64 ? acc64 : (double)acc, rb.partials, &st->ticket, &total)) return;
+  if (!grid_sum(f64 ? cacc.value() : (double)acc, rb.partials, &st->ticket, &total)) return;
   if (threadIdx.x == 0) {
     st->pAp = total;
     st->alpha = (float)(st->zTr_old / (total + eps));
@@ -421,16 +434,16 @@ __global__ void __launch_bounds__(kReduceThreads) k_update_xr(float* __restrict_
   if (st->done) return;
   const float alpha = st->alpha;
   float acc = 0.f;
-  double acc64 = 0.0;
+  CompSum cacc;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
     x[e] += alpha * p[e];
     float re = r[e] - alpha * Ap[e];
     r[e] = re;
-    if (f64) acc64 += (double)re * (double)re;
+    if (f64) cacc.add(re * re);
     else acc += re * re;
   }
   double total;
-  if (!grid_sum(f64 ? acc64 : (double)acc, rb.partials, &st->ticket, &total)) return;
+  if (!grid_sum(f64 ? cacc.value() : (double)acc, rb.partials, &st->ticket, &total)) return;
   if (threadIdx.x == 0) {
     st->rTr = total;
     if (total > 0.0) st->hscale = (float)(1.0 / sqrt(total * inv_n));
@@ -457,40 +470,29 @@ __global__ void __launch_bounds__(256) k_residual(float* __restrict__ r, const f
   }
 }
 
-// The true residual r = b - A x replaces the recursive one every `every` iterations (f64 norm),
-// so rounding drift of the recursive update does not accumulate.  It does not gate convergence: x
-// is stored in f32, which puts a floor under the true residual (about 2e-5 relative at 64^3 for a
-// smooth pressure) that the reference's recursive 1e-6 rule never sees.
+// True-residual check: |b - A x|^2 (compensated f32 partials, f64 combination) into rTr_true,
+// every `every` iterations and, with every < 0, unconditionally (after the loop).  It reports and
+// does not steer: x is stored in f32, which puts a floor under the true residual (about 2e-5
+// relative at 64^3 for a smooth pressure, more at 256^3) below the reference's recursive 1e-6
+// rule, so replacing the recursive residual by it would hold every solve above its tolerance.
 template <int D>
-__global__ void __launch_bounds__(kReduceThreads) k_true_residual(float* __restrict__ r, const float* __restrict__ b,
+__global__ void __launch_bounds__(kReduceThreads) k_true_residual(const float* __restrict__ b,
                                                                   const float* __restrict__ x, Lvl L, BC bc,
-                                                                  RedBuf rb, double tol, int tol_mode, int every,
-                                                                  double inv_n) {
+                                                                  RedBuf rb, int every) {
   SolveState* st = rb.st;
-  if (st->done != 0 || every <= 0 || (st->it + 1) % every != 0) return;
-  double acc = 0.0;
+  if (every > 0 && (st->done != 0 || (st->it + 1) % every != 0)) return;
+  CompSum acc;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < L.count; e += (int64_t)gridDim.x * blockDim.x) {
     int i, j, k;
     decode(L, e, i, j, k);
     float nb, mult;
     stencil<D>(x, L, bc, i, j, k, e, nb, mult);
     const float re = b[e] - (mult * x[e] - nb);
-    r[e] = re;
-    acc += (double)re * (double)re;
+    acc.add(re * re);
   }
   double total;
-  if (!grid_sum(acc, rb.partials, &st->ticket, &total)) return;
-  if (threadIdx.x == 0) {
-    st->rTr = total;
-    if (total > 0.0) st->hscale = (float)(1.0 / sqrt(total * inv_n));
-    if (!isfinite(total)) {
-      st->done = 3;
-      st->conv_it = st->it;
-    } else if (converged(total, st, tol, tol_mode)) {
-      st->done = 1;
-      st->conv_it = st->it;
-    }
-  }
+  if (!grid_sum(acc.value(), rb.partials, &st->ticket, &total)) return;
+  if (threadIdx.x == 0) st->rTr_true = total;
 }
 
 // update_p: p = z + beta p (3D/mgpcg.py:147-150)
@@ -818,8 +820,8 @@ static int solve_impl(pfm_handle* h, const pfm_solve_opts& o, pfm_solve_stats* s
       launch(h, k_update_xr, red_blocks(n), kReduceThreads, 0, q, x, (const float*)p, r0, (const float*)Ap, n, rb, o.tol,
              o.tol_mode, f64, inv_n);
       if (true_res)
-        launch(h, k_true_residual<D>, red_blocks(n), kReduceThreads, 0, q, r0, (const float*)bvec, (const float*)x, L0,
-               bc, rb, o.tol, o.tol_mode, o.true_residual_every, inv_n);
+        launch(h, k_true_residual<D>, red_blocks(n), kReduceThreads, 0, q, (const float*)bvec, (const float*)x, L0, bc,
+               rb, o.true_residual_every);
     };
     auto setup = [&](cudaStream_t q) {
       // init(): x = p = Ap = 0 (3D/mgpcg.py:63-79); z0 is zeroed by the V-cycle
@@ -876,6 +878,9 @@ static int solve_impl(pfm_handle* h, const pfm_solve_opts& o, pfm_solve_stats* s
     if (!rc)
       rc = check_cuda(h, cudaStreamUpdateCaptureDependencies(cs, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies),
                       "capture dependencies");
+    if (!rc && true_res)  // the final true residual of the solve
+      launch(h, k_true_residual<D>, red_blocks(n), kReduceThreads, 0, cs, (const float*)bvec, (const float*)x, L0, bc,
+             rb, -1);
     if (!rc) cudaMemcpyAsync(hs, st, sizeof(SolveState), cudaMemcpyDeviceToHost, cs);
     cudaGraph_t top = nullptr;
     int rc_end = check_cuda(h, cudaStreamEndCapture(cs, &top), "end capture");
@@ -920,8 +925,9 @@ static int solve_impl(pfm_handle* h, const pfm_solve_opts& o, pfm_solve_stats* s
     if (rc) return rc;
     rc = check_cuda(h, cudaStreamSynchronize(s), "mgpcg sync");
     if (rc) return rc;
-    // kernels launched: k_loop_begin, one body per completed iteration, k_loop_cond inside
-    h->launches += 1 + (uint64_t)h->g_body_nodes * (uint64_t)(hs->it - it_before);
+    // kernels launched: k_loop_begin, one body per completed iteration (k_loop_cond inside), and
+    // the final true-residual check
+    h->launches += 1 + (uint64_t)h->g_body_nodes * (uint64_t)(hs->it - it_before) + (true_res ? 1 : 0);
     it_before = hs->it;
     if (hs->done || mi >= 0) break;
   }
@@ -931,6 +937,7 @@ static int solve_impl(pfm_handle* h, const pfm_solve_opts& o, pfm_solve_stats* s
     stats->rTr = hs->rTr;
     stats->rTr0 = hs->rTr0;
     stats->bTb = hs->bTb;
+    stats->rTr_true = true_res ? hs->rTr_true : -1.0;
   }
   if (hs->done == 3) return set_error(h, PFM_ERR_NONFINITE, "MGPCG: non-finite residual");
   if (hs->done != 1) return set_error(h, PFM_ERR_NOT_CONVERGED, "MGPCG: iteration limit reached");

@@ -35,7 +35,8 @@ class SolveOpts(ctypes.Structure):
 
 class SolveStats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("converged", ctypes.c_int), ("rTr", ctypes.c_double),
-                ("rTr0", ctypes.c_double), ("bTb", ctypes.c_double)]
+                ("rTr0", ctypes.c_double), ("bTb", ctypes.c_double),
+                ("rTr_true", ctypes.c_double)]
 
 
 # name -> argument types (all return int status unless listed in _RESTYPE)

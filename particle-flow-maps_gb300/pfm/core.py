@@ -24,6 +24,7 @@ class SolveInfo:
         self.rTr = float(stats.rTr)
         self.rTr0 = float(stats.rTr0)
         self.bTb = float(stats.bTb)
+        self.rTr_true = float(stats.rTr_true)
         self.status = status
 
     def __repr__(self):

@@ -61,7 +61,8 @@ int main(void) {
          offsetof(pfm_config, boundary), offsetof(pfm_config, use_apic));
   printf("%zu %zu %zu %zu\n", sizeof(pfm_solve_opts), offsetof(pfm_solve_opts, tol), offsetof(pfm_solve_opts, check_every),
          offsetof(pfm_solve_opts, true_residual_every));
-  printf("%zu %zu %zu\n", sizeof(pfm_solve_stats), offsetof(pfm_solve_stats, rTr0), offsetof(pfm_solve_stats, bTb));
+  printf("%zu %zu %zu %zu\n", sizeof(pfm_solve_stats), offsetof(pfm_solve_stats, rTr0), offsetof(pfm_solve_stats, bTb),
+         offsetof(pfm_solve_stats, rTr_true));
   return 0;
 }
 """
@@ -83,7 +84,7 @@ def test_struct_layouts_match_header():
     O = _lib.SolveOpts
     assert c[5:9] == [ctypes.sizeof(O), O.tol.offset, O.check_every.offset, O.true_residual_every.offset]
     S = _lib.SolveStats
-    assert c[9:12] == [ctypes.sizeof(S), S.rTr0.offset, S.bTb.offset]
+    assert c[9:13] == [ctypes.sizeof(S), S.rTr0.offset, S.bTb.offset, S.rTr_true.offset]
 
 
 def test_scene_fails_loudly_without_cuda():

@@ -64,7 +64,11 @@ def test_mixed_solve_against_fp64_oracle(ring64, precision):
     b = div3(ub)
     b -= b.mean()
     r = div3(got)
-    assert np.linalg.norm(r) <= 1e-4 * np.linalg.norm(b), (precision, np.linalg.norm(r) / np.linalg.norm(b))
+    true_rel = np.linalg.norm(r) / np.linalg.norm(b)
+    assert true_rel <= 1e-4, (precision, true_rel)
+    # the solver's own true-residual check (before subtract_grad_p) agrees with it
+    assert info.rTr_true >= 0
+    assert np.sqrt(info.rTr_true / info.bTb) == pytest.approx(true_rel, rel=0.25)
     print(f"{precision}: iterations {info.iterations}, velocity err {err_u:.2e}, pressure err {err_p:.2e}, "
           f"true residual {np.linalg.norm(r) / np.linalg.norm(b):.2e}")
 
