@@ -342,15 +342,17 @@ def main():
     F3 = 3 * (n + 1) * n * n
     peak, peak_kind = measured_peak()
     rk4_ms = statistics.mean(phases["rk4"])
-    # k_rk4_T_forward3 with the P2G records: pos + T_gm read and written (96 B), init_imp + T_init +
-    # init_C read (84 B), record (64 B) + key + slot (8 B) written per particle; the velocity grid once
-    rk4_bytes = P * (96 + 84 + 64 + 8) + F3 * 4
+    # k_rk4_T_forward3 with the gradient reinitialisation and the P2G records, per particle: pos read
+    # and written (24 B), T_gm read and written (72 B), T_init read and written (72 B), init_C
+    # written (36 B), init_imp read (12 B), record (64 B) + key + slot (8 B) written = 288 B; the
+    # pre-midpoint and midpoint velocity grids once each
+    rk4_bytes = P * 288 + 2 * F3 * 4
     achieved = rk4_bytes / (rk4_ms / 1e3) / 1e9
     # DRAM bytes of one launch: dram__bytes_read.sum + dram__bytes_write.sum of the ncu capture of
-    # k_rk4_T_forward3<true> at 128^3 (2,248,936,960 + 1,970,354,944 B for 16,777,216 particles,
-    # profiles/k_rk4_T_forward3_128.md), scaled by the particle count (the grid scales with it at a
-    # fixed particle density)
-    traffic = (2248936960 + 1970354944) / 16777216 * P
+    # k_rk4_T_forward3<true, true> at 128^3 (1,671,280,384 + 3,168,529,152 B for 16,777,216
+    # particles, profiles/k_rk4_T_forward3_128.md), scaled by the particle count (the grid scales
+    # with it at a fixed particle density)
+    traffic = (1671280384 + 3168529152) / 16777216 * P
     roofline = {"bound": "hbm", "kernel": "k_rk4_T_forward3", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                 "traffic_source": "ncu capture at 128^3 scaled by the particle count",

@@ -176,6 +176,18 @@ int pfm3_rk4_p2g_records(pfm_handle* h, float* pos, float* T_gm, const float* ua
                          const float* T_init, const float* init_C, void* stream);
 int pfm3_p2g_from_records(pfm_handle* h, float* u_x, float* u_y, float* u_z, float* w_x,
                           float* w_y, float* w_z, void* stream);
+
+/* pfm3_rk4_p2g_records preceded by the flow-map gradient reinitialisation of the step
+ * (3D/run_3D.py:768-772), in the same kernel: init_C <- grad u(pos) in the velocity u
+ * (init_particles_imp_grad_m), T_init <- cols(T_gm) @ cols(T_init) (update_T), T_gm <- I, then
+ * RK4 of pos/T_gm in ua over dt from the identity, and the P2G records.  Bitwise the same as
+ * pfm3_g2p(pos, u, NULL, init_C), pfm3_update_T(T_init, T_gm, 1) and
+ * pfm3_rk4_p2g_records(pos, T_gm, ua, dt, init_imp, T_init, init_C); the reinitialisation reads
+ * the same pos as the RK4, so it may run after the midpoint solve. */
+int pfm3_gradm_rk4_p2g_records(pfm_handle* h, float* pos, float* T_gm, float* T_init, float* init_C,
+                               const float* init_imp, const float* u_x, const float* u_y,
+                               const float* u_z, const float* ua_x, const float* ua_y,
+                               const float* ua_z, float dt, void* stream);
 int pfm3_rk4_p2g(pfm_handle* h, float* pos, float* T_gm, const float* ua_x, const float* ua_y,
                  const float* ua_z, float dt, const float* init_imp, const float* T_init,
                  const float* init_C, float* u_x, float* u_y, float* u_z, float* w_x, float* w_y,

@@ -379,9 +379,10 @@ __device__ __forceinline__ void write_p2g_record3(const P2GRecords3& R, int64_t 
 }
 
 // Launches RK4_T_forward (3D); with R non-null the kernel also writes the P2G records and keys
-// of the advected particles (defined in pfm_particles.cu).
+// of the advected particles, and with Fg non-null it first does the flow-map gradient
+// reinitialisation (init_C = grad u(p) in Fg, update_T, T_gm = I) (defined in pfm_particles.cu).
 int launch_rk4_T_forward3(pfm_handle* h, float* pos, float* T, const MacFields3& F, float dt, const P2GRecords3* R,
-                          cudaStream_t st);
+                          const MacFields3* Fg, cudaStream_t st);
 
 // ------------------------------------------------------------------------------------------
 // 2D (2D/taichi_utils.py:214-261)

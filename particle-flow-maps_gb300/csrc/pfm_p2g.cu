@@ -612,7 +612,29 @@ int pfm3_rk4_p2g_records(pfm_handle* h, float* pos, float* T_gm, const float* ua
   if (rc) return rc;
   const P2GRecords3 R = records3(h, init_imp, T_init, init_C);
   const MacFields3 F{{ua_x, ua_y, ua_z}};
-  rc = launch_rk4_T_forward3(h, pos, T_gm, F, dt, &R, st);
+  rc = launch_rk4_T_forward3(h, pos, T_gm, F, dt, &R, nullptr, st);
+  if (rc) return rc;
+  h->rec_valid = 1;
+  return PFM_OK;
+}
+
+int pfm3_gradm_rk4_p2g_records(pfm_handle* h, float* pos, float* T_gm, float* T_init, float* init_C,
+                               const float* init_imp, const float* u_x, const float* u_y, const float* u_z,
+                               const float* ua_x, const float* ua_y, const float* ua_z, float dt, void* stream) {
+  if (!h) return PFM_ERR_NULL;
+  if (h->cfg.dim != 3) return set_error(h, PFM_ERR_SHAPE, "pfm3_gradm_rk4_p2g_records on a 2D handle");
+  if (!u_x || !u_y || !u_z || !ua_x || !ua_y || !ua_z)
+    return set_error(h, PFM_ERR_NULL, "pfm3_gradm_rk4_p2g_records: null grid");
+  if (h->P > 0 && (!init_imp || !pos || !T_gm || !T_init || !init_C))
+    return set_error(h, PFM_ERR_NULL, "pfm3_gradm_rk4_p2g_records: null particle field");
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = require_ws(h);
+  if (rc) return rc;
+  rc = check_cuda(h, cudaMemsetAsync(ws_ptr<int>(h, h->o_count), 0, h->cells * 4, st), "memset counts");
+  if (rc) return rc;
+  const P2GRecords3 R = records3(h, init_imp, T_init, init_C);
+  const MacFields3 F{{ua_x, ua_y, ua_z}}, Fg{{u_x, u_y, u_z}};
+  rc = launch_rk4_T_forward3(h, pos, T_gm, F, dt, &R, &Fg, st);
   if (rc) return rc;
   h->rec_valid = 1;
   return PFM_OK;

@@ -76,18 +76,52 @@ __global__ void __launch_bounds__(256) k_reset_T(float* __restrict__ T, int64_t 
 // The stage sums (k1 + 2 k2 + 2 k3 + k4) accumulate in the reference's left-to-right order.
 // With PAY the kernel also writes the P2G record and cell key of the advected particle
 // (write_p2g_record3), the input of the P2G tiles that follow RK4_T_forward in the step.
-template <bool PAY>
+// With GRADM it first does the flow-map gradient reinitialisation of the step
+// (3D/run_3D.py:768-772): init_C rows = grad u(p) in the velocity Fg (init_particles_imp_grad_m,
+// as k_g2p3), T_init <- cols(T_gm) @ cols(T_init) (update_T, as k_update_T3) and T_gm <- I, so the
+// RK4 starts from the identity without reading T_gm back.
+template <bool PAY, bool GRADM>
 __global__ void __launch_bounds__(kPThreads, 4) k_rk4_T_forward3(float* __restrict__ pos, float* __restrict__ T,
                                                              int64_t P, MacFields3 F, MacGeom g, float dt,
-                                                             P2GRecords3 R) {
+                                                             P2GRecords3 R, MacFields3 Fg) {
   int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= P) return;
   float p0[3] = {pos[q], pos[P + q], pos[2 * P + q]};
   float T0[3][3];
+  if (GRADM) {
+    {
+      float ug[3], G[3][3];
+      interp_mac3(Fg, g, p0, ug, G, true);
+      float* C = const_cast<float*>(R.C);
 #pragma unroll
-  for (int v = 0; v < 3; ++v)
+      for (int c = 0; c < 3; ++c)
 #pragma unroll
-    for (int c = 0; c < 3; ++c) T0[v][c] = T[(v * 3 + c) * P + q];
+        for (int r = 0; r < 3; ++r) C[(c * 3 + r) * P + q] = G[c][r];
+    }
+    float* Ti = const_cast<float*>(R.Ti);
+    float M[3][3], N[3][3];
+#pragma unroll
+    for (int v = 0; v < 3; ++v)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        M[c][v] = T[(v * 3 + c) * P + q];   // M[r][k] = T_gm_k[r]
+        N[c][v] = Ti[(v * 3 + c) * P + q];  // N[k][c] = T_init_c[k]
+      }
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+        Ti[(c * 3 + r) * P + q] = M[r][0] * N[0][c] + M[r][1] * N[1][c] + M[r][2] * N[2][c];
+#pragma unroll
+    for (int v = 0; v < 3; ++v)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) T0[v][c] = (v == c) ? 1.f : 0.f;
+  } else {
+#pragma unroll
+    for (int v = 0; v < 3; ++v)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) T0[v][c] = T[(v * 3 + c) * P + q];
+  }
   float pk[3] = {p0[0], p0[1], p0[2]};
   float Tk[3][3];
 #pragma unroll
@@ -285,13 +319,16 @@ using namespace pfm;
 namespace pfm {
 
 int launch_rk4_T_forward3(pfm_handle* h, float* pos, float* T, const MacFields3& F, float dt, const P2GRecords3* R,
-                          cudaStream_t st) {
+                          const MacFields3* Fg, cudaStream_t st) {
   if (h->P == 0) return PFM_OK;
-  if (R)
-    launch(h, k_rk4_T_forward3<true>, grid_for(h->P, kPThreads), kPThreads, 0, st, pos, T, h->P, F, h->geom, dt, *R);
+  const unsigned nb = grid_for(h->P, kPThreads);
+  if (R && Fg)
+    launch(h, k_rk4_T_forward3<true, true>, nb, kPThreads, 0, st, pos, T, h->P, F, h->geom, dt, *R, *Fg);
+  else if (R)
+    launch(h, k_rk4_T_forward3<true, false>, nb, kPThreads, 0, st, pos, T, h->P, F, h->geom, dt, *R, MacFields3{});
   else
-    launch(h, k_rk4_T_forward3<false>, grid_for(h->P, kPThreads), kPThreads, 0, st, pos, T, h->P, F, h->geom, dt,
-           P2GRecords3{});
+    launch(h, k_rk4_T_forward3<false, false>, nb, kPThreads, 0, st, pos, T, h->P, F, h->geom, dt, P2GRecords3{},
+           MacFields3{});
   return launch_check(h, "k_rk4_T_forward3");
 }
 
@@ -335,7 +372,7 @@ int pfm3_rk4_T_forward(pfm_handle* h, float* pos, float* T, const float* u_x, co
   if (!pos || !T || !u_x || !u_y || !u_z) return set_error(h, PFM_ERR_NULL, "pfm3_rk4_T_forward: null input");
   if (h->P == 0) return PFM_OK;
   MacFields3 F{{u_x, u_y, u_z}};
-  return launch_rk4_T_forward3(h, pos, T, F, dt, nullptr, (cudaStream_t)stream);
+  return launch_rk4_T_forward3(h, pos, T, F, dt, nullptr, nullptr, (cudaStream_t)stream);
 }
 
 int pfm2_g2p(pfm_handle* h, const float* pos, const float* u_x, const float* u_y, float* imp_out,

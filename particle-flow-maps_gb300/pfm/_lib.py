@@ -66,6 +66,7 @@ SIGNATURES = {
     "pfm3_rk4_p2g": [_P, _P, _P, _P, _P, _P, _F, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "pfm3_rk4_p2g_records": [_P, _P, _P, _P, _P, _P, _F, _P, _P, _P, _P],
     "pfm3_p2g_from_records": [_P, _P, _P, _P, _P, _P, _P, _P],
+    "pfm3_gradm_rk4_p2g_records": [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _F, _P],
     "pfm3_poisson": [_P, _P, _P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats), _P],
     "pfm2_calc_max_speed": [_P, _P, _P, _P, _P],
     "pfm2_g2p": [_P, _P, _P, _P, _P, _P, _P],

@@ -262,6 +262,19 @@ class Scene:
         self._check(self.lib.pfm3_rk4_p2g_records(self.h, _ptr(pos), _ptr(T_gm), *map(_ptr, u_adv), ctypes.c_float(dt),
                                                   _ptr(init_imp), _ptr(T_init), _ptr(init_C), self._stream()))
 
+    def gradm_rk4_records3(self, pos, T_gm, T_init, init_C, init_imp, u, u_adv, dt):
+        """Gradient reinitialisation (init_C = grad u(pos), update_T, T_gm = I) + RK4 in u_adv + P2G
+        records in one kernel (bitwise g2p + update_T + rk4_p2g_records3)."""
+        self._part(pos, 3, "pos")
+        for t, n in ((T_gm, "T_gm"), (T_init, "T_init"), (init_C, "init_C")):
+            self._part(t, 3, n, vec=3)
+        self._part(init_imp, 3, "init_imp")
+        u = self._grids(u, "u")
+        u_adv = self._grids(u_adv, "u_adv")
+        self._check(self.lib.pfm3_gradm_rk4_p2g_records(self.h, _ptr(pos), _ptr(T_gm), _ptr(T_init), _ptr(init_C),
+                                                        _ptr(init_imp), *map(_ptr, u), *map(_ptr, u_adv),
+                                                        ctypes.c_float(dt), self._stream()))
+
     def p2g_from_records3(self, u_out, w_out):
         """The rest of P2G (bin sort, cell tiles, normalisation) from the records of
         rk4_p2g_records3 (second half of rk4_p2g3)."""

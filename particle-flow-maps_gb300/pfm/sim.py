@@ -118,7 +118,8 @@ class Sim3D:
     ``u``: the three face grids (numpy arrays or CUDA tensors); ``seeds``: reinit positions, AoS
     numpy [P, 3] or a device SoA tensor [3, P].  Pass ``timer`` (a callable taking a phase name and
     returning a context manager) to bracket the phases with CUDA events.  ``fused_rk4_p2g`` runs
-    RK4_T_forward and P2G as one library call (same results, particle state read once)."""
+    the step's particle work as one RK4 kernel (gradient reinitialisation, RK4, P2G records) and
+    the P2G tiles (the same results as the separate calls, particle state read once)."""
 
     def __init__(self, u, seeds, res, dx, CFL=0.5, visualize_dt=0.1, reinit_every=20,
                  reinit_every_grad_m=1, use_midpoint_vel=True, reinit_particle_pos=True, use_apic=True,
@@ -180,7 +181,9 @@ class Sim3D:
                 sc.reset_T(self.T_init)
                 sc.reset_T(self.T_gm)
         k = (i - self.ik) % self.grad_m
-        if k == 0:
+        # with fused_rk4_p2g the gradient reinitialisation runs inside the RK4 kernel after the
+        # midpoint solve (it reads the same positions and the pre-midpoint velocity)
+        if k == 0 and not self.fused_rk4_p2g:
             with self._t("g2p"):
                 sc.g2p(self.pos, self.u, C_out=self.init_C)
             with self._t("update_T"):
@@ -194,8 +197,12 @@ class Sim3D:
             adv = self.u_mid
         if self.fused_rk4_p2g:
             with self._t("rk4"):
-                sc.rk4_p2g_records3(self.pos, self.T_gm, adv, float(np.float32(curr_dt)), self.init_imp, self.T_init,
-                                    self.init_C)
+                if k == 0:
+                    sc.gradm_rk4_records3(self.pos, self.T_gm, self.T_init, self.init_C, self.init_imp, self.u, adv,
+                                          float(np.float32(curr_dt)))
+                else:
+                    sc.rk4_p2g_records3(self.pos, self.T_gm, adv, float(np.float32(curr_dt)), self.init_imp,
+                                        self.T_init, self.init_C)
             with self._t("p2g"):
                 sc.p2g_from_records3(self.u, self.w)
         else:

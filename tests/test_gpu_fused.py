@@ -62,3 +62,26 @@ def test_p2g_from_records_needs_records():
     sc.sort_particles(st["pos"])  # overwrites the keys of the records
     with pytest.raises(pfm.PfmError, match="no P2G records"):
         sc.p2g_from_records3(out, w)
+
+
+def test_gradm_rk4_records_matches_separate_calls():
+    """g2p(C) + update_T(reset) + rk4_p2g_records + p2g_from_records against the fused gradient
+    reinitialisation kernel: bitwise equal particle state and grids."""
+    sc, u, st = _scene(seed=7)
+    rng = np.random.default_rng(9)
+    ua = [torch.from_numpy((0.3 * rng.standard_normal(s)).astype(np.float32)).cuda() for s in sc.face_shapes]
+    dt = 0.01
+    a, b = _clone(st), _clone(st)
+    wa, wb = sc.alloc_faces(), sc.alloc_faces()
+    oa, ob = sc.alloc_faces(), sc.alloc_faces()
+    sc.g2p(a["pos"], u, C_out=a["init_C"])
+    sc.update_T(a["T_init"], a["T_gm"], reset_gm=True)
+    sc.rk4_p2g_records3(a["pos"], a["T_gm"], ua, dt, a["init_imp"], a["T_init"], a["init_C"])
+    sc.p2g_from_records3(oa, wa)
+    sc.gradm_rk4_records3(b["pos"], b["T_gm"], b["T_init"], b["init_C"], b["init_imp"], u, ua, dt)
+    sc.p2g_from_records3(ob, wb)
+    torch.cuda.synchronize()
+    for k in ("pos", "T_gm", "T_init", "init_C"):
+        assert torch.equal(a[k], b[k]), k
+    for f in range(3):
+        assert torch.equal(oa[f], ob[f]) and torch.equal(wa[f], wb[f]), f
