@@ -221,7 +221,7 @@ __device__ __forceinline__ void interp_mac3(const MacFields3& F, const MacGeom& 
   Axis3 A0[3], A1[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    float u = p[a] / g.dx;
+    float u = p[a] * g.inv_dx;  // = p / dx exactly when dx is a power of two
     axis_taps(u - 0.0f, g.hi[a][a], A0[a]);            // the component along a
     axis_taps(u - 0.5f, g.hi[(a + 1) % 3][a], A1[a]);  // the others
   }
@@ -415,7 +415,7 @@ __device__ __forceinline__ void interp_mac2(const MacFields2& F, const MacGeom& 
   Axis3 A0[2], A1[2];
 #pragma unroll
   for (int a = 0; a < 2; ++a) {
-    float u = p[a] / g.dx;
+    float u = p[a] * g.inv_dx;  // = p / dx exactly when dx is a power of two
     axis_taps(u - 0.0f, g.hi[a][a], A0[a]);
     axis_taps(u - 0.5f, g.hi[1 - a][a], A1[a]);
   }
