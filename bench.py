@@ -80,6 +80,8 @@ def make_sim(res, ppc_axis, poisson_opts, device="cuda"):
     sc.split_central_vector(vc, sim.u)
     del vc
     sc.poisson(sim.u, sim.p, **poisson_opts)  # split_central_vector + Poisson (run_3D.py:667-670); p starts at 0
+    # the set-up projection's pressure answers a different problem: warm starts begin at the first step
+    sim.p.zero_()
     torch.cuda.synchronize()
     return sim
 
