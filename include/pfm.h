@@ -250,7 +250,84 @@ int pfm2_p2g(pfm_handle* h, const float* imp, const float* pos, const float* C, 
 int pfm2_poisson(pfm_handle* h, float* u_x, float* u_y, float* p_out, const pfm_solve_opts* opts,
                  pfm_solve_stats* stats, void* stream);
 
+/* ---- the reference's alternative ("evolve m") dataflow ---------------------------------------
+ * Kernels the reference defines beside its live step (their call sites in 3D/run_3D.py:795-808
+ * are commented out).  grad_T_init is the three per-particle 3x3 matrices grad_T_init_x/y/z as
+ * [3 (row vector r)][3][3][P]. */
+
+/* RK4_T_and_T_grad_m_forward (3D/run_3D.py:221-292): RK4 of pos [3][P] and of two Jacobian sets
+ * T and T_grad_m ([3][3][P] each, must not alias) with the same velocity gradient; in place. */
+int pfm3_rk4_T_and_T_grad_m_forward(pfm_handle* h, float* pos, float* T, float* T_grad_m, const float* u_x,
+                                    const float* u_y, const float* u_z, float dt, void* stream);
+/* update_particles_imp (3D/run_3D.py:395-401): imp = cols(T) @ init_imp. */
+int pfm3_update_imp(pfm_handle* h, float* imp, const float* init_imp, const float* T, void* stream);
+/* update_particles_grad_m (3D/run_3D.py:412-428): C_r = grad_T_init_r @ init_imp + (T^T init_C T)_r
+ * with T = rows(T) ([3][3][P]); grad_T_init may be NULL (zero). */
+int pfm3_update_grad_m(pfm_handle* h, float* C, const float* init_C, const float* T, const float* grad_T_init,
+                       const float* init_imp, void* stream);
+/* compute_dT_dx (3D/run_3D.py:353-390): grad_T_init of every particle from the particles in the
+ * 4x4x4 cells around its initial position init_pos, using the cell lists of the current positions
+ * pos (get_particles_id_in_every_cell, at most cap particles per cell in particle-index order) and
+ * the neighbours' T ([3][3][P]).  Distances are in world units, as the reference writes them.
+ * Neighbour cells outside the grid are skipped (the reference reads outside its fields there). */
+int pfm3_compute_dT_dx(pfm_handle* h, const float* pos, const float* init_pos, const float* T, int cap,
+                       float* grad_T_init, void* stream);
+
+/* ---- scalar (smoke) transport ---------------------------------------------------------------
+ * The smoke grid is cell-centred AoS like the reference's ti.Vector.field(4, float, shape=res):
+ * smoke [nx][ny][nz][4] f32 (3D, 16-byte aligned), [nx][ny][3] (2D).  Particle smoke is SoA:
+ * smoke_p [4][P]; the per-particle 3x4 smoke gradient is [3][4][P] (row r = d/dx_r, column = channel).
+ * psi_x/psi_y/psi_z are the backward-map face grids [F][3] (3D) / [F][2] (2D) that pfm3_midpoint /
+ * pfm2_midpoint write through psi_out. */
+
+/* init_particles_smoke (3D/init_conditions.py:275-279) via interp_u_MAC_smoke / interp_grad_2_smoke
+ * (3D/taichi_utils.py:379-428): smoke value and gradient at the particle positions pos [3][P].
+ * smoke_p and grad_smoke may be NULL. */
+int pfm3_init_particles_smoke(pfm_handle* h, const float* pos, const float* smoke, float* smoke_p,
+                              float* grad_smoke, void* stream);
+
+/* P2G_smoke (3D/run_3D.py:554-593): APIC transfer of the particle smoke with the affine term
+ * dpos . ((cols(T_gm) @ cols(T_init)) @ init_grad_smoke) when use_apic_smoke is nonzero
+ * (hyperparameters.use_APIC_smoke), normalised by the weight sums (weight [nx][ny][nz]) and clamped
+ * to [0, 1] where the weight is positive.  Deterministic (bin sort + cell tiles, no float atomics).
+ * Overwrites the P2G records of pfm3_rk4_p2g_records in the workspace. */
+int pfm3_p2g_smoke(pfm_handle* h, const float* smoke_p, const float* init_grad_smoke, const float* pos,
+                   const float* T_gm, const float* T_init, int use_apic_smoke, float* smoke, float* weight,
+                   void* stream);
+
+/* advect_smoke (3D/run_3D.py:315-323): smoke1 = trilinear interp_1 of smoke0 at the cell-centre
+ * average of the six face backward maps; clamp_smoke (3D/run_3D.py:326-334): clamps smoke1 to the
+ * min/max of the eight smoke0 corners there.  dx is the reference's kernel argument. */
+int pfm3_advect_smoke(pfm_handle* h, const float* smoke0, float* smoke1, const float* psi_x,
+                      const float* psi_y, const float* psi_z, float dx, void* stream);
+int pfm3_clamp_smoke(pfm_handle* h, const float* smoke0, float* smoke1, const float* psi_x,
+                     const float* psi_y, const float* psi_z, float dx, void* stream);
+/* advect_smoke (2D/run_2D.py:444-450), 3-channel smoke. */
+int pfm2_advect_smoke(pfm_handle* h, const float* smoke0, float* smoke1, const float* psi_x,
+                      const float* psi_y, float dx, void* stream);
+
+/* ---- diagnostics ------------------------------------------------------------------------------ */
+
+/* get_central_vector (3D/taichi_utils.py:80-85): vc [nx][ny][nz][3] = face averages. */
+int pfm3_get_central_vector(pfm_handle* h, const float* u_x, const float* u_y, const float* u_z, float* vc,
+                            void* stream);
+/* curl (3D/taichi_utils.py:56-78): w [nx][ny][nz][3], central differences of vc with clamped
+ * neighbours and 1/(2 dx). */
+int pfm3_curl(pfm_handle* h, const float* vc, float* w, float dx, void* stream);
+/* get_central_vector (2D/taichi_utils.py:50-55): vc [nx][ny][2]. */
+int pfm2_get_central_vector(pfm_handle* h, const float* u_x, const float* u_y, float* vc, void* stream);
+/* curl (2D/taichi_utils.py:96-104): scalar vorticity w [nx][ny]. */
+int pfm2_curl(pfm_handle* h, const float* vc, float* w, float dx, void* stream);
+
 /* ---- initial conditions --------------------------------------------------------------------- */
+
+/* add_vortex_ring_and_smoke (3D/init_conditions.py:29-56): adds the ring's velocity to vc (as
+ * pfm3_add_vortex_ring) and its marker sum(curve_length * exp(-(r/delta)^3)) to smoke[..][3], then
+ * sets every cell whose marker exceeds 0.002 to (color, 1) and every other cell to 0.
+ * smoke [nx][ny][nz][4], 16-byte aligned; c/unit_x/unit_y/color are host arrays. */
+int pfm3_add_vortex_ring_and_smoke(pfm_handle* h, float w, float rad, float delta, const float c[3],
+                                   const float unit_x[3], const float unit_y[3], const float color[3],
+                                   int num_samples, float* vc, float* smoke, void* stream);
 
 /* add_vortex_ring (3D/init_conditions.py:10-22): adds the Biot-Savart velocity of a ring of
  * strength w, radius rad and core delta (mollifier 1-exp(-(r/delta)^3)) centred at c in the plane

@@ -157,6 +157,111 @@ def poisson3(ux, uy, uz, base_level=3, boundary=(2, 2, 2, 2, 2, 2), levels=0, ma
 
 
 # ------------------------------------------------------------------------------------------------
+# scalar (smoke) transport and diagnostics (Taichi layouts: smoke [nx, ny, nz, 4], particle smoke
+# [P, 4], smoke gradient [P, 3, 4], psi grids [F, 3])
+# ------------------------------------------------------------------------------------------------
+def central_vector3(ux, uy, uz):
+    nx, ny, nz = uy.shape[0], ux.shape[1], ux.shape[2]
+    vc = np.zeros((nx, ny, nz, 3), np.float32)
+    lib().oracle3_central_vector(_p(f32(ux)), _p(f32(uy)), _p(f32(uz)), nx, ny, nz, _p(vc))
+    return vc
+
+
+def curl3(vc, dx):
+    vc = f32(vc)
+    w = np.zeros_like(vc)
+    lib().oracle3_curl(_p(vc), vc.shape[0], vc.shape[1], vc.shape[2], _cf(np.float32(dx)), _p(w))
+    return w
+
+
+def central_vector2(ux, uy):
+    nx, ny = uy.shape[0], ux.shape[1]
+    vc = np.zeros((nx, ny, 2), np.float32)
+    lib().oracle2_central_vector(_p(f32(ux)), _p(f32(uy)), nx, ny, _p(vc))
+    return vc
+
+
+def curl2(vc, dx):
+    vc = f32(vc)
+    w = np.zeros(vc.shape[:2], np.float32)
+    lib().oracle2_curl(_p(vc), vc.shape[0], vc.shape[1], _cf(np.float32(dx)), _p(w))
+    return w
+
+
+def init_particles_smoke3(pos, smoke, dx):
+    pos, smoke = f32(pos), f32(smoke)
+    P = pos.shape[0]
+    s = np.zeros((P, 4), np.float32)
+    G = np.zeros((P, 3, 4), np.float32)
+    lib().oracle3_init_particles_smoke(_p(pos), P, _p(smoke), smoke.shape[0], smoke.shape[1], smoke.shape[2],
+                                       _cf(np.float32(dx)), _p(s), _p(G))
+    return s, G
+
+
+def p2g_smoke3(s, G, pos, T_gm, T_init, res, dx, use_apic=True):
+    nx, ny, nz = (int(r) for r in res)
+    smoke = np.zeros((nx, ny, nz, 4), np.float32)
+    w = np.zeros((nx, ny, nz), np.float32)
+    pos = f32(pos)
+    lib().oracle3_p2g_smoke(_p(f32(s)), _p(f32(G)), _p(pos), _p(f32(T_gm)), _p(f32(T_init)), pos.shape[0],
+                            _p(smoke), _p(w), nx, ny, nz, _cd(dx), int(use_apic))
+    return smoke, w
+
+
+def advect_smoke3(smoke0, smoke1, psi_x, psi_y, psi_z, dx, clamp=False):
+    """advect_smoke (clamp False) / clamp_smoke (clamp True) on a copy of smoke1."""
+    s0 = f32(smoke0)
+    s1 = f32(smoke1).copy()
+    nx, ny, nz = s0.shape[:3]
+    lib().oracle3_advect_smoke(_p(s0), _p(s1), _p(f32(psi_x)), _p(f32(psi_y)), _p(f32(psi_z)), nx, ny, nz,
+                               _cf(np.float32(dx)), int(bool(clamp)))
+    return s1
+
+
+def advect_smoke2(smoke0, psi_x, psi_y, dx):
+    s0 = f32(smoke0)
+    s1 = np.zeros_like(s0)
+    lib().oracle2_advect_smoke(_p(s0), _p(s1), _p(f32(psi_x)), _p(f32(psi_y)), s0.shape[0], s0.shape[1],
+                               _cf(np.float32(dx)))
+    return s1
+
+
+# ------------------------------------------------------------------------------------------------
+# the alternative ("evolve m") dataflow
+# ------------------------------------------------------------------------------------------------
+def rk4_T_and_T_grad_m_forward3(pos, T, T2, ux, uy, uz, dx, dt):
+    pos, T, T2 = f32(pos).copy(), f32(T).copy(), f32(T2).copy()
+    nx, ny, nz = uy.shape[0], ux.shape[1], ux.shape[2]
+    lib().oracle3_rk4_T_and_T_grad_m_forward(_p(pos), _p(T), _p(T2), pos.shape[0], _p(f32(ux)), _p(f32(uy)),
+                                             _p(f32(uz)), nx, ny, nz, _cd(dx), _cf(np.float32(dt)))
+    return pos, T, T2
+
+
+def update_imp3(imp0, T):
+    imp0 = f32(imp0)
+    out = np.zeros_like(imp0)
+    lib().oracle3_update_imp(_p(out), _p(imp0), _p(f32(T)), imp0.shape[0])
+    return out
+
+
+def update_grad_m3(C0, T, gT, imp0):
+    C0 = f32(C0)
+    out = np.zeros_like(C0)
+    lib().oracle3_update_grad_m(_p(out), _p(C0), _p(f32(T)), _p(None if gT is None else f32(gT)), _p(f32(imp0)),
+                                C0.shape[0])
+    return out
+
+
+def compute_dT_dx3(pos, pos0, T, res, dx, cap):
+    pos = f32(pos)
+    P = pos.shape[0]
+    gT = np.zeros((P, 3, 3, 3), np.float32)
+    lib().oracle3_compute_dT_dx(_p(pos), _p(f32(pos0)), _p(f32(T)), P, int(res[0]), int(res[1]), int(res[2]),
+                                _cd(dx), int(cap), _p(gT))
+    return gT
+
+
+# ------------------------------------------------------------------------------------------------
 # 2D kernels
 # ------------------------------------------------------------------------------------------------
 def calc_max_speed2(ux, uy):

@@ -1121,4 +1121,374 @@ int oracle2_poisson_f64(double* ux, double* uy, double* p_out, const int* N, int
   return poisson2<double>(ux, uy, p_out, N, base_level, bt, levels, max_iters, tol, final_rTr, tol_mode);
 }
 
+// ------------------------------------------------------------------------------------------------
+// scalar (smoke) transport and diagnostics
+// ------------------------------------------------------------------------------------------------
+
+// get_central_vector (3D/taichi_utils.py:80-85): vc [nx][ny][nz][3]
+void oracle3_central_vector(const float* ux, const float* uy, const float* uz, int nx, int ny, int nz, float* vc) {
+  for (int i = 0; i < nx; ++i)
+    for (int j = 0; j < ny; ++j)
+      for (int k = 0; k < nz; ++k) {
+        size_t e = ((size_t)i * ny + j) * nz + k;
+        vc[e * 3 + 0] = 0.5f * (ux[((size_t)(i + 1) * ny + j) * nz + k] + ux[((size_t)i * ny + j) * nz + k]);
+        vc[e * 3 + 1] = 0.5f * (uy[((size_t)i * (ny + 1) + j + 1) * nz + k] + uy[((size_t)i * (ny + 1) + j) * nz + k]);
+        vc[e * 3 + 2] = 0.5f * (uz[((size_t)i * ny + j) * (nz + 1) + k + 1] + uz[((size_t)i * ny + j) * (nz + 1) + k]);
+      }
+}
+
+// curl (3D/taichi_utils.py:56-78): w [nx][ny][nz][3]; sample() clamps the neighbour indices.
+void oracle3_curl(const float* vc, int nx, int ny, int nz, float dx, float* w) {
+  const float inv_dist = 1.0f / (2.0f * dx);
+  auto at = [&](int i, int j, int k, int c) {
+    i = clampi(i, 0, nx - 1); j = clampi(j, 0, ny - 1); k = clampi(k, 0, nz - 1);
+    return vc[(((size_t)i * ny + j) * nz + k) * 3 + c];
+  };
+  for (int i = 0; i < nx; ++i)
+    for (int j = 0; j < ny; ++j)
+      for (int k = 0; k < nz; ++k) {
+        float d_vx_dz = inv_dist * (at(i, j, k + 1, 0) - at(i, j, k - 1, 0));
+        float d_vx_dy = inv_dist * (at(i, j + 1, k, 0) - at(i, j - 1, k, 0));
+        float d_vy_dx = inv_dist * (at(i + 1, j, k, 1) - at(i - 1, j, k, 1));
+        float d_vy_dz = inv_dist * (at(i, j, k + 1, 1) - at(i, j, k - 1, 1));
+        float d_vz_dx = inv_dist * (at(i + 1, j, k, 2) - at(i - 1, j, k, 2));
+        float d_vz_dy = inv_dist * (at(i, j + 1, k, 2) - at(i, j - 1, k, 2));
+        size_t e = ((size_t)i * ny + j) * nz + k;
+        w[e * 3 + 0] = d_vz_dy - d_vy_dz;
+        w[e * 3 + 1] = d_vx_dz - d_vz_dx;
+        w[e * 3 + 2] = d_vy_dx - d_vx_dy;
+      }
+}
+
+// get_central_vector (2D/taichi_utils.py:50-55): vc [nx][ny][2]
+void oracle2_central_vector(const float* ux, const float* uy, int nx, int ny, float* vc) {
+  for (int i = 0; i < nx; ++i)
+    for (int j = 0; j < ny; ++j) {
+      size_t e = (size_t)i * ny + j;
+      vc[e * 2 + 0] = 0.5f * (ux[(size_t)(i + 1) * ny + j] + ux[(size_t)i * ny + j]);
+      vc[e * 2 + 1] = 0.5f * (uy[(size_t)i * (ny + 1) + j + 1] + uy[(size_t)i * (ny + 1) + j]);
+    }
+}
+
+// curl (2D/taichi_utils.py:96-104): w [nx][ny] = (vr.y - vl.y - vt.x + vb.x) / (2 dx)
+void oracle2_curl(const float* vc, int nx, int ny, float dx, float* w) {
+  auto at = [&](int i, int j, int c) {
+    i = clampi(i, 0, nx - 1); j = clampi(j, 0, ny - 1);
+    return vc[((size_t)i * ny + j) * 2 + c];
+  };
+  for (int i = 0; i < nx; ++i)
+    for (int j = 0; j < ny; ++j)
+      w[(size_t)i * ny + j] = (at(i + 1, j, 1) - at(i - 1, j, 1) - at(i, j + 1, 0) + at(i, j - 1, 0)) / (2.0f * dx);
+}
+
+// init_particles_smoke (3D/init_conditions.py:275-279) with interp_grad_2_smoke
+// (3D/taichi_utils.py:379-420), BL = 0.5.  smoke [nx][ny][nz][4]; s_out [P][4]; grad_out [P][3][4].
+void oracle3_init_particles_smoke(const float* pos, int P, const float* smoke, int nx, int ny, int nz, float dx,
+                                  float* s_out, float* grad_out) {
+  const int n[3] = {nx, ny, nz};
+#pragma omp parallel for schedule(static)
+  for (int q = 0; q < P; ++q) {
+    float u[3], st[3], iu[3];
+    for (int a = 0; a < 3; ++a) {
+      u[a] = pos[(size_t)q * 3 + a] / dx;
+      u[a] = u[a] - 0.5f;
+      st[a] = std::max(1.0f, std::min(u[a], float(n[a] - 2 - kEps)));
+      iu[a] = std::floor(st[a]);
+    }
+    const float inv = 1.0f / dx;
+    float val[4] = {0, 0, 0, 0}, C[3][4] = {{0}};
+    for (int i = -1; i < 3; ++i)
+      for (int j = -1; j < 3; ++j)
+        for (int k = -1; k < 3; ++k) {
+          float xi = st[0] - (iu[0] + float(i)), yj = st[1] - (iu[1] + float(j)), zk = st[2] - (iu[2] + float(k));
+          int ci = clampi((int)(iu[0] + float(i)), 0, nx - 1), cj = clampi((int)(iu[1] + float(j)), 0, ny - 1),
+              ck = clampi((int)(iu[2] + float(k)), 0, nz - 1);
+          const float* v = smoke + (((size_t)ci * ny + cj) * nz + ck) * 4;
+          float dw[3] = {inv * dN2(xi) * N2(yj) * N2(zk), inv * N2(xi) * dN2(yj) * N2(zk),
+                         inv * N2(xi) * N2(yj) * dN2(zk)};
+          for (int ch = 0; ch < 4; ++ch) {
+            val[ch] += v[ch] * N2(xi) * N2(yj) * N2(zk);
+            for (int r = 0; r < 3; ++r) C[r][ch] += dw[r] * v[ch];
+          }
+        }
+    for (int ch = 0; ch < 4; ++ch) {
+      if (s_out) s_out[(size_t)q * 4 + ch] = val[ch];
+      if (grad_out)
+        for (int r = 0; r < 3; ++r) grad_out[(size_t)q * 12 + r * 4 + ch] = C[r][ch];
+    }
+  }
+}
+
+// P2G_smoke (3D/run_3D.py:554-593), particles scattered in index order.  s [P][4],
+// G = init_grad_smoke [P][3][4], T_gm/T_init [P][3][3] (x, y, z vectors); smoke [nx][ny][nz][4],
+// w [nx][ny][nz].
+void oracle3_p2g_smoke(const float* s, const float* G, const float* pos, const float* T_gm, const float* T_init, int P,
+                       float* smoke, float* w, int nx, int ny, int nz, double dx, int use_apic) {
+  const size_t C = (size_t)nx * ny * nz;
+  std::fill(smoke, smoke + C * 4, 0.f);
+  std::fill(w, w + C, 0.f);
+  const float dxr = float(dx);
+  for (int q = 0; q < P; ++q) {
+    float AT[3][3], Tin[3][3], TT[3][3];
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) {
+        AT[r][c] = T_gm[(size_t)q * 9 + c * 3 + r];   // cols(T_gm)
+        Tin[r][c] = T_init[(size_t)q * 9 + c * 3 + r]; // cols(T_init)
+      }
+    matmul3(AT, Tin, TT);
+    float M[3][4];
+    for (int r = 0; r < 3; ++r)
+      for (int ch = 0; ch < 4; ++ch)
+        M[r][ch] = TT[r][0] * G[(size_t)q * 12 + 0 * 4 + ch] + TT[r][1] * G[(size_t)q * 12 + 1 * 4 + ch] +
+                   TT[r][2] * G[(size_t)q * 12 + 2 * 4 + ch];
+    float p[3] = {pos[(size_t)q * 3] / dxr, pos[(size_t)q * 3 + 1] / dxr, pos[(size_t)q * 3 + 2] / dxr};
+    int base[3] = {(int)(p[0] - 0.5f), (int)(p[1] - 0.5f), (int)(p[2] - 0.5f)};
+    for (int oi = -1; oi < 3; ++oi)
+      for (int oj = -1; oj < 3; ++oj)
+        for (int ok = -1; ok < 3; ++ok) {
+          int f[3] = {base[0] + oi, base[1] + oj, base[2] + ok};
+          if (!(0 <= f[0] && f[0] < nx && 0 <= f[1] && f[1] < ny && 0 <= f[2] && f[2] < nz)) continue;
+          float weight = N2((p[0] - float(f[0])) - 0.5f) * N2((p[1] - float(f[1])) - 0.5f) *
+                         N2((p[2] - float(f[2])) - 0.5f);
+          float dp[3];
+          for (int d = 0; d < 3; ++d) dp[d] = ((float(f[d]) + 0.5f) - p[d]) * dxr;
+          size_t id = ((size_t)f[0] * ny + f[1]) * nz + f[2];
+          w[id] += weight;
+          for (int ch = 0; ch < 4; ++ch) {
+            float delta = dp[0] * M[0][ch] + dp[1] * M[1][ch] + dp[2] * M[2][ch];
+            float v = s[(size_t)q * 4 + ch];
+            smoke[id * 4 + ch] += (use_apic ? (v + delta) : v) * weight;
+          }
+        }
+  }
+  for (size_t e = 0; e < C; ++e)
+    if (w[e] > 0) {
+      for (int ch = 0; ch < 4; ++ch) {
+        float x = smoke[e * 4 + ch] / w[e];
+        if (x < 0.f) x = 0.f;
+        if (x > 1.f) x = 1.f;
+        smoke[e * 4 + ch] = x;
+      }
+    }
+}
+
+// advect_smoke (clamp = 0) / clamp_smoke (clamp = 1): 3D/run_3D.py:315-334 with interp_1 /
+// sample_min_max_1 (3D/taichi_utils.py:192-250).  smoke [nx][ny][nz][4], psi grids [F][3].
+void oracle3_advect_smoke(const float* s0, float* s1, const float* px, const float* py, const float* pz, int nx,
+                          int ny, int nz, float dx, int clamp) {
+  const int n[3] = {nx, ny, nz};
+  const float sixth = float(1.0 / 6.0);
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < nx; ++i)
+    for (int j = 0; j < ny; ++j)
+      for (int k = 0; k < nz; ++k) {
+        const float* a = px + (((size_t)i * ny + j) * nz + k) * 3;
+        const float* b = px + (((size_t)(i + 1) * ny + j) * nz + k) * 3;
+        const float* c = py + (((size_t)i * (ny + 1) + j) * nz + k) * 3;
+        const float* d = py + (((size_t)i * (ny + 1) + j + 1) * nz + k) * 3;
+        const float* e = pz + (((size_t)i * ny + j) * (nz + 1) + k) * 3;
+        const float* f = pz + (((size_t)i * ny + j) * (nz + 1) + k + 1) * 3;
+        float st[3], iu[3];
+        for (int t = 0; t < 3; ++t) {
+          float pc = sixth * (a[t] + b[t] + c[t] + d[t] + e[t] + f[t]);
+          float u = pc / dx;
+          u = u - 0.5f;
+          st[t] = std::max(1.0f, std::min(u, float(n[t] - 1 - kEps)));
+          iu[t] = std::floor(st[t]);
+        }
+        auto at = [&](float fi, float fj, float fk) {
+          int ci = clampi((int)fi, 0, nx - 1), cj = clampi((int)fj, 0, ny - 1), ck = clampi((int)fk, 0, nz - 1);
+          return s0 + (((size_t)ci * ny + cj) * nz + ck) * 4;
+        };
+        float* out = s1 + (((size_t)i * ny + j) * nz + k) * 4;
+        if (!clamp) {
+          const float* v0 = at(iu[0], iu[1], iu[2]);
+          float acc[4];
+          for (int ch = 0; ch < 4; ++ch) acc[ch] = 0.f * v0[ch];
+          for (int a2 = 0; a2 < 2; ++a2)
+            for (int b2 = 0; b2 < 2; ++b2)
+              for (int c2 = 0; c2 < 2; ++c2) {
+                float x = st[0] - (iu[0] + float(a2)), y = st[1] - (iu[1] + float(b2)), z = st[2] - (iu[2] + float(c2));
+                const float* v = at(iu[0] + float(a2), iu[1] + float(b2), iu[2] + float(c2));
+                float nxw = 1.0f - std::fabs(x), nyw = 1.0f - std::fabs(y), nzw = 1.0f - std::fabs(z);
+                for (int ch = 0; ch < 4; ++ch) acc[ch] += v[ch] * nxw * nyw * nzw;
+              }
+          for (int ch = 0; ch < 4; ++ch) out[ch] = acc[ch];
+        } else {
+          const float* v0 = at(iu[0], iu[1], iu[2]);
+          float mn[4], mx[4];
+          for (int ch = 0; ch < 4; ++ch) mn[ch] = mx[ch] = v0[ch];
+          for (int a2 = 0; a2 < 2; ++a2)
+            for (int b2 = 0; b2 < 2; ++b2)
+              for (int c2 = 0; c2 < 2; ++c2) {
+                const float* v = at(iu[0] + float(a2), iu[1] + float(b2), iu[2] + float(c2));
+                for (int ch = 0; ch < 4; ++ch) {
+                  mn[ch] = std::min(mn[ch], v[ch]);
+                  mx[ch] = std::max(mx[ch], v[ch]);
+                }
+              }
+          for (int ch = 0; ch < 4; ++ch) out[ch] = std::min(std::max(out[ch], mn[ch]), mx[ch]);
+        }
+      }
+}
+
+// advect_smoke (2D/run_2D.py:444-450) with interp_1 (2D/taichi_utils.py:118-143).  smoke [nx][ny][3],
+// psi grids [F][2].
+void oracle2_advect_smoke(const float* s0, float* s1, const float* px, const float* py, int nx, int ny, float dx) {
+  const int n[2] = {nx, ny};
+  for (int i = 0; i < nx; ++i)
+    for (int j = 0; j < ny; ++j) {
+      const float* a = px + ((size_t)i * ny + j) * 2;
+      const float* b = px + ((size_t)(i + 1) * ny + j) * 2;
+      const float* c = py + ((size_t)i * (ny + 1) + j) * 2;
+      const float* d = py + ((size_t)i * (ny + 1) + j + 1) * 2;
+      float st[2], iu[2];
+      for (int t = 0; t < 2; ++t) {
+        float pc = 0.25f * (a[t] + b[t] + c[t] + d[t]);
+        float u = pc / dx;
+        u = u - 0.5f;
+        st[t] = std::max(0.0f, std::min(u, float(n[t] - 1 - kEps)));
+        iu[t] = std::floor(st[t]);
+      }
+      float fu = st[0] - iu[0], fv = st[1] - iu[1];
+      auto at = [&](float fi, float fj) {
+        int ci = clampi((int)fi, 0, nx - 1), cj = clampi((int)fj, 0, ny - 1);
+        return s0 + ((size_t)ci * ny + cj) * 3;
+      };
+      const float *va = at(iu[0], iu[1]), *vb = at(iu[0] + 1, iu[1]), *vc = at(iu[0], iu[1] + 1),
+                  *vd = at(iu[0] + 1, iu[1] + 1);
+      auto N1 = [](float x) { return 1.0f - std::fabs(x); };
+      for (int ch = 0; ch < 3; ++ch)
+        s1[((size_t)i * ny + j) * 3 + ch] = va[ch] * N1(fu) * N1(fv) + vb[ch] * N1(fu - 1) * N1(fv) +
+                                            vc[ch] * N1(fu) * N1(fv - 1) + vd[ch] * N1(fu - 1) * N1(fv - 1);
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// the alternative ("evolve m") dataflow: kernels the live step does not call
+// ------------------------------------------------------------------------------------------------
+
+// RK4_T_and_T_grad_m_forward: 3D/run_3D.py:221-292.  pos [P][3]; T, T2 [P][3][3] (x, y, z vectors).
+void oracle3_rk4_T_and_T_grad_m_forward(float* pos, float* T, float* T2, int P, const float* ux, const float* uy,
+                                        const float* uz, int nx, int ny, int nz, double dx, float dt) {
+  Grid3<float> u[3] = {{ux, nx + 1, ny, nz}, {uy, nx, ny + 1, nz}, {uz, nx, ny, nz + 1}};
+  const float one_sixth = float(1.0 / 6.0);
+#pragma omp parallel for schedule(static)
+  for (int q = 0; q < P; ++q) {
+    float* ps = pos + (size_t)q * 3;
+    float* Tq[2] = {T + (size_t)q * 9, T2 + (size_t)q * 9};
+    float p0[3] = {ps[0], ps[1], ps[2]};
+    float T0[2][3][3];
+    for (int s2 = 0; s2 < 2; ++s2)
+      for (int v = 0; v < 3; ++v)
+        for (int c = 0; c < 3; ++c) T0[s2][v][c] = Tq[s2][v * 3 + c];
+    float uk[4][3], dT[4][2][3][3];
+    const float half_dt = 0.5f * dt;
+    const float stage_c[3] = {half_dt, half_dt, dt};
+    float pk[3] = {p0[0], p0[1], p0[2]};
+    float Tk[2][3][3];
+    std::memcpy(Tk, T0, sizeof(Tk));
+    for (int s = 0; s < 4; ++s) {
+      float g[3][3];
+      interp_u_MAC_grad_3(u, pk, dx, uk[s], g, true);
+      for (int s2 = 0; s2 < 2; ++s2)
+        for (int v = 0; v < 3; ++v) matvec3(g, Tk[s2][v], dT[s][s2][v]);
+      if (s < 3) {
+        float cdt = stage_c[s];
+        for (int c = 0; c < 3; ++c) pk[c] = p0[c] + cdt * uk[s][c];
+        for (int s2 = 0; s2 < 2; ++s2)
+          for (int v = 0; v < 3; ++v)
+            for (int c = 0; c < 3; ++c) Tk[s2][v][c] = T0[s2][v][c] - cdt * dT[s][s2][v][c];
+      }
+    }
+    const float coef = dt * one_sixth;
+    for (int c = 0; c < 3; ++c) ps[c] = p0[c] + coef * (uk[0][c] + 2.0f * uk[1][c] + 2.0f * uk[2][c] + uk[3][c]);
+    for (int s2 = 0; s2 < 2; ++s2)
+      for (int v = 0; v < 3; ++v)
+        for (int c = 0; c < 3; ++c)
+          Tq[s2][v * 3 + c] = T0[s2][v][c] - coef * (dT[0][s2][v][c] + 2.0f * dT[1][s2][v][c] +
+                                                     2.0f * dT[2][s2][v][c] + dT[3][s2][v][c]);
+  }
+}
+
+// update_particles_imp: 3D/run_3D.py:395-401.  imp [P][3] = cols(T) @ init_imp
+void oracle3_update_imp(float* imp, const float* imp0, const float* T, int P) {
+  for (int q = 0; q < P; ++q) {
+    const float* Tq = T + (size_t)q * 9;
+    const float* m = imp0 + (size_t)q * 3;
+    for (int r = 0; r < 3; ++r) imp[(size_t)q * 3 + r] = Tq[0 * 3 + r] * m[0] + Tq[1 * 3 + r] * m[1] + Tq[2 * 3 + r] * m[2];
+  }
+}
+
+// update_particles_grad_m: 3D/run_3D.py:412-428.  C, C0 [P][3][3] rows; T [P][3][3];
+// gT [P][3][3][3] (grad_T_init_x/y/z matrices, may be null); imp0 [P][3].
+void oracle3_update_grad_m(float* C, const float* C0, const float* T, const float* gT, const float* imp0, int P) {
+  for (int q = 0; q < P; ++q) {
+    float A[3][3], AT[3][3], Cm[3][3], CA[3][3], TCT[3][3];
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) {
+        A[r][c] = T[(size_t)q * 9 + r * 3 + c];
+        AT[r][c] = T[(size_t)q * 9 + c * 3 + r];
+        Cm[r][c] = C0[(size_t)q * 9 + r * 3 + c];
+      }
+    matmul3(Cm, A, CA);
+    matmul3(AT, CA, TCT);
+    const float* m = imp0 + (size_t)q * 3;
+    for (int r = 0; r < 3; ++r)
+      for (int a = 0; a < 3; ++a) {
+        float gm = 0.f;
+        if (gT) {
+          const float* G = gT + (size_t)q * 27 + r * 9 + a * 3;
+          gm = G[0] * m[0] + G[1] * m[1] + G[2] * m[2];
+        }
+        C[(size_t)q * 9 + r * 3 + a] = gm + TCT[r][a];
+      }
+  }
+}
+
+// compute_dT_dx: 3D/run_3D.py:353-390, with the cell lists of get_particles_id_in_every_cell
+// (3D/run_3D.py:342-351) built from pos in index order and capped at cap; neighbour cells
+// outside the grid are skipped.  pos, pos0 [P][3]; T [P][3][3]; gT [P][3][3][3].
+void oracle3_compute_dT_dx(const float* pos, const float* pos0, const float* T, int P, int nx, int ny, int nz,
+                           double dx, int cap, float* gT) {
+  const float dxr = float(dx);
+  const float inv = float(1.0 / dx);
+  const size_t C = (size_t)nx * ny * nz;
+  std::vector<std::vector<int>> lists(C);
+  for (int q = 0; q < P; ++q) {
+    int c[3];
+    for (int a = 0; a < 3; ++a) {
+      int v = (int)(pos[(size_t)q * 3 + a] / dxr);
+      c[a] = clampi(v, 0, (a == 0 ? nx : (a == 1 ? ny : nz)) - 1);
+    }
+    std::vector<int>& L = lists[((size_t)c[0] * ny + c[1]) * nz + c[2]];
+    if ((int)L.size() < cap) L.push_back(q);
+  }
+#pragma omp parallel for schedule(static)
+  for (int q = 0; q < P; ++q) {
+    float acc[3][3][3] = {{{0}}};
+    const float* xi = pos0 + (size_t)q * 3;
+    int base[3] = {(int)(xi[0] / dxr), (int)(xi[1] / dxr), (int)(xi[2] / dxr)};
+    for (int oi = -1; oi < 3; ++oi)
+      for (int oj = -1; oj < 3; ++oj)
+        for (int ok = -1; ok < 3; ++ok) {
+          int ci = base[0] + oi, cj = base[1] + oj, ck = base[2] + ok;
+          if (ci < 0 || ci >= nx || cj < 0 || cj >= ny || ck < 0 || ck >= nz) continue;
+          for (int n : lists[((size_t)ci * ny + cj) * nz + ck]) {
+            const float* xn = pos0 + (size_t)n * 3;
+            float d0 = xn[0] - xi[0], d1 = xn[1] - xi[1], d2 = xn[2] - xi[2];
+            float dw[3] = {inv * dN2(d0) * N2(d1) * N2(d2), inv * N2(d0) * dN2(d1) * N2(d2),
+                           inv * N2(d0) * N2(d1) * dN2(d2)};
+            const float* Tn = T + (size_t)n * 9;
+            for (int r = 0; r < 3; ++r)
+              for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) acc[r][a][b] += dw[a] * Tn[b * 3 + r];
+          }
+        }
+    for (int r = 0; r < 3; ++r)
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) gT[(size_t)q * 27 + r * 9 + a * 3 + b] = acc[r][a][b];
+  }
+}
+
 }  // extern "C"

@@ -266,6 +266,9 @@ class _Value:
                 for c in range(B.shape[1]):
                     out[r, c] = _seq_dot(A[r], B[:, c])
             return self._wrap(out)
+        if A.ndim == 1 and B.ndim == 2:  # vector @ matrix: the vector as a row, v^T M
+            return self._wrap(np.array([_seq_dot(A, B[:, c]) for c in range(B.shape[1])],
+                                       dtype=np.result_type(A, B)))
         raise TypeError("unsupported matmul")
 
     # reductions / linear algebra ---------------------------------------------------------------

@@ -41,6 +41,20 @@ def leapfrog_vel_func(vf, pf):
     vf.copy_(torch.from_numpy(out))
 
 
+def stripe_func(qf, pf, x_start, x_end):
+    """Smoke stripe (2D/init_conditions.py:108-113): qf [nx, ny, 3] = 0 where the cell centre lies in
+    x_start <= x <= x_end and 0.15 <= y <= 0.85, else 1.  pf (the cell centres (I + 0.5) dx,
+    dx = 1 / ny) is implied by qf's grid; the centres are formed in f32 as the reference's."""
+    nx, ny = int(qf.shape[0]), int(qf.shape[1])
+    dxf = np.float32(1.0 / ny)
+    x = (np.arange(nx, dtype=np.float32) + np.float32(0.5)) * dxf
+    y = (np.arange(ny, dtype=np.float32) + np.float32(0.5)) * dxf
+    inside = ((x[:, None] >= np.float32(x_start)) & (x[:, None] <= np.float32(x_end))
+              & (y[None, :] >= np.float32(0.15)) & (y[None, :] <= np.float32(0.85)))
+    out = np.where(inside[..., None], np.float32(0.0), np.float32(1.0)) * np.ones((1, 1, 3), np.float32)
+    qf.copy_(torch.from_numpy(out.astype(np.float32)))
+
+
 def init_particles_pos_uniform(particles_pos, X, res_x, particles_per_cell, dx, particles_per_cell_axis,
                                dist_between_neighbor):
     """Particles on the x-fastest lattice at (index + 0.5) * dist_between_neighbor

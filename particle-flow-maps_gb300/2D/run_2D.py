@@ -21,8 +21,9 @@ sys.path.insert(0, os.path.dirname(_HERE))
 from pfm import dropin as _d  # noqa: E402
 from hyperparameters import *  # noqa: E402,F401,F403
 from init_conditions import (init_particles_imp, init_particles_imp_grad_m,  # noqa: E402,F401
-                             init_particles_pos_uniform, leapfrog_vel_func)
+                             init_particles_pos_uniform, leapfrog_vel_func, stripe_func)
 from mgpcg import MGPCG_2  # noqa: E402
+from taichi_utils import curl, get_central_vector  # noqa: E402,F401
 
 dx = 1. / res_y  # noqa: F405
 particles_per_cell_axis = int(np.sqrt(particles_per_cell))  # noqa: F405
@@ -64,6 +65,9 @@ def _allocate():
     g["T_x_grid"], g["T_y_grid"] = (torch.zeros(s + (2,), device=dev) for s in _face_shapes)
     g["cell_particle_num"] = torch.zeros(_res, dtype=torch.int32, device=dev)
     g["X"] = None  # cell centres (I + 0.5) dx: implied by the grid
+    g["w"] = torch.zeros(_res, device=dev)  # curl of u
+    for name in ("init_smoke", "smoke", "tmp_smoke", "err_smoke"):  # 2D/run_2D.py:95-99
+        g[name] = torch.zeros(_res + (3,), device=dev)
 
 
 if torch.cuda.is_available():
@@ -176,6 +180,12 @@ def split_central_vector(vc, u_x_, u_y_):
     _scene().split_central_vector(vc, [u_x_, u_y_])
 
 
+def advect_smoke(smoke0, smoke1, psi_x, psi_y, dx_):
+    """smoke1 = smoke0 at the cell-centre average of the face backward maps, bilinear
+    (2D/run_2D.py:444-450); smoke grids [nx, ny, 3], psi grids [F, 2]."""
+    _scene().advect_smoke(smoke0, smoke1, [psi_x, psi_y], dx=float(dx_))
+
+
 # ---------------------------------------------------------------------------------------------
 # main loop (2D/run_2D.py:676-976)
 # ---------------------------------------------------------------------------------------------
@@ -189,11 +199,18 @@ def main(from_frame=0, testing=False, logs_root="logs"):
         leapfrog_vel_func(u, X)  # noqa: F821
         split_central_vector(u, u_x, u_y)  # noqa: F821
         solver.Poisson(u_x, u_y)  # noqa: F821
+        stripe_func(smoke, X, 0.25, 0.48)  # noqa: F821
     else:
         for t, n in zip(U, "xy"):
             t.copy_(torch.from_numpy(np.load(os.path.join(ckptdir, f"vel_{n}_numpy_{from_frame}.npy"))))
-    for t, n in zip(U, "xy"):
-        np.save(os.path.join(ckptdir, f"vel_{n}_numpy_{from_frame}"), t.cpu().numpy())
+        smoke.copy_(torch.from_numpy(np.load(os.path.join(ckptdir, f"smoke_numpy_{from_frame}.npy"))))  # noqa: F821
+    # vorticity for the frame output (2D/run_2D.py:741-742); the image writers are not built
+    get_central_vector(u_x, u_y, u)  # noqa: F821
+    curl(u, w, dx)  # noqa: F821
+    if save_ckpt:  # noqa: F405
+        for t, n in zip(U, "xy"):
+            np.save(os.path.join(ckptdir, f"vel_{n}_numpy_{from_frame}"), t.cpu().numpy())
+        np.save(os.path.join(ckptdir, f"smoke_numpy_{from_frame}"), smoke.cpu().numpy())  # noqa: F821
 
     sub_t = 0.
     frame_idx = from_frame
@@ -250,9 +267,12 @@ def main(from_frame=0, testing=False, logs_root="logs"):
               f"MGPCG iterations {solver.last_info.iterations}", flush=True)  # noqa: F821
         done = False
         if output_frame:
+            get_central_vector(u_x, u_y, u)  # noqa: F821
+            curl(u, w, dx)  # noqa: F821
             if save_ckpt and frame_idx % ckpt_every == 0:  # noqa: F405
                 for t, n in zip(U, "xy"):
                     np.save(os.path.join(ckptdir, f"vel_{n}_numpy_{frame_idx}"), t.cpu().numpy())
+                np.save(os.path.join(ckptdir, f"smoke_numpy_{frame_idx}"), smoke.cpu().numpy())  # noqa: F821
             done = frame_idx >= total_frames  # noqa: F405
         if use_total_steps and i >= total_steps - 1:  # noqa: F405
             done = True

@@ -21,8 +21,9 @@ sys.path.insert(0, os.path.dirname(_HERE))
 from pfm import dropin as _d  # noqa: E402
 from hyperparameters import *  # noqa: E402,F401,F403
 from init_conditions import (init_particles_imp, init_particles_imp_grad_m,  # noqa: E402,F401
-                             init_particles_pos_uniform, init_vorts_leapfrog)
+                             init_particles_pos_uniform, init_particles_smoke, init_vorts_leapfrog)
 from mgpcg import MGPCG_3  # noqa: E402
+from taichi_utils import curl, get_central_vector  # noqa: E402,F401
 
 dx = 1. / res_y  # noqa: F405
 particles_per_cell_axis = 2
@@ -61,11 +62,26 @@ def _allocate():
     g["u_x"], g["u_y"], g["u_z"] = (torch.zeros(s, device=dev) for s in _face_shapes)
     g["p2g_weight_x"], g["p2g_weight_y"], g["p2g_weight_z"] = (torch.zeros(s, device=dev) for s in _face_shapes)
     g["X"] = None  # cell centres (I + 0.5) dx: implied by the grid in the kernels that use them
-    g["smoke"] = g["tmp_smoke"] = None
+    g["w"] = torch.zeros(_res + (3,), device=dev)  # curl of u
+    g["smoke"] = torch.zeros(_res + (4,), device=dev)
+    g["tmp_smoke"] = torch.zeros(_res + (4,), device=dev)
 
 
 if torch.cuda.is_available():
     _allocate()
+
+# Per-particle smoke fields of the reference (3D/run_3D.py:47-48), allocated on first use: the
+# step never touches them (its smoke calls are commented out) and they hold 64 B per particle.
+_LAZY = {"particles_smoke": lambda: torch.zeros(4, particle_num, device="cuda"),
+         "particles_init_grad_smoke": lambda: torch.zeros(3, 4, particle_num, device="cuda")}
+
+
+def __getattr__(name):
+    if name in _LAZY and torch.cuda.is_available():
+        t = _LAZY[name]()
+        globals()[name] = t
+        return t
+    raise AttributeError(name)
 
 
 # ---------------------------------------------------------------------------------------------
@@ -168,6 +184,69 @@ def P2G(particles_init_imp, particles_init_imp_grad_m, particles_pos, u_x, u_y, 
 
 def split_central_vector(vc, u_x_, u_y_, u_z_):
     _scene().split_central_vector(vc, [u_x_, u_y_, u_z_])
+
+
+# ---------------------------------------------------------------------------------------------
+# smoke transport (3D/run_3D.py:315-334, 554-593) and the alternative "evolve m" dataflow
+# (3D/run_3D.py:221-292, 338-340, 353-428); the reference's step loop leaves them commented out
+# ---------------------------------------------------------------------------------------------
+def advect_smoke(smoke0, smoke1, psi_x, psi_y, psi_z, dx_):
+    """smoke1 = smoke0 at the cell-centre average of the face backward maps (3D/run_3D.py:315-323)."""
+    _scene().advect_smoke(smoke0, smoke1, [psi_x, psi_y, psi_z], dx=float(dx_))
+
+
+def clamp_smoke(smoke0, smoke1, psi_x, psi_y, psi_z, dx_):
+    """Clamp smoke1 to the range of smoke0's eight corners there (3D/run_3D.py:326-334)."""
+    _scene().clamp_smoke(smoke0, smoke1, [psi_x, psi_y, psi_z], dx=float(dx_))
+
+
+def P2G_smoke(particles_smoke_, particles_init_grad_smoke_, particles_pos_, smoke_, T_x_grad_m_, T_y_grad_m_,
+              T_z_grad_m_, T_x_init_, T_y_init_, T_z_init_, p2g_weight):
+    """APIC P2G of the particle smoke into smoke_ [nx, ny, nz, 4], normalised and clamped to [0, 1]
+    (3D/run_3D.py:554-593), with use_APIC_smoke; deterministic.  p2g_weight is a cell grid."""
+    with _d.Rows((T_x_grad_m_, T_y_grad_m_, T_z_grad_m_)) as Tg, _d.Rows((T_x_init_, T_y_init_, T_z_init_)) as Ti:
+        _scene().p2g_smoke(particles_smoke_, particles_init_grad_smoke_, particles_pos_, Tg, Ti, smoke_, p2g_weight,
+                           use_apic_smoke=use_APIC_smoke)  # noqa: F405
+
+
+def RK4_T_and_T_grad_m_forward(psi, T_x, T_y, T_z, T_x_grad_m_, T_y_grad_m_, T_z_grad_m_, u_x0, u_y0, u_z0, dt):
+    """RK4 of the positions and of both Jacobian sets (3D/run_3D.py:221-292)."""
+    with _d.Rows((T_x, T_y, T_z), out=True) as T, _d.Rows((T_x_grad_m_, T_y_grad_m_, T_z_grad_m_), out=True) as T2:
+        _scene().rk4_T_and_T_grad_m_forward(psi, T, T2, [u_x0, u_y0, u_z0], float(np.float32(dt)))
+
+
+def stretch_T_and_T_grad_m_and_advect_particles(particles_pos_, T_x, T_y, T_z, T_x_grad_m_, T_y_grad_m_, T_z_grad_m_,
+                                                u_x_, u_y_, u_z_, dt):
+    RK4_T_and_T_grad_m_forward(particles_pos_, T_x, T_y, T_z, T_x_grad_m_, T_y_grad_m_, T_z_grad_m_, u_x_, u_y_, u_z_,
+                               dt)
+
+
+def update_particles_imp(particles_imp_, particles_init_imp_, T_x, T_y, T_z):
+    """imp = cols(T) @ init_imp (3D/run_3D.py:395-401)."""
+    with _d.Rows((T_x, T_y, T_z)) as T:
+        _scene().update_imp3(particles_imp_, particles_init_imp_, T)
+
+
+def update_particles_grad_m(C_x, C_y, C_z, init_C_x_, init_C_y_, init_C_z_, T_x, T_y, T_z, grad_T_init_x,
+                            grad_T_init_y, grad_T_init_z, particles_init_imp_):
+    """C_r = grad_T_init_r @ init_imp + (T^T init_C T)_r (3D/run_3D.py:412-428); the grad_T_init
+    matrices are [3, 3, P] tensors (rows of one [3, 3, 3, P] buffer, or separate)."""
+    gT = torch.stack([grad_T_init_x, grad_T_init_y, grad_T_init_z]).contiguous()
+    with _d.Rows((C_x, C_y, C_z), out=True) as C, _d.Rows((init_C_x_, init_C_y_, init_C_z_)) as C0, \
+            _d.Rows((T_x, T_y, T_z)) as T:
+        _scene().update_grad_m3(C, C0, T, gT, particles_init_imp_)
+
+
+def compute_dT_dx(grad_T_init_x, grad_T_init_y, grad_T_init_z, T_x, T_y, T_z, particles_init_pos, cell_particles_id_,
+                  cell_particle_num_, cap=0):
+    """compute_dT_dx (3D/run_3D.py:353-390) on the cell lists of the module's particles_pos.  The
+    reference's inner loop ti.ndrange(0, n) is an empty two-axis range, so its result is zero: that
+    is cap = 0 (the default); cap = cell_max_particle_num computes the neighbourhood sum its body
+    describes."""
+    with _d.Rows((T_x, T_y, T_z)) as T:
+        gT = _scene().compute_dT_dx(particles_pos, particles_init_pos, T, int(cap))  # noqa: F821
+    for r, out in enumerate((grad_T_init_x, grad_T_init_y, grad_T_init_z)):
+        out.copy_(gT[r])
 
 
 # ---------------------------------------------------------------------------------------------

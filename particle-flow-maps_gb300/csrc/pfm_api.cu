@@ -127,7 +127,8 @@ int pfm_create(const pfm_config* cfg, pfm_handle** out) {
   h->o_start = take((C + 1) * 4);
   size_t per_block = (size_t)kScanItems * kScanThreads;
   h->o_blocksums = take(((C + per_block - 1) / per_block + 1) * 4);
-  h->o_payload = take(P * 16 * (D == 3 ? 4 : 3));
+  // P2G records: pos4 + 3 impulse families (3D velocity), pos4 + 4 smoke channels (P2G_smoke)
+  h->o_payload = take(P * 16 * (D == 3 ? 5 : 3));
   for (int l = 0; l < L; ++l) {
     h->o_r[l] = take((size_t)h->lv[l].count * 4);
     h->o_z[l] = take((size_t)h->lv[l].count * 4);

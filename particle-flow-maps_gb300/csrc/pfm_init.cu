@@ -1,5 +1,6 @@
 // Initial-condition kernels used to set up large scenes on the device: the vortex-ring
-// Biot-Savart sum (add_vortex_ring, 3D/init_conditions.py:10-22) and the centre-to-face split
+// Biot-Savart sum (add_vortex_ring, 3D/init_conditions.py:10-22; with the smoke marker,
+// add_vortex_ring_and_smoke, 3D/init_conditions.py:29-56) and the centre-to-face split
 // (split_central_vector, 3D/taichi_utils.py:87-100; 2D/taichi_utils.py:56-67).
 #include "pfm_internal.cuh"
 
@@ -7,8 +8,13 @@ namespace pfm {
 
 // vf[i,j,k] += sum_l curve_length * (-1/(4 pi r^3) * (1 - exp(-(r/delta)^3))) * (p - p_l) x w_l
 // with p the cell centre (I + 0.5) * dx (center_coords_func, 3D/taichi_utils.py:28-31).
-__global__ void __launch_bounds__(256) k_vortex_ring(float* __restrict__ vc, MacGeom g, float w, float rad,
-                                                     float delta, float3 c, float3 ux, float3 uy, int num_samples) {
+// SMOKE (add_vortex_ring_and_smoke, 3D/init_conditions.py:29-56, first loop) also adds
+// curve_length * exp(-(r/delta)^3) to smoke[3] sample by sample; the velocity arithmetic is the
+// same code in both forms, so their velocities are bitwise equal.
+template <bool SMOKE>
+__global__ void __launch_bounds__(256) k_vortex_ring(float* __restrict__ vc, float* __restrict__ smoke, MacGeom g,
+                                                     float w, float rad, float delta, float3 c, float3 ux, float3 uy,
+                                                     int num_samples) {
   const int64_t C = (int64_t)g.N[0] * g.N[1] * g.N[2];
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= C) return;
@@ -18,6 +24,7 @@ __global__ void __launch_bounds__(256) k_vortex_ring(float* __restrict__ vc, Mac
   const float pi = 3.14159265358979323846f;
   const float curve_length = (2.f * pi * rad) / (float)num_samples;
   float ax = 0.f, ay = 0.f, az = 0.f;
+  float s3 = SMOKE ? smoke[e * 4 + 3] : 0.f;
   for (int l = 0; l < num_samples; ++l) {
     float theta = (float)l / (float)num_samples * 2.f * pi;
     float ct = cosf(theta), st = sinf(theta);
@@ -28,14 +35,26 @@ __global__ void __launch_bounds__(256) k_vortex_ring(float* __restrict__ vc, Mac
     float r = sqrtf(dx * dx + dy * dy + dz * dz);
     float wx = w * (-st * ux.x + ct * uy.x), wy = w * (-st * ux.y + ct * uy.y), wz = w * (-st * ux.z + ct * uy.z);
     float rd = r / delta;
-    float f = curve_length * (-1.f / (4.f * pi * r * r * r) * (1.f - expf(-(rd * rd * rd))));
+    float ex = expf(-(rd * rd * rd));
+    float f = curve_length * (-1.f / (4.f * pi * r * r * r) * (1.f - ex));
     ax += f * (dy * wz - dz * wy);
     ay += f * (dz * wx - dx * wz);
     az += f * (dx * wy - dy * wx);
+    if (SMOKE) s3 += curve_length * ex;
   }
   vc[e * 3 + 0] += ax;
   vc[e * 3 + 1] += ay;
   vc[e * 3 + 2] += az;
+  if (SMOKE) smoke[e * 4 + 3] = s3;
+}
+
+// add_vortex_ring_and_smoke, second loop: cells whose marker exceeds 0.002 become (color, 1),
+// the others 0.
+__global__ void __launch_bounds__(256) k_smoke_marker(float4* __restrict__ smoke, int64_t C, float3 color) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= C) return;
+  const float4 s = smoke[e];
+  smoke[e] = (s.w > 0.002f) ? make_float4(color.x, color.y, color.z, 1.f) : make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 // split_central_vector: face = 0.5 * (sample(vc, I) + sample(vc, I - e_fam)) with clamped samples
@@ -110,10 +129,28 @@ int pfm3_add_vortex_ring(pfm_handle* h, float w, float rad, float delta, const f
   if (h->cfg.dim != 3) return set_error(h, PFM_ERR_SHAPE, "pfm3_add_vortex_ring on a 2D handle");
   if (!c || !unit_x || !unit_y || !vc) return set_error(h, PFM_ERR_NULL, "pfm3_add_vortex_ring: null input");
   if (num_samples < 1) return set_error(h, PFM_ERR_ARG, "pfm3_add_vortex_ring: num_samples < 1");
-  launch(h, k_vortex_ring, grid_for(h->cells, 256), 256, 0, (cudaStream_t)stream, vc, h->geom, w, rad, delta,
-         make_float3(c[0], c[1], c[2]), make_float3(unit_x[0], unit_x[1], unit_x[2]),
+  launch(h, k_vortex_ring<false>, grid_for(h->cells, 256), 256, 0, (cudaStream_t)stream, vc, (float*)nullptr, h->geom,
+         w, rad, delta, make_float3(c[0], c[1], c[2]), make_float3(unit_x[0], unit_x[1], unit_x[2]),
          make_float3(unit_y[0], unit_y[1], unit_y[2]), num_samples);
   return launch_check(h, "k_vortex_ring");
+}
+
+int pfm3_add_vortex_ring_and_smoke(pfm_handle* h, float w, float rad, float delta, const float c[3],
+                                   const float unit_x[3], const float unit_y[3], const float color[3], int num_samples,
+                                   float* vc, float* smoke, void* stream) {
+  if (!h) return PFM_ERR_NULL;
+  if (h->cfg.dim != 3) return set_error(h, PFM_ERR_SHAPE, "pfm3_add_vortex_ring_and_smoke on a 2D handle");
+  if (!c || !unit_x || !unit_y || !color || !vc || !smoke)
+    return set_error(h, PFM_ERR_NULL, "pfm3_add_vortex_ring_and_smoke: null input");
+  if (num_samples < 1) return set_error(h, PFM_ERR_ARG, "pfm3_add_vortex_ring_and_smoke: num_samples < 1");
+  if (((uintptr_t)smoke) & 15) return set_error(h, PFM_ERR_ARG, "pfm3_add_vortex_ring_and_smoke: smoke not 16-byte aligned");
+  cudaStream_t st = (cudaStream_t)stream;
+  const unsigned gr = grid_for(h->cells, 256);
+  launch(h, k_vortex_ring<true>, gr, 256, 0, st, vc, smoke, h->geom, w, rad, delta, make_float3(c[0], c[1], c[2]),
+         make_float3(unit_x[0], unit_x[1], unit_x[2]), make_float3(unit_y[0], unit_y[1], unit_y[2]), num_samples);
+  launch(h, k_smoke_marker, gr, 256, 0, st, reinterpret_cast<float4*>(smoke), h->cells,
+         make_float3(color[0], color[1], color[2]));
+  return launch_check(h, "k_vortex_ring<true>");
 }
 
 int pfm_split_central_vector(pfm_handle* h, const float* vc, float* u_x, float* u_y, float* u_z, void* stream) {

@@ -344,6 +344,185 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_tile3(const float4* __restr
                  out.w[2]);
 }
 
+// ---------------------------------------------------------------------------------------------
+// P2G_smoke (3D/run_3D.py:554-593): the cell-centred 4-channel smoke field with the APIC term
+// delta = dpos . (T_transpose @ init_grad_smoke), T_transpose = cols(T_gm) @ cols(T_init), weights
+// N_2(pos - I - 1/2) per axis, normalised by the weight sum and clamped to [0, 1] where it is
+// positive.  Same deterministic scheme as the impulse: bin sort, per-cell register windows (the
+// 3 x 3 x 3 cells a particle cell reaches), parity-ordered cell tiles, no float atomics.
+// ---------------------------------------------------------------------------------------------
+
+// Record pass in particle order: pos4 = (pos/dx, 0), chrec[ch][q] = (s_ch, M[0][ch], M[1][ch],
+// M[2][ch]) with M = T_transpose @ init_grad_smoke; cell key + bin slot as k_bin_keys.
+__global__ void __launch_bounds__(kBinThreads) k_payload_smoke3(int64_t P, MacGeom g, const float* __restrict__ pos,
+                                                                const float* __restrict__ Tg,
+                                                                const float* __restrict__ Ti,
+                                                                const float* __restrict__ s,
+                                                                const float* __restrict__ Gs, float4* __restrict__ pos4,
+                                                                float4* __restrict__ chrec, int* __restrict__ key,
+                                                                int* __restrict__ slot, int* __restrict__ count) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= P) return;
+  float v[3];
+  int c[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    v[a] = pos[a * P + q] / g.dx;
+    const int ci = __float2int_rz(v[a]);
+    c[a] = ci < 0 ? 0 : (ci > g.N[a] - 1 ? g.N[a] - 1 : ci);
+  }
+  const int k = (c[0] * g.N[1] + c[1]) * g.N[2] + c[2];
+  key[q] = k;
+  slot[q] = atomicAdd(&count[k], 1);
+  // TT[r][cc] = sum_k T_gm_k[r] * T_init_cc[k]
+  float M[3][3], N[3][3], TT[3][3];
+#pragma unroll
+  for (int vv = 0; vv < 3; ++vv)
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc) {
+      M[cc][vv] = Tg[(vv * 3 + cc) * P + q];
+      N[cc][vv] = Ti[(vv * 3 + cc) * P + q];
+    }
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc) TT[r][cc] = M[r][0] * N[0][cc] + M[r][1] * N[1][cc] + M[r][2] * N[2][cc];
+  pos4[q] = make_float4(v[0], v[1], v[2], 0.f);
+#pragma unroll
+  for (int ch = 0; ch < 4; ++ch) {
+    const float g0 = Gs[(0 * 4 + ch) * P + q], g1 = Gs[(1 * 4 + ch) * P + q], g2 = Gs[(2 * 4 + ch) * P + q];
+    float m[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) m[r] = TT[r][0] * g0 + TT[r][1] * g1 + TT[r][2] * g2;
+    chrec[ch * P + q] = make_float4(s[ch * P + q], m[0], m[1], m[2]);
+  }
+}
+
+constexpr int kExtCell = (kTX + 2) * (kTY + 2) * (kTZ + 2);  // cell region of a tile (halo 1)
+static_assert(kExtCell <= kTileExtMax, "smoke tile region exceeds the shared buffer");
+
+// One channel of one tile: window sums of (s + delta) w and w over the 3 x 3 x 3 cells, merged
+// through shared memory in 27 passes, added into smoke[.][ch] (and the weight grid for ch 0).
+__device__ __forceinline__ void tile_smoke_channel(float2* __restrict__ acc, const float4* __restrict__ pos4,
+                                                   const float4* __restrict__ rec, const int* __restrict__ order,
+                                                   int sb, int se, int ci, int cj, int ck, int lx, int ly, int lz,
+                                                   int x0, int y0, int z0, const MacGeom& g, int use_apic, int ch,
+                                                   float* __restrict__ smoke, float* __restrict__ wsum) {
+  constexpr int E0 = kTX + 2, E1 = kTY + 2, E2 = kTZ + 2, NE = E0 * E1 * E2;
+  for (int e = threadIdx.x; e < NE; e += kTileThreads) acc[e] = make_float2(0.f, 0.f);
+  float num[3][3][3], den[3][3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) num[a][b][k] = den[a][b][k] = 0.f;
+  const float dx = g.dx;
+  for (int s = sb; s < se; ++s) {
+    const int q = __ldg(order + s);
+    const float4 p = __ldg(pos4 + q);
+    const float4 fr = __ldg(rec + q);
+    float w0[3], d0[3], w1[3], d1[3], w2[3], d2[3];
+    tile_axis<false>(p.x, ci, dx, w0, d0);
+    tile_axis<false>(p.y, cj, dx, w1, d1);
+    tile_axis<false>(p.z, ck, dx, w2, d2);
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        const float w01 = w0[a] * w1[b];
+        const float d01 = fr.y * d0[a] + fr.z * d1[b];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const float wt = w01 * w2[k];
+          const float delta = d01 + fr.w * d2[k];
+          num[a][b][k] += (use_apic ? (fr.x + delta) : fr.x) * wt;
+          den[a][b][k] += wt;
+        }
+      }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        float2* cell = acc + ((lx + a) * E1 + (ly + b)) * E2 + (lz + k);
+        float2 v = *cell;
+        v.x += num[a][b][k];
+        v.y += den[a][b][k];
+        *cell = v;
+        __syncthreads();
+      }
+  const int n0 = g.N[0], n1 = g.N[1], n2 = g.N[2];
+  constexpr int NPT = (NE + kTileThreads - 1) / kTileThreads;
+  int64_t qs[NPT];
+  float2 vs[NPT];
+#pragma unroll
+  for (int j = 0; j < NPT; ++j) {
+    const int e = threadIdx.x + j * kTileThreads;
+    const int ez = e % E2, r = e / E2, ey = r % E1, ex = r / E1;
+    const int gi = x0 - 1 + ex, gj = y0 - 1 + ey, gk = z0 - 1 + ez;
+    qs[j] = -1;
+    if (e < NE && gi >= 0 && gi < n0 && gj >= 0 && gj < n1 && gk >= 0 && gk < n2) {
+      qs[j] = ((int64_t)gi * n1 + gj) * n2 + gk;
+      const float2 v = acc[e];
+      vs[j] = make_float2(v.x + smoke[qs[j] * 4 + ch], ch == 0 ? v.y + wsum[qs[j]] : 0.f);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < NPT; ++j) {
+    if (qs[j] >= 0) {
+      smoke[qs[j] * 4 + ch] = vs[j].x;
+      if (ch == 0) wsum[qs[j]] = vs[j].y;
+    }
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kTileThreads, 1) k_tile_smoke3(const float4* __restrict__ pos4,
+                                                                 const float4* __restrict__ chrec,
+                                                                 const int* __restrict__ order,
+                                                                 const int* __restrict__ start, MacGeom g, int use_apic,
+                                                                 int64_t P, int px, int py, int pz,
+                                                                 float* __restrict__ smoke, float* __restrict__ wsum) {
+  __shared__ float2 acc[kExtCell];
+  const int x0 = (2 * (int)blockIdx.z + px) * kTX, y0 = (2 * (int)blockIdx.y + py) * kTY;
+  const int z0 = (2 * (int)blockIdx.x + pz) * kTZ;
+  const int lz = threadIdx.x % kTZ, ly = (threadIdx.x / kTZ) % kTY, lx = threadIdx.x / (kTZ * kTY);
+  const int ci = x0 + lx, cj = y0 + ly, ck = z0 + lz;
+  int sb = 0, se = 0;
+  if (ci < g.N[0] && cj < g.N[1] && ck < g.N[2]) {
+    const int c = (ci * g.N[1] + cj) * g.N[2] + ck;
+    sb = __ldg(start + c);
+    se = __ldg(start + c + 1);
+  }
+#pragma unroll 1
+  for (int ch = 0; ch < 4; ++ch)
+    tile_smoke_channel(acc, pos4, chrec + ch * P, order, sb, se, ci, cj, ck, lx, ly, lz, x0, y0, z0, g, use_apic, ch,
+                       smoke, wsum);
+}
+
+// smoke /= w and clamp every channel to [0, 1] where w > 0 (3D/run_3D.py:584-591)
+__global__ void __launch_bounds__(kBinThreads) k_normalize_smoke3(float4* __restrict__ smoke,
+                                                                  const float* __restrict__ wsum, int64_t C) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= C) return;
+  const float w = wsum[e];
+  if (!(w > 0.f)) return;
+  float4 s = smoke[e];
+  float* c = reinterpret_cast<float*>(&s);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    float x = c[j] / w;
+    if (x < 0.f) x = 0.f;
+    if (x > 1.f) x = 1.f;
+    c[j] = x;
+  }
+  smoke[e] = s;
+}
+
 // u = u / w where w > 0 (3D/run_3D.py:530-552), all three families in one pass
 __global__ void __launch_bounds__(kBinThreads) k_normalize3(FaceOut3 out, int64_t F0, int64_t F1, int64_t F2) {
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -663,6 +842,49 @@ int pfm3_rk4_p2g(pfm_handle* h, float* pos, float* T_gm, const float* ua_x, cons
   int rc = pfm3_rk4_p2g_records(h, pos, T_gm, ua_x, ua_y, ua_z, dt, init_imp, T_init, init_C, stream);
   if (rc) return rc;
   return pfm3_p2g_from_records(h, u_x, u_y, u_z, w_x, w_y, w_z, stream);
+}
+
+int pfm3_p2g_smoke(pfm_handle* h, const float* smoke_p, const float* init_grad_smoke, const float* pos,
+                   const float* T_gm, const float* T_init, int use_apic_smoke, float* smoke, float* weight,
+                   void* stream) {
+  if (!h) return PFM_ERR_NULL;
+  if (h->cfg.dim != 3) return set_error(h, PFM_ERR_SHAPE, "pfm3_p2g_smoke on a 2D handle");
+  if (!smoke || !weight) return set_error(h, PFM_ERR_NULL, "pfm3_p2g_smoke: null grid");
+  if (((uintptr_t)smoke) & 15) return set_error(h, PFM_ERR_ARG, "pfm3_p2g_smoke: smoke not 16-byte aligned");
+  if (h->P > 0 && (!smoke_p || !init_grad_smoke || !pos || !T_gm || !T_init))
+    return set_error(h, PFM_ERR_NULL, "pfm3_p2g_smoke: null particle field");
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = require_ws(h);
+  if (rc) return rc;
+  rc = check_cuda(h, cudaMemsetAsync(ws_ptr<int>(h, h->o_count), 0, h->cells * 4, st), "memset counts");
+  if (!rc) rc = check_cuda(h, cudaMemsetAsync(smoke, 0, h->cells * 16, st), "zero smoke");
+  if (!rc) rc = check_cuda(h, cudaMemsetAsync(weight, 0, h->cells * 4, st), "zero weight");
+  if (rc) return rc;
+  h->rec_valid = 0;  // the impulse records share the payload
+  float4* pos4 = ws_ptr<float4>(h, h->o_payload);
+  float4* chrec = pos4 + h->P;
+  if (h->P > 0)
+    launch(h, k_payload_smoke3, grid_for(h->P, kBinThreads), kBinThreads, 0, st, h->P, h->geom, pos, T_gm, T_init,
+           smoke_p, init_grad_smoke, pos4, chrec, ws_ptr<int>(h, h->o_key), ws_ptr<int>(h, h->o_slot),
+           ws_ptr<int>(h, h->o_count));
+  rc = sort_from_keys(h, st);
+  if (rc) return rc;
+  if (h->P > 0) {
+    const int* start = ws_ptr<int>(h, h->o_start);
+    const int* order = ws_ptr<int>(h, h->o_order);
+    const int nt[3] = {(h->geom.N[0] + kTX - 1) / kTX, (h->geom.N[1] + kTY - 1) / kTY, (h->geom.N[2] + kTZ - 1) / kTZ};
+    for (int px = 0; px < 2; ++px)
+      for (int py = 0; py < 2; ++py)
+        for (int pz = 0; pz < 2; ++pz) {
+          const unsigned bx = (nt[0] - px + 1) / 2, by = (nt[1] - py + 1) / 2, bz = (nt[2] - pz + 1) / 2;
+          if (!bx || !by || !bz) continue;
+          launch(h, k_tile_smoke3, dim3(bz, by, bx), kTileThreads, 0, st, (const float4*)pos4, (const float4*)chrec,
+                 order, start, h->geom, use_apic_smoke ? 1 : 0, h->P, px, py, pz, smoke, weight);
+        }
+    launch(h, k_normalize_smoke3, grid_for(h->cells, kBinThreads), kBinThreads, 0, st,
+           reinterpret_cast<float4*>(smoke), (const float*)weight, h->cells);
+  }
+  return launch_check(h, "pfm3_p2g_smoke");
 }
 
 int pfm2_p2g(pfm_handle* h, const float* imp, const float* pos, const float* C, const float* psi, float* u_x,

@@ -84,6 +84,21 @@ SIGNATURES = {
     "pfm_divergence": [_P, _P, _P, _P, _P, _P],
     "pfm_subtract_grad_p": [_P, _P, _P, _P, _P, _P],
     "pfm_sort_particles_noalloc": [_I, ctypes.POINTER(_I), ctypes.c_double, ctypes.c_int64, _P, _P, _P, _P],
+    "pfm3_get_central_vector": [_P, _P, _P, _P, _P, _P],
+    "pfm3_curl": [_P, _P, _P, _F, _P],
+    "pfm2_get_central_vector": [_P, _P, _P, _P, _P],
+    "pfm2_curl": [_P, _P, _P, _F, _P],
+    "pfm3_init_particles_smoke": [_P, _P, _P, _P, _P, _P],
+    "pfm3_p2g_smoke": [_P, _P, _P, _P, _P, _P, _I, _P, _P, _P],
+    "pfm3_advect_smoke": [_P, _P, _P, _P, _P, _P, _F, _P],
+    "pfm3_clamp_smoke": [_P, _P, _P, _P, _P, _P, _F, _P],
+    "pfm2_advect_smoke": [_P, _P, _P, _P, _P, _F, _P],
+    "pfm3_add_vortex_ring_and_smoke": [_P, _F, _F, _F, ctypes.POINTER(_F), ctypes.POINTER(_F), ctypes.POINTER(_F),
+                                       ctypes.POINTER(_F), _I, _P, _P, _P],
+    "pfm3_rk4_T_and_T_grad_m_forward": [_P, _P, _P, _P, _P, _P, _P, _F, _P],
+    "pfm3_update_imp": [_P, _P, _P, _P, _P],
+    "pfm3_update_grad_m": [_P, _P, _P, _P, _P, _P, _P],
+    "pfm3_compute_dT_dx": [_P, _P, _P, _P, _I, _P, _P],
 }
 # scratch limits of pfm_sort_particles_noalloc (include/pfm.h)
 NOALLOC_MAX_PARTICLES = 1 << 21

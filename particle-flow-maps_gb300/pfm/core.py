@@ -416,6 +416,175 @@ class Scene:
         self._check(self.lib.pfm_divergence(self.h, _ptr(u[0]), _ptr(u[1]), self._uz(u), _ptr(div_out),
                                             self._stream()))
 
+    # ------------------------------------------------------------------------------------------
+    # scalar (smoke) transport and diagnostics
+    # ------------------------------------------------------------------------------------------
+    def _cellvec(self, t, n, name):
+        self._dev(t, name)
+        if tuple(t.shape) != self.cell_shape + (n,):
+            raise PfmError(2, f"{name} must have shape {self.cell_shape + (n,)}, got {tuple(t.shape)}")
+        if t.data_ptr() % 16:
+            raise PfmError(7, f"{name} must be 16-byte aligned")
+        return t
+
+    def _psi(self, psi, name="psi"):
+        if len(psi) != self.dim:
+            raise PfmError(2, f"{name} needs {self.dim} face grids")
+        for f, t in enumerate(psi):
+            self._dev(t, f"{name}[{f}]")
+            if tuple(t.shape) != self.face_shapes[f] + (self.dim,):
+                raise PfmError(2, f"{name}[{f}]: shape {tuple(t.shape)} != {self.face_shapes[f] + (self.dim,)}")
+        return psi
+
+    def get_central_vector(self, u, vc=None):
+        """get_central_vector (3D/taichi_utils.py:80-85, 2D/taichi_utils.py:50-55): cell-centred
+        face averages [*res, dim]."""
+        u = self._grids(u)
+        vc = torch.empty(self.cell_shape + (self.dim,), device=self.device) if vc is None else vc
+        self._cellvec(vc, self.dim, "vc")
+        if self.dim == 3:
+            self._check(self.lib.pfm3_get_central_vector(self.h, *map(_ptr, u), _ptr(vc), self._stream()))
+        else:
+            self._check(self.lib.pfm2_get_central_vector(self.h, *map(_ptr, u), _ptr(vc), self._stream()))
+        return vc
+
+    def curl(self, vc, w=None, dx=None):
+        """curl (3D/taichi_utils.py:56-78: w [*res, 3]; 2D/taichi_utils.py:96-104: w [*res])."""
+        self._cellvec(vc, self.dim, "vc")
+        shape = self.cell_shape + ((3,) if self.dim == 3 else ())
+        w = torch.empty(shape, device=self.device) if w is None else w
+        self._dev(w, "w")
+        if tuple(w.shape) != shape:
+            raise PfmError(2, f"w must have shape {shape}")
+        dxf = ctypes.c_float(self.dx if dx is None else dx)
+        fn = self.lib.pfm3_curl if self.dim == 3 else self.lib.pfm2_curl
+        self._check(fn(self.h, _ptr(vc), _ptr(w), dxf, self._stream()))
+        return w
+
+    def init_particles_smoke(self, pos, smoke, smoke_p=None, grad_smoke=None):
+        """init_particles_smoke (3D/init_conditions.py:275-279): particle smoke [4, P] and its
+        gradient [3, 4, P] from the smoke grid [*res, 4]."""
+        self._need3("init_particles_smoke")
+        self._part(pos, 3, "pos")
+        self._cellvec(smoke, 4, "smoke")
+        if smoke_p is not None:
+            self._part(smoke_p, 4, "smoke_p")
+        if grad_smoke is not None:
+            self._dev(grad_smoke, "grad_smoke")
+            if tuple(grad_smoke.shape) != (3, 4, self.P):
+                raise PfmError(2, f"grad_smoke must be [3, 4, {self.P}]")
+        self._check(self.lib.pfm3_init_particles_smoke(self.h, _ptr(pos), _ptr(smoke), _ptr(smoke_p), _ptr(grad_smoke),
+                                                       self._stream()))
+
+    def p2g_smoke(self, smoke_p, grad_smoke, pos, T_gm, T_init, smoke_out, w_out, use_apic_smoke=True):
+        """P2G_smoke (3D/run_3D.py:554-593) into smoke_out [*res, 4] and the weights w_out [*res]."""
+        self._need3("p2g_smoke")
+        self._part(smoke_p, 4, "smoke_p")
+        self._dev(grad_smoke, "grad_smoke")
+        if tuple(grad_smoke.shape) != (3, 4, self.P):
+            raise PfmError(2, f"grad_smoke must be [3, 4, {self.P}]")
+        self._part(pos, 3, "pos")
+        self._part(T_gm, 3, "T_gm", vec=3)
+        self._part(T_init, 3, "T_init", vec=3)
+        self._cellvec(smoke_out, 4, "smoke_out")
+        self._cells(w_out, "w_out")
+        self._check(self.lib.pfm3_p2g_smoke(self.h, _ptr(smoke_p), _ptr(grad_smoke), _ptr(pos), _ptr(T_gm),
+                                            _ptr(T_init), int(bool(use_apic_smoke)), _ptr(smoke_out), _ptr(w_out),
+                                            self._stream()))
+
+    def advect_smoke(self, smoke0, smoke1, psi, dx=None):
+        """advect_smoke (3D/run_3D.py:315-323; 2D/run_2D.py:444-450): smoke1 = smoke0 at the
+        cell-centre backward map averaged from the face maps psi (pfm3/pfm2_midpoint's psi_out)."""
+        nch = 4 if self.dim == 3 else 3
+        self._cellvec(smoke0, nch, "smoke0")
+        self._cellvec(smoke1, nch, "smoke1")
+        psi = self._psi(psi)
+        dxf = ctypes.c_float(self.dx if dx is None else dx)
+        if self.dim == 3:
+            self._check(self.lib.pfm3_advect_smoke(self.h, _ptr(smoke0), _ptr(smoke1), *map(_ptr, psi), dxf,
+                                                   self._stream()))
+        else:
+            self._check(self.lib.pfm2_advect_smoke(self.h, _ptr(smoke0), _ptr(smoke1), *map(_ptr, psi), dxf,
+                                                   self._stream()))
+
+    def clamp_smoke(self, smoke0, smoke1, psi, dx=None):
+        """clamp_smoke (3D/run_3D.py:326-334): clamps smoke1 to the range of smoke0's trilinear
+        corners at the backward map, in place."""
+        self._need3("clamp_smoke")
+        self._cellvec(smoke0, 4, "smoke0")
+        self._cellvec(smoke1, 4, "smoke1")
+        psi = self._psi(psi)
+        dxf = ctypes.c_float(self.dx if dx is None else dx)
+        self._check(self.lib.pfm3_clamp_smoke(self.h, _ptr(smoke0), _ptr(smoke1), *map(_ptr, psi), dxf,
+                                              self._stream()))
+
+    def add_vortex_ring_and_smoke(self, vc, smoke, w, rad, delta, c, unit_x, unit_y, color, num_samples):
+        """add_vortex_ring_and_smoke (3D/init_conditions.py:29-56): ring velocity into vc [*res, 3],
+        marker into smoke [*res, 4], then smoke = (color, 1) where the marker exceeds 0.002, else 0."""
+        self._need3("add_vortex_ring_and_smoke")
+        self._dev(vc, "vc")
+        if tuple(vc.shape) != self.cell_shape + (3,):
+            raise PfmError(2, "vc must be [nx, ny, nz, 3]")
+        self._cellvec(smoke, 4, "smoke")
+        f3 = ctypes.c_float * 3
+        self._check(self.lib.pfm3_add_vortex_ring_and_smoke(
+            self.h, ctypes.c_float(w), ctypes.c_float(rad), ctypes.c_float(delta), f3(*c), f3(*unit_x), f3(*unit_y),
+            f3(*color), int(num_samples), _ptr(vc), _ptr(smoke), self._stream()))
+
+    # ------------------------------------------------------------------------------------------
+    # the reference's alternative ("evolve m") dataflow (3D/run_3D.py:221-292, 353-428)
+    # ------------------------------------------------------------------------------------------
+    def rk4_T_and_T_grad_m_forward(self, pos, T, T_grad_m, u, dt):
+        """RK4_T_and_T_grad_m_forward: positions and both Jacobian sets advanced in place."""
+        self._need3("rk4_T_and_T_grad_m_forward")
+        self._part(pos, 3, "pos")
+        self._part(T, 3, "T", vec=3)
+        self._part(T_grad_m, 3, "T_grad_m", vec=3)
+        u = self._grids(u)
+        self._check(self.lib.pfm3_rk4_T_and_T_grad_m_forward(self.h, _ptr(pos), _ptr(T), _ptr(T_grad_m), *map(_ptr, u),
+                                                             ctypes.c_float(dt), self._stream()))
+
+    def update_imp3(self, imp, init_imp, T):
+        """update_particles_imp (3D): imp = cols(T) @ init_imp."""
+        self._need3("update_imp3")
+        self._part(imp, 3, "imp")
+        self._part(init_imp, 3, "init_imp")
+        self._part(T, 3, "T", vec=3)
+        self._check(self.lib.pfm3_update_imp(self.h, _ptr(imp), _ptr(init_imp), _ptr(T), self._stream()))
+
+    def update_grad_m3(self, C, init_C, T, grad_T_init=None, init_imp=None):
+        """update_particles_grad_m (3D): C_r = grad_T_init_r @ init_imp + (T^T init_C T)_r;
+        grad_T_init [3, 3, 3, P] or None (zero)."""
+        self._need3("update_grad_m3")
+        for t, n in ((C, "C"), (init_C, "init_C"), (T, "T")):
+            self._part(t, 3, n, vec=3)
+        if grad_T_init is not None:
+            self._dev(grad_T_init, "grad_T_init")
+            if tuple(grad_T_init.shape) != (3, 3, 3, self.P):
+                raise PfmError(2, f"grad_T_init must be [3, 3, 3, {self.P}]")
+            self._part(init_imp, 3, "init_imp")
+        self._check(self.lib.pfm3_update_grad_m(self.h, _ptr(C), _ptr(init_C), _ptr(T), _ptr(grad_T_init),
+                                                _ptr(init_imp), self._stream()))
+
+    def compute_dT_dx(self, pos, init_pos, T, cap, grad_T_init=None):
+        """compute_dT_dx: grad_T_init [3, 3, 3, P] from the neighbours in the cell lists of pos (at
+        most cap per cell); cap = 0 gives the reference kernel's own (empty-loop) result."""
+        self._need3("compute_dT_dx")
+        self._part(pos, 3, "pos")
+        self._part(init_pos, 3, "init_pos")
+        self._part(T, 3, "T", vec=3)
+        out = torch.empty(3, 3, 3, self.P, device=self.device) if grad_T_init is None else grad_T_init
+        self._dev(out, "grad_T_init")
+        if tuple(out.shape) != (3, 3, 3, self.P):
+            raise PfmError(2, f"grad_T_init must be [3, 3, 3, {self.P}]")
+        self._check(self.lib.pfm3_compute_dT_dx(self.h, _ptr(pos), _ptr(init_pos), _ptr(T), int(cap), _ptr(out),
+                                                self._stream()))
+        return out
+
+    def _need3(self, what):
+        if self.dim != 3:
+            raise PfmError(2, f"{what} is a 3D phase")
+
     def subtract_grad_p(self, u, p):
         """MGPCG subtract_grad_p (3D/mgpcg.py:392-418): u -= grad p, in place."""
         u = self._grids(u, "u")

@@ -6,6 +6,9 @@ Run in a container that has the reference checked out (it reads ``/root/referenc
     python tests/golden/make_golden.py ref2d_kernels   # per-kernel cases, 2D
     python tests/golden/make_golden.py ref3d_steps     # run_3D.main(): 10 steps at 8^3
     python tests/golden/make_golden.py ref2d_steps     # run_2D.main(): 20 steps at 32^2
+    python tests/golden/make_golden.py ref3d_fields    # smoke transport + curl, 16x12x8
+    python tests/golden/make_golden.py ref2d_fields    # advect_smoke + curl, 32x24
+    python tests/golden/make_golden.py ref3d_variants  # the "evolve m" kernels, 12x10x8
 
 Taichi 1.5.0 is not installable here, so the reference modules are executed through
 ``oracle/ref_shim`` (a restatement of the Taichi semantics the step uses: f32 arithmetic,
@@ -424,8 +427,230 @@ def ref2d_steps():
     return snaps
 
 
+# ------------------------------------------------------------------------------------------------
+# scalar (smoke) transport and diagnostics: the reference's kernels outside the live step loop
+# (their call sites in main() are commented out or run only at frame output)
+# ------------------------------------------------------------------------------------------------
+def _face_psi(shape, fam, rng, dx, amp):
+    """Backward-map face grids [F, 3]: face centres moved by a smooth field, some out of range."""
+    idx = np.meshgrid(*[np.arange(s, dtype=np.float64) for s in shape], indexing="ij")
+    out = np.zeros(shape + (len(shape),), np.float32)
+    for d in range(len(shape)):
+        x = (idx[d] + (0.0 if d == fam else 0.5)) * dx
+        out[..., d] = x + smooth_field(shape, rng, amp, dx)
+    return out
+
+
+def ref3d_fields():
+    import taichi as ti
+    res = (16, 12, 8)
+    R = load3d(hp3d(res))
+    import init_conditions as IC
+    import taichi_utils as TU
+    rng = np.random.default_rng(777)
+    dx = R.dx
+    nx, ny, nz = res
+    out = {"res": np.array(res), "dx": np.float32(dx)}
+    ux = smooth_field((nx + 1, ny, nz), rng, 0.6, dx)
+    uy = smooth_field((nx, ny + 1, nz), rng, 0.6, dx)
+    uz = smooth_field((nx, ny, nz + 1), rng, 0.6, dx)
+    out.update(u_x=ux, u_y=uy, u_z=uz)
+    R.u_x.from_numpy(ux); R.u_y.from_numpy(uy); R.u_z.from_numpy(uz)
+
+    # get_central_vector + curl (3D/taichi_utils.py:56-85)
+    TU.get_central_vector(R.u_x, R.u_y, R.u_z, R.u)
+    out["central"] = R.u.to_numpy()
+    TU.curl(R.u, R.w, dx)
+    out["curl"] = R.w.to_numpy()
+
+    # init_particles_smoke (3D/init_conditions.py:275-279) on a smooth 4-channel smoke field
+    smoke = np.stack([np.abs(smooth_field(res, rng, 0.8, dx)) for _ in range(4)], axis=-1).astype(np.float32)
+    out["smoke"] = smoke
+    n = 512
+    pos = (rng.uniform(0.0, 1.0, size=(n, 3)) * np.array([nx, ny, nz]) * dx).astype(np.float32)
+    pos[:6] = np.array([[0.001, 0.5, 0.3], [nx * dx - 0.0005, 0.4, 0.2], [0.3, -0.01, 0.3],
+                        [0.5, 0.5, nz * dx + 0.004], [0.02, 0.98 * ny * dx, 0.01], [0.5, 0.5, 0.25]],
+                       dtype=np.float32)
+    out["pos"] = pos
+    mk = lambda k: ti.Vector.field(k, float, shape=n)  # noqa: E731
+    sm_f = ti.Vector.field(4, float, shape=res); sm_f.from_numpy(smoke)
+    p_f = mk(3); set_vec(p_f, pos)
+    s_f = mk(4)
+    g_f = ti.Matrix.field(3, 4, float, shape=n)
+    IC.init_particles_smoke(s_f, g_f, p_f, sm_f, dx)
+    out["g2p_smoke"] = s_f.to_numpy()
+    out["g2p_grad_smoke"] = g_f.to_numpy()
+
+    # P2G_smoke (3D/run_3D.py:554-593) with T_gm, T_init and a random smoke gradient
+    T = (np.eye(3)[None] + 0.05 * rng.standard_normal((n, 3, 3))).astype(np.float32)
+    T_init = (np.eye(3)[None] + 0.05 * rng.standard_normal((n, 3, 3))).astype(np.float32)
+    s_p = rng.uniform(0.0, 1.0, size=(n, 4)).astype(np.float32)
+    G = (2.0 * rng.standard_normal((n, 3, 4))).astype(np.float32)
+    out.update(T_gm=T, T_init=T_init, smoke_p=s_p, grad_smoke=G)
+    s_f = mk(4); s_f.from_numpy(s_p)
+    g_f = ti.Matrix.field(3, 4, float, shape=n); g_f.from_numpy(G)
+    Tg = [mk(3) for _ in range(3)]
+    Ti = [mk(3) for _ in range(3)]
+    for v in range(3):
+        set_vec(Tg[v], T[:, v]); set_vec(Ti[v], T_init[:, v])
+    out_sm = ti.Vector.field(4, float, shape=res)
+    wgt = ti.field(float, shape=res)
+    R.P2G_smoke(s_f, g_f, p_f, out_sm, *Tg, *Ti, wgt)
+    out["p2g_smoke"] = out_sm.to_numpy()
+    out["p2g_smoke_w"] = wgt.to_numpy()
+
+    # advect_smoke / clamp_smoke (3D/run_3D.py:315-334) through perturbed backward maps
+    shapes = [(nx + 1, ny, nz), (nx, ny + 1, nz), (nx, ny, nz + 1)]
+    psi = [_face_psi(shapes[f], f, rng, dx, 2.5 * dx) for f in range(3)]
+    out.update(psi_x=psi[0], psi_y=psi[1], psi_z=psi[2])
+    pf = [ti.Vector.field(3, float, shape=shapes[f]) for f in range(3)]
+    for f in range(3):
+        pf[f].from_numpy(psi[f])
+    s1 = ti.Vector.field(4, float, shape=res)
+    R.advect_smoke(sm_f, s1, *pf, dx)
+    out["advect_smoke"] = s1.to_numpy()
+    s1_in = (s1.to_numpy() + 0.3 * rng.standard_normal(res + (4,))).astype(np.float32)
+    out["clamp_in"] = s1_in
+    s1.from_numpy(s1_in)
+    R.clamp_smoke(sm_f, s1, *pf, dx)
+    out["clamp_smoke"] = s1.to_numpy()
+
+    # add_vortex_ring_and_smoke (3D/init_conditions.py:29-56), 64 samples
+    vf = ti.Vector.field(3, float, shape=res)
+    smf = ti.Vector.field(4, float, shape=res)
+    IC.add_vortex_ring_and_smoke(w=0.02, rad=0.2, delta=0.04, c=ti.Vector([0.45, 0.5, 0.33]),
+                                 unit_x=ti.Vector([0., 0., -1.]), unit_y=ti.Vector([0., 1., 0.]),
+                                 pf=R.X, vf=vf, smokef=smf, color=ti.Vector([1., 0.5, 0.25]), num_samples=64)
+    out["ring_u"] = vf.to_numpy()
+    out["ring_smoke"] = smf.to_numpy()
+    return out
+
+
+def ref2d_fields():
+    import taichi as ti
+    res = (32, 24)
+    R = load2d(hp2d(res))
+    import taichi_utils as TU
+    rng = np.random.default_rng(999)
+    dx = R.dx
+    nx, ny = res
+    out = {"res": np.array(res), "dx": np.float32(dx)}
+    ux = smooth_field((nx + 1, ny), rng, 0.6, dx)
+    uy = smooth_field((nx, ny + 1), rng, 0.6, dx)
+    out.update(u_x=ux, u_y=uy)
+    R.u_x.from_numpy(ux); R.u_y.from_numpy(uy)
+    # get_central_vector + curl (2D/taichi_utils.py:50-55, 96-104)
+    TU.get_central_vector(R.u_x, R.u_y, R.u)
+    out["central"] = R.u.to_numpy()
+    TU.curl(R.u, R.w, dx)
+    out["curl"] = R.w.to_numpy()
+    # advect_smoke (2D/run_2D.py:444-450)
+    smoke = np.stack([np.abs(smooth_field(res, rng, 0.8, dx)) for _ in range(3)], axis=-1).astype(np.float32)
+    out["smoke"] = smoke
+    shapes = [(nx + 1, ny), (nx, ny + 1)]
+    psi = [_face_psi(shapes[f], f, rng, dx, 2.5 * dx) for f in range(2)]
+    out.update(psi_x=psi[0], psi_y=psi[1])
+    pf = [ti.Vector.field(2, float, shape=shapes[f]) for f in range(2)]
+    for f in range(2):
+        pf[f].from_numpy(psi[f])
+    s0 = ti.Vector.field(3, float, shape=res); s0.from_numpy(smoke)
+    s1 = ti.Vector.field(3, float, shape=res)
+    R.advect_smoke(s0, s1, *pf, dx)
+    out["advect_smoke"] = s1.to_numpy()
+    return out
+
+
+def ref3d_variants():
+    """RK4_T_and_T_grad_m_forward, update_particles_imp, update_particles_grad_m and compute_dT_dx
+    (3D/run_3D.py:221-292, 353-428), whose call sites the reference's step has commented out."""
+    import taichi as ti
+    res = (12, 10, 8)
+    R = load3d(hp3d(res))
+    rng = np.random.default_rng(4242)
+    dx = R.dx
+    nx, ny, nz = res
+    out = {"res": np.array(res), "dx": np.float32(dx)}
+    ux = smooth_field((nx + 1, ny, nz), rng, 0.6, dx)
+    uy = smooth_field((nx, ny + 1, nz), rng, 0.6, dx)
+    uz = smooth_field((nx, ny, nz + 1), rng, 0.6, dx)
+    out.update(u_x=ux, u_y=uy, u_z=uz)
+    R.u_x.from_numpy(ux); R.u_y.from_numpy(uy); R.u_z.from_numpy(uz)
+    R.calc_max_speed(R.u_x, R.u_y, R.u_z)
+    dt = np.float32(0.4 * dx / float(R.max_speed[None]))
+    out["dt"] = dt
+
+    # every cell holds 8 particles (a jittered 2x2x2 lattice); interior particles (whose 4x4x4
+    # neighbour cells lie in the grid) come first, so compute_dT_dx is evaluated on them only
+    cells = np.stack(np.meshgrid(*[np.arange(r) for r in res], indexing="ij"), -1).reshape(-1, 3)
+    sub = np.stack(np.meshgrid(*[np.arange(2)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    x0 = ((cells[:, None, :] * 2 + sub[None, :, :]).reshape(-1, 3) + rng.uniform(0.05, 0.95, (cells.shape[0] * 8, 3)))
+    x0 = (x0 * (dx / 2)).astype(np.float32)
+    base = np.floor(x0 / np.float32(dx)).astype(int)
+    inner = np.all((base >= 1) & (base <= np.array(res) - 3), axis=1)
+    order = np.concatenate([np.nonzero(inner)[0], np.nonzero(~inner)[0]])
+    x0 = x0[order]
+    n_in = int(inner.sum())
+    P = x0.shape[0]
+    xc = np.clip(x0 + rng.normal(0, 0.2 * dx, x0.shape), 1e-4, np.array(res) * dx - 1e-4).astype(np.float32)
+    T = (np.eye(3)[None] + 0.05 * rng.standard_normal((P, 3, 3))).astype(np.float32)
+    T2 = (np.eye(3)[None] + 0.05 * rng.standard_normal((P, 3, 3))).astype(np.float32)
+    C0 = (0.5 * rng.standard_normal((P, 3, 3))).astype(np.float32)
+    m0 = (0.5 * rng.standard_normal((P, 3))).astype(np.float32)
+    out.update(init_pos=x0, pos=xc, T=T, T2=T2, init_C=C0, init_imp=m0, n_inner=np.int32(n_in))
+    mk = lambda: ti.Vector.field(3, float, shape=P)  # noqa: E731
+
+    # RK4_T_and_T_grad_m_forward on the current positions
+    p_f = mk(); set_vec(p_f, xc)
+    Ta = [mk() for _ in range(3)]
+    Tb = [mk() for _ in range(3)]
+    for v in range(3):
+        set_vec(Ta[v], T[:, v]); set_vec(Tb[v], T2[:, v])
+    R.RK4_T_and_T_grad_m_forward(p_f, *Ta, *Tb, R.u_x, R.u_y, R.u_z, dt)
+    out["rk4_pos"] = vec_field_np(p_f)
+    out["rk4_T"] = np.stack([vec_field_np(f) for f in Ta], axis=1)
+    out["rk4_T2"] = np.stack([vec_field_np(f) for f in Tb], axis=1)
+
+    # update_particles_imp
+    Tf = [mk() for _ in range(3)]
+    for v in range(3):
+        set_vec(Tf[v], T[:, v])
+    imp_f, m_f = mk(), mk(); set_vec(m_f, m0)
+    R.update_particles_imp(imp_f, m_f, *Tf)
+    out["update_imp"] = vec_field_np(imp_f)
+
+    # compute_dT_dx on the cell lists of the current positions (cap cell_max_particle_num).  Its
+    # inner loop ti.ndrange(0, cell_particle_num[..]) is a two-axis range whose first axis is
+    # empty, so the reference's kernel accumulates nothing and grad_T_init stays zero.
+    pc_f = mk(); set_vec(pc_f, xc)
+    R.get_particles_id_in_every_cell(R.cell_particles_id, R.cell_particle_num, pc_f)
+    x0_f = mk(); set_vec(x0_f, x0)
+    gT = [ti.Matrix.field(3, 3, float, shape=n_in) for _ in range(3)]
+    R.compute_dT_dx(*gT, *Tf, x0_f, R.cell_particles_id, R.cell_particle_num)
+    gTn = np.stack([f.to_numpy() for f in gT], axis=1)  # [n_in, r, a, b]
+    out["dT_dx"] = gTn
+    out["cap"] = np.int32(R.cell_max_particle_num)
+
+    # update_particles_grad_m with a random grad_T_init (inner particles)
+    n = n_in
+    gT_in = (0.5 * rng.standard_normal((n, 3, 3, 3))).astype(np.float32)
+    out["grad_T_init"] = gT_in
+    for r in range(3):
+        gT[r].from_numpy(gT_in[:, r])
+    mk_n = lambda: ti.Vector.field(3, float, shape=n)  # noqa: E731
+    Cf = [mk_n() for _ in range(3)]
+    iC = [mk_n() for _ in range(3)]
+    Tn = [mk_n() for _ in range(3)]
+    for v in range(3):
+        set_vec(iC[v], C0[:n, v]); set_vec(Tn[v], T[:n, v])
+    mn = mk_n(); set_vec(mn, m0[:n])
+    R.update_particles_grad_m(*Cf, *iC, *Tn, *gT, mn)
+    out["grad_m_C"] = np.stack([vec_field_np(f) for f in Cf], axis=1)
+    return out
+
+
 CASES = dict(ref3d_kernels=ref3d_kernels, ref2d_kernels=ref2d_kernels, ref3d_steps=ref3d_steps,
-             ref2d_steps=ref2d_steps)
+             ref2d_steps=ref2d_steps, ref3d_fields=ref3d_fields, ref2d_fields=ref2d_fields,
+             ref3d_variants=ref3d_variants)
 
 if __name__ == "__main__":
     name = sys.argv[1]

@@ -20,7 +20,7 @@ def _import_2d(**hp):
     if DROPIN in sys.path:
         sys.path.remove(DROPIN)
     sys.path.insert(0, DROPIN)
-    for m in ("run_2D", "run_3D", "mgpcg", "init_conditions", "hyperparameters"):
+    for m in ("run_2D", "run_3D", "mgpcg", "init_conditions", "taichi_utils", "hyperparameters"):
         sys.modules.pop(m, None)
     h = importlib.import_module("hyperparameters")
     for k, v in hp.items():
@@ -33,8 +33,10 @@ def test_dropin2d_names_match_the_reference_surface():
     assert h.dim == 2
     for name in ("calc_max_speed", "reset_to_identity", "reset_T_to_identity", "RK4_grid", "RK4_T_forward",
                  "advect_u", "stretch_T_and_advect_particles", "update_particles_imp", "update_particles_grad_m",
-                 "update_T", "P2G", "main"):
+                 "update_T", "P2G", "main", "advect_smoke", "curl", "get_central_vector"):
         assert callable(getattr(r, name)), name
+    tu = importlib.import_module("taichi_utils")
+    assert tu.__file__.startswith(DROPIN)
     m = importlib.import_module("mgpcg")
     assert hasattr(m, "MGPCG_2") and hasattr(m.MGPCG_2, "Poisson")
     ic = importlib.import_module("init_conditions")

@@ -22,7 +22,7 @@ def _import_3d(**hp):
     if DROPIN in sys.path:
         sys.path.remove(DROPIN)
     sys.path.insert(0, DROPIN)
-    for m in ("run_3D", "run_2D", "mgpcg", "init_conditions", "hyperparameters"):
+    for m in ("run_3D", "run_2D", "mgpcg", "init_conditions", "taichi_utils", "hyperparameters"):
         sys.modules.pop(m, None)
     h = importlib.import_module("hyperparameters")
     for k, v in hp.items():
@@ -36,8 +36,13 @@ def test_dropin_names_match_the_reference_surface():
                  "particles_per_cell", "use_midpoint_vel", "use_APIC", "exp_name", "total_steps"):
         assert hasattr(h, name), name
     for name in ("calc_max_speed", "reset_T_to_identity", "RK4_grid", "RK4_T_forward", "advect_u",
-                 "stretch_T_and_advect_particles", "get_particles_id_in_every_cell", "update_T", "P2G", "main"):
+                 "stretch_T_and_advect_particles", "get_particles_id_in_every_cell", "update_T", "P2G", "main",
+                 "P2G_smoke", "advect_smoke", "clamp_smoke", "RK4_T_and_T_grad_m_forward",
+                 "stretch_T_and_T_grad_m_and_advect_particles", "update_particles_imp", "update_particles_grad_m",
+                 "compute_dT_dx", "curl", "get_central_vector", "init_particles_smoke"):
         assert callable(getattr(r, name)), name
+    tu = importlib.import_module("taichi_utils")
+    assert tu.__file__.startswith(DROPIN)
     m = importlib.import_module("mgpcg")
     for name in ("init", "solve", "get_result", "Poisson", "apply_bc", "divergence", "subtract_grad_p",
                  "solve_pressure_MGPCG"):
@@ -183,3 +188,56 @@ def test_poisson_pieces_match_numpy():
     i2 = sc.mgpcg_solve(r, x2, k=1.0)
     assert i1.iterations == i2.iterations and i1.converged
     assert torch.equal(x1, -x2)
+
+
+@pytest.mark.gpu
+def test_dropin_smoke_and_variants():
+    """init_vorts_leapfrog with smoke fields adds the same velocity as without them, colours the
+    rings' cells; the drop-in smoke/variant functions equal the Scene calls they wrap."""
+    import pfm
+    _, r = _import_3d(res_x=32, res_y=16, res_z=16, particles_per_cell=8)
+    vc_a = torch.zeros((32, 16, 16, 3), device="cuda")
+    vc_b = torch.zeros_like(vc_a)
+    s1 = torch.zeros((32, 16, 16, 4), device="cuda")
+    s2 = torch.zeros_like(s1)
+    r.init_vorts_leapfrog(None, vc_a, s1, s2)
+    r.init_vorts_leapfrog(None, vc_b, None, None)
+    torch.cuda.synchronize()
+    assert torch.equal(vc_a, vc_b)
+    vals = {tuple(v) for v in s1.reshape(-1, 4).cpu().numpy().tolist()}
+    assert vals <= {(0., 0., 0., 0.), (1., 0., 0., 1.), (0., 0., 1., 1.), (1., 0., 1., 2.)}
+    assert (1., 0., 0., 1.) in vals and (0., 0., 1., 1.) in vals
+    # advect_smoke through the midpoint's backward map, against the oracle (bitwise)
+    import oracle as O
+    psi = [torch.zeros(s + (3,), device="cuda") for s in r._face_shapes]
+    r._scene().midpoint([r.u_x, r.u_y, r.u_z], [torch.zeros(s, device="cuda") for s in r._face_shapes], 0.01,
+                        psi_out=psi)
+    out = torch.zeros_like(s1)
+    r.advect_smoke(s1, out, *psi, r.dx)
+    torch.cuda.synchronize()
+    want = O.advect_smoke3(s1.cpu().numpy(), np.zeros((32, 16, 16, 4), np.float32), *(t.cpu().numpy() for t in psi),
+                           r.dx)
+    assert np.array_equal(out.cpu().numpy(), want)
+    # the particle smoke round trip: G2P then P2G_smoke
+    P = r.particle_num
+    pos = pfm.soa(pfm.jittered((32, 16, 16), r.dx, 8, seed=1))
+    sp = r.particles_smoke
+    gs = r.particles_init_grad_smoke
+    assert tuple(sp.shape) == (4, P) and tuple(gs.shape) == (3, 4, P)
+    r.init_particles_smoke(sp, gs, pos, s1, r.dx)
+    sm = torch.zeros_like(s1)
+    wgt = torch.zeros((32, 16, 16), device="cuda")
+    eye = torch.eye(3, device="cuda")[:, :, None].expand(3, 3, P).contiguous()
+    r.P2G_smoke(sp, gs, pos, sm, *eye, *eye, wgt)
+    ref = torch.zeros_like(s1)
+    wref = torch.zeros_like(wgt)
+    r._scene().p2g_smoke(sp, gs, pos, eye, eye, ref, wref)
+    torch.cuda.synchronize()
+    assert torch.equal(sm, ref) and torch.equal(wgt, wref)
+    assert float(sm.min()) >= 0 and float(sm.max()) <= 1
+    # compute_dT_dx with the reference's own (empty) inner loop gives zero
+    gx, gy, gz = (torch.ones(3, 3, P, device="cuda") for _ in range(3))
+    r.particles_pos.copy_(pos)
+    r.compute_dT_dx(gx, gy, gz, *eye, pos, r.cell_particles_id, r.cell_particle_num)
+    torch.cuda.synchronize()
+    assert not gx.any() and not gy.any() and not gz.any()

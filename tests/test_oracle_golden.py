@@ -129,3 +129,50 @@ def test_oracle_steps_3d(golden):
             T_init = np.stack([g[f"s{s}_T_{v}_init"] for v in "xyz"], 1)
             assert rel(sim.T_init, T_init) < 1e-5
     assert sim.iters == [int(i) for i in g["iters"][1:]]
+
+
+def test_oracle_fields_3d(golden):
+    """Smoke transport and diagnostics (3D/taichi_utils.py:56-85, 3D/init_conditions.py:275-279,
+    3D/run_3D.py:315-334, 554-593) against the reference's kernels on a 16x12x8 grid."""
+    g = golden("ref3d_fields")
+    dx = float(g["dx"])
+    vc = O.central_vector3(g["u_x"], g["u_y"], g["u_z"])
+    assert np.array_equal(vc, g["central"])
+    assert np.array_equal(O.curl3(vc, dx), g["curl"])
+    s, G = O.init_particles_smoke3(g["pos"], g["smoke"], dx)
+    assert rel(s, g["g2p_smoke"]) < KTOL and rel(G, g["g2p_grad_smoke"]) < KTOL
+    sm, w = O.p2g_smoke3(g["smoke_p"], g["grad_smoke"], g["pos"], g["T_gm"], g["T_init"], tuple(g["res"]), dx)
+    assert rel(w, g["p2g_smoke_w"]) < KTOL and rel(sm, g["p2g_smoke"]) < KTOL
+    psi = (g["psi_x"], g["psi_y"], g["psi_z"])
+    a = O.advect_smoke3(g["smoke"], np.zeros_like(g["smoke"]), *psi, dx)
+    assert np.array_equal(a, g["advect_smoke"])
+    c = O.advect_smoke3(g["smoke"], g["clamp_in"], *psi, dx, clamp=True)
+    assert np.array_equal(c, g["clamp_smoke"])
+
+
+def test_oracle_fields_2d(golden):
+    g = golden("ref2d_fields")
+    dx = float(g["dx"])
+    vc = O.central_vector2(g["u_x"], g["u_y"])
+    assert np.array_equal(vc, g["central"])
+    assert np.array_equal(O.curl2(vc, dx), g["curl"])
+    assert np.array_equal(O.advect_smoke2(g["smoke"], g["psi_x"], g["psi_y"], dx), g["advect_smoke"])
+
+
+def test_oracle_variants_3d(golden):
+    """RK4_T_and_T_grad_m_forward, update_particles_imp/_grad_m and compute_dT_dx
+    (3D/run_3D.py:221-292, 353-428) against the reference's kernels."""
+    g = golden("ref3d_variants")
+    dx = float(g["dx"])
+    u = (g["u_x"], g["u_y"], g["u_z"])
+    pos, T, T2 = O.rk4_T_and_T_grad_m_forward3(g["pos"], g["T"], g["T2"], *u, 1.0 / int(g["res"][1]), g["dt"])
+    assert rel(pos, g["rk4_pos"]) < KTOL and rel(T, g["rk4_T"]) < KTOL and rel(T2, g["rk4_T2"]) < KTOL
+    assert np.array_equal(O.update_imp3(g["init_imp"], g["T"]), g["update_imp"])
+    n = int(g["n_inner"])
+    # the reference's compute_dT_dx visits no list entry (ti.ndrange(0, n) is an empty 2-D range):
+    # its result is the oracle's with cap = 0
+    assert not np.any(g["dT_dx"])
+    gT = O.compute_dT_dx3(g["pos"], g["init_pos"], g["T"], tuple(g["res"]), dx, 0)
+    assert np.array_equal(gT[:n], g["dT_dx"])
+    C = O.update_grad_m3(g["init_C"][:n], g["T"][:n], g["grad_T_init"], g["init_imp"][:n])
+    assert rel(C, g["grad_m_C"]) < KTOL
