@@ -5,6 +5,12 @@
 namespace pfm {
 
 constexpr int kGThreads = 128;
+// Resident blocks per SM the 3D midpoint kernel is compiled for: 6 (80 registers, a 4-byte spill)
+// measured 4.39 ms at 256^3 against 4.43-4.86 ms uncapped (88 registers, 5 blocks) and 4.61 ms at
+// 8 (64 registers, spills).
+#ifndef PFM_MID_MINB
+#define PFM_MID_MINB 6
+#endif
 
 // calc_max_speed (3D/run_3D.py:95-103; 2D/run_2D.py:101-108).  Max is order independent, so the
 // per-block maxima are combined by the last block without atomics on floats.
@@ -69,7 +75,7 @@ __global__ void __launch_bounds__(256) k_max_speed(const float* __restrict__ ux,
 // centre X_fam (taichi_utils.py:33-46), T at the unit vector e_fam; RK4 over -dt_half with the
 // rows-form gradient (dT/dt = grad u . T); then u1 = T . u0(psi).
 template <int fam>
-__global__ void __launch_bounds__(kGThreads) k_midpoint3(MacFields3 F, MacGeom g, float dt_half,
+__global__ void __launch_bounds__(kGThreads, PFM_MID_MINB) k_midpoint3(MacFields3 F, MacGeom g, float dt_half,
                                                         float* __restrict__ u1, float* __restrict__ psi_out,
                                                         float* __restrict__ T_out) {
   const int n0 = g.n[fam][0], n1 = g.n[fam][1], n2 = g.n[fam][2];

@@ -6,6 +6,17 @@
 namespace pfm {
 
 constexpr int kPThreads = 128;
+// Block size of the RK4 kernel and the resident blocks per SM it is compiled for.  64 threads x
+// 10 blocks caps it at 96 registers (16 bytes of spills; 20 warps per SM).  Measured at 256^3 (the
+// gradient-reinit + RK4 + records kernel): 128 x 4 (128 registers) 19.2 ms, 128 x 5 18.0 ms,
+// 128 x 6 (80 registers, spills) 18.8 ms, 256 x 2 20.9 ms, 64 x 10 17.6 ms.
+#ifndef PFM_RK4_MINB
+#define PFM_RK4_MINB 10
+#endif
+#ifndef PFM_RK4_THREADS
+#define PFM_RK4_THREADS 64
+#endif
+constexpr int kRK4Threads = PFM_RK4_THREADS;
 
 // ---------------------------------------------------------------------------------------------
 // 3D
@@ -81,7 +92,7 @@ __global__ void __launch_bounds__(256) k_reset_T(float* __restrict__ T, int64_t 
 // as k_g2p3), T_init <- cols(T_gm) @ cols(T_init) (update_T, as k_update_T3) and T_gm <- I, so the
 // RK4 starts from the identity without reading T_gm back.
 template <bool PAY, bool GRADM>
-__global__ void __launch_bounds__(kPThreads, 4) k_rk4_T_forward3(float* __restrict__ pos, float* __restrict__ T,
+__global__ void __launch_bounds__(kRK4Threads, PFM_RK4_MINB) k_rk4_T_forward3(float* __restrict__ pos, float* __restrict__ T,
                                                              int64_t P, MacFields3 F, MacGeom g, float dt,
                                                              P2GRecords3 R, MacFields3 Fg) {
   int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -321,13 +332,13 @@ namespace pfm {
 int launch_rk4_T_forward3(pfm_handle* h, float* pos, float* T, const MacFields3& F, float dt, const P2GRecords3* R,
                           const MacFields3* Fg, cudaStream_t st) {
   if (h->P == 0) return PFM_OK;
-  const unsigned nb = grid_for(h->P, kPThreads);
+  const unsigned nb = grid_for(h->P, kRK4Threads);
   if (R && Fg)
-    launch(h, k_rk4_T_forward3<true, true>, nb, kPThreads, 0, st, pos, T, h->P, F, h->geom, dt, *R, *Fg);
+    launch(h, k_rk4_T_forward3<true, true>, nb, kRK4Threads, 0, st, pos, T, h->P, F, h->geom, dt, *R, *Fg);
   else if (R)
-    launch(h, k_rk4_T_forward3<true, false>, nb, kPThreads, 0, st, pos, T, h->P, F, h->geom, dt, *R, MacFields3{});
+    launch(h, k_rk4_T_forward3<true, false>, nb, kRK4Threads, 0, st, pos, T, h->P, F, h->geom, dt, *R, MacFields3{});
   else
-    launch(h, k_rk4_T_forward3<false, false>, nb, kPThreads, 0, st, pos, T, h->P, F, h->geom, dt, P2GRecords3{},
+    launch(h, k_rk4_T_forward3<false, false>, nb, kRK4Threads, 0, st, pos, T, h->P, F, h->geom, dt, P2GRecords3{},
            MacFields3{});
   return launch_check(h, "k_rk4_T_forward3");
 }
