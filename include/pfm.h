@@ -250,6 +250,89 @@ int pfm2_p2g(pfm_handle* h, const float* imp, const float* pos, const float* C, 
 int pfm2_poisson(pfm_handle* h, float* u_x, float* u_y, float* p_out, const pfm_solve_opts* opts,
                  pfm_solve_stats* stats, void* stream);
 
+/* ---- the whole step as one CUDA graph --------------------------------------------------------
+ * pfm3_step / pfm2_step run one iteration of the step loop (3D/run_3D.py:716-822,
+ * 2D/run_2D.py:772-909) as a single CUDA graph launch on `stream`, with no host synchronization:
+ * calc_max_speed, the frame clock (dt = CFL dx / max_speed clamped to the next frame, in double as
+ * the reference's Python), the reinitialisation schedule, the midpoint velocity and its projection,
+ * RK4 + P2G and the final projection all run on the device; the reinitialisations are IF nodes
+ * and each MGPCG solve is a WHILE node, so a step does exactly the work of the eager phase calls
+ * (pfm.Sim3D / Sim2D), bitwise.  The 3D step is the fused form (gradient reinitialisation + RK4
+ * + P2G records in one kernel).  The graph is captured on the first call and rebuilt only when a
+ * field pointer or a parameter changes.  The clock state (step index, sub_t, frame index) lives in
+ * the workspace: it starts at step -1 and is set by pfm_step_reset; pfm_step_info reads it and the
+ * two solves' statistics (a synchronization point).  poisson.max_iters must be >= 0 (the loop
+ * ends on the device); p_mid may be NULL (the midpoint solve then starts from zero). */
+typedef struct pfm_step_params {
+  double CFL;                 /* hyperparameters.CFL */
+  double visualize_dt;        /* hyperparameters.visualize_dt */
+  int save_frame_each_step;   /* hyperparameters.save_frame_each_step */
+  int reinit_every;           /* hyperparameters.reinit_every */
+  int reinit_every_grad_m;    /* hyperparameters.reinit_every_grad_m */
+  int use_midpoint_vel;       /* hyperparameters.use_midpoint_vel */
+  int reinit_particle_pos;    /* hyperparameters.reinit_particle_pos */
+  pfm_solve_opts poisson;     /* both projections */
+} pfm_step_params;
+
+typedef struct pfm3_step_fields {
+  float* u[3];      /* face velocity, in/out */
+  float* u_mid[3];  /* midpoint velocity (scratch) */
+  float* w[3];      /* P2G weights (scratch) */
+  float* p;         /* pressure of the final projection (warm start in, result out) */
+  float* p_mid;     /* pressure of the midpoint projection, or NULL */
+  const float* seeds;  /* [3][P] reseeding positions */
+  float* pos;       /* [3][P] */
+  float* init_imp;  /* [3][P] */
+  float* T_init;    /* [3][3][P] */
+  float* T_gm;      /* [3][3][P] */
+  float* init_C;    /* [3][3][P] */
+} pfm3_step_fields;
+
+typedef struct pfm2_step_fields {
+  float* u[2];
+  float* u_mid[2];
+  float* w[2];
+  float* psi_grid[2];  /* P2G of the reference map psi ([F][2] per family), or NULL */
+  float* p;
+  float* p_mid;
+  const float* seeds;  /* [2][P] */
+  float* pos;       /* [2][P] */
+  float* imp;       /* [2][P] */
+  float* init_imp;  /* [2][P] */
+  float* psi;       /* [2][P] */
+  float* T;         /* [2][2][P] */
+  float* T_init;    /* [2][2][P] */
+  float* T_gm;      /* [2][2][P] */
+  float* init_C;    /* [2][2][P] */
+  float* C;         /* [2][2][P] */
+} pfm2_step_fields;
+
+typedef struct pfm_step_info_t {
+  int step;           /* index i of the last step */
+  int ik;             /* step of the last reseed (the gradient schedule's origin) */
+  int frame_idx;
+  int output_frame;   /* the last step ended a frame */
+  int reinit;         /* the last step reinitialised the flow map (j == 0) */
+  int reseed;         /* ... and reseeded the particles */
+  int gradm_reinit;   /* the last step reinitialised the flow-map gradient (k == 0) */
+  double dt;          /* its dt */
+  double sub_t;
+  float max_speed;
+  int iterations[2];  /* MGPCG iterations: midpoint [0], final [1] */
+  int converged[2];
+  double rTr[2];
+  int history[64][2]; /* iterations of the two solves of step s at s % 64 (the last 64 steps) */
+} pfm_step_info_t;
+
+int pfm3_step(pfm_handle* h, const pfm3_step_fields* f, const pfm_step_params* p, void* stream);
+int pfm2_step(pfm_handle* h, const pfm2_step_fields* f, const pfm_step_params* p, void* stream);
+/* Sets the step clock: the next step is i + 1; ik, sub_t and frame_idx as the reference's loop
+ * variables (restart from a checkpoint).  pfm_step_reset(h, -1, 0, 0, 0) is a fresh start. */
+int pfm_step_reset(pfm_handle* h, int i, int ik, double sub_t, int frame_idx, void* stream);
+/* SYNCHRONIZATION POINT: the state after the last step.  Also adds the kernels the step graphs
+ * ran to pfm_launch_count. */
+int pfm_step_info(pfm_handle* h, pfm_step_info_t* info, void* stream);
+
 /* ---- the reference's alternative ("evolve m") dataflow ---------------------------------------
  * Kernels the reference defines beside its live step (their call sites in 3D/run_3D.py:795-808
  * are commented out).  grad_T_init is the three per-particle 3x3 matrices grad_T_init_x/y/z as

@@ -28,6 +28,80 @@ int require_ws(pfm_handle* h) {
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// ---- GraphCursor ------------------------------------------------------------------------------
+cudaStream_t GraphCursor::seg() {
+  if (open) return cs;
+  cudaGraph_t target = G;
+  const cudaGraphNode_t* d = deps;
+  size_t nd = ndeps;
+  if (rc) {  // keep later launches out of the stream: capture them into a graph that is dropped
+    if (!junk && cudaGraphCreate(&junk, 0) != cudaSuccess) junk = nullptr;
+    target = junk;
+    d = nullptr;
+    nd = 0;
+  }
+  const cudaError_t e = target ? cudaStreamBeginCaptureToGraph(cs, target, d, nullptr, nd, cudaStreamCaptureModeThreadLocal)
+                               : cudaErrorInvalidValue;
+  if (e != cudaSuccess) {
+    if (!rc) rc = check_cuda(h, e, "begin graph segment");
+    return cs;
+  }
+  open = true;
+  return cs;
+}
+
+void GraphCursor::close() {
+  if (!open) return;
+  cudaStreamCaptureStatus cst;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* d = nullptr;
+  size_t nd = 0;
+  const cudaError_t e = cudaStreamGetCaptureInfo(cs, &cst, nullptr, &g, &d, nullptr, &nd);
+  if (e == cudaSuccess && !junk && !rc) {
+    if (nd > sizeof(deps) / sizeof(deps[0])) {
+      rc = set_error(h, PFM_ERR_ARG, "graph segment ends in too many nodes");
+    } else {
+      for (size_t i = 0; i < nd; ++i) deps[i] = d[i];
+      ndeps = nd;
+    }
+  }
+  cudaGraph_t out = nullptr;
+  const cudaError_t e2 = cudaStreamEndCapture(cs, &out);
+  open = false;
+  if (junk) {
+    cudaGraphDestroy(junk);
+    junk = nullptr;
+  }
+  if (!rc && e != cudaSuccess) rc = check_cuda(h, e, "graph segment info");
+  if (!rc && e2 != cudaSuccess) rc = check_cuda(h, e2, "end graph segment");
+}
+
+cudaGraph_t GraphCursor::add_conditional(cudaGraphConditionalHandle cond, cudaGraphConditionalNodeType type) {
+  close();
+  if (rc) return nullptr;
+  cudaGraphNodeParams cp{};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = cond;
+  cp.conditional.type = type;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  rc = check_cuda(h, cudaGraphAddNode(&node, G, ndeps ? deps : nullptr, nullptr, ndeps, &cp), "conditional node");
+  if (rc) return nullptr;
+  deps[0] = node;
+  ndeps = 1;
+  return cp.conditional.phGraph_out[0];
+}
+
+int GraphCursor::begin_body(cudaGraph_t body) {
+  return check_cuda(h, cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+                    "begin body capture");
+}
+
+int GraphCursor::end_body() {
+  cudaGraph_t b = nullptr;
+  return check_cuda(h, cudaStreamEndCapture(cs, &b), "end body capture");
+}
+
 }  // namespace pfm
 
 using namespace pfm;
@@ -140,6 +214,7 @@ int pfm_create(const pfm_config* cfg, pfm_handle** out) {
   h->o_partials = take(kReduceBlocks * sizeof(double));
   h->o_state = take(sizeof(SolveState));
   h->o_maxpart = take(kReduceBlocks * sizeof(float) + 256);
+  h->o_step = take(sizeof(StepCtl));
 
   h->ws_need = off;
   if (cudaHostAlloc((void**)&h->h_state, sizeof(SolveState), cudaHostAllocDefault) != cudaSuccess) {
@@ -156,6 +231,7 @@ int pfm_destroy(pfm_handle* h) {
   if (!h) return PFM_ERR_NULL;
   if (h->g_setup) cudaGraphExecDestroy(h->g_setup);
   if (h->g_loop) cudaGraphExecDestroy(h->g_loop);
+  if (h->g_step) cudaGraphExecDestroy(h->g_step);
   if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
   if (h->h_state) cudaFreeHost(h->h_state);
   delete h;
@@ -173,6 +249,15 @@ int pfm_set_workspace(pfm_handle* h, void* dptr, size_t bytes) {
   if (!dptr) return set_error(h, PFM_ERR_NULL, "workspace pointer is NULL");
   if (((uintptr_t)dptr) & 255) return set_error(h, PFM_ERR_ARG, "workspace must be 256-byte aligned");
   if (bytes < h->ws_need) return set_error(h, PFM_ERR_WORKSPACE, "workspace smaller than pfm_workspace_size");
+  if (h->ws != (char*)dptr) {  // a new workspace: the captured graphs and the step clock refer to the old one
+    if (h->g_step) cudaGraphExecDestroy(h->g_step);
+    if (h->g_setup) cudaGraphExecDestroy(h->g_setup);
+    if (h->g_loop) cudaGraphExecDestroy(h->g_loop);
+    h->g_step = h->g_setup = h->g_loop = nullptr;
+    h->g_valid = 0;
+    h->step_key.clear();
+    h->step_clock_init = 0;
+  }
   h->ws = (char*)dptr;
   h->ws_bytes = bytes;
   h->rec_valid = 0;

@@ -77,7 +77,9 @@ __global__ void __launch_bounds__(256) k_max_speed(const float* __restrict__ ux,
 template <int fam>
 __global__ void __launch_bounds__(kGThreads, PFM_MID_MINB) k_midpoint3(MacFields3 F, MacGeom g, float dt_half,
                                                         float* __restrict__ u1, float* __restrict__ psi_out,
-                                                        float* __restrict__ T_out) {
+                                                        float* __restrict__ T_out,
+                                                        const float* __restrict__ dt_half_dev) {
+  if (dt_half_dev) dt_half = *dt_half_dev;  // the whole-step graph keeps dt on the device
   const int n0 = g.n[fam][0], n1 = g.n[fam][1], n2 = g.n[fam][2];
   const int64_t nf = (int64_t)n0 * n1 * n2;
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -140,7 +142,9 @@ __global__ void __launch_bounds__(kGThreads, PFM_MID_MINB) k_midpoint3(MacFields
 template <int fam>
 __global__ void __launch_bounds__(kGThreads) k_midpoint2(MacFields2 F, MacGeom g, float dt_half,
                                                         float* __restrict__ u1, float* __restrict__ psi_out,
-                                                        float* __restrict__ T_out) {
+                                                        float* __restrict__ T_out,
+                                                        const float* __restrict__ dt_half_dev) {
+  if (dt_half_dev) dt_half = *dt_half_dev;
   const int n0 = g.n[fam][0], n1 = g.n[fam][1];
   const int64_t nf = (int64_t)n0 * n1;
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -191,6 +195,33 @@ __global__ void __launch_bounds__(kGThreads) k_midpoint2(MacFields2 F, MacGeom g
   float ua[2], G[2][2];
   interp_mac2(F, g, pf, ua, G);
   u1[e] = Tf[0] * ua[0] + Tf[1] * ua[1];
+}
+
+// The midpoint kernels of every face family, dt_half from the host value or (dt_half_dev non-null)
+// from device memory.
+int launch_midpoint(pfm_handle* h, const float* const* u0, float* const* u1, float dt_half, const float* dt_half_dev,
+                    cudaStream_t st) {
+  const int D = h->cfg.dim;
+  for (int fam = 0; fam < D; ++fam) {
+    const int64_t nf = (int64_t)h->geom.n[fam][0] * h->geom.n[fam][1] * h->geom.n[fam][2];
+    const dim3 gr(grid_for(nf, kGThreads));
+    if (D == 3) {
+      const MacFields3 F{{u0[0], u0[1], u0[2]}};
+      if (fam == 0) launch(h, k_midpoint3<0>, gr, kGThreads, 0, st, F, h->geom, dt_half, u1[0], (float*)nullptr,
+                           (float*)nullptr, dt_half_dev);
+      if (fam == 1) launch(h, k_midpoint3<1>, gr, kGThreads, 0, st, F, h->geom, dt_half, u1[1], (float*)nullptr,
+                           (float*)nullptr, dt_half_dev);
+      if (fam == 2) launch(h, k_midpoint3<2>, gr, kGThreads, 0, st, F, h->geom, dt_half, u1[2], (float*)nullptr,
+                           (float*)nullptr, dt_half_dev);
+    } else {
+      const MacFields2 F{{u0[0], u0[1]}};
+      if (fam == 0) launch(h, k_midpoint2<0>, gr, kGThreads, 0, st, F, h->geom, dt_half, u1[0], (float*)nullptr,
+                           (float*)nullptr, dt_half_dev);
+      if (fam == 1) launch(h, k_midpoint2<1>, gr, kGThreads, 0, st, F, h->geom, dt_half, u1[1], (float*)nullptr,
+                           (float*)nullptr, dt_half_dev);
+    }
+  }
+  return launch_check(h, "midpoint");
 }
 
 int max_speed_async(pfm_handle* h, const float* ux, const float* uy, const float* uz, float* out,
@@ -247,9 +278,12 @@ int pfm3_midpoint(pfm_handle* h, const float* u0_x, const float* u0_y, const flo
     float* to = T_out ? T_out[fam] : nullptr;
     dim3 gr(grid_for(nf, kGThreads));
     cudaStream_t st = (cudaStream_t)stream;
-    if (fam == 0) launch(h, k_midpoint3<0>, gr, kGThreads, 0, st, F, h->geom, dt_half, outs[fam], po, to);
-    if (fam == 1) launch(h, k_midpoint3<1>, gr, kGThreads, 0, st, F, h->geom, dt_half, outs[fam], po, to);
-    if (fam == 2) launch(h, k_midpoint3<2>, gr, kGThreads, 0, st, F, h->geom, dt_half, outs[fam], po, to);
+    if (fam == 0) launch(h, k_midpoint3<0>, gr, kGThreads, 0, st, F, h->geom, dt_half, outs[fam], po, to,
+                       (const float*)nullptr);
+    if (fam == 1) launch(h, k_midpoint3<1>, gr, kGThreads, 0, st, F, h->geom, dt_half, outs[fam], po, to,
+                       (const float*)nullptr);
+    if (fam == 2) launch(h, k_midpoint3<2>, gr, kGThreads, 0, st, F, h->geom, dt_half, outs[fam], po, to,
+                       (const float*)nullptr);
     int s = launch_check(h, "k_midpoint3");
     if (s) return s;
   }
@@ -270,8 +304,10 @@ int pfm2_midpoint(pfm_handle* h, const float* u0_x, const float* u0_y, float* u1
     float* to = T_out ? T_out[fam] : nullptr;
     dim3 gr(grid_for(nf, kGThreads));
     cudaStream_t st = (cudaStream_t)stream;
-    if (fam == 0) launch(h, k_midpoint2<0>, gr, kGThreads, 0, st, F, h->geom, dt_half, outs[fam], po, to);
-    if (fam == 1) launch(h, k_midpoint2<1>, gr, kGThreads, 0, st, F, h->geom, dt_half, outs[fam], po, to);
+    if (fam == 0) launch(h, k_midpoint2<0>, gr, kGThreads, 0, st, F, h->geom, dt_half, outs[fam], po, to,
+                       (const float*)nullptr);
+    if (fam == 1) launch(h, k_midpoint2<1>, gr, kGThreads, 0, st, F, h->geom, dt_half, outs[fam], po, to,
+                       (const float*)nullptr);
     int s = launch_check(h, "k_midpoint2");
     if (s) return s;
   }

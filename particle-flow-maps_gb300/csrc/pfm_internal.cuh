@@ -65,6 +65,24 @@ __device__ __forceinline__ void split3(unsigned e, const Div32& d1, const Div32&
   i = (int)u;
 }
 
+// Device state of the whole-step graph (pfm3_step / pfm2_step): the frame clock of
+// 3D/run_3D.py:725-743 (2D/run_2D.py:782-799) in double precision, this step's dt, the reinit
+// flags, and the statistics of the step's two MGPCG solves.
+struct StepCtl {
+  double sub_t;        // time since the last frame
+  double curr_dt;      // this step's dt (CFL dx / max_speed, clamped to the frame)
+  double rTr[2];       // final r.r of the midpoint [0] and final [1] solves
+  unsigned long long kernels;  // kernels the step graphs ran since the host last read this
+  float max_speed;     // calc_max_speed of this step
+  float dt;            // f32(curr_dt)
+  float dt_half;       // f32(0.5 curr_dt)
+  int i, ik, frame_idx, output_frame;
+  int reinit, repos, gradm;
+  int iters[2];        // MGPCG iterations of the two solves
+  int done[2];         // their end codes (1 converged, 2 iteration limit, 3 non-finite)
+  int history[64][2];  // iterations of step s's two solves at s % 64
+};
+
 struct LevelDims {
   int n[3];
   int64_t count;
@@ -99,7 +117,7 @@ struct pfm_handle {
   // workspace offsets
   size_t o_key, o_slot, o_order, o_count, o_start, o_blocksums, o_payload;
   size_t o_r[pfm::kMaxLevels], o_z[pfm::kMaxLevels];
-  size_t o_x, o_p, o_Ap, o_b, o_partials, o_state, o_maxpart;
+  size_t o_x, o_p, o_Ap, o_b, o_partials, o_state, o_maxpart, o_step;
 
   // pinned host mirror of the solve state
   pfm::SolveState* h_state;
@@ -112,6 +130,10 @@ struct pfm_handle {
   int g_setup_nodes, g_body_nodes;
   double g_eps, g_tol;
   int g_mode, g_valid, g_max_iters, g_chunk, g_variant, g_true_every;
+  // whole-step graph (pfm3_step / pfm2_step), rebuilt when its fields or parameters change
+  cudaGraphExec_t g_step;
+  std::string step_key;
+  int step_clock_init;  // the step state has been initialised (pfm_step_reset or the first step)
   std::string err;
 };
 
@@ -133,6 +155,39 @@ inline void launch(pfm_handle* h, void (*kernel)(KArgs...), dim3 grid, dim3 bloc
   kernel<<<grid, block, smem, st>>>(args...);
   h->launches++;
 }
+
+// Appends work to a CUDA graph G behind a set of dependency nodes: seg() opens a stream-capture
+// segment (cudaStreamBeginCaptureToGraph) on the handle's capture stream, add_conditional()
+// closes it and adds an IF/WHILE node, capture_body() fills a conditional node's body graph.
+// The first error is kept in rc; later calls do nothing.
+struct GraphCursor {
+  pfm_handle* h;
+  cudaGraph_t G;
+  cudaStream_t cs;
+  cudaGraphNode_t deps[64];
+  size_t ndeps = 0;
+  bool open = false;
+  int rc = 0;
+  cudaGraph_t junk = nullptr;  // after an error, segments are captured here and discarded
+  uint64_t body_launches = 0;  // kernels launched into conditional bodies
+  GraphCursor(pfm_handle* hh, cudaGraph_t g, cudaStream_t s) : h(hh), G(g), cs(s) {}
+  cudaStream_t seg();
+  void close();
+  cudaGraph_t add_conditional(cudaGraphConditionalHandle cond, cudaGraphConditionalNodeType type);
+  template <class F>
+  void capture_body(cudaGraph_t body, F&& f) {
+    if (rc) return;
+    close();
+    rc = begin_body(body);
+    if (rc) return;
+    const uint64_t b0 = h->launches;
+    f(cs);
+    body_launches += h->launches - b0;
+    rc = end_body();
+  }
+  int begin_body(cudaGraph_t body);
+  int end_body();
+};
 
 inline unsigned grid_for(int64_t n, int threads) {
   int64_t b = (n + threads - 1) / threads;
@@ -382,7 +437,7 @@ __device__ __forceinline__ void write_p2g_record3(const P2GRecords3& R, int64_t 
 // of the advected particles, and with Fg non-null it first does the flow-map gradient
 // reinitialisation (init_C = grad u(p) in Fg, update_T, T_gm = I) (defined in pfm_particles.cu).
 int launch_rk4_T_forward3(pfm_handle* h, float* pos, float* T, const MacFields3& F, float dt, const P2GRecords3* R,
-                          const MacFields3* Fg, cudaStream_t st);
+                          const MacFields3* Fg, cudaStream_t st, const float* dt_dev = nullptr);
 
 // ------------------------------------------------------------------------------------------
 // 2D (2D/taichi_utils.py:214-261)
@@ -436,6 +491,19 @@ int launch_check(pfm_handle* h, const char* what);
 // r_0 of the workspace (already written).  x may be a caller buffer.
 int mgpcg_solve_in_place(pfm_handle* h, float* x, const pfm_solve_opts* opts, pfm_solve_stats* stats,
                          cudaStream_t st);
+
+// The whole-step graph's pieces (pfm_step.cu): Poisson with a device-side solve (pfm_mgpcg.cu), the
+// midpoint kernels and calc_max_speed (pfm_grid.cu), the 3D P2G tiles from records (pfm_p2g.cu),
+// the 2D RK4 (pfm_particles.cu).
+int append_poisson(GraphCursor& gc, float* const* u, float* p_io, const pfm_solve_opts& opts, StepCtl* ctl,
+                   int which);
+int launch_midpoint(pfm_handle* h, const float* const* u0, float* const* u1, float dt_half, const float* dt_half_dev,
+                    cudaStream_t st);
+int max_speed_async(pfm_handle* h, const float* ux, const float* uy, const float* uz, float* out, cudaStream_t st);
+int p2g3_from_records(pfm_handle* h, float* const* us, float* const* ws, cudaStream_t st);
+P2GRecords3 records3(pfm_handle* h, const float* init_imp, const float* T_init, const float* init_C);
+int launch_rk4_T_forward2(pfm_handle* h, float* pos, float* T, const MacFields2& F, float dt, int advect_psi,
+                          cudaStream_t st, const float* dt_dev);
 
 // Counting sort of the particle cells (pfm_p2g.cu).
 int sort_particles(pfm_handle* h, const float* pos, cudaStream_t st);

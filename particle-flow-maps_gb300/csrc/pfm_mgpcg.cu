@@ -761,150 +761,161 @@ static int run_graph(pfm_handle* h, cudaGraphExec_t exec, int nodes, cudaStream_
   return check_cuda(h, cudaGraphLaunch(exec, s), "graph launch");
 }
 
+// k_loop_begin, the WHILE node whose body is one solver iteration, and the solve's finish, appended
+// to the graph behind the cursor.  Returns the body's kernel count.
+template <class K>
+static int append_solve_loop(GraphCursor& gc, K& k) {
+  pfm_handle* h = gc.h;
+  cudaGraphConditionalHandle cond{};
+  if (!gc.rc) gc.rc = check_cuda(h, cudaGraphConditionalHandleCreate(&cond, gc.G, 0, 0), "conditional handle");
+  if (gc.rc) return 0;
+  launch(h, k_loop_begin, 1, 1, 0, gc.seg(), k.st, k.chunk, cond);
+  cudaGraph_t body = gc.add_conditional(cond, cudaGraphCondTypeWhile);
+  if (gc.rc) return 0;
+  const uint64_t b0 = h->launches;
+  gc.capture_body(body, [&](cudaStream_t q) { k.body(q, cond); });
+  const int nodes = (int)(h->launches - b0);
+  if (!gc.rc) k.finish(gc.seg());
+  return nodes;
+}
+
+// The kernels of one MGPCG.solve (3D/mgpcg.py:202-280) with level storage S (float: the reference
+// solve; __half / __nv_bfloat16: the mixed solve, which also accumulates every inner product in
+// f64), grouped as the graphs use them:
+//   setup:  x (unless warm-started) = p = Ap = 0, recenter, [b = r0, b.b, r0 = b - A x for a warm
+//           start], r0.r0, first V-cycle, p = z, z.r, and the first half of iteration 1 (Ap,
+//           alpha, x/r update, convergence test [, true residual]);
+//   body:   one WHILE iteration: the second half of iteration k and the first half of k+1, then
+//           k_loop_cond clears the loop condition once converged or at the iteration limit;
+//   finish: the final true residual (when monitored).
+template <int D, typename S>
+struct SolveKernels {
+  pfm_handle* h;
+  pfm_solve_opts o;
+  bool mixed, warm, true_res, keep_b, neu;
+  int f64, chunk, mi;
+  int64_t n;
+  double inv_n;
+  SolveState* st;
+  RedBuf rb;
+  float *r0, *x, *p, *Ap, *bvec;
+  S *z0, *rh;
+  Lvl L0;
+  BC bc;
+
+  SolveKernels(pfm_handle* hh, const pfm_solve_opts& oo) : h(hh), o(oo) {
+    mixed = sizeof(S) == 2;
+    f64 = mixed ? 1 : 0;
+    warm = o.warm_start != 0;
+    true_res = o.true_residual_every > 0;
+    keep_b = warm || true_res || o.tol_mode == 2;
+    chunk = o.max_iters >= 0 ? o.max_iters + 1 : o.check_every;
+    mi = o.max_iters;
+    n = h->cells;
+    inv_n = 1.0 / (double)n;
+    neu = all_neumann(h);
+    st = ws_ptr<SolveState>(h, h->o_state);
+    rb = RedBuf{ws_ptr<double>(h, h->o_partials), st};
+    r0 = ws_ptr<float>(h, h->o_r[0]);
+    z0 = level_z<S>(h, 0);
+    rh = mixed ? level_r<S>(h, 0) : nullptr;
+    x = ws_ptr<float>(h, h->o_x);
+    p = ws_ptr<float>(h, h->o_p);
+    Ap = ws_ptr<float>(h, h->o_Ap);
+    bvec = ws_ptr<float>(h, h->o_b);
+    L0 = lvl_of(h, 0);
+    bc = bc_of(h);
+  }
+  // recenter r0 (all-Neumann) and, in the mixed solve with `storage`, refresh its scaled
+  // level-storage copy
+  void recenter(cudaStream_t q, bool storage) {
+    S* out = (mixed && storage) ? rh : nullptr;
+    if (neu) {
+      launch(h, k_dot<float>, red_blocks(n), kReduceThreads, 0, q, (const float*)r0, (const float*)nullptr, n, rb,
+             (int)RED_MEAN, o.eps, inv_n, mi, f64);
+      launch(h, k_sub_mean<S>, stream_blocks(n), 256, 0, q, r0, out, n, (const SolveState*)st);
+    } else if (out) {
+      launch(h, k_to_storage<S>, stream_blocks(n), 256, 0, q, out, (const float*)r0, n, (const SolveState*)st);
+    }
+  }
+  void first_half(cudaStream_t q) {
+    launch(h, k_Ap_dot<D>, red_blocks(n), kReduceThreads, 0, q, (const float*)p, Ap, L0, bc, rb, o.eps, f64);
+    launch(h, k_update_xr, red_blocks(n), kReduceThreads, 0, q, x, (const float*)p, r0, (const float*)Ap, n, rb, o.tol,
+           o.tol_mode, f64, inv_n);
+    if (true_res)
+      launch(h, k_true_residual<D>, red_blocks(n), kReduceThreads, 0, q, (const float*)bvec, (const float*)x, L0, bc, rb,
+             o.true_residual_every);
+  }
+  void setup(cudaStream_t q) {
+    // init(): x = p = Ap = 0 (3D/mgpcg.py:63-79); z0 is zeroed by the V-cycle
+    cudaMemsetAsync(st, 0, sizeof(SolveState), q);
+    if (!warm) cudaMemsetAsync(x, 0, n * 4, q);
+    cudaMemsetAsync(p, 0, n * 4, q);
+    cudaMemsetAsync(Ap, 0, n * 4, q);
+    recenter(q, false);
+    if (keep_b) {
+      cudaMemcpyAsync(bvec, r0, n * 4, cudaMemcpyDeviceToDevice, q);
+      launch(h, k_dot<float>, red_blocks(n), kReduceThreads, 0, q, (const float*)bvec, (const float*)bvec, n, rb,
+             (int)RED_BTB, o.eps, inv_n, mi, 1);
+    }
+    if (warm) launch(h, k_residual<D>, stream_blocks(n), 256, 0, q, r0, (const float*)bvec, (const float*)x, L0, bc);
+    launch(h, k_dot<float>, red_blocks(n), kReduceThreads, 0, q, (const float*)r0, (const float*)r0, n, rb,
+           (int)RED_RTR0, o.eps, inv_n, mi, f64);
+    // the scaled level-storage copy of r0, once r0.r0 (and so the scale) is known
+    if (mixed) launch(h, k_to_storage<S>, stream_blocks(n), 256, 0, q, rh, (const float*)r0, n, (const SolveState*)st);
+    vcycle<D, S>(h, st, q);
+    launch(h, k_update_p<S>, stream_blocks(n), 256, 0, q, p, (const S*)z0, n, (const SolveState*)st);
+    launch(h, k_dot<S>, red_blocks(n), kReduceThreads, 0, q, (const S*)z0, (const float*)r0, n, rb, (int)RED_ZTR_INIT,
+           o.eps, inv_n, mi, f64);
+    first_half(q);
+  }
+  void body(cudaStream_t q, cudaGraphConditionalHandle cond) {
+    recenter(q, true);
+    vcycle<D, S>(h, st, q);
+    launch(h, k_dot<S>, red_blocks(n), kReduceThreads, 0, q, (const S*)z0, (const float*)r0, n, rb, (int)RED_ZTR, o.eps,
+           inv_n, mi, f64);
+    launch(h, k_update_p<S>, stream_blocks(n), 256, 0, q, p, (const S*)z0, n, (const SolveState*)st);
+    first_half(q);
+    launch(h, k_loop_cond, 1, 1, 0, q, (const SolveState*)st, cond);
+  }
+  void finish(cudaStream_t q) {
+    if (true_res)  // the final true residual of the solve
+      launch(h, k_true_residual<D>, red_blocks(n), kReduceThreads, 0, q, (const float*)bvec, (const float*)x, L0, bc, rb,
+             -1);
+  }
+};
+
 // MGPCG.solve (3D/mgpcg.py:202-280) on r_0 (already k r); the solution is left in the workspace
-// vector x.  Two graphs per handle, captured once per option set:
-//   setup: x (unless warm-started) = p = Ap = 0, recenter, [b = r0, b.b, r0 = b - A x for a warm
-//          start], r0.r0, first V-cycle, p = z, z.r, and the first half of iteration 1 (Ap,
-//          alpha, x/r update, convergence test [, true residual]);
-//   loop:  WHILE(not done and it < it_stop) { second half of iteration k, first half of k+1 },
-//          then the device state is copied to pinned host memory.
-// S is the multigrid level storage (float: the reference solve; __half / __nv_bfloat16: the
-// mixed solve, which also accumulates every inner product in f64).  With a finite max_iters one
-// loop launch finishes the solve; with max_iters = -1 the host relaunches the loop every
-// check_every iterations until the state reports convergence.
+// vector x.  Two graphs per handle, captured once per option set: the setup graph and the loop
+// graph (k_loop_begin -> WHILE(not done and it < it_stop) { body } -> finish -> the device state
+// copied to pinned host memory).  With a finite max_iters one loop launch finishes the solve;
+// with max_iters = -1 the host relaunches the loop every check_every iterations until the state
+// reports convergence.
 template <int D, typename S>
 static int solve_impl(pfm_handle* h, const pfm_solve_opts& o, pfm_solve_stats* stats, cudaStream_t s) {
-  const bool mixed = sizeof(S) == 2;
-  const int f64 = mixed ? 1 : 0;
-  const bool warm = o.warm_start != 0;
-  const bool true_res = o.true_residual_every > 0;
-  const bool keep_b = warm || true_res || o.tol_mode == 2;
-  const int chunk = o.max_iters >= 0 ? o.max_iters + 1 : o.check_every;
-  const int64_t n = h->cells;
-  SolveState* st = ws_ptr<SolveState>(h, h->o_state);
-  RedBuf rb{ws_ptr<double>(h, h->o_partials), st};
-  float* r0 = ws_ptr<float>(h, h->o_r[0]);
-  S* z0 = level_z<S>(h, 0);
-  S* rh = mixed ? level_r<S>(h, 0) : nullptr;
-  float* x = ws_ptr<float>(h, h->o_x);
-  float* p = ws_ptr<float>(h, h->o_p);
-  float* Ap = ws_ptr<float>(h, h->o_Ap);
-  float* bvec = ws_ptr<float>(h, h->o_b);
+  SolveKernels<D, S> K(h, o);
+  const int mi = K.mi;
+  const int chunk = K.chunk;
   SolveState* hs = h->h_state;
-  const Lvl L0 = lvl_of(h, 0);
-  const BC bc = bc_of(h);
-  const double inv_n = 1.0 / (double)n;
-  const bool neu = all_neumann(h);
-  const int mi = o.max_iters;
-  const int key_mode = (o.precision & 3) | (warm ? 4 : 0);
+  const int key_mode = (o.precision & 3) | (K.warm ? 4 : 0);
   if (!h->g_valid || h->g_eps != o.eps || h->g_tol != o.tol || h->g_mode != o.tol_mode || h->g_max_iters != mi ||
       h->g_chunk != chunk || h->g_variant != key_mode || h->g_true_every != o.true_residual_every) {
     if (h->g_setup) cudaGraphExecDestroy(h->g_setup);
     if (h->g_loop) cudaGraphExecDestroy(h->g_loop);
     h->g_setup = h->g_loop = nullptr;
     h->g_valid = 0;
-    // recenter r0 (all-Neumann) and, in the mixed solve with `storage`, refresh its scaled
-    // level-storage copy
-    auto recenter = [&](cudaStream_t q, bool storage) {
-      S* out = (mixed && storage) ? rh : nullptr;
-      if (neu) {
-        launch(h, k_dot<float>, red_blocks(n), kReduceThreads, 0, q, (const float*)r0, (const float*)nullptr, n, rb,
-               (int)RED_MEAN, o.eps, inv_n, mi, f64);
-        launch(h, k_sub_mean<S>, stream_blocks(n), 256, 0, q, r0, out, n, (const SolveState*)st);
-      } else if (out) {
-        launch(h, k_to_storage<S>, stream_blocks(n), 256, 0, q, out, (const float*)r0, n, (const SolveState*)st);
-      }
-    };
-    auto first_half = [&](cudaStream_t q) {
-      launch(h, k_Ap_dot<D>, red_blocks(n), kReduceThreads, 0, q, (const float*)p, Ap, L0, bc, rb, o.eps, f64);
-      launch(h, k_update_xr, red_blocks(n), kReduceThreads, 0, q, x, (const float*)p, r0, (const float*)Ap, n, rb, o.tol,
-             o.tol_mode, f64, inv_n);
-      if (true_res)
-        launch(h, k_true_residual<D>, red_blocks(n), kReduceThreads, 0, q, (const float*)bvec, (const float*)x, L0, bc,
-               rb, o.true_residual_every);
-    };
-    auto setup = [&](cudaStream_t q) {
-      // init(): x = p = Ap = 0 (3D/mgpcg.py:63-79); z0 is zeroed by the V-cycle
-      cudaMemsetAsync(st, 0, sizeof(SolveState), q);
-      if (!warm) cudaMemsetAsync(x, 0, n * 4, q);
-      cudaMemsetAsync(p, 0, n * 4, q);
-      cudaMemsetAsync(Ap, 0, n * 4, q);
-      recenter(q, false);
-      if (keep_b) {
-        cudaMemcpyAsync(bvec, r0, n * 4, cudaMemcpyDeviceToDevice, q);
-        launch(h, k_dot<float>, red_blocks(n), kReduceThreads, 0, q, (const float*)bvec, (const float*)bvec, n, rb,
-               (int)RED_BTB, o.eps, inv_n, mi, 1);
-      }
-      if (warm) launch(h, k_residual<D>, stream_blocks(n), 256, 0, q, r0, (const float*)bvec, (const float*)x, L0, bc);
-      launch(h, k_dot<float>, red_blocks(n), kReduceThreads, 0, q, (const float*)r0, (const float*)r0, n, rb,
-             (int)RED_RTR0, o.eps, inv_n, mi, f64);
-      // the scaled level-storage copy of r0, once r0.r0 (and so the scale) is known
-      if (mixed) launch(h, k_to_storage<S>, stream_blocks(n), 256, 0, q, rh, (const float*)r0, n, (const SolveState*)st);
-      vcycle<D, S>(h, st, q);
-      launch(h, k_update_p<S>, stream_blocks(n), 256, 0, q, p, (const S*)z0, n, (const SolveState*)st);
-      launch(h, k_dot<S>, red_blocks(n), kReduceThreads, 0, q, (const S*)z0, (const float*)r0, n, rb,
-             (int)RED_ZTR_INIT, o.eps, inv_n, mi, f64);
-      first_half(q);
-    };
-    int rc = capture(h, setup, &h->g_setup, &h->g_setup_nodes);
+    int rc = capture(h, [&](cudaStream_t q) { K.setup(q); }, &h->g_setup, &h->g_setup_nodes);
     if (rc) return rc;
-    // loop graph: k_loop_begin -> WHILE(cond) { body } -> state readback
-    cudaStream_t cs = h->cap_stream;
-    rc = check_cuda(h, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "begin capture");
-    if (rc) return rc;
-    cudaStreamCaptureStatus cst;
-    cudaGraph_t g = nullptr;
-    const cudaGraphNode_t* deps = nullptr;
-    size_t ndeps = 0;
-    cudaGraphConditionalHandle cond;
-    cudaGraph_t body = nullptr;
-    cudaGraphNode_t cnode;
-    const uint64_t before = h->launches;
-    rc = check_cuda(h, cudaStreamGetCaptureInfo(cs, &cst, nullptr, &g, nullptr, nullptr, nullptr), "capture info");
-    if (!rc) rc = check_cuda(h, cudaGraphConditionalHandleCreate(&cond, g, 0, 0), "conditional handle");
-    if (!rc) {
-      launch(h, k_loop_begin, 1, 1, 0, cs, st, chunk, cond);
-      rc = check_cuda(h, cudaStreamGetCaptureInfo(cs, &cst, nullptr, &g, &deps, nullptr, &ndeps), "capture info");
-    }
-    if (!rc) {
-      cudaGraphNodeParams cp{};
-      cp.type = cudaGraphNodeTypeConditional;
-      cp.conditional.handle = cond;
-      cp.conditional.type = cudaGraphCondTypeWhile;
-      cp.conditional.size = 1;
-      rc = check_cuda(h, cudaGraphAddNode(&cnode, g, deps, nullptr, ndeps, &cp), "while node");
-      if (!rc) body = cp.conditional.phGraph_out[0];
-    }
-    if (!rc)
-      rc = check_cuda(h, cudaStreamUpdateCaptureDependencies(cs, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies),
-                      "capture dependencies");
-    if (!rc && true_res)  // the final true residual of the solve
-      launch(h, k_true_residual<D>, red_blocks(n), kReduceThreads, 0, cs, (const float*)bvec, (const float*)x, L0, bc,
-             rb, -1);
-    if (!rc) cudaMemcpyAsync(hs, st, sizeof(SolveState), cudaMemcpyDeviceToHost, cs);
     cudaGraph_t top = nullptr;
-    int rc_end = check_cuda(h, cudaStreamEndCapture(cs, &top), "end capture");
-    if (rc || rc_end) {
-      if (top) cudaGraphDestroy(top);
-      h->launches = before;
-      return rc ? rc : rc_end;
-    }
-    rc = check_cuda(h, cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
-                    "begin body capture");
-    if (!rc) {
-      const uint64_t b0 = h->launches;
-      recenter(cs, true);
-      vcycle<D, S>(h, st, cs);
-      launch(h, k_dot<S>, red_blocks(n), kReduceThreads, 0, cs, (const S*)z0, (const float*)r0, n, rb, (int)RED_ZTR,
-             o.eps, inv_n, mi, f64);
-      launch(h, k_update_p<S>, stream_blocks(n), 256, 0, cs, p, (const S*)z0, n, (const SolveState*)st);
-      first_half(cs);
-      launch(h, k_loop_cond, 1, 1, 0, cs, (const SolveState*)st, cond);
-      h->g_body_nodes = (int)(h->launches - b0);
-      cudaGraph_t b2 = nullptr;
-      rc = check_cuda(h, cudaStreamEndCapture(cs, &b2), "end body capture");
-    }
+    rc = check_cuda(h, cudaGraphCreate(&top, 0), "graph create");
+    if (rc) return rc;
+    GraphCursor gc(h, top, h->cap_stream);
+    const uint64_t before = h->launches;
+    h->g_body_nodes = append_solve_loop(gc, K);
+    if (!gc.rc) cudaMemcpyAsync(hs, K.st, sizeof(SolveState), cudaMemcpyDeviceToHost, gc.seg());
+    gc.close();
     h->launches = before;
+    rc = gc.rc;
     if (!rc) rc = check_cuda(h, cudaGraphInstantiate(&h->g_loop, top, 0), "loop graph instantiate");
     cudaGraphDestroy(top);
     if (rc) return rc;
@@ -927,7 +938,7 @@ static int solve_impl(pfm_handle* h, const pfm_solve_opts& o, pfm_solve_stats* s
     if (rc) return rc;
     // kernels launched: k_loop_begin, one body per completed iteration (k_loop_cond inside), and
     // the final true-residual check
-    h->launches += 1 + (uint64_t)h->g_body_nodes * (uint64_t)(hs->it - it_before) + (true_res ? 1 : 0);
+    h->launches += 1 + (uint64_t)h->g_body_nodes * (uint64_t)(hs->it - it_before) + (K.true_res ? 1 : 0);
     it_before = hs->it;
     if (hs->done || mi >= 0) break;
   }
@@ -937,7 +948,7 @@ static int solve_impl(pfm_handle* h, const pfm_solve_opts& o, pfm_solve_stats* s
     stats->rTr = hs->rTr;
     stats->rTr0 = hs->rTr0;
     stats->bTb = hs->bTb;
-    stats->rTr_true = true_res ? hs->rTr_true : -1.0;
+    stats->rTr_true = K.true_res ? hs->rTr_true : -1.0;
   }
   if (hs->done == 3) return set_error(h, PFM_ERR_NONFINITE, "MGPCG: non-finite residual");
   if (hs->done != 1) return set_error(h, PFM_ERR_NOT_CONVERGED, "MGPCG: iteration limit reached");
@@ -1004,6 +1015,78 @@ static int poisson_impl(pfm_handle* h, float* const* u, float* p_out, const pfm_
   rc = launch_check(h, "subtract_grad_p");
   if (rc) return rc;
   return solve_rc;
+}
+
+// Records the finished solve in the step state: iterations, done code, final r.r, and the kernels
+// its WHILE body ran (iterations x body).
+__global__ void k_record_solve(StepCtl* ctl, const SolveState* st, int which, int body_nodes) {
+  ctl->iters[which] = st->done ? st->conv_it : st->it;
+  ctl->history[(ctl->i & 63)][which] = ctl->iters[which];
+  ctl->done[which] = st->done;
+  ctl->rTr[which] = st->rTr;
+  ctl->kernels += (unsigned long long)st->it * (unsigned long long)body_nodes;
+}
+
+template <int D, typename S>
+static void append_solve(GraphCursor& gc, const pfm_solve_opts& o, StepCtl* ctl, int which) {
+  SolveKernels<D, S> K(gc.h, o);
+  K.setup(gc.seg());
+  const int body = append_solve_loop(gc, K);
+  if (gc.rc) return;
+  launch(gc.h, k_record_solve, 1, 1, 0, gc.seg(), ctl, (const SolveState*)K.st, which, body);
+}
+
+// MGPCG_3/MGPCG_2.Poisson appended to a whole-step graph: apply_bc, divergence, [warm start from
+// p_io], the solve's setup, its device loop, [pressure to p_io], subtract_grad_p with the wall
+// reset.  Nothing waits on the host; the statistics go to ctl (slot `which`).
+int append_poisson(GraphCursor& gc, float* const* u, float* p_io, const pfm_solve_opts& opts, StepCtl* ctl,
+                   int which) {
+  pfm_handle* h = gc.h;
+  const int D = h->cfg.dim;
+  const MacGeom& g = h->geom;
+  pfm_solve_opts o = opts;
+  if (!p_io) o.warm_start = 0;
+  cudaStream_t q = gc.seg();
+  for (int f = 0; f < D; ++f) {
+    const int a1 = (f == 0) ? 1 : 0, a2 = (f == 2) ? 1 : 2;
+    const int64_t plane = (int64_t)g.n[f][a1] * (D == 3 ? g.n[f][a2] : 1);
+    if (D == 3)
+      launch(h, k_apply_bc<3>, grid_for(2 * plane, 256), 256, 0, q, u[f], f, g, h->cfg.boundary[f][0] == 2,
+             h->cfg.boundary[f][1] == 2);
+    else
+      launch(h, k_apply_bc<2>, grid_for(2 * plane, 256), 256, 0, q, u[f], f, g, h->cfg.boundary[f][0] == 2,
+             h->cfg.boundary[f][1] == 2);
+  }
+  float* r0 = ws_ptr<float>(h, h->o_r[0]);
+  float* x = ws_ptr<float>(h, h->o_x);
+  if (D == 3)
+    launch(h, k_divergence<3>, grid_for(h->cells, 256), 256, 0, q, u[0], u[1], u[2], lvl_of(h, 0), r0, -1.f);
+  else
+    launch(h, k_divergence<2>, grid_for(h->cells, 256), 256, 0, q, u[0], u[1], (const float*)nullptr, lvl_of(h, 0), r0,
+           -1.f);
+  if (o.warm_start) cudaMemcpyAsync(x, p_io, h->cells * 4, cudaMemcpyDeviceToDevice, q);
+  if (D == 3) {
+    if (o.precision == 1) append_solve<3, __half>(gc, o, ctl, which);
+    else if (o.precision == 2) append_solve<3, __nv_bfloat16>(gc, o, ctl, which);
+    else append_solve<3, float>(gc, o, ctl, which);
+  } else {
+    if (o.precision == 1) append_solve<2, __half>(gc, o, ctl, which);
+    else if (o.precision == 2) append_solve<2, __nv_bfloat16>(gc, o, ctl, which);
+    else append_solve<2, float>(gc, o, ctl, which);
+  }
+  if (gc.rc) return gc.rc;
+  q = gc.seg();
+  if (p_io) cudaMemcpyAsync(p_io, x, h->cells * 4, cudaMemcpyDeviceToDevice, q);
+  for (int f = 0; f < D; ++f) {
+    const int64_t nf = (int64_t)g.n[f][0] * g.n[f][1] * g.n[f][2];
+    const int lo = h->cfg.boundary[f][0] == 2, hi = h->cfg.boundary[f][1] == 2;
+    if (D == 3 && f == 0) launch(h, k_subtract_grad_p<3, 0>, grid_for(nf, 256), 256, 0, q, u[f], (const float*)x, g, lo, hi);
+    if (D == 3 && f == 1) launch(h, k_subtract_grad_p<3, 1>, grid_for(nf, 256), 256, 0, q, u[f], (const float*)x, g, lo, hi);
+    if (D == 3 && f == 2) launch(h, k_subtract_grad_p<3, 2>, grid_for(nf, 256), 256, 0, q, u[f], (const float*)x, g, lo, hi);
+    if (D == 2 && f == 0) launch(h, k_subtract_grad_p<2, 0>, grid_for(nf, 256), 256, 0, q, u[f], (const float*)x, g, lo, hi);
+    if (D == 2 && f == 1) launch(h, k_subtract_grad_p<2, 1>, grid_for(nf, 256), 256, 0, q, u[f], (const float*)x, g, lo, hi);
+  }
+  return gc.rc;
 }
 
 }  // namespace pfm

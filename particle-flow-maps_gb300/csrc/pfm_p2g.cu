@@ -693,14 +693,14 @@ static int copy_sort_out(pfm_handle* h, int* cell_count, int* order, cudaStream_
   return PFM_OK;
 }
 
-static P2GRecords3 records3(pfm_handle* h, const float* init_imp, const float* T_init, const float* init_C) {
+P2GRecords3 records3(pfm_handle* h, const float* init_imp, const float* T_init, const float* init_C) {
   float4* pos4 = ws_ptr<float4>(h, h->o_payload);
   return P2GRecords3{init_imp, T_init, init_C, pos4, pos4 + h->P, ws_ptr<int>(h, h->o_key), ws_ptr<int>(h, h->o_slot),
                      ws_ptr<int>(h, h->o_count)};
 }
 
 // P2G from records and keys already in the workspace: bin sort, tiles, normalisation.
-static int p2g3_from_records(pfm_handle* h, float* const* us, float* const* ws, cudaStream_t st) {
+int p2g3_from_records(pfm_handle* h, float* const* us, float* const* ws, cudaStream_t st) {
   int rc = sort_from_keys(h, st);
   if (rc) return rc;
   const float4* pos4 = ws_ptr<float4>(h, h->o_payload);

@@ -94,9 +94,11 @@ __global__ void __launch_bounds__(256) k_reset_T(float* __restrict__ T, int64_t 
 template <bool PAY, bool GRADM>
 __global__ void __launch_bounds__(kRK4Threads, PFM_RK4_MINB) k_rk4_T_forward3(float* __restrict__ pos, float* __restrict__ T,
                                                              int64_t P, MacFields3 F, MacGeom g, float dt,
-                                                             P2GRecords3 R, MacFields3 Fg) {
+                                                             P2GRecords3 R, MacFields3 Fg,
+                                                             const float* __restrict__ dt_dev) {
   int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= P) return;
+  if (dt_dev) dt = *dt_dev;  // the whole-step graph keeps dt on the device
   float p0[3] = {pos[q], pos[P + q], pos[2 * P + q]};
   float T0[3][3];
   if (GRADM) {
@@ -218,9 +220,10 @@ __global__ void __launch_bounds__(kPThreads) k_g2p2(const float* __restrict__ po
 // RK4_T_forward 2D (2D/run_2D.py:304-341): interp_u_MAC_grad (rows) then grad^T @ T.
 __global__ void __launch_bounds__(kPThreads) k_rk4_T_forward2(float* __restrict__ pos, float* __restrict__ T,
                                                              int64_t P, MacFields2 F, MacGeom g, float dt,
-                                                             int advect_psi) {
+                                                             int advect_psi, const float* __restrict__ dt_dev) {
   int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= P) return;
+  if (dt_dev) dt = *dt_dev;
   float p0[2] = {pos[q], pos[P + q]};
   float T0[2][2] = {{T[q], T[P + q]}, {T[2 * P + q], T[3 * P + q]}};
   float pk[2] = {p0[0], p0[1]};
@@ -330,17 +333,26 @@ using namespace pfm;
 namespace pfm {
 
 int launch_rk4_T_forward3(pfm_handle* h, float* pos, float* T, const MacFields3& F, float dt, const P2GRecords3* R,
-                          const MacFields3* Fg, cudaStream_t st) {
+                          const MacFields3* Fg, cudaStream_t st, const float* dt_dev) {
   if (h->P == 0) return PFM_OK;
   const unsigned nb = grid_for(h->P, kRK4Threads);
   if (R && Fg)
-    launch(h, k_rk4_T_forward3<true, true>, nb, kRK4Threads, 0, st, pos, T, h->P, F, h->geom, dt, *R, *Fg);
+    launch(h, k_rk4_T_forward3<true, true>, nb, kRK4Threads, 0, st, pos, T, h->P, F, h->geom, dt, *R, *Fg, dt_dev);
   else if (R)
-    launch(h, k_rk4_T_forward3<true, false>, nb, kRK4Threads, 0, st, pos, T, h->P, F, h->geom, dt, *R, MacFields3{});
+    launch(h, k_rk4_T_forward3<true, false>, nb, kRK4Threads, 0, st, pos, T, h->P, F, h->geom, dt, *R, MacFields3{},
+           dt_dev);
   else
     launch(h, k_rk4_T_forward3<false, false>, nb, kRK4Threads, 0, st, pos, T, h->P, F, h->geom, dt, P2GRecords3{},
-           MacFields3{});
+           MacFields3{}, dt_dev);
   return launch_check(h, "k_rk4_T_forward3");
+}
+
+int launch_rk4_T_forward2(pfm_handle* h, float* pos, float* T, const MacFields2& F, float dt, int advect_psi,
+                          cudaStream_t st, const float* dt_dev) {
+  if (h->P == 0) return PFM_OK;
+  launch(h, k_rk4_T_forward2, grid_for(h->P, kPThreads), kPThreads, 0, st, pos, T, h->P, F, h->geom, dt, advect_psi,
+         dt_dev);
+  return launch_check(h, "k_rk4_T_forward2");
 }
 
 }  // namespace pfm
@@ -405,7 +417,7 @@ int pfm2_rk4_T_forward(pfm_handle* h, float* pos, float* T, const float* u_x, co
   if (h->P == 0) return PFM_OK;
   MacFields2 F{{u_x, u_y}};
   launch(h, k_rk4_T_forward2, grid_for(h->P, kPThreads), kPThreads, 0, (cudaStream_t)stream, pos, T, h->P, F, h->geom,
-                                                                                       dt, advect_psi);
+         dt, advect_psi, (const float*)nullptr);
   return launch_check(h, "k_rk4_T_forward2");
 }
 

@@ -1,0 +1,401 @@
+// The whole time step as one CUDA graph (the loop body of 3D/run_3D.py:716-822 and
+// 2D/run_2D.py:772-909).  The step's decisions are made on the device, so nothing waits on the
+// host between phases:
+//   * calc_max_speed writes max_speed to the step state and k_step_control runs the reference's
+//     frame clock in double precision (curr_dt = CFL dx / max_speed, clamped to the next frame),
+//     advances the step index and sets the graph's IF conditions: reinitialise this step (j == 0),
+//     reseed the positions, reinitialise the flow-map gradient (k == 0);
+//   * the kernels take dt from the step state (dt, dt_half), the reinitialisations run inside IF
+//     nodes, and each MGPCG solve is its setup followed by a WHILE node whose body is one solver
+//     iteration (the same kernels as the eager solve, so the results are bitwise the same).
+// The graph is built on the first call and rebuilt only when the fields or parameters change.
+#include <cstring>
+#include <string>
+
+#include "pfm_internal.cuh"
+
+namespace pfm {
+
+struct StepParams {
+  double CFL, dx, visualize_dt;
+  int save_each, reinit_every, grad_m, repos_always, dim;
+  int else_branch;  // the graph has an IF node on "not k == 0" (3D: RK4 without the gradient reinit)
+};
+
+// The frame clock (DtClock of the step loop, 3D/run_3D.py:725-743), the reinit schedule and the
+// IF conditions of this step.  One thread.
+__global__ void k_step_control(StepCtl* c, StepParams prm, cudaGraphConditionalHandle h_repos,
+                               cudaGraphConditionalHandle h_reinit, cudaGraphConditionalHandle h_gradm,
+                               cudaGraphConditionalHandle h_nogradm, unsigned long long fixed_kernels,
+                               unsigned n_repos, unsigned n_reinit, unsigned n_gradm, unsigned n_nogradm) {
+  const int i = c->i + 1;
+  c->i = i;
+  const int j = i % prm.reinit_every;
+  double curr_dt = prm.CFL * prm.dx / (double)c->max_speed;
+  int out = 0;
+  if (prm.save_each) {
+    c->frame_idx += 1;
+    out = 1;
+  } else if (c->sub_t + curr_dt >= prm.visualize_dt) {
+    curr_dt = prm.visualize_dt - c->sub_t;
+    c->sub_t = 0.0;
+    c->frame_idx += 1;
+    out = 1;
+  } else {
+    c->sub_t += curr_dt;
+  }
+  c->curr_dt = curr_dt;
+  c->dt = (float)curr_dt;
+  c->dt_half = (float)(0.5 * curr_dt);
+  c->output_frame = out;
+  const int reinit = j == 0;
+  const int repos = reinit && (prm.repos_always || i == 0);
+  // 3D restarts the gradient schedule only when it reseeds (3D/run_3D.py:753-758); 2D at every
+  // reinitialisation (2D/run_2D.py:812-818)
+  if (prm.dim == 3 ? repos : reinit) c->ik = i;
+  const int gradm = ((i - c->ik) % prm.grad_m) == 0;
+  c->reinit = reinit;
+  c->repos = repos;
+  c->gradm = gradm;
+  cudaGraphSetConditional(h_repos, repos ? 1u : 0u);
+  cudaGraphSetConditional(h_reinit, reinit ? 1u : 0u);
+  cudaGraphSetConditional(h_gradm, gradm ? 1u : 0u);
+  if (prm.else_branch) cudaGraphSetConditional(h_nogradm, gradm ? 0u : 1u);
+  c->kernels += fixed_kernels + (repos ? n_repos : 0u) + (reinit ? n_reinit : 0u) + (gradm ? n_gradm : n_nogradm);
+}
+
+__global__ void __launch_bounds__(256) k_copy_f32(float* __restrict__ dst, const float* __restrict__ src, int64_t n) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n) dst[e] = src[e];
+}
+
+__global__ void k_step_clock_set(StepCtl* c, int i, int ik, double sub_t, int frame_idx) {
+  c->i = i;
+  c->ik = ik;
+  c->sub_t = sub_t;
+  c->frame_idx = frame_idx;
+}
+
+static int copy_launch(pfm_handle* h, float* dst, const float* src, int64_t n, cudaStream_t q) {
+  if (n > 0) launch(h, k_copy_f32, grid_for(n, 256), 256, 0, q, dst, src, n);
+  return PFM_OK;
+}
+
+static int ensure_cap_stream(pfm_handle* h) {
+  if (h->cap_stream) return PFM_OK;
+  return check_cuda(h, cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking), "capture stream");
+}
+
+static int check_step_params(pfm_handle* h, const pfm_step_params* p) {
+  if (!p) return set_error(h, PFM_ERR_NULL, "step: null parameters");
+  if (p->reinit_every < 1 || p->reinit_every_grad_m < 1)
+    return set_error(h, PFM_ERR_ARG, "step: reinit_every and reinit_every_grad_m must be >= 1");
+  if (!(p->CFL > 0.0) || !(p->visualize_dt > 0.0)) return set_error(h, PFM_ERR_ARG, "step: CFL and visualize_dt must be > 0");
+  if (p->poisson.max_iters < 0)
+    return set_error(h, PFM_ERR_ARG, "step: the device solve needs a finite max_iters (the host does not relaunch it)");
+  if (p->poisson.tol_mode < 0 || p->poisson.tol_mode > 2 || p->poisson.precision < 0 || p->poisson.precision > 2)
+    return set_error(h, PFM_ERR_ARG, "step: tol_mode must be 0..2 and precision 0..2");
+  return PFM_OK;
+}
+
+static StepParams step_params(const pfm_handle* h, const pfm_step_params* p) {
+  return StepParams{p->CFL, h->cfg.dx, p->visualize_dt, p->save_frame_each_step, p->reinit_every,
+                    p->reinit_every_grad_m, p->reinit_particle_pos, h->cfg.dim, h->cfg.dim == 3 ? 1 : 0};
+}
+
+static int init_clock(pfm_handle* h, cudaStream_t s) {
+  StepCtl* ctl = ws_ptr<StepCtl>(h, h->o_step);
+  int rc = check_cuda(h, cudaMemsetAsync(ctl, 0, sizeof(StepCtl), s), "step state");
+  if (rc) return rc;
+  launch(h, k_step_clock_set, 1, 1, 0, s, ctl, -1, 0, 0.0, 0);
+  h->step_clock_init = 1;
+  return launch_check(h, "k_step_clock_set");
+}
+
+// Builds the step graph: `emit` appends the phases between the control kernel and the end.
+template <class Emit>
+static int build_step_graph(pfm_handle* h, const pfm_step_params* p, Emit&& emit) {
+  int rc = ensure_cap_stream(h);
+  if (rc) return rc;
+  StepCtl* ctl = ws_ptr<StepCtl>(h, h->o_step);
+  cudaGraph_t G = nullptr;
+  rc = check_cuda(h, cudaGraphCreate(&G, 0), "graph create");
+  if (rc) return rc;
+  const uint64_t before = h->launches;
+  GraphCursor gc(h, G, h->cap_stream);
+  // one handle per IF node (a handle without a node does not instantiate)
+  cudaGraphConditionalHandle c_repos{}, c_reinit{}, c_gradm{}, c_nogradm{};
+  for (cudaGraphConditionalHandle* c : {&c_repos, &c_reinit, &c_gradm, &c_nogradm})
+    if (!gc.rc && (c != &c_nogradm || step_params(h, p).else_branch))
+      gc.rc = check_cuda(h, cudaGraphConditionalHandleCreate(c, G, 0, 0), "conditional handle");
+  // The control kernel is captured first with zero kernel counts; once the phases are emitted
+  // (and so counted) its node parameters are set to the real counts.
+  cudaGraphNode_t ctl_node = nullptr;
+  unsigned long long fixed = 0;
+  unsigned counts[4] = {0, 0, 0, 0};
+  if (!gc.rc) emit(gc, ctl, c_repos, c_reinit, c_gradm, c_nogradm, &ctl_node, counts, step_params(h, p));
+  gc.close();
+  // top-level kernels: all that were launched but the conditional and loop bodies (the loops count
+  // their iterations on the device, the IF bodies are counted by the control kernel)
+  fixed = (h->launches - before) - gc.body_launches;
+  h->launches = before;
+  rc = gc.rc;
+  if (!rc && ctl_node) {  // the control kernel's kernel counts, known only now
+    cudaKernelNodeParams kp{};
+    rc = check_cuda(h, cudaGraphKernelNodeGetParams(ctl_node, &kp), "control node params");
+    if (!rc) {
+      StepParams prm = step_params(h, p);
+      void* args[] = {&ctl, &prm, &c_repos, &c_reinit, &c_gradm, &c_nogradm, &fixed,
+                      &counts[0], &counts[1], &counts[2], &counts[3]};
+      kp.kernelParams = args;
+      kp.extra = nullptr;
+      rc = check_cuda(h, cudaGraphKernelNodeSetParams(ctl_node, &kp), "control node params");
+    }
+  }
+  if (h->g_step) cudaGraphExecDestroy(h->g_step);
+  h->g_step = nullptr;
+  if (!rc) rc = check_cuda(h, cudaGraphInstantiate(&h->g_step, G, 0), "step graph instantiate");
+  cudaGraphDestroy(G);
+  return rc;
+}
+
+// max_speed + control: the first segment of every step graph; returns the control kernel's node.
+static cudaGraphNode_t emit_head(GraphCursor& gc, StepCtl* ctl, const float* u0, const float* u1, const float* u2,
+                                 const StepParams& prm, cudaGraphConditionalHandle c_repos,
+                                 cudaGraphConditionalHandle c_reinit, cudaGraphConditionalHandle c_gradm,
+                                 cudaGraphConditionalHandle c_nogradm) {
+  pfm_handle* h = gc.h;
+  cudaStream_t q = gc.seg();
+  max_speed_async(h, u0, u1, u2, &ctl->max_speed, q);
+  launch(h, k_step_control, 1, 1, 0, q, ctl, prm, c_repos, c_reinit, c_gradm, c_nogradm, 0ull, 0u, 0u, 0u, 0u);
+  gc.close();
+  return gc.ndeps == 1 ? gc.deps[0] : nullptr;
+}
+
+// Kernels launched by `f` into the body of an IF node on `cond`.
+template <class F>
+static unsigned emit_if(GraphCursor& gc, cudaGraphConditionalHandle cond, F&& f) {
+  cudaGraph_t body = gc.add_conditional(cond, cudaGraphCondTypeIf);
+  if (gc.rc) return 0;
+  const uint64_t b0 = gc.h->launches;
+  gc.capture_body(body, [&](cudaStream_t q) { f(q); });
+  return (unsigned)(gc.h->launches - b0);
+}
+
+// The step graph's key: every pointer and parameter it bakes in, member by member (no padding).
+struct KeyBuf {
+  std::string s;
+  template <class T>
+  KeyBuf& operator<<(const T& v) {
+    s.append(reinterpret_cast<const char*>(&v), sizeof(T));
+    return *this;
+  }
+};
+
+static void key_params(KeyBuf& k, const pfm_step_params* p) {
+  const pfm_solve_opts& o = p->poisson;
+  k << p->CFL << p->visualize_dt << p->save_frame_each_step << p->reinit_every << p->reinit_every_grad_m
+    << p->use_midpoint_vel << p->reinit_particle_pos << o.max_iters << o.eps << o.tol << o.tol_mode << o.precision
+    << o.warm_start << o.true_residual_every;
+}
+
+static bool same_key(pfm_handle* h, const std::string& k) {
+  if (h->g_step && k == h->step_key) return true;
+  h->step_key = k;
+  return false;
+}
+
+}  // namespace pfm
+
+using namespace pfm;
+
+extern "C" {
+
+int pfm3_step(pfm_handle* h, const pfm3_step_fields* f, const pfm_step_params* p, void* stream) {
+  if (!h) return PFM_ERR_NULL;
+  if (h->cfg.dim != 3) return set_error(h, PFM_ERR_SHAPE, "pfm3_step on a 2D handle");
+  if (!f) return set_error(h, PFM_ERR_NULL, "pfm3_step: null fields");
+  int rc = check_step_params(h, p);
+  if (rc) return rc;
+  rc = require_ws(h);
+  if (rc) return rc;
+  for (int a = 0; a < 3; ++a)
+    if (!f->u[a] || !f->w[a] || (p->use_midpoint_vel && !f->u_mid[a]))
+      return set_error(h, PFM_ERR_NULL, "pfm3_step: null grid");
+  if (!f->p) return set_error(h, PFM_ERR_NULL, "pfm3_step: null pressure");
+  if (h->P > 0 && (!f->seeds || !f->pos || !f->init_imp || !f->T_init || !f->T_gm || !f->init_C))
+    return set_error(h, PFM_ERR_NULL, "pfm3_step: null particle field");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!h->step_clock_init) {
+    rc = init_clock(h, s);
+    if (rc) return rc;
+  }
+  KeyBuf key;
+  key << 3;
+  for (int a = 0; a < 3; ++a) key << f->u[a] << f->u_mid[a] << f->w[a];
+  key << f->p << f->p_mid << f->seeds << f->pos << f->init_imp << f->T_init << f->T_gm << f->init_C;
+  key_params(key, p);
+  if (!same_key(h, key.s)) {
+    rc = build_step_graph(h, p, [&](GraphCursor& gc, StepCtl* ctl, cudaGraphConditionalHandle c_repos,
+                                    cudaGraphConditionalHandle c_reinit, cudaGraphConditionalHandle c_gradm,
+                                    cudaGraphConditionalHandle c_nogradm, cudaGraphNode_t* ctl_node, unsigned* counts,
+                                    const StepParams& prm) {
+      *ctl_node = emit_head(gc, ctl, f->u[0], f->u[1], f->u[2], prm, c_repos, c_reinit, c_gradm, c_nogradm);
+      const int64_t P = h->P;
+      // j == 0: reseed (run_3D.py:753-757), G2P of the impulse, T_init = T_gm = I (:759-764)
+      counts[0] = emit_if(gc, c_repos, [&](cudaStream_t q) { copy_launch(h, f->pos, f->seeds, 3 * P, q); });
+      counts[1] = emit_if(gc, c_reinit, [&](cudaStream_t q) {
+        pfm3_g2p(h, f->pos, f->u[0], f->u[1], f->u[2], f->init_imp, nullptr, q);
+        pfm3_reset_T(h, f->T_init, q);
+        pfm3_reset_T(h, f->T_gm, q);
+      });
+      const float* ua[3] = {f->u[0], f->u[1], f->u[2]};
+      if (p->use_midpoint_vel) {  // midpoint velocity and its projection (run_3D.py:779-788)
+        launch_midpoint(h, f->u, f->u_mid, 0.f, &ctl->dt_half, gc.seg());
+        append_poisson(gc, f->u_mid, f->p_mid, p->poisson, ctl, 0);
+        for (int a = 0; a < 3; ++a) ua[a] = f->u_mid[a];
+      }
+      // RK4_T_forward + the P2G records, with the k == 0 gradient reinitialisation in the same kernel
+      cudaMemsetAsync(ws_ptr<int>(h, h->o_count), 0, h->cells * 4, gc.seg());
+      const P2GRecords3 R = records3(h, f->init_imp, f->T_init, f->init_C);
+      const MacFields3 F{{ua[0], ua[1], ua[2]}}, Fg{{f->u[0], f->u[1], f->u[2]}};
+      counts[2] = emit_if(gc, c_gradm, [&](cudaStream_t q) {
+        launch_rk4_T_forward3(h, f->pos, f->T_gm, F, 0.f, &R, &Fg, q, &ctl->dt);
+      });
+      counts[3] = emit_if(gc, c_nogradm, [&](cudaStream_t q) {
+        launch_rk4_T_forward3(h, f->pos, f->T_gm, F, 0.f, &R, nullptr, q, &ctl->dt);
+      });
+      p2g3_from_records(h, f->u, f->w, gc.seg());
+      append_poisson(gc, f->u, f->p, p->poisson, ctl, 1);
+    });
+    if (rc) {
+      h->step_key.clear();
+      return rc;
+    }
+    h->rec_valid = 1;
+  }
+  return check_cuda(h, cudaGraphLaunch(h->g_step, s), "step graph launch");
+}
+
+int pfm2_step(pfm_handle* h, const pfm2_step_fields* f, const pfm_step_params* p, void* stream) {
+  if (!h) return PFM_ERR_NULL;
+  if (h->cfg.dim != 2) return set_error(h, PFM_ERR_SHAPE, "pfm2_step on a 3D handle");
+  if (!f) return set_error(h, PFM_ERR_NULL, "pfm2_step: null fields");
+  int rc = check_step_params(h, p);
+  if (rc) return rc;
+  rc = require_ws(h);
+  if (rc) return rc;
+  for (int a = 0; a < 2; ++a)
+    if (!f->u[a] || !f->w[a] || (p->use_midpoint_vel && !f->u_mid[a]))
+      return set_error(h, PFM_ERR_NULL, "pfm2_step: null grid");
+  if (!f->p) return set_error(h, PFM_ERR_NULL, "pfm2_step: null pressure");
+  if (h->P > 0 && (!f->seeds || !f->pos || !f->imp || !f->init_imp || !f->psi || !f->T || !f->T_init || !f->T_gm ||
+                   !f->init_C || !f->C))
+    return set_error(h, PFM_ERR_NULL, "pfm2_step: null particle field");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!h->step_clock_init) {
+    rc = init_clock(h, s);
+    if (rc) return rc;
+  }
+  KeyBuf key;
+  key << 2;
+  for (int a = 0; a < 2; ++a) key << f->u[a] << f->u_mid[a] << f->w[a] << f->psi_grid[a];
+  key << f->p << f->p_mid << f->seeds << f->pos << f->imp << f->init_imp << f->psi << f->T << f->T_init << f->T_gm
+      << f->init_C << f->C;
+  key_params(key, p);
+  if (!same_key(h, key.s)) {
+    rc = build_step_graph(h, p, [&](GraphCursor& gc, StepCtl* ctl, cudaGraphConditionalHandle c_repos,
+                                    cudaGraphConditionalHandle c_reinit, cudaGraphConditionalHandle c_gradm,
+                                    cudaGraphConditionalHandle c_nogradm, cudaGraphNode_t* ctl_node, unsigned* counts,
+                                    const StepParams& prm) {
+      *ctl_node = emit_head(gc, ctl, f->u[0], f->u[1], nullptr, prm, c_repos, c_reinit, c_gradm, c_nogradm);
+      const int64_t P = h->P;
+      // j == 0 (2D/run_2D.py:812-832): reseed, imp = init_imp = u(pos), psi = pos, T = T_init = I
+      counts[0] = emit_if(gc, c_repos, [&](cudaStream_t q) { copy_launch(h, f->pos, f->seeds, 2 * P, q); });
+      counts[1] = emit_if(gc, c_reinit, [&](cudaStream_t q) {
+        pfm2_g2p(h, f->pos, f->u[0], f->u[1], f->imp, nullptr, q);
+        copy_launch(h, f->init_imp, f->imp, 2 * P, q);
+        copy_launch(h, f->psi, f->pos, 2 * P, q);
+        pfm2_reset_T(h, f->T, q);
+        pfm2_reset_T(h, f->T_init, q);
+      });
+      // k == 0 (2D/run_2D.py:834-843): init_C = grad u(pos), T_gm = I, T_init = T
+      counts[2] = emit_if(gc, c_gradm, [&](cudaStream_t q) {
+        pfm2_g2p(h, f->pos, f->u[0], f->u[1], nullptr, f->init_C, q);
+        pfm2_reset_T(h, f->T_gm, q);
+        copy_launch(h, f->T_init, f->T, 4 * P, q);
+      });
+      counts[3] = 0;
+      float* ua[2] = {f->u[0], f->u[1]};
+      if (p->use_midpoint_vel) {  // 2D/run_2D.py:866-872
+        launch_midpoint(h, f->u, f->u_mid, 0.f, &ctl->dt_half, gc.seg());
+        append_poisson(gc, f->u_mid, f->p_mid, p->poisson, ctl, 0);
+        ua[0] = f->u_mid[0];
+        ua[1] = f->u_mid[1];
+      }
+      // RK4 of positions and T_gm, then the 2D updates and P2G (2D/run_2D.py:875-905)
+      cudaStream_t q = gc.seg();
+      const MacFields2 F{{ua[0], ua[1]}};
+      launch_rk4_T_forward2(h, f->pos, f->T_gm, F, 0.f, 1, q, &ctl->dt);
+      pfm2_update_grad_m(h, f->C, f->init_C, f->T_gm, q);
+      pfm2_update_T(h, f->T, f->T_init, f->T_gm, q);
+      pfm2_update_imp(h, f->imp, f->init_imp, f->T, q);
+      pfm2_p2g(h, f->imp, f->pos, f->C, f->psi, f->u[0], f->u[1], f->psi_grid[0], f->psi_grid[1], f->w[0], f->w[1], q);
+      append_poisson(gc, f->u, f->p, p->poisson, ctl, 1);
+    });
+    if (rc) {
+      h->step_key.clear();
+      return rc;
+    }
+  }
+  return check_cuda(h, cudaGraphLaunch(h->g_step, s), "step graph launch");
+}
+
+int pfm_step_reset(pfm_handle* h, int i, int ik, double sub_t, int frame_idx, void* stream) {
+  if (!h) return PFM_ERR_NULL;
+  int rc = require_ws(h);
+  if (rc) return rc;
+  StepCtl* ctl = ws_ptr<StepCtl>(h, h->o_step);
+  cudaStream_t s = (cudaStream_t)stream;
+  rc = check_cuda(h, cudaMemsetAsync(ctl, 0, sizeof(StepCtl), s), "step state");
+  if (rc) return rc;
+  launch(h, k_step_clock_set, 1, 1, 0, s, ctl, i, ik, sub_t, frame_idx);
+  h->step_clock_init = 1;
+  return launch_check(h, "k_step_clock_set");
+}
+
+int pfm_step_info(pfm_handle* h, pfm_step_info_t* info, void* stream) {
+  if (!h || !info) return PFM_ERR_NULL;
+  int rc = require_ws(h);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  StepCtl c;
+  StepCtl* ctl = ws_ptr<StepCtl>(h, h->o_step);
+  rc = check_cuda(h, cudaMemcpyAsync(&c, ctl, sizeof(StepCtl), cudaMemcpyDeviceToHost, s), "step state read");
+  if (!rc) rc = check_cuda(h, cudaStreamSynchronize(s), "step state sync");
+  if (!rc) rc = check_cuda(h, cudaMemsetAsync(&ctl->kernels, 0, sizeof(ctl->kernels), s), "step kernel count");
+  if (rc) return rc;
+  h->launches += c.kernels;
+  info->step = c.i;
+  info->ik = c.ik;
+  info->frame_idx = c.frame_idx;
+  info->output_frame = c.output_frame;
+  info->reinit = c.reinit;
+  info->reseed = c.repos;
+  info->gradm_reinit = c.gradm;
+  info->dt = c.curr_dt;
+  info->sub_t = c.sub_t;
+  info->max_speed = c.max_speed;
+  for (int k = 0; k < 2; ++k) {
+    info->iterations[k] = c.iters[k];
+    info->converged[k] = c.done[k] == 1;
+    info->rTr[k] = c.rTr[k];
+  }
+  for (int k = 0; k < 64; ++k) {
+    info->history[k][0] = c.history[k][0];
+    info->history[k][1] = c.history[k][1];
+  }
+  return PFM_OK;
+}
+
+}  // extern "C"

@@ -39,6 +39,36 @@ class SolveStats(ctypes.Structure):
                 ("rTr_true", ctypes.c_double)]
 
 
+class StepParams(ctypes.Structure):
+    _fields_ = [("CFL", ctypes.c_double), ("visualize_dt", ctypes.c_double), ("save_frame_each_step", ctypes.c_int),
+                ("reinit_every", ctypes.c_int), ("reinit_every_grad_m", ctypes.c_int),
+                ("use_midpoint_vel", ctypes.c_int), ("reinit_particle_pos", ctypes.c_int), ("poisson", SolveOpts)]
+
+
+class Step3Fields(ctypes.Structure):
+    _fields_ = [("u", ctypes.c_void_p * 3), ("u_mid", ctypes.c_void_p * 3), ("w", ctypes.c_void_p * 3),
+                ("p", ctypes.c_void_p), ("p_mid", ctypes.c_void_p), ("seeds", ctypes.c_void_p),
+                ("pos", ctypes.c_void_p), ("init_imp", ctypes.c_void_p), ("T_init", ctypes.c_void_p),
+                ("T_gm", ctypes.c_void_p), ("init_C", ctypes.c_void_p)]
+
+
+class Step2Fields(ctypes.Structure):
+    _fields_ = [("u", ctypes.c_void_p * 2), ("u_mid", ctypes.c_void_p * 2), ("w", ctypes.c_void_p * 2),
+                ("psi_grid", ctypes.c_void_p * 2), ("p", ctypes.c_void_p), ("p_mid", ctypes.c_void_p),
+                ("seeds", ctypes.c_void_p), ("pos", ctypes.c_void_p), ("imp", ctypes.c_void_p),
+                ("init_imp", ctypes.c_void_p), ("psi", ctypes.c_void_p), ("T", ctypes.c_void_p),
+                ("T_init", ctypes.c_void_p), ("T_gm", ctypes.c_void_p), ("init_C", ctypes.c_void_p),
+                ("C", ctypes.c_void_p)]
+
+
+class StepInfo(ctypes.Structure):
+    _fields_ = [("step", ctypes.c_int), ("ik", ctypes.c_int), ("frame_idx", ctypes.c_int),
+                ("output_frame", ctypes.c_int), ("reinit", ctypes.c_int), ("reseed", ctypes.c_int),
+                ("gradm_reinit", ctypes.c_int), ("dt", ctypes.c_double), ("sub_t", ctypes.c_double),
+                ("max_speed", ctypes.c_float), ("iterations", ctypes.c_int * 2), ("converged", ctypes.c_int * 2),
+                ("rTr", ctypes.c_double * 2), ("history", (ctypes.c_int * 2) * 64)]
+
+
 # name -> argument types (all return int status unless listed in _RESTYPE)
 _P = ctypes.c_void_p
 _I = ctypes.c_int
@@ -99,6 +129,10 @@ SIGNATURES = {
     "pfm3_update_imp": [_P, _P, _P, _P, _P],
     "pfm3_update_grad_m": [_P, _P, _P, _P, _P, _P, _P],
     "pfm3_compute_dT_dx": [_P, _P, _P, _P, _I, _P, _P],
+    "pfm3_step": [_P, ctypes.POINTER(Step3Fields), ctypes.POINTER(StepParams), _P],
+    "pfm2_step": [_P, ctypes.POINTER(Step2Fields), ctypes.POINTER(StepParams), _P],
+    "pfm_step_reset": [_P, _I, _I, ctypes.c_double, _I, _P],
+    "pfm_step_info": [_P, ctypes.POINTER(StepInfo), _P],
 }
 # scratch limits of pfm_sort_particles_noalloc (include/pfm.h)
 NOALLOC_MAX_PARTICLES = 1 << 21

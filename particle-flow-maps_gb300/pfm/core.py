@@ -417,6 +417,41 @@ class Scene:
                                             self._stream()))
 
     # ------------------------------------------------------------------------------------------
+    # the whole step as one CUDA graph
+    # ------------------------------------------------------------------------------------------
+    @staticmethod
+    def step_params(CFL=0.5, visualize_dt=0.1, save_frame_each_step=False, reinit_every=20, reinit_every_grad_m=1,
+                    use_midpoint_vel=True, reinit_particle_pos=True, max_iters=400, tol=1e-12, tol_mode=0, eps=1e-12,
+                    precision=0, warm_start=False, true_residual_every=0, check_every=4):
+        """pfm_step_params: the step loop's hyperparameters and the options of both projections."""
+        sp = _lib.StepParams()
+        sp.CFL, sp.visualize_dt = float(CFL), float(visualize_dt)
+        sp.save_frame_each_step = int(bool(save_frame_each_step))
+        sp.reinit_every, sp.reinit_every_grad_m = int(reinit_every), int(reinit_every_grad_m)
+        sp.use_midpoint_vel, sp.reinit_particle_pos = int(bool(use_midpoint_vel)), int(bool(reinit_particle_pos))
+        sp.poisson = Scene._opts(max_iters, tol, tol_mode, check_every, eps=eps, precision=precision,
+                                 warm_start=warm_start, true_residual_every=true_residual_every)
+        return sp
+
+    def step_graph(self, fields, params):
+        """One whole step (pfm3_step / pfm2_step) as a single graph launch on the current stream;
+        ``fields`` is a Step3Fields / Step2Fields of device pointers (the caller keeps the tensors
+        alive).  No host synchronization."""
+        fn = self.lib.pfm3_step if self.dim == 3 else self.lib.pfm2_step
+        self._check(fn(self.h, ctypes.byref(fields), ctypes.byref(params), self._stream()))
+
+    def step_reset(self, i=-1, ik=0, sub_t=0.0, frame_idx=0):
+        """Sets the device step clock (pfm_step_reset); the next graph step is i + 1."""
+        self._check(self.lib.pfm_step_reset(self.h, int(i), int(ik), ctypes.c_double(sub_t), int(frame_idx),
+                                            self._stream()))
+
+    def step_info(self):
+        """The device step state after the last graph step (a host sync): a pfm_step_info_t."""
+        info = _lib.StepInfo()
+        self._check(self.lib.pfm_step_info(self.h, ctypes.byref(info), self._stream()))
+        return info
+
+    # ------------------------------------------------------------------------------------------
     # scalar (smoke) transport and diagnostics
     # ------------------------------------------------------------------------------------------
     def _cellvec(self, t, n, name):

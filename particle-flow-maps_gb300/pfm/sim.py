@@ -6,6 +6,7 @@ Phase order, reinitialisation cadence and the CFL/frame clock follow 3D/run_3D.p
 import numpy as np
 import torch
 
+from . import _lib
 from .core import Scene
 
 __all__ = ["DtClock", "Sim3D", "Sim2D", "soa", "aos", "soa_T", "aos_T", "lattice3", "lattice2",
@@ -123,8 +124,9 @@ class Sim3D:
 
     def __init__(self, u, seeds, res, dx, CFL=0.5, visualize_dt=0.1, reinit_every=20,
                  reinit_every_grad_m=1, use_midpoint_vel=True, reinit_particle_pos=True, use_apic=True,
-                 base_level=3, mg_levels=0, poisson_opts=None, device="cuda", fused_rk4_p2g=True):
+                 base_level=3, mg_levels=0, poisson_opts=None, device="cuda", fused_rk4_p2g=True, graph=False):
         self.fused_rk4_p2g = bool(fused_rk4_p2g)  # RK4_T_forward + P2G through pfm3_rk4_p2g
+        self.graph = bool(graph)  # step() = one pfm3_step graph launch, no host synchronization
         if isinstance(seeds, torch.Tensor):
             self.P = int(seeds.shape[1])
         else:
@@ -163,7 +165,34 @@ class Sim3D:
         import contextlib
         return self.timer(name) if self.timer is not None else contextlib.nullcontext()
 
+    def _graph_args(self):
+        if getattr(self, "_gargs", None) is None:
+            f = _lib.Step3Fields()
+            for a in range(3):
+                f.u[a], f.u_mid[a], f.w[a] = self.u[a].data_ptr(), self.u_mid[a].data_ptr(), self.w[a].data_ptr()
+            f.p, f.p_mid = self.p.data_ptr(), self.p_mid.data_ptr()
+            for name in ("seeds", "pos", "init_imp", "T_init", "T_gm", "init_C"):
+                setattr(f, name, getattr(self, name).data_ptr())
+            o = {k: v for k, v in self.poisson_opts.items() if k != "raise_on_limit"}
+            prm = Scene.step_params(CFL=self.clock.CFL, visualize_dt=self.clock.visualize_dt,
+                                    save_frame_each_step=self.clock.save_frame_each_step,
+                                    reinit_every=self.reinit_every, reinit_every_grad_m=self.grad_m,
+                                    use_midpoint_vel=self.use_midpoint_vel,
+                                    reinit_particle_pos=self.reinit_particle_pos, **o)
+            self._gargs = (f, prm)
+            self.scene.step_reset(self.i, self.ik, self.clock.sub_t, self.clock.frame_idx)
+        return self._gargs
+
+    def step_info(self):
+        """Graph mode: the device step state after the last step (a host sync)."""
+        return self.scene.step_info()
+
     def step(self):
+        if self.graph:  # the whole step as one graph launch; dt and the solves stay on the device
+            f, prm = self._graph_args()
+            self.scene.step_graph(f, prm)
+            self.i += 1
+            return None
         sc = self.scene
         self.i += 1
         i = self.i
@@ -220,7 +249,8 @@ class Sim2D:
 
     def __init__(self, u, seeds, res, dx, CFL=0.5, visualize_dt=0.1, reinit_every=12,
                  reinit_every_grad_m=8, use_midpoint_vel=True, reinit_particle_pos=True, use_apic=True,
-                 base_level=3, mg_levels=0, poisson_opts=None, device="cuda"):
+                 base_level=3, mg_levels=0, poisson_opts=None, device="cuda", graph=False):
+        self.graph = bool(graph)  # step() = one pfm2_step graph launch, no host synchronization
         seeds = np.asarray(seeds, np.float32)
         self.P = seeds.shape[0]
         self.scene = Scene(2, res, dx, self.P, base_level=base_level, mg_levels=mg_levels, use_apic=use_apic,
@@ -255,7 +285,35 @@ class Sim2D:
         self.infos = []
         self.last_dt = None
 
+    def _graph_args(self):
+        if getattr(self, "_gargs", None) is None:
+            f = _lib.Step2Fields()
+            for a in range(2):
+                f.u[a], f.u_mid[a], f.w[a] = self.u[a].data_ptr(), self.u_mid[a].data_ptr(), self.w[a].data_ptr()
+                f.psi_grid[a] = self.psi_grid[a].data_ptr()
+            f.p, f.p_mid = self.p.data_ptr(), None  # the midpoint solve has no pressure buffer (as step())
+            for name in ("seeds", "pos", "imp", "init_imp", "psi", "T", "T_init", "T_gm", "init_C", "C"):
+                setattr(f, name, getattr(self, name).data_ptr())
+            o = {k: v for k, v in self.poisson_opts.items() if k != "raise_on_limit"}
+            prm = Scene.step_params(CFL=self.clock.CFL, visualize_dt=self.clock.visualize_dt,
+                                    save_frame_each_step=self.clock.save_frame_each_step,
+                                    reinit_every=self.reinit_every, reinit_every_grad_m=self.grad_m,
+                                    use_midpoint_vel=self.use_midpoint_vel,
+                                    reinit_particle_pos=self.reinit_particle_pos, **o)
+            self._gargs = (f, prm)
+            self.scene.step_reset(self.i, self.ik, self.clock.sub_t, self.clock.frame_idx)
+        return self._gargs
+
+    def step_info(self):
+        """Graph mode: the device step state after the last step (a host sync)."""
+        return self.scene.step_info()
+
     def step(self):
+        if self.graph:
+            f, prm = self._graph_args()
+            self.scene.step_graph(f, prm)
+            self.i += 1
+            return None
         sc = self.scene
         self.i += 1
         i = self.i

@@ -63,6 +63,12 @@ int main(void) {
          offsetof(pfm_solve_opts, true_residual_every));
   printf("%zu %zu %zu %zu\n", sizeof(pfm_solve_stats), offsetof(pfm_solve_stats, rTr0), offsetof(pfm_solve_stats, bTb),
          offsetof(pfm_solve_stats, rTr_true));
+  printf("%zu %zu %zu\n", sizeof(pfm_step_params), offsetof(pfm_step_params, reinit_particle_pos),
+         offsetof(pfm_step_params, poisson));
+  printf("%zu %zu %zu\n", sizeof(pfm3_step_fields), offsetof(pfm3_step_fields, p), offsetof(pfm3_step_fields, init_C));
+  printf("%zu %zu %zu\n", sizeof(pfm2_step_fields), offsetof(pfm2_step_fields, psi_grid), offsetof(pfm2_step_fields, C));
+  printf("%zu %zu %zu %zu %zu\n", sizeof(pfm_step_info_t), offsetof(pfm_step_info_t, dt),
+         offsetof(pfm_step_info_t, max_speed), offsetof(pfm_step_info_t, rTr), offsetof(pfm_step_info_t, history));
   return 0;
 }
 """
@@ -85,6 +91,13 @@ def test_struct_layouts_match_header():
     assert c[5:9] == [ctypes.sizeof(O), O.tol.offset, O.check_every.offset, O.true_residual_every.offset]
     S = _lib.SolveStats
     assert c[9:13] == [ctypes.sizeof(S), S.rTr0.offset, S.bTb.offset, S.rTr_true.offset]
+    P = _lib.StepParams
+    assert c[13:16] == [ctypes.sizeof(P), P.reinit_particle_pos.offset, P.poisson.offset]
+    F3, F2 = _lib.Step3Fields, _lib.Step2Fields
+    assert c[16:19] == [ctypes.sizeof(F3), F3.p.offset, F3.init_C.offset]
+    assert c[19:22] == [ctypes.sizeof(F2), F2.psi_grid.offset, F2.C.offset]
+    I = _lib.StepInfo
+    assert c[22:27] == [ctypes.sizeof(I), I.dt.offset, I.max_speed.offset, I.rTr.offset, I.history.offset]
 
 
 def test_scene_fails_loudly_without_cuda():

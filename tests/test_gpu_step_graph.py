@@ -1,0 +1,100 @@
+"""The whole step as one CUDA graph (pfm3_step / pfm2_step): the same kernels as the eager phase
+calls of pfm.Sim3D / pfm.Sim2D, with dt, the reinitialisation schedule and the MGPCG loops on the
+device, so the graph steps are compared with the eager steps bit for bit over runs that cross the
+reinitialisations, the gradient schedule and a frame boundary."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import pfm  # noqa: E402
+from __graft_entry__ import _ring_velocity  # noqa: E402
+
+MIXED = dict(tol=1e-6, tol_mode=2, max_iters=400, precision="fp16", warm_start=True, true_residual_every=5)
+PLAIN = dict(tol=1e-12, tol_mode=0, max_iters=400)
+
+
+def _pair3(res, opts, **kw):
+    dx = 1.0 / res[1]
+    u0 = _ring_velocity(res, dx)
+    seeds = pfm.jittered(res, dx, 8, seed=2)
+    a = pfm.Sim3D(u0, seeds, res, dx, poisson_opts=opts, **kw)
+    b = pfm.Sim3D(u0, seeds, res, dx, poisson_opts=opts, graph=True, **kw)
+    return a, b
+
+
+@pytest.mark.parametrize("opts", [MIXED, PLAIN], ids=["mixed", "plain"])
+def test_step3_graph_equals_eager(opts):
+    a, b = _pair3((32, 16, 16), opts, reinit_every=3, reinit_every_grad_m=2, visualize_dt=0.02)
+    iters = []
+    for _ in range(7):
+        a.step()
+        b.step()
+        iters.append([inf.iterations for inf in a.infos[-2:]])
+    torch.cuda.synchronize()
+    for f in range(3):
+        assert torch.equal(a.u[f], b.u[f]), f
+    for name in ("pos", "init_imp", "T_init", "T_gm", "init_C", "p", "p_mid"):
+        assert torch.equal(getattr(a, name), getattr(b, name)), name
+    info = b.step_info()
+    assert info.step == 6 and info.step == a.i
+    assert info.dt == a.last_dt and info.frame_idx == a.clock.frame_idx and info.sub_t == a.clock.sub_t
+    assert [[info.history[s][0], info.history[s][1]] for s in range(7)] == iters
+    assert [info.converged[0], info.converged[1]] == [int(inf.converged) for inf in a.infos[-2:]], iters
+
+
+def test_step3_graph_restart_and_rebuild():
+    """pfm_step_reset restarts the device clock; new field pointers rebuild the graph."""
+    a, b = _pair3((16, 16, 16), MIXED, reinit_every=4, reinit_every_grad_m=1)
+    for _ in range(2):
+        a.step()
+        b.step()
+    # continue the graph run from copies of its state (new pointers) and a reset clock
+    c = pfm.Sim3D([t.clone() for t in b.u], b.seeds.clone(), (16, 16, 16), 1.0 / 16, poisson_opts=MIXED,
+                  reinit_every=4, reinit_every_grad_m=1, graph=True)
+    for name in ("pos", "init_imp", "T_init", "T_gm", "init_C", "p", "p_mid"):
+        getattr(c, name).copy_(getattr(b, name))
+    c.i, c.ik = a.i, a.ik
+    c.clock.sub_t, c.clock.frame_idx = a.clock.sub_t, a.clock.frame_idx
+    for _ in range(3):
+        a.step()
+        c.step()
+    torch.cuda.synchronize()
+    for f in range(3):
+        assert torch.equal(a.u[f], c.u[f])
+    assert torch.equal(a.pos, c.pos)
+    launches0 = c.scene.launches
+    info = c.step_info()
+    assert info.step == a.i and c.scene.launches > launches0
+
+
+def test_step2_graph_equals_eager():
+    res = (64, 32)
+    dx = 1.0 / 32
+    rng = np.random.default_rng(4)
+    idx = np.meshgrid(np.arange(65) / 32, (np.arange(32) + 0.5) / 32, indexing="ij")
+    ux = (0.3 * np.sin(3 * idx[0]) * np.cos(2 * idx[1])).astype(np.float32)
+    idy = np.meshgrid((np.arange(64) + 0.5) / 32, np.arange(33) / 32, indexing="ij")
+    uy = (0.2 * np.cos(2 * idy[0]) * np.sin(3 * idy[1])).astype(np.float32)
+    seeds = pfm.jittered(res, dx, 4, seed=int(rng.integers(100)))
+    kw = dict(reinit_every=4, reinit_every_grad_m=3, visualize_dt=0.05, poisson_opts=PLAIN)
+    a = pfm.Sim2D([ux, uy], seeds, res, dx, **kw)
+    b = pfm.Sim2D([ux, uy], seeds, res, dx, graph=True, **kw)
+    for _ in range(9):
+        a.step()
+        b.step()
+    torch.cuda.synchronize()
+    for f in range(2):
+        assert torch.equal(a.u[f], b.u[f]), f
+        assert torch.equal(a.psi_grid[f], b.psi_grid[f]), f
+    for name in ("pos", "imp", "init_imp", "psi", "T", "T_init", "T_gm", "init_C", "C", "p"):
+        assert torch.equal(getattr(a, name), getattr(b, name)), name
+    info = b.step_info()
+    assert info.step == 8 and info.dt == a.last_dt
+
+
+def test_step_rejects_unbounded_solve():
+    a, b = _pair3((16, 16, 16), dict(tol=1e-6, tol_mode=1, max_iters=-1))
+    with pytest.raises(pfm.PfmError):
+        b.step()
