@@ -50,6 +50,9 @@ def parse():
                     help="plain FP32 MGPCG and/or the mixed-precision warm-started MGPCG (the headline)")
     ap.add_argument("--precision", default="fp16", choices=["fp16", "bf16"],
                     help="multigrid level storage of the mixed arm")
+    ap.add_argument("--eager", action="store_true",
+                    help="time the eager phase calls instead of the whole-step graph (kernels inside graph "
+                         "conditional nodes are invisible to ncu launch lists)")
     return ap.parse_args()
 
 
@@ -62,7 +65,7 @@ def ring_params():
 # ------------------------------------------------------------------------------------------------
 # GPU scene set-up
 # ------------------------------------------------------------------------------------------------
-def make_sim(res, ppc_axis, poisson_opts, device="cuda"):
+def make_sim(res, ppc_axis, poisson_opts, device="cuda", graph=True):
     import torch
     import pfm
     n = res
@@ -71,7 +74,7 @@ def make_sim(res, ppc_axis, poisson_opts, device="cuda"):
     seeds = torch.empty(3, P, device=device)
     zeros = [torch.zeros(s, device=device) for s in ((n + 1, n, n), (n, n + 1, n), (n, n, n + 1))]
     sim = pfm.Sim3D(zeros, seeds, (n, n, n), dx, CFL=0.5, visualize_dt=0.1, reinit_every=20, reinit_every_grad_m=1,
-                    poisson_opts=poisson_opts, device=device)
+                    poisson_opts=poisson_opts, device=device)  # set-up phases run eagerly
     sc = sim.scene
     sc.seed_jittered(sim.seeds, 0, ppc_axis)
     vc = torch.zeros((n, n, n, 3), device=device)
@@ -83,6 +86,7 @@ def make_sim(res, ppc_axis, poisson_opts, device="cuda"):
     # the set-up projection's pressure answers a different problem: warm starts begin at the first step
     sim.p.zero_()
     torch.cuda.synchronize()
+    sim.set_graph(graph)  # the timed steps: one CUDA graph launch per step
     return sim
 
 
@@ -292,15 +296,15 @@ def main():
         torch.cuda.synchronize()
 
     def timed_arm(popts):
-        """W warm-up steps, then K steps timed with CUDA events (max over ranks), phase events,
-        launch counts and the SM clocks sampled during the timed region."""
-        sim = make_sim(args.res, args.ppc_axis, popts)
+        """W warm-up steps, then K steps timed with CUDA events (max over ranks), launch counts and
+        the SM clocks sampled during the timed region.  Every step is one whole-step CUDA graph
+        launch (pfm3_step): no host synchronization between steps.  The phase breakdown comes from
+        a few more steps of the same scene through the eager phase calls, bracketed by CUDA events."""
+        sim = make_sim(args.res, args.ppc_axis, popts, graph=not args.eager)
         for _ in range(args.warmup):
             sim.step()
+        sim.step_info()  # settles the launch count of the warm-up steps
         torch.cuda.synchronize()
-        timer = PhaseTimer()
-        sim.timer = timer
-        iters_before = len(sim.infos)
         launches0 = sim.scene.launches
         clocks = ClockSampler(local)
         barrier()
@@ -317,11 +321,29 @@ def main():
         wall = time.perf_counter() - t0
         clk = clocks.stop()
         barrier()
-        sim.timer = None
         value, elapsed = job_rate(e0.elapsed_time(e1) / 1e3, args.steps, world, dist, "cuda")
-        return dict(sim=sim, value=value, elapsed=elapsed, wall=wall, clocks=clk,
-                    launches=sim.scene.launches - launches0, phases=timer.summary(),
-                    mg_iters=[i.iterations for i in sim.infos[iters_before:]])
+        if args.eager:
+            mg_iters = [i.iterations for i in sim.infos[-2 * args.steps:]]
+            launches = sim.scene.launches - launches0
+        else:
+            info = sim.step_info()
+            launches = sim.scene.launches - launches0
+            last = info.step
+            mg_iters = []
+            for st in range(max(last - args.steps + 1, last - 63), last + 1):
+                mg_iters += [int(info.history[st % 64][0]), int(info.history[st % 64][1])]
+        # phase breakdown: eager phase calls with CUDA events on the launching stream
+        sim.set_graph(False)
+        timer = PhaseTimer()
+        sim.timer = timer
+        for _ in range(min(3, args.steps)):
+            sim.step()
+        torch.cuda.synchronize()
+        sim.timer = None
+        eager_ms = sum(statistics.mean(v) for v in timer.summary().values())
+        sim.set_graph(not args.eager)
+        return dict(sim=sim, value=value, elapsed=elapsed, wall=wall, clocks=clk, launches=launches,
+                    phases=timer.summary(), mg_iters=mg_iters, eager_ms=eager_ms)
 
     # the two arms of the metric, at the same residual: MGPCG stops at |r| < tol |b| in both
     plain_opts = dict(tol=args.tol, tol_mode=args.tol_mode, max_iters=400, check_every=4)
@@ -381,8 +403,16 @@ def main():
         torch.cuda.synchronize()
         e_rate, _ = job_rate(a.elapsed_time(b) / 1e3, args.steps, world, dist, "cuda")
         gbytes = sum(h.numel() * 4 for h in host_u)
+        if args.eager:
+            e_iters = [i.iterations for i in sim.infos[-2 * args.steps:]]
+        else:
+            hist = sim.step_info()
+            last = hist.step
+            e_iters = []
+            for st in range(max(last - args.steps + 1, last - 63), last + 1):
+                e_iters += [int(hist.history[st % 64][0]), int(hist.history[st % 64][1])]
         e2e = {"value": e_rate, "unit": UNIT, "h2d_bytes_per_step": gbytes,
-               "d2h_bytes_per_step": gbytes, "mgpcg_iters": [i.iterations for i in sim.infos[-2 * args.steps:]]}
+               "d2h_bytes_per_step": gbytes, "mgpcg_iters": e_iters}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -394,6 +424,8 @@ def main():
                f"every 5 iterations) warm-started from the previous step's pressure" if mixed else
                "plain FP32 MGPCG from a zero initial guess")
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "step_form": ("eager phase calls (pfm3_* entry points)" if args.eager else
+                              "one whole-step CUDA graph launch per step (pfm3_step)"),
                 "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3, "wall_s": wall,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded two-ring initial condition and jittered particles)",
@@ -404,6 +436,8 @@ def main():
                 "particle_updates_per_s": value * P,
                 "mgpcg_iters": mg_iters,
                 "phase_ms": {k: statistics.mean(v) for k, v in phases.items()},
+                "phase_note": "phase_ms: CUDA events around the eager phase calls of 3 further steps "
+                              "(sum %.2f ms/step)" % head["eager_ms"],
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches}
         if plain is not None and mixed:
             line["plain_fp32"] = {"value": plain["value"], "ms_per_step": plain["elapsed"] / args.steps * 1e3,

@@ -187,6 +187,20 @@ class Sim3D:
         """Graph mode: the device step state after the last step (a host sync)."""
         return self.scene.step_info()
 
+    def set_graph(self, on):
+        """Switches between graph steps and eager phase calls, handing the frame clock and the
+        reinitialisation schedule over between the device and the host."""
+        on = bool(on)
+        if on == self.graph:
+            return
+        if not on and getattr(self, "_gargs", None) is not None:
+            info = self.scene.step_info()
+            self.ik, self.clock.sub_t, self.clock.frame_idx = info.ik, info.sub_t, info.frame_idx
+            self.last_dt = info.dt if info.step >= 0 else self.last_dt
+        elif on and getattr(self, "_gargs", None) is not None:
+            self.scene.step_reset(self.i, self.ik, self.clock.sub_t, self.clock.frame_idx)
+        self.graph = on
+
     def step(self):
         if self.graph:  # the whole step as one graph launch; dt and the solves stay on the device
             f, prm = self._graph_args()
