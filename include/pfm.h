@@ -333,6 +333,23 @@ int pfm_step_reset(pfm_handle* h, int i, int ik, double sub_t, int frame_idx, vo
  * ran to pfm_launch_count. */
 int pfm_step_info(pfm_handle* h, pfm_step_info_t* info, void* stream);
 
+/* ---- batches of independent scenes -------------------------------------------------------------
+ * A batch advances many scenes (of any sizes, 2D and 3D mixed) one step with ONE graph launch: the
+ * graph holds every scene's whole step (as pfm3_step / pfm2_step) as an independent branch, so the
+ * GPU runs the scenes' kernels concurrently and the small scenes fill the SMs the large ones leave
+ * idle.  Each scene keeps its own handle (whose workspace holds its step clock and solver state;
+ * a handle can be in one batch once) and its own fields; results are bitwise those of stepping the
+ * scenes one by one.  The graph is built on the first pfm_batch_step after the last add.  Errors
+ * of batch calls are reported by pfm_batch_last_error; pfm_step_info / pfm_step_reset work on each
+ * scene's handle. */
+typedef struct pfm_batch pfm_batch;
+int pfm_batch_create(pfm_batch** out);
+int pfm_batch_destroy(pfm_batch* b);
+int pfm_batch_add3(pfm_batch* b, pfm_handle* h, const pfm3_step_fields* f, const pfm_step_params* p);
+int pfm_batch_add2(pfm_batch* b, pfm_handle* h, const pfm2_step_fields* f, const pfm_step_params* p);
+int pfm_batch_step(pfm_batch* b, void* stream);
+const char* pfm_batch_last_error(const pfm_batch* b);
+
 /* ---- the reference's alternative ("evolve m") dataflow ---------------------------------------
  * Kernels the reference defines beside its live step (their call sites in 3D/run_3D.py:795-808
  * are commented out).  grad_T_init is the three per-particle 3x3 matrices grad_T_init_x/y/z as

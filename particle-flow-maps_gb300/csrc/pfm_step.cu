@@ -10,7 +10,9 @@
 //     iteration (the same kernels as the eager solve, so the results are bitwise the same).
 // The graph is built on the first call and rebuilt only when the fields or parameters change.
 #include <cstring>
+#include <new>
 #include <string>
+#include <vector>
 
 #include "pfm_internal.cuh"
 
@@ -112,46 +114,61 @@ static int init_clock(pfm_handle* h, cudaStream_t s) {
   return launch_check(h, "k_step_clock_set");
 }
 
-// Builds the step graph: `emit` appends the phases between the control kernel and the end.
+// What emitting one scene's step leaves for the finishing touch: the control kernel's node and the
+// arguments it gets once the step's kernels are counted.
+struct SceneEmit {
+  cudaGraphNode_t ctl_node = nullptr;
+  StepCtl* ctl = nullptr;
+  StepParams prm{};
+  cudaGraphConditionalHandle c[4] = {0, 0, 0, 0};  // reseed, reinit, k == 0, k != 0
+  unsigned counts[4] = {0, 0, 0, 0};                // kernels in each IF body
+  unsigned long long fixed = 0;                     // kernels outside the IF and WHILE bodies
+};
+
+// Creates the scene's IF handles in the cursor's graph, emits the step with `emit`, and counts its
+// kernels.  The control kernel is captured with zero counts; patch_control sets the real ones.
+template <class Emit>
+static int emit_scene(GraphCursor& gc, const pfm_step_params* p, SceneEmit& se, Emit&& emit) {
+  pfm_handle* h = gc.h;
+  se.ctl = ws_ptr<StepCtl>(h, h->o_step);
+  se.prm = step_params(h, p);
+  const uint64_t before = h->launches;
+  const uint64_t body0 = gc.body_launches;
+  for (int k = 0; k < 4; ++k)  // one handle per IF node (a handle without a node does not instantiate)
+    if (!gc.rc && (k != 3 || se.prm.else_branch))
+      gc.rc = check_cuda(h, cudaGraphConditionalHandleCreate(&se.c[k], gc.G, 0, 0), "conditional handle");
+  if (!gc.rc) emit(gc, se);
+  gc.close();
+  // the IF bodies are counted by the control kernel, the loops by the solves (on the device)
+  se.fixed = (h->launches - before) - (gc.body_launches - body0);
+  h->launches = before;
+  return gc.rc;
+}
+
+static int patch_control(pfm_handle* h, SceneEmit& se) {
+  if (!se.ctl_node) return set_error(h, PFM_ERR_CUDA, "step graph: no control node");
+  cudaKernelNodeParams kp{};
+  int rc = check_cuda(h, cudaGraphKernelNodeGetParams(se.ctl_node, &kp), "control node params");
+  if (rc) return rc;
+  void* args[] = {&se.ctl, &se.prm, &se.c[0], &se.c[1], &se.c[2], &se.c[3], &se.fixed,
+                  &se.counts[0], &se.counts[1], &se.counts[2], &se.counts[3]};
+  kp.kernelParams = args;
+  kp.extra = nullptr;
+  return check_cuda(h, cudaGraphKernelNodeSetParams(se.ctl_node, &kp), "control node params");
+}
+
+// Builds a handle's own step graph from one scene emission.
 template <class Emit>
 static int build_step_graph(pfm_handle* h, const pfm_step_params* p, Emit&& emit) {
   int rc = ensure_cap_stream(h);
   if (rc) return rc;
-  StepCtl* ctl = ws_ptr<StepCtl>(h, h->o_step);
   cudaGraph_t G = nullptr;
   rc = check_cuda(h, cudaGraphCreate(&G, 0), "graph create");
   if (rc) return rc;
-  const uint64_t before = h->launches;
   GraphCursor gc(h, G, h->cap_stream);
-  // one handle per IF node (a handle without a node does not instantiate)
-  cudaGraphConditionalHandle c_repos{}, c_reinit{}, c_gradm{}, c_nogradm{};
-  for (cudaGraphConditionalHandle* c : {&c_repos, &c_reinit, &c_gradm, &c_nogradm})
-    if (!gc.rc && (c != &c_nogradm || step_params(h, p).else_branch))
-      gc.rc = check_cuda(h, cudaGraphConditionalHandleCreate(c, G, 0, 0), "conditional handle");
-  // The control kernel is captured first with zero kernel counts; once the phases are emitted
-  // (and so counted) its node parameters are set to the real counts.
-  cudaGraphNode_t ctl_node = nullptr;
-  unsigned long long fixed = 0;
-  unsigned counts[4] = {0, 0, 0, 0};
-  if (!gc.rc) emit(gc, ctl, c_repos, c_reinit, c_gradm, c_nogradm, &ctl_node, counts, step_params(h, p));
-  gc.close();
-  // top-level kernels: all that were launched but the conditional and loop bodies (the loops count
-  // their iterations on the device, the IF bodies are counted by the control kernel)
-  fixed = (h->launches - before) - gc.body_launches;
-  h->launches = before;
-  rc = gc.rc;
-  if (!rc && ctl_node) {  // the control kernel's kernel counts, known only now
-    cudaKernelNodeParams kp{};
-    rc = check_cuda(h, cudaGraphKernelNodeGetParams(ctl_node, &kp), "control node params");
-    if (!rc) {
-      StepParams prm = step_params(h, p);
-      void* args[] = {&ctl, &prm, &c_repos, &c_reinit, &c_gradm, &c_nogradm, &fixed,
-                      &counts[0], &counts[1], &counts[2], &counts[3]};
-      kp.kernelParams = args;
-      kp.extra = nullptr;
-      rc = check_cuda(h, cudaGraphKernelNodeSetParams(ctl_node, &kp), "control node params");
-    }
-  }
+  SceneEmit se;
+  rc = emit_scene(gc, p, se, emit);
+  if (!rc) rc = patch_control(h, se);
   if (h->g_step) cudaGraphExecDestroy(h->g_step);
   h->g_step = nullptr;
   if (!rc) rc = check_cuda(h, cudaGraphInstantiate(&h->g_step, G, 0), "step graph instantiate");
@@ -159,17 +176,14 @@ static int build_step_graph(pfm_handle* h, const pfm_step_params* p, Emit&& emit
   return rc;
 }
 
-// max_speed + control: the first segment of every step graph; returns the control kernel's node.
-static cudaGraphNode_t emit_head(GraphCursor& gc, StepCtl* ctl, const float* u0, const float* u1, const float* u2,
-                                 const StepParams& prm, cudaGraphConditionalHandle c_repos,
-                                 cudaGraphConditionalHandle c_reinit, cudaGraphConditionalHandle c_gradm,
-                                 cudaGraphConditionalHandle c_nogradm) {
+// max_speed + control: the first segment of every scene's step; records the control kernel's node.
+static void emit_head(GraphCursor& gc, SceneEmit& se, const float* u0, const float* u1, const float* u2) {
   pfm_handle* h = gc.h;
   cudaStream_t q = gc.seg();
-  max_speed_async(h, u0, u1, u2, &ctl->max_speed, q);
-  launch(h, k_step_control, 1, 1, 0, q, ctl, prm, c_repos, c_reinit, c_gradm, c_nogradm, 0ull, 0u, 0u, 0u, 0u);
+  max_speed_async(h, u0, u1, u2, &se.ctl->max_speed, q);
+  launch(h, k_step_control, 1, 1, 0, q, se.ctl, se.prm, se.c[0], se.c[1], se.c[2], se.c[3], 0ull, 0u, 0u, 0u, 0u);
   gc.close();
-  return gc.ndeps == 1 ? gc.deps[0] : nullptr;
+  se.ctl_node = gc.ndeps == 1 ? gc.deps[0] : nullptr;
 }
 
 // Kernels launched by `f` into the body of an IF node on `cond`.
@@ -205,13 +219,7 @@ static bool same_key(pfm_handle* h, const std::string& k) {
   return false;
 }
 
-}  // namespace pfm
-
-using namespace pfm;
-
-extern "C" {
-
-int pfm3_step(pfm_handle* h, const pfm3_step_fields* f, const pfm_step_params* p, void* stream) {
+static int check_fields3(pfm_handle* h, const pfm3_step_fields* f, const pfm_step_params* p) {
   if (!h) return PFM_ERR_NULL;
   if (h->cfg.dim != 3) return set_error(h, PFM_ERR_SHAPE, "pfm3_step on a 2D handle");
   if (!f) return set_error(h, PFM_ERR_NULL, "pfm3_step: null fields");
@@ -225,59 +233,10 @@ int pfm3_step(pfm_handle* h, const pfm3_step_fields* f, const pfm_step_params* p
   if (!f->p) return set_error(h, PFM_ERR_NULL, "pfm3_step: null pressure");
   if (h->P > 0 && (!f->seeds || !f->pos || !f->init_imp || !f->T_init || !f->T_gm || !f->init_C))
     return set_error(h, PFM_ERR_NULL, "pfm3_step: null particle field");
-  cudaStream_t s = (cudaStream_t)stream;
-  if (!h->step_clock_init) {
-    rc = init_clock(h, s);
-    if (rc) return rc;
-  }
-  KeyBuf key;
-  key << 3;
-  for (int a = 0; a < 3; ++a) key << f->u[a] << f->u_mid[a] << f->w[a];
-  key << f->p << f->p_mid << f->seeds << f->pos << f->init_imp << f->T_init << f->T_gm << f->init_C;
-  key_params(key, p);
-  if (!same_key(h, key.s)) {
-    rc = build_step_graph(h, p, [&](GraphCursor& gc, StepCtl* ctl, cudaGraphConditionalHandle c_repos,
-                                    cudaGraphConditionalHandle c_reinit, cudaGraphConditionalHandle c_gradm,
-                                    cudaGraphConditionalHandle c_nogradm, cudaGraphNode_t* ctl_node, unsigned* counts,
-                                    const StepParams& prm) {
-      *ctl_node = emit_head(gc, ctl, f->u[0], f->u[1], f->u[2], prm, c_repos, c_reinit, c_gradm, c_nogradm);
-      const int64_t P = h->P;
-      // j == 0: reseed (run_3D.py:753-757), G2P of the impulse, T_init = T_gm = I (:759-764)
-      counts[0] = emit_if(gc, c_repos, [&](cudaStream_t q) { copy_launch(h, f->pos, f->seeds, 3 * P, q); });
-      counts[1] = emit_if(gc, c_reinit, [&](cudaStream_t q) {
-        pfm3_g2p(h, f->pos, f->u[0], f->u[1], f->u[2], f->init_imp, nullptr, q);
-        pfm3_reset_T(h, f->T_init, q);
-        pfm3_reset_T(h, f->T_gm, q);
-      });
-      const float* ua[3] = {f->u[0], f->u[1], f->u[2]};
-      if (p->use_midpoint_vel) {  // midpoint velocity and its projection (run_3D.py:779-788)
-        launch_midpoint(h, f->u, f->u_mid, 0.f, &ctl->dt_half, gc.seg());
-        append_poisson(gc, f->u_mid, f->p_mid, p->poisson, ctl, 0);
-        for (int a = 0; a < 3; ++a) ua[a] = f->u_mid[a];
-      }
-      // RK4_T_forward + the P2G records, with the k == 0 gradient reinitialisation in the same kernel
-      cudaMemsetAsync(ws_ptr<int>(h, h->o_count), 0, h->cells * 4, gc.seg());
-      const P2GRecords3 R = records3(h, f->init_imp, f->T_init, f->init_C);
-      const MacFields3 F{{ua[0], ua[1], ua[2]}}, Fg{{f->u[0], f->u[1], f->u[2]}};
-      counts[2] = emit_if(gc, c_gradm, [&](cudaStream_t q) {
-        launch_rk4_T_forward3(h, f->pos, f->T_gm, F, 0.f, &R, &Fg, q, &ctl->dt);
-      });
-      counts[3] = emit_if(gc, c_nogradm, [&](cudaStream_t q) {
-        launch_rk4_T_forward3(h, f->pos, f->T_gm, F, 0.f, &R, nullptr, q, &ctl->dt);
-      });
-      p2g3_from_records(h, f->u, f->w, gc.seg());
-      append_poisson(gc, f->u, f->p, p->poisson, ctl, 1);
-    });
-    if (rc) {
-      h->step_key.clear();
-      return rc;
-    }
-    h->rec_valid = 1;
-  }
-  return check_cuda(h, cudaGraphLaunch(h->g_step, s), "step graph launch");
+  return PFM_OK;
 }
 
-int pfm2_step(pfm_handle* h, const pfm2_step_fields* f, const pfm_step_params* p, void* stream) {
+static int check_fields2(pfm_handle* h, const pfm2_step_fields* f, const pfm_step_params* p) {
   if (!h) return PFM_ERR_NULL;
   if (h->cfg.dim != 2) return set_error(h, PFM_ERR_SHAPE, "pfm2_step on a 3D handle");
   if (!f) return set_error(h, PFM_ERR_NULL, "pfm2_step: null fields");
@@ -292,63 +251,270 @@ int pfm2_step(pfm_handle* h, const pfm2_step_fields* f, const pfm_step_params* p
   if (h->P > 0 && (!f->seeds || !f->pos || !f->imp || !f->init_imp || !f->psi || !f->T || !f->T_init || !f->T_gm ||
                    !f->init_C || !f->C))
     return set_error(h, PFM_ERR_NULL, "pfm2_step: null particle field");
-  cudaStream_t s = (cudaStream_t)stream;
-  if (!h->step_clock_init) {
-    rc = init_clock(h, s);
-    if (rc) return rc;
-  }
+  return PFM_OK;
+}
+
+static std::string key3(const pfm3_step_fields* f, const pfm_step_params* p) {
+  KeyBuf key;
+  key << 3;
+  for (int a = 0; a < 3; ++a) key << f->u[a] << f->u_mid[a] << f->w[a];
+  key << f->p << f->p_mid << f->seeds << f->pos << f->init_imp << f->T_init << f->T_gm << f->init_C;
+  key_params(key, p);
+  return key.s;
+}
+
+static std::string key2(const pfm2_step_fields* f, const pfm_step_params* p) {
   KeyBuf key;
   key << 2;
   for (int a = 0; a < 2; ++a) key << f->u[a] << f->u_mid[a] << f->w[a] << f->psi_grid[a];
   key << f->p << f->p_mid << f->seeds << f->pos << f->imp << f->init_imp << f->psi << f->T << f->T_init << f->T_gm
       << f->init_C << f->C;
   key_params(key, p);
-  if (!same_key(h, key.s)) {
-    rc = build_step_graph(h, p, [&](GraphCursor& gc, StepCtl* ctl, cudaGraphConditionalHandle c_repos,
-                                    cudaGraphConditionalHandle c_reinit, cudaGraphConditionalHandle c_gradm,
-                                    cudaGraphConditionalHandle c_nogradm, cudaGraphNode_t* ctl_node, unsigned* counts,
-                                    const StepParams& prm) {
-      *ctl_node = emit_head(gc, ctl, f->u[0], f->u[1], nullptr, prm, c_repos, c_reinit, c_gradm, c_nogradm);
-      const int64_t P = h->P;
-      // j == 0 (2D/run_2D.py:812-832): reseed, imp = init_imp = u(pos), psi = pos, T = T_init = I
-      counts[0] = emit_if(gc, c_repos, [&](cudaStream_t q) { copy_launch(h, f->pos, f->seeds, 2 * P, q); });
-      counts[1] = emit_if(gc, c_reinit, [&](cudaStream_t q) {
-        pfm2_g2p(h, f->pos, f->u[0], f->u[1], f->imp, nullptr, q);
-        copy_launch(h, f->init_imp, f->imp, 2 * P, q);
-        copy_launch(h, f->psi, f->pos, 2 * P, q);
-        pfm2_reset_T(h, f->T, q);
-        pfm2_reset_T(h, f->T_init, q);
-      });
-      // k == 0 (2D/run_2D.py:834-843): init_C = grad u(pos), T_gm = I, T_init = T
-      counts[2] = emit_if(gc, c_gradm, [&](cudaStream_t q) {
-        pfm2_g2p(h, f->pos, f->u[0], f->u[1], nullptr, f->init_C, q);
-        pfm2_reset_T(h, f->T_gm, q);
-        copy_launch(h, f->T_init, f->T, 4 * P, q);
-      });
-      counts[3] = 0;
-      float* ua[2] = {f->u[0], f->u[1]};
-      if (p->use_midpoint_vel) {  // 2D/run_2D.py:866-872
-        launch_midpoint(h, f->u, f->u_mid, 0.f, &ctl->dt_half, gc.seg());
-        append_poisson(gc, f->u_mid, f->p_mid, p->poisson, ctl, 0);
-        ua[0] = f->u_mid[0];
-        ua[1] = f->u_mid[1];
-      }
-      // RK4 of positions and T_gm, then the 2D updates and P2G (2D/run_2D.py:875-905)
-      cudaStream_t q = gc.seg();
-      const MacFields2 F{{ua[0], ua[1]}};
-      launch_rk4_T_forward2(h, f->pos, f->T_gm, F, 0.f, 1, q, &ctl->dt);
-      pfm2_update_grad_m(h, f->C, f->init_C, f->T_gm, q);
-      pfm2_update_T(h, f->T, f->T_init, f->T_gm, q);
-      pfm2_update_imp(h, f->imp, f->init_imp, f->T, q);
-      pfm2_p2g(h, f->imp, f->pos, f->C, f->psi, f->u[0], f->u[1], f->psi_grid[0], f->psi_grid[1], f->w[0], f->w[1], q);
-      append_poisson(gc, f->u, f->p, p->poisson, ctl, 1);
-    });
+  return key.s;
+}
+
+// One 3D step (Sim3D.step, the fused form) behind the cursor.
+static void emit_step3(GraphCursor& gc, SceneEmit& se, const pfm3_step_fields* f, const pfm_step_params* p) {
+  pfm_handle* h = gc.h;
+  StepCtl* ctl = se.ctl;
+  emit_head(gc, se, f->u[0], f->u[1], f->u[2]);
+  const int64_t P = h->P;
+  // j == 0: reseed (run_3D.py:753-757), G2P of the impulse, T_init = T_gm = I (:759-764)
+  se.counts[0] = emit_if(gc, se.c[0], [&](cudaStream_t q) { copy_launch(h, f->pos, f->seeds, 3 * P, q); });
+  se.counts[1] = emit_if(gc, se.c[1], [&](cudaStream_t q) {
+    pfm3_g2p(h, f->pos, f->u[0], f->u[1], f->u[2], f->init_imp, nullptr, q);
+    pfm3_reset_T(h, f->T_init, q);
+    pfm3_reset_T(h, f->T_gm, q);
+  });
+  const float* ua[3] = {f->u[0], f->u[1], f->u[2]};
+  if (p->use_midpoint_vel) {  // midpoint velocity and its projection (run_3D.py:779-788)
+    launch_midpoint(h, f->u, f->u_mid, 0.f, &ctl->dt_half, gc.seg());
+    append_poisson(gc, f->u_mid, f->p_mid, p->poisson, ctl, 0);
+    for (int a = 0; a < 3; ++a) ua[a] = f->u_mid[a];
+  }
+  // RK4_T_forward + the P2G records, with the k == 0 gradient reinitialisation in the same kernel
+  cudaMemsetAsync(ws_ptr<int>(h, h->o_count), 0, h->cells * 4, gc.seg());
+  const P2GRecords3 R = records3(h, f->init_imp, f->T_init, f->init_C);
+  const MacFields3 F{{ua[0], ua[1], ua[2]}}, Fg{{f->u[0], f->u[1], f->u[2]}};
+  se.counts[2] = emit_if(gc, se.c[2], [&](cudaStream_t q) {
+    launch_rk4_T_forward3(h, f->pos, f->T_gm, F, 0.f, &R, &Fg, q, &ctl->dt);
+  });
+  se.counts[3] = emit_if(gc, se.c[3], [&](cudaStream_t q) {
+    launch_rk4_T_forward3(h, f->pos, f->T_gm, F, 0.f, &R, nullptr, q, &ctl->dt);
+  });
+  p2g3_from_records(h, f->u, f->w, gc.seg());
+  append_poisson(gc, f->u, f->p, p->poisson, ctl, 1);
+}
+
+// One 2D step (Sim2D.step) behind the cursor.
+static void emit_step2(GraphCursor& gc, SceneEmit& se, const pfm2_step_fields* f, const pfm_step_params* p) {
+  pfm_handle* h = gc.h;
+  StepCtl* ctl = se.ctl;
+  emit_head(gc, se, f->u[0], f->u[1], nullptr);
+  const int64_t P = h->P;
+  // j == 0 (2D/run_2D.py:812-832): reseed, imp = init_imp = u(pos), psi = pos, T = T_init = I
+  se.counts[0] = emit_if(gc, se.c[0], [&](cudaStream_t q) { copy_launch(h, f->pos, f->seeds, 2 * P, q); });
+  se.counts[1] = emit_if(gc, se.c[1], [&](cudaStream_t q) {
+    pfm2_g2p(h, f->pos, f->u[0], f->u[1], f->imp, nullptr, q);
+    copy_launch(h, f->init_imp, f->imp, 2 * P, q);
+    copy_launch(h, f->psi, f->pos, 2 * P, q);
+    pfm2_reset_T(h, f->T, q);
+    pfm2_reset_T(h, f->T_init, q);
+  });
+  // k == 0 (2D/run_2D.py:834-843): init_C = grad u(pos), T_gm = I, T_init = T
+  se.counts[2] = emit_if(gc, se.c[2], [&](cudaStream_t q) {
+    pfm2_g2p(h, f->pos, f->u[0], f->u[1], nullptr, f->init_C, q);
+    pfm2_reset_T(h, f->T_gm, q);
+    copy_launch(h, f->T_init, f->T, 4 * P, q);
+  });
+  float* ua[2] = {f->u[0], f->u[1]};
+  if (p->use_midpoint_vel) {  // 2D/run_2D.py:866-872
+    launch_midpoint(h, f->u, f->u_mid, 0.f, &ctl->dt_half, gc.seg());
+    append_poisson(gc, f->u_mid, f->p_mid, p->poisson, ctl, 0);
+    ua[0] = f->u_mid[0];
+    ua[1] = f->u_mid[1];
+  }
+  // RK4 of positions and T_gm, then the 2D updates and P2G (2D/run_2D.py:875-905)
+  cudaStream_t q = gc.seg();
+  const MacFields2 F{{ua[0], ua[1]}};
+  launch_rk4_T_forward2(h, f->pos, f->T_gm, F, 0.f, 1, q, &ctl->dt);
+  pfm2_update_grad_m(h, f->C, f->init_C, f->T_gm, q);
+  pfm2_update_T(h, f->T, f->T_init, f->T_gm, q);
+  pfm2_update_imp(h, f->imp, f->init_imp, f->T, q);
+  pfm2_p2g(h, f->imp, f->pos, f->C, f->psi, f->u[0], f->u[1], f->psi_grid[0], f->psi_grid[1], f->w[0], f->w[1], q);
+  append_poisson(gc, f->u, f->p, p->poisson, ctl, 1);
+}
+
+}  // namespace pfm
+
+// A batch: many scenes' steps in one CUDA graph, one branch per scene (the branches share no
+// data, so the graph runs them concurrently).
+struct pfm_batch {
+  struct Scene {
+    pfm_handle* h;
+    int dim;
+    pfm3_step_fields f3;
+    pfm2_step_fields f2;
+    pfm_step_params p;
+  };
+  std::vector<Scene> scenes;
+  cudaStream_t cap = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int valid = 0;
+  std::string err;
+};
+
+using namespace pfm;
+
+extern "C" {
+
+int pfm3_step(pfm_handle* h, const pfm3_step_fields* f, const pfm_step_params* p, void* stream) {
+  int rc = check_fields3(h, f, p);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!h->step_clock_init) {
+    rc = init_clock(h, s);
+    if (rc) return rc;
+  }
+  if (!same_key(h, key3(f, p))) {
+    rc = build_step_graph(h, p, [&](GraphCursor& gc, SceneEmit& se) { emit_step3(gc, se, f, p); });
+    if (rc) {
+      h->step_key.clear();
+      return rc;
+    }
+    h->rec_valid = 1;
+  }
+  return check_cuda(h, cudaGraphLaunch(h->g_step, s), "step graph launch");
+}
+
+int pfm2_step(pfm_handle* h, const pfm2_step_fields* f, const pfm_step_params* p, void* stream) {
+  int rc = check_fields2(h, f, p);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!h->step_clock_init) {
+    rc = init_clock(h, s);
+    if (rc) return rc;
+  }
+  if (!same_key(h, key2(f, p))) {
+    rc = build_step_graph(h, p, [&](GraphCursor& gc, SceneEmit& se) { emit_step2(gc, se, f, p); });
     if (rc) {
       h->step_key.clear();
       return rc;
     }
   }
   return check_cuda(h, cudaGraphLaunch(h->g_step, s), "step graph launch");
+}
+
+int pfm_batch_create(pfm_batch** out) {
+  if (!out) return PFM_ERR_NULL;
+  *out = new (std::nothrow) pfm_batch();
+  return *out ? PFM_OK : PFM_ERR_CUDA;
+}
+
+int pfm_batch_destroy(pfm_batch* b) {
+  if (!b) return PFM_ERR_NULL;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->cap) cudaStreamDestroy(b->cap);
+  delete b;
+  return PFM_OK;
+}
+
+const char* pfm_batch_last_error(const pfm_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+static int batch_add(pfm_batch* b, pfm_handle* h, int dim, const pfm3_step_fields* f3, const pfm2_step_fields* f2,
+                     const pfm_step_params* p) {
+  if (!b || !h || !p) return PFM_ERR_NULL;
+  for (const auto& sc : b->scenes)
+    if (sc.h == h) {
+      b->err = "pfm_batch_add: a handle can be in a batch once (its workspace holds the scene's state)";
+      return PFM_ERR_ARG;
+    }
+  int rc = dim == 3 ? check_fields3(h, f3, p) : check_fields2(h, f2, p);
+  if (rc) {
+    b->err = std::string("pfm_batch_add: ") + h->err;
+    return rc;
+  }
+  pfm_batch::Scene sc{};
+  sc.h = h;
+  sc.dim = dim;
+  if (f3) sc.f3 = *f3;
+  if (f2) sc.f2 = *f2;
+  sc.p = *p;
+  b->scenes.push_back(sc);
+  b->valid = 0;
+  return PFM_OK;
+}
+
+int pfm_batch_add3(pfm_batch* b, pfm_handle* h, const pfm3_step_fields* f, const pfm_step_params* p) {
+  return batch_add(b, h, 3, f, nullptr, p);
+}
+
+int pfm_batch_add2(pfm_batch* b, pfm_handle* h, const pfm2_step_fields* f, const pfm_step_params* p) {
+  return batch_add(b, h, 2, nullptr, f, p);
+}
+
+int pfm_batch_step(pfm_batch* b, void* stream) {
+  if (!b) return PFM_ERR_NULL;
+  if (b->scenes.empty()) {
+    b->err = "pfm_batch_step: empty batch";
+    return PFM_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  for (auto& sc : b->scenes)
+    if (!sc.h->step_clock_init) {
+      int rc = init_clock(sc.h, s);
+      if (rc) {
+        b->err = sc.h->err;
+        return rc;
+      }
+    }
+  if (!b->valid) {
+    if (!b->cap) {
+      cudaError_t e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking);
+      if (e != cudaSuccess) {
+        b->err = std::string("capture stream: ") + cudaGetErrorString(e);
+        return PFM_ERR_CUDA;
+      }
+    }
+    cudaGraph_t G = nullptr;
+    if (cudaGraphCreate(&G, 0) != cudaSuccess) {
+      b->err = "graph create failed";
+      return PFM_ERR_CUDA;
+    }
+    int rc = PFM_OK;
+    for (auto& sc : b->scenes) {  // every scene a branch from the graph's roots
+      GraphCursor gc(sc.h, G, b->cap);
+      SceneEmit se;
+      if (sc.dim == 3)
+        rc = emit_scene(gc, &sc.p, se, [&](GraphCursor& g, SceneEmit& e) { emit_step3(g, e, &sc.f3, &sc.p); });
+      else
+        rc = emit_scene(gc, &sc.p, se, [&](GraphCursor& g, SceneEmit& e) { emit_step2(g, e, &sc.f2, &sc.p); });
+      if (!rc) rc = patch_control(sc.h, se);
+      if (rc) {
+        b->err = sc.h->err;
+        break;
+      }
+      if (sc.dim == 3) sc.h->rec_valid = 1;
+    }
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+    if (!rc) {
+      cudaError_t e = cudaGraphInstantiate(&b->exec, G, 0);
+      if (e != cudaSuccess) {
+        b->err = std::string("batch graph instantiate: ") + cudaGetErrorString(e);
+        rc = PFM_ERR_CUDA;
+      }
+    }
+    cudaGraphDestroy(G);
+    if (rc) return rc;
+    b->valid = 1;
+  }
+  const cudaError_t e = cudaGraphLaunch(b->exec, s);
+  if (e != cudaSuccess) {
+    b->err = std::string("batch graph launch: ") + cudaGetErrorString(e);
+    return PFM_ERR_CUDA;
+  }
+  return PFM_OK;
 }
 
 int pfm_step_reset(pfm_handle* h, int i, int ik, double sub_t, int frame_idx, void* stream) {

@@ -133,11 +133,18 @@ SIGNATURES = {
     "pfm2_step": [_P, ctypes.POINTER(Step2Fields), ctypes.POINTER(StepParams), _P],
     "pfm_step_reset": [_P, _I, _I, ctypes.c_double, _I, _P],
     "pfm_step_info": [_P, ctypes.POINTER(StepInfo), _P],
+    "pfm_batch_create": [ctypes.POINTER(_P)],
+    "pfm_batch_destroy": [_P],
+    "pfm_batch_add3": [_P, _P, ctypes.POINTER(Step3Fields), ctypes.POINTER(StepParams)],
+    "pfm_batch_add2": [_P, _P, ctypes.POINTER(Step2Fields), ctypes.POINTER(StepParams)],
+    "pfm_batch_step": [_P, _P],
+    "pfm_batch_last_error": [_P],
 }
 # scratch limits of pfm_sort_particles_noalloc (include/pfm.h)
 NOALLOC_MAX_PARTICLES = 1 << 21
 NOALLOC_MAX_CELLS = 1 << 18
-_RESTYPE = {"pfm_last_error": ctypes.c_char_p, "pfm_status_string": ctypes.c_char_p}
+_RESTYPE = {"pfm_last_error": ctypes.c_char_p, "pfm_status_string": ctypes.c_char_p,
+            "pfm_batch_last_error": ctypes.c_char_p}
 
 _lib = None
 

@@ -90,6 +90,34 @@ def jittered(res, dx, ppc, seed=0):
     return ((lat + u) * np.float32(dx / axis)).astype(np.float32)
 
 
+def vortex_blobs2(res, dx, seed):
+    """Face velocity of 2-8 Gaussian-core point vortices for one scene of the batched workload:
+    centres uniform in [0.2, 0.8]^2 (of the unit-height domain), circulation uniform in
+    +-[0.5, 1.5], core sigma uniform in [0.01, 0.04], all drawn from numpy default_rng(seed).  Each
+    blob adds u = G / (2 pi) (1 - exp(-r^2 / sigma^2)) / r^2 (-(y - yc), x - xc) (the Gaussian-core
+    profile of 2D/init_conditions.py:5-9), evaluated in f64 at the face centres and cast to f32."""
+    rng = np.random.default_rng(seed)
+    nb = int(rng.integers(2, 9))
+    c = rng.uniform(0.2, 0.8, size=(nb, 2))
+    g = rng.uniform(0.5, 1.5, size=nb) * rng.choice([-1.0, 1.0], size=nb)
+    sig = rng.uniform(0.01, 0.04, size=nb)
+    nx, ny = res
+    out = []
+    for fam in range(2):
+        shp = (nx + (fam == 0), ny + (fam == 1))
+        ii, jj = np.meshgrid(np.arange(shp[0], dtype=np.float64), np.arange(shp[1], dtype=np.float64), indexing="ij")
+        x = (ii + (0.0 if fam == 0 else 0.5)) * dx
+        y = (jj + (0.0 if fam == 1 else 0.5)) * dx
+        u = np.zeros(shp)
+        for k in range(nb):
+            rx, ry = x - c[k, 0], y - c[k, 1]
+            r2 = rx * rx + ry * ry + 1e-12
+            f = g[k] / (2 * np.pi) * (1.0 - np.exp(-r2 / sig[k] ** 2)) / r2
+            u += f * (-ry if fam == 0 else rx)
+        out.append(u.astype(np.float32))
+    return out
+
+
 class DtClock:
     """CFL step with the frame clamp of run_3D.py:725-743 / run_2D.py:782-799 (Python doubles)."""
 
@@ -321,6 +349,20 @@ class Sim2D:
     def step_info(self):
         """Graph mode: the device step state after the last step (a host sync)."""
         return self.scene.step_info()
+
+    def set_graph(self, on):
+        """Switches between graph steps and eager phase calls, handing the frame clock and the
+        reinitialisation schedule over between the device and the host."""
+        on = bool(on)
+        if on == self.graph:
+            return
+        if not on and getattr(self, "_gargs", None) is not None:
+            info = self.scene.step_info()
+            self.ik, self.clock.sub_t, self.clock.frame_idx = info.ik, info.sub_t, info.frame_idx
+            self.last_dt = info.dt if info.step >= 0 else self.last_dt
+        elif on and getattr(self, "_gargs", None) is not None:
+            self.scene.step_reset(self.i, self.ik, self.clock.sub_t, self.clock.frame_idx)
+        self.graph = on
 
     def step(self):
         if self.graph:
