@@ -114,6 +114,16 @@ int pfm_mg_levels(const pfm_handle* h, int* levels);
 /* Number of kernels launched through this handle since pfm_create (bookkeeping for benchmarks). */
 int pfm_launch_count(const pfm_handle* h, uint64_t* launches);
 
+/* Launch-shape tunables of a handle.  Every value gives the same results bit for bit (the sums keep
+ * their order); they only change how the work maps to the GPU.  Setting one drops the handle's
+ * captured graphs (they are rebuilt on next use); a batch that holds the handle must be rebuilt
+ * (a new pfm_batch).  pfm.tune.autotune picks them by timing on a scene's own data. */
+#define PFM_TUNE_P2G2_COLUMN 1    /* faces per thread of the 2D P2G column gather, 1..64 (8) */
+#define PFM_TUNE_MG_TAIL_CELLS 2  /* MGPCG levels with at most this many cells run the rest of the
+                                     V-cycle in one thread block; 0 = none (4096) */
+int pfm_set_tuning(pfm_handle* h, int key, int value);
+int pfm_get_tuning(const pfm_handle* h, int key, int* value);
+
 /* ---- 3D step phases ------------------------------------------------------------------------ */
 
 /* calc_max_speed (3D/run_3D.py:95-103): max over cells of the centre-averaged speed, floor 1e-3.

@@ -217,6 +217,8 @@ int pfm_create(const pfm_config* cfg, pfm_handle** out) {
   h->o_step = take(sizeof(StepCtl));
 
   h->ws_need = off;
+  h->p2g2_column = 8;
+  h->tail_cells = 4096;
   if (cudaHostAlloc((void**)&h->h_state, sizeof(SolveState), cudaHostAllocDefault) != cudaSuccess) {
     cudaGetLastError();
     delete h;
@@ -267,6 +269,36 @@ int pfm_set_workspace(pfm_handle* h, void* dptr, size_t bytes) {
 int pfm_launch_count(const pfm_handle* h, uint64_t* launches) {
   if (!h || !launches) return PFM_ERR_NULL;
   *launches = h->launches;
+  return PFM_OK;
+}
+
+int pfm_set_tuning(pfm_handle* h, int key, int value) {
+  if (!h) return PFM_ERR_NULL;
+  int rc = PFM_OK;
+  if (key == PFM_TUNE_P2G2_COLUMN) {
+    if (value < 1 || value > 64) return set_error(h, PFM_ERR_ARG, "P2G column length must be 1..64");
+    h->p2g2_column = value;
+  } else if (key == PFM_TUNE_MG_TAIL_CELLS) {
+    rc = set_tail_cells(h, value);
+  } else {
+    return set_error(h, PFM_ERR_ARG, "unknown tuning key");
+  }
+  if (rc) return rc;
+  // captured graphs bake the old value in
+  if (h->g_setup) cudaGraphExecDestroy(h->g_setup);
+  if (h->g_loop) cudaGraphExecDestroy(h->g_loop);
+  if (h->g_step) cudaGraphExecDestroy(h->g_step);
+  h->g_setup = h->g_loop = h->g_step = nullptr;
+  h->g_valid = 0;
+  h->step_key.clear();
+  return PFM_OK;
+}
+
+int pfm_get_tuning(const pfm_handle* h, int key, int* value) {
+  if (!h || !value) return PFM_ERR_NULL;
+  if (key == PFM_TUNE_P2G2_COLUMN) *value = h->p2g2_column;
+  else if (key == PFM_TUNE_MG_TAIL_CELLS) *value = h->tail_cells;
+  else return PFM_ERR_ARG;
   return PFM_OK;
 }
 

@@ -130,6 +130,10 @@ struct pfm_handle {
   int g_setup_nodes, g_body_nodes;
   double g_eps, g_tol;
   int g_mode, g_valid, g_max_iters, g_chunk, g_variant, g_true_every;
+  // tunables (pfm_set_tuning): faces per thread of the 2D P2G column gather; MGPCG levels with at
+  // most tail_cells cells run in one thread block
+  int p2g2_column;
+  int tail_cells;
   // whole-step graph (pfm3_step / pfm2_step), rebuilt when its fields or parameters change
   cudaGraphExec_t g_step;
   std::string step_key;
@@ -504,6 +508,10 @@ int p2g3_from_records(pfm_handle* h, float* const* us, float* const* ws, cudaStr
 P2GRecords3 records3(pfm_handle* h, const float* init_imp, const float* T_init, const float* init_C);
 int launch_rk4_T_forward2(pfm_handle* h, float* pos, float* T, const MacFields2& F, float dt, int advect_psi,
                           cudaStream_t st, const float* dt_dev);
+
+// Sets the MGPCG tail threshold and the shared-memory limit of the one-block V-cycle tail
+// (pfm_mgpcg.cu).
+int set_tail_cells(pfm_handle* h, int cells);
 
 // Counting sort of the particle cells (pfm_p2g.cu).
 int sort_particles(pfm_handle* h, const float* pos, cudaStream_t st);

@@ -527,11 +527,10 @@ __global__ void k_loop_cond(const SolveState* st, cudaGraphConditionalHandle con
 // ---------------------------------------------------------------------------------------------
 // coarse-level V-cycle tail in one CTA
 // ---------------------------------------------------------------------------------------------
-// Levels whose cell count fits kTailMaxCells run the rest of the V-cycle (pre-smoothing,
+// Levels whose cell count fits the handle's tail_cells (4096 by default) run the rest of the V-cycle (pre-smoothing,
 // restriction, the bottom sweeps, prolongation, post-smoothing; 3D/mgpcg.py:182-200) inside one
 // thread block, with the level vectors in shared memory and __syncthreads() between half-sweeps.
 // Each cell update is the same expression as in the grid-wide kernels, in the same sweep order.
-constexpr int kTailMaxCells = 4096;
 constexpr int kTailThreads = 1024;
 
 struct TailPlan {
@@ -675,8 +674,40 @@ static void smooth_launch(pfm_handle* h, int l, int phase, const SolveState* st,
 
 static int tail_level(const pfm_handle* h) {
   for (int l = 0; l < h->L; ++l)
-    if (h->lv[l].count <= kTailMaxCells) return l;
+    if (h->lv[l].count <= h->tail_cells) return l;
   return h->L;  // no level small enough: every level runs as grid-wide kernels
+}
+
+// Shared memory of the tail kernel (z and r of the tail levels, f32) for a threshold.
+static size_t tail_smem(const pfm_handle* h, int cells) {
+  size_t total = 0;
+  bool in = false;
+  for (int l = 0; l < h->L; ++l) {
+    if (h->lv[l].count <= cells) in = true;
+    if (in) total += (size_t)h->lv[l].count;
+  }
+  return total * 2 * sizeof(float);
+}
+
+template <int D, typename S>
+static cudaError_t allow_tail_smem(size_t bytes) {
+  return cudaFuncSetAttribute(k_vcycle_tail<D, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+int set_tail_cells(pfm_handle* h, int cells) {
+  if (cells < 0) return set_error(h, PFM_ERR_ARG, "tail_cells must be >= 0");
+  const size_t bytes = tail_smem(h, cells);
+  if (bytes > 227 * 1024) return set_error(h, PFM_ERR_ARG, "tail_cells: the tail levels exceed 227 KB of shared memory");
+  if (bytes > 48 * 1024) {  // above the default dynamic shared-memory limit: opt in (once per kernel)
+    cudaError_t e = h->cfg.dim == 3 ? allow_tail_smem<3, float>(bytes) : allow_tail_smem<2, float>(bytes);
+    if (e == cudaSuccess) e = h->cfg.dim == 3 ? allow_tail_smem<3, __half>(bytes) : allow_tail_smem<2, __half>(bytes);
+    if (e == cudaSuccess)
+      e = h->cfg.dim == 3 ? allow_tail_smem<3, __nv_bfloat16>(bytes) : allow_tail_smem<2, __nv_bfloat16>(bytes);
+    int rc = check_cuda(h, e, "tail shared memory");
+    if (rc) return rc;
+  }
+  h->tail_cells = cells;
+  return PFM_OK;
 }
 
 // apply_preconditioner (3D/mgpcg.py:182-200) with level storage S

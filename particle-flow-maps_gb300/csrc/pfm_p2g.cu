@@ -18,7 +18,6 @@
 namespace pfm {
 
 constexpr int kBinThreads = 256;
-constexpr int kColumn2 = 8;   // faces per thread along j (2D column gather)
 
 // cell key + slot in the bin (slot order is arbitrary here; fixed by k_cell_sort)
 template <int D>
@@ -909,7 +908,7 @@ int pfm2_p2g(pfm_handle* h, const float* imp, const float* pos, const float* C, 
   const int* start = ws_ptr<int>(h, h->o_start);
   for (int f = 0; f < 2; ++f) {
     const int n1 = h->geom.n[f][1];
-    const int K = n1 < kColumn2 ? n1 : kColumn2;
+    const int K = n1 < h->p2g2_column ? n1 : h->p2g2_column;
     const int64_t ncol = (int64_t)h->geom.n[f][0] * ((n1 + K - 1) / K);
     if (f == 0) launch(h, k_gather2<0>, grid_for(ncol, 128), 128, 0, st, pos4, famrec, start, h->geom, K,
                        h->cfg.use_apic, h->P, us[f], ws[f], ps[f]);

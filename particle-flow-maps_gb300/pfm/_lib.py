@@ -139,7 +139,12 @@ SIGNATURES = {
     "pfm_batch_add2": [_P, _P, ctypes.POINTER(Step2Fields), ctypes.POINTER(StepParams)],
     "pfm_batch_step": [_P, _P],
     "pfm_batch_last_error": [_P],
+    "pfm_set_tuning": [_P, _I, _I],
+    "pfm_get_tuning": [_P, _I, ctypes.POINTER(_I)],
 }
+# tuning keys (include/pfm.h)
+TUNE_P2G2_COLUMN = 1
+TUNE_MG_TAIL_CELLS = 2
 # scratch limits of pfm_sort_particles_noalloc (include/pfm.h)
 NOALLOC_MAX_PARTICLES = 1 << 21
 NOALLOC_MAX_CELLS = 1 << 18

@@ -376,6 +376,15 @@ class Scene:
         self._part(pos, self.dim, "pos")
         self._check(self.lib.pfm_seed_jittered(self.h, ctypes.c_uint64(seed), int(ppc_axis), _ptr(pos), self._stream()))
 
+    def set_tuning(self, key, value):
+        """pfm_set_tuning: a launch-shape tunable (results are the same for every value)."""
+        self._check(self.lib.pfm_set_tuning(self.h, int(key), int(value)))
+
+    def get_tuning(self, key):
+        v = ctypes.c_int()
+        self._check(self.lib.pfm_get_tuning(self.h, int(key), ctypes.byref(v)))
+        return v.value
+
     @property
     def launches(self):
         n = ctypes.c_uint64()

@@ -61,11 +61,22 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--eager-steps", type=int, default=10)
     ap.add_argument("--scale", type=int, default=1, help="divide every scene's resolution (quick runs)")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes")
     args = ap.parse_args()
     import torch
     import pfm
+    from pfm import tune
     torch.cuda.set_device(0)
     sims = make_scenes(args.scale)
+    if not args.no_tune:  # one autotune per scene size, applied to every scene of that size
+        chosen = {}
+        for s in sims:
+            if s.res not in chosen:
+                chosen[s.res] = tune.autotune(s)
+            else:
+                tune.apply(s, chosen[s.res])
+        print(json.dumps({"autotune": {"%dx%d" % r: {k: {"chosen": v[0], "ms": v[1]} for k, v in c.items()}
+                                       for r, c in chosen.items()}}), flush=True)
     P = sum(s.P for s in sims)
     cells = sum(s.res[0] * s.res[1] for s in sims)
     n = len(sims)

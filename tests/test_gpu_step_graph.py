@@ -130,3 +130,30 @@ def test_batch_equals_scenes_alone():
         assert torch.equal(a.pos, b.pos) and torch.equal(a.p, b.p)
         info = b.step_info()
         assert info.step == a.i == 5 and info.dt == a.last_dt
+
+
+def test_tunables_do_not_change_results():
+    """The autotuner's knobs (2D P2G column length, MGPCG tail threshold) change launch shapes only:
+    steps with different values are bitwise equal."""
+    from pfm import tune
+    res = (64, 48)
+    dx = 1.0 / 48
+    u = pfm.vortex_blobs2(res, dx, seed=9)
+    seeds = pfm.jittered(res, dx, 4, seed=3)
+    kw = dict(reinit_every=4, reinit_every_grad_m=2, poisson_opts=dict(tol=1e-6, tol_mode=1, max_iters=400))
+    a = pfm.Sim2D(u, seeds, res, dx, graph=True, **kw)
+    b = pfm.Sim2D(u, seeds, res, dx, graph=True, **kw)
+    b.scene.set_tuning(1, 3)
+    b.scene.set_tuning(2, 0)
+    for _ in range(5):
+        a.step()
+        b.step()
+    torch.cuda.synchronize()
+    for f in range(2):
+        assert torch.equal(a.u[f], b.u[f])
+    assert torch.equal(a.p, b.p) and torch.equal(a.pos, b.pos)
+    chosen = tune.autotune(a, reps=1)
+    assert set(chosen) == {"mg_tail_cells", "p2g2_column"}
+    assert a.scene.get_tuning(2) == chosen["mg_tail_cells"][0]
+    with pytest.raises(pfm.PfmError):
+        a.scene.set_tuning(1, 0)
