@@ -477,6 +477,95 @@ int pfm_divergence(pfm_handle* h, const float* u_x, const float* u_y, const floa
                    void* stream);
 int pfm_subtract_grad_p(pfm_handle* h, float* u_x, float* u_y, float* u_z, const float* p, void* stream);
 
+/* The Boussinesq smoke plume that trains and evaluates the learned warm start (the reference has
+ * no forces or plume; these run around its unchanged step).  rho is a cell field [nx][ny][nz].
+ *  - plume_source: rho = value in the cells whose centre lies within `radius` of (cx, cy, cz);
+ *  - advect_density: rho1(x) = rho0(x - dt u(x)), u averaged from the faces to the cell centre,
+ *    trilinear sampling clamped to the cell centres (rho0 != rho1);
+ *  - add_buoyancy_impulse: the force coef * rho(x_p) along `axis` applied to each particle's
+ *    impulse: init_imp += M^-1 f with M = cols(T_gm) cols(T_init), the map P2G applies to init_imp
+ *    (3D/run_3D.py:462-475), so the impulse P2G sees grows by f (coef = dt * buoyancy). */
+int pfm3_plume_source(pfm_handle* h, float* rho, float cx, float cy, float cz, float radius, float value,
+                      void* stream);
+int pfm3_advect_density(pfm_handle* h, const float* rho0, float* rho1, const float* u_x, const float* u_y,
+                        const float* u_z, float dt, void* stream);
+int pfm3_add_buoyancy_impulse(pfm_handle* h, const float* pos, const float* T_gm, const float* T_init, float* init_imp,
+                              const float* rho, float coef, int axis, void* stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * Learned warm start: the layers of the pressure U-Net (the learned variant beside the solver;
+ * the reference has no network -- these entry points serve pfm.nn, which predicts an initial
+ * pressure that MGPCG (3D/mgpcg.py:202-280) then refines to the same residual).
+ *
+ * Activations are BF16 "channel-blocked": C channels on an d0 x d1 x d2 grid (d2 fastest) are
+ * [C/8][d0][d1][d2][8].  Weights are f32 masters W [cout][cin][27] (tap = 9 a + 3 b + c for the
+ * offsets (a-1, b-1, c-1) along d0, d1, d2: cross-correlation with zero padding), packed to BF16
+ * by pfm_nn_pack_weights.  Every convolution accumulates in F32 on the tensor cores.  `err` is a
+ * device int that a kernel sets nonzero if one of its bounded waits gave up (a CUDA fault
+ * otherwise never passes silently: the caller checks it after synchronizing).
+ * ------------------------------------------------------------------------------------------- */
+typedef struct pfm_conv3_args {
+  int d0, d1, d2;       /* grid */
+  const void* x1;       /* input, c1 channels (multiple of 16) */
+  int c1;
+  const void* x2;       /* optional second input concatenated after x1 (c2 multiple of 16, or 0) */
+  int c2;
+  const void* w;        /* packed [27][(c1+c2)/8][npad][8], npad = cout rounded up to 16 */
+  const float* bias;    /* [cout] or NULL */
+  int cout;             /* output channels, <= 128 */
+  int relu;             /* 1: max(0, .) */
+  void* y1;             /* BF16 channel-blocked output of channels [0, cy1) */
+  int cy1;
+  void* y2;             /* channels [cy1, cout) (NULL if cy1 == cout) */
+  float* yf;            /* if not NULL: F32 planar output [cout][d0][d1][d2] instead of y1/y2 */
+  const float* yf_scale;/* device scalar multiplying yf (NULL: 1) */
+  int* err;
+} pfm_conv3_args;
+
+typedef struct pfm_conv3_wgrad_args {
+  int d0, d1, d2;
+  const void* x1;       /* the layer's input(s), as in pfm_conv3_args */
+  int c1;
+  const void* x2;
+  int c2;
+  const void* dy;       /* gradient of the layer's pre-activation output, cdy channels (multiple of 8) */
+  int cdy;
+  int cout;             /* real output channels (<= cdy) */
+  float* dw;            /* out: dL/dW [cout][c1+c2][27], overwritten */
+  float* partial;       /* device workspace of pfm_nn_wgrad_workspace bytes */
+  size_t partial_bytes;
+  int* err;
+} pfm_conv3_wgrad_args;
+
+/* 3x3x3 convolution, stride 1, zero padding (forward, or the data gradient with flipped weights). */
+int pfm_nn_conv3(const pfm_conv3_args* a, void* stream);
+/* Weight gradient dW = sum over voxels of x(v + tap) dy(v); deterministic. */
+int pfm_nn_conv3_wgrad(const pfm_conv3_wgrad_args* a, void* stream);
+int pfm_nn_wgrad_workspace(const pfm_conv3_wgrad_args* a, size_t* bytes);
+/* Packs W [cout][cin][27] into [27][kin/8][npad][8] BF16 for the forward (flip 0: rows = cout,
+ * K = cin) or the data gradient (flip 1: rows = cin, K = cout, taps mirrored). */
+int pfm_nn_pack_weights(const float* W, int cout, int cin, int flip, int kin, int npad, void* wp, void* stream);
+/* A scalar field f [d0][d1][d2] -> 16-channel block tensor, channel 0 = f * (*inv_scale). */
+int pfm_nn_pack_scalar(const float* f, int d0, int d1, int d2, const float* inv_scale, void* x, void* stream);
+/* mode 0: 2x2x2 average pool of the fine grid d0 x d1 x d2; 1: its backward; 2: nearest
+ * upsampling to the fine grid; 3: its backward (sum of the 8 children). */
+int pfm_nn_resample(const void* in, void* out, int channels, int d0, int d1, int d2, int mode, void* stream);
+/* mode 0: g *= (y > 0) (ReLU backward); mode 1: g += y.  `elements` = channels x voxels. */
+int pfm_nn_elementwise(void* g, const void* y, size_t elements, int mode, void* stream);
+/* floats of scratch that pfm_nn_bias_grad / pfm_nn_loss need for `channels` channels */
+size_t pfm_nn_scratch_floats(int channels);
+/* db[c] = sum over voxels of dy channel c, c < cout (deterministic). */
+int pfm_nn_bias_grad(const void* dy, int channels, int d0, int d1, int d2, int cout, float* db, float* scratch,
+                     void* stream);
+/* e = pred - target * (*inv_scale): out4 = {mean(e^2) - mean(e)^2, mean e, 1 / rms(e), rms(e)};
+ * with grad != NULL also dL/dpred as channel 0 of a 16-channel block tensor.  pred = NULL gives
+ * the RMS of the target (the scale of a right-hand side). */
+int pfm_nn_loss(const float* pred, const float* target, const float* inv_scale, int d0, int d1, int d2,
+                float* out4, void* grad, float* scratch, void* stream);
+/* Adam step (bias-corrected, step >= 1) on f32 parameters with the gradient times gscale. */
+int pfm_nn_adam(float* p, const float* g, float* m, float* v, size_t n, float lr, float beta1, float beta2,
+                float eps, int step, float gscale, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -422,7 +422,8 @@ struct MG {
 
   // solve(max_iters, eps, tol): mgpcg.py:202-280.  Returns the iteration reported by the
   // reference's print (it at convergence), or -max_iters when it returns without converging.
-  // tol_mode 0: the reference's r.r < tol; 1: |r| < tol |r0| with r0 the recentred initial residual.
+  // tol_mode 0: the reference's r.r < tol; 1: |r| < tol |r0| with r0 the recentred initial residual
+  // (an exactly zero residual also stops: a zero right-hand side).
   int solve(int max_iters, double eps, double tol, double* final_rTr, int tol_mode = 0, double beta_in = 0.0) {
     bool all_neumann = true;
     for (int d = 0; d < dim; ++d)
@@ -443,7 +444,7 @@ struct MG {
       for (size_t q = 0; q < n0; ++q) x[q] += alpha * p[q];
       for (size_t q = 0; q < n0; ++q) r[0][q] -= alpha * Ap[q];
       rTr = (double)reduce(r[0].data(), r[0].data());
-      bool stop = tol_mode == 0 ? (rTr < tol) : (std::sqrt(rTr) < tol * std::sqrt(rTr0));
+      bool stop = tol_mode == 0 ? (rTr < tol) : (rTr == 0.0 || std::sqrt(rTr) < tol * std::sqrt(rTr0));
       if (stop) {
         *final_rTr = rTr;
         return it;

@@ -317,11 +317,12 @@ struct CompSum {
   __device__ __forceinline__ double value() const { return (double)s + (double)c; }
 };
 
-// the stopping rule of k_update_xr / k_true_residual
+// the stopping rule of k_update_xr / k_true_residual; the relative rules accept an exactly zero
+// residual, so a zero right-hand side (a fluid at rest) ends at the first check
 __device__ __forceinline__ bool converged(double rTr, const SolveState* st, double tol, int tol_mode) {
   if (tol_mode == 0) return rTr < tol;
   const double ref = (tol_mode == 1) ? st->rTr0 : st->bTb;
-  return sqrt(rTr) < tol * sqrt(ref);
+  return rTr == 0.0 || sqrt(rTr) < tol * sqrt(ref);
 }
 
 // sum(a*b) (or sum(a) for RED_MEAN) with a finalizer that updates the solve state.  Per-thread

@@ -69,6 +69,21 @@ class StepInfo(ctypes.Structure):
                 ("rTr", ctypes.c_double * 2), ("history", (ctypes.c_int * 2) * 64)]
 
 
+class Conv3Args(ctypes.Structure):
+    _fields_ = [("d0", ctypes.c_int), ("d1", ctypes.c_int), ("d2", ctypes.c_int), ("x1", ctypes.c_void_p),
+                ("c1", ctypes.c_int), ("x2", ctypes.c_void_p), ("c2", ctypes.c_int), ("w", ctypes.c_void_p),
+                ("bias", ctypes.c_void_p), ("cout", ctypes.c_int), ("relu", ctypes.c_int), ("y1", ctypes.c_void_p),
+                ("cy1", ctypes.c_int), ("y2", ctypes.c_void_p), ("yf", ctypes.c_void_p),
+                ("yf_scale", ctypes.c_void_p), ("err", ctypes.c_void_p)]
+
+
+class Conv3WgradArgs(ctypes.Structure):
+    _fields_ = [("d0", ctypes.c_int), ("d1", ctypes.c_int), ("d2", ctypes.c_int), ("x1", ctypes.c_void_p),
+                ("c1", ctypes.c_int), ("x2", ctypes.c_void_p), ("c2", ctypes.c_int), ("dy", ctypes.c_void_p),
+                ("cdy", ctypes.c_int), ("cout", ctypes.c_int), ("dw", ctypes.c_void_p),
+                ("partial", ctypes.c_void_p), ("partial_bytes", ctypes.c_size_t), ("err", ctypes.c_void_p)]
+
+
 # name -> argument types (all return int status unless listed in _RESTYPE)
 _P = ctypes.c_void_p
 _I = ctypes.c_int
@@ -141,6 +156,20 @@ SIGNATURES = {
     "pfm_batch_last_error": [_P],
     "pfm_set_tuning": [_P, _I, _I],
     "pfm_get_tuning": [_P, _I, ctypes.POINTER(_I)],
+    "pfm3_plume_source": [_P, _P, _F, _F, _F, _F, _F, _P],
+    "pfm3_advect_density": [_P, _P, _P, _P, _P, _P, _F, _P],
+    "pfm3_add_buoyancy_impulse": [_P, _P, _P, _P, _P, _P, _F, _I, _P],
+    "pfm_nn_conv3": [ctypes.POINTER(Conv3Args), _P],
+    "pfm_nn_conv3_wgrad": [ctypes.POINTER(Conv3WgradArgs), _P],
+    "pfm_nn_wgrad_workspace": [ctypes.POINTER(Conv3WgradArgs), ctypes.POINTER(ctypes.c_size_t)],
+    "pfm_nn_pack_weights": [_P, _I, _I, _I, _I, _I, _P, _P],
+    "pfm_nn_pack_scalar": [_P, _I, _I, _I, _P, _P, _P],
+    "pfm_nn_resample": [_P, _P, _I, _I, _I, _I, _I, _P],
+    "pfm_nn_elementwise": [_P, _P, ctypes.c_size_t, _I, _P],
+    "pfm_nn_scratch_floats": [_I],
+    "pfm_nn_bias_grad": [_P, _I, _I, _I, _I, _I, _P, _P, _P],
+    "pfm_nn_loss": [_P, _P, _P, _I, _I, _I, _P, _P, _P, _P],
+    "pfm_nn_adam": [_P, _P, _P, _P, ctypes.c_size_t, _F, _F, _F, _F, _I, _F, _P],
 }
 # tuning keys (include/pfm.h)
 TUNE_P2G2_COLUMN = 1
@@ -149,7 +178,7 @@ TUNE_MG_TAIL_CELLS = 2
 NOALLOC_MAX_PARTICLES = 1 << 21
 NOALLOC_MAX_CELLS = 1 << 18
 _RESTYPE = {"pfm_last_error": ctypes.c_char_p, "pfm_status_string": ctypes.c_char_p,
-            "pfm_batch_last_error": ctypes.c_char_p}
+            "pfm_batch_last_error": ctypes.c_char_p, "pfm_nn_scratch_floats": ctypes.c_size_t}
 
 _lib = None
 

@@ -7,6 +7,7 @@ import numpy as np
 import torch
 
 from . import _lib
+from ._lib import PfmError
 from .core import Scene
 
 __all__ = ["DtClock", "Sim3D", "Sim2D", "soa", "aos", "soa_T", "aos_T", "lattice3", "lattice2",
@@ -188,6 +189,9 @@ class Sim3D:
         self.infos = []
         self.last_dt = None
         self.timer = None
+        # optional callbacks of scenes built on this step (pfm.plume): before_rk4(dt) after the
+        # midpoint solve, before_poisson() -> overrides of the final solve's options, after_step(dt)
+        self.before_rk4 = self.before_poisson = self.after_step = None
 
     def _t(self, name):
         import contextlib
@@ -231,6 +235,8 @@ class Sim3D:
 
     def step(self):
         if self.graph:  # the whole step as one graph launch; dt and the solves stay on the device
+            if self.before_rk4 or self.before_poisson or self.after_step:
+                raise PfmError(7, "step callbacks run only with eager steps (graph=False)")
             f, prm = self._graph_args()
             self.scene.step_graph(f, prm)
             self.i += 1
@@ -266,6 +272,8 @@ class Sim3D:
             with self._t("poisson_mid"):
                 self.infos.append(sc.poisson(self.u_mid, self.p_mid, **self.poisson_opts))
             adv = self.u_mid
+        if self.before_rk4 is not None:
+            self.before_rk4(curr_dt)
         if self.fused_rk4_p2g:
             with self._t("rk4"):
                 if k == 0:
@@ -281,8 +289,13 @@ class Sim3D:
                 sc.rk4_T_forward(self.pos, self.T_gm, adv, float(np.float32(curr_dt)))
             with self._t("p2g"):
                 sc.p2g3(self.init_imp, self.pos, self.T_gm, self.T_init, self.init_C, self.u, self.w)
+        opts = self.poisson_opts
+        if self.before_poisson is not None:
+            opts = dict(opts, **(self.before_poisson() or {}))
         with self._t("poisson"):
-            self.infos.append(sc.poisson(self.u, self.p, **self.poisson_opts))
+            self.infos.append(sc.poisson(self.u, self.p, **opts))
+        if self.after_step is not None:
+            self.after_step(curr_dt)
         return curr_dt
 
 
