@@ -192,6 +192,7 @@ class Sim3D:
         # optional callbacks of scenes built on this step (pfm.plume): before_rk4(dt) after the
         # midpoint solve, before_poisson() -> overrides of the final solve's options, after_step(dt)
         self.before_rk4 = self.before_poisson = self.after_step = None
+        self.poisson_mid_opts = None  # options of the midpoint solve if they differ (eager steps)
 
     def _t(self, name):
         import contextlib
@@ -270,7 +271,7 @@ class Sim3D:
             with self._t("midpoint"):
                 sc.midpoint(self.u, self.u_mid, float(np.float32(0.5 * curr_dt)))
             with self._t("poisson_mid"):
-                self.infos.append(sc.poisson(self.u_mid, self.p_mid, **self.poisson_opts))
+                self.infos.append(sc.poisson(self.u_mid, self.p_mid, **(self.poisson_mid_opts or self.poisson_opts)))
             adv = self.u_mid
         if self.before_rk4 is not None:
             self.before_rk4(curr_dt)

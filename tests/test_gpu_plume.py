@@ -85,7 +85,7 @@ def test_plume_run_and_guess_path():
     for _ in range(6):
         sim.step()
     torch.cuda.synchronize()
-    assert all(i.converged for i in sim.infos)
+    assert all(i.converged for i in sim.infos), [repr(i) for i in sim.infos]
     rho = sim.rho.cpu().numpy()
     assert rho.max() == 1.0 and rho.sum() > 20
     uy = sim.u[1].cpu().numpy()
