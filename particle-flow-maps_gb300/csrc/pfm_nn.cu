@@ -183,6 +183,7 @@ struct ConvFwdParams {
   int cin, c1;         // input channels (x1 holds the first c1)
   int npad, cout;      // MMA N (multiple of 16) and real output channels
   int ncols;           // TMEM columns allocated
+  int nstage;          // weight ring depth in taps (27: every tap's weights loaded up front)
   uint32_t idesc;
   const __nv_bfloat16* w;  // [27][cin/8][npad][8]
   const float* bias;       // [cout] or null
@@ -211,19 +212,20 @@ __global__ void __launch_bounds__(kThreads) k_conv3_fwd(const __grid_constant__ 
   const uint32_t stage_bytes = (uint32_t)p.npad * p.cin * 2;
   unsigned char* box = smem;
   unsigned char* wring = smem + ((box_bytes + 127) & ~127u);
-  uint64_t* bars = (uint64_t*)(wring + kStages * stage_bytes);
+  const int ns = p.nstage;
+  uint64_t* bars = (uint64_t*)(wring + ns * stage_bytes);
   uint64_t* box_bar = bars;
   uint64_t* full = bars + 1;
-  uint64_t* done = bars + 1 + kStages;
-  uint64_t* final_bar = bars + 1 + 2 * kStages;
-  uint32_t* slot = (uint32_t*)(bars + 2 + 2 * kStages);
+  uint64_t* done = bars + 1 + ns;
+  uint64_t* final_bar = bars + 1 + 2 * ns;
+  uint32_t* slot = (uint32_t*)(bars + 2 + 2 * ns);
 
   const int t1 = blockIdx.x / p.tiles2, t2 = blockIdx.x - t1 * p.tiles2;
   const int z = blockIdx.y, y0 = t1 * kTileD1, x0 = t2 * kTileD2;
 
   if (tid == 0) {
     mbar_init(box_bar, 1);
-    for (int s = 0; s < kStages; ++s) {
+    for (int s = 0; s < ns; ++s) {
       mbar_init(full + s, 1);
       mbar_init(done + s, 1);
     }
@@ -241,7 +243,7 @@ __global__ void __launch_bounds__(kThreads) k_conv3_fwd(const __grid_constant__ 
     mbar_expect_tx(box_bar, box_bytes);
     tma_load_5d(box, &tm1, 0, x0 - 1, y0 - 1, z - 1, 0, box_bar);
     if (p.cin > p.c1) tma_load_5d(box + (size_t)(p.c1 >> 3) * kChunkBytes, &tm2, 0, x0 - 1, y0 - 1, z - 1, 0, box_bar);
-    for (int t = 0; t < kStages; ++t) {
+    for (int t = 0; t < ns; ++t) {
       mbar_expect_tx(full + t, stage_bytes);
       bulk_load(wring + t * stage_bytes, (const unsigned char*)p.w + (size_t)t * stage_bytes, stage_bytes, full + t);
     }
@@ -249,8 +251,8 @@ __global__ void __launch_bounds__(kThreads) k_conv3_fwd(const __grid_constant__ 
     const uint32_t box_addr = su32(box), ring_addr = su32(wring);
     const uint32_t blbo = (uint32_t)p.npad * 16;
     for (int t = 0; t < 27 && ok; ++t) {
-      const int s = t % kStages;
-      ok = mbar_wait(full + s, (t / kStages) & 1, p.err, 2);
+      const int s = t % ns;
+      ok = mbar_wait(full + s, (t / ns) & 1, p.err, 2);
       if (!ok) break;
       tc_fence_after();
       const int a = t / 9, b = (t / 3) % 3, c = t % 3;
@@ -263,12 +265,12 @@ __global__ void __launch_bounds__(kThreads) k_conv3_fwd(const __grid_constant__ 
       }
       mma_commit(done + s);
       // refill the stage the previous tap used once its MMAs have completed
-      if (t >= 1 && t - 1 + kStages < 27) {
-        const int sp = (t - 1) % kStages;
-        ok = mbar_wait(done + sp, ((t - 1) / kStages) & 1, p.err, 3);
+      if (t >= 1 && t - 1 + ns < 27) {
+        const int sp = (t - 1) % ns;
+        ok = mbar_wait(done + sp, ((t - 1) / ns) & 1, p.err, 3);
         if (!ok) break;
         mbar_expect_tx(full + sp, stage_bytes);
-        bulk_load(wring + sp * stage_bytes, (const unsigned char*)p.w + (size_t)(t - 1 + kStages) * stage_bytes,
+        bulk_load(wring + sp * stage_bytes, (const unsigned char*)p.w + (size_t)(t - 1 + ns) * stage_bytes,
                   stage_bytes, full + sp);
       }
     }
@@ -760,9 +762,11 @@ int pow2_cols(int n) {
   return c;
 }
 
-// dynamic shared memory that also keeps resident CTAs x TMEM columns within the SM's 512 columns
+// dynamic shared memory that also keeps resident CTAs x TMEM columns within the SM's 512 columns:
+// at most k = 512 / ncols CTAs may share an SM, so k + 1 CTAs (each with 1 KB reserved) must not fit
 size_t occupancy_smem(size_t need, int ncols) {
-  const size_t floor_bytes = (size_t)kSmPerGpuSmem * (size_t)ncols / 512 + 1;
+  const size_t k = 512 / (size_t)ncols;
+  const size_t floor_bytes = (size_t)kSmPerGpuSmem / (k + 1) - 1024 + 1;
   return need > floor_bytes ? need : floor_bytes;
 }
 
@@ -820,7 +824,11 @@ extern "C" int pfm_nn_conv3(const pfm_conv3_args* a, void* stream) {
   p.yf_scale = a->yf_scale;
   p.err = a->err;
   const size_t box = ((size_t)(cin / 8) * kChunkBytes + 127) & ~(size_t)127;
-  const size_t need = 1024 + box + (size_t)kStages * npad * cin * 2 + 8 * (2 + 2 * kStages) + 16;
+  // weight ring of 4 taps: deeper rings (up to all 27 taps) remove refill round trips but cost
+  // shared memory, hence CTAs per SM, and concurrent CTAs are what keeps the tensor core busy
+  const size_t stage = (size_t)npad * cin * 2;
+  p.nstage = kStages;
+  const size_t need = 1024 + box + (size_t)p.nstage * stage + 8 * (2 + 2 * p.nstage) + 16;
   const size_t smem = occupancy_smem(need, p.ncols);
   if (smem > kMaxDynSmem) return PFM_ERR_SHAPE;
   static std::once_flag attr;
