@@ -241,6 +241,90 @@ __global__ void __launch_bounds__(256) k_smooth(S* __restrict__ z, const S* __re
   stv(z + c, (ldv(r + c) + nb) / mult);
 }
 
+// Eight consecutive values along the last axis (n2 % 8 == 0, so a run is 16- or 32-byte aligned).
+__device__ __forceinline__ void ld8(const float* p, float (&v)[8]) {
+  const float4 a = *reinterpret_cast<const float4*>(p), b = *reinterpret_cast<const float4*>(p + 4);
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+__device__ __forceinline__ void st8(float* p, const float (&v)[8]) {
+  *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  *reinterpret_cast<float4*>(p + 4) = make_float4(v[4], v[5], v[6], v[7]);
+}
+template <typename H>
+__device__ __forceinline__ void ld8h(const H* p, float (&v)[8]) {
+  const uint4 u = *reinterpret_cast<const uint4*>(p);
+  const H* h = reinterpret_cast<const H*>(&u);
+#pragma unroll
+  for (int q = 0; q < 8; ++q) v[q] = ldv(h + q);
+}
+template <typename H>
+__device__ __forceinline__ void st8h(H* p, const float (&v)[8]) {
+  uint4 u;
+  H* h = reinterpret_cast<H*>(&u);
+#pragma unroll
+  for (int q = 0; q < 8; ++q) stv(h + q, v[q]);
+  *reinterpret_cast<uint4*>(p) = u;
+}
+__device__ __forceinline__ void ld8(const __half* p, float (&v)[8]) { ld8h(p, v); }
+__device__ __forceinline__ void ld8(const __nv_bfloat16* p, float (&v)[8]) { ld8h(p, v); }
+__device__ __forceinline__ void st8(__half* p, const float (&v)[8]) { st8h(p, v); }
+__device__ __forceinline__ void st8(__nv_bfloat16* p, const float (&v)[8]) { st8h(p, v); }
+
+// smooth(l, phase) in 3D with one thread per run of eight cells along the last axis: the run, r
+// and the four neighbouring runs are read as whole vectors (the cells of the other colour, which a
+// half-sweep never changes, are written back unchanged) and each cell of the colour is updated
+// with the same sum, in the same order, as stencil<3> -- bitwise the result of k_smooth.
+template <typename S>
+__global__ void __launch_bounds__(256) k_smooth8(S* __restrict__ z, const S* __restrict__ r, Lvl L, BC bc,
+                                                 int phase, const SolveState* st) {
+  if (st && st->done) return;
+  const int runs = L.n2 >> 3;
+  const unsigned e = blockIdx.x * blockDim.x + threadIdx.x;
+  if ((int64_t)e >= (int64_t)L.n0 * L.n1 * runs) return;
+  const unsigned row = e / (unsigned)runs;
+  const int k0 = (int)(e - row * (unsigned)runs) * 8;
+  const unsigned i_ = udiv(row, L.d1);
+  const int i = (int)i_, j = (int)(row - i_ * (unsigned)L.n1);
+  const int64_t sx = (int64_t)L.n1 * L.n2, sy = L.n2;
+  const int64_t c0 = ((int64_t)i * L.n1 + j) * L.n2 + k0;
+  float zc[8], rr[8], xp[8], xm[8], yp[8], ym[8];
+  ld8(z + c0, zc);
+  ld8(r + c0, rr);
+  const bool hx = i < L.n0 - 1, lx = i > 0, hy = j < L.n1 - 1, ly = j > 0;
+  if (hx) ld8(z + c0 + sx, xp);
+  if (lx) ld8(z + c0 - sx, xm);
+  if (hy) ld8(z + c0 + sy, yp);
+  if (ly) ld8(z + c0 - sy, ym);
+  const float zl = k0 > 0 ? ldv(z + c0 - 1) : 0.f;
+  const float zr = k0 + 8 < L.n2 ? ldv(z + c0 + 8) : 0.f;
+  float base = 6.f;
+  if (i <= 0 && bc.lo[0] == 2) base -= 1.f;
+  if (i >= L.n0 - 1 && bc.hi[0] == 2) base -= 1.f;
+  if (j <= 0 && bc.lo[1] == 2) base -= 1.f;
+  if (j >= L.n1 - 1 && bc.hi[1] == 2) base -= 1.f;
+  const int first = (i + j + k0 + phase) & 1;  // run offset of the first cell of the colour
+  float out[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) out[q] = zc[q];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    if ((q & 1) != first) continue;
+    const int k = k0 + q;
+    float ret = 0.f;
+    if (hx) ret += xp[q];
+    if (lx) ret += xm[q];
+    if (hy) ret += yp[q];
+    if (ly) ret += ym[q];
+    if (k < L.n2 - 1) ret += (q < 7) ? zc[q + 1] : zr;
+    if (k > 0) ret += (q > 0) ? zc[q - 1] : zl;
+    float num = base;
+    if (k <= 0 && bc.lo[2] == 2) num -= 1.f;
+    if (k >= L.n2 - 1 && bc.hi[2] == 2) num -= 1.f;
+    out[q] = (rr[q] + ret) / num;
+  }
+  st8(z + c0, out);
+}
+
 // restrict(l) as a gather: rc[I] = sum over children (fine-index order) of res/(dim-1),
 // res = r - (mult z - nbsum(z)).
 template <int D, typename S>
@@ -669,6 +753,12 @@ static void smooth_launch(pfm_handle* h, int l, int phase, const SolveState* st,
   Lvl L = lvl_of(h, l);
   const int nl = (D == 3) ? L.n2 : L.n1;
   int64_t npairs = (D == 3) ? (int64_t)L.n0 * L.n1 * ((nl + 1) / 2) : (int64_t)L.n0 * ((nl + 1) / 2);
+  if (D == 3 && L.n2 % 8 == 0) {
+    const int64_t nvec = (int64_t)L.n0 * L.n1 * (L.n2 / 8);
+    launch(h, k_smooth8<S>, grid_for(nvec, 256), 256, 0, s, level_z<S>(h, l), (const S*)level_r<S>(h, l), L,
+           bc_of(h), phase, st);
+    return;
+  }
   launch(h, k_smooth<D, S>, grid_for(npairs, 256), 256, 0, s, level_z<S>(h, l), (const S*)level_r<S>(h, l), L,
          bc_of(h), phase, st);
 }
