@@ -298,3 +298,32 @@ def test_unet_state_roundtrip_and_partial_tiles(lib):
     ref = pred / cache["s"]
     got = ya.cpu().numpy()
     assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-2
+
+
+def test_conv_argument_checks(lib):
+    """The host side rejects what the kernels cannot take: channel counts that are not multiples of
+    16 (inputs) or 8 (bf16 outputs), more than 128 channels, unaligned pointers, null pointers; no
+    kernel runs for a rejected call."""
+    from pfm import _lib
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    dims = (4, 16, 8)
+    V = int(np.prod(dims))
+    x = torch.zeros(32 * V + 8, dtype=torch.bfloat16, device="cuda")
+    w = torch.zeros(27 * 32 * 32, dtype=torch.bfloat16, device="cuda")
+    y = torch.zeros(32 * V + 8, dtype=torch.bfloat16, device="cuda")
+
+    def call(c1=16, c2=0, cout=16, cy1=None, xp=None, wp=None, yp=None, errp=None):
+        a = _lib.Conv3Args(dims[0], dims[1], dims[2], xp if xp is not None else P(x), c1, P(x) if c2 else None, c2,
+                           wp if wp is not None else P(w), None, cout, 0, yp if yp is not None else P(y),
+                           cy1 or cout, None, None, None, errp if errp is not None else P(err))
+        return lib.pfm_nn_conv3(ctypes.byref(a), None)
+
+    assert call() == 0
+    torch.cuda.synchronize()
+    assert call(c1=8) == 2 and call(c1=16, c2=8) == 2 and call(c1=144) == 2
+    assert call(cout=12) == 2 and call(cout=16, cy1=12) == 2 and call(cout=136) == 2
+    assert call(xp=ctypes.c_void_p(x.data_ptr() + 2)) == 7
+    assert call(yp=ctypes.c_void_p(y.data_ptr() + 8)) == 7
+    assert call(xp=ctypes.c_void_p(0)) == 1 and call(errp=ctypes.c_void_p(0)) == 1
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
