@@ -327,3 +327,66 @@ def test_bad_arguments_raise():
         sc.calc_max_speed([torch.zeros(9, 8, 8, device="cuda")] * 3)
     with pytest.raises(pfm.PfmError):
         sc.g2p(torch.zeros(3, 16), sc.alloc_faces(), imp_out=torch.zeros(3, 16, device="cuda"))
+
+
+def _clustered_positions(res, dx, rng):
+    """Collisions and edges of the cell binning: 5,000 particles in one cell, particles exactly on
+    grid planes and at the domain's corners and walls, and a uniform background."""
+    hi = np.array(res, np.float64) * dx
+    lone = (np.array([5, 6, 7]) + rng.uniform(0.0, 1.0, (5000, 3))) * dx
+    planes = np.floor(rng.uniform(0, 1, (600, 3)) * np.array(res)) * dx  # on cell corners and faces
+    corners = np.array([[0, 0, 0], hi, [hi[0], 0, 0], [0, hi[1], hi[2]]], np.float64)
+    walls = rng.uniform(0, 1, (400, 3)) * hi
+    walls[:200, 0] = 0.0
+    walls[200:, 2] = hi[2]
+    back = rng.uniform(0, 1, (3000, 3)) * hi
+    return np.concatenate([lone, planes, corners, walls, back]).astype(np.float32)
+
+
+def test_p2g3_and_sort_collisions_and_edges():
+    rng = np.random.default_rng(11)
+    res = (16, 12, 20)
+    dx = 1.0 / res[1]
+    pos = _clustered_positions(res, dx, rng)
+    P = pos.shape[0]
+    sc = pfm.Scene(3, res, dx, P)
+    count, order = sc.sort_particles(pfm.soa(pos))
+    cells = np.clip((pos / np.float32(dx)).astype(np.int64), 0, np.array(res) - 1)
+    key = (cells[:, 0] * res[1] + cells[:, 1]) * res[2] + cells[:, 2]
+    assert np.array_equal(host(order), np.argsort(key, kind="stable"))
+    assert np.array_equal(host(count).ravel(), np.bincount(key, minlength=int(np.prod(res))))
+    T_gm = (np.eye(3)[None] + 0.1 * rng.standard_normal((P, 3, 3))).astype(np.float32)
+    Ti = (np.eye(3)[None] + 0.1 * rng.standard_normal((P, 3, 3))).astype(np.float32)
+    C = (0.3 * rng.standard_normal((P, 3, 3))).astype(np.float32)
+    m0 = rng.standard_normal((P, 3)).astype(np.float32)
+    u, w = sc.alloc_faces(), sc.alloc_faces()
+    sc.p2g3(pfm.soa(m0), pfm.soa(pos), pfm.soa_T(T_gm), pfm.soa_T(Ti), pfm.soa_T(C), u, w)
+    (gx, gy, gz), (wx, wy, wz) = O.p2g3(m0, pos, T_gm, Ti, C, res, dx)
+    for t, o in zip(u + w, [gx, gy, gz, wx, wy, wz]):
+        assert rel(host(t), o) < TOL
+    u2, w2 = sc.alloc_faces(), sc.alloc_faces()  # and still bitwise reproducible
+    sc.p2g3(pfm.soa(m0), pfm.soa(pos), pfm.soa_T(T_gm), pfm.soa_T(Ti), pfm.soa_T(C), u2, w2)
+    for a, b in zip(u + w, u2 + w2):
+        assert torch.equal(a, b)
+
+
+def test_p2g2_collisions_and_edges():
+    rng = np.random.default_rng(12)
+    res = (24, 16)
+    dx = 1.0 / res[1]
+    hi = np.array(res, np.float64) * dx
+    pos = np.concatenate([(np.array([3, 9]) + rng.uniform(0, 1, (4000, 2))) * dx,
+                          np.floor(rng.uniform(0, 1, (300, 2)) * np.array(res)) * dx,
+                          np.array([[0, 0], hi, [hi[0], 0], [0, hi[1]]]),
+                          rng.uniform(0, 1, (1500, 2)) * hi]).astype(np.float32)
+    P = pos.shape[0]
+    sc = pfm.Scene(2, res, dx, P)
+    imp = rng.standard_normal((P, 2)).astype(np.float32)
+    C = (0.3 * rng.standard_normal((P, 2, 2))).astype(np.float32)
+    psi = (pos + 0.01 * rng.standard_normal((P, 2))).astype(np.float32)
+    u, w = sc.alloc_faces(), sc.alloc_faces()
+    psi_g = [torch.zeros(s + (2,), device="cuda") for s in sc.face_shapes]
+    sc.p2g2(pfm.soa(imp), pfm.soa(pos), pfm.soa_T(C), pfm.soa(psi), u, w, psi_out=psi_g)
+    (ox, oy), (owx, owy), (opx, opy) = O.p2g2(imp, pos, C, psi, res, dx)
+    for t, o in zip(u + w + psi_g, [ox, oy, owx, owy, opx, opy]):
+        assert rel(host(t), o) < TOL
