@@ -91,3 +91,19 @@ def test_unet_backward_matches_finite_differences(seed):
         fd = (L(th + eps * d) - L(th - eps * d)) / (2 * eps)
         an = float(g @ d)
         assert abs(fd - an) <= 1e-5 * max(abs(fd), 1e-3), (k, fd, an)
+
+
+def test_product_layer_table_matches_oracle():
+    """pfm.nn runs the same network the oracle restates, and every layer fits the tensor-core
+    kernels: inputs in multiples of 16 channels, outputs in multiples of 8 (the 1-channel output
+    layer is written in f32), skip concatenations joining tensors of the same resolution."""
+    import pfm.nn as N
+    assert [tuple(l) for l in N.LAYERS] == [tuple(l) for l in O.LAYERS]
+    level_of = {}
+    for (name, c1, c2, cout, relu, level) in N.LAYERS:
+        assert c1 % 16 == 0 and c2 % 16 == 0 and c1 + c2 <= 128
+        assert cout == 1 or cout % 8 == 0
+        level_of[name] = level
+    assert level_of["dec1a"] == level_of["enc1b"] and level_of["dec0a"] == level_of["enc0b"]
+    n_params = sum(cout * (c1 + c2) * 27 + cout for (_, c1, c2, cout, _, _) in N.LAYERS)
+    assert n_params == 360177
