@@ -121,6 +121,8 @@ int pfm_launch_count(const pfm_handle* h, uint64_t* launches);
 #define PFM_TUNE_P2G2_COLUMN 1    /* faces per thread of the 2D P2G column gather, 1..64 (8) */
 #define PFM_TUNE_MG_TAIL_CELLS 2  /* MGPCG levels with at most this many cells run the rest of the
                                      V-cycle in one thread block; 0 = none (4096) */
+#define PFM_TUNE_SMOOTH_TMA 3     /* 1: 3D 16-bit MGPCG levels are smoothed from tiles the TMA stages
+                                     in shared memory; 0: from global memory (0) */
 int pfm_set_tuning(pfm_handle* h, int key, int value);
 int pfm_get_tuning(const pfm_handle* h, int key, int* value);
 

@@ -219,6 +219,7 @@ int pfm_create(const pfm_config* cfg, pfm_handle** out) {
   h->ws_need = off;
   h->p2g2_column = 8;
   h->tail_cells = 4096;
+  h->smooth_tma = 0;
   if (cudaHostAlloc((void**)&h->h_state, sizeof(SolveState), cudaHostAllocDefault) != cudaSuccess) {
     cudaGetLastError();
     delete h;
@@ -280,6 +281,9 @@ int pfm_set_tuning(pfm_handle* h, int key, int value) {
     h->p2g2_column = value;
   } else if (key == PFM_TUNE_MG_TAIL_CELLS) {
     rc = set_tail_cells(h, value);
+  } else if (key == PFM_TUNE_SMOOTH_TMA) {
+    if (value != 0 && value != 1) return set_error(h, PFM_ERR_ARG, "smoother staging must be 0 or 1");
+    h->smooth_tma = value;
   } else {
     return set_error(h, PFM_ERR_ARG, "unknown tuning key");
   }
@@ -298,6 +302,7 @@ int pfm_get_tuning(const pfm_handle* h, int key, int* value) {
   if (!h || !value) return PFM_ERR_NULL;
   if (key == PFM_TUNE_P2G2_COLUMN) *value = h->p2g2_column;
   else if (key == PFM_TUNE_MG_TAIL_CELLS) *value = h->tail_cells;
+  else if (key == PFM_TUNE_SMOOTH_TMA) *value = h->smooth_tma;
   else return PFM_ERR_ARG;
   return PFM_OK;
 }

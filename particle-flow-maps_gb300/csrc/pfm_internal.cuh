@@ -33,7 +33,7 @@ struct SolveState {
   float mean;      // recenter mean
   float hscale;    // 16-bit level storage holds r * hscale (unit RMS), z is read back / hscale
   int it;          // completed iterations
-  int done;        // 1 converged, 2 iteration limit, 3 non-finite
+  int done;        // 1 converged, 2 iteration limit, 3 non-finite, 4 a tile copy did not arrive
   int conv_it;     // iteration index at convergence
   unsigned ticket; // last-block counter of the reductions
   int it_stop;     // the device loop pauses when `it` reaches this count
@@ -134,6 +134,7 @@ struct pfm_handle {
   // most tail_cells cells run in one thread block
   int p2g2_column;
   int tail_cells;
+  int smooth_tma;  // 3D 16-bit MGPCG levels smoothed from TMA-staged tiles (same results)
   // whole-step graph (pfm3_step / pfm2_step), rebuilt when its fields or parameters change
   cudaGraphExec_t g_step;
   std::string step_key;

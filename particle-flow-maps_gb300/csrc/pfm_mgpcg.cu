@@ -13,8 +13,10 @@
 #include <cuda_fp16.h>
 
 #include <cmath>
+#include <type_traits>
 
 #include "pfm_internal.cuh"
+#include "pfm_tma.cuh"
 
 namespace pfm {
 
@@ -323,6 +325,97 @@ __global__ void __launch_bounds__(256) k_smooth8(S* __restrict__ z, const S* __r
     out[q] = (rr[q] + ret) / num;
   }
   st8(z + c0, out);
+}
+
+// smooth(l, phase) in 3D for 16-bit level storage with the tile staged by the TMA: a block owns
+// 4 x 8 x TK cells; one tiled load brings z over the tile and its one-cell halo (the innermost
+// coordinate starts 8 cells early so that it stays 16-byte aligned; zero fill outside the level,
+// where the stencil reads nothing) and one brings r over the tile.  Each thread then updates the
+// cells of the colour in its run of 8 from shared memory, with the sums of stencil<3> in their
+// order, and stores the run (the other colour unchanged) -- bitwise the result of k_smooth8.
+// The one wait is bounded: on expiry the solve ends with code 4.
+constexpr int kTmaI = 4, kTmaJ = 8, kTmaMaxK = 64;
+
+template <typename S>
+__global__ void __launch_bounds__(256) k_smooth_tma(const __grid_constant__ CUtensorMap tz,
+                                                    const __grid_constant__ CUtensorMap tr, S* __restrict__ z, Lvl L,
+                                                    BC bc, int phase, SolveState* st, int TK) {
+  __shared__ __align__(128) S zb[(kTmaI + 2) * (kTmaJ + 2) * (kTmaMaxK + 16)];
+  __shared__ __align__(128) S rb[kTmaI * kTmaJ * kTmaMaxK];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ int s_skip;
+  if (threadIdx.x == 0) s_skip = st ? *(volatile int*)&st->done : 0;
+  __syncthreads();
+  if (s_skip) return;
+  const int tk = L.n2 / TK, tj = (L.n1 + kTmaJ - 1) / kTmaJ;
+  const int b = blockIdx.x;
+  const int bk = b % tk, bj = (b / tk) % tj, bi = b / (tk * tj);
+  const int i0 = bi * kTmaI, j0 = bj * kTmaJ, k0 = bk * TK;
+  const int W = TK + 16;  // brick row: 8 cells of halo room on each side
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    mbar_expect_tx(&bar, (uint32_t)(((kTmaI + 2) * (kTmaJ + 2) * W + kTmaI * kTmaJ * TK) * sizeof(S)));
+    tma_load_3d(zb, &tz, k0 - 8, j0 - 1, i0 - 1, &bar);
+    tma_load_3d(rb, &tr, k0, j0, i0, &bar);
+  }
+  bool ok = mbar_try_wait(&bar, 0);
+  if (!ok) {
+    const unsigned long long t0 = now_ns();
+    while (!(ok = mbar_try_wait(&bar, 0)) && now_ns() - t0 < kWaitNs) {
+    }
+    if (!ok && st) atomicCAS(&st->done, 0, 4);
+  }
+  if (__syncthreads_or(!ok)) return;  // the copies never arrived: nothing is written
+  const int R = TK >> 3;
+  const int t = threadIdx.x;
+  if (t >= kTmaI * kTmaJ * R) return;
+  const int ii = t / (kTmaJ * R), jj = (t / R) % kTmaJ, run = t % R;
+  const int i = i0 + ii, j = j0 + jj, k0r = k0 + 8 * run;
+  if (i >= L.n0 || j >= L.n1) return;
+  const S* row = zb + ((ii + 1) * (kTmaJ + 2) + (jj + 1)) * W + 8 + 8 * run;  // this run in the brick
+  const int pw = (kTmaJ + 2) * W;                                            // brick plane
+  float zc[8], rr[8], xp[8], xm[8], yp[8], ym[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    zc[q] = ldv(row + q);
+    xp[q] = ldv(row + pw + q);
+    xm[q] = ldv(row - pw + q);
+    yp[q] = ldv(row + W + q);
+    ym[q] = ldv(row - W + q);
+    rr[q] = ldv(rb + (ii * kTmaJ + jj) * TK + 8 * run + q);
+  }
+  const float zl = ldv(row - 1), zr = ldv(row + 8);
+  const bool hx = i < L.n0 - 1, lx = i > 0, hy = j < L.n1 - 1, ly = j > 0;
+  float base = 6.f;
+  if (i <= 0 && bc.lo[0] == 2) base -= 1.f;
+  if (i >= L.n0 - 1 && bc.hi[0] == 2) base -= 1.f;
+  if (j <= 0 && bc.lo[1] == 2) base -= 1.f;
+  if (j >= L.n1 - 1 && bc.hi[1] == 2) base -= 1.f;
+  const int first = (i + j + k0r + phase) & 1;
+  float out[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) out[q] = zc[q];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    if ((q & 1) != first) continue;
+    const int k = k0r + q;
+    float ret = 0.f;
+    if (hx) ret += xp[q];
+    if (lx) ret += xm[q];
+    if (hy) ret += yp[q];
+    if (ly) ret += ym[q];
+    if (k < L.n2 - 1) ret += (q < 7) ? zc[q + 1] : zr;
+    if (k > 0) ret += (q > 0) ? zc[q - 1] : zl;
+    float num = base;
+    if (k <= 0 && bc.lo[2] == 2) num -= 1.f;
+    if (k >= L.n2 - 1 && bc.hi[2] == 2) num -= 1.f;
+    out[q] = (rr[q] + ret) / num;
+  }
+  st8(z + ((int64_t)i * L.n1 + j) * L.n2 + k0r, out);
 }
 
 // restrict(l) as a gather: rc[I] = sum over children (fine-index order) of res/(dim-1),
@@ -753,6 +846,18 @@ static void smooth_launch(pfm_handle* h, int l, int phase, const SolveState* st,
   Lvl L = lvl_of(h, l);
   const int nl = (D == 3) ? L.n2 : L.n1;
   int64_t npairs = (D == 3) ? (int64_t)L.n0 * L.n1 * ((nl + 1) / 2) : (int64_t)L.n0 * ((nl + 1) / 2);
+  if (D == 3 && sizeof(S) == 2 && L.n2 % 8 == 0 && h->smooth_tma) {  // 16-bit levels: the TMA-staged tile
+    const int TK = L.n2 % 64 == 0 ? 64 : (L.n2 % 32 == 0 ? 32 : (L.n2 % 16 == 0 ? 16 : 8));
+    CUtensorMap tz, tr;
+    const bool bf = sizeof(S) == 2 && !std::is_same<S, __half>::value;
+    if (make_map_3d_16bit(&tz, level_z<S>(h, l), bf, L.n0, L.n1, L.n2, kTmaI + 2, kTmaJ + 2, TK + 16) &&
+        make_map_3d_16bit(&tr, level_r<S>(h, l), bf, L.n0, L.n1, L.n2, kTmaI, kTmaJ, TK)) {
+      const int64_t blocks = (int64_t)((L.n0 + kTmaI - 1) / kTmaI) * ((L.n1 + kTmaJ - 1) / kTmaJ) * (L.n2 / TK);
+      launch(h, k_smooth_tma<S>, (unsigned)blocks, 256, 0, s, tz, tr, level_z<S>(h, l), L, bc_of(h), phase,
+             const_cast<SolveState*>(st), TK);
+      return;
+    }
+  }
   if (D == 3 && L.n2 % 8 == 0) {
     const int64_t nvec = (int64_t)L.n0 * L.n1 * (L.n2 / 8);
     launch(h, k_smooth8<S>, grid_for(nvec, 256), 256, 0, s, level_z<S>(h, l), (const S*)level_r<S>(h, l), L,
@@ -1073,6 +1178,7 @@ static int solve_impl(pfm_handle* h, const pfm_solve_opts& o, pfm_solve_stats* s
     stats->rTr_true = K.true_res ? hs->rTr_true : -1.0;
   }
   if (hs->done == 3) return set_error(h, PFM_ERR_NONFINITE, "MGPCG: non-finite residual");
+  if (hs->done == 4) return set_error(h, PFM_ERR_CUDA, "MGPCG: a smoother's tile copy did not arrive");
   if (hs->done != 1) return set_error(h, PFM_ERR_NOT_CONVERGED, "MGPCG: iteration limit reached");
   return PFM_OK;
 }

@@ -36,6 +36,7 @@
 #include <mutex>
 
 #include "pfm_internal.cuh"
+#include "pfm_tma.cuh"
 
 namespace pfm {
 namespace nn {
@@ -48,75 +49,8 @@ constexpr int kChunkBytes = kBoxVox * 16;          // one 8-channel block of the
 constexpr int kRowBytes = kBoxD2 * 16;             // one brick row along d2: 160 B
 constexpr int kStages = 4;                         // weight ring depth
 constexpr int kMaxCin = 128, kMaxNpad = 128;
-constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
 constexpr int kSmPerGpuSmem = 233472;                  // shared memory per SM (228 KB)
 constexpr int kMaxDynSmem = 232448 - 64;               // per-CTA limit (227 KB) less the static flag
-
-__device__ __forceinline__ uint32_t su32(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
-
-__device__ __forceinline__ unsigned long long now_ns() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-
-// orders this thread's generic-proxy shared-memory accesses against later async-proxy ones
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(bar)), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}\n"
-      : "=r"(ok)
-      : "r"(su32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// Bounded wait for the phase of `bar` with the given parity.  Gives up (and raises *err) after
-// kWaitNs, or early once another CTA has raised *err.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int* err, int code) {
-  if (mbar_try_wait(bar, parity)) return true;
-  const unsigned long long t0 = now_ns();
-  for (unsigned it = 1;; ++it) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if ((it & 255u) == 0) {
-      if (*(volatile int*)err != 0) return false;
-      if (now_ns() - t0 > kWaitNs) {
-        atomicCAS(err, 0, code);
-        return false;
-      }
-    }
-  }
-}
-
-__device__ __forceinline__ void tma_load_5d(void* dst, const CUtensorMap* tm, int c0, int c1, int c2, int c3, int c4,
-                                            uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], "
-      "[%7];" ::"r"(su32(dst)),
-      "l"(reinterpret_cast<uint64_t>(tm)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(su32(bar))
-      : "memory");
-}
-
-__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   su32(dst)),
-               "l"(src), "r"(bytes), "r"(su32(bar))
-               : "memory");
-}
 
 __device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
   asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(slot)), "r"(ncols)
@@ -725,23 +659,6 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
 
 // ---------------------------------------------------------------------------------------------
 // host side
-
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn encode_fn() {
-  static EncodeTiledFn fn = nullptr;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    void* f = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = (EncodeTiledFn)f;
-  });
-  return fn;
-}
 
 // tensor map of a channel-blocked bf16 tensor: dims (8, n2, n1, n0, C/8), box (8, b2, b1, b0, C/8)
 bool make_map(CUtensorMap* tm, const void* base, int C, int n0, int n1, int n2, int b0, int b1, int b2) {

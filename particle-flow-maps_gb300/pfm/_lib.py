@@ -174,6 +174,7 @@ SIGNATURES = {
 # tuning keys (include/pfm.h)
 TUNE_P2G2_COLUMN = 1
 TUNE_MG_TAIL_CELLS = 2
+TUNE_SMOOTH_TMA = 3
 # scratch limits of pfm_sort_particles_noalloc (include/pfm.h)
 NOALLOC_MAX_PARTICLES = 1 << 21
 NOALLOC_MAX_CELLS = 1 << 18

@@ -7,7 +7,9 @@ simulation; it is done once per scene size, before the step or batch graphs are 
     in one thread block (fewer launches, one SM) instead of grid-wide kernels; timed on a solve of
     the scene's current divergence (into a scratch pressure);
   * ``p2g2_column`` (2D): faces per thread of the P2G column gather; timed on the scene's P2G into
-    its scratch grids.
+    its scratch grids;
+  * ``smooth_tma`` (3D, 16-bit MGPCG levels): smoothing from tiles the TMA stages in shared memory
+    (1) or from global memory (0); timed on the same solve.
 """
 import statistics
 
@@ -52,6 +54,14 @@ def autotune(sim, reps=3, tails=TAILS, columns=COLUMNS):
     best = min(times, key=times.get)
     sc.set_tuning(_lib.TUNE_MG_TAIL_CELLS, best)
     out["mg_tail_cells"] = (best, times)
+    if sc.dim == 3 and opts.get("precision", 0) in (1, 2):
+        times = {}
+        for v in (0, 1):
+            sc.set_tuning(_lib.TUNE_SMOOTH_TMA, v)
+            times[v] = _time(lambda: sc.mgpcg_solve(r, x, **opts), reps)
+        best = min(times, key=times.get)
+        sc.set_tuning(_lib.TUNE_SMOOTH_TMA, best)
+        out["smooth_tma"] = (best, times)
     if sc.dim == 2:
         times = {}
         for k in columns:
@@ -66,6 +76,7 @@ def autotune(sim, reps=3, tails=TAILS, columns=COLUMNS):
 
 def apply(sim, tuned):
     """Sets the values an autotune() of a scene of the same size chose."""
-    keys = {"mg_tail_cells": _lib.TUNE_MG_TAIL_CELLS, "p2g2_column": _lib.TUNE_P2G2_COLUMN}
+    keys = {"mg_tail_cells": _lib.TUNE_MG_TAIL_CELLS, "p2g2_column": _lib.TUNE_P2G2_COLUMN,
+            "smooth_tma": _lib.TUNE_SMOOTH_TMA}
     for name, (value, _) in tuned.items():
         sim.scene.set_tuning(keys[name], value)

@@ -110,3 +110,23 @@ def test_bad_precision_is_rejected():
     sc = pfm.Scene(3, (16, 16, 16), 1 / 16, 0)
     with pytest.raises(pfm.PfmError, match="precision"):
         sc.poisson(sc.alloc_faces(), torch.zeros(16, 16, 16, device="cuda"), precision=5)
+
+
+@pytest.mark.parametrize("prec", [1, 2])
+@pytest.mark.parametrize("res", [(64, 64, 64), (40, 24, 48)])
+def test_tma_smoother_is_bitwise_the_global_one(prec, res):
+    """The 16-bit levels smoothed from TMA-staged tiles (PFM_TUNE_SMOOTH_TMA = 1) and from global
+    memory (0) give bitwise the same solve: pressure, iterations and residual."""
+    from pfm import _lib
+    rng = np.random.default_rng(21)
+    dx = 1.0 / res[1]
+    sc = pfm.Scene(3, res, dx, 0)
+    r = torch.as_tensor(rng.standard_normal(res).astype(np.float32)).cuda()
+    out = []
+    for tma in (0, 1):
+        sc.set_tuning(_lib.TUNE_SMOOTH_TMA, tma)
+        x = torch.zeros_like(r)
+        info = sc.mgpcg_solve(r, x, k=-1.0, tol=1e-6, tol_mode=1, max_iters=200, precision=prec)
+        torch.cuda.synchronize()
+        out.append((x, info.iterations, info.rTr))
+    assert torch.equal(out[0][0], out[1][0]) and out[0][1:] == out[1][1:]
