@@ -264,6 +264,7 @@ struct ConvWgradParams {
   int n0, n1, n2, tiles2, ntiles;  // voxel tiles of 1 x 16 x 8
   int cin, c1, cdy, npad;          // input channels, dY channels (multiple of 8), MMA N
   int mtiles, mt_per_cta;          // M tiles of 128 (tap, ci) rows; per CTA group (blockIdx.y)
+  int nabuf;                       // operand buffers for A (2: staging overlaps the MMAs; 1: more CTAs per SM)
   int ncols;
   uint32_t idesc;
   float* partial;  // [gridDim.x][mtiles * 128][npad]
@@ -295,7 +296,9 @@ __device__ __forceinline__ void copy_core_T(const unsigned char* src, unsigned c
 constexpr int kCoresA = 16 * 16;           // 16 row groups x 16 voxel groups per M tile
 constexpr int kAbufBytes = kCoresA * 128;  // 32 KB
 
-__global__ void __launch_bounds__(kThreads) k_conv3_wgrad(const __grid_constant__ CUtensorMap tm1,
+constexpr int kWgThreads = 256;  // 8 warps stage the operand cores; warps 0-3 also drain TMEM
+
+__global__ void __launch_bounds__(kWgThreads) k_conv3_wgrad(const __grid_constant__ CUtensorMap tm1,
                                                           const __grid_constant__ CUtensorMap tm2,
                                                           const __grid_constant__ CUtensorMap tmdy,
                                                           const ConvWgradParams p) {
@@ -313,8 +316,8 @@ __global__ void __launch_bounds__(kThreads) k_conv3_wgrad(const __grid_constant_
   unsigned char* box = smem;
   unsigned char* dybox = box + ((box_bytes + 127) & ~127u);
   unsigned char* bcore = dybox + dy_bytes;           // [16 voxel groups][npad/8][128 B]
-  unsigned char* abuf = bcore + (size_t)p.npad * 256;  // 2 x [16 voxel groups][16 row groups][128 B]
-  uint64_t* bars = (uint64_t*)(abuf + 2 * kAbufBytes);
+  unsigned char* abuf = bcore + (size_t)p.npad * 256;  // nabuf x [16 voxel groups][16 row groups][128 B]
+  uint64_t* bars = (uint64_t*)(abuf + p.nabuf * kAbufBytes);
   uint64_t* box_bar = bars;
   uint64_t* done = bars + 1;  // [2], one per A buffer
   uint64_t* final_bar = bars + 3;
@@ -331,7 +334,7 @@ __global__ void __launch_bounds__(kThreads) k_conv3_wgrad(const __grid_constant_
     fence_mbar_init();
   }
   // B groups beyond the dY channels stay zero
-  for (int i = tid; i < p.npad * 16; i += kThreads) ((uint4*)bcore)[i] = make_uint4(0, 0, 0, 0);
+  for (int i = tid; i < p.npad * 16; i += blockDim.x) ((uint4*)bcore)[i] = make_uint4(0, 0, 0, 0);
   if (warp == 0) tmem_alloc(slot, (uint32_t)p.ncols);
   fence_proxy_async();
   tc_fence_before();
@@ -364,18 +367,18 @@ __global__ void __launch_bounds__(kThreads) k_conv3_wgrad(const __grid_constant_
     if (w && last >= 0) w = mbar_wait(done + last, (uses[last] - 1) & 1, p.err, 12);
     ok = __syncthreads_and(w) != 0;  // every thread takes the same path through the barriers below
     if (!ok) break;
-    for (int i = tid; i < dchunk * 16; i += kThreads) {  // B core (channel group g, voxel group k)
+    for (int i = tid; i < dchunk * 16; i += blockDim.x) {  // B core (channel group g, voxel group k)
       const int g = i % dchunk, k = i / dchunk;
       copy_core_T(dybox + g * 2048 + k * 128, bcore + k * blbo + g * 128);
     }
     for (int mi = 0; mi < nmt && ok; ++mi) {
-      const int buf = (uses[0] + uses[1]) & 1;
+      const int buf = p.nabuf == 2 ? ((uses[0] + uses[1]) & 1) : 0;
       bool wb = true;
       if (uses[buf] > 0) wb = mbar_wait(done + buf, (uses[buf] - 1) & 1, p.err, 13);
       ok = __syncthreads_and(wb) != 0;
       if (!ok) break;
       unsigned char* A = abuf + buf * kAbufBytes;
-      for (int i = tid; i < kCoresA; i += kThreads) {  // A core (row group g, voxel group k)
+      for (int i = tid; i < kCoresA; i += blockDim.x) {  // A core (row group g, voxel group k)
         const int g = i & 15, k = i >> 4;
         const int G = (mt0 + mi) * 16 + g;
         const int tap = G / nchunk, ch = G - tap * nchunk;
@@ -412,7 +415,7 @@ __global__ void __launch_bounds__(kThreads) k_conv3_wgrad(const __grid_constant_
   tc_fence_after();
 
   const int rows = p.mtiles * 128;
-  for (int mi = 0; mi < nmt; ++mi) {
+  for (int mi = 0; mi < nmt && warp < 4; ++mi) {  // TMEM lanes 32w..32w+31 belong to warp w % 4
     for (int c0 = 0; c0 < p.npad; c0 += 16) {
       float v[16];
       tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(mi * p.npad + c0), v);
@@ -808,13 +811,16 @@ extern "C" int pfm_nn_conv3_wgrad(const pfm_conv3_wgrad_args* a, void* stream) {
   pfm_nn_wgrad_workspace(a, &ws);
   if (a->partial_bytes < ws) return PFM_ERR_WORKSPACE;
   const size_t box = ((size_t)(cin / 8) * kChunkBytes + 127) & ~(size_t)127;
-  const size_t need = 1024 + box + (size_t)(a->cdy / 8) * 2048 + (size_t)npad * 256 + 2 * kAbufBytes + 8 * 4 + 16;
+  const size_t base = 1024 + box + (size_t)(a->cdy / 8) * 2048 + (size_t)npad * 256 + 8 * 4 + 16;
+  // one A buffer when that lets two CTAs share an SM (their stagings then overlap each other)
+  p.nabuf = (2 * (base + 2 * kAbufBytes + 1024) > (size_t)kSmPerGpuSmem && 2 * (base + kAbufBytes + 1024) <= (size_t)kSmPerGpuSmem) ? 1 : 2;
+  const size_t need = base + (size_t)p.nabuf * kAbufBytes;
   const size_t smem = occupancy_smem(need, p.ncols);
   if (smem > kMaxDynSmem) return PFM_ERR_SHAPE;
   static std::once_flag attr;
   std::call_once(attr, [] { cudaFuncSetAttribute(k_conv3_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem); });
   cudaStream_t st = (cudaStream_t)stream;
-  k_conv3_wgrad<<<dim3((unsigned)gx, (unsigned)gy), kThreads, smem, st>>>(tm1, tm2, tmdy, p);
+  k_conv3_wgrad<<<dim3((unsigned)gx, (unsigned)gy), kWgThreads, smem, st>>>(tm1, tm2, tmdy, p);
   const int total = a->cout * cin * 27;
   k_wgrad_reduce<<<(total + 255) / 256, 256, 0, st>>>(a->partial, gx, p.mtiles * 128, npad, cin, a->cout, a->dw);
   return cudaGetLastError() == cudaSuccess ? PFM_OK : PFM_ERR_CUDA;
