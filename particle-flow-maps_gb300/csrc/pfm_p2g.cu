@@ -13,6 +13,8 @@
 //     Particles outside the grid keep a clamped key, which stays inside every neighbourhood they
 //     can reach, and their weights come from their real positions, exactly as the reference's
 //     bounds-checked scatter.
+#include <mutex>
+
 #include "pfm_internal.cuh"
 
 namespace pfm {
@@ -183,12 +185,14 @@ __global__ void __launch_bounds__(kBinThreads) k_payload2(const int* __restrict_
 // Tiled P2G (3D).  Cells are grouped in kTX x kTY x kTZ tiles, one thread per cell.  For each
 // face family the thread sums its cell's particles (particle-index order) into a register window
 // of the 4 x 3 x 3 faces they can reach (4 along the family's own axis: faces c-1 .. c+2; 3 along
-// the others: c-1 .. c+1), the tile adds the windows into a shared copy of the faces around it in
-// 36 passes (one window offset per pass, a barrier between passes), and then adds that region into
+// the others: c-1 .. c+1), every thread stores its window in shared memory (36 slots x 512 cells,
+// 147 KB: the kernel runs one block per SM anyway), and after one barrier each face of the region
+// around the tile sums the slots of the cells that reach it, in slot order, and adds the sum into
 // the face grids.  Tiles run in 8 launches by the parity of their tile coordinates: tiles of one
 // parity are a tile apart and their face regions (one face below, two above) never overlap, so no
 // atomics are needed.  Each face sums in a fixed order (launch, pass, particle index): the result
-// is bitwise reproducible.  Particles outside the grid sit in the clamped edge cell, whose window
+// is bitwise reproducible (the same sums, in the same order, as merging the windows into a shared
+// copy of the region in 36 passes with a barrier between passes).  Particles outside the grid sit in the clamped edge cell, whose window
 // still holds every in-grid face they reach; their weights come from their real positions.
 constexpr int kTX = 8, kTY = 8, kTZ = 8;
 constexpr int kTileThreads = kTX * kTY * kTZ;
@@ -196,6 +200,8 @@ constexpr int kExt0 = (kTX + 3) * (kTY + 2) * (kTZ + 2);  // face region of fami
 constexpr int kExt1 = (kTX + 2) * (kTY + 3) * (kTZ + 2);  // family y
 constexpr int kExt2 = (kTX + 2) * (kTY + 2) * (kTZ + 3);  // family z
 constexpr int kTileExtMax = kExt0 > kExt1 ? (kExt0 > kExt2 ? kExt0 : kExt2) : (kExt1 > kExt2 ? kExt1 : kExt2);
+constexpr int kWinSlots = 4 * 3 * 3;                                              // window faces per cell
+constexpr size_t kTileSmem = (size_t)kWinSlots * kTileThreads * sizeof(float2);  // 147,456 B
 
 struct FaceOut3 {
   float* u[3];
@@ -239,15 +245,14 @@ __device__ __forceinline__ void tile_axis(float p, int c, float dx, float* w, fl
 }
 
 template <int FAM>
-__device__ __forceinline__ void tile_family(float2* __restrict__ acc, const float4* __restrict__ pos4,
+__device__ __forceinline__ void tile_family(float2* __restrict__ win, const float4* __restrict__ pos4,
                                             const float4* __restrict__ rec, const int* __restrict__ order, int sb,
-                                            int se, int ci, int cj, int ck,
-                                            int lx, int ly, int lz, int x0, int y0, int z0, const MacGeom& g,
-                                            int use_apic, float* __restrict__ u, float* __restrict__ w) {
+                                            int se, int ci, int cj, int ck, int x0, int y0, int z0,
+                                            const MacGeom& g, int use_apic, float* __restrict__ u,
+                                            float* __restrict__ w) {
   constexpr int W0 = FAM == 0 ? 4 : 3, W1 = FAM == 1 ? 4 : 3, W2 = FAM == 2 ? 4 : 3;
   constexpr int E0 = kTX + W0 - 1, E1 = kTY + W1 - 1, E2 = kTZ + W2 - 1, NE = E0 * E1 * E2;
-  static_assert(NE <= kTileExtMax, "tile face region exceeds the shared buffer");
-  for (int e = threadIdx.x; e < NE; e += kTileThreads) acc[e] = make_float2(0.f, 0.f);
+  static_assert(W0 * W1 * W2 <= kWinSlots, "window exceeds the shared buffer");
   float num[W0][W1][W2], den[W0][W1][W2];
 #pragma unroll
   for (int a = 0; a < W0; ++a)
@@ -256,8 +261,12 @@ __device__ __forceinline__ void tile_family(float2* __restrict__ acc, const floa
 #pragma unroll
       for (int k = 0; k < W2; ++k) num[a][b][k] = den[a][b][k] = 0.f;
   const float dx = g.dx;
+  // the next slot's particle index is read one iteration ahead, so each particle costs one
+  // memory round trip (its records) instead of two (index, then records)
+  int qn = sb < se ? __ldg(order + sb) : 0;
   for (int s = sb; s < se; ++s) {
-    const int q = __ldg(order + s);  // sorted slot -> particle
+    const int q = qn;  // sorted slot -> particle
+    if (s + 1 < se) qn = __ldg(order + s + 1);
     const float4 p = __ldg(pos4 + q);
     const float4 fr = __ldg(rec + q);
     float w0[W0], d0[W0], w1[W1], d1[W1], w2[W2], d2[W2];
@@ -279,33 +288,47 @@ __device__ __forceinline__ void tile_family(float2* __restrict__ acc, const floa
         }
       }
   }
-  __syncthreads();
 #pragma unroll
   for (int a = 0; a < W0; ++a)
 #pragma unroll
     for (int b = 0; b < W1; ++b)
 #pragma unroll
-      for (int k = 0; k < W2; ++k) {
-        float2* cell = acc + ((lx + a) * E1 + (ly + b)) * E2 + (lz + k);
-        float2 v = *cell;
-        v.x += num[a][b][k];
-        v.y += den[a][b][k];
-        *cell = v;
-        __syncthreads();
-      }
+      for (int k = 0; k < W2; ++k)
+        win[((a * W1 + b) * W2 + k) * kTileThreads + threadIdx.x] = make_float2(num[a][b][k], den[a][b][k]);
+  __syncthreads();
+  // Face e of the tile's region (origin one face below the tile) takes window slot (a, b, k) of
+  // the cell e - (a, b, k), summed from zero in slot order (a, then b, then k)
   const int n0 = g.n[FAM][0], n1 = g.n[FAM][1], n2 = g.n[FAM][2];
   constexpr int NPT = (NE + kTileThreads - 1) / kTileThreads;
   int64_t qs[NPT];
   float2 vs[NPT];
 #pragma unroll
-  for (int j = 0; j < NPT; ++j) {  // all reads first: one memory latency for the whole add-back
+  for (int j = 0; j < NPT; ++j) {
     const int e = threadIdx.x + j * kTileThreads;
     const int ez = e % E2, r = e / E2, ey = r % E1, ex = r / E1;
     const int gi = x0 - 1 + ex, gj = y0 - 1 + ey, gk = z0 - 1 + ez;
     qs[j] = -1;
     if (e < NE && gi >= 0 && gi < n0 && gj >= 0 && gj < n1 && gk >= 0 && gk < n2) {
       qs[j] = ((int64_t)gi * n1 + gj) * n2 + gk;
-      const float2 v = acc[e];
+      float2 v = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int a = 0; a < W0; ++a) {
+        const int sx = ex - a;
+        if (sx < 0 || sx >= kTX) continue;
+#pragma unroll
+        for (int b = 0; b < W1; ++b) {
+          const int sy = ey - b;
+          if (sy < 0 || sy >= kTY) continue;
+#pragma unroll
+          for (int k = 0; k < W2; ++k) {
+            const int sz = ez - k;
+            if (sz < 0 || sz >= kTZ) continue;
+            const float2 f = win[((a * W1 + b) * W2 + k) * kTileThreads + (sx * kTY + sy) * kTZ + sz];
+            v.x += f.x;
+            v.y += f.y;
+          }
+        }
+      }
       vs[j] = make_float2(v.x + u[qs[j]], v.y + w[qs[j]]);
     }
   }
@@ -325,7 +348,7 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_tile3(const float4* __restr
                                                            const int* __restrict__ order,
                                                            const int* __restrict__ start, MacGeom g, int use_apic,
                                                            int64_t P, int px, int py, int pz, FaceOut3 out) {
-  __shared__ float2 acc[kTileExtMax];
+  extern __shared__ float2 win[];  // kWinSlots x kTileThreads window values (num, den)
   const int x0 = (2 * (int)blockIdx.z + px) * kTX, y0 = (2 * (int)blockIdx.y + py) * kTY;
   const int z0 = (2 * (int)blockIdx.x + pz) * kTZ;
   const int lz = threadIdx.x % kTZ, ly = (threadIdx.x / kTZ) % kTY, lx = threadIdx.x / (kTZ * kTY);
@@ -336,11 +359,9 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_tile3(const float4* __restr
     sb = __ldg(start + c);
     se = __ldg(start + c + 1);
   }
-  tile_family<0>(acc, pos4, famrec, order, sb, se, ci, cj, ck, lx, ly, lz, x0, y0, z0, g, use_apic, out.u[0], out.w[0]);
-  tile_family<1>(acc, pos4, famrec + P, order, sb, se, ci, cj, ck, lx, ly, lz, x0, y0, z0, g, use_apic, out.u[1],
-                 out.w[1]);
-  tile_family<2>(acc, pos4, famrec + 2 * P, order, sb, se, ci, cj, ck, lx, ly, lz, x0, y0, z0, g, use_apic, out.u[2],
-                 out.w[2]);
+  tile_family<0>(win, pos4, famrec, order, sb, se, ci, cj, ck, x0, y0, z0, g, use_apic, out.u[0], out.w[0]);
+  tile_family<1>(win, pos4, famrec + P, order, sb, se, ci, cj, ck, x0, y0, z0, g, use_apic, out.u[1], out.w[1]);
+  tile_family<2>(win, pos4, famrec + 2 * P, order, sb, se, ci, cj, ck, x0, y0, z0, g, use_apic, out.u[2], out.w[2]);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -417,8 +438,10 @@ __device__ __forceinline__ void tile_smoke_channel(float2* __restrict__ acc, con
 #pragma unroll
       for (int k = 0; k < 3; ++k) num[a][b][k] = den[a][b][k] = 0.f;
   const float dx = g.dx;
+  int qn = sb < se ? __ldg(order + sb) : 0;  // next slot's particle read one iteration ahead
   for (int s = sb; s < se; ++s) {
-    const int q = __ldg(order + s);
+    const int q = qn;
+    if (s + 1 < se) qn = __ldg(order + s + 1);
     const float4 p = __ldg(pos4 + q);
     const float4 fr = __ldg(rec + q);
     float w0[3], d0[3], w1[3], d1[3], w2[3], d2[3];
@@ -715,13 +738,20 @@ int p2g3_from_records(pfm_handle* h, float* const* us, float* const* ws, cudaStr
     if (rc) return rc;
   }
   if (h->P > 0) {
+    static std::once_flag attr;  // above the default 48 KB of dynamic shared memory: opt in once
+    static cudaError_t attr_rc = cudaSuccess;
+    std::call_once(attr, [] {
+      attr_rc = cudaFuncSetAttribute(k_tile3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem);
+    });
+    rc = check_cuda(h, attr_rc, "k_tile3 shared-memory attribute");
+    if (rc) return rc;
     const int nt[3] = {(h->geom.N[0] + kTX - 1) / kTX, (h->geom.N[1] + kTY - 1) / kTY, (h->geom.N[2] + kTZ - 1) / kTZ};
     for (int px = 0; px < 2; ++px)
       for (int py = 0; py < 2; ++py)
         for (int pz = 0; pz < 2; ++pz) {
           const unsigned bx = (nt[0] - px + 1) / 2, by = (nt[1] - py + 1) / 2, bz = (nt[2] - pz + 1) / 2;
           if (!bx || !by || !bz) continue;
-          launch(h, k_tile3, dim3(bz, by, bx), kTileThreads, 0, st, pos4, famrec, order, start, h->geom,
+          launch(h, k_tile3, dim3(bz, by, bx), kTileThreads, kTileSmem, st, pos4, famrec, order, start, h->geom,
                  h->cfg.use_apic, h->P, px, py, pz, out);
         }
     launch(h, k_normalize3, grid_for(F[0] + F[1] + F[2], kBinThreads), kBinThreads, 0, st, out, F[0], F[1], F[2]);
