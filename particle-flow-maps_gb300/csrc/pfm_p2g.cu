@@ -196,10 +196,6 @@ __global__ void __launch_bounds__(kBinThreads) k_payload2(const int* __restrict_
 // still holds every in-grid face they reach; their weights come from their real positions.
 constexpr int kTX = 8, kTY = 8, kTZ = 8;
 constexpr int kTileThreads = kTX * kTY * kTZ;
-constexpr int kExt0 = (kTX + 3) * (kTY + 2) * (kTZ + 2);  // face region of family x
-constexpr int kExt1 = (kTX + 2) * (kTY + 3) * (kTZ + 2);  // family y
-constexpr int kExt2 = (kTX + 2) * (kTY + 2) * (kTZ + 3);  // family z
-constexpr int kTileExtMax = kExt0 > kExt1 ? (kExt0 > kExt2 ? kExt0 : kExt2) : (kExt1 > kExt2 ? kExt1 : kExt2);
 constexpr int kWinSlots = 4 * 3 * 3;                                              // window faces per cell
 constexpr size_t kTileSmem = (size_t)kWinSlots * kTileThreads * sizeof(float2);  // 147,456 B
 
@@ -418,18 +414,20 @@ __global__ void __launch_bounds__(kBinThreads) k_payload_smoke3(int64_t P, MacGe
   }
 }
 
-constexpr int kExtCell = (kTX + 2) * (kTY + 2) * (kTZ + 2);  // cell region of a tile (halo 1)
-static_assert(kExtCell <= kTileExtMax, "smoke tile region exceeds the shared buffer");
 
-// One channel of one tile: window sums of (s + delta) w and w over the 3 x 3 x 3 cells, merged
-// through shared memory in 27 passes, added into smoke[.][ch] (and the weight grid for ch 0).
-__device__ __forceinline__ void tile_smoke_channel(float2* __restrict__ acc, const float4* __restrict__ pos4,
+// One channel of one tile: window sums of (s + delta) w (and, with DEN, of w) over the 3 x 3 x 3
+// cells; every thread stores its window in shared memory (27 slots x 512 cells) and after one
+// barrier each cell of the tile's region sums the slots that reach it, from zero in slot order --
+// the sums, in the order, of merging the windows in 27 barrier-separated passes -- and adds the
+// sum into smoke[.][ch] (and the weight grid for ch 0).  The weights do not depend on the channel,
+// so only channel 0 sums them.
+template <bool DEN>
+__device__ __forceinline__ void tile_smoke_channel(float2* __restrict__ win, const float4* __restrict__ pos4,
                                                    const float4* __restrict__ rec, const int* __restrict__ order,
-                                                   int sb, int se, int ci, int cj, int ck, int lx, int ly, int lz,
-                                                   int x0, int y0, int z0, const MacGeom& g, int use_apic, int ch,
+                                                   int sb, int se, int ci, int cj, int ck, int x0, int y0, int z0,
+                                                   const MacGeom& g, int use_apic, int ch,
                                                    float* __restrict__ smoke, float* __restrict__ wsum) {
   constexpr int E0 = kTX + 2, E1 = kTY + 2, E2 = kTZ + 2, NE = E0 * E1 * E2;
-  for (int e = threadIdx.x; e < NE; e += kTileThreads) acc[e] = make_float2(0.f, 0.f);
   float num[3][3][3], den[3][3][3];
 #pragma unroll
   for (int a = 0; a < 3; ++a)
@@ -459,24 +457,18 @@ __device__ __forceinline__ void tile_smoke_channel(float2* __restrict__ acc, con
           const float wt = w01 * w2[k];
           const float delta = d01 + fr.w * d2[k];
           num[a][b][k] += (use_apic ? (fr.x + delta) : fr.x) * wt;
-          den[a][b][k] += wt;
+          if (DEN) den[a][b][k] += wt;
         }
       }
   }
-  __syncthreads();
 #pragma unroll
   for (int a = 0; a < 3; ++a)
 #pragma unroll
     for (int b = 0; b < 3; ++b)
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        float2* cell = acc + ((lx + a) * E1 + (ly + b)) * E2 + (lz + k);
-        float2 v = *cell;
-        v.x += num[a][b][k];
-        v.y += den[a][b][k];
-        *cell = v;
-        __syncthreads();
-      }
+      for (int k = 0; k < 3; ++k)
+        win[((a * 3 + b) * 3 + k) * kTileThreads + threadIdx.x] = make_float2(num[a][b][k], den[a][b][k]);
+  __syncthreads();
   const int n0 = g.N[0], n1 = g.N[1], n2 = g.N[2];
   constexpr int NPT = (NE + kTileThreads - 1) / kTileThreads;
   int64_t qs[NPT];
@@ -489,19 +481,39 @@ __device__ __forceinline__ void tile_smoke_channel(float2* __restrict__ acc, con
     qs[j] = -1;
     if (e < NE && gi >= 0 && gi < n0 && gj >= 0 && gj < n1 && gk >= 0 && gk < n2) {
       qs[j] = ((int64_t)gi * n1 + gj) * n2 + gk;
-      const float2 v = acc[e];
-      vs[j] = make_float2(v.x + smoke[qs[j] * 4 + ch], ch == 0 ? v.y + wsum[qs[j]] : 0.f);
+      float2 v = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const int sx = ex - a;
+        if (sx < 0 || sx >= kTX) continue;
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+          const int sy = ey - b;
+          if (sy < 0 || sy >= kTY) continue;
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            const int sz = ez - k;
+            if (sz < 0 || sz >= kTZ) continue;
+            const float2 f = win[((a * 3 + b) * 3 + k) * kTileThreads + (sx * kTY + sy) * kTZ + sz];
+            v.x += f.x;
+            if (DEN) v.y += f.y;
+          }
+        }
+      }
+      vs[j] = make_float2(v.x + smoke[qs[j] * 4 + ch], DEN ? v.y + wsum[qs[j]] : 0.f);
     }
   }
 #pragma unroll
   for (int j = 0; j < NPT; ++j) {
     if (qs[j] >= 0) {
       smoke[qs[j] * 4 + ch] = vs[j].x;
-      if (ch == 0) wsum[qs[j]] = vs[j].y;
+      if (DEN) wsum[qs[j]] = vs[j].y;
     }
   }
   __syncthreads();
 }
+
+constexpr size_t kSmokeTileSmem = (size_t)27 * kTileThreads * sizeof(float2);  // 110,592 B
 
 __global__ void __launch_bounds__(kTileThreads, 1) k_tile_smoke3(const float4* __restrict__ pos4,
                                                                  const float4* __restrict__ chrec,
@@ -509,7 +521,7 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_tile_smoke3(const float4* _
                                                                  const int* __restrict__ start, MacGeom g, int use_apic,
                                                                  int64_t P, int px, int py, int pz,
                                                                  float* __restrict__ smoke, float* __restrict__ wsum) {
-  __shared__ float2 acc[kExtCell];
+  extern __shared__ float2 win[];  // 27 x kTileThreads window values (num, den)
   const int x0 = (2 * (int)blockIdx.z + px) * kTX, y0 = (2 * (int)blockIdx.y + py) * kTY;
   const int z0 = (2 * (int)blockIdx.x + pz) * kTZ;
   const int lz = threadIdx.x % kTZ, ly = (threadIdx.x / kTZ) % kTY, lx = threadIdx.x / (kTZ * kTY);
@@ -520,10 +532,11 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_tile_smoke3(const float4* _
     sb = __ldg(start + c);
     se = __ldg(start + c + 1);
   }
+  tile_smoke_channel<true>(win, pos4, chrec, order, sb, se, ci, cj, ck, x0, y0, z0, g, use_apic, 0, smoke, wsum);
 #pragma unroll 1
-  for (int ch = 0; ch < 4; ++ch)
-    tile_smoke_channel(acc, pos4, chrec + ch * P, order, sb, se, ci, cj, ck, lx, ly, lz, x0, y0, z0, g, use_apic, ch,
-                       smoke, wsum);
+  for (int ch = 1; ch < 4; ++ch)
+    tile_smoke_channel<false>(win, pos4, chrec + ch * P, order, sb, se, ci, cj, ck, x0, y0, z0, g, use_apic, ch,
+                              smoke, wsum);
 }
 
 // smoke /= w and clamp every channel to [0, 1] where w > 0 (3D/run_3D.py:584-591)
@@ -901,14 +914,22 @@ int pfm3_p2g_smoke(pfm_handle* h, const float* smoke_p, const float* init_grad_s
   if (h->P > 0) {
     const int* start = ws_ptr<int>(h, h->o_start);
     const int* order = ws_ptr<int>(h, h->o_order);
+    static std::once_flag attr;  // above the default 48 KB of dynamic shared memory: opt in once
+    static cudaError_t attr_rc = cudaSuccess;
+    std::call_once(attr, [] {
+      attr_rc = cudaFuncSetAttribute(k_tile_smoke3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmokeTileSmem);
+    });
+    rc = check_cuda(h, attr_rc, "k_tile_smoke3 shared-memory attribute");
+    if (rc) return rc;
     const int nt[3] = {(h->geom.N[0] + kTX - 1) / kTX, (h->geom.N[1] + kTY - 1) / kTY, (h->geom.N[2] + kTZ - 1) / kTZ};
     for (int px = 0; px < 2; ++px)
       for (int py = 0; py < 2; ++py)
         for (int pz = 0; pz < 2; ++pz) {
           const unsigned bx = (nt[0] - px + 1) / 2, by = (nt[1] - py + 1) / 2, bz = (nt[2] - pz + 1) / 2;
           if (!bx || !by || !bz) continue;
-          launch(h, k_tile_smoke3, dim3(bz, by, bx), kTileThreads, 0, st, (const float4*)pos4, (const float4*)chrec,
-                 order, start, h->geom, use_apic_smoke ? 1 : 0, h->P, px, py, pz, smoke, weight);
+          launch(h, k_tile_smoke3, dim3(bz, by, bx), kTileThreads, kSmokeTileSmem, st, (const float4*)pos4,
+                 (const float4*)chrec, order, start, h->geom, use_apic_smoke ? 1 : 0, h->P, px, py, pz, smoke,
+                 weight);
         }
     launch(h, k_normalize_smoke3, grid_for(h->cells, kBinThreads), kBinThreads, 0, st,
            reinterpret_cast<float4*>(smoke), (const float*)weight, h->cells);
