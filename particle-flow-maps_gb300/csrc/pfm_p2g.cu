@@ -13,6 +13,7 @@
 //     Particles outside the grid keep a clamped key, which stays inside every neighbourhood they
 //     can reach, and their weights come from their real positions, exactly as the reference's
 //     bounds-checked scatter.
+#include <climits>
 #include <mutex>
 
 #include "pfm_internal.cuh"
@@ -137,13 +138,49 @@ __global__ void __launch_bounds__(kBinThreads) k_scatter_order(const int* __rest
   order[start[key[q]] + slot[q]] = (int)q;
 }
 
+// Bins of at most N entries: all loads issued together into registers (INT_MAX past the end), a
+// bitonic sorting network, and the first n values stored back.  The entries are distinct particle
+// indices, so the result is the ascending order whatever the network.
+template <int N>
+__device__ __forceinline__ void sort_bin_small(int* __restrict__ order, int b, int n) {
+  int v[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) v[i] = i < n ? order[b + i] : INT_MAX;
+#pragma unroll
+  for (int k = 2; k <= N; k <<= 1)
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1)
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        const int l = i ^ j;
+        if (l > i) {
+          const int lo = min(v[i], v[l]), hi = max(v[i], v[l]);
+          const bool up = (i & k) == 0;
+          v[i] = up ? lo : hi;
+          v[l] = up ? hi : lo;
+        }
+      }
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+    if (i < n) order[b + i] = v[i];
+}
+
 // each bin in ascending particle index: the stable order of a CPU counting sort
 __global__ void __launch_bounds__(kBinThreads) k_cell_sort(const int* __restrict__ start, int64_t C,
                                                            int* __restrict__ order) {
   int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= C) return;
   const int b = start[c], e = start[c + 1];
-  for (int i = b + 1; i < e; ++i) {
+  if (e - b <= 1) return;
+  if (e - b <= 8) {
+    sort_bin_small<8>(order, b, e - b);
+    return;
+  }
+  if (e - b <= 16) {
+    sort_bin_small<16>(order, b, e - b);
+    return;
+  }
+  for (int i = b + 1; i < e; ++i) {  // larger bins: insertion sort in place
     int v = order[i];
     int j = i - 1;
     while (j >= b && order[j] > v) {
