@@ -732,6 +732,66 @@ __device__ void tail_smooth(float* z, const float* r, const Lvl& L, const BC& bc
   __syncthreads();
 }
 
+// `iters` red-black sweeps (colour `first`, then the other) of one tail level.  When the level has
+// at most kTailCpt cells per thread, each thread decodes its cells once and keeps their offsets,
+// colours, neighbour masks, neighbour counts and r in registers for all the sweeps; every update
+// sums the neighbours in stencil<D>'s order and divides as tail_smooth does (the same results).
+constexpr int kTailCpt = 4;
+
+template <int D>
+__device__ void tail_sweeps(float* z, const float* r, const Lvl& L, const BC& bc, int iters, int first) {
+  if ((int)L.count > kTailCpt * (int)blockDim.x) {  // block-uniform
+    for (int it = 0; it < iters; ++it) {
+      tail_smooth<D>(z, r, L, bc, first);
+      tail_smooth<D>(z, r, L, bc, first ^ 1);
+    }
+    return;
+  }
+  const int sx = L.n1 * L.n2, sy = L.n2;  // a tail level holds at most kTailCpt * 1024 cells
+  // per cell: bits 0-5 the neighbours present (+x, -x, +y, -y, +z, -z), bit 6 the colour, bit 7
+  // the cell exists; the cell is threadIdx.x + c * blockDim.x
+  unsigned msk[kTailCpt];
+  float rc[kTailCpt], mc[kTailCpt];
+#pragma unroll
+  for (int c = 0; c < kTailCpt; ++c) {
+    const int e = threadIdx.x + c * blockDim.x;
+    msk[c] = 0;
+    rc[c] = 0.f;
+    mc[c] = 1.f;
+    if (e < (int)L.count) {
+      int i, j, k;
+      decode(L, e, i, j, k);
+      float nb, mult;
+      stencil<D>(z, L, bc, i, j, k, e, nb, mult);
+      msk[c] = (i < L.n0 - 1 ? 1u : 0u) | (i > 0 ? 2u : 0u) | (j < L.n1 - 1 ? 4u : 0u) | (j > 0 ? 8u : 0u) |
+               (D == 3 && k < L.n2 - 1 ? 16u : 0u) | (D == 3 && k > 0 ? 32u : 0u) |
+               ((unsigned)((i + j + k) & 1) << 6) | 128u;
+      rc[c] = r[e];
+      mc[c] = mult;
+    }
+  }
+  for (int it = 0; it < iters; ++it)
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const unsigned want = 128u | ((unsigned)(first ^ h) << 6);
+#pragma unroll
+      for (int c = 0; c < kTailCpt; ++c) {
+        if ((msk[c] & 192u) == want) {
+          const int e = threadIdx.x + c * blockDim.x;
+          float ret = 0.f;
+          if (msk[c] & 1u) ret += z[e + sx];
+          if (msk[c] & 2u) ret += z[e - sx];
+          if (msk[c] & 4u) ret += z[e + sy];
+          if (msk[c] & 8u) ret += z[e - sy];
+          if (msk[c] & 16u) ret += z[e + 1];
+          if (msk[c] & 32u) ret += z[e - 1];
+          z[e] = (rc[c] + ret) / mc[c];
+        }
+      }
+      __syncthreads();
+    }
+}
+
 template <int D, typename S>
 __global__ void __launch_bounds__(kTailThreads) k_vcycle_tail(S* __restrict__ zg, const S* __restrict__ rg,
                                                               TailPlan T, BC bc, int pre_post, int bottom,
@@ -749,10 +809,7 @@ __global__ void __launch_bounds__(kTailThreads) k_vcycle_tail(S* __restrict__ zg
   for (int l = l0; l < T.L - 1; ++l) {
     float* z = Z + T.off[l];
     const float* r = R + T.off[l];
-    for (int it = 0; it < pre_post; ++it) {
-      tail_smooth<D>(z, r, T.lv[l], bc, 0);
-      tail_smooth<D>(z, r, T.lv[l], bc, 1);
-    }
+    tail_sweeps<D>(z, r, T.lv[l], bc, pre_post, 0);
     const Lvl Lf = T.lv[l], Lc = T.lv[l + 1];
     float* zc = Z + T.off[l + 1];
     float* rc = R + T.off[l + 1];
@@ -779,10 +836,7 @@ __global__ void __launch_bounds__(kTailThreads) k_vcycle_tail(S* __restrict__ zg
   {
     float* z = Z + T.off[T.L - 1];
     const float* r = R + T.off[T.L - 1];
-    for (int it = 0; it < bottom; ++it) {
-      tail_smooth<D>(z, r, T.lv[T.L - 1], bc, 0);
-      tail_smooth<D>(z, r, T.lv[T.L - 1], bc, 1);
-    }
+    tail_sweeps<D>(z, r, T.lv[T.L - 1], bc, bottom, 0);
   }
   for (int l = T.L - 2; l >= l0; --l) {
     float* z = Z + T.off[l];
@@ -797,10 +851,7 @@ __global__ void __launch_bounds__(kTailThreads) k_vcycle_tail(S* __restrict__ zg
       z[e] += zc[ce];
     }
     __syncthreads();
-    for (int it = 0; it < pre_post; ++it) {
-      tail_smooth<D>(z, r, Lf, bc, 1);
-      tail_smooth<D>(z, r, Lf, bc, 0);
-    }
+    tail_sweeps<D>(z, r, Lf, bc, pre_post, 1);
   }
   for (int e = threadIdx.x; e < (int)T.lv[l0].count; e += blockDim.x) stv(zg + e, Z[T.off[l0] + e]);
 }

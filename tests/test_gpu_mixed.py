@@ -130,3 +130,27 @@ def test_tma_smoother_is_bitwise_the_global_one(prec, res):
         torch.cuda.synchronize()
         out.append((x, info.iterations, info.rTr))
     assert torch.equal(out[0][0], out[1][0]) and out[0][1:] == out[1][1:]
+
+
+def test_vcycle_tail_is_bitwise_the_grid_kernels():
+    """The one-block V-cycle tail gives bitwise the solve of the grid-wide kernels, whether its
+    levels take the register path (at most four cells per thread: 12x8x8 and 6x4x4) or the generic
+    loop (the 24x16x16 level, 6,144 cells): pressure, iterations and residual for tail thresholds
+    0 (no tail), 4,096 and 8,192 cells, FP32 levels.  (With 16-bit levels the tail keeps its
+    levels in FP32 shared memory while the grid-wide kernels round every store to the level
+    storage, so the two differ there by design.)"""
+    prec = 0
+    from pfm import _lib
+    rng = np.random.default_rng(8)
+    res = (48, 32, 32)
+    sc = pfm.Scene(3, res, 1.0 / 32, 0, base_level=2)
+    r = torch.as_tensor(rng.standard_normal(res).astype(np.float32)).cuda()
+    out = []
+    for cells in (0, 4096, 8192):
+        sc.set_tuning(_lib.TUNE_MG_TAIL_CELLS, cells)
+        x = torch.zeros_like(r)
+        info = sc.mgpcg_solve(r, x, k=-1.0, tol=1e-6, tol_mode=1, max_iters=200, precision=prec)
+        torch.cuda.synchronize()
+        out.append((x, info.iterations, info.rTr))
+    for x, it, rtr in out[1:]:
+        assert torch.equal(out[0][0], x) and (it, rtr) == out[0][1:]
