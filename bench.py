@@ -381,6 +381,19 @@ def main():
                 "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                 "traffic_source": "ncu capture at 128^3 scaled by the particle count",
                 "bytes_per_launch": rk4_bytes, "ms_per_launch": rk4_ms}
+    # The same launch against the FP32 roofline: executed FP32 flops (fadd + fmul + 2 ffma) of an ncu
+    # count of k_rk4_T_forward3<true, true> at 128^3 (2,511,667,223 + 5,469,372,416 + 2 x
+    # 11,005,853,696 for 16,777,216 particles: 1,787.7 per particle), scaled by the particle count,
+    # over the FMA-throughput probe of this GPU (outside every timed region)
+    import pfm
+    rk4_flops = (2511667223 + 5469372416 + 2 * 11005853696) / 16777216 * P
+    fp32_peak = pfm.measure_fp32_peak()
+    fp32_achieved = rk4_flops / (rk4_ms / 1e3) / 1e12
+    roofline_fp32 = {"bound": "fp32", "kernel": "k_rk4_T_forward3", "achieved": fp32_achieved, "peak": fp32_peak,
+                     "unit": "TFLOP/s", "frac": fp32_achieved / fp32_peak,
+                     "peak_kind": "measured (pfm_measure_fp32_peak: 8-chain FMA loop)",
+                     "flops_per_launch": rk4_flops,
+                     "flops_source": "executed FP32 flops of an ncu count at 128^3 scaled by the particle count"}
 
     e2e = None
     if not args.no_e2e:
@@ -438,7 +451,8 @@ def main():
                 "phase_ms": {k: statistics.mean(v) for k, v in phases.items()},
                 "phase_note": "phase_ms: CUDA events around the eager phase calls of 3 further steps "
                               "(sum %.2f ms/step)" % head["eager_ms"],
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches}
+                "roofline": roofline, "roofline_fp32": roofline_fp32, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+                "gpu_launches": launches}
         if plain is not None and mixed:
             line["plain_fp32"] = {"value": plain["value"], "ms_per_step": plain["elapsed"] / args.steps * 1e3,
                                   "mgpcg_iters": plain["mg_iters"],

@@ -1,0 +1,21 @@
+"""The FP32 throughput probe behind the FP32 roofline: a plausible GB300 rate (152 SMs x 128 FP32
+lanes x 2 flops at 1-2.1 GHz is 39-81 TFLOP/s nominal) and argument checks on the host."""
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def test_fp32_peak_probe():
+    import pfm
+    torch.cuda.set_device(0)
+    rate = pfm.measure_fp32_peak(blocks_per_sm=4, iters=8192, reps=2)
+    assert 20.0 < rate < 120.0, rate
+
+
+def test_fp32_peak_probe_rejects_bad_arguments():
+    import pfm
+    with pytest.raises(pfm.PfmError):
+        pfm.measure_fp32_peak(blocks_per_sm=0)
+    with pytest.raises(pfm.PfmError):
+        pfm.measure_fp32_peak(iters=0)
