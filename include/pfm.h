@@ -458,7 +458,7 @@ int pfm3_add_vortex_ring(pfm_handle* h, float w, float rad, float delta, const f
 int pfm_split_central_vector(pfm_handle* h, const float* vc, float* u_x, float* u_y, float* u_z,
                              void* stream);
 
-/* Jittered particle seeding (the BASELINE configs' "uniformly jittered from seed"): each cell
+/* Jittered particle seeding (particles uniformly jittered from a seed): each cell
  * holds ppc_axis^dim particles, one per sub-cell, at (sub-lattice index + U) * dx / ppc_axis with
  * U from a counter-based splitmix64 hash of (seed, particle index, axis); cell-major order,
  * last axis fastest.  P must equal ppc_axis^dim * cells.  pos [dim][P].  Bit-identical to
