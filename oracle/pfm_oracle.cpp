@@ -1,7 +1,8 @@
 // CPU oracle for the particle-flow-map time step: a restatement of the reference's Taichi kernels.
 //
 // TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
-// call this library, always as the checker / the timed CPU baseline, never as the product path.
+// call this library, always as the oracle that results are compared with or as the timed CPU
+// baseline, never as the product path.
 //
 // Parity status: the reference ships no tests or golden vectors and Taichi 1.5.0 cannot be
 // installed here, so this oracle is pinned against golden vectors produced by executing the
