@@ -381,17 +381,18 @@ def main():
                 "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                 "traffic_source": "ncu capture at 128^3 scaled by the particle count",
                 "bytes_per_launch": rk4_bytes, "ms_per_launch": rk4_ms}
-    # The same launch against the FP32 roofline: executed FP32 flops (fadd + fmul + 2 ffma) of an ncu
-    # count of k_rk4_T_forward3<true, true> at 128^3 (2,511,667,223 + 5,469,372,416 + 2 x
-    # 11,005,853,696 for 16,777,216 particles: 1,787.7 per particle), scaled by the particle count,
-    # over the FMA-throughput probe of this GPU (outside every timed region)
+    # The same launch against the FP32 roofline: executed FP32 flops of an ncu count of
+    # k_rk4_T_forward3<true, true> at 128^3 for 16,777,216 particles -- FADD 2,511,667,223, FMUL
+    # 5,469,372,416, FFMA 11,005,853,696 (2 flops), packed FMUL2 1,509,949,440 (2 flops) and FFMA2
+    # 6,241,124,352 (4 flops): 3,455.7 per particle -- scaled by the particle count, over the
+    # FMA-throughput probe of this GPU (the better of scalar and packed FMAs; outside every timed region)
     import pfm
-    rk4_flops = (2511667223 + 5469372416 + 2 * 11005853696) / 16777216 * P
+    rk4_flops = (2511667223 + 5469372416 + 2 * 11005853696 + 2 * 1509949440 + 4 * 6241124352) / 16777216 * P
     fp32_peak = pfm.measure_fp32_peak()
     fp32_achieved = rk4_flops / (rk4_ms / 1e3) / 1e12
     roofline_fp32 = {"bound": "fp32", "kernel": "k_rk4_T_forward3", "achieved": fp32_achieved, "peak": fp32_peak,
                      "unit": "TFLOP/s", "frac": fp32_achieved / fp32_peak,
-                     "peak_kind": "measured (pfm_measure_fp32_peak: 8-chain FMA loop)",
+                     "peak_kind": "measured (pfm_measure_fp32_peak: 8-chain FMA loop, best of scalar and packed f32x2)",
                      "flops_per_launch": rk4_flops,
                      "flops_source": "executed FP32 flops of an ncu count at 128^3 scaled by the particle count"}
 

@@ -114,10 +114,12 @@ int pfm_mg_levels(const pfm_handle* h, int* levels);
 /* Number of kernels launched through this handle since pfm_create (bookkeeping for benchmarks). */
 int pfm_launch_count(const pfm_handle* h, uint64_t* launches);
 /* FP32 roofline denominator: times `reps` launches of an FMA-throughput kernel (8 independent
- * chains per thread, `blocks_per_sm` x SMs blocks of 256 threads, `iters` iterations) on `stream`
- * with CUDA events and writes the best rate in TFLOP/s (2 flops per FMA).  `sink` is one device
- * float the kernel may write (it does not, for any result the chains reach).  Synchronous. */
-int pfm_measure_fp32_peak(float* sink, int blocks_per_sm, int iters, int reps, double* tflops, void* stream);
+ * chains per thread, `blocks_per_sm` x SMs blocks of 256 threads, `iters` iterations; packed = 1
+ * advances them as 4 pairs with packed f32x2 FMAs) on `stream` with CUDA events and writes the
+ * best rate in TFLOP/s (2 flops per FMA).  `sink` is one device float the kernel may write (it
+ * does not, for any result the chains reach).  Synchronous. */
+int pfm_measure_fp32_peak(float* sink, int blocks_per_sm, int iters, int reps, int packed, double* tflops,
+                          void* stream);
 
 /* Launch-shape tunables of a handle.  Every value gives the same results bit for bit (the sums keep
  * their order); they only change how the work maps to the GPU.  Setting one drops the handle's

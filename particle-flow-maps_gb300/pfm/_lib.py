@@ -97,7 +97,7 @@ SIGNATURES = {
     "pfm_status_string": [_I],
     "pfm_mg_levels": [_P, ctypes.POINTER(_I)],
     "pfm_launch_count": [_P, ctypes.POINTER(ctypes.c_uint64)],
-    "pfm_measure_fp32_peak": [_P, _I, _I, _I, ctypes.POINTER(ctypes.c_double), _P],
+    "pfm_measure_fp32_peak": [_P, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_double), _P],
     "pfm3_add_vortex_ring": [_P, _F, _F, _F, ctypes.POINTER(_F), ctypes.POINTER(_F), ctypes.POINTER(_F), _I, _P, _P],
     "pfm_split_central_vector": [_P, _P, _P, _P, _P, _P],
     "pfm_seed_jittered": [_P, ctypes.c_uint64, _I, _P, _P],

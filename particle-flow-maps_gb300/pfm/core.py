@@ -666,15 +666,20 @@ def sort_particles_noalloc(pos, res, dx, cell_count, order):
         raise PfmError(st, "pfm_sort_particles_noalloc failed")
 
 
-def measure_fp32_peak(blocks_per_sm=4, iters=65536, reps=3, device=None):
+def measure_fp32_peak(blocks_per_sm=4, iters=65536, reps=3, packed=None, device=None):
     """FP32 FMA throughput of the current GPU in TFLOP/s (``pfm_measure_fp32_peak``): the best of
-    ``reps`` timed launches of an 8-chain FMA loop, 2 flops per FMA.  The denominator of the FP32
-    roofline beside HBM bandwidth.  Synchronous."""
+    ``reps`` timed launches of an 8-chain FMA loop, 2 flops per FMA, with scalar FMAs
+    (``packed=False``), packed f32x2 FMAs (``packed=True``) or the better of the two (``None``).
+    The denominator of the FP32 roofline beside HBM bandwidth.  Synchronous."""
     device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
     sink = torch.zeros(1, dtype=torch.float32, device=device)
-    out = ctypes.c_double(0.0)
-    st = _lib.load().pfm_measure_fp32_peak(_ptr(sink), int(blocks_per_sm), int(iters), int(reps), ctypes.byref(out),
-                                           ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream))
-    if st != 0:
-        raise PfmError(st, "pfm_measure_fp32_peak failed")
-    return out.value
+    best = 0.0
+    for mode in ((0, 1) if packed is None else (1 if packed else 0,)):
+        out = ctypes.c_double(0.0)
+        st = _lib.load().pfm_measure_fp32_peak(_ptr(sink), int(blocks_per_sm), int(iters), int(reps), mode,
+                                               ctypes.byref(out),
+                                               ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream))
+        if st != 0:
+            raise PfmError(st, "pfm_measure_fp32_peak failed")
+        best = max(best, out.value)
+    return best
