@@ -254,7 +254,8 @@ int pfm2_sort_particles(pfm_handle* h, const float* pos, int* cell_count, int* o
  * (nothing launched).  Every call on a device shares that array and leaves its last contents
  * there; calls that overlap in time (two streams, two host threads) race on it and must be
  * serialised by the caller.  The first call on each device (that device current) looks up the
- * array's address; make that first call before any stream capture.
+ * array's address; make that first call before any stream capture.  The address is kept for the
+ * life of the process: after a cudaDeviceReset() of a device, do not call this on that device.
  * Returns PFM_ERR_ARG (dim not 2/3, dx <= 0, particles < 0), PFM_ERR_NULL, PFM_ERR_SHAPE or
  * PFM_ERR_CUDA (launch error). */
 #define PFM_NOALLOC_MAX_PARTICLES (1 << 21)

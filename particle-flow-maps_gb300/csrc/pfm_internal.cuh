@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <string>
 
 #include "../../include/pfm.h"
@@ -193,6 +194,21 @@ struct GraphCursor {
   int begin_body(cudaGraph_t body);
   int end_body();
 };
+
+// cudaFuncSetAttribute acts on the current device's context only, so a kernel that needs more than
+// the default 48 KB of dynamic shared memory is opted in once per device: `done` holds a bit per
+// device ordinal (ordinals of 64 and above are opted in on every call).
+template <class K>
+inline cudaError_t opt_in_smem(K* kernel, int bytes, std::atomic<unsigned long long>& done) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0ull;
+  if (bit && (done.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess && bit) done.fetch_or(bit, std::memory_order_acq_rel);
+  return e;
+}
 
 inline unsigned grid_for(int64_t n, int threads) {
   int64_t b = (n + threads - 1) / threads;

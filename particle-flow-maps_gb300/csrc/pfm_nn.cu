@@ -751,8 +751,8 @@ extern "C" int pfm_nn_conv3(const pfm_conv3_args* a, void* stream) {
   const size_t need = 1024 + box + (size_t)p.nstage * stage + 8 * (2 + 2 * p.nstage) + 16;
   const size_t smem = occupancy_smem(need, p.ncols);
   if (smem > kMaxDynSmem) return PFM_ERR_SHAPE;
-  static std::once_flag attr;
-  std::call_once(attr, [] { cudaFuncSetAttribute(k_conv3_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem); });
+  static std::atomic<unsigned long long> attr{0};  // above the default 48 KB: opt in per device
+  if (pfm::opt_in_smem(k_conv3_fwd, kMaxDynSmem, attr) != cudaSuccess) return PFM_ERR_CUDA;
   dim3 grid((unsigned)(tiles1 * p.tiles2), (unsigned)a->d0);
   if (grid.y > 65535) return PFM_ERR_SHAPE;
   k_conv3_fwd<<<grid, kThreads, smem, (cudaStream_t)stream>>>(tm1, tm2, p);
@@ -817,8 +817,8 @@ extern "C" int pfm_nn_conv3_wgrad(const pfm_conv3_wgrad_args* a, void* stream) {
   const size_t need = base + (size_t)p.nabuf * kAbufBytes;
   const size_t smem = occupancy_smem(need, p.ncols);
   if (smem > kMaxDynSmem) return PFM_ERR_SHAPE;
-  static std::once_flag attr;
-  std::call_once(attr, [] { cudaFuncSetAttribute(k_conv3_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem); });
+  static std::atomic<unsigned long long> attr{0};  // above the default 48 KB: opt in per device
+  if (pfm::opt_in_smem(k_conv3_wgrad, kMaxDynSmem, attr) != cudaSuccess) return PFM_ERR_CUDA;
   cudaStream_t st = (cudaStream_t)stream;
   k_conv3_wgrad<<<dim3((unsigned)gx, (unsigned)gy), kWgThreads, smem, st>>>(tm1, tm2, tmdy, p);
   const int total = a->cout * cin * 27;

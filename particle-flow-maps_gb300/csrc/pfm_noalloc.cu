@@ -5,6 +5,7 @@
 // bit for bit: counts by int(pos/dx) clamped to the grid, each bin in ascending particle index.
 #include <mutex>
 
+#include "pfm_binsort.cuh"
 #include "pfm_internal.cuh"
 
 namespace pfm {
@@ -97,24 +98,20 @@ __global__ void __launch_bounds__(kNaThreads) k_na_scatter(const float* __restri
   order[start[na_key<D>(pos, P, q, g)] + slot[q]] = (int)q;
 }
 
-// each bin in ascending particle index (insertion sort of its few entries)
+// each bin in ascending particle index: bins of up to kSmallBin entries one thread each, larger
+// ones by a whole block in k_bin_sort_big (pfm_binsort.cuh), so a bin holding every particle takes
+// O(n log^2 n) work spread over a block instead of O(n^2) dependent steps
 __global__ void __launch_bounds__(kNaThreads) k_na_cell_sort(const int* __restrict__ start, int64_t C,
                                                              int* __restrict__ order) {
   int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= C) return;
   const int b = start[c], e = start[c + 1];
-  for (int i = b + 1; i < e; ++i) {
-    int v = order[i];
-    int j = i - 1;
-    while (j >= b && order[j] > v) {
-      order[j + 1] = order[j];
-      --j;
-    }
-    order[j + 1] = v;
-  }
+  sort_bin_by_thread(order, b, e - b);
 }
 
-// Device address of g_noalloc_scratch for the current device, looked up once per device.
+// Device address of g_noalloc_scratch for the current device, looked up once per device and kept
+// for the life of the process.  A cudaDeviceReset() ends the context that address belongs to: a
+// process that resets a device must not call this entry point on that device afterwards.
 int scratch_for_current_device(int** out) {
   static std::mutex mu;
   static int* addr[kNaMaxDevices] = {};
@@ -172,6 +169,7 @@ extern "C" int pfm_sort_particles_noalloc(int dim, const int res[3], double dx, 
     else
       k_na_scatter<2><<<blocks_for(P), kNaThreads, 0, st>>>(pos, P, g, slot, start, order);
     k_na_cell_sort<<<blocks_for(C), kNaThreads, 0, st>>>(start, C, order);
+    k_bin_sort_big<<<(unsigned)((C + kBigThreads - 1) / kBigThreads), kBigThreads, 0, st>>>(start, C, order);
   }
   return cudaGetLastError() == cudaSuccess ? PFM_OK : PFM_ERR_CUDA;
 }

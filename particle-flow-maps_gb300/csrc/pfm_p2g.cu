@@ -16,6 +16,7 @@
 #include <climits>
 #include <mutex>
 
+#include "pfm_binsort.cuh"
 #include "pfm_internal.cuh"
 
 namespace pfm {
@@ -138,57 +139,14 @@ __global__ void __launch_bounds__(kBinThreads) k_scatter_order(const int* __rest
   order[start[key[q]] + slot[q]] = (int)q;
 }
 
-// Bins of at most N entries: all loads issued together into registers (INT_MAX past the end), a
-// bitonic sorting network, and the first n values stored back.  The entries are distinct particle
-// indices, so the result is the ascending order whatever the network.
-template <int N>
-__device__ __forceinline__ void sort_bin_small(int* __restrict__ order, int b, int n) {
-  int v[N];
-#pragma unroll
-  for (int i = 0; i < N; ++i) v[i] = i < n ? order[b + i] : INT_MAX;
-#pragma unroll
-  for (int k = 2; k <= N; k <<= 1)
-#pragma unroll
-    for (int j = k >> 1; j > 0; j >>= 1)
-#pragma unroll
-      for (int i = 0; i < N; ++i) {
-        const int l = i ^ j;
-        if (l > i) {
-          const int lo = min(v[i], v[l]), hi = max(v[i], v[l]);
-          const bool up = (i & k) == 0;
-          v[i] = up ? lo : hi;
-          v[l] = up ? hi : lo;
-        }
-      }
-#pragma unroll
-  for (int i = 0; i < N; ++i)
-    if (i < n) order[b + i] = v[i];
-}
-
-// each bin in ascending particle index: the stable order of a CPU counting sort
+// each bin in ascending particle index: the stable order of a CPU counting sort.  Bins of up to
+// kSmallBin entries here, one thread per bin; larger ones in k_bin_sort_big (pfm_binsort.cuh).
 __global__ void __launch_bounds__(kBinThreads) k_cell_sort(const int* __restrict__ start, int64_t C,
                                                            int* __restrict__ order) {
   int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= C) return;
   const int b = start[c], e = start[c + 1];
-  if (e - b <= 1) return;
-  if (e - b <= 8) {
-    sort_bin_small<8>(order, b, e - b);
-    return;
-  }
-  if (e - b <= 16) {
-    sort_bin_small<16>(order, b, e - b);
-    return;
-  }
-  for (int i = b + 1; i < e; ++i) {  // larger bins: insertion sort in place
-    int v = order[i];
-    int j = i - 1;
-    while (j >= b && order[j] > v) {
-      order[j + 1] = order[j];
-      --j;
-    }
-    order[j + 1] = v;
-  }
+  sort_bin_by_thread(order, b, e - b);
 }
 
 // Payload and cell keys (3D), one pass in particle order q (coalesced reads and writes); the
@@ -728,6 +686,7 @@ static int sort_from_keys(pfm_handle* h, cudaStream_t st) {
   if (P > 0) {
     launch(h, k_scatter_order, grid_for(P, kBinThreads), kBinThreads, 0, st, key, slot, (const int*)start, P, order);
     launch(h, k_cell_sort, grid_for(C, kBinThreads), kBinThreads, 0, st, (const int*)start, C, order);
+    launch(h, k_bin_sort_big, grid_for(C, kBigThreads), kBigThreads, 0, st, (const int*)start, C, order);
   }
   return launch_check(h, "sort_particles");
 }
@@ -788,12 +747,8 @@ int p2g3_from_records(pfm_handle* h, float* const* us, float* const* ws, cudaStr
     if (rc) return rc;
   }
   if (h->P > 0) {
-    static std::once_flag attr;  // above the default 48 KB of dynamic shared memory: opt in once
-    static cudaError_t attr_rc = cudaSuccess;
-    std::call_once(attr, [] {
-      attr_rc = cudaFuncSetAttribute(k_tile3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem);
-    });
-    rc = check_cuda(h, attr_rc, "k_tile3 shared-memory attribute");
+    static std::atomic<unsigned long long> attr{0};  // above the default 48 KB: opt in per device
+    rc = check_cuda(h, opt_in_smem(k_tile3, (int)kTileSmem, attr), "k_tile3 shared-memory attribute");
     if (rc) return rc;
     const int nt[3] = {(h->geom.N[0] + kTX - 1) / kTX, (h->geom.N[1] + kTY - 1) / kTY, (h->geom.N[2] + kTZ - 1) / kTZ};
     for (int px = 0; px < 2; ++px)
@@ -951,12 +906,8 @@ int pfm3_p2g_smoke(pfm_handle* h, const float* smoke_p, const float* init_grad_s
   if (h->P > 0) {
     const int* start = ws_ptr<int>(h, h->o_start);
     const int* order = ws_ptr<int>(h, h->o_order);
-    static std::once_flag attr;  // above the default 48 KB of dynamic shared memory: opt in once
-    static cudaError_t attr_rc = cudaSuccess;
-    std::call_once(attr, [] {
-      attr_rc = cudaFuncSetAttribute(k_tile_smoke3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmokeTileSmem);
-    });
-    rc = check_cuda(h, attr_rc, "k_tile_smoke3 shared-memory attribute");
+    static std::atomic<unsigned long long> attr{0};  // above the default 48 KB: opt in per device
+    rc = check_cuda(h, opt_in_smem(k_tile_smoke3, (int)kSmokeTileSmem, attr), "k_tile_smoke3 shared-memory attribute");
     if (rc) return rc;
     const int nt[3] = {(h->geom.N[0] + kTX - 1) / kTX, (h->geom.N[1] + kTY - 1) / kTY, (h->geom.N[2] + kTZ - 1) / kTZ};
     for (int px = 0; px < 2; ++px)

@@ -659,9 +659,13 @@ def sort_particles_noalloc(pos, res, dx, cell_count, order):
         if t.dtype != dt or not t.is_cuda or not t.is_contiguous() or (n is not None and t.numel() < n):
             raise PfmError(2, f"{name} must be a contiguous CUDA {dt} tensor"
                               + (f" with at least {n} entries" if n is not None else ""))
+        if t.device != pos.device:
+            raise PfmError(7, f"{name} is on {t.device}, pos on {pos.device}: all three must share a device")
     r = (ctypes.c_int * 3)(*(list(int(x) for x in res) + [1] * (3 - dim)))
-    st = _lib.load().pfm_sort_particles_noalloc(dim, r, float(dx), P, _ptr(pos), _ptr(cell_count), _ptr(order),
-                                                 ctypes.c_void_p(torch.cuda.current_stream(pos.device).cuda_stream))
+    # the entry point takes its scratch on the current device: make it pos's device for the call
+    with torch.cuda.device(pos.device):
+        st = _lib.load().pfm_sort_particles_noalloc(dim, r, float(dx), P, _ptr(pos), _ptr(cell_count), _ptr(order),
+                                                     ctypes.c_void_p(torch.cuda.current_stream(pos.device).cuda_stream))
     if st != 0:
         raise PfmError(st, "pfm_sort_particles_noalloc failed")
 

@@ -370,6 +370,38 @@ def test_p2g3_and_sort_collisions_and_edges():
         assert torch.equal(a, b)
 
 
+def test_sort_large_bins_bitexact_and_bounded():
+    """Bins far beyond the register network's 16 entries: 1.5M particles in one cell, 300K in
+    another, 4,000 and 17 in two more, the rest spread, in a shuffled particle order (so the atomic
+    slot order inside each bin is scrambled): the permutation equals numpy's stable argsort bit for
+    bit, and the sort of 2.1M particles ends within a time bound."""
+    import time
+    rng = np.random.default_rng(21)
+    res = (16, 12, 20)
+    dx = 1.0 / res[1]
+    parts = [(np.array([5, 6, 7]) + rng.random((1_500_000, 3))) * dx,
+             (np.array([0, 0, 0]) + rng.random((300_000, 3))) * dx,
+             (np.array([15, 11, 19]) + rng.random((4000, 3))) * dx,
+             (np.array([9, 2, 3]) + rng.random((17, 3))) * dx,
+             rng.random((300_000, 3)) * np.array(res) * dx]
+    pos = np.concatenate(parts).astype(np.float32)
+    pos = pos[rng.permutation(pos.shape[0])]
+    P = pos.shape[0]
+    sc = pfm.Scene(3, res, dx, P)
+    pos_d = pfm.soa(pos)
+    cells = np.clip((pos / np.float32(dx)).astype(np.int64), 0, np.array(res) - 1)
+    key = (cells[:, 0] * res[1] + cells[:, 1]) * res[2] + cells[:, 2]
+    want = np.argsort(key, kind="stable")
+    for _ in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        count, order = sc.sort_particles(pos_d)
+        torch.cuda.synchronize()
+        assert time.perf_counter() - t0 < 2.0
+        assert np.array_equal(host(order), want)
+        assert np.array_equal(host(count).ravel(), np.bincount(key, minlength=int(np.prod(res))))
+
+
 def test_p2g2_collisions_and_edges():
     rng = np.random.default_rng(12)
     res = (24, 16)

@@ -67,6 +67,38 @@ def test_noalloc_sort_zero_particles():
     assert int(count.abs().sum()) == 0
 
 
+@pytest.mark.gpu
+def test_noalloc_sort_all_particles_in_one_cell():
+    """The largest input the scratch holds, every particle in one bin (half of them inside the
+    cell, half clamped into it from outside the grid), on two consecutive calls: the permutation is
+    the stable one, and each call ends within a time bound (the per-bin ordering does O(n log^2 n)
+    work spread over a thread block, not O(n^2) dependent steps in one thread)."""
+    import time
+    dev = torch.device("cuda:0")
+    res, dx = (8, 8, 8), 0.125
+    P = _lib.NOALLOC_MAX_PARTICLES
+    rng = np.random.default_rng(5)
+    pos = np.empty((3, P), np.float32)
+    half = P // 2
+    pos[:, :half] = ((np.array([[7], [7], [7]]) + rng.random((3, half))) * dx).astype(np.float32)
+    pos[:, half:] = (1.0 + rng.random((3, P - half))).astype(np.float32)  # beyond the grid: clamped
+    pos = np.ascontiguousarray(pos[:, rng.permutation(P)])
+    pos_d = torch.from_numpy(pos).to(dev)
+    ref_count, ref_order = _stable(pos, res, dx)
+    assert ref_count.max() == P
+    for _ in range(2):
+        count = torch.full((512,), -7, dtype=torch.int32, device=dev)
+        order = torch.full((P,), -7, dtype=torch.int32, device=dev)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pfm.sort_particles_noalloc(pos_d, res, dx, count, order)
+        torch.cuda.synchronize()
+        elapsed = time.perf_counter() - t0
+        assert elapsed < 2.0, elapsed
+        assert np.array_equal(count.cpu().numpy(), ref_count)
+        assert np.array_equal(order.cpu().numpy(), ref_order)
+
+
 def test_noalloc_rejects_sizes_beyond_its_scratch():
     """Validation happens before any CUDA call, so this runs without a GPU."""
     lib = pfm.load()
