@@ -85,3 +85,25 @@ def test_run_2d_main_matches_sim2d(tmp_path):
     torch.cuda.synchronize()
     assert torch.equal(r.u_x, sim.u[0]) and torch.equal(r.u_y, sim.u[1])
     assert torch.equal(r.particles_pos, sim.pos)
+
+
+@pytest.mark.gpu
+def test_run_2d_restart_from_checkpoint(tmp_path):
+    """main(from_frame=k) (2D/run_2D.py:725-728) reloads vel_{x,y}_numpy_<k>.npy and
+    smoke_numpy_<k>.npy bit for bit; with a reinitialisation every 2 steps and one step per frame
+    the continued run writes the uninterrupted run's frames 3 and 4 bit for bit."""
+    hp = dict(res_x=64, res_y=32, particles_per_cell=4, save_frame_each_step=True, ckpt_every=1, total_frames=4,
+              use_total_steps=False, reinit_every=2, reinit_every_grad_m=1, CFL=0.5, exp_name="rs2")
+    _, r = _import_2d(**hp)
+    assert r.main(logs_root=str(tmp_path)) == 4
+    ck = tmp_path / "rs2" / "ckpts"
+    first = {f: {n: np.load(ck / f"vel_{n}_numpy_{f}.npy") for n in "xy"} for f in (2, 3, 4)}
+    smoke2 = np.load(ck / "smoke_numpy_2.npy")
+    _, r = _import_2d(**hp)
+    assert r.main(from_frame=2, logs_root=str(tmp_path)) == 2
+    assert np.array_equal(np.load(ck / "smoke_numpy_2.npy"), smoke2)
+    for n, t in zip("xy", (r.u_x, r.u_y)):
+        assert np.array_equal(np.load(ck / f"vel_{n}_numpy_2.npy"), first[2][n]), n
+        for f in (3, 4):
+            assert np.array_equal(np.load(ck / f"vel_{n}_numpy_{f}.npy"), first[f][n]), (f, n)
+        assert np.array_equal(t.cpu().numpy(), first[4][n]), n

@@ -241,3 +241,37 @@ def test_dropin_smoke_and_variants():
     r.compute_dT_dx(gx, gy, gz, *eye, pos, r.cell_particles_id, r.cell_particle_num)
     torch.cuda.synchronize()
     assert not gx.any() and not gy.any() and not gz.any()
+
+
+@pytest.mark.gpu
+def test_run_3d_restart_from_checkpoint(tmp_path):
+    """main(from_frame=k) (3D/run_3D.py:676-680) reloads vel_{x,y,z}_numpy_<k>.npy, the files main()
+    writes at every checkpoint frame (3D/run_3D.py:846-853): the reloaded velocity is the saved one
+    bit for bit, and because the restart reseeds the particles exactly as the uninterrupted run
+    does at a reinitialisation step (reinit every 2 steps, one step per frame), the continued run
+    writes the same frames 3 and 4 bit for bit."""
+    hp = dict(res_x=32, res_y=16, res_z=16, save_frame_each_step=True, ckpt_every=1, total_frames=4,
+              use_total_steps=False, reinit_every=2, reinit_every_grad_m=1, exp_name="rs")
+    _, r = _import_3d(**hp)
+    assert r.main(logs_root=str(tmp_path)) == 4
+    ck = tmp_path / "rs" / "ckpts"
+    first = {f: {n: np.load(ck / f"vel_{n}_numpy_{f}.npy") for n in "xyz"} for f in (2, 3, 4)}
+    _, r = _import_3d(**hp)
+    assert r.main(from_frame=2, logs_root=str(tmp_path)) == 2
+    for n, t in zip("xyz", (r.u_x, r.u_y, r.u_z)):
+        # main() writes the velocity it loaded back under the restart frame before stepping
+        assert np.array_equal(np.load(ck / f"vel_{n}_numpy_2.npy"), first[2][n]), n
+        for f in (3, 4):
+            assert np.array_equal(np.load(ck / f"vel_{n}_numpy_{f}.npy"), first[f][n]), (f, n)
+        assert np.array_equal(t.cpu().numpy(), first[4][n]), n
+    # the continued run equals pfm.Sim3D started from the frame-2 velocity with lattice seeds
+    import pfm
+    u2 = [torch.from_numpy(first[2][n]).cuda() for n in "xyz"]
+    sim = pfm.Sim3D(u2, pfm.lattice3((32, 16, 16), r.dx), (32, 16, 16), r.dx, CFL=r.CFL, reinit_every=2,
+                    reinit_every_grad_m=1)
+    sim.clock.save_frame_each_step = True
+    for _ in range(2):
+        sim.step()
+    torch.cuda.synchronize()
+    for n, t in zip("xyz", sim.u):
+        assert np.array_equal(t.cpu().numpy(), first[4][n]), n
