@@ -181,23 +181,81 @@ __global__ void __launch_bounds__(kBinThreads) k_payload2(const int* __restrict_
 // face family the thread sums its cell's particles (particle-index order) into a register window
 // of the 4 x 3 x 3 faces they can reach (4 along the family's own axis: faces c-1 .. c+2; 3 along
 // the others: c-1 .. c+1), every thread stores its window in shared memory (36 slots x 512 cells,
-// 147 KB: the kernel runs one block per SM anyway), and after one barrier each face of the region
-// around the tile sums the slots of the cells that reach it, in slot order, and adds the sum into
-// the face grids.  Tiles run in 8 launches by the parity of their tile coordinates: tiles of one
-// parity are a tile apart and their face regions (one face below, two above) never overlap, so no
-// atomics are needed.  Each face sums in a fixed order (launch, pass, particle index): the result
-// is bitwise reproducible (the same sums, in the same order, as merging the windows into a shared
-// copy of the region in 36 passes with a barrier between passes).  Particles outside the grid sit in the clamped edge cell, whose window
-// still holds every in-grid face they reach; their weights come from their real positions.
-constexpr int kTX = 8, kTY = 8, kTZ = 8;
+// 147 KB), and after one barrier each face of the region around the tile sums the slots of the
+// cells that reach it, in slot order, and adds the sum into the face grids.  Tiles run in 8
+// launches by the parity of their tile coordinates: tiles of one parity are a tile apart and their
+// face regions (one face below, two above) never overlap, so no atomics are needed.  Each face
+// sums in a fixed order (launch, pass, particle index): the result is bitwise reproducible (the
+// same sums, in the same order, as merging the windows into a shared copy of the region in 36
+// passes with a barrier between passes).  Particles outside the grid sit in the clamped edge cell,
+// whose window still holds every in-grid face they reach; their weights come from their real
+// positions.
+//
+// Record staging: a cell's particles are gathered through the sorted order, so each one costs a
+// memory round trip.  Every thread keeps a ring of kRing particle slots in shared memory (pos4 and
+// the family record, 32 B) filled by 16-byte asynchronous copies (cp.async, no registers held), so
+// kRing - 1 particles are in flight while one is summed; the next slot's particle index is read one
+// iteration ahead.  The first kRing copies of the next family are issued before the window merge
+// and face add-back of the current one, so that memory latency overlaps the merge.
+// Tile of 4 x 8 x 16 cells: 16 along the last axis, the length of the seeding order's cell groups
+// (pfm_seed_jittered), so the records of a group's particles are read by one tile in one launch
+// (with 8-cell tiles a group's 128-particle runs are split between tiles of different parity
+// launches and every record line is fetched twice).
+#ifndef PFM_TILE_X
+#define PFM_TILE_X 4
+#endif
+#ifndef PFM_TILE_Y
+#define PFM_TILE_Y 8
+#endif
+#ifndef PFM_TILE_Z
+#define PFM_TILE_Z 16
+#endif
+constexpr int kTX = PFM_TILE_X, kTY = PFM_TILE_Y, kTZ = PFM_TILE_Z;
 constexpr int kTileThreads = kTX * kTY * kTZ;
+static_assert(kTileThreads == 512, "the P2G tiles are 512-cell blocks");
+static_assert(kTX >= 3 && kTY >= 3 && kTZ >= 3, "same-parity tiles must be far enough apart for their face regions");
 constexpr int kWinSlots = 4 * 3 * 3;                                              // window faces per cell
-constexpr size_t kTileSmem = (size_t)kWinSlots * kTileThreads * sizeof(float2);  // 147,456 B
+constexpr int kRing = 5;                                                          // staged particles per thread
+constexpr size_t kWinBytes = (size_t)kWinSlots * kTileThreads * sizeof(float2);  // 147,456 B
+constexpr size_t kRingBytes = (size_t)kRing * 2 * kTileThreads * sizeof(float4);  // 81,920 B
+constexpr size_t kTileSmem = kWinBytes + kRingBytes;                              // 229,376 B
+static_assert(kTileSmem <= 227 * 1024, "k_tile3 exceeds the 227 KB of shared memory of a block");
 
 struct FaceOut3 {
   float* u[3];
   float* w[3];
 };
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Ring slot d of this thread: ring[(2 d) * kTileThreads + t] = pos4, ring[(2 d + 1) * kTileThreads + t] = record
+// (a warp's 32 lanes read 512 contiguous bytes per slot array: no bank conflicts).
+__device__ __forceinline__ void ring_fill(float4* ring, int d, const float4* __restrict__ pos4,
+                                          const float4* __restrict__ rec, int q) {
+  cp_async16(ring + (2 * d) * kTileThreads + threadIdx.x, pos4 + q);
+  cp_async16(ring + (2 * d + 1) * kTileThreads + threadIdx.x, rec + q);
+}
+
+// The first kRing particles of a family's loop; one commit group per slot (empty past the end).
+// Returns the particle index of slot sb + kRing (read ahead for the loop).
+__device__ __forceinline__ int ring_prologue(float4* ring, const float4* __restrict__ pos4,
+                                             const float4* __restrict__ rec, const int* __restrict__ order, int sb,
+                                             int se) {
+#pragma unroll
+  for (int d = 0; d < kRing; ++d) {
+    if (sb + d < se) ring_fill(ring, d, pos4, rec, __ldg(order + sb + d));
+    cp_async_commit();
+  }
+  return sb + kRing < se ? __ldg(order + sb + kRing) : 0;
+}
 
 // Weights and offsets of the window faces c-1 .. c-1+W-1 along one axis (N_2 of 3D/run_3D.py:486)
 template <bool OWN>
@@ -235,49 +293,71 @@ __device__ __forceinline__ void tile_axis(float p, int c, float dx, float* w, fl
   }
 }
 
-template <int FAM>
-__device__ __forceinline__ void tile_family(float2* __restrict__ win, const float4* __restrict__ pos4,
-                                            const float4* __restrict__ rec, const int* __restrict__ order, int sb,
-                                            int se, int ci, int cj, int ck, int x0, int y0, int z0,
-                                            const MacGeom& g, int use_apic, float* __restrict__ u,
-                                            float* __restrict__ w) {
+// One family: the particle loop from the ring (whose prologue was issued earlier; qn is the index
+// of slot sb + kRing), the window store, and -- after the barrier -- the next family's ring
+// prologue (NEXT >= 0), the window merge and the face add-back.
+template <int FAM, int NEXT>
+__device__ __forceinline__ int tile_family(float2* __restrict__ win, float4* ring, const float4* __restrict__ pos4,
+                                           const float4* __restrict__ rec, const float4* __restrict__ rec_next,
+                                           const int* __restrict__ order, int sb, int se, int qn, int ci, int cj,
+                                           int ck, int x0, int y0, int z0, const MacGeom& g, int use_apic,
+                                           float* __restrict__ u, float* __restrict__ w) {
   constexpr int W0 = FAM == 0 ? 4 : 3, W1 = FAM == 1 ? 4 : 3, W2 = FAM == 2 ? 4 : 3;
   constexpr int E0 = kTX + W0 - 1, E1 = kTY + W1 - 1, E2 = kTZ + W2 - 1, NE = E0 * E1 * E2;
   static_assert(W0 * W1 * W2 <= kWinSlots, "window exceeds the shared buffer");
-  float num[W0][W1][W2], den[W0][W1][W2];
+  float2 acc[W0][W1][W2];  // (numerator, weight sum) of each window face
 #pragma unroll
   for (int a = 0; a < W0; ++a)
 #pragma unroll
     for (int b = 0; b < W1; ++b)
 #pragma unroll
-      for (int k = 0; k < W2; ++k) num[a][b][k] = den[a][b][k] = 0.f;
+      for (int k = 0; k < W2; ++k) acc[a][b][k] = make_float2(0.f, 0.f);
   const float dx = g.dx;
-  // the next slot's particle index is read one iteration ahead, so each particle costs one
-  // memory round trip (its records) instead of two (index, then records)
-  int qn = sb < se ? __ldg(order + sb) : 0;
+  int d = 0;
   for (int s = sb; s < se; ++s) {
-    const int q = qn;  // sorted slot -> particle
-    if (s + 1 < se) qn = __ldg(order + s + 1);
-    const float4 p = __ldg(pos4 + q);
-    const float4 fr = __ldg(rec + q);
+    cp_async_wait<kRing - 1>();  // slot d (group s - sb of this family) has landed
+    const float4 p = ring[(2 * d) * kTileThreads + threadIdx.x];
+    const float4 fr = ring[(2 * d + 1) * kTileThreads + threadIdx.x];
     float w0[W0], d0[W0], w1[W1], d1[W1], w2[W2], d2[W2];
     tile_axis<FAM == 0>(p.x, ci, dx, w0, d0);
     tile_axis<FAM == 1>(p.y, cj, dx, w1, d1);
     tile_axis<FAM == 2>(p.z, ck, dx, w2, d2);
+    // Face (a, b, k) receives w0[a] w1[b] w2[k] (m + c1 d0[a] + c2 d1[b] + c3 d2[k]) with
+    // (m, c1, c2, c3) the record (APIC: run_3D.py:486-528); factored per axis as
+    // w2[k] P_ab + (w2[k] d2[k]) Q_ab, P_ab = w1[b] (m w0[a] + c1 w0[a] d0[a]) + c2 w0[a] (w1[b] d1[b]),
+    // Q_ab = c3 w0[a] w1[b], the weight sum w0[a] w1[b] w2[k] riding in the same packed FMA:
+    // two instructions per face instead of five (the same terms, associated differently).
+    const float m = fr.x;
+    const float c1 = use_apic ? fr.y : 0.f, c2 = use_apic ? fr.z : 0.f, c3 = use_apic ? fr.w : 0.f;
+    float e1[W1], e2[W2];
 #pragma unroll
-    for (int a = 0; a < W0; ++a)
+    for (int b = 0; b < W1; ++b) e1[b] = w1[b] * d1[b];
+#pragma unroll
+    for (int k = 0; k < W2; ++k) e2[k] = w2[k] * d2[k];
+#pragma unroll
+    for (int a = 0; a < W0; ++a) {
+      const float alpha = fmaf(c1, w0[a] * d0[a], m * w0[a]);
+      const float beta = c2 * w0[a], gamma = c3 * w0[a];
 #pragma unroll
       for (int b = 0; b < W1; ++b) {
-        const float w01 = w0[a] * w1[b];
-        const float d01 = fr.y * d0[a] + fr.z * d1[b];
+        const float2 pw = make_float2(fmaf(beta, e1[b], alpha * w1[b]), w0[a] * w1[b]);
+        const float Q = gamma * w1[b];
 #pragma unroll
         for (int k = 0; k < W2; ++k) {
-          const float wt = w01 * w2[k];
-          const float delta = d01 + fr.w * d2[k];
-          num[a][b][k] += (use_apic ? (fr.x + delta) : fr.x) * wt;
-          den[a][b][k] += wt;
+          acc[a][b][k] = __ffma2_rn(make_float2(w2[k], w2[k]), pw, acc[a][b][k]);
+          acc[a][b][k].x = fmaf(e2[k], Q, acc[a][b][k].x);
         }
       }
+    }
+    // refill the slot just read with particle s + kRing.  The empty asm takes sums that depend on
+    // every value read from the slot, so those reads have completed before the copy is issued.
+    asm volatile("" ::"f"(acc[W0 - 1][W1 - 1][W2 - 1].x), "f"(acc[W0 - 1][W1 - 1][W2 - 1].y) : "memory");
+    if (s + kRing < se) {
+      ring_fill(ring, d, pos4, rec, qn);
+      if (s + kRing + 1 < se) qn = __ldg(order + s + kRing + 1);
+    }
+    cp_async_commit();
+    d = d + 1 == kRing ? 0 : d + 1;
   }
 #pragma unroll
   for (int a = 0; a < W0; ++a)
@@ -285,8 +365,10 @@ __device__ __forceinline__ void tile_family(float2* __restrict__ win, const floa
     for (int b = 0; b < W1; ++b)
 #pragma unroll
       for (int k = 0; k < W2; ++k)
-        win[((a * W1 + b) * W2 + k) * kTileThreads + threadIdx.x] = make_float2(num[a][b][k], den[a][b][k]);
+        win[((a * W1 + b) * W2 + k) * kTileThreads + threadIdx.x] = acc[a][b][k];
   __syncthreads();
+  int qnext = 0;
+  if (NEXT >= 0) qnext = ring_prologue(ring, pos4, rec_next, order, sb, se);
   // Face e of the tile's region (origin one face below the tile) takes window slot (a, b, k) of
   // the cell e - (a, b, k), summed from zero in slot order (a, then b, then k)
   const int n0 = g.n[FAM][0], n1 = g.n[FAM][1], n2 = g.n[FAM][2];
@@ -314,9 +396,7 @@ __device__ __forceinline__ void tile_family(float2* __restrict__ win, const floa
           for (int k = 0; k < W2; ++k) {
             const int sz = ez - k;
             if (sz < 0 || sz >= kTZ) continue;
-            const float2 f = win[((a * W1 + b) * W2 + k) * kTileThreads + (sx * kTY + sy) * kTZ + sz];
-            v.x += f.x;
-            v.y += f.y;
+            v = __fadd2_rn(v, win[((a * W1 + b) * W2 + k) * kTileThreads + (sx * kTY + sy) * kTZ + sz]);
           }
         }
       }
@@ -331,6 +411,7 @@ __device__ __forceinline__ void tile_family(float2* __restrict__ win, const floa
     }
   }
   __syncthreads();
+  return qnext;
 }
 
 // One parity class (px, py, pz) of tiles; grid = (tiles along z, y, x of that parity).
@@ -339,7 +420,9 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_tile3(const float4* __restr
                                                            const int* __restrict__ order,
                                                            const int* __restrict__ start, MacGeom g, int use_apic,
                                                            int64_t P, int px, int py, int pz, FaceOut3 out) {
-  extern __shared__ float2 win[];  // kWinSlots x kTileThreads window values (num, den)
+  extern __shared__ __align__(16) unsigned char tile_smem[];
+  float2* win = reinterpret_cast<float2*>(tile_smem);  // kWinSlots x kTileThreads window values (num, den)
+  float4* ring = reinterpret_cast<float4*>(tile_smem + kWinBytes);
   const int x0 = (2 * (int)blockIdx.z + px) * kTX, y0 = (2 * (int)blockIdx.y + py) * kTY;
   const int z0 = (2 * (int)blockIdx.x + pz) * kTZ;
   const int lz = threadIdx.x % kTZ, ly = (threadIdx.x / kTZ) % kTY, lx = threadIdx.x / (kTZ * kTY);
@@ -350,9 +433,17 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_tile3(const float4* __restr
     sb = __ldg(start + c);
     se = __ldg(start + c + 1);
   }
-  tile_family<0>(win, pos4, famrec, order, sb, se, ci, cj, ck, x0, y0, z0, g, use_apic, out.u[0], out.w[0]);
-  tile_family<1>(win, pos4, famrec + P, order, sb, se, ci, cj, ck, x0, y0, z0, g, use_apic, out.u[1], out.w[1]);
-  tile_family<2>(win, pos4, famrec + 2 * P, order, sb, se, ci, cj, ck, x0, y0, z0, g, use_apic, out.u[2], out.w[2]);
+  const float4* r0 = famrec;
+  const float4* r1 = famrec + P;
+  const float4* r2 = famrec + 2 * P;
+  int qn = ring_prologue(ring, pos4, r0, order, sb, se);
+  qn = tile_family<0, 1>(win, ring, pos4, r0, r1, order, sb, se, qn, ci, cj, ck, x0, y0, z0, g, use_apic, out.u[0],
+                         out.w[0]);
+  qn = tile_family<1, 2>(win, ring, pos4, r1, r2, order, sb, se, qn, ci, cj, ck, x0, y0, z0, g, use_apic, out.u[1],
+                         out.w[1]);
+  tile_family<2, -1>(win, ring, pos4, r2, r2, order, sb, se, qn, ci, cj, ck, x0, y0, z0, g, use_apic, out.u[2],
+                     out.w[2]);
+  cp_async_wait<0>();
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -69,23 +69,40 @@ def _hash_uniform(seed, n):
     return (z >> np.uint64(40)).astype(np.float32) * np.float32(1.0 / 16777216.0)
 
 
+SEED_GROUP = 16  # cells of a line along the last axis that the seeding order interleaves
+
+
 def jittered(res, dx, ppc, seed=0):
     """Stratified jittered seeding, bit-identical to the device kernel pfm_seed_jittered.
 
     Each cell holds ppc particles, one per sub-cell of a ppc_axis^d lattice, at
     (sub-lattice index + U) * dx / ppc_axis, U a splitmix64 hash of (seed, particle, axis).
-    Cell-major order with the last axis fastest, so consecutive particles share grid
-    neighbourhoods."""
+    Order: the lines of cells along the last axis in turn, each in groups of 16 cells (the last
+    group takes the remainder), inside a group [leading sub-indices][cell][last sub-index]; with 8
+    particles per cell, 32 consecutive particles are 16 neighbouring cells with the same leading
+    sub-cell, so a warp's interpolation stencils share their rows."""
     d = len(res)
     axis = int(round(ppc ** (1.0 / d)))
     if axis ** d != ppc:
         raise ValueError("particles per cell must be a perfect square (2D) or cube (3D)")
     cells = int(np.prod(res))
     P = cells * ppc
+    nl = int(res[-1])
     q = np.arange(P, dtype=np.int64)
-    cell, sub = q // ppc, q % ppc
-    ci = np.stack(np.unravel_index(cell, res), axis=1)
-    si = np.stack(np.unravel_index(sub, (axis,) * d), axis=1)
+    line_len = nl * ppc
+    line, rem = q // line_len, q % line_len
+    gi = rem // (SEED_GROUP * ppc)
+    r = rem % (SEED_GROUP * ppc)
+    k0 = gi * SEED_GROUP
+    gsz = np.minimum(SEED_GROUP, nl - k0)
+    s_last = r % axis
+    t = r // axis
+    kk = t % gsz
+    o = t // gsz
+    lead = np.stack(np.unravel_index(line, tuple(res[:-1])), axis=1) if d > 1 else np.zeros((P, 0), np.int64)
+    ci = np.concatenate([lead, (k0 + kk)[:, None]], axis=1)
+    si_lead = np.stack(np.unravel_index(o, (axis,) * (d - 1)), axis=1)
+    si = np.concatenate([si_lead, s_last[:, None]], axis=1)
     lat = (ci * axis + si).astype(np.float32)
     u = _hash_uniform(seed, (q[:, None] * d + np.arange(d)[None, :]))
     return ((lat + u) * np.float32(dx / axis)).astype(np.float32)

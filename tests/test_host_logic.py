@@ -36,16 +36,26 @@ def test_lattice_is_the_reference_order():
     assert np.array_equal(pfm.lattice2((8, 4), 0.25, 4), O.lattice2((8, 4), 0.25, 4))
 
 
-def test_jitter_is_seeded_stratified_and_cell_major():
+def test_jitter_is_seeded_stratified_and_line_grouped():
     a = pfm.jittered((4, 4, 4), 0.25, 8, seed=0)
     b = pfm.jittered((4, 4, 4), 0.25, 8, seed=0)
     c = pfm.jittered((4, 4, 4), 0.25, 8, seed=1)
     assert np.array_equal(a, b) and not np.array_equal(a, c)
     cells = np.floor(a / 0.25).astype(int)
     lin = (cells[:, 0] * 4 + cells[:, 1]) * 4 + cells[:, 2]
-    assert np.array_equal(lin, np.repeat(np.arange(64), 8))  # 8 per cell, cell-major order
+    # each line of 4 cells along z holds its 32 particles consecutively, 8 per cell
+    assert np.array_equal(lin // 4, np.repeat(np.arange(16), 32))
+    assert np.array_equal(np.bincount(lin, minlength=64), np.full(64, 8))
     sub = np.floor(a / 0.125).astype(int) % 2
-    assert len({tuple(s) for s in sub[:8]}) == 8  # one per sub-cell
+    for cell in range(64):  # one per sub-cell
+        assert len({tuple(s) for s in sub[lin == cell]}) == 8
+    # 32 consecutive particles of a 16-cell group: 16 cells along z, one leading sub-cell
+    g = pfm.jittered((2, 2, 32), 1 / 32, 8, seed=0)
+    gc = np.floor(g / np.float32(1 / 32)).astype(int)
+    gs = np.floor(g / np.float32(1 / 64)).astype(int) % 2
+    for w in range(4):
+        blk = slice(32 * w, 32 * w + 32)
+        assert len({tuple(s) for s in gs[blk, :2]}) == 1 and len(set(gc[blk, 2])) == 16
     two = pfm.jittered((8, 8), 1 / 8, 4, seed=0)
     assert two.shape == (256, 2)
     with pytest.raises(ValueError):
