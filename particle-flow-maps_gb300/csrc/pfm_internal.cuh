@@ -48,7 +48,7 @@ struct Div32 {
   unsigned d, m, s;
 };
 
-inline Div32 make_div32(unsigned d) {
+__host__ __device__ inline Div32 make_div32(unsigned d) {
   unsigned s = 0;
   while ((1ull << s) < d) ++s;
   const unsigned long long m = ((1ull << 32) * ((1ull << s) - d)) / d + 1;
@@ -170,7 +170,7 @@ struct GraphCursor {
   pfm_handle* h;
   cudaGraph_t G;
   cudaStream_t cs;
-  cudaGraphNode_t deps[64];
+  cudaGraphNode_t deps[256];  // a batch joins one node per scene
   size_t ndeps = 0;
   bool open = false;
   int rc = 0;
@@ -518,6 +518,15 @@ int mgpcg_solve_in_place(pfm_handle* h, float* x, const pfm_solve_opts* opts, pf
 // the 2D RK4 (pfm_particles.cu).
 int append_poisson(GraphCursor& gc, float* const* u, float* p_io, const pfm_solve_opts& opts, StepCtl* ctl,
                    int which);
+// append_poisson in its three parts (pre: apply_bc, divergence, warm start, the solve's setup;
+// loop: the WHILE node and the statistics; post: the pressure copy and subtract_grad_p), and the
+// loops of many scenes' solves as one WHILE node of batched work-list kernels.
+int append_poisson_pre(GraphCursor& gc, float* const* u, float* p_io, const pfm_solve_opts& opts);
+int append_poisson_loop(GraphCursor& gc, const pfm_solve_opts& opts, float* p_io, StepCtl* ctl, int which);
+int append_poisson_post(GraphCursor& gc, float* const* u, float* p_io);
+int append_batched_loop(GraphCursor& gc, pfm_handle* const* hs, int n, const pfm_solve_opts& opts,
+                        StepCtl* const* ctls, int which);
+int append_poisson_finish(GraphCursor& gc, const pfm_solve_opts& opts, float* p_io, StepCtl* ctl, int which);
 int launch_midpoint(pfm_handle* h, const float* const* u0, float* const* u1, float dt_half, const float* dt_half_dev,
                     cudaStream_t st);
 int max_speed_async(pfm_handle* h, const float* ux, const float* uy, const float* uz, float* out, cudaStream_t st);

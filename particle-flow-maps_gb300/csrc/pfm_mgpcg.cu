@@ -13,7 +13,10 @@
 #include <cuda_fp16.h>
 
 #include <cmath>
+#include <algorithm>
+#include <atomic>
 #include <type_traits>
+#include <vector>
 
 #include "pfm_internal.cuh"
 #include "pfm_tma.cuh"
@@ -93,9 +96,10 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// Sums `v` over the grid.  Returns true in the last block to finish, where *total holds the
-// grid sum (combined in block order).  Fixed partition => bitwise reproducible.
-__device__ bool grid_sum(double v, double* partials, unsigned* ticket, double* total) {
+// Sums `v` over the `nb` blocks of a fixed partition (this block is `bid`).  Returns true in the
+// last block to finish, where *total holds the sum (combined in block order): bitwise
+// reproducible.  A batched launch passes each scene's own partition (bid, nb) of its work items.
+__device__ bool grid_sum(double v, double* partials, unsigned* ticket, double* total, unsigned bid, unsigned nb) {
   __shared__ double ws[32];
   __shared__ bool last;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -106,17 +110,17 @@ __device__ bool grid_sum(double v, double* partials, unsigned* ticket, double* t
     double b = lane < (int)(blockDim.x >> 5) ? ws[lane] : 0.0;
     b = warp_sum(b);
     if (lane == 0) {
-      partials[blockIdx.x] = b;
+      partials[bid] = b;
       __threadfence();
       unsigned t = atomicAdd(ticket, 1u);
-      last = (t == gridDim.x - 1);
+      last = (t == nb - 1);
     }
   }
   __syncthreads();
   if (!last) return false;
   __threadfence();
   double s = 0.0;
-  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s += ((volatile double*)partials)[b];
+  for (int b = threadIdx.x; b < (int)nb; b += blockDim.x) s += ((volatile double*)partials)[b];
   s = warp_sum(s);
   if (lane == 0) ws[wid] = s;
   __syncthreads();
@@ -211,16 +215,20 @@ __global__ void __launch_bounds__(256) k_subtract_grad_p(float* __restrict__ u, 
 // multigrid V-cycle kernels (3D/mgpcg.py:152-200)
 // ---------------------------------------------------------------------------------------------
 
+// Every kernel of the solver iteration is an operation struct whose run(bid, nb) does the work of
+// block `bid` of an `nb`-block launch; the kernel is run(blockIdx.x, gridDim.x), and a batched
+// launch (k_worklist) runs the blocks of many scenes' operations from one work list.
+
 // smooth(l, phase): z = (r + nbsum(z)) / mult on cells with (i+j+k)&1 == phase.  One thread per
 // pair of cells along the last axis; the thread updates the member of the right colour.
 template <int D, typename S>
-__global__ void __launch_bounds__(256) k_smooth(S* __restrict__ z, const S* __restrict__ r, Lvl L,
-                                                BC bc, int phase, const SolveState* st) {
+__device__ __forceinline__ void smooth_blk(S* __restrict__ z, const S* __restrict__ r, const Lvl& L, const BC& bc,
+                                           int phase, const SolveState* st, unsigned bid) {
   if (st && st->done) return;
   const int nl = (D == 3) ? L.n2 : L.n1;
   const int half = (nl + 1) >> 1;
   const int64_t npairs = (D == 3) ? (int64_t)L.n0 * L.n1 * half : (int64_t)L.n0 * half;
-  const unsigned e = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned e = bid * blockDim.x + threadIdx.x;
   if (e >= (unsigned)npairs) return;
   int i, j, k;
   const unsigned t = udiv(e, L.dh);
@@ -241,6 +249,23 @@ __global__ void __launch_bounds__(256) k_smooth(S* __restrict__ z, const S* __re
   float nb, mult;
   stencil<D>(z, L, bc, i, j, k, c, nb, mult);
   stv(z + c, (ldv(r + c) + nb) / mult);
+}
+
+template <int D, typename S>
+struct OpSmooth {
+  S* z;
+  const S* r;
+  Lvl L;
+  BC bc;
+  int phase;
+  const SolveState* st;
+  __device__ __forceinline__ void run(unsigned bid, unsigned) const { smooth_blk<D, S>(z, r, L, bc, phase, st, bid); }
+};
+
+template <int D, typename S>
+__global__ void __launch_bounds__(256) k_smooth(S* __restrict__ z, const S* __restrict__ r, Lvl L,
+                                                BC bc, int phase, const SolveState* st) {
+  smooth_blk<D, S>(z, r, L, bc, phase, st, blockIdx.x);
 }
 
 // Eight consecutive values along the last axis (n2 % 8 == 0, so a run is 16- or 32-byte aligned).
@@ -277,11 +302,11 @@ __device__ __forceinline__ void st8(__nv_bfloat16* p, const float (&v)[8]) { st8
 // half-sweep never changes, are written back unchanged) and each cell of the colour is updated
 // with the same sum, in the same order, as stencil<3> -- bitwise the result of k_smooth.
 template <typename S>
-__global__ void __launch_bounds__(256) k_smooth8(S* __restrict__ z, const S* __restrict__ r, Lvl L, BC bc,
-                                                 int phase, const SolveState* st) {
+__device__ __forceinline__ void smooth8_blk(S* __restrict__ z, const S* __restrict__ r, const Lvl& L, const BC& bc,
+                                            int phase, const SolveState* st, unsigned bid) {
   if (st && st->done) return;
   const int runs = L.n2 >> 3;
-  const unsigned e = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned e = bid * blockDim.x + threadIdx.x;
   if ((int64_t)e >= (int64_t)L.n0 * L.n1 * runs) return;
   const unsigned row = e / (unsigned)runs;
   const int k0 = (int)(e - row * (unsigned)runs) * 8;
@@ -325,6 +350,23 @@ __global__ void __launch_bounds__(256) k_smooth8(S* __restrict__ z, const S* __r
     out[q] = (rr[q] + ret) / num;
   }
   st8(z + c0, out);
+}
+
+template <typename S>
+struct OpSmooth8 {
+  S* z;
+  const S* r;
+  Lvl L;
+  BC bc;
+  int phase;
+  const SolveState* st;
+  __device__ __forceinline__ void run(unsigned bid, unsigned) const { smooth8_blk<S>(z, r, L, bc, phase, st, bid); }
+};
+
+template <typename S>
+__global__ void __launch_bounds__(256) k_smooth8(S* __restrict__ z, const S* __restrict__ r, Lvl L, BC bc,
+                                                 int phase, const SolveState* st) {
+  smooth8_blk<S>(z, r, L, bc, phase, st, blockIdx.x);
 }
 
 // smooth(l, phase) in 3D for 16-bit level storage with the tile staged by the TMA: a block owns
@@ -421,11 +463,11 @@ __global__ void __launch_bounds__(256) k_smooth_tma(const __grid_constant__ CUte
 // restrict(l) as a gather: rc[I] = sum over children (fine-index order) of res/(dim-1),
 // res = r - (mult z - nbsum(z)).
 template <int D, typename S>
-__global__ void __launch_bounds__(256) k_restrict(const S* __restrict__ zf, const S* __restrict__ rf,
-                                                  Lvl Lf, S* __restrict__ rc, Lvl Lc, BC bc,
-                                                  const SolveState* st) {
+__device__ __forceinline__ void restrict_blk(const S* __restrict__ zf, const S* __restrict__ rf, const Lvl& Lf,
+                                             S* __restrict__ rc, const Lvl& Lc, const BC& bc, const SolveState* st,
+                                             unsigned bid) {
   if (st && st->done) return;
-  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t e = (int64_t)bid * blockDim.x + threadIdx.x;
   if (e >= Lc.count) return;
   int I, J, K;
   decode(Lc, e, I, J, K);
@@ -448,18 +490,53 @@ __global__ void __launch_bounds__(256) k_restrict(const S* __restrict__ zf, cons
   stv(rc + e, acc);
 }
 
+template <int D, typename S>
+struct OpRestrict {
+  const S* zf;
+  const S* rf;
+  Lvl Lf;
+  S* rc;
+  Lvl Lc;
+  BC bc;
+  const SolveState* st;
+  __device__ __forceinline__ void run(unsigned bid, unsigned) const { restrict_blk<D, S>(zf, rf, Lf, rc, Lc, bc, st, bid); }
+};
+
+template <int D, typename S>
+__global__ void __launch_bounds__(256) k_restrict(const S* __restrict__ zf, const S* __restrict__ rf,
+                                                  Lvl Lf, S* __restrict__ rc, Lvl Lc, BC bc,
+                                                  const SolveState* st) {
+  restrict_blk<D, S>(zf, rf, Lf, rc, Lc, bc, st, blockIdx.x);
+}
+
 // prolongate(l): z_l[I] += z_{l+1}[I//2]
 template <int D, typename S>
-__global__ void __launch_bounds__(256) k_prolong(S* __restrict__ zf, Lvl Lf, const S* __restrict__ zc,
-                                                 Lvl Lc, const SolveState* st) {
+__device__ __forceinline__ void prolong_blk(S* __restrict__ zf, const Lvl& Lf, const S* __restrict__ zc,
+                                            const Lvl& Lc, const SolveState* st, unsigned bid) {
   if (st && st->done) return;
-  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t e = (int64_t)bid * blockDim.x + threadIdx.x;
   if (e >= Lf.count) return;
   int i, j, k;
   decode(Lf, e, i, j, k);
   int64_t ce = (D == 3) ? ((int64_t)(i >> 1) * Lc.n1 + (j >> 1)) * Lc.n2 + (k >> 1)
                         : (int64_t)(i >> 1) * Lc.n1 + (j >> 1);
   stv(zf + e, ldv(zf + e) + ldv(zc + ce));
+}
+
+template <int D, typename S>
+struct OpProlong {
+  S* zf;
+  Lvl Lf;
+  const S* zc;
+  Lvl Lc;
+  const SolveState* st;
+  __device__ __forceinline__ void run(unsigned bid, unsigned) const { prolong_blk<D, S>(zf, Lf, zc, Lc, st, bid); }
+};
+
+template <int D, typename S>
+__global__ void __launch_bounds__(256) k_prolong(S* __restrict__ zf, Lvl Lf, const S* __restrict__ zc,
+                                                 Lvl Lc, const SolveState* st) {
+  prolong_blk<D, S>(zf, Lf, zc, Lc, st, blockIdx.x);
 }
 
 // init(r, k) (3D/mgpcg.py:71-79): r0 = r * k
@@ -470,10 +547,22 @@ __global__ void __launch_bounds__(256) k_scale(float* __restrict__ out, const fl
 }
 
 template <typename S>
-__global__ void __launch_bounds__(256) k_zero(S* __restrict__ a, int64_t n, const SolveState* st) {
+__device__ __forceinline__ void zero_blk(S* __restrict__ a, int64_t n, const SolveState* st, unsigned bid, unsigned nb) {
   if (st && st->done) return;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
-    stv(a + e, 0.f);
+  for (int64_t e = (int64_t)bid * blockDim.x + threadIdx.x; e < n; e += (int64_t)nb * blockDim.x) stv(a + e, 0.f);
+}
+
+template <typename S>
+struct OpZero {
+  S* a;
+  int64_t n;
+  const SolveState* st;
+  __device__ __forceinline__ void run(unsigned bid, unsigned nb) const { zero_blk<S>(a, n, st, bid, nb); }
+};
+
+template <typename S>
+__global__ void __launch_bounds__(256) k_zero(S* __restrict__ a, int64_t n, const SolveState* st) {
+  zero_blk<S>(a, n, st, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -505,9 +594,9 @@ __device__ __forceinline__ bool converged(double rTr, const SolveState* st, doub
 // sum(a*b) (or sum(a) for RED_MEAN) with a finalizer that updates the solve state.  Per-thread
 // partials accumulate in f32 (the reference solve) or f64 (f64 != 0, the mixed solve).
 template <typename SA>
-__global__ void __launch_bounds__(kReduceThreads) k_dot(const SA* __restrict__ a, const float* __restrict__ b,
-                                                        int64_t n, RedBuf rb, int kind, double eps, double inv_n,
-                                                        int max_iters, int f64) {
+__device__ __forceinline__ void dot_blk(const SA* __restrict__ a, const float* __restrict__ b, int64_t n, RedBuf rb,
+                                        int kind, double eps, double inv_n, int max_iters, int f64, unsigned bid,
+                                        unsigned nb) {
   SolveState* st = rb.st;
   if (st->done) return;
   double total;
@@ -515,14 +604,14 @@ __global__ void __launch_bounds__(kReduceThreads) k_dot(const SA* __restrict__ a
     // a 16-bit level vector (z) holds the scaled values: undo the scale of the residual it answers
     const double us = (sizeof(SA) == 2) ? 1.0 / (double)st->hscale : 1.0;
     CompSum acc;
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    for (int64_t e = (int64_t)bid * blockDim.x + threadIdx.x; e < n; e += (int64_t)nb * blockDim.x)
       acc.add((kind == RED_MEAN) ? ldv(a + e) : ldv(a + e) * b[e]);
-    if (!grid_sum(acc.value() * us, rb.partials, &st->ticket, &total)) return;
+    if (!grid_sum(acc.value() * us, rb.partials, &st->ticket, &total, bid, nb)) return;
   } else {
     float acc = 0.f;
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    for (int64_t e = (int64_t)bid * blockDim.x + threadIdx.x; e < n; e += (int64_t)nb * blockDim.x)
       acc += (kind == RED_MEAN) ? ldv(a + e) : ldv(a + e) * b[e];
-    if (!grid_sum((double)acc, rb.partials, &st->ticket, &total)) return;
+    if (!grid_sum((double)acc, rb.partials, &st->ticket, &total, bid, nb)) return;
   }
   if (threadIdx.x != 0) return;
   if (kind == RED_ZTR_INIT) {
@@ -551,69 +640,137 @@ __global__ void __launch_bounds__(kReduceThreads) k_dot(const SA* __restrict__ a
   }
 }
 
+template <typename SA>
+struct OpDot {
+  const SA* a;
+  const float* b;
+  int64_t n;
+  RedBuf rb;
+  int kind;
+  double eps, inv_n;
+  int max_iters, f64;
+  __device__ __forceinline__ void run(unsigned bid, unsigned nb) const {
+    dot_blk<SA>(a, b, n, rb, kind, eps, inv_n, max_iters, f64, bid, nb);
+  }
+};
+
+template <typename SA>
+__global__ void __launch_bounds__(kReduceThreads) k_dot(const SA* __restrict__ a, const float* __restrict__ b,
+                                                        int64_t n, RedBuf rb, int kind, double eps, double inv_n,
+                                                        int max_iters, int f64) {
+  dot_blk<SA>(a, b, n, rb, kind, eps, inv_n, max_iters, f64, blockIdx.x, gridDim.x);
+}
+
 // recenter (3D/mgpcg.py:174-180): r -= mean; with rh, also the level-storage copy of r that the
 // mixed-precision V-cycle smooths against
 template <typename S>
-__global__ void __launch_bounds__(256) k_sub_mean(float* __restrict__ r, S* __restrict__ rh, int64_t n,
-                                                  const SolveState* st) {
+__device__ __forceinline__ void sub_mean_blk(float* __restrict__ r, S* __restrict__ rh, int64_t n,
+                                             const SolveState* st, unsigned bid, unsigned nb) {
   if (st->done) return;
   const float m = st->mean;
   const float hs = (sizeof(S) == 2) ? st->hscale : 1.f;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t e = (int64_t)bid * blockDim.x + threadIdx.x; e < n; e += (int64_t)nb * blockDim.x) {
     const float v = r[e] - m;
     r[e] = v;
     if (rh) stv(rh + e, v * hs);
   }
 }
 
+template <typename S>
+struct OpSubMean {
+  float* r;
+  S* rh;
+  int64_t n;
+  const SolveState* st;
+  __device__ __forceinline__ void run(unsigned bid, unsigned nb) const { sub_mean_blk<S>(r, rh, n, st, bid, nb); }
+};
+
+template <typename S>
+__global__ void __launch_bounds__(256) k_sub_mean(float* __restrict__ r, S* __restrict__ rh, int64_t n,
+                                                  const SolveState* st) {
+  sub_mean_blk<S>(r, rh, n, st, blockIdx.x, gridDim.x);
+}
+
 // the level-storage copy of r (mixed solve without recentring)
+template <typename S>
+__device__ __forceinline__ void to_storage_blk(S* __restrict__ out, const float* __restrict__ in, int64_t n,
+                                               const SolveState* st, unsigned bid, unsigned nb) {
+  if (st->done) return;
+  const float hs = (sizeof(S) == 2) ? st->hscale : 1.f;
+  for (int64_t e = (int64_t)bid * blockDim.x + threadIdx.x; e < n; e += (int64_t)nb * blockDim.x)
+    stv(out + e, in[e] * hs);
+}
+
+template <typename S>
+struct OpToStorage {
+  S* out;
+  const float* in;
+  int64_t n;
+  const SolveState* st;
+  __device__ __forceinline__ void run(unsigned bid, unsigned nb) const { to_storage_blk<S>(out, in, n, st, bid, nb); }
+};
+
 template <typename S>
 __global__ void __launch_bounds__(256) k_to_storage(S* __restrict__ out, const float* __restrict__ in, int64_t n,
                                                     const SolveState* st) {
-  if (st->done) return;
-  const float hs = (sizeof(S) == 2) ? st->hscale : 1.f;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
-    stv(out + e, in[e] * hs);
+  to_storage_blk<S>(out, in, n, st, blockIdx.x, gridDim.x);
 }
 
 // compute_Ap + reduce(p, Ap) + alpha = zTr / (pAp + eps)   (3D/mgpcg.py:237-240)
 template <int D>
-__global__ void __launch_bounds__(kReduceThreads) k_Ap_dot(const float* __restrict__ p, float* __restrict__ Ap,
-                                                           Lvl L, BC bc, RedBuf rb, double eps, int f64) {
+__device__ __forceinline__ void Ap_dot_blk(const float* __restrict__ p, float* __restrict__ Ap, const Lvl& L,
+                                           const BC& bc, RedBuf rb, double eps, int f64, unsigned bid, unsigned nb) {
   SolveState* st = rb.st;
   if (st->done) return;
   float acc = 0.f;
   CompSum cacc;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < L.count; e += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t e = (int64_t)bid * blockDim.x + threadIdx.x; e < L.count; e += (int64_t)nb * blockDim.x) {
     int i, j, k;
     decode(L, e, i, j, k);
-    float nb, mult;
-    stencil<D>(p, L, bc, i, j, k, e, nb, mult);
+    float nbs, mult;
+    stencil<D>(p, L, bc, i, j, k, e, nbs, mult);
     float pe = p[e];
-    float ap = mult * pe - nb;
+    float ap = mult * pe - nbs;
     Ap[e] = ap;
     if (f64) cacc.add(pe * ap);
     else acc += pe * ap;
   }
   double total;
-  if (!grid_sum(f64 ? cacc.value() : (double)acc, rb.partials, &st->ticket, &total)) return;
+  if (!grid_sum(f64 ? cacc.value() : (double)acc, rb.partials, &st->ticket, &total, bid, nb)) return;
   if (threadIdx.x == 0) {
     st->pAp = total;
     st->alpha = (float)(st->zTr_old / (total + eps));
   }
 }
 
+template <int D>
+struct OpApDot {
+  const float* p;
+  float* Ap;
+  Lvl L;
+  BC bc;
+  RedBuf rb;
+  double eps;
+  int f64;
+  __device__ __forceinline__ void run(unsigned bid, unsigned nb) const { Ap_dot_blk<D>(p, Ap, L, bc, rb, eps, f64, bid, nb); }
+};
+
+template <int D>
+__global__ void __launch_bounds__(kReduceThreads) k_Ap_dot(const float* __restrict__ p, float* __restrict__ Ap,
+                                                           Lvl L, BC bc, RedBuf rb, double eps, int f64) {
+  Ap_dot_blk<D>(p, Ap, L, bc, rb, eps, f64, blockIdx.x, gridDim.x);
+}
+
 // update_x, update_r, reduce(r, r) and the convergence test (3D/mgpcg.py:243-258).
-__global__ void __launch_bounds__(kReduceThreads) k_update_xr(float* __restrict__ x, const float* __restrict__ p,
-                                                              float* __restrict__ r, const float* __restrict__ Ap,
-                                                              int64_t n, RedBuf rb, double tol, int tol_mode,
-                                                              int f64, double inv_n) {
+__device__ __forceinline__ void update_xr_blk(float* __restrict__ x, const float* __restrict__ p, float* __restrict__ r,
+                                              const float* __restrict__ Ap, int64_t n, RedBuf rb, double tol,
+                                              int tol_mode, int f64, double inv_n, unsigned bid, unsigned nb) {
   SolveState* st = rb.st;
   if (st->done) return;
   const float alpha = st->alpha;
   float acc = 0.f;
   CompSum cacc;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t e = (int64_t)bid * blockDim.x + threadIdx.x; e < n; e += (int64_t)nb * blockDim.x) {
     x[e] += alpha * p[e];
     float re = r[e] - alpha * Ap[e];
     r[e] = re;
@@ -621,7 +778,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_update_xr(float* __restrict_
     else acc += re * re;
   }
   double total;
-  if (!grid_sum(f64 ? cacc.value() : (double)acc, rb.partials, &st->ticket, &total)) return;
+  if (!grid_sum(f64 ? cacc.value() : (double)acc, rb.partials, &st->ticket, &total, bid, nb)) return;
   if (threadIdx.x == 0) {
     st->rTr = total;
     if (total > 0.0) st->hscale = (float)(1.0 / sqrt(total * inv_n));
@@ -633,6 +790,28 @@ __global__ void __launch_bounds__(kReduceThreads) k_update_xr(float* __restrict_
       st->conv_it = st->it;
     }
   }
+}
+
+struct OpUpdateXr {
+  float* x;
+  const float* p;
+  float* r;
+  const float* Ap;
+  int64_t n;
+  RedBuf rb;
+  double tol;
+  int tol_mode, f64;
+  double inv_n;
+  __device__ __forceinline__ void run(unsigned bid, unsigned nb) const {
+    update_xr_blk(x, p, r, Ap, n, rb, tol, tol_mode, f64, inv_n, bid, nb);
+  }
+};
+
+__global__ void __launch_bounds__(kReduceThreads) k_update_xr(float* __restrict__ x, const float* __restrict__ p,
+                                                              float* __restrict__ r, const float* __restrict__ Ap,
+                                                              int64_t n, RedBuf rb, double tol, int tol_mode,
+                                                              int f64, double inv_n) {
+  update_xr_blk(x, p, r, Ap, n, rb, tol, tol_mode, f64, inv_n, blockIdx.x, gridDim.x);
 }
 
 // r = b - A x: the initial residual of a warm-started solve
@@ -654,39 +833,74 @@ __global__ void __launch_bounds__(256) k_residual(float* __restrict__ r, const f
 // relative at 64^3 for a smooth pressure, more at 256^3) below the reference's recursive 1e-6
 // rule, so replacing the recursive residual by it would hold every solve above its tolerance.
 template <int D>
-__global__ void __launch_bounds__(kReduceThreads) k_true_residual(const float* __restrict__ b,
-                                                                  const float* __restrict__ x, Lvl L, BC bc,
-                                                                  RedBuf rb, int every) {
+__device__ __forceinline__ void true_residual_blk(const float* __restrict__ b, const float* __restrict__ x,
+                                                  const Lvl& L, const BC& bc, RedBuf rb, int every, unsigned bid,
+                                                  unsigned nb) {
   SolveState* st = rb.st;
   if (every > 0 && (st->done != 0 || (st->it + 1) % every != 0)) return;
   CompSum acc;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < L.count; e += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t e = (int64_t)bid * blockDim.x + threadIdx.x; e < L.count; e += (int64_t)nb * blockDim.x) {
     int i, j, k;
     decode(L, e, i, j, k);
-    float nb, mult;
-    stencil<D>(x, L, bc, i, j, k, e, nb, mult);
-    const float re = b[e] - (mult * x[e] - nb);
+    float nbs, mult;
+    stencil<D>(x, L, bc, i, j, k, e, nbs, mult);
+    const float re = b[e] - (mult * x[e] - nbs);
     acc.add(re * re);
   }
   double total;
-  if (!grid_sum(acc.value(), rb.partials, &st->ticket, &total)) return;
+  if (!grid_sum(acc.value(), rb.partials, &st->ticket, &total, bid, nb)) return;
   if (threadIdx.x == 0) st->rTr_true = total;
+}
+
+template <int D>
+struct OpTrueResidual {
+  const float* b;
+  const float* x;
+  Lvl L;
+  BC bc;
+  RedBuf rb;
+  int every;
+  __device__ __forceinline__ void run(unsigned bid, unsigned nb) const {
+    true_residual_blk<D>(b, x, L, bc, rb, every, bid, nb);
+  }
+};
+
+template <int D>
+__global__ void __launch_bounds__(kReduceThreads) k_true_residual(const float* __restrict__ b,
+                                                                  const float* __restrict__ x, Lvl L, BC bc,
+                                                                  RedBuf rb, int every) {
+  true_residual_blk<D>(b, x, L, bc, rb, every, blockIdx.x, gridDim.x);
 }
 
 // update_p: p = z + beta p (3D/mgpcg.py:147-150)
 template <typename SZ>
-__global__ void __launch_bounds__(256) k_update_p(float* __restrict__ p, const SZ* __restrict__ z, int64_t n,
-                                                  const SolveState* st) {
+__device__ __forceinline__ void update_p_blk(float* __restrict__ p, const SZ* __restrict__ z, int64_t n,
+                                             const SolveState* st, unsigned bid, unsigned nb) {
   if (st->done) return;
   const float beta = st->beta;
   if (sizeof(SZ) == 2) {  // z answers the scaled residual
     const float us = 1.f / st->hscale;
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    for (int64_t e = (int64_t)bid * blockDim.x + threadIdx.x; e < n; e += (int64_t)nb * blockDim.x)
       p[e] = ldv(z + e) * us + beta * p[e];
   } else {
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    for (int64_t e = (int64_t)bid * blockDim.x + threadIdx.x; e < n; e += (int64_t)nb * blockDim.x)
       p[e] = ldv(z + e) + beta * p[e];
   }
+}
+
+template <typename SZ>
+struct OpUpdateP {
+  float* p;
+  const SZ* z;
+  int64_t n;
+  const SolveState* st;
+  __device__ __forceinline__ void run(unsigned bid, unsigned nb) const { update_p_blk<SZ>(p, z, n, st, bid, nb); }
+};
+
+template <typename SZ>
+__global__ void __launch_bounds__(256) k_update_p(float* __restrict__ p, const SZ* __restrict__ z, int64_t n,
+                                                  const SolveState* st) {
+  update_p_blk<SZ>(p, z, n, st, blockIdx.x, gridDim.x);
 }
 
 // Device loop control.  The loop body is the second half of iteration k (recenter, V-cycle, beta,
@@ -793,9 +1007,8 @@ __device__ void tail_sweeps(float* z, const float* r, const Lvl& L, const BC& bc
 }
 
 template <int D, typename S>
-__global__ void __launch_bounds__(kTailThreads) k_vcycle_tail(S* __restrict__ zg, const S* __restrict__ rg,
-                                                              TailPlan T, BC bc, int pre_post, int bottom,
-                                                              const SolveState* st) {
+__device__ __forceinline__ void tail_blk(S* __restrict__ zg, const S* __restrict__ rg, const TailPlan& T, const BC& bc,
+                                         int pre_post, int bottom, const SolveState* st) {
   if (st && st->done) return;
   extern __shared__ float sh[];
   float* Z = sh;
@@ -855,6 +1068,44 @@ __global__ void __launch_bounds__(kTailThreads) k_vcycle_tail(S* __restrict__ zg
   }
   for (int e = threadIdx.x; e < (int)T.lv[l0].count; e += blockDim.x) stv(zg + e, Z[T.off[l0] + e]);
 }
+
+template <int D, typename S>
+__global__ void __launch_bounds__(kTailThreads) k_vcycle_tail(S* __restrict__ zg, const S* __restrict__ rg,
+                                                              TailPlan T, BC bc, int pre_post, int bottom,
+                                                              const SolveState* st) {
+  tail_blk<D, S>(zg, rg, T, bc, pre_post, bottom, st);
+}
+
+// The tail of one scene in a batched launch (one work item): the level extents travel in the work
+// list and the block rebuilds the TailPlan (levels, divisors, offsets) in shared memory.
+template <int D, typename S>
+struct OpTail {
+  S* zg;
+  const S* rg;
+  int l0, L;
+  int n[kMaxLevels][3];
+  BC bc;
+  int pre_post, bottom;
+  const SolveState* st;
+  __device__ __forceinline__ void run(unsigned, unsigned) const {
+    __shared__ TailPlan T;
+    if (threadIdx.x == 0) {
+      T.l0 = l0;
+      T.L = L;
+      int off = 0;
+      for (int l = l0; l < L; ++l) {
+        const int last = (D == 3) ? n[l][2] : n[l][1];
+        T.lv[l] = Lvl{n[l][0], n[l][1], n[l][2], (int64_t)n[l][0] * n[l][1] * n[l][2], make_div32((unsigned)n[l][1]),
+                      make_div32((unsigned)n[l][2]), make_div32((unsigned)((last + 1) >> 1))};
+        T.off[l] = off;
+        off += n[l][0] * n[l][1] * n[l][2];
+      }
+      T.total = off;
+    }
+    __syncthreads();
+    tail_blk<D, S>(zg, rg, T, bc, pre_post, bottom, st);
+  }
+};
 
 // ---------------------------------------------------------------------------------------------
 // host orchestration
@@ -1309,17 +1560,30 @@ __global__ void k_record_solve(StepCtl* ctl, const SolveState* st, int which, in
 template <int D, typename S>
 static void append_solve(GraphCursor& gc, const pfm_solve_opts& o, StepCtl* ctl, int which) {
   SolveKernels<D, S> K(gc.h, o);
-  K.setup(gc.seg());
   const int body = append_solve_loop(gc, K);
   if (gc.rc) return;
   launch(gc.h, k_record_solve, 1, 1, 0, gc.seg(), ctl, (const SolveState*)K.st, which, body);
 }
 
-// MGPCG_3/MGPCG_2.Poisson appended to a whole-step graph: apply_bc, divergence, [warm start from
-// p_io], the solve's setup, its device loop, [pressure to p_io], subtract_grad_p with the wall
-// reset.  Nothing waits on the host; the statistics go to ctl (slot `which`).
-int append_poisson(GraphCursor& gc, float* const* u, float* p_io, const pfm_solve_opts& opts, StepCtl* ctl,
-                   int which) {
+template <class F>
+static void dispatch_solve(int D, int precision, F&& f) {
+  if (D == 3) {
+    if (precision == 1) f(std::integral_constant<int, 3>(), __half());
+    else if (precision == 2) f(std::integral_constant<int, 3>(), __nv_bfloat16());
+    else f(std::integral_constant<int, 3>(), float());
+  } else {
+    if (precision == 1) f(std::integral_constant<int, 2>(), __half());
+    else if (precision == 2) f(std::integral_constant<int, 2>(), __nv_bfloat16());
+    else f(std::integral_constant<int, 2>(), float());
+  }
+}
+
+// MGPCG_3/MGPCG_2.Poisson appended to a whole-step graph in three parts -- pre: apply_bc,
+// divergence, [warm start from p_io], the solve's setup; loop: the device iteration loop and the
+// statistics to ctl (slot `which`); post: [pressure to p_io], subtract_grad_p with the wall reset.
+// Nothing waits on the host.  A batch in work-list mode emits every scene's pre and post parts in
+// the scene's own branch and one batched loop for all of them (append_batched_loop).
+int append_poisson_pre(GraphCursor& gc, float* const* u, float* p_io, const pfm_solve_opts& opts) {
   pfm_handle* h = gc.h;
   const int D = h->cfg.dim;
   const MacGeom& g = h->geom;
@@ -1344,17 +1608,28 @@ int append_poisson(GraphCursor& gc, float* const* u, float* p_io, const pfm_solv
     launch(h, k_divergence<2>, grid_for(h->cells, 256), 256, 0, q, u[0], u[1], (const float*)nullptr, lvl_of(h, 0), r0,
            -1.f);
   if (o.warm_start) cudaMemcpyAsync(x, p_io, h->cells * 4, cudaMemcpyDeviceToDevice, q);
-  if (D == 3) {
-    if (o.precision == 1) append_solve<3, __half>(gc, o, ctl, which);
-    else if (o.precision == 2) append_solve<3, __nv_bfloat16>(gc, o, ctl, which);
-    else append_solve<3, float>(gc, o, ctl, which);
-  } else {
-    if (o.precision == 1) append_solve<2, __half>(gc, o, ctl, which);
-    else if (o.precision == 2) append_solve<2, __nv_bfloat16>(gc, o, ctl, which);
-    else append_solve<2, float>(gc, o, ctl, which);
-  }
+  dispatch_solve(D, o.precision, [&](auto dd, auto ss) {
+    SolveKernels<decltype(dd)::value, decltype(ss)> K(h, o);
+    K.setup(gc.seg());
+  });
+  return gc.rc;
+}
+
+int append_poisson_loop(GraphCursor& gc, const pfm_solve_opts& opts, float* p_io, StepCtl* ctl, int which) {
+  pfm_solve_opts o = opts;
+  if (!p_io) o.warm_start = 0;
+  dispatch_solve(gc.h->cfg.dim, o.precision,
+                 [&](auto dd, auto ss) { append_solve<decltype(dd)::value, decltype(ss)>(gc, o, ctl, which); });
+  return gc.rc;
+}
+
+int append_poisson_post(GraphCursor& gc, float* const* u, float* p_io) {
+  pfm_handle* h = gc.h;
   if (gc.rc) return gc.rc;
-  q = gc.seg();
+  const int D = h->cfg.dim;
+  const MacGeom& g = h->geom;
+  float* x = ws_ptr<float>(h, h->o_x);
+  cudaStream_t q = gc.seg();
   if (p_io) cudaMemcpyAsync(p_io, x, h->cells * 4, cudaMemcpyDeviceToDevice, q);
   for (int f = 0; f < D; ++f) {
     const int64_t nf = (int64_t)g.n[f][0] * g.n[f][1] * g.n[f][2];
@@ -1365,6 +1640,332 @@ int append_poisson(GraphCursor& gc, float* const* u, float* p_io, const pfm_solv
     if (D == 2 && f == 0) launch(h, k_subtract_grad_p<2, 0>, grid_for(nf, 256), 256, 0, q, u[f], (const float*)x, g, lo, hi);
     if (D == 2 && f == 1) launch(h, k_subtract_grad_p<2, 1>, grid_for(nf, 256), 256, 0, q, u[f], (const float*)x, g, lo, hi);
   }
+  return gc.rc;
+}
+
+int append_poisson(GraphCursor& gc, float* const* u, float* p_io, const pfm_solve_opts& opts, StepCtl* ctl,
+                   int which) {
+  append_poisson_pre(gc, u, p_io, opts);
+  if (gc.rc) return gc.rc;
+  append_poisson_loop(gc, opts, p_io, ctl, which);
+  if (gc.rc) return gc.rc;
+  return append_poisson_post(gc, u, p_io);
+}
+
+// ---------------------------------------------------------------------------------------------
+// batched MGPCG iterations: persistent kernels over a work list of (scene, block) items
+// ---------------------------------------------------------------------------------------------
+// A work list: scene s owns items [prefix[s], prefix[s+1]), item w of it is block w - prefix[s] of
+// the scene's own launch of the operation (the same partition as the scene's standalone kernel,
+// so its reductions combine the same partials in the same order: bitwise the standalone result).
+// The list travels as the kernel's parameter (no device allocation): at most kBatchMax scenes per
+// launch.
+constexpr int kBatchMax = 64;
+
+template <class Op>
+struct WorkList {
+  int n;
+  int prefix[kBatchMax + 1];
+  Op op[kBatchMax];
+};
+
+// A grid sized for the GPU's resident blocks walks the list; a scene whose solve has finished
+// costs one read of its done flag per item (every operation starts with that test).
+template <class Op, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_worklist(const __grid_constant__ WorkList<Op> wl) {
+  const int total = wl.prefix[wl.n];
+  for (int w = blockIdx.x; w < total; w += gridDim.x) {
+    int lo = 0, hi = wl.n - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (wl.prefix[mid] <= w) lo = mid;
+      else hi = mid - 1;
+    }
+    wl.op[lo].run((unsigned)(w - wl.prefix[lo]), (unsigned)(wl.prefix[lo + 1] - wl.prefix[lo]));
+    __syncthreads();
+  }
+}
+
+template <class Op>
+struct WorkItems {
+  std::vector<Op> ops;
+  std::vector<unsigned> blocks;
+  void add(const Op& op, unsigned nb) {
+    if (nb == 0) return;
+    ops.push_back(op);
+    blocks.push_back(nb);
+  }
+};
+
+template <class Op, int THREADS>
+static void launch_worklist(pfm_handle* h, cudaStream_t q, const WorkItems<Op>& it, size_t smem = 0) {
+  constexpr unsigned kResident = 152u * (2048u / THREADS);  // resident blocks of the 152 SMs
+  for (size_t c0 = 0; c0 < it.ops.size(); c0 += kBatchMax) {
+    WorkList<Op> wl{};
+    wl.n = (int)std::min<size_t>(kBatchMax, it.ops.size() - c0);
+    int tot = 0;
+    for (int i = 0; i < wl.n; ++i) {
+      wl.prefix[i] = tot;
+      wl.op[i] = it.ops[c0 + i];
+      tot += (int)it.blocks[c0 + i];
+    }
+    wl.prefix[wl.n] = tot;
+    if (tot == 0) continue;
+    launch(h, k_worklist<Op, THREADS>, std::min((unsigned)tot, kResident), THREADS, smem, q, wl);
+  }
+}
+
+// Loop control over every scene of the batch: the WHILE condition holds while any scene's solve
+// is running (not done, under its iteration limit); the batched body's kernels are counted on the
+// first scene's step state.
+constexpr int kBatchScenes = 2 * kBatchMax;
+
+struct LoopAll {
+  int n;
+  SolveState* st[kBatchScenes];
+};
+
+__global__ void k_loop_begin_all(LoopAll la, int chunk, cudaGraphConditionalHandle cond) {
+  unsigned any = 0;
+  for (int s = 0; s < la.n; ++s) {
+    SolveState* st = la.st[s];
+    st->it_stop = st->it + chunk;
+    if (st->done == 0 && chunk > 0) any = 1;
+  }
+  cudaGraphSetConditional(cond, any);
+}
+
+__global__ void k_loop_cond_all(LoopAll la, cudaGraphConditionalHandle cond, StepCtl* ctl0,
+                                unsigned long long body_nodes) {
+  unsigned any = 0;
+  for (int s = 0; s < la.n; ++s) {
+    const SolveState* st = la.st[s];
+    if (st->done == 0 && st->it < st->it_stop) any = 1;
+  }
+  cudaGraphSetConditional(cond, any);
+  if (ctl0) ctl0->kernels += body_nodes;
+}
+
+// One scene of a batched solve: its kernels' arguments and the shape of its V-cycle.
+template <int D, typename S>
+struct BatchScene {
+  SolveKernels<D, S> K;
+  int L, l0, down_end;
+  BatchScene(pfm_handle* h, const pfm_solve_opts& o) : K(h, o) {
+    L = h->L;
+    l0 = tail_level(h);
+    down_end = l0 < L ? l0 : L - 1;
+  }
+};
+
+// One red-black half-sweep for the scenes `level` picks: level(scene) is the level to smooth, or -1
+// to leave the scene out.  The kernel of each scene is the one smooth_launch picks.
+template <int D, typename S, class Level>
+static void batched_smooth(std::vector<BatchScene<D, S>>& B, cudaStream_t q, int phase, Level level) {
+  WorkItems<OpSmooth<D, S>> wide;
+  WorkItems<OpSmooth8<S>> runs;
+  for (auto& b : B) {
+    const int lv = level(b);
+    if (lv < 0) continue;
+    pfm_handle* h = b.K.h;
+    const Lvl L = lvl_of(h, lv);
+    if (D == 3 && L.n2 % 8 == 0) {
+      const int64_t nvec = (int64_t)L.n0 * L.n1 * (L.n2 / 8);
+      runs.add(OpSmooth8<S>{level_z<S>(h, lv), level_r<S>(h, lv), L, b.K.bc, phase, b.K.st}, grid_for(nvec, 256));
+    } else {
+      const int nl = (D == 3) ? L.n2 : L.n1;
+      const int64_t npairs = (D == 3) ? (int64_t)L.n0 * L.n1 * ((nl + 1) / 2) : (int64_t)L.n0 * ((nl + 1) / 2);
+      wide.add(OpSmooth<D, S>{level_z<S>(h, lv), level_r<S>(h, lv), L, b.K.bc, phase, b.K.st}, grid_for(npairs, 256));
+    }
+  }
+  pfm_handle* h0 = B[0].K.h;
+  launch_worklist<OpSmooth<D, S>, 256>(h0, q, wide);
+  launch_worklist<OpSmooth8<S>, 256>(h0, q, runs);
+}
+
+// apply_preconditioner for every scene of the batch: each scene's kernels in the order of vcycle()
+// (the batched schedule interleaves the scenes level by level; a scene takes part in the steps its
+// own hierarchy has, so its own sequence of updates is unchanged).
+template <int D, typename S>
+static void batched_vcycle(std::vector<BatchScene<D, S>>& B, cudaStream_t q) {
+  pfm_handle* h0 = B[0].K.h;
+  int dmax = 0, pmax = 0, bmax = 0;
+  for (auto& b : B) {
+    dmax = std::max(dmax, b.down_end);
+    pmax = std::max(pmax, b.K.h->cfg.pre_post_smoothing);
+    bmax = std::max(bmax, b.K.h->cfg.bottom_smoothing);
+  }
+  {
+    WorkItems<OpZero<S>> z;
+    for (auto& b : B)
+      z.add(OpZero<S>{level_z<S>(b.K.h, 0), b.K.h->lv[0].count, b.K.st}, stream_blocks(b.K.h->lv[0].count));
+    launch_worklist<OpZero<S>, 256>(h0, q, z);
+  }
+  for (int l = 0; l < dmax; ++l) {
+    for (int i = 0; i < pmax; ++i) {
+      auto pre = [&](const BatchScene<D, S>& b) { return (l < b.down_end && i < b.K.h->cfg.pre_post_smoothing) ? l : -1; };
+      batched_smooth<D, S>(B, q, 0, pre);
+      batched_smooth<D, S>(B, q, 1, pre);
+    }
+    WorkItems<OpZero<S>> z;
+    WorkItems<OpRestrict<D, S>> r;
+    for (auto& b : B) {
+      if (l >= b.down_end) continue;
+      pfm_handle* h = b.K.h;
+      if (l + 1 != b.l0)
+        z.add(OpZero<S>{level_z<S>(h, l + 1), h->lv[l + 1].count, b.K.st}, stream_blocks(h->lv[l + 1].count));
+      const Lvl Lf = lvl_of(h, l), Lc = lvl_of(h, l + 1);
+      r.add(OpRestrict<D, S>{level_z<S>(h, l), level_r<S>(h, l), Lf, level_r<S>(h, l + 1), Lc, b.K.bc, b.K.st},
+            grid_for(Lc.count, 256));
+    }
+    launch_worklist<OpZero<S>, 256>(h0, q, z);
+    launch_worklist<OpRestrict<D, S>, 256>(h0, q, r);
+  }
+  // the coarse levels: one block per scene that has a tail, the bottom sweeps for the others
+  WorkItems<OpTail<D, S>> t;
+  size_t tail_smem_max = 0;
+  for (auto& b : B) {
+    if (b.l0 >= b.L) continue;
+    pfm_handle* h = b.K.h;
+    OpTail<D, S> op{};
+    op.zg = level_z<S>(h, b.l0);
+    op.rg = level_r<S>(h, b.l0);
+    op.l0 = b.l0;
+    op.L = b.L;
+    size_t cells = 0;
+    for (int l = 0; l < b.L; ++l) {
+      for (int a = 0; a < 3; ++a) op.n[l][a] = h->lv[l].n[a];
+      if (l >= b.l0) cells += (size_t)h->lv[l].count;
+    }
+    op.bc = b.K.bc;
+    op.pre_post = h->cfg.pre_post_smoothing;
+    op.bottom = h->cfg.bottom_smoothing;
+    op.st = b.K.st;
+    t.add(op, 1);
+    tail_smem_max = std::max(tail_smem_max, cells * 2 * sizeof(float));
+  }
+  if (!t.ops.empty()) {
+    static std::atomic<unsigned long long> attr{0};  // above the default 48 KB: opt in per device
+    if (tail_smem_max > 48 * 1024) opt_in_smem(k_worklist<OpTail<D, S>, kTailThreads>, 227 * 1024, attr);
+    launch_worklist<OpTail<D, S>, kTailThreads>(h0, q, t, tail_smem_max);
+  }
+  for (int i = 0; i < bmax; ++i) {
+    auto bottom = [&](const BatchScene<D, S>& b) {
+      return (b.l0 >= b.L && i < b.K.h->cfg.bottom_smoothing) ? b.L - 1 : -1;
+    };
+    batched_smooth<D, S>(B, q, 0, bottom);
+    batched_smooth<D, S>(B, q, 1, bottom);
+  }
+  for (int l = dmax - 1; l >= 0; --l) {
+    WorkItems<OpProlong<D, S>> pr;
+    for (auto& b : B) {
+      if (l >= b.down_end) continue;
+      pfm_handle* h = b.K.h;
+      const Lvl Lf = lvl_of(h, l), Lc = lvl_of(h, l + 1);
+      pr.add(OpProlong<D, S>{level_z<S>(h, l), Lf, level_z<S>(h, l + 1), Lc, b.K.st}, grid_for(Lf.count, 256));
+    }
+    launch_worklist<OpProlong<D, S>, 256>(h0, q, pr);
+    for (int i = 0; i < pmax; ++i) {
+      auto post = [&](const BatchScene<D, S>& b) { return (l < b.down_end && i < b.K.h->cfg.pre_post_smoothing) ? l : -1; };
+      batched_smooth<D, S>(B, q, 1, post);
+      batched_smooth<D, S>(B, q, 0, post);
+    }
+  }
+}
+
+// One WHILE iteration for every scene: SolveKernels::body's kernels, each one batched launch.
+template <int D, typename S>
+static void batched_body(std::vector<BatchScene<D, S>>& B, cudaStream_t q) {
+  pfm_handle* h0 = B[0].K.h;
+  {  // recenter with the level-storage copy
+    WorkItems<OpDot<float>> mean;
+    WorkItems<OpSubMean<S>> sub;
+    WorkItems<OpToStorage<S>> sto;
+    for (auto& b : B) {
+      auto& K = b.K;
+      if (K.neu) {
+        mean.add(OpDot<float>{K.r0, nullptr, K.n, K.rb, (int)RED_MEAN, K.o.eps, K.inv_n, K.mi, K.f64}, red_blocks(K.n));
+        sub.add(OpSubMean<S>{K.r0, K.mixed ? K.rh : nullptr, K.n, K.st}, stream_blocks(K.n));
+      } else if (K.mixed) {
+        sto.add(OpToStorage<S>{K.rh, K.r0, K.n, K.st}, stream_blocks(K.n));
+      }
+    }
+    launch_worklist<OpDot<float>, kReduceThreads>(h0, q, mean);
+    launch_worklist<OpSubMean<S>, 256>(h0, q, sub);
+    launch_worklist<OpToStorage<S>, 256>(h0, q, sto);
+  }
+  batched_vcycle<D, S>(B, q);
+  WorkItems<OpDot<S>> ztr;
+  WorkItems<OpUpdateP<S>> up;
+  WorkItems<OpApDot<D>> ap;
+  WorkItems<OpUpdateXr> xr;
+  WorkItems<OpTrueResidual<D>> tr;
+  for (auto& b : B) {
+    auto& K = b.K;
+    ztr.add(OpDot<S>{K.z0, K.r0, K.n, K.rb, (int)RED_ZTR, K.o.eps, K.inv_n, K.mi, K.f64}, red_blocks(K.n));
+    up.add(OpUpdateP<S>{K.p, K.z0, K.n, K.st}, stream_blocks(K.n));
+    ap.add(OpApDot<D>{K.p, K.Ap, K.L0, K.bc, K.rb, K.o.eps, K.f64}, red_blocks(K.n));
+    xr.add(OpUpdateXr{K.x, K.p, K.r0, K.Ap, K.n, K.rb, K.o.tol, K.o.tol_mode, K.f64, K.inv_n}, red_blocks(K.n));
+    if (K.true_res) tr.add(OpTrueResidual<D>{K.bvec, K.x, K.L0, K.bc, K.rb, K.o.true_residual_every}, red_blocks(K.n));
+  }
+  launch_worklist<OpDot<S>, kReduceThreads>(h0, q, ztr);
+  launch_worklist<OpUpdateP<S>, 256>(h0, q, up);
+  launch_worklist<OpApDot<D>, kReduceThreads>(h0, q, ap);
+  launch_worklist<OpUpdateXr, kReduceThreads>(h0, q, xr);
+  launch_worklist<OpTrueResidual<D>, kReduceThreads>(h0, q, tr);
+}
+
+template <int D, typename S>
+static int append_batched_loop_t(GraphCursor& gc, pfm_handle* const* hs, int n, const pfm_solve_opts& o,
+                                 StepCtl* const* ctls, int which) {
+  pfm_handle* h0 = gc.h;
+  std::vector<BatchScene<D, S>> B;
+  B.reserve(n);
+  for (int s = 0; s < n; ++s) B.emplace_back(hs[s], o);
+  LoopAll la{};
+  la.n = n;
+  for (int s = 0; s < n; ++s) la.st[s] = B[s].K.st;
+  cudaGraphConditionalHandle cond{};
+  if (!gc.rc) gc.rc = check_cuda(h0, cudaGraphConditionalHandleCreate(&cond, gc.G, 0, 0), "conditional handle");
+  if (gc.rc) return gc.rc;
+  launch(h0, k_loop_begin_all, 1, 1, 0, gc.seg(), la, B[0].K.chunk, cond);
+  cudaGraph_t body = gc.add_conditional(cond, cudaGraphCondTypeWhile);
+  if (gc.rc) return gc.rc;
+  // the body's kernels are counted by k_loop_cond_all on the device, once per iteration
+  uint64_t nodes = 0;
+  const uint64_t b0 = h0->launches;
+  gc.capture_body(body, [&](cudaStream_t q) {
+    batched_body<D, S>(B, q);
+    nodes = h0->launches - b0 + 1;
+    launch(h0, k_loop_cond_all, 1, 1, 0, q, la, cond, ctls[0], (unsigned long long)nodes);
+  });
+  return gc.rc;
+}
+
+// The iteration loops of n scenes' solves as one WHILE node whose body is batched launches; every
+// scene's setup must already be in the graph behind the cursor, and its post part follows.  The
+// scenes share dim, precision and options (pfm_batch checks).
+int append_batched_loop(GraphCursor& gc, pfm_handle* const* hs, int n, const pfm_solve_opts& opts,
+                        StepCtl* const* ctls, int which) {
+  if (n < 1 || n > kBatchScenes) return set_error(gc.h, PFM_ERR_ARG, "batched solve: 1 to 128 scenes");
+  int rc = PFM_OK;
+  dispatch_solve(gc.h->cfg.dim, opts.precision, [&](auto dd, auto ss) {
+    rc = append_batched_loop_t<decltype(dd)::value, decltype(ss)>(gc, hs, n, opts, ctls, which);
+  });
+  return rc ? rc : gc.rc;
+}
+
+// A scene's part after a batched loop: the solve's finish (the final true residual) and its
+// statistics in the step state (the loop's kernels are counted by the loop itself).
+int append_poisson_finish(GraphCursor& gc, const pfm_solve_opts& opts, float* p_io, StepCtl* ctl, int which) {
+  pfm_solve_opts o = opts;
+  if (!p_io) o.warm_start = 0;
+  dispatch_solve(gc.h->cfg.dim, o.precision, [&](auto dd, auto ss) {
+    SolveKernels<decltype(dd)::value, decltype(ss)> K(gc.h, o);
+    cudaStream_t q = gc.seg();
+    K.finish(q);
+    launch(gc.h, k_record_solve, 1, 1, 0, q, ctl, (const SolveState*)K.st, which, 0);
+  });
   return gc.rc;
 }
 

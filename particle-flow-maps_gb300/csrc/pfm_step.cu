@@ -10,6 +10,7 @@
 //     iteration (the same kernels as the eager solve, so the results are bitwise the same).
 // The graph is built on the first call and rebuilt only when the fields or parameters change.
 #include <cstring>
+#include <memory>
 #include <new>
 #include <string>
 #include <vector>
@@ -273,25 +274,42 @@ static std::string key2(const pfm2_step_fields* f, const pfm_step_params* p) {
   return key.s;
 }
 
+// The parts of a scene's step around its two MGPCG iteration loops: kPartAll emits the whole step
+// (the loops included); a batch in work-list mode emits kPartHead (up to the midpoint solve's
+// setup), kPartMid (the midpoint solve's post part up to the final solve's setup) and kPartTail
+// (the final solve's post part) per scene, and the loops as batched WHILE nodes in between.
+constexpr int kPartAll = -1, kPartHead = 0, kPartMid = 1, kPartTail = 2;
+
 // One 3D step (Sim3D.step, the fused form) behind the cursor.
-static void emit_step3(GraphCursor& gc, SceneEmit& se, const pfm3_step_fields* f, const pfm_step_params* p) {
+static void emit_step3(GraphCursor& gc, SceneEmit& se, const pfm3_step_fields* f, const pfm_step_params* p,
+                       int part = kPartAll) {
   pfm_handle* h = gc.h;
   StepCtl* ctl = se.ctl;
-  emit_head(gc, se, f->u[0], f->u[1], f->u[2]);
+  const bool all = part == kPartAll, mid = p->use_midpoint_vel != 0;
   const int64_t P = h->P;
-  // j == 0: reseed (run_3D.py:753-757), G2P of the impulse, T_init = T_gm = I (:759-764)
-  se.counts[0] = emit_if(gc, se.c[0], [&](cudaStream_t q) { copy_launch(h, f->pos, f->seeds, 3 * P, q); });
-  se.counts[1] = emit_if(gc, se.c[1], [&](cudaStream_t q) {
-    pfm3_g2p(h, f->pos, f->u[0], f->u[1], f->u[2], f->init_imp, nullptr, q);
-    pfm3_reset_T(h, f->T_init, q);
-    pfm3_reset_T(h, f->T_gm, q);
-  });
-  const float* ua[3] = {f->u[0], f->u[1], f->u[2]};
-  if (p->use_midpoint_vel) {  // midpoint velocity and its projection (run_3D.py:779-788)
-    launch_midpoint(h, f->u, f->u_mid, 0.f, &ctl->dt_half, gc.seg());
-    append_poisson(gc, f->u_mid, f->p_mid, p->poisson, ctl, 0);
-    for (int a = 0; a < 3; ++a) ua[a] = f->u_mid[a];
+  if (all || part == kPartHead) {
+    emit_head(gc, se, f->u[0], f->u[1], f->u[2]);
+    // j == 0: reseed (run_3D.py:753-757), G2P of the impulse, T_init = T_gm = I (:759-764)
+    se.counts[0] = emit_if(gc, se.c[0], [&](cudaStream_t q) { copy_launch(h, f->pos, f->seeds, 3 * P, q); });
+    se.counts[1] = emit_if(gc, se.c[1], [&](cudaStream_t q) {
+      pfm3_g2p(h, f->pos, f->u[0], f->u[1], f->u[2], f->init_imp, nullptr, q);
+      pfm3_reset_T(h, f->T_init, q);
+      pfm3_reset_T(h, f->T_gm, q);
+    });
+    if (mid) {  // midpoint velocity and its projection (run_3D.py:779-788)
+      launch_midpoint(h, f->u, f->u_mid, 0.f, &ctl->dt_half, gc.seg());
+      append_poisson_pre(gc, f->u_mid, f->p_mid, p->poisson);
+    }
   }
+  if (all && mid) append_poisson_loop(gc, p->poisson, f->p_mid, ctl, 0);
+  if (!(all || part == kPartMid)) {
+    if (part == kPartTail) append_poisson_post(gc, f->u, f->p);
+    return;
+  }
+  if (mid) append_poisson_post(gc, f->u_mid, f->p_mid);
+  const float* ua[3] = {f->u[0], f->u[1], f->u[2]};
+  if (mid)
+    for (int a = 0; a < 3; ++a) ua[a] = f->u_mid[a];
   // RK4_T_forward + the P2G records, with the k == 0 gradient reinitialisation in the same kernel
   cudaMemsetAsync(ws_ptr<int>(h, h->o_count), 0, h->cells * 4, gc.seg());
   const P2GRecords3 R = records3(h, f->init_imp, f->T_init, f->init_C);
@@ -303,34 +321,50 @@ static void emit_step3(GraphCursor& gc, SceneEmit& se, const pfm3_step_fields* f
     launch_rk4_T_forward3(h, f->pos, f->T_gm, F, 0.f, &R, nullptr, q, &ctl->dt);
   });
   p2g3_from_records(h, f->u, f->w, gc.seg());
-  append_poisson(gc, f->u, f->p, p->poisson, ctl, 1);
+  append_poisson_pre(gc, f->u, f->p, p->poisson);
+  if (all) {
+    append_poisson_loop(gc, p->poisson, f->p, ctl, 1);
+    append_poisson_post(gc, f->u, f->p);
+  }
 }
 
-// One 2D step (Sim2D.step) behind the cursor.
-static void emit_step2(GraphCursor& gc, SceneEmit& se, const pfm2_step_fields* f, const pfm_step_params* p) {
+// One 2D step (Sim2D.step) behind the cursor (parts as emit_step3).
+static void emit_step2(GraphCursor& gc, SceneEmit& se, const pfm2_step_fields* f, const pfm_step_params* p,
+                       int part = kPartAll) {
   pfm_handle* h = gc.h;
   StepCtl* ctl = se.ctl;
-  emit_head(gc, se, f->u[0], f->u[1], nullptr);
+  const bool all = part == kPartAll, mid = p->use_midpoint_vel != 0;
   const int64_t P = h->P;
-  // j == 0 (2D/run_2D.py:812-832): reseed, imp = init_imp = u(pos), psi = pos, T = T_init = I
-  se.counts[0] = emit_if(gc, se.c[0], [&](cudaStream_t q) { copy_launch(h, f->pos, f->seeds, 2 * P, q); });
-  se.counts[1] = emit_if(gc, se.c[1], [&](cudaStream_t q) {
-    pfm2_g2p(h, f->pos, f->u[0], f->u[1], f->imp, nullptr, q);
-    copy_launch(h, f->init_imp, f->imp, 2 * P, q);
-    copy_launch(h, f->psi, f->pos, 2 * P, q);
-    pfm2_reset_T(h, f->T, q);
-    pfm2_reset_T(h, f->T_init, q);
-  });
-  // k == 0 (2D/run_2D.py:834-843): init_C = grad u(pos), T_gm = I, T_init = T
-  se.counts[2] = emit_if(gc, se.c[2], [&](cudaStream_t q) {
-    pfm2_g2p(h, f->pos, f->u[0], f->u[1], nullptr, f->init_C, q);
-    pfm2_reset_T(h, f->T_gm, q);
-    copy_launch(h, f->T_init, f->T, 4 * P, q);
-  });
+  if (all || part == kPartHead) {
+    emit_head(gc, se, f->u[0], f->u[1], nullptr);
+    // j == 0 (2D/run_2D.py:812-832): reseed, imp = init_imp = u(pos), psi = pos, T = T_init = I
+    se.counts[0] = emit_if(gc, se.c[0], [&](cudaStream_t q) { copy_launch(h, f->pos, f->seeds, 2 * P, q); });
+    se.counts[1] = emit_if(gc, se.c[1], [&](cudaStream_t q) {
+      pfm2_g2p(h, f->pos, f->u[0], f->u[1], f->imp, nullptr, q);
+      copy_launch(h, f->init_imp, f->imp, 2 * P, q);
+      copy_launch(h, f->psi, f->pos, 2 * P, q);
+      pfm2_reset_T(h, f->T, q);
+      pfm2_reset_T(h, f->T_init, q);
+    });
+    // k == 0 (2D/run_2D.py:834-843): init_C = grad u(pos), T_gm = I, T_init = T
+    se.counts[2] = emit_if(gc, se.c[2], [&](cudaStream_t q) {
+      pfm2_g2p(h, f->pos, f->u[0], f->u[1], nullptr, f->init_C, q);
+      pfm2_reset_T(h, f->T_gm, q);
+      copy_launch(h, f->T_init, f->T, 4 * P, q);
+    });
+    if (mid) {  // 2D/run_2D.py:866-872
+      launch_midpoint(h, f->u, f->u_mid, 0.f, &ctl->dt_half, gc.seg());
+      append_poisson_pre(gc, f->u_mid, f->p_mid, p->poisson);
+    }
+  }
+  if (all && mid) append_poisson_loop(gc, p->poisson, f->p_mid, ctl, 0);
+  if (!(all || part == kPartMid)) {
+    if (part == kPartTail) append_poisson_post(gc, f->u, f->p);
+    return;
+  }
+  if (mid) append_poisson_post(gc, f->u_mid, f->p_mid);
   float* ua[2] = {f->u[0], f->u[1]};
-  if (p->use_midpoint_vel) {  // 2D/run_2D.py:866-872
-    launch_midpoint(h, f->u, f->u_mid, 0.f, &ctl->dt_half, gc.seg());
-    append_poisson(gc, f->u_mid, f->p_mid, p->poisson, ctl, 0);
+  if (mid) {
     ua[0] = f->u_mid[0];
     ua[1] = f->u_mid[1];
   }
@@ -342,7 +376,11 @@ static void emit_step2(GraphCursor& gc, SceneEmit& se, const pfm2_step_fields* f
   pfm2_update_T(h, f->T, f->T_init, f->T_gm, q);
   pfm2_update_imp(h, f->imp, f->init_imp, f->T, q);
   pfm2_p2g(h, f->imp, f->pos, f->C, f->psi, f->u[0], f->u[1], f->psi_grid[0], f->psi_grid[1], f->w[0], f->w[1], q);
-  append_poisson(gc, f->u, f->p, p->poisson, ctl, 1);
+  append_poisson_pre(gc, f->u, f->p, p->poisson);
+  if (all) {
+    append_poisson_loop(gc, p->poisson, f->p, ctl, 1);
+    append_poisson_post(gc, f->u, f->p);
+  }
 }
 
 }  // namespace pfm
@@ -361,8 +399,138 @@ struct pfm_batch {
   cudaStream_t cap = nullptr;
   cudaGraphExec_t exec = nullptr;
   int valid = 0;
+  int worklist = 0;  // 1: the scenes' MGPCG iterations run as batched work-list kernels
   std::string err;
 };
+
+namespace pfm {
+
+static bool same_solve(const pfm_step_params& a, const pfm_step_params& b) {
+  const pfm_solve_opts &x = a.poisson, &y = b.poisson;
+  return a.use_midpoint_vel == b.use_midpoint_vel && x.max_iters == y.max_iters && x.eps == y.eps &&
+         x.tol == y.tol && x.tol_mode == y.tol_mode && x.precision == y.precision &&
+         x.true_residual_every == y.true_residual_every;
+}
+
+// Work-list form of a batch step: every scene's step runs in its own branch up to the setup of a
+// solve, the branches join, one WHILE node advances every scene's MGPCG iterations with batched
+// work-list kernels (each kernel of the iteration one launch for all scenes, work items = the
+// scenes' own thread blocks; a scene whose solve has converged skips its items), and the branches
+// fork again behind it.  Each scene's kernels run in their own order on their own data, so the
+// results are bitwise those of stepping the scenes alone.
+static int build_batch_worklist(pfm_batch* b, cudaGraph_t G) {
+  const size_t n = b->scenes.size();
+  const pfm_batch::Scene& s0 = b->scenes[0];
+  if (n > 128) {
+    b->err = "work-list batch: at most 128 scenes";
+    return PFM_ERR_ARG;
+  }
+  for (const auto& sc : b->scenes) {
+    if (sc.dim != s0.dim || !same_solve(sc.p, s0.p)) {
+      b->err = "work-list batch: the scenes must share the dimension, the midpoint flag and the solver options";
+      return PFM_ERR_ARG;
+    }
+    if (sc.h->smooth_tma) {
+      b->err = "work-list batch: the TMA-staged smoother is not batched (tuning key PFM_TUNE_SMOOTH_TMA = 0)";
+      return PFM_ERR_ARG;
+    }
+  }
+  std::vector<std::unique_ptr<GraphCursor>> cur;
+  std::vector<SceneEmit> se(n);
+  std::vector<uint64_t> before(n);
+  std::vector<pfm_handle*> hs(n);
+  std::vector<StepCtl*> ctls(n);
+  for (size_t s = 0; s < n; ++s) {
+    const auto& sc = b->scenes[s];
+    hs[s] = sc.h;
+    cur.emplace_back(new GraphCursor(sc.h, G, b->cap));
+    se[s].ctl = ws_ptr<StepCtl>(sc.h, sc.h->o_step);
+    se[s].prm = step_params(sc.h, &sc.p);
+    ctls[s] = se[s].ctl;
+    before[s] = sc.h->launches;
+    GraphCursor& gc = *cur[s];
+    for (int k = 0; k < 4; ++k)
+      if (!gc.rc && (k != 3 || se[s].prm.else_branch))
+        gc.rc = check_cuda(sc.h, cudaGraphConditionalHandleCreate(&se[s].c[k], G, 0, 0), "conditional handle");
+    if (gc.rc) {
+      b->err = sc.h->err;
+      return gc.rc;
+    }
+  }
+  auto emit_part = [&](int part) -> int {
+    for (size_t s = 0; s < n; ++s) {
+      const auto& sc = b->scenes[s];
+      GraphCursor& gc = *cur[s];
+      if (sc.dim == 3)
+        emit_step3(gc, se[s], &sc.f3, &sc.p, part);
+      else
+        emit_step2(gc, se[s], &sc.f2, &sc.p, part);
+      gc.close();
+      if (gc.rc) {
+        b->err = sc.h->err;
+        return gc.rc;
+      }
+    }
+    return PFM_OK;
+  };
+  uint64_t joint_body = 0;  // batched body kernels: counted on the device, not as fixed kernels
+  auto batched = [&](int which) -> int {
+    GraphCursor J(hs[0], G, b->cap);
+    J.ndeps = 0;
+    for (size_t s = 0; s < n; ++s)
+      for (size_t d = 0; d < cur[s]->ndeps; ++d) {
+        if (J.ndeps == sizeof(J.deps) / sizeof(J.deps[0])) {
+          b->err = "work-list batch: too many branch ends to join";
+          return PFM_ERR_ARG;
+        }
+        J.deps[J.ndeps++] = cur[s]->deps[d];
+      }
+    int rc = append_batched_loop(J, hs.data(), (int)n, s0.p.poisson, ctls.data(), which);
+    J.close();
+    if (!rc) rc = J.rc;
+    if (rc) {
+      b->err = hs[0]->err;
+      return rc;
+    }
+    joint_body += J.body_launches;
+    for (size_t s = 0; s < n; ++s) {  // fork: each scene's finish and statistics, then its next part
+      const auto& sc = b->scenes[s];
+      GraphCursor& gc = *cur[s];
+      gc.ndeps = J.ndeps;
+      for (size_t d = 0; d < J.ndeps; ++d) gc.deps[d] = J.deps[d];
+      float* p_io = which == 0 ? (sc.dim == 3 ? sc.f3.p_mid : sc.f2.p_mid) : (sc.dim == 3 ? sc.f3.p : sc.f2.p);
+      append_poisson_finish(gc, sc.p.poisson, p_io, ctls[s], which);
+      gc.close();  // the branches share one capture stream: one open segment at a time
+      if (gc.rc) {
+        b->err = sc.h->err;
+        return gc.rc;
+      }
+    }
+    return PFM_OK;
+  };
+  int rc = emit_part(kPartHead);
+  if (!rc && s0.p.use_midpoint_vel) rc = batched(0);
+  if (!rc) rc = emit_part(kPartMid);
+  if (!rc) rc = batched(1);
+  if (!rc) rc = emit_part(kPartTail);
+  if (rc) return rc;
+  for (size_t s = 0; s < n; ++s) {
+    const auto& sc = b->scenes[s];
+    GraphCursor& gc = *cur[s];
+    gc.close();
+    se[s].fixed = (sc.h->launches - before[s]) - gc.body_launches - (s == 0 ? joint_body : 0);
+    sc.h->launches = before[s];
+    rc = patch_control(sc.h, se[s]);
+    if (rc) {
+      b->err = sc.h->err;
+      return rc;
+    }
+    if (sc.dim == 3) sc.h->rec_valid = 1;
+  }
+  return PFM_OK;
+}
+
+}  // namespace pfm
 
 using namespace pfm;
 
@@ -420,6 +588,17 @@ int pfm_batch_destroy(pfm_batch* b) {
 }
 
 const char* pfm_batch_last_error(const pfm_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+int pfm_batch_set_worklist(pfm_batch* b, int on) {
+  if (!b) return PFM_ERR_NULL;
+  if (on != 0 && on != 1) {
+    b->err = "pfm_batch_set_worklist: on must be 0 or 1";
+    return PFM_ERR_ARG;
+  }
+  if (b->worklist != on) b->valid = 0;
+  b->worklist = on;
+  return PFM_OK;
+}
 
 static int batch_add(pfm_batch* b, pfm_handle* h, int dim, const pfm3_step_fields* f3, const pfm2_step_fields* f2,
                      const pfm_step_params* p) {
@@ -482,7 +661,9 @@ int pfm_batch_step(pfm_batch* b, void* stream) {
       return PFM_ERR_CUDA;
     }
     int rc = PFM_OK;
+    if (b->worklist) rc = build_batch_worklist(b, G);
     for (auto& sc : b->scenes) {  // every scene a branch from the graph's roots
+      if (b->worklist) break;
       GraphCursor gc(sc.h, G, b->cap);
       SceneEmit se;
       if (sc.dim == 3)

@@ -130,6 +130,8 @@ SIGNATURES = {
     "pfm_divergence": [_P, _P, _P, _P, _P, _P],
     "pfm_subtract_grad_p": [_P, _P, _P, _P, _P, _P],
     "pfm_sort_particles_noalloc": [_I, ctypes.POINTER(_I), ctypes.c_double, ctypes.c_int64, _P, _P, _P, _P],
+    "pfm_add_fields": [_P, _P, _F, _P, ctypes.c_int64, _P],
+    "pfm_scale_field": [_P, _F, _P, ctypes.c_int64, _P],
     "pfm3_get_central_vector": [_P, _P, _P, _P, _P, _P],
     "pfm3_curl": [_P, _P, _P, _F, _P],
     "pfm2_get_central_vector": [_P, _P, _P, _P, _P],
@@ -154,6 +156,7 @@ SIGNATURES = {
     "pfm_batch_add3": [_P, _P, ctypes.POINTER(Step3Fields), ctypes.POINTER(StepParams)],
     "pfm_batch_add2": [_P, _P, ctypes.POINTER(Step2Fields), ctypes.POINTER(StepParams)],
     "pfm_batch_step": [_P, _P],
+    "pfm_batch_set_worklist": [_P, _I],
     "pfm_batch_last_error": [_P],
     "pfm_set_tuning": [_P, _I, _I],
     "pfm_get_tuning": [_P, _I, ctypes.POINTER(_I)],

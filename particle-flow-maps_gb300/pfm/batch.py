@@ -1,8 +1,11 @@
 """Batches of independent scenes advanced with one CUDA graph launch per step (pfm_batch_*).
 
-Each scene is a :class:`pfm.Sim2D` or :class:`pfm.Sim3D` (its handle, workspace and fields); the
-batch graph holds every scene's whole step as an independent branch, so the GPU runs the scenes
-concurrently.  Results are bitwise those of stepping each scene alone.
+Each scene is a :class:`pfm.Sim2D` or :class:`pfm.Sim3D` (its handle, workspace and fields).  In
+the branch form the batch graph holds every scene's whole step as an independent branch, so the
+GPU runs the scenes concurrently.  In the work-list form (``worklist=True``) the branches join at
+each MGPCG solve and one device loop advances every scene's solver iterations with persistent
+kernels over a (scene, block) work list -- one launch per kernel of the iteration for the whole
+batch.  Either way the results are bitwise those of stepping each scene alone.
 """
 import ctypes
 
@@ -15,7 +18,7 @@ __all__ = ["Batch"]
 
 
 class Batch:
-    def __init__(self, sims):
+    def __init__(self, sims, worklist=False):
         self.lib = _lib.load()
         self.sims = list(sims)
         if not self.sims:
@@ -32,6 +35,12 @@ class Batch:
             fn = self.lib.pfm_batch_add3 if sim.scene.dim == 3 else self.lib.pfm_batch_add2
             self._check(fn(self.b, sim.scene.h, ctypes.byref(f), ctypes.byref(prm)))
             sim.graph = True
+        self.set_worklist(worklist)
+
+    def set_worklist(self, on):
+        """Switches between the branch form and the work-list form (from the next step on)."""
+        self._check(self.lib.pfm_batch_set_worklist(self.b, int(bool(on))))
+        self.worklist = bool(on)
 
     def _check(self, status):
         if status != 0:

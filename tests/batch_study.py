@@ -9,6 +9,9 @@ cell (35,651,584 particles), reinit every 12 steps, gradient reinit every 8 (the
 CFL 0.5, MGPCG to a 1e-6 relative residual.  Three ways to advance every scene one step:
   batched   one CUDA graph launch for all 64 scenes (pfm_batch_step: one branch per scene, run
             concurrently),
+  batched_worklist  the same graph with the branches joined at each MGPCG solve and every
+            scene's solver iterations run by batched persistent kernels over a (scene, block) work
+            list (pfm_batch_set_worklist),
   graphs    one whole-step graph launch per scene (pfm2_step), the 64 launches in sequence,
   eager     the phase calls of each scene (Sim2D.step), with its host synchronizations.
 Each mode is timed with CUDA events around its steps (after warm-up steps) and prints one JSON
@@ -89,13 +92,21 @@ def main():
                           "wall_s": wall}), flush=True)
         return rate
 
-    # batched: one graph launch for every scene
+    # batched: one graph launch for every scene (branch form)
     batch = pfm.Batch(sims)
     for _ in range(args.warmup):
         batch.step()
     t, w = timed(batch.step, args.steps)
     r_batch = report("batched", t, args.steps, w)
     info = [s.step_info() for s in sims]
+
+    # work-list form: the scenes' MGPCG iterations as batched persistent kernels
+    batch.set_worklist(True)
+    for _ in range(args.warmup):
+        batch.step()
+    t, w = timed(batch.step, args.steps)
+    r_work = report("batched_worklist", t, args.steps, w)
+    batch.set_worklist(False)
 
     # one whole-step graph launch per scene, in sequence
     def one_by_one():
@@ -118,6 +129,7 @@ def main():
     t, w = timed(eager, args.eager_steps)
     r_eager = report("eager", t, args.eager_steps, w)
     print(json.dumps({"speedup_batched_vs_graphs": r_batch / r_graphs, "speedup_batched_vs_eager": r_batch / r_eager,
+                      "speedup_worklist_vs_graphs": r_work / r_graphs, "worklist_vs_branches": r_work / r_batch,
                       "mgpcg_iters_last_step_first_scenes": [[i.iterations[0], i.iterations[1]] for i in info[:4]]}),
           flush=True)
 

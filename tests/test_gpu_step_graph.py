@@ -132,6 +132,65 @@ def test_batch_equals_scenes_alone():
         assert info.step == a.i == 5 and info.dt == a.last_dt
 
 
+@pytest.mark.parametrize("dim", [2, 3])
+def test_batch_worklist_equals_scenes_alone(dim):
+    """The work-list form (the scenes' MGPCG iterations as batched persistent kernels over a
+    (scene, block) work list, joined at each solve) is bitwise the scenes stepped alone: scenes of
+    uneven sizes whose solves converge at different iterations and whose hierarchies have different
+    depths, with and without a one-block V-cycle tail, in plain FP32 and in the mixed form."""
+    from pfm import _lib
+
+    def make(spec, graph, opts):
+        dx = 1.0 / spec[1]
+        if len(spec) == 2:
+            return pfm.Sim2D(pfm.vortex_blobs2(spec, dx, seed=sum(spec)), pfm.jittered(spec, dx, 4, seed=1), spec, dx,
+                             reinit_every=5, reinit_every_grad_m=2, poisson_opts=opts, graph=graph)
+        return pfm.Sim3D(_ring_velocity(spec, dx), pfm.jittered(spec, dx, 8, seed=1), spec, dx, reinit_every=4,
+                         poisson_opts=opts, graph=graph)
+
+    specs = [(32, 32), (64, 32), (128, 128), (48, 48), (256, 64)] if dim == 2 else [(16, 16, 16), (32, 16, 24),
+                                                                                    (24, 24, 24)]
+    for opts in (dict(tol=1e-6, tol_mode=1, max_iters=400),
+                 dict(tol=1e-6, tol_mode=2, max_iters=400, precision="fp16", warm_start=dim == 3,
+                      true_residual_every=5)):  # the 2D midpoint solve keeps no pressure to start from
+        alone = [make(s, False, opts) for s in specs]
+        together = [make(s, True, opts) for s in specs]
+        together[0].scene.set_tuning(_lib.TUNE_MG_TAIL_CELLS, 0)  # one scene without a tail
+        alone[0].scene.set_tuning(_lib.TUNE_MG_TAIL_CELLS, 0)
+        batch = pfm.Batch(together, worklist=True)
+        for _ in range(6):
+            for sim in alone:
+                sim.step()
+            batch.step()
+        torch.cuda.synchronize()
+        for a, b in zip(alone, together):
+            for f in range(len(a.u)):
+                assert torch.equal(a.u[f], b.u[f])
+            assert torch.equal(a.pos, b.pos) and torch.equal(a.p, b.p)
+            info = b.step_info()
+            assert info.step == a.i == 5 and info.dt == a.last_dt
+            assert [info.iterations[0], info.iterations[1]] == [a.infos[-2].iterations, a.infos[-1].iterations]
+        # the batch can go back to the branch form and carries on identically
+        batch.set_worklist(False)
+        for sim in alone:
+            sim.step()
+        batch.step()
+        torch.cuda.synchronize()
+        for a, b in zip(alone, together):
+            assert all(torch.equal(x, y) for x, y in zip(a.u, b.u))
+
+
+def test_batch_worklist_rejects_mixed_scenes():
+    opts = dict(tol=1e-6, tol_mode=1, max_iters=400)
+    s2 = pfm.Sim2D(pfm.vortex_blobs2((32, 32), 1 / 32, seed=1), pfm.jittered((32, 32), 1 / 32, 4, seed=1), (32, 32),
+                   1 / 32, poisson_opts=opts, graph=True)
+    s3 = pfm.Sim3D(_ring_velocity((16, 16, 16), 1 / 16), pfm.jittered((16, 16, 16), 1 / 16, 8, seed=1), (16, 16, 16),
+                   1 / 16, poisson_opts=opts, graph=True)
+    batch = pfm.Batch([s2, s3], worklist=True)
+    with pytest.raises(pfm.PfmError, match="share the dimension"):
+        batch.step()
+
+
 def test_tunables_do_not_change_results():
     """The autotuner's knobs (2D P2G column length, MGPCG tail threshold) change launch shapes only:
     steps with different values are bitwise equal."""
