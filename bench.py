@@ -50,6 +50,8 @@ def parse():
                     help="plain FP32 MGPCG and/or the mixed-precision warm-started MGPCG (the headline)")
     ap.add_argument("--precision", default="fp16", choices=["fp16", "bf16"],
                     help="multigrid level storage of the mixed arm")
+    ap.add_argument("--fp64-res", type=int, default=-1,
+                    help="grid of the FP64-oracle check of each arm's projection (-1: the bench grid, 0: off)")
     ap.add_argument("--eager", action="store_true",
                     help="time the eager phase calls instead of the whole-step graph (kernels inside graph "
                          "conditional nodes are invisible to ncu launch lists)")
@@ -170,6 +172,77 @@ def measured_peak():
             return float(json.load(f)["hbm_gbs"]), "measured"
     except (OSError, ValueError, KeyError):
         return FALLBACK_HBM_GBS, "fallback"
+
+
+def _div3(u):
+    import numpy as np
+    ux, uy, uz = (np.asarray(a, np.float64) for a in u)
+    return (ux[1:] - ux[:-1]) + (uy[:, 1:] - uy[:, :-1]) + (uz[:, :, 1:] - uz[:, :, :-1])
+
+
+def _rel(a, b):
+    import numpy as np
+    a = np.asarray(a, np.float64).ravel()
+    b = np.asarray(b, np.float64).ravel()
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def fp64_check(sim, oracle_tol=1e-7):
+    """Accuracy of one step's final projection against an FP64 oracle solve of the identical field
+    (outside every timed region).  One more eager step of ``sim`` runs with the final Poisson
+    solve's input velocity and output velocity/pressure copied to the host; the CPU oracle
+    (MGPCG_3.Poisson restated in C++, FP64 instance) then solves the copied input to a 1e-7
+    relative residual (below that the reference's eps = 1e-12 in alpha stalls the FP64 iteration:
+    at 64^3 it reaches 1e-7 in 5 iterations and 1e-8 only after 50).  Returns the relative L2 errors of the GPU velocity and mean-free pressure
+    against it, and the divergence the GPU velocity keeps relative to the input's."""
+    import numpy as np
+    import torch
+    import oracle as O
+    was_graph = sim.graph
+    sim.set_graph(False)
+    sc = sim.scene
+    real = sc.poisson
+    calls = []
+
+    def poisson(u, p_out=None, **kw):
+        calls.append(None)
+        if len(calls) == 2:  # the step's second solve: the final projection
+            u_in = [t.detach().cpu().numpy().copy() for t in u]
+            info = real(u, p_out, **kw)
+            calls[-1] = (u_in, [t.detach().cpu().numpy().copy() for t in u], p_out.detach().cpu().numpy().copy(),
+                         info)
+            return info
+        return real(u, p_out, **kw)
+
+    sc.poisson = poisson
+    try:
+        sim.step()
+        torch.cuda.synchronize()
+    finally:
+        del sc.poisson
+    sim.set_graph(was_graph)
+    u_in, u_gpu, p_gpu, info = calls[1]
+    t0 = time.perf_counter()
+    ux, uy, uz, p64, it64, _ = O.poisson3(*u_in, fp64=True, tol=oracle_tol, tol_mode=1)
+    t_or = time.perf_counter() - t0
+    b = []
+    for f, a in enumerate(u_in):  # apply_bc zeroes the wall faces before the divergence
+        a = a.copy()
+        idx = [slice(None)] * 3
+        idx[f] = 0
+        a[tuple(idx)] = 0
+        idx[f] = -1
+        a[tuple(idx)] = 0
+        b.append(a)
+    bdiv = _div3(b)
+    pg = p_gpu.astype(np.float64)
+    return {"res": int(u_in[1].shape[0]), "step": int(sim.i), "mgpcg_iters": info.iterations,
+            "velocity_rel_l2": _rel(np.concatenate([a.ravel() for a in u_gpu]),
+                                    np.concatenate([a.ravel() for a in (ux, uy, uz)])),
+            "pressure_rel_l2": _rel(pg - pg.mean(), p64 - p64.mean()),
+            "divergence_left_rel": float(np.linalg.norm(_div3(u_gpu)) / np.linalg.norm(bdiv - bdiv.mean())),
+            "oracle": f"FP64 MGPCG_3.Poisson on the host cores to |r| < {oracle_tol:g} |r0| ({it64} iterations, "
+                      f"{t_or:.1f} s)"}
 
 
 # ------------------------------------------------------------------------------------------------
@@ -342,8 +415,19 @@ def main():
         sim.timer = None
         eager_ms = sum(statistics.mean(v) for v in timer.summary().values())
         sim.set_graph(not args.eager)
+        check = None
+        if rank == 0 and args.fp64_res != 0:
+            if args.fp64_res in (-1, args.res):
+                check = fp64_check(sim)
+            else:  # a smaller scene of the same workload, a few steps in
+                small = make_sim(args.fp64_res, args.ppc_axis, popts, graph=True)
+                for _ in range(3):
+                    small.step()
+                check = fp64_check(small)
+                del small
+                torch.cuda.empty_cache()
         return dict(sim=sim, value=value, elapsed=elapsed, wall=wall, clocks=clk, launches=launches,
-                    phases=timer.summary(), mg_iters=mg_iters, eager_ms=eager_ms)
+                    phases=timer.summary(), mg_iters=mg_iters, eager_ms=eager_ms, fp64_check=check)
 
     # the two arms of the metric, at the same residual: MGPCG stops at |r| < tol |b| in both
     plain_opts = dict(tol=args.tol, tol_mode=args.tol_mode, max_iters=400, check_every=4)
@@ -453,12 +537,12 @@ def main():
                 "phase_note": "phase_ms: CUDA events around the eager phase calls of 3 further steps "
                               "(sum %.2f ms/step)" % head["eager_ms"],
                 "roofline": roofline, "roofline_fp32": roofline_fp32, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
-                "gpu_launches": launches}
+                "gpu_launches": launches, "fp64_check": head["fp64_check"]}
         if plain is not None and mixed:
             line["plain_fp32"] = {"value": plain["value"], "ms_per_step": plain["elapsed"] / args.steps * 1e3,
                                   "mgpcg_iters": plain["mg_iters"],
                                   "phase_ms": {k: statistics.mean(v) for k, v in plain["phases"].items()},
-                                  "clocks": plain["clocks"]}
+                                  "clocks": plain["clocks"], "fp64_check": plain["fp64_check"]}
             line["speedup_vs_plain_fp32"] = value / plain["value"]
         print(json.dumps(line), flush=True)
     if dist is not None:

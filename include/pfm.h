@@ -369,6 +369,15 @@ int pfm_batch_add3(pfm_batch* b, pfm_handle* h, const pfm3_step_fields* f, const
 int pfm_batch_add2(pfm_batch* b, pfm_handle* h, const pfm2_step_fields* f, const pfm_step_params* p);
 int pfm_batch_step(pfm_batch* b, void* stream);
 const char* pfm_batch_last_error(const pfm_batch* b);
+/* Work-list form of the batch (on = 1; 0 = the branch form above, the default): each scene's step
+ * runs in its own branch up to the setup of an MGPCG solve (3D/mgpcg.py:202-280 inside the step
+ * loop of 3D/run_3D.py:716-822, 2D/run_2D.py:772-909); then one WHILE node advances every scene's
+ * solver iterations with persistent kernels over a work list of (scene, thread block) items, one
+ * launch per kernel of the iteration for the whole batch, a converged scene skipping its items;
+ * the branches continue behind it.  Same results bit for bit.  The scenes must share the dimension,
+ * the midpoint flag and the solver options, and leave PFM_TUNE_SMOOTH_TMA at 0 (else
+ * pfm_batch_step returns PFM_ERR_ARG); at most 128 scenes.  Takes effect at the next step. */
+int pfm_batch_set_worklist(pfm_batch* b, int on);
 
 /* ---- the reference's alternative ("evolve m") dataflow ---------------------------------------
  * Kernels the reference defines beside its live step (their call sites in 3D/run_3D.py:795-808
@@ -428,6 +437,11 @@ int pfm2_advect_smoke(pfm_handle* h, const float* smoke0, float* smoke1, const f
 
 /* ---- diagnostics ------------------------------------------------------------------------------ */
 
+/* add_fields (3D/taichi_utils.py:18-21, 2D/taichi_utils.py:13-16): dest = f1 + multiplier * f2,
+ * and scale_field (3D/taichi_utils.py:13-16, 2D/taichi_utils.py:8-11): result = alpha * a, over n
+ * floats of any field shape (f32, the product rounded before the sum).  No handle. */
+int pfm_add_fields(const float* f1, const float* f2, float multiplier, float* dest, int64_t n, void* stream);
+int pfm_scale_field(const float* a, float alpha, float* result, int64_t n, void* stream);
 /* get_central_vector (3D/taichi_utils.py:80-85): vc [nx][ny][nz][3] = face averages. */
 int pfm3_get_central_vector(pfm_handle* h, const float* u_x, const float* u_y, const float* u_z, float* vc,
                             void* stream);
@@ -463,8 +477,11 @@ int pfm_split_central_vector(pfm_handle* h, const float* vc, float* u_x, float* 
 
 /* Jittered particle seeding (particles uniformly jittered from a seed): each cell
  * holds ppc_axis^dim particles, one per sub-cell, at (sub-lattice index + U) * dx / ppc_axis with
- * U from a counter-based splitmix64 hash of (seed, particle index, axis); cell-major order,
- * last axis fastest.  P must equal ppc_axis^dim * cells.  pos [dim][P].  Bit-identical to
+ * U from a counter-based splitmix64 hash of (seed, particle index, axis).  Order: the lines of
+ * cells along the last axis in turn, each in groups of 16 cells; inside a group
+ * [leading sub-indices][cell][last sub-index] (8 particles per cell: 32 consecutive particles
+ * are 16 neighbouring cells with the same leading sub-cell, which keeps a warp's interpolation
+ * stencils on shared rows).  P must equal ppc_axis^dim * cells.  pos [dim][P].  Bit-identical to
  * pfm.sim.jittered() on the host. */
 int pfm_seed_jittered(pfm_handle* h, uint64_t seed, int ppc_axis, float* pos, void* stream);
 

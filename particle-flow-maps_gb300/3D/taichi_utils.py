@@ -6,6 +6,7 @@ import os
 import sys
 
 sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+import pfm as _pfm  # noqa: E402
 from pfm import dropin as _d  # noqa: E402
 
 
@@ -19,13 +20,13 @@ def copy_to(source, dest):
 
 
 def add_fields(f1, f2, dest, multiplier):
-    """dest = f1 + f2 * multiplier (3D/taichi_utils.py:18-21)."""
-    dest.copy_(f1 + f2 * float(multiplier))
+    """dest = f1 + multiplier * f2 (3D/taichi_utils.py:18-21), by libpfm's elementwise kernel."""
+    _pfm.add_fields(f1, f2, dest, multiplier)
 
 
 def scale_field(a, alpha, result):
-    """result = a * alpha (3D/taichi_utils.py:13-16)."""
-    result.copy_(a * float(alpha))
+    """result = alpha * a (3D/taichi_utils.py:13-16), by libpfm's elementwise kernel."""
+    _pfm.scale_field(a, alpha, result)
 
 
 def get_central_vector(vx, vy, vz, vc):

@@ -284,6 +284,25 @@ __global__ void __launch_bounds__(kFThreads) k_advect_smoke2(const float* __rest
 
 static bool aligned16(const void* p) { return (((uintptr_t)p) & 15) == 0; }
 
+// add_fields / scale_field (3D/taichi_utils.py:13-21, 2D/taichi_utils.py:9-16): elementwise over
+// any field, f32, the product rounded before the sum (no contraction), in the reference's order.
+__global__ void __launch_bounds__(256) k_add_fields(const float* __restrict__ f1, const float* __restrict__ f2,
+                                                    float multiplier, float* __restrict__ dest, int64_t n) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    dest[e] = __fadd_rn(f1[e], __fmul_rn(multiplier, f2[e]));
+}
+
+__global__ void __launch_bounds__(256) k_scale_field(const float* __restrict__ a, float alpha,
+                                                     float* __restrict__ result, int64_t n) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    result[e] = __fmul_rn(alpha, a[e]);
+}
+
+static unsigned elementwise_blocks(int64_t n) {
+  const int64_t b = (n + 255) / 256;
+  return (unsigned)(b < 1 ? 1 : (b > 152 * 32 ? 152 * 32 : b));
+}
+
 }  // namespace pfm
 
 using namespace pfm;
@@ -374,6 +393,23 @@ int pfm2_advect_smoke(pfm_handle* h, const float* smoke0, float* smoke1, const f
   launch(h, k_advect_smoke2, grid_for(h->cells, kFThreads), kFThreads, 0, (cudaStream_t)stream, smoke0, smoke1, psi_x,
          psi_y, h->geom, dx);
   return launch_check(h, "k_advect_smoke2");
+}
+
+
+int pfm_add_fields(const float* f1, const float* f2, float multiplier, float* dest, int64_t n, void* stream) {
+  if (n < 0) return PFM_ERR_ARG;
+  if (n == 0) return PFM_OK;
+  if (!f1 || !f2 || !dest) return PFM_ERR_NULL;
+  k_add_fields<<<elementwise_blocks(n), 256, 0, (cudaStream_t)stream>>>(f1, f2, multiplier, dest, n);
+  return cudaGetLastError() == cudaSuccess ? PFM_OK : PFM_ERR_CUDA;
+}
+
+int pfm_scale_field(const float* a, float alpha, float* result, int64_t n, void* stream) {
+  if (n < 0) return PFM_ERR_ARG;
+  if (n == 0) return PFM_OK;
+  if (!a || !result) return PFM_ERR_NULL;
+  k_scale_field<<<elementwise_blocks(n), 256, 0, (cudaStream_t)stream>>>(a, alpha, result, n);
+  return cudaGetLastError() == cudaSuccess ? PFM_OK : PFM_ERR_CUDA;
 }
 
 }  // extern "C"

@@ -12,7 +12,7 @@ import torch
 from . import _lib
 from ._lib import PfmError, SolveOpts, SolveStats
 
-__all__ = ["Scene", "PfmError", "SolveInfo", "sort_particles_noalloc"]
+__all__ = ["Scene", "PfmError", "SolveInfo", "sort_particles_noalloc", "add_fields", "scale_field"]
 
 
 class SolveInfo:
@@ -668,6 +668,36 @@ def sort_particles_noalloc(pos, res, dx, cell_count, order):
                                                      ctypes.c_void_p(torch.cuda.current_stream(pos.device).cuda_stream))
     if st != 0:
         raise PfmError(st, "pfm_sort_particles_noalloc failed")
+
+
+def _field_check(name, t, like=None):
+    if not isinstance(t, torch.Tensor) or t.dtype != torch.float32 or not t.is_cuda or not t.is_contiguous():
+        raise PfmError(7, f"{name} must be a contiguous CUDA float32 tensor")
+    if like is not None and (t.shape != like.shape or t.device != like.device):
+        raise PfmError(2, f"{name} must match the shape and device of the destination")
+
+
+def add_fields(f1, f2, dest, multiplier):
+    """add_fields (3D/taichi_utils.py:18-21): dest = f1 + multiplier * f2 through pfm_add_fields."""
+    _field_check("dest", dest)
+    _field_check("f1", f1, dest)
+    _field_check("f2", f2, dest)
+    with torch.cuda.device(dest.device):
+        st = _lib.load().pfm_add_fields(_ptr(f1), _ptr(f2), float(multiplier), _ptr(dest), dest.numel(),
+                                        ctypes.c_void_p(torch.cuda.current_stream(dest.device).cuda_stream))
+    if st != 0:
+        raise PfmError(st, "pfm_add_fields failed")
+
+
+def scale_field(a, alpha, result):
+    """scale_field (3D/taichi_utils.py:13-16): result = alpha * a through pfm_scale_field."""
+    _field_check("result", result)
+    _field_check("a", a, result)
+    with torch.cuda.device(result.device):
+        st = _lib.load().pfm_scale_field(_ptr(a), float(alpha), _ptr(result), result.numel(),
+                                         ctypes.c_void_p(torch.cuda.current_stream(result.device).cuda_stream))
+    if st != 0:
+        raise PfmError(st, "pfm_scale_field failed")
 
 
 def measure_fp32_peak(blocks_per_sm=4, iters=65536, reps=3, packed=None, device=None):

@@ -1,14 +1,15 @@
 """Generate the golden vectors by running the reference's own Python/Taichi source.
 
-Run in a container that has the reference checked out (it reads ``/root/reference``)::
+Run where the reference is checked out, with its root directory (the one holding ``2D/`` and
+``3D/``) as the first argument::
 
-    python tests/golden/make_golden.py ref3d_kernels   # per-kernel cases, 3D
-    python tests/golden/make_golden.py ref2d_kernels   # per-kernel cases, 2D
-    python tests/golden/make_golden.py ref3d_steps     # run_3D.main(): 10 steps at 8^3
-    python tests/golden/make_golden.py ref2d_steps     # run_2D.main(): 20 steps at 32^2
-    python tests/golden/make_golden.py ref3d_fields    # smoke transport + curl, 16x12x8
-    python tests/golden/make_golden.py ref2d_fields    # advect_smoke + curl, 32x24
-    python tests/golden/make_golden.py ref3d_variants  # the "evolve m" kernels, 12x10x8
+    python tests/golden/make_golden.py REFERENCE_ROOT ref3d_kernels   # per-kernel cases, 3D
+    python tests/golden/make_golden.py REFERENCE_ROOT ref2d_kernels   # per-kernel cases, 2D
+    python tests/golden/make_golden.py REFERENCE_ROOT ref3d_steps     # run_3D.main(): 10 steps at 8^3
+    python tests/golden/make_golden.py REFERENCE_ROOT ref2d_steps     # run_2D.main(): 20 steps at 32^2
+    python tests/golden/make_golden.py REFERENCE_ROOT ref3d_fields    # smoke transport + curl, 16x12x8
+    python tests/golden/make_golden.py REFERENCE_ROOT ref2d_fields    # advect_smoke + curl, 32x24
+    python tests/golden/make_golden.py REFERENCE_ROOT ref3d_variants  # the "evolve m" kernels, 12x10x8
 
 Taichi 1.5.0 is not installable here, so the reference modules are executed through
 ``oracle/ref_shim`` (a restatement of the Taichi semantics the step uses: f32 arithmetic,
@@ -30,7 +31,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = "/root/reference"
+REF = None  # the reference checkout, from the command line
 sys.path.insert(0, os.path.join(REPO, "oracle", "ref_shim"))
 import loader  # noqa: E402
 
@@ -653,7 +654,12 @@ CASES = dict(ref3d_kernels=ref3d_kernels, ref2d_kernels=ref2d_kernels, ref3d_ste
              ref3d_variants=ref3d_variants)
 
 if __name__ == "__main__":
-    name = sys.argv[1]
+    if len(sys.argv) != 3 or sys.argv[2] not in CASES:
+        sys.exit("usage: make_golden.py REFERENCE_ROOT CASE  (CASE: %s)" % ", ".join(CASES))
+    REF = os.path.abspath(sys.argv[1])
+    if not (os.path.isdir(os.path.join(REF, "3D")) and os.path.isdir(os.path.join(REF, "2D"))):
+        sys.exit(f"{REF} does not hold the reference's 2D/ and 3D/ directories")
+    name = sys.argv[2]
     data = CASES[name]()
     path = os.path.join(HERE, f"{name}.npz")
     np.savez_compressed(path, **{k: np.asarray(v) for k, v in data.items()})

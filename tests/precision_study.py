@@ -48,7 +48,7 @@ def main():
             "mixed": dict(tol=1e-6, tol_mode=2, max_iters=400, precision="fp16", warm_start=True,
                           true_residual_every=5)}
     for arm in args.arms:
-        sim = bench.make_sim(args.res, 2, arms[arm])
+        sim = bench.make_sim(args.res, 2, arms[arm], graph=False)  # eager steps: the solves are host calls
         sc = sim.scene
         captured = {}
         calls = {"n": 0}

@@ -214,3 +214,21 @@ def test_smoke_errors():
     s2 = pfm.Scene(2, (8, 8), 1.0 / 8, 0)
     with pytest.raises(pfm.PfmError):
         s2.clamp_smoke(s0, s0, [])
+
+
+def test_add_fields_and_scale_field_bitwise():
+    """add_fields / scale_field (3D/taichi_utils.py:13-21) through the library's elementwise
+    kernels: bitwise the f32 expression with the product rounded before the sum."""
+    rng = np.random.default_rng(17)
+    f1 = rng.standard_normal((33, 17, 9)).astype(np.float32)
+    f2 = rng.standard_normal((33, 17, 9)).astype(np.float32)
+    m = np.float32(-0.3711)
+    dest = torch.empty(f1.shape, device="cuda")
+    pfm.add_fields(torch.from_numpy(f1).cuda(), torch.from_numpy(f2).cuda(), dest, float(m))
+    res = torch.empty(f1.shape, device="cuda")
+    pfm.scale_field(torch.from_numpy(f2).cuda(), float(m), res)
+    torch.cuda.synchronize()
+    assert np.array_equal(dest.cpu().numpy(), (f1 + (m * f2).astype(np.float32)).astype(np.float32))
+    assert np.array_equal(res.cpu().numpy(), (m * f2).astype(np.float32))
+    with pytest.raises(pfm.PfmError):
+        pfm.add_fields(torch.zeros(3, device="cuda"), torch.zeros(4, device="cuda"), torch.zeros(3, device="cuda"), 1.0)
