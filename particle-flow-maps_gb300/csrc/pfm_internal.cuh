@@ -292,15 +292,30 @@ struct MacFields3 {
 // x/y weights form natural pairs, so they run together on packed f32x2 FMAs; z runs scalar.
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 
-__device__ __forceinline__ void interp_mac3(const MacFields3& F, const MacGeom& g, const float p[3],
-                                            float uo[3], float G[3][3], bool want_grad) {
-  Axis3 A0[3], A1[3];
+// The two tap sets per axis at p (A0: the component along the axis, A1: the others).
+__device__ __forceinline__ void mac_taps3(const MacGeom& g, const float p[3], Axis3 A0[3], Axis3 A1[3]) {
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     float u = p[a] * g.inv_dx;  // = p / dx exactly when dx is a power of two
     axis_taps(u - 0.0f, g.hi[a][a], A0[a]);            // the component along a
     axis_taps(u - 0.5f, g.hi[(a + 1) % 3][a], A1[a]);  // the others
   }
+}
+
+// The tap sums of interp_mac3 for taps already computed (two fields of the same shape sampled at
+// one position share them).
+__device__ __forceinline__ void interp_mac3_taps(const MacFields3& F, const MacGeom& g, const Axis3 A0[3],
+                                                 const Axis3 A1[3], float uo[3], float G[3][3], bool want_grad);
+
+__device__ __forceinline__ void interp_mac3(const MacFields3& F, const MacGeom& g, const float p[3],
+                                            float uo[3], float G[3][3], bool want_grad) {
+  Axis3 A0[3], A1[3];
+  mac_taps3(g, p, A0, A1);
+  interp_mac3_taps(F, g, A0, A1, uo, G, want_grad);
+}
+
+__device__ __forceinline__ void interp_mac3_taps(const MacFields3& F, const MacGeom& g, const Axis3 A0[3],
+                                                 const Axis3 A1[3], float uo[3], float G[3][3], bool want_grad) {
   const float inv_dx = g.inv_dx;
   // ---- components x and y together: x uses (A0x, A1y, A1z), y uses (A1x, A0y, A1z)
   {

@@ -101,15 +101,21 @@ __global__ void __launch_bounds__(kRK4Threads, PFM_RK4_MINB) k_rk4_T_forward3(fl
   if (dt_dev) dt = *dt_dev;  // the whole-step graph keeps dt on the device
   float p0[3] = {pos[q], pos[P + q], pos[2 * P + q]};
   float T0[3][3];
+  float u[3], G[3][3];  // the RK4 stage's velocity and gradient
   if (GRADM) {
     {
-      float ug[3], G[3][3];
-      interp_mac3(Fg, g, p0, ug, G, true);
+      // grad u(p0) of the pre-midpoint velocity and the first RK4 stage's u_mid(p0) share their
+      // taps, and their loads are independent: both gathers are issued together
+      Axis3 A0[3], A1[3];
+      mac_taps3(g, p0, A0, A1);
+      float ug[3], Gg[3][3];
+      interp_mac3_taps(Fg, g, A0, A1, ug, Gg, true);
+      interp_mac3_taps(F, g, A0, A1, u, G, true);
       float* C = const_cast<float*>(R.C);
 #pragma unroll
       for (int c = 0; c < 3; ++c)
 #pragma unroll
-        for (int r = 0; r < 3; ++r) C[(c * 3 + r) * P + q] = G[c][r];
+        for (int r = 0; r < 3; ++r) C[(c * 3 + r) * P + q] = Gg[c][r];
     }
     float* Ti = const_cast<float*>(R.Ti);
     float M[3][3], N[3][3];
@@ -149,8 +155,7 @@ __global__ void __launch_bounds__(kRK4Threads, PFM_RK4_MINB) k_rk4_T_forward3(fl
   const float half_dt = 0.5f * dt;
 #pragma unroll 1
   for (int s = 0; s < 4; ++s) {
-    float u[3], G[3][3];
-    interp_mac3(F, g, pk, u, G, true);
+    if (!GRADM || s > 0) interp_mac3(F, g, pk, u, G, true);
     float dT[3][3];
 #pragma unroll
     for (int v = 0; v < 3; ++v)
