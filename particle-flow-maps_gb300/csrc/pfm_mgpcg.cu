@@ -83,6 +83,21 @@ __device__ __forceinline__ void stencil(const S* __restrict__ f, const Lvl& L, c
   mult = num;
 }
 
+// num_fluid_neighbors alone (the mult of stencil<D>, no loads)
+template <int D>
+__device__ __forceinline__ float stencil_mult(const Lvl& L, const BC& bc, int i, int j, int k) {
+  float num = 2.f * D;
+  if (i <= 0 && bc.lo[0] == 2) num -= 1.f;
+  if (i >= L.n0 - 1 && bc.hi[0] == 2) num -= 1.f;
+  if (j <= 0 && bc.lo[1] == 2) num -= 1.f;
+  if (j >= L.n1 - 1 && bc.hi[1] == 2) num -= 1.f;
+  if (D == 3) {
+    if (k <= 0 && bc.lo[2] == 2) num -= 1.f;
+    if (k >= L.n2 - 1 && bc.hi[2] == 2) num -= 1.f;
+  }
+  return num;
+}
+
 __device__ __forceinline__ void decode(const Lvl& L, int64_t e, int& i, int& j, int& k) {
   split3((unsigned)e, L.d1, L.d2, i, j, k);
 }
@@ -220,10 +235,13 @@ __global__ void __launch_bounds__(256) k_subtract_grad_p(float* __restrict__ u, 
 // launch (k_worklist) runs the blocks of many scenes' operations from one work list.
 
 // smooth(l, phase): z = (r + nbsum(z)) / mult on cells with (i+j+k)&1 == phase.  One thread per
-// pair of cells along the last axis; the thread updates the member of the right colour.
+// pair of cells along the last axis; the thread updates the member of the right colour.  `fresh`:
+// the level's z is to start at zero (the V-cycle zeroes a level before its first sweep), so the
+// sweep reads no neighbours -- every neighbour sum is 0 -- and writes zero to the other colour:
+// bitwise the zeroing launch followed by the sweep, in one pass.
 template <int D, typename S>
 __device__ __forceinline__ void smooth_blk(S* __restrict__ z, const S* __restrict__ r, const Lvl& L, const BC& bc,
-                                           int phase, const SolveState* st, unsigned bid) {
+                                           int phase, const SolveState* st, unsigned bid, bool fresh = false) {
   if (st && st->done) return;
   const int nl = (D == 3) ? L.n2 : L.n1;
   const int half = (nl + 1) >> 1;
@@ -233,19 +251,28 @@ __device__ __forceinline__ void smooth_blk(S* __restrict__ z, const S* __restric
   int i, j, k;
   const unsigned t = udiv(e, L.dh);
   const int m = (int)(e - t * (unsigned)half);
+  int other;  // the pair's member of the other colour along the last axis
   if (D == 3) {
     const unsigned q = udiv(t, L.d1);
     j = (int)(t - q * (unsigned)L.n1);
     i = (int)q;
     k = 2 * m + ((i + j + phase) & 1);
+    other = k ^ 1;
+    if (fresh && other < L.n2) stv(z + ((int64_t)i * L.n1 + j) * L.n2 + other, 0.f);
     if (k >= L.n2) return;
   } else {
     i = (int)t;
     j = 2 * m + ((i + phase) & 1);
     k = 0;
+    other = j ^ 1;
+    if (fresh && other < L.n1) stv(z + (int64_t)i * L.n1 + other, 0.f);
     if (j >= L.n1) return;
   }
   const int64_t c = ((int64_t)i * L.n1 + j) * L.n2 + k;
+  if (fresh) {
+    stv(z + c, (ldv(r + c) + 0.f) / stencil_mult<D>(L, bc, i, j, k));
+    return;
+  }
   float nb, mult;
   stencil<D>(z, L, bc, i, j, k, c, nb, mult);
   stv(z + c, (ldv(r + c) + nb) / mult);
@@ -264,8 +291,8 @@ struct OpSmooth {
 
 template <int D, typename S>
 __global__ void __launch_bounds__(256) k_smooth(S* __restrict__ z, const S* __restrict__ r, Lvl L,
-                                                BC bc, int phase, const SolveState* st) {
-  smooth_blk<D, S>(z, r, L, bc, phase, st, blockIdx.x);
+                                                BC bc, int phase, const SolveState* st, int fresh) {
+  smooth_blk<D, S>(z, r, L, bc, phase, st, blockIdx.x, fresh != 0);
 }
 
 // Eight consecutive values along the last axis (n2 % 8 == 0, so a run is 16- or 32-byte aligned).
@@ -303,7 +330,7 @@ __device__ __forceinline__ void st8(__nv_bfloat16* p, const float (&v)[8]) { st8
 // with the same sum, in the same order, as stencil<3> -- bitwise the result of k_smooth.
 template <typename S>
 __device__ __forceinline__ void smooth8_blk(S* __restrict__ z, const S* __restrict__ r, const Lvl& L, const BC& bc,
-                                            int phase, const SolveState* st, unsigned bid) {
+                                            int phase, const SolveState* st, unsigned bid, bool fresh = false) {
   if (st && st->done) return;
   const int runs = L.n2 >> 3;
   const unsigned e = bid * blockDim.x + threadIdx.x;
@@ -315,8 +342,27 @@ __device__ __forceinline__ void smooth8_blk(S* __restrict__ z, const S* __restri
   const int64_t sx = (int64_t)L.n1 * L.n2, sy = L.n2;
   const int64_t c0 = ((int64_t)i * L.n1 + j) * L.n2 + k0;
   float zc[8], rr[8], xp[8], xm[8], yp[8], ym[8];
-  ld8(z + c0, zc);
   ld8(r + c0, rr);
+  if (fresh) {  // z starts at zero: the colour gets (r + 0) / mult, the other colour zero
+    float base = 6.f;
+    if (i <= 0 && bc.lo[0] == 2) base -= 1.f;
+    if (i >= L.n0 - 1 && bc.hi[0] == 2) base -= 1.f;
+    if (j <= 0 && bc.lo[1] == 2) base -= 1.f;
+    if (j >= L.n1 - 1 && bc.hi[1] == 2) base -= 1.f;
+    const int first = (i + j + k0 + phase) & 1;
+    float out[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int k = k0 + q;
+      float num = base;
+      if (k <= 0 && bc.lo[2] == 2) num -= 1.f;
+      if (k >= L.n2 - 1 && bc.hi[2] == 2) num -= 1.f;
+      out[q] = ((q & 1) == first) ? (rr[q] + 0.f) / num : 0.f;
+    }
+    st8(z + c0, out);
+    return;
+  }
+  ld8(z + c0, zc);
   const bool hx = i < L.n0 - 1, lx = i > 0, hy = j < L.n1 - 1, ly = j > 0;
   if (hx) ld8(z + c0 + sx, xp);
   if (lx) ld8(z + c0 - sx, xm);
@@ -365,8 +411,8 @@ struct OpSmooth8 {
 
 template <typename S>
 __global__ void __launch_bounds__(256) k_smooth8(S* __restrict__ z, const S* __restrict__ r, Lvl L, BC bc,
-                                                 int phase, const SolveState* st) {
-  smooth8_blk<S>(z, r, L, bc, phase, st, blockIdx.x);
+                                                 int phase, const SolveState* st, int fresh) {
+  smooth8_blk<S>(z, r, L, bc, phase, st, blockIdx.x, fresh != 0);
 }
 
 // smooth(l, phase) in 3D for 16-bit level storage with the tile staged by the TMA: a block owns
@@ -1143,12 +1189,28 @@ static S* level_r(pfm_handle* h, int l) {
   return ws_ptr<S>(h, h->o_r[l]);
 }
 
+template <typename S>
+static void zero_launch(pfm_handle* h, int l, const SolveState* st, cudaStream_t s) {
+  launch(h, k_zero<S>, stream_blocks(h->lv[l].count), 256, 0, s, level_z<S>(h, l), h->lv[l].count, st);
+}
+
+// One red-black half-sweep of level l.  With *zero_first set, the level's z is due to be zeroed
+// first: the grid-wide smoothers do both in one pass (`fresh`), the TMA-staged one after a zeroing
+// launch; either way *zero_first is cleared.
 template <int D, typename S>
-static void smooth_launch(pfm_handle* h, int l, int phase, const SolveState* st, cudaStream_t s) {
+static void smooth_launch(pfm_handle* h, int l, int phase, const SolveState* st, cudaStream_t s,
+                          bool* zero_first = nullptr) {
   Lvl L = lvl_of(h, l);
   const int nl = (D == 3) ? L.n2 : L.n1;
   int64_t npairs = (D == 3) ? (int64_t)L.n0 * L.n1 * ((nl + 1) / 2) : (int64_t)L.n0 * ((nl + 1) / 2);
+  int fresh = 0;
+  if (zero_first && *zero_first) {
+    *zero_first = false;
+    fresh = 1;
+  }
   if (D == 3 && sizeof(S) == 2 && L.n2 % 8 == 0 && h->smooth_tma) {  // 16-bit levels: the TMA-staged tile
+    if (fresh) zero_launch<S>(h, l, st, s);
+    fresh = 0;
     const int TK = L.n2 % 64 == 0 ? 64 : (L.n2 % 32 == 0 ? 32 : (L.n2 % 16 == 0 ? 16 : 8));
     CUtensorMap tz, tr;
     const bool bf = sizeof(S) == 2 && !std::is_same<S, __half>::value;
@@ -1163,11 +1225,11 @@ static void smooth_launch(pfm_handle* h, int l, int phase, const SolveState* st,
   if (D == 3 && L.n2 % 8 == 0) {
     const int64_t nvec = (int64_t)L.n0 * L.n1 * (L.n2 / 8);
     launch(h, k_smooth8<S>, grid_for(nvec, 256), 256, 0, s, level_z<S>(h, l), (const S*)level_r<S>(h, l), L,
-           bc_of(h), phase, st);
+           bc_of(h), phase, st, fresh);
     return;
   }
   launch(h, k_smooth<D, S>, grid_for(npairs, 256), 256, 0, s, level_z<S>(h, l), (const S*)level_r<S>(h, l), L,
-         bc_of(h), phase, st);
+         bc_of(h), phase, st, fresh);
 }
 
 static int tail_level(const pfm_handle* h) {
@@ -1209,20 +1271,30 @@ int set_tail_cells(pfm_handle* h, int cells) {
 }
 
 // apply_preconditioner (3D/mgpcg.py:182-200) with level storage S
+// The levels' z start at zero: each level's zeroing is folded into its first half-sweep (which
+// then reads no neighbours), or launched on its own where the level's first use is not a sweep
+// (no pre-smoothing); the updates are the same, two to four launches fewer per V-cycle.
 template <int D, typename S>
 static void vcycle(pfm_handle* h, const SolveState* st, cudaStream_t s) {
   const int L = h->L;
   const BC bc = bc_of(h);
   const int l0 = tail_level(h);
-  launch(h, k_zero<S>, stream_blocks(h->lv[0].count), 256, 0, s, level_z<S>(h, 0), h->lv[0].count, st);
+  bool zero_first[kMaxLevels] = {};
+  auto flush = [&](int l) {  // a use of z_l other than a half-sweep: zero it now if still due
+    if (zero_first[l]) {
+      zero_launch<S>(h, l, st, s);
+      zero_first[l] = false;
+    }
+  };
+  zero_first[0] = true;
   const int down_end = l0 < L ? l0 : L - 1;  // grid-wide levels that restrict to a coarser one
   for (int l = 0; l < down_end; ++l) {
     for (int i = 0; i < h->cfg.pre_post_smoothing; ++i) {
-      smooth_launch<D, S>(h, l, 0, st, s);
+      smooth_launch<D, S>(h, l, 0, st, s, &zero_first[l]);
       smooth_launch<D, S>(h, l, 1, st, s);
     }
-    if (l + 1 != l0)
-      launch(h, k_zero<S>, stream_blocks(h->lv[l + 1].count), 256, 0, s, level_z<S>(h, l + 1), h->lv[l + 1].count, st);
+    flush(l);  // the restriction reads z_l
+    if (l + 1 != l0) zero_first[l + 1] = true;
     Lvl Lf = lvl_of(h, l), Lc = lvl_of(h, l + 1);
     launch(h, k_restrict<D, S>, grid_for(Lc.count, 256), 256, 0, s, (const S*)level_z<S>(h, l),
            (const S*)level_r<S>(h, l), Lf, level_r<S>(h, l + 1), Lc, bc, st);
@@ -1239,16 +1311,20 @@ static void vcycle(pfm_handle* h, const SolveState* st, cudaStream_t s) {
     }
     T.total = off;
     const size_t smem = (size_t)off * 2 * sizeof(float);
+    zero_first[l0] = false;  // the tail starts its levels from zero and writes all of z_l0
     launch(h, k_vcycle_tail<D, S>, 1, kTailThreads, smem, s, level_z<S>(h, l0), (const S*)level_r<S>(h, l0), T, bc,
            h->cfg.pre_post_smoothing, h->cfg.bottom_smoothing, st);
   } else {
     for (int i = 0; i < h->cfg.bottom_smoothing; ++i) {
-      smooth_launch<D, S>(h, L - 1, 0, st, s);
+      smooth_launch<D, S>(h, L - 1, 0, st, s, &zero_first[L - 1]);
       smooth_launch<D, S>(h, L - 1, 1, st, s);
     }
+    flush(L - 1);
   }
   for (int l = down_end - 1; l >= 0; --l) {
     Lvl Lf = lvl_of(h, l), Lc = lvl_of(h, l + 1);
+    flush(l);  // the prolongation reads z_l and z_{l+1}
+    flush(l + 1);
     launch(h, k_prolong<D, S>, grid_for(Lf.count, 256), 256, 0, s, level_z<S>(h, l), Lf, (const S*)level_z<S>(h, l + 1),
            Lc, st);
     for (int i = 0; i < h->cfg.pre_post_smoothing; ++i) {
