@@ -215,6 +215,9 @@ int pfm_create(const pfm_config* cfg, pfm_handle** out) {
   h->o_state = take(sizeof(SolveState));
   h->o_maxpart = take(kReduceBlocks * sizeof(float) + 256);
   h->o_step = take(sizeof(StepCtl));
+  h->o_hist = take(2 * C * 4);
+  h->o_hist_flag = take(2 * sizeof(int));
+  h->hist_ptr[0] = h->hist_ptr[1] = nullptr;
 
   h->ws_need = off;
   h->p2g2_column = 8;
@@ -264,6 +267,10 @@ int pfm_set_workspace(pfm_handle* h, void* dptr, size_t bytes) {
   h->ws = (char*)dptr;
   h->ws_bytes = bytes;
   h->rec_valid = 0;
+  // no pressure history yet in this workspace (warm_start 2)
+  h->hist_ptr[0] = h->hist_ptr[1] = nullptr;
+  const cudaError_t e = cudaMemset(ws_ptr<int>(h, h->o_hist_flag), 0, 2 * sizeof(int));
+  if (e != cudaSuccess) return check_cuda(h, e, "pressure history flags");
   return PFM_OK;
 }
 

@@ -119,6 +119,10 @@ struct pfm_handle {
   size_t o_key, o_slot, o_order, o_count, o_start, o_blocksums, o_payload;
   size_t o_r[pfm::kMaxLevels], o_z[pfm::kMaxLevels];
   size_t o_x, o_p, o_Ap, o_b, o_partials, o_state, o_maxpart, o_step;
+  // warm_start 2: the previous solution of up to two pressure buffers (the caller's pointers name
+  // the slots) and a device flag per slot saying whether it holds one
+  size_t o_hist, o_hist_flag;
+  const float* hist_ptr[2];
 
   // pinned host mirror of the solve state
   pfm::SolveState* h_state;
@@ -553,6 +557,10 @@ int launch_rk4_T_forward2(pfm_handle* h, float* pos, float* T, const MacFields2&
 // Sets the MGPCG tail threshold and the shared-memory limit of the one-block V-cycle tail
 // (pfm_mgpcg.cu).
 int set_tail_cells(pfm_handle* h, int cells);
+
+// Initial guess of a warm-started solve into x (pfm_mgpcg.cu): mode 1 copies the caller's pressure
+// p_io, mode 2 extrapolates 2 p_io - (the solution before it) once that history exists.
+int warm_start_init(pfm_handle* h, float* x, const float* p_io, int mode, cudaStream_t st);
 
 // Counting sort of the particle cells (pfm_p2g.cu).
 int sort_particles(pfm_handle* h, const float* pos, cudaStream_t st);

@@ -1573,12 +1573,47 @@ static int solve_dispatch(pfm_handle* h, const pfm_solve_opts* opts, pfm_solve_s
   return solve_impl<D, float>(h, o, stats, s);
 }
 
+// x = 2 p - hist (the linear extrapolation of the last two solutions) where the slot holds a
+// previous solution, else x = p; the slot then takes p.  One thread sets the flag afterwards.
+__global__ void __launch_bounds__(256) k_warm_extrap(float* __restrict__ x, float* __restrict__ hist,
+                                                     const float* __restrict__ p, int64_t n, const int* flag) {
+  const bool have = *flag != 0;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const float v = p[e];
+    x[e] = have ? __fsub_rn(2.f * v, hist[e]) : v;
+    hist[e] = v;
+  }
+}
+
+__global__ void k_set_flag(int* flag) { *flag = 1; }
+
+int warm_start_init(pfm_handle* h, float* x, const float* p_io, int mode, cudaStream_t s) {
+  if (!p_io) return set_error(h, PFM_ERR_NULL, "MGPCG: warm_start needs the pressure buffer");
+  if (mode == 1)
+    return check_cuda(h, cudaMemcpyAsync(x, p_io, h->cells * 4, cudaMemcpyDeviceToDevice, s), "copy initial guess");
+  int slot = -1;
+  for (int k = 0; k < 2 && slot < 0; ++k)
+    if (h->hist_ptr[k] == p_io) slot = k;
+  for (int k = 0; k < 2 && slot < 0; ++k)
+    if (!h->hist_ptr[k]) {
+      h->hist_ptr[k] = p_io;
+      slot = k;
+    }
+  if (slot < 0)
+    return set_error(h, PFM_ERR_ARG, "MGPCG: warm_start 2 keeps the history of at most two pressure buffers per handle");
+  float* hist = ws_ptr<float>(h, h->o_hist) + (size_t)slot * h->cells;
+  int* flag = ws_ptr<int>(h, h->o_hist_flag) + slot;
+  launch(h, k_warm_extrap, stream_blocks(h->cells), 256, 0, s, x, hist, p_io, (int64_t)h->cells, (const int*)flag);
+  launch(h, k_set_flag, 1, 1, 0, s, flag);
+  return launch_check(h, "warm start");
+}
+
 int mgpcg_solve_in_place(pfm_handle* h, float* x_out, const pfm_solve_opts* opts, pfm_solve_stats* stats,
                          cudaStream_t s) {
-  if (opts && opts->warm_start) {  // the initial guess is the caller's current x_out
-    if (!x_out) return set_error(h, PFM_ERR_NULL, "MGPCG: warm_start needs the pressure buffer");
-    int c = check_cuda(h, cudaMemcpyAsync(ws_ptr<float>(h, h->o_x), x_out, h->cells * 4, cudaMemcpyDeviceToDevice, s),
-                       "copy initial guess");
+  if (opts && (opts->warm_start < 0 || opts->warm_start > 2))
+    return set_error(h, PFM_ERR_ARG, "MGPCG: warm_start must be 0, 1 or 2");
+  if (opts && opts->warm_start) {  // the initial guess from the caller's current x_out
+    int c = warm_start_init(h, ws_ptr<float>(h, h->o_x), x_out, opts->warm_start, s);
     if (c) return c;
   }
   int rc = h->cfg.dim == 3 ? solve_dispatch<3>(h, opts, stats, s) : solve_dispatch<2>(h, opts, stats, s);
@@ -1683,7 +1718,7 @@ int append_poisson_pre(GraphCursor& gc, float* const* u, float* p_io, const pfm_
   else
     launch(h, k_divergence<2>, grid_for(h->cells, 256), 256, 0, q, u[0], u[1], (const float*)nullptr, lvl_of(h, 0), r0,
            -1.f);
-  if (o.warm_start) cudaMemcpyAsync(x, p_io, h->cells * 4, cudaMemcpyDeviceToDevice, q);
+  if (o.warm_start && !gc.rc) gc.rc = warm_start_init(h, x, p_io, o.warm_start, q);
   dispatch_solve(D, o.precision, [&](auto dd, auto ss) {
     SolveKernels<decltype(dd)::value, decltype(ss)> K(h, o);
     K.setup(gc.seg());

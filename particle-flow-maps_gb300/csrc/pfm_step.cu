@@ -96,8 +96,9 @@ static int check_step_params(pfm_handle* h, const pfm_step_params* p) {
   if (!(p->CFL > 0.0) || !(p->visualize_dt > 0.0)) return set_error(h, PFM_ERR_ARG, "step: CFL and visualize_dt must be > 0");
   if (p->poisson.max_iters < 0)
     return set_error(h, PFM_ERR_ARG, "step: the device solve needs a finite max_iters (the host does not relaunch it)");
-  if (p->poisson.tol_mode < 0 || p->poisson.tol_mode > 2 || p->poisson.precision < 0 || p->poisson.precision > 2)
-    return set_error(h, PFM_ERR_ARG, "step: tol_mode must be 0..2 and precision 0..2");
+  if (p->poisson.tol_mode < 0 || p->poisson.tol_mode > 2 || p->poisson.precision < 0 || p->poisson.precision > 2 ||
+      p->poisson.warm_start < 0 || p->poisson.warm_start > 2)
+    return set_error(h, PFM_ERR_ARG, "step: tol_mode, precision and warm_start must be 0..2");
   return PFM_OK;
 }
 
@@ -709,6 +710,14 @@ int pfm_step_reset(pfm_handle* h, int i, int ik, double sub_t, int frame_idx, vo
   launch(h, k_step_clock_set, 1, 1, 0, s, ctl, i, ik, sub_t, frame_idx);
   h->step_clock_init = 1;
   return launch_check(h, "k_step_clock_set");
+}
+
+int pfm_reset_warm_history(pfm_handle* h, void* stream) {
+  if (!h) return PFM_ERR_NULL;
+  int rc = require_ws(h);
+  if (rc) return rc;
+  return check_cuda(h, cudaMemsetAsync(ws_ptr<int>(h, h->o_hist_flag), 0, 2 * sizeof(int), (cudaStream_t)stream),
+                    "pressure history flags");
 }
 
 int pfm_step_info(pfm_handle* h, pfm_step_info_t* info, void* stream) {

@@ -150,6 +150,7 @@ SIGNATURES = {
     "pfm3_step": [_P, ctypes.POINTER(Step3Fields), ctypes.POINTER(StepParams), _P],
     "pfm2_step": [_P, ctypes.POINTER(Step2Fields), ctypes.POINTER(StepParams), _P],
     "pfm_step_reset": [_P, _I, _I, ctypes.c_double, _I, _P],
+    "pfm_reset_warm_history": [_P, _P],
     "pfm_step_info": [_P, ctypes.POINTER(StepInfo), _P],
     "pfm_batch_create": [ctypes.POINTER(_P)],
     "pfm_batch_destroy": [_P],

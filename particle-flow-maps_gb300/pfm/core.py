@@ -323,7 +323,9 @@ class Scene:
         o.max_iters, o.eps, o.tol, o.tol_mode, o.check_every = int(max_iters), float(eps), float(tol), int(tol_mode), int(check_every)
         o.precision = {"fp32": 0, "fp16": 1, "bf16": 2}.get(precision, precision)
         o.precision = int(o.precision)
-        o.warm_start = int(bool(warm_start))
+        # False/True -> 0/1 (start from zero / from the caller's pressure); 2: extrapolate from the
+        # caller's pressure and the solution before it (the library keeps that one per buffer)
+        o.warm_start = 2 if (not isinstance(warm_start, bool) and warm_start == 2) else int(bool(warm_start))
         o.true_residual_every = int(true_residual_every)
         return o
 
@@ -332,7 +334,9 @@ class Scene:
         """MGPCG_{2,3}.Poisson in place on u (a sync point).  Returns SolveInfo.
 
         ``precision`` "fp32" (0, the reference), "fp16" (1) or "bf16" (2) multigrid level storage;
-        ``warm_start`` starts from p_out's current pressure; ``true_residual_every`` K > 0
+        ``warm_start`` starts from p_out's current pressure (``warm_start=2``: from the linear
+        extrapolation 2 p - p_before of it and the solution before it, which the library keeps per
+        p_out buffer, two buffers per scene); ``true_residual_every`` K > 0
         recomputes r = b - A x every K iterations and before accepting convergence."""
         u = self._grids(u)
         if p_out is not None:
@@ -448,6 +452,11 @@ class Scene:
         alive).  No host synchronization."""
         fn = self.lib.pfm3_step if self.dim == 3 else self.lib.pfm2_step
         self._check(fn(self.h, ctypes.byref(fields), ctypes.byref(params), self._stream()))
+
+    def reset_warm_history(self):
+        """Forgets the pressures kept for ``warm_start=2`` (the next solve of each buffer starts from
+        the buffer's pressure alone)."""
+        self._check(self.lib.pfm_reset_warm_history(self.h, self._stream()))
 
     def step_reset(self, i=-1, ik=0, sub_t=0.0, frame_idx=0):
         """Sets the device step clock (pfm_step_reset); the next graph step is i + 1."""

@@ -154,3 +154,60 @@ def test_vcycle_tail_is_bitwise_the_grid_kernels():
         out.append((x, info.iterations, info.rTr))
     for x, it, rtr in out[1:]:
         assert torch.equal(out[0][0], x) and (it, rtr) == out[0][1:]
+
+
+def test_extrapolated_warm_start_in_the_step():
+    """warm_start 2: each solve starts from 2 p - p_before, the linear extrapolation of its buffer's
+    last two solutions (the library keeps p_before per pressure buffer).  On the two-ring scene the
+    final solve needs fewer iterations than from the previous pressure alone, the whole-step graph
+    is bitwise the eager phase calls, and the results stay within the solver tolerance of the
+    warm_start 1 run."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    base = dict(tol=1e-6, tol_mode=2, max_iters=400, precision="fp16", true_residual_every=5)
+    runs = {}
+    for name, ws, graph in (("prev", True, True), ("extrap", 2, True), ("extrap_eager", 2, False)):
+        sim = bench.make_sim(64, 2, dict(base, warm_start=ws), graph=graph)
+        its = []
+        for _ in range(8):
+            sim.step()
+            if not graph:
+                its.append((sim.infos[-2].iterations, sim.infos[-1].iterations))
+        torch.cuda.synchronize()
+        if graph:
+            info = sim.step_info()
+            its = [tuple(info.history[s % 64]) for s in range(info.step - 7, info.step + 1)]
+        runs[name] = (its, [t.clone() for t in sim.u], sim.p.clone())
+        del sim
+    for a, b in zip(runs["extrap"][1] + [runs["extrap"][2]], runs["extrap_eager"][1] + [runs["extrap_eager"][2]]):
+        assert torch.equal(a, b)
+    assert runs["extrap"][0] == runs["extrap_eager"][0]
+    final_prev = sum(i[1] for i in runs["prev"][0][2:])
+    final_extrap = sum(i[1] for i in runs["extrap"][0][2:])
+    assert final_extrap < final_prev, (runs["prev"][0], runs["extrap"][0])
+    for a, b in zip(runs["extrap"][1], runs["prev"][1]):
+        assert (a - b).norm().item() <= 1e-5 * b.norm().item()
+
+
+def test_extrapolated_warm_start_history_per_buffer():
+    """The history is kept per pressure buffer (two per handle); a third buffer is refused, and
+    pfm_reset_warm_history makes the next solve start from the buffer alone again (bitwise the
+    warm_start 1 solve)."""
+    res = (32, 32, 32)
+    sc = pfm.Scene(3, res, 1 / 32, 0)
+    import __graft_entry__ as G
+    u = G._ring_velocity(res, 1 / 32)
+    kw = dict(tol=1e-6, tol_mode=2, max_iters=400)
+    ps = [torch.zeros(res, device="cuda") for _ in range(3)]
+    for p in ps[:2]:
+        sc.poisson([torch.from_numpy(a).cuda() for a in u], p, warm_start=2, **kw)
+    with pytest.raises(pfm.PfmError, match="two pressure buffers"):
+        sc.poisson([torch.from_numpy(a).cuda() for a in u], ps[2], warm_start=2, **kw)
+    sc.reset_warm_history()
+    a, b = ps[0].clone(), ps[0].clone()
+    ia = sc.poisson([torch.from_numpy(x).cuda() for x in u], a, warm_start=True, **kw)
+    ib = sc.poisson([torch.from_numpy(x).cuda() for x in u], ps[0], warm_start=2, **kw)
+    torch.cuda.synchronize()
+    assert ia.iterations == ib.iterations and torch.equal(a, ps[0])
