@@ -76,7 +76,10 @@ typedef struct pfm_handle pfm_handle;
  * true_residual_every K > 0 recomputes the true residual |b - A x| every K iterations and after
  * the last one and reports it (stats.rTr_true); the stopping rule stays the reference's, on the
  * recursive residual (x is stored in f32, whose rounding alone leaves a true residual of about
- * 2e-5 relative at 64^3, above a 1e-6 rule). */
+ * 2e-5 relative at 64^3, above a 1e-6 rule).  With true_residual_replace (mixed solves) x is kept
+ * in FP64 during the solve, and every K iterations, and whenever the recursive residual passes
+ * the rule, b - A x is formed in FP64, replaces the recursive residual and decides convergence:
+ * the solve stops on its true residual; the caller receives x rounded to f32. */
 typedef struct pfm_solve_opts {
   int max_iters;   /* 400 in Poisson() (3D/mgpcg.py:422); -1 = unlimited */
   double eps;      /* 1e-12, added to the denominators of alpha and beta */
@@ -88,6 +91,9 @@ typedef struct pfm_solve_opts {
   int precision;   /* 0 FP32 (reference), 1 FP16 multigrid levels, 2 BF16 multigrid levels */
   int warm_start;  /* 1: initial guess = the caller's pressure buffer; 2: its extrapolation */
   int true_residual_every; /* 0: never (reference); K > 0: check every K iterations and at the end */
+  int true_residual_replace; /* mixed solve with K > 0: 1 = x accumulates in FP64 and the true residual
+                                b - A x (FP64) replaces the recursive one every K iterations and before
+                                convergence is accepted; 0 = the check only reports */
 } pfm_solve_opts;
 
 typedef struct pfm_solve_stats {

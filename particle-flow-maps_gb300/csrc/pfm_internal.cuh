@@ -122,6 +122,7 @@ struct pfm_handle {
   // warm_start 2: the previous solution of up to two pressure buffers (the caller's pointers name
   // the slots) and a device flag per slot saying whether it holds one
   size_t o_hist, o_hist_flag;
+  size_t o_x64;
   const float* hist_ptr[2];
 
   // pinned host mirror of the solve state

@@ -807,17 +807,23 @@ __global__ void __launch_bounds__(kReduceThreads) k_Ap_dot(const float* __restri
   Ap_dot_blk<D>(p, Ap, L, bc, rb, eps, f64, blockIdx.x, gridDim.x);
 }
 
-// update_x, update_r, reduce(r, r) and the convergence test (3D/mgpcg.py:243-258).
+// update_x, update_r, reduce(r, r) and the convergence test (3D/mgpcg.py:243-258).  With x64
+// (the residual-replacement solve) x accumulates in FP64 and a passing test only marks the solve
+// for verification (done = 5): k_true_residual, next in the iteration, decides on the true residual.
 __device__ __forceinline__ void update_xr_blk(float* __restrict__ x, const float* __restrict__ p, float* __restrict__ r,
                                               const float* __restrict__ Ap, int64_t n, RedBuf rb, double tol,
-                                              int tol_mode, int f64, double inv_n, unsigned bid, unsigned nb) {
+                                              int tol_mode, int f64, double inv_n, unsigned bid, unsigned nb,
+                                              double* __restrict__ x64 = nullptr) {
   SolveState* st = rb.st;
   if (st->done) return;
   const float alpha = st->alpha;
   float acc = 0.f;
   CompSum cacc;
   for (int64_t e = (int64_t)bid * blockDim.x + threadIdx.x; e < n; e += (int64_t)nb * blockDim.x) {
-    x[e] += alpha * p[e];
+    if (x64)
+      x64[e] = fma((double)alpha, (double)p[e], x64[e]);
+    else
+      x[e] += alpha * p[e];
     float re = r[e] - alpha * Ap[e];
     r[e] = re;
     if (f64) cacc.add(re * re);
@@ -832,7 +838,7 @@ __device__ __forceinline__ void update_xr_blk(float* __restrict__ x, const float
       st->done = 3;
       st->conv_it = st->it;
     } else if (converged(total, st, tol, tol_mode)) {
-      st->done = 1;
+      st->done = x64 ? 5 : 1;
       st->conv_it = st->it;
     }
   }
@@ -848,16 +854,30 @@ struct OpUpdateXr {
   double tol;
   int tol_mode, f64;
   double inv_n;
+  double* x64;
   __device__ __forceinline__ void run(unsigned bid, unsigned nb) const {
-    update_xr_blk(x, p, r, Ap, n, rb, tol, tol_mode, f64, inv_n, bid, nb);
+    update_xr_blk(x, p, r, Ap, n, rb, tol, tol_mode, f64, inv_n, bid, nb, x64);
   }
 };
 
 __global__ void __launch_bounds__(kReduceThreads) k_update_xr(float* __restrict__ x, const float* __restrict__ p,
                                                               float* __restrict__ r, const float* __restrict__ Ap,
                                                               int64_t n, RedBuf rb, double tol, int tol_mode,
-                                                              int f64, double inv_n) {
-  update_xr_blk(x, p, r, Ap, n, rb, tol, tol_mode, f64, inv_n, blockIdx.x, gridDim.x);
+                                                              int f64, double inv_n, double* x64) {
+  update_xr_blk(x, p, r, Ap, n, rb, tol, tol_mode, f64, inv_n, blockIdx.x, gridDim.x, x64);
+}
+
+// FP32 <-> FP64 copies of x for the residual-replacement solve
+__global__ void __launch_bounds__(256) k_x_to64(double* __restrict__ x64, const float* __restrict__ x, int64_t n,
+                                                const SolveState* st) {
+  if (st->done) return;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    x64[e] = (double)x[e];
+}
+
+__global__ void __launch_bounds__(256) k_x_from64(float* __restrict__ x, const double* __restrict__ x64, int64_t n) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    x[e] = (float)x64[e];
 }
 
 // r = b - A x: the initial residual of a warm-started solve
@@ -878,6 +898,53 @@ __global__ void __launch_bounds__(256) k_residual(float* __restrict__ r, const f
 // does not steer: x is stored in f32, which puts a floor under the true residual (about 2e-5
 // relative at 64^3 for a smooth pressure, more at 256^3) below the reference's recursive 1e-6
 // rule, so replacing the recursive residual by it would hold every solve above its tolerance.
+// With x64 and r (the residual-replacement solve, every > 0): the residual b - A x is formed in
+// FP64 from the FP64 x, replaces the recursive residual r, and its norm decides convergence --
+// every `every` iterations and whenever k_update_xr marked the solve for verification (done 5).
+template <int D>
+__device__ __forceinline__ void true_residual_replace_blk(const float* __restrict__ b, const double* __restrict__ x64,
+                                                          float* __restrict__ r, const Lvl& L, const BC& bc,
+                                                          RedBuf rb, int every, double tol, int tol_mode,
+                                                          double inv_n, unsigned bid, unsigned nb) {
+  SolveState* st = rb.st;
+  const int done = st->done;
+  if (!(done == 5 || (done == 0 && (st->it + 1) % every == 0))) return;
+  double acc = 0.0;
+  const int64_t sx = (int64_t)L.n1 * L.n2, sy = L.n2;
+  for (int64_t e = (int64_t)bid * blockDim.x + threadIdx.x; e < L.count; e += (int64_t)nb * blockDim.x) {
+    int i, j, k;
+    decode(L, e, i, j, k);
+    double nbs = 0.0;
+    if (i < L.n0 - 1) nbs += x64[e + sx];
+    if (i > 0) nbs += x64[e - sx];
+    if (j < L.n1 - 1) nbs += x64[e + sy];
+    if (j > 0) nbs += x64[e - sy];
+    if (D == 3) {
+      if (k < L.n2 - 1) nbs += x64[e + 1];
+      if (k > 0) nbs += x64[e - 1];
+    }
+    const double re = (double)b[e] - ((double)stencil_mult<D>(L, bc, i, j, k) * x64[e] - nbs);
+    r[e] = (float)re;
+    acc += re * re;
+  }
+  double total;
+  if (!grid_sum(acc, rb.partials, &st->ticket, &total, bid, nb)) return;
+  if (threadIdx.x == 0) {
+    st->rTr_true = total;
+    st->rTr = total;
+    if (total > 0.0) st->hscale = (float)(1.0 / sqrt(total * inv_n));
+    if (!isfinite(total)) {
+      st->done = 3;
+      st->conv_it = st->it;
+    } else if (converged(total, st, tol, tol_mode)) {
+      st->done = 1;
+      st->conv_it = st->it;
+    } else {
+      st->done = 0;  // the recursive residual had drifted below the true one: iterate on
+    }
+  }
+}
+
 template <int D>
 __device__ __forceinline__ void true_residual_blk(const float* __restrict__ b, const float* __restrict__ x,
                                                   const Lvl& L, const BC& bc, RedBuf rb, int every, unsigned bid,
@@ -906,8 +973,16 @@ struct OpTrueResidual {
   BC bc;
   RedBuf rb;
   int every;
+  const double* x64;  // non-null: the replacement form
+  float* r;
+  double tol;
+  int tol_mode;
+  double inv_n;
   __device__ __forceinline__ void run(unsigned bid, unsigned nb) const {
-    true_residual_blk<D>(b, x, L, bc, rb, every, bid, nb);
+    if (x64)
+      true_residual_replace_blk<D>(b, x64, r, L, bc, rb, every, tol, tol_mode, inv_n, bid, nb);
+    else
+      true_residual_blk<D>(b, x, L, bc, rb, every, bid, nb);
   }
 };
 
@@ -916,6 +991,15 @@ __global__ void __launch_bounds__(kReduceThreads) k_true_residual(const float* _
                                                                   const float* __restrict__ x, Lvl L, BC bc,
                                                                   RedBuf rb, int every) {
   true_residual_blk<D>(b, x, L, bc, rb, every, blockIdx.x, gridDim.x);
+}
+
+template <int D>
+__global__ void __launch_bounds__(kReduceThreads) k_true_residual_replace(const float* __restrict__ b,
+                                                                          const double* __restrict__ x64,
+                                                                          float* __restrict__ r, Lvl L, BC bc,
+                                                                          RedBuf rb, int every, double tol,
+                                                                          int tol_mode, double inv_n) {
+  true_residual_replace_blk<D>(b, x64, r, L, bc, rb, every, tol, tol_mode, inv_n, blockIdx.x, gridDim.x);
 }
 
 // update_p: p = z + beta p (3D/mgpcg.py:147-150)
@@ -1397,13 +1481,14 @@ template <int D, typename S>
 struct SolveKernels {
   pfm_handle* h;
   pfm_solve_opts o;
-  bool mixed, warm, true_res, keep_b, neu;
+  bool mixed, warm, true_res, keep_b, neu, replace;
   int f64, chunk, mi;
   int64_t n;
   double inv_n;
   SolveState* st;
   RedBuf rb;
   float *r0, *x, *p, *Ap, *bvec;
+  double* x64;  // the residual-replacement solve's FP64 x (else null)
   S *z0, *rh;
   Lvl L0;
   BC bc;
@@ -1413,6 +1498,7 @@ struct SolveKernels {
     f64 = mixed ? 1 : 0;
     warm = o.warm_start != 0;
     true_res = o.true_residual_every > 0;
+    replace = mixed && true_res && o.true_residual_replace != 0;
     keep_b = warm || true_res || o.tol_mode == 2;
     chunk = o.max_iters >= 0 ? o.max_iters + 1 : o.check_every;
     mi = o.max_iters;
@@ -1428,6 +1514,7 @@ struct SolveKernels {
     p = ws_ptr<float>(h, h->o_p);
     Ap = ws_ptr<float>(h, h->o_Ap);
     bvec = ws_ptr<float>(h, h->o_b);
+    x64 = replace ? ws_ptr<double>(h, h->o_x64) : nullptr;
     L0 = lvl_of(h, 0);
     bc = bc_of(h);
   }
@@ -1446,8 +1533,11 @@ struct SolveKernels {
   void first_half(cudaStream_t q) {
     launch(h, k_Ap_dot<D>, red_blocks(n), kReduceThreads, 0, q, (const float*)p, Ap, L0, bc, rb, o.eps, f64);
     launch(h, k_update_xr, red_blocks(n), kReduceThreads, 0, q, x, (const float*)p, r0, (const float*)Ap, n, rb, o.tol,
-           o.tol_mode, f64, inv_n);
-    if (true_res)
+           o.tol_mode, f64, inv_n, x64);
+    if (replace)
+      launch(h, k_true_residual_replace<D>, red_blocks(n), kReduceThreads, 0, q, (const float*)bvec,
+             (const double*)x64, r0, L0, bc, rb, o.true_residual_every, o.tol, o.tol_mode, inv_n);
+    else if (true_res)
       launch(h, k_true_residual<D>, red_blocks(n), kReduceThreads, 0, q, (const float*)bvec, (const float*)x, L0, bc, rb,
              o.true_residual_every);
   }
@@ -1464,6 +1554,7 @@ struct SolveKernels {
              (int)RED_BTB, o.eps, inv_n, mi, 1);
     }
     if (warm) launch(h, k_residual<D>, stream_blocks(n), 256, 0, q, r0, (const float*)bvec, (const float*)x, L0, bc);
+    if (replace) launch(h, k_x_to64, stream_blocks(n), 256, 0, q, x64, (const float*)x, n, (const SolveState*)st);
     launch(h, k_dot<float>, red_blocks(n), kReduceThreads, 0, q, (const float*)r0, (const float*)r0, n, rb,
            (int)RED_RTR0, o.eps, inv_n, mi, f64);
     // the scaled level-storage copy of r0, once r0.r0 (and so the scale) is known
@@ -1484,7 +1575,9 @@ struct SolveKernels {
     launch(h, k_loop_cond, 1, 1, 0, q, (const SolveState*)st, cond);
   }
   void finish(cudaStream_t q) {
-    if (true_res)  // the final true residual of the solve
+    if (replace)  // the FP32 pressure the caller receives
+      launch(h, k_x_from64, stream_blocks(n), 256, 0, q, x, (const double*)x64, n);
+    if (true_res)  // the final true residual of the solve (of the FP32 pressure)
       launch(h, k_true_residual<D>, red_blocks(n), kReduceThreads, 0, q, (const float*)bvec, (const float*)x, L0, bc, rb,
              -1);
   }
@@ -1502,7 +1595,7 @@ static int solve_impl(pfm_handle* h, const pfm_solve_opts& o, pfm_solve_stats* s
   const int mi = K.mi;
   const int chunk = K.chunk;
   SolveState* hs = h->h_state;
-  const int key_mode = (o.precision & 3) | (K.warm ? 4 : 0);
+  const int key_mode = (o.precision & 3) | (K.warm ? 4 : 0) | (K.replace ? 8 : 0);
   if (!h->g_valid || h->g_eps != o.eps || h->g_tol != o.tol || h->g_mode != o.tol_mode || h->g_max_iters != mi ||
       h->g_chunk != chunk || h->g_variant != key_mode || h->g_true_every != o.true_residual_every) {
     if (h->g_setup) cudaGraphExecDestroy(h->g_setup);
@@ -1543,7 +1636,7 @@ static int solve_impl(pfm_handle* h, const pfm_solve_opts& o, pfm_solve_stats* s
     if (rc) return rc;
     // kernels launched: k_loop_begin, one body per completed iteration (k_loop_cond inside), and
     // the final true-residual check
-    h->launches += 1 + (uint64_t)h->g_body_nodes * (uint64_t)(hs->it - it_before) + (K.true_res ? 1 : 0);
+    h->launches += 1 + (uint64_t)h->g_body_nodes * (uint64_t)(hs->it - it_before) + (K.true_res ? 1 : 0) + (K.replace ? 1 : 0);
     it_before = hs->it;
     if (hs->done || mi >= 0) break;
   }
@@ -1563,7 +1656,7 @@ static int solve_impl(pfm_handle* h, const pfm_solve_opts& o, pfm_solve_stats* s
 
 template <int D>
 static int solve_dispatch(pfm_handle* h, const pfm_solve_opts* opts, pfm_solve_stats* stats, cudaStream_t s) {
-  pfm_solve_opts o{400, 1e-12, 1e-12, 0, 4, 0, 0, 0};
+  pfm_solve_opts o{400, 1e-12, 1e-12, 0, 4, 0, 0, 0, 0};
   if (opts) o = *opts;
   if (o.check_every < 1) o.check_every = 1;
   if (o.tol_mode < 0 || o.tol_mode > 2) return set_error(h, PFM_ERR_ARG, "MGPCG: tol_mode must be 0, 1 or 2");
@@ -2016,8 +2109,11 @@ static void batched_body(std::vector<BatchScene<D, S>>& B, cudaStream_t q) {
     ztr.add(OpDot<S>{K.z0, K.r0, K.n, K.rb, (int)RED_ZTR, K.o.eps, K.inv_n, K.mi, K.f64}, red_blocks(K.n));
     up.add(OpUpdateP<S>{K.p, K.z0, K.n, K.st}, stream_blocks(K.n));
     ap.add(OpApDot<D>{K.p, K.Ap, K.L0, K.bc, K.rb, K.o.eps, K.f64}, red_blocks(K.n));
-    xr.add(OpUpdateXr{K.x, K.p, K.r0, K.Ap, K.n, K.rb, K.o.tol, K.o.tol_mode, K.f64, K.inv_n}, red_blocks(K.n));
-    if (K.true_res) tr.add(OpTrueResidual<D>{K.bvec, K.x, K.L0, K.bc, K.rb, K.o.true_residual_every}, red_blocks(K.n));
+    xr.add(OpUpdateXr{K.x, K.p, K.r0, K.Ap, K.n, K.rb, K.o.tol, K.o.tol_mode, K.f64, K.inv_n, K.x64}, red_blocks(K.n));
+    if (K.true_res)
+      tr.add(OpTrueResidual<D>{K.bvec, K.x, K.L0, K.bc, K.rb, K.o.true_residual_every, K.x64, K.r0, K.o.tol,
+                               K.o.tol_mode, K.inv_n},
+             red_blocks(K.n));
   }
   launch_worklist<OpDot<S>, kReduceThreads>(h0, q, ztr);
   launch_worklist<OpUpdateP<S>, 256>(h0, q, up);

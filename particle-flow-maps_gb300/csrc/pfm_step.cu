@@ -212,7 +212,7 @@ static void key_params(KeyBuf& k, const pfm_step_params* p) {
   const pfm_solve_opts& o = p->poisson;
   k << p->CFL << p->visualize_dt << p->save_frame_each_step << p->reinit_every << p->reinit_every_grad_m
     << p->use_midpoint_vel << p->reinit_particle_pos << o.max_iters << o.eps << o.tol << o.tol_mode << o.precision
-    << o.warm_start << o.true_residual_every;
+    << o.warm_start << o.true_residual_every << o.true_residual_replace;
 }
 
 static bool same_key(pfm_handle* h, const std::string& k) {
@@ -410,7 +410,7 @@ static bool same_solve(const pfm_step_params& a, const pfm_step_params& b) {
   const pfm_solve_opts &x = a.poisson, &y = b.poisson;
   return a.use_midpoint_vel == b.use_midpoint_vel && x.max_iters == y.max_iters && x.eps == y.eps &&
          x.tol == y.tol && x.tol_mode == y.tol_mode && x.precision == y.precision &&
-         x.true_residual_every == y.true_residual_every;
+         x.true_residual_every == y.true_residual_every && x.true_residual_replace == y.true_residual_replace;
 }
 
 // Work-list form of a batch step: every scene's step runs in its own branch up to the setup of a

@@ -30,7 +30,8 @@ class Config(ctypes.Structure):
 class SolveOpts(ctypes.Structure):
     _fields_ = [("max_iters", ctypes.c_int), ("eps", ctypes.c_double), ("tol", ctypes.c_double),
                 ("tol_mode", ctypes.c_int), ("check_every", ctypes.c_int), ("precision", ctypes.c_int),
-                ("warm_start", ctypes.c_int), ("true_residual_every", ctypes.c_int)]
+                ("warm_start", ctypes.c_int), ("true_residual_every", ctypes.c_int),
+                ("true_residual_replace", ctypes.c_int)]
 
 
 class SolveStats(ctypes.Structure):

@@ -318,7 +318,8 @@ class Scene:
         self._check(self.lib.pfm2_update_imp(self.h, _ptr(imp), _ptr(init_imp), _ptr(T), self._stream()))
 
     @staticmethod
-    def _opts(max_iters, tol, tol_mode, check_every, eps=1e-12, precision=0, warm_start=False, true_residual_every=0):
+    def _opts(max_iters, tol, tol_mode, check_every, eps=1e-12, precision=0, warm_start=False, true_residual_every=0,
+              true_residual_replace=False):
         o = SolveOpts()
         o.max_iters, o.eps, o.tol, o.tol_mode, o.check_every = int(max_iters), float(eps), float(tol), int(tol_mode), int(check_every)
         o.precision = {"fp32": 0, "fp16": 1, "bf16": 2}.get(precision, precision)
@@ -327,17 +328,20 @@ class Scene:
         # caller's pressure and the solution before it (the library keeps that one per buffer)
         o.warm_start = 2 if (not isinstance(warm_start, bool) and warm_start == 2) else int(bool(warm_start))
         o.true_residual_every = int(true_residual_every)
+        o.true_residual_replace = int(bool(true_residual_replace))
         return o
 
     def poisson(self, u, p_out=None, max_iters=400, tol=1e-12, tol_mode=0, check_every=4, raise_on_limit=False,
-                precision=0, warm_start=False, true_residual_every=0):
+                precision=0, warm_start=False, true_residual_every=0, true_residual_replace=False):
         """MGPCG_{2,3}.Poisson in place on u (a sync point).  Returns SolveInfo.
 
         ``precision`` "fp32" (0, the reference), "fp16" (1) or "bf16" (2) multigrid level storage;
         ``warm_start`` starts from p_out's current pressure (``warm_start=2``: from the linear
         extrapolation 2 p - p_before of it and the solution before it, which the library keeps per
         p_out buffer, two buffers per scene); ``true_residual_every`` K > 0
-        recomputes r = b - A x every K iterations and before accepting convergence."""
+        recomputes |b - A x| every K iterations and reports it; with ``true_residual_replace`` (FP16/BF16
+        levels) x is kept in FP64 and that residual, formed in FP64, replaces the recursive one every K
+        iterations and before convergence is accepted."""
         u = self._grids(u)
         if p_out is not None:
             self._dev(p_out, "p_out")
@@ -346,7 +350,7 @@ class Scene:
         elif warm_start:
             raise PfmError(1, "warm_start needs p_out (the previous pressure)")
         o = self._opts(max_iters, tol, tol_mode, check_every, precision=precision, warm_start=warm_start,
-                       true_residual_every=true_residual_every)
+                       true_residual_every=true_residual_every, true_residual_replace=true_residual_replace)
         s = SolveStats()
         fn = self.lib.pfm3_poisson if self.dim == 3 else self.lib.pfm2_poisson
         allow = () if raise_on_limit else (_lib.PFM_ERR_NOT_CONVERGED,)
@@ -396,13 +400,13 @@ class Scene:
         return int(n.value)
 
     def mgpcg_solve(self, r, x_out, k=-1.0, max_iters=400, tol=1e-12, tol_mode=0, check_every=4, precision=0,
-                    warm_start=False, true_residual_every=0):
+                    warm_start=False, true_residual_every=0, true_residual_replace=False):
         """MGPCG init(r, k) + solve + get_result: lap(x) = k r (k = -1 for the divergence);
         with warm_start the solve starts from x_out's current values."""
         self._cells(r, "r")
         self._cells(x_out, "x_out")
         o = self._opts(max_iters, tol, tol_mode, check_every, precision=precision, warm_start=warm_start,
-                       true_residual_every=true_residual_every)
+                       true_residual_every=true_residual_every, true_residual_replace=true_residual_replace)
         s = SolveStats()
         st = self._check(self.lib.pfm_mgpcg_solve(self.h, _ptr(r), ctypes.c_float(k), _ptr(x_out), ctypes.byref(o),
                                                   ctypes.byref(s), self._stream()),
@@ -435,7 +439,7 @@ class Scene:
     @staticmethod
     def step_params(CFL=0.5, visualize_dt=0.1, save_frame_each_step=False, reinit_every=20, reinit_every_grad_m=1,
                     use_midpoint_vel=True, reinit_particle_pos=True, max_iters=400, tol=1e-12, tol_mode=0, eps=1e-12,
-                    precision=0, warm_start=False, true_residual_every=0, check_every=4):
+                    precision=0, warm_start=False, true_residual_every=0, check_every=4, true_residual_replace=False):
         """pfm_step_params: the step loop's hyperparameters and the options of both projections."""
         sp = _lib.StepParams()
         sp.CFL, sp.visualize_dt = float(CFL), float(visualize_dt)
@@ -443,7 +447,8 @@ class Scene:
         sp.reinit_every, sp.reinit_every_grad_m = int(reinit_every), int(reinit_every_grad_m)
         sp.use_midpoint_vel, sp.reinit_particle_pos = int(bool(use_midpoint_vel)), int(bool(reinit_particle_pos))
         sp.poisson = Scene._opts(max_iters, tol, tol_mode, check_every, eps=eps, precision=precision,
-                                 warm_start=warm_start, true_residual_every=true_residual_every)
+                                 warm_start=warm_start, true_residual_every=true_residual_every,
+                                 true_residual_replace=true_residual_replace)
         return sp
 
     def step_graph(self, fields, params):

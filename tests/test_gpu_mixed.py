@@ -211,3 +211,49 @@ def test_extrapolated_warm_start_history_per_buffer():
     ib = sc.poisson([torch.from_numpy(x).cuda() for x in u], ps[0], warm_start=2, **kw)
     torch.cuda.synchronize()
     assert ia.iterations == ib.iterations and torch.equal(a, ps[0])
+
+
+@pytest.mark.parametrize("precision", ["fp16", "bf16"])
+def test_true_residual_replacement_against_fp64_oracle(ring64, precision):
+    """true_residual_replace: x accumulates in FP64 and every 5 iterations, and before convergence
+    is accepted, b - A x formed in FP64 replaces the recursive residual and decides.  The solve then
+    stops on its true residual (|b - A x| < tol |b| with the FP64 x), the delivered velocity and
+    pressure stay within 1e-4 of the FP64 oracle, and it takes no fewer iterations than the
+    monitor-only solve of the same field."""
+    res, u, u64, p64 = ring64
+    sc = pfm.Scene(3, res, 1 / 64, 0)
+    ud = [torch.from_numpy(a).cuda() for a in u]
+    p = torch.zeros(res, device="cuda")
+    info = sc.poisson(ud, p, precision=precision, true_residual_replace=True, **OPTS)
+    assert info.converged
+    assert info.rTr < (1e-6) ** 2 * info.bTb  # the deciding residual is the true one
+    got = [t.cpu().numpy() for t in ud]
+    err_u = rel(np.concatenate([g.ravel() for g in got]), np.concatenate([a.ravel() for a in u64]))
+    pg = p.cpu().numpy().astype(np.float64)
+    err_p = rel(pg - pg.mean(), p64 - p64.mean())
+    assert err_u < 1e-4 and err_p < 1e-4, (err_u, err_p)
+    mon = sc.poisson([torch.from_numpy(a).cuda() for a in u], torch.zeros(res, device="cuda"), precision=precision,
+                     **OPTS)
+    assert info.iterations >= mon.iterations
+    print(f"{precision} replacement: iterations {info.iterations} (monitor {mon.iterations}), velocity err "
+          f"{err_u:.2e}, pressure err {err_p:.2e}, true residual {np.sqrt(info.rTr / info.bTb):.2e}")
+
+
+def test_true_residual_replacement_in_the_step_graph_equals_eager():
+    """The replacement solve inside the whole-step graph is bitwise the eager phase calls."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    opts = dict(tol=1e-6, tol_mode=2, max_iters=400, precision="fp16", warm_start=2, true_residual_every=5,
+                true_residual_replace=True)
+    out = []
+    for graph in (True, False):
+        sim = bench.make_sim(48, 2, opts, graph=graph)
+        for _ in range(5):
+            sim.step()
+        torch.cuda.synchronize()
+        out.append([t.clone() for t in sim.u] + [sim.p.clone(), sim.pos.clone()])
+        del sim
+    for a, b in zip(*out):
+        assert torch.equal(a, b)
