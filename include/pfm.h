@@ -139,6 +139,9 @@ int pfm_measure_fp32_peak(float* sink, int blocks_per_sm, int iters, int reps, i
                                      V-cycle in one thread block; 0 = none (4096) */
 #define PFM_TUNE_SMOOTH_TMA 3     /* 1: 3D 16-bit MGPCG levels are smoothed from tiles the TMA stages
                                      in shared memory; 0: from global memory (0) */
+#define PFM_TUNE_CUBE_KERNELS 4   /* 1: on cubic 64^3, 128^3, 256^3 and 512^3 grids the 3D RK4 and
+                                     midpoint kernels run instances compiled for that extent (the
+                                     face-field strides are constants); 0: strides read at run time (1) */
 int pfm_set_tuning(pfm_handle* h, int key, int value);
 int pfm_get_tuning(const pfm_handle* h, int key, int* value);
 

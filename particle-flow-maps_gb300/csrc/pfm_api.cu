@@ -224,6 +224,7 @@ int pfm_create(const pfm_config* cfg, pfm_handle** out) {
   h->p2g2_column = 8;
   h->tail_cells = 4096;
   h->smooth_tma = 0;
+  h->cube_kernels = 1;
   if (cudaHostAlloc((void**)&h->h_state, sizeof(SolveState), cudaHostAllocDefault) != cudaSuccess) {
     cudaGetLastError();
     delete h;
@@ -292,6 +293,9 @@ int pfm_set_tuning(pfm_handle* h, int key, int value) {
   } else if (key == PFM_TUNE_SMOOTH_TMA) {
     if (value != 0 && value != 1) return set_error(h, PFM_ERR_ARG, "smoother staging must be 0 or 1");
     h->smooth_tma = value;
+  } else if (key == PFM_TUNE_CUBE_KERNELS) {
+    if (value != 0 && value != 1) return set_error(h, PFM_ERR_ARG, "cube kernels must be 0 or 1");
+    h->cube_kernels = value;
   } else {
     return set_error(h, PFM_ERR_ARG, "unknown tuning key");
   }
@@ -311,6 +315,7 @@ int pfm_get_tuning(const pfm_handle* h, int key, int* value) {
   if (key == PFM_TUNE_P2G2_COLUMN) *value = h->p2g2_column;
   else if (key == PFM_TUNE_MG_TAIL_CELLS) *value = h->tail_cells;
   else if (key == PFM_TUNE_SMOOTH_TMA) *value = h->smooth_tma;
+  else if (key == PFM_TUNE_CUBE_KERNELS) *value = h->cube_kernels;
   else return PFM_ERR_ARG;
   return PFM_OK;
 }

@@ -5,11 +5,13 @@
 namespace pfm {
 
 constexpr int kGThreads = 128;
-// Resident blocks per SM the 3D midpoint kernel is compiled for: 6 (80 registers, a 4-byte spill)
-// measured 4.39 ms at 256^3 against 4.43-4.86 ms uncapped (88 registers, 5 blocks) and 4.61 ms at
-// 8 (64 registers, spills).
+// Resident blocks per SM the 3D midpoint kernel is compiled for: 5 (94 registers, no spills).  With
+// the strides of a cube grid compiled in (interp_mac3_taps<NC>) it measured 3.90 ms at 256^3
+// against 3.96 ms at 6 (80 registers, a 20-byte spill).  With strides read at run time, 6 measured
+// 4.39 ms against 4.43-4.86 ms uncapped (88 registers, 5 blocks) and 4.61 ms at 8 (64 registers,
+// spills).
 #ifndef PFM_MID_MINB
-#define PFM_MID_MINB 6
+#define PFM_MID_MINB 5
 #endif
 
 // calc_max_speed (3D/run_3D.py:95-103; 2D/run_2D.py:101-108).  Max is order independent, so the
@@ -74,7 +76,8 @@ __global__ void __launch_bounds__(256) k_max_speed(const float* __restrict__ ux,
 // Midpoint for face family `fam` (3D/run_3D.py:106-120, 144-173, 296-312): psi starts at the face
 // centre X_fam (taichi_utils.py:33-46), T at the unit vector e_fam; RK4 over -dt_half with the
 // rows-form gradient (dT/dt = grad u . T); then u1 = T . u0(psi).
-template <int fam>
+// NC: the grid's cube extent when the interpolation is compiled for it (interp_mac3_taps<NC>), else 0.
+template <int fam, int NC>
 __global__ void __launch_bounds__(kGThreads, PFM_MID_MINB) k_midpoint3(MacFields3 F, MacGeom g, float dt_half,
                                                         float* __restrict__ u1, float* __restrict__ psi_out,
                                                         float* __restrict__ T_out,
@@ -99,7 +102,7 @@ __global__ void __launch_bounds__(kGThreads, PFM_MID_MINB) k_midpoint3(MacFields
 #pragma unroll 1
   for (int s = 0; s < 4; ++s) {
     float u[3], G[3][3];
-    interp_mac3(F, g, pk, u, G, true);
+    interp_mac3<NC>(F, g, pk, u, G, true);
     float dT[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) dT[c] = G[c][0] * Tk[0] + G[c][1] * Tk[1] + G[c][2] * Tk[2];
@@ -134,7 +137,7 @@ __global__ void __launch_bounds__(kGThreads, PFM_MID_MINB) k_midpoint3(MacFields
     for (int c = 0; c < 3; ++c) T_out[e * 3 + c] = Tf[c];
   }
   float ua[3], G[3][3];
-  interp_mac3(F, g, pf, ua, G, false);
+  interp_mac3<NC>(F, g, pf, ua, G, false);
   u1[e] = Tf[0] * ua[0] + Tf[1] * ua[1] + Tf[2] * ua[2];
 }
 
@@ -197,6 +200,17 @@ __global__ void __launch_bounds__(kGThreads) k_midpoint2(MacFields2 F, MacGeom g
   u1[e] = Tf[0] * ua[0] + Tf[1] * ua[1];
 }
 
+// k_midpoint3 of face family fam, instantiated for the grid's cube extent when there is one.
+static void launch_midpoint3(pfm_handle* h, int fam, dim3 gr, cudaStream_t st, const MacFields3& F, float dt_half,
+                             float* u1, float* psi_out, float* T_out, const float* dt_half_dev) {
+  with_cube(h, [&](auto nc) {
+    constexpr int NC = decltype(nc)::value;
+    if (fam == 0) launch(h, k_midpoint3<0, NC>, gr, kGThreads, 0, st, F, h->geom, dt_half, u1, psi_out, T_out, dt_half_dev);
+    if (fam == 1) launch(h, k_midpoint3<1, NC>, gr, kGThreads, 0, st, F, h->geom, dt_half, u1, psi_out, T_out, dt_half_dev);
+    if (fam == 2) launch(h, k_midpoint3<2, NC>, gr, kGThreads, 0, st, F, h->geom, dt_half, u1, psi_out, T_out, dt_half_dev);
+  });
+}
+
 // The midpoint kernels of every face family, dt_half from the host value or (dt_half_dev non-null)
 // from device memory.
 int launch_midpoint(pfm_handle* h, const float* const* u0, float* const* u1, float dt_half, const float* dt_half_dev,
@@ -207,12 +221,7 @@ int launch_midpoint(pfm_handle* h, const float* const* u0, float* const* u1, flo
     const dim3 gr(grid_for(nf, kGThreads));
     if (D == 3) {
       const MacFields3 F{{u0[0], u0[1], u0[2]}};
-      if (fam == 0) launch(h, k_midpoint3<0>, gr, kGThreads, 0, st, F, h->geom, dt_half, u1[0], (float*)nullptr,
-                           (float*)nullptr, dt_half_dev);
-      if (fam == 1) launch(h, k_midpoint3<1>, gr, kGThreads, 0, st, F, h->geom, dt_half, u1[1], (float*)nullptr,
-                           (float*)nullptr, dt_half_dev);
-      if (fam == 2) launch(h, k_midpoint3<2>, gr, kGThreads, 0, st, F, h->geom, dt_half, u1[2], (float*)nullptr,
-                           (float*)nullptr, dt_half_dev);
+      launch_midpoint3(h, fam, gr, st, F, dt_half, u1[fam], nullptr, nullptr, dt_half_dev);
     } else {
       const MacFields2 F{{u0[0], u0[1]}};
       if (fam == 0) launch(h, k_midpoint2<0>, gr, kGThreads, 0, st, F, h->geom, dt_half, u1[0], (float*)nullptr,
@@ -277,13 +286,7 @@ int pfm3_midpoint(pfm_handle* h, const float* u0_x, const float* u0_y, const flo
     float* po = psi_out ? psi_out[fam] : nullptr;
     float* to = T_out ? T_out[fam] : nullptr;
     dim3 gr(grid_for(nf, kGThreads));
-    cudaStream_t st = (cudaStream_t)stream;
-    if (fam == 0) launch(h, k_midpoint3<0>, gr, kGThreads, 0, st, F, h->geom, dt_half, outs[fam], po, to,
-                       (const float*)nullptr);
-    if (fam == 1) launch(h, k_midpoint3<1>, gr, kGThreads, 0, st, F, h->geom, dt_half, outs[fam], po, to,
-                       (const float*)nullptr);
-    if (fam == 2) launch(h, k_midpoint3<2>, gr, kGThreads, 0, st, F, h->geom, dt_half, outs[fam], po, to,
-                       (const float*)nullptr);
+    launch_midpoint3(h, fam, gr, (cudaStream_t)stream, F, dt_half, outs[fam], po, to, nullptr);
     int s = launch_check(h, "k_midpoint3");
     if (s) return s;
   }

@@ -7,6 +7,7 @@
 
 #include <atomic>
 #include <string>
+#include <type_traits>
 
 #include "../../include/pfm.h"
 
@@ -141,6 +142,7 @@ struct pfm_handle {
   int p2g2_column;
   int tail_cells;
   int smooth_tma;  // 3D 16-bit MGPCG levels smoothed from TMA-staged tiles (same results)
+  int cube_kernels;  // 3D interpolating kernels instantiated for the grid's cube extent (same results)
   // whole-step graph (pfm3_step / pfm2_step), rebuilt when its fields or parameters change
   cudaGraphExec_t g_step;
   std::string step_key;
@@ -308,17 +310,22 @@ __device__ __forceinline__ void mac_taps3(const MacGeom& g, const float p[3], Ax
 }
 
 // The tap sums of interp_mac3 for taps already computed (two fields of the same shape sampled at
-// one position share them).
+// one position share them).  NC > 0: the grid is NC^3 cells, so the face fields' strides are
+// compile-time constants and every row of a field is its base pointer plus a load immediate (the
+// same loads and sums as NC = 0, which reads the strides from g).
+template <int NC = 0>
 __device__ __forceinline__ void interp_mac3_taps(const MacFields3& F, const MacGeom& g, const Axis3 A0[3],
                                                  const Axis3 A1[3], float uo[3], float G[3][3], bool want_grad);
 
+template <int NC = 0>
 __device__ __forceinline__ void interp_mac3(const MacFields3& F, const MacGeom& g, const float p[3],
                                             float uo[3], float G[3][3], bool want_grad) {
   Axis3 A0[3], A1[3];
   mac_taps3(g, p, A0, A1);
-  interp_mac3_taps(F, g, A0, A1, uo, G, want_grad);
+  interp_mac3_taps<NC>(F, g, A0, A1, uo, G, want_grad);
 }
 
+template <int NC>
 __device__ __forceinline__ void interp_mac3_taps(const MacFields3& F, const MacGeom& g, const Axis3 A0[3],
                                                  const Axis3 A1[3], float uo[3], float G[3][3], bool want_grad) {
   const float inv_dx = g.inv_dx;
@@ -326,7 +333,8 @@ __device__ __forceinline__ void interp_mac3_taps(const MacFields3& F, const MacG
   {
     const float* __restrict__ f0 = F.u[0];
     const float* __restrict__ f1 = F.u[1];
-    const int m01 = g.n[0][1], m02 = g.n[0][2], m11 = g.n[1][1], m12 = g.n[1][2];
+    const int m01 = NC ? NC : g.n[0][1], m02 = NC ? NC : g.n[0][2];
+    const int m11 = NC ? NC + 1 : g.n[1][1], m12 = NC ? NC : g.n[1][2];
     const Axis3& Z = A1[2];
     const float* __restrict__ b0 = f0 + ((A0[0].first * m01 + A1[1].first) * m02 + Z.first);
     const float* __restrict__ b1 = f1 + ((A1[0].first * m11 + A0[1].first) * m12 + Z.first);
@@ -379,7 +387,7 @@ __device__ __forceinline__ void interp_mac3_taps(const MacFields3& F, const MacG
   // ---- component z: (A1x, A1y, A0z)
   {
     const float* __restrict__ f = F.u[2];
-    const int m1 = g.n[2][1], m2 = g.n[2][2];
+    const int m1 = NC ? NC : g.n[2][1], m2 = NC ? NC + 1 : g.n[2][2];
     const Axis3 &X = A1[0], &Y = A1[1], &Z = A0[2];
     const float* __restrict__ base = f + ((X.first * m1 + Y.first) * m2 + Z.first);
     const int sx = m1 * m2;
@@ -412,6 +420,27 @@ __device__ __forceinline__ void interp_mac3_taps(const MacFields3& F, const MacG
       G[2][1] = y_ * inv_dx;
       G[2][2] = z_ * inv_dx;
     }
+  }
+}
+
+// The cube extents the 3D interpolating kernels are instantiated for (interp_mac3_taps<NC>).
+// with_cube(h, f) calls f(std::integral_constant<int, NC>()) with NC the grid's extent when the grid
+// is a cube of one of them (and the handle's PFM_TUNE_CUBE_KERNELS is on), else with NC = 0
+// (strides from the geometry).
+inline int cube_extent(const MacGeom& g) {
+  const int n = g.N[0];
+  if (g.dim != 3 || g.N[1] != n || g.N[2] != n) return 0;
+  return (n == 64 || n == 128 || n == 256 || n == 512) ? n : 0;
+}
+
+template <class Fn>
+inline void with_cube(const pfm_handle* h, Fn&& f) {
+  switch (h->cube_kernels ? cube_extent(h->geom) : 0) {
+    case 64: f(std::integral_constant<int, 64>()); break;
+    case 128: f(std::integral_constant<int, 128>()); break;
+    case 256: f(std::integral_constant<int, 256>()); break;
+    case 512: f(std::integral_constant<int, 512>()); break;
+    default: f(std::integral_constant<int, 0>()); break;
   }
 }
 

@@ -7,9 +7,10 @@ namespace pfm {
 
 constexpr int kPThreads = 128;
 // Block size of the RK4 kernel and the resident blocks per SM it is compiled for.  64 threads x
-// 10 blocks caps it at 96 registers (16 bytes of spills; 20 warps per SM).  Measured at 256^3 (the
-// gradient-reinit + RK4 + records kernel): 128 x 4 (128 registers) 19.2 ms, 128 x 5 18.0 ms,
-// 128 x 6 (80 registers, spills) 18.8 ms, 256 x 2 20.9 ms, 64 x 10 17.6 ms.
+// 10 blocks caps it at 96 registers (20 warps per SM; the cube-extent instances spill 8 bytes, and
+// with a cap of 9 blocks the compiler still picks 96).  Measured at 256^3 (the gradient-reinit +
+// RK4 + records kernel, strides read at run time): 128 x 4 (128 registers) 19.2 ms, 128 x 5
+// 18.0 ms, 128 x 6 (80 registers, spills) 18.8 ms, 256 x 2 20.9 ms, 64 x 10 17.6 ms.
 #ifndef PFM_RK4_MINB
 #define PFM_RK4_MINB 10
 #endif
@@ -91,7 +92,8 @@ __global__ void __launch_bounds__(256) k_reset_T(float* __restrict__ T, int64_t 
 // (3D/run_3D.py:768-772): init_C rows = grad u(p) in the velocity Fg (init_particles_imp_grad_m,
 // as k_g2p3), T_init <- cols(T_gm) @ cols(T_init) (update_T, as k_update_T3) and T_gm <- I, so the
 // RK4 starts from the identity without reading T_gm back.
-template <bool PAY, bool GRADM>
+// NC: the grid's cube extent when the interpolation is compiled for it (interp_mac3_taps<NC>), else 0.
+template <bool PAY, bool GRADM, int NC>
 __global__ void __launch_bounds__(kRK4Threads, PFM_RK4_MINB) k_rk4_T_forward3(float* __restrict__ pos, float* __restrict__ T,
                                                              int64_t P, MacFields3 F, MacGeom g, float dt,
                                                              P2GRecords3 R, MacFields3 Fg,
@@ -109,8 +111,8 @@ __global__ void __launch_bounds__(kRK4Threads, PFM_RK4_MINB) k_rk4_T_forward3(fl
       Axis3 A0[3], A1[3];
       mac_taps3(g, p0, A0, A1);
       float ug[3], Gg[3][3];
-      interp_mac3_taps(Fg, g, A0, A1, ug, Gg, true);
-      interp_mac3_taps(F, g, A0, A1, u, G, true);
+      interp_mac3_taps<NC>(Fg, g, A0, A1, ug, Gg, true);
+      interp_mac3_taps<NC>(F, g, A0, A1, u, G, true);
       float* C = const_cast<float*>(R.C);
 #pragma unroll
       for (int c = 0; c < 3; ++c)
@@ -155,7 +157,7 @@ __global__ void __launch_bounds__(kRK4Threads, PFM_RK4_MINB) k_rk4_T_forward3(fl
   const float half_dt = 0.5f * dt;
 #pragma unroll 1
   for (int s = 0; s < 4; ++s) {
-    if (!GRADM || s > 0) interp_mac3(F, g, pk, u, G, true);
+    if (!GRADM || s > 0) interp_mac3<NC>(F, g, pk, u, G, true);
     float dT[3][3];
 #pragma unroll
     for (int v = 0; v < 3; ++v)
@@ -341,14 +343,18 @@ int launch_rk4_T_forward3(pfm_handle* h, float* pos, float* T, const MacFields3&
                           const MacFields3* Fg, cudaStream_t st, const float* dt_dev) {
   if (h->P == 0) return PFM_OK;
   const unsigned nb = grid_for(h->P, kRK4Threads);
-  if (R && Fg)
-    launch(h, k_rk4_T_forward3<true, true>, nb, kRK4Threads, 0, st, pos, T, h->P, F, h->geom, dt, *R, *Fg, dt_dev);
-  else if (R)
-    launch(h, k_rk4_T_forward3<true, false>, nb, kRK4Threads, 0, st, pos, T, h->P, F, h->geom, dt, *R, MacFields3{},
-           dt_dev);
-  else
-    launch(h, k_rk4_T_forward3<false, false>, nb, kRK4Threads, 0, st, pos, T, h->P, F, h->geom, dt, P2GRecords3{},
-           MacFields3{}, dt_dev);
+  with_cube(h, [&](auto nc) {
+    constexpr int NC = decltype(nc)::value;
+    if (R && Fg)
+      launch(h, k_rk4_T_forward3<true, true, NC>, nb, kRK4Threads, 0, st, pos, T, h->P, F, h->geom, dt, *R, *Fg,
+             dt_dev);
+    else if (R)
+      launch(h, k_rk4_T_forward3<true, false, NC>, nb, kRK4Threads, 0, st, pos, T, h->P, F, h->geom, dt, *R,
+             MacFields3{}, dt_dev);
+    else
+      launch(h, k_rk4_T_forward3<false, false, NC>, nb, kRK4Threads, 0, st, pos, T, h->P, F, h->geom, dt,
+             P2GRecords3{}, MacFields3{}, dt_dev);
+  });
   return launch_check(h, "k_rk4_T_forward3");
 }
 

@@ -181,6 +181,7 @@ SIGNATURES = {
 TUNE_P2G2_COLUMN = 1
 TUNE_MG_TAIL_CELLS = 2
 TUNE_SMOOTH_TMA = 3
+TUNE_CUBE_KERNELS = 4
 # scratch limits of pfm_sort_particles_noalloc (include/pfm.h)
 NOALLOC_MAX_PARTICLES = 1 << 21
 NOALLOC_MAX_CELLS = 1 << 18

@@ -85,3 +85,27 @@ def test_gradm_rk4_records_matches_separate_calls():
         assert torch.equal(a[k], b[k]), k
     for f in range(3):
         assert torch.equal(oa[f], ob[f]) and torch.equal(wa[f], wb[f]), f
+
+
+@pytest.mark.parametrize("n", [64, 128])
+def test_cube_instances_equal_runtime_strides(n):
+    """PFM_TUNE_CUBE_KERNELS: on an n^3 grid the RK4 kernels (with and without the gradient
+    reinitialisation) and the midpoint kernels run instances compiled for the extent n; with the
+    tunable off they read the strides at run time.  Same loads and sums: bitwise equal outputs."""
+    from pfm import _lib
+    sc, u, st = _scene(res=(n, n, n), ppc=1, seed=11)
+    rng = np.random.default_rng(12)
+    ua = [torch.from_numpy((0.3 * rng.standard_normal(s)).astype(np.float32)).cuda() for s in sc.face_shapes]
+    dt = 0.4 / n
+    outs = []
+    for cube in (1, 0):
+        sc.set_tuning(_lib.TUNE_CUBE_KERNELS, cube)
+        a, b = _clone(st), _clone(st)
+        sc.gradm_rk4_records3(a["pos"], a["T_gm"], a["T_init"], a["init_C"], a["init_imp"], u, ua, dt)
+        sc.rk4_T_forward(b["pos"], b["T_gm"], ua, dt)
+        mid = sc.alloc_faces()
+        sc.midpoint(u, mid, 0.5 * dt)
+        torch.cuda.synchronize()
+        outs.append([a[k] for k in ("pos", "T_gm", "T_init", "init_C")] + [b["pos"], b["T_gm"]] + list(mid))
+    for x, y in zip(*outs):
+        assert torch.equal(x, y)
