@@ -16,6 +16,9 @@ namespace pfm {
 constexpr int kMaxLevels = 16;
 constexpr int kReduceBlocks = 1024;  // fixed partition of every deterministic reduction
 constexpr int kReduceThreads = 256;
+// The reduction kernels are compiled for 8 resident blocks per SM (at most 32 registers), so the
+// 1024 blocks of the partition run in one wave on GB300's 152 SMs instead of 912 + 112.
+constexpr int kReduceResident = 8;
 constexpr int kScanItems = 8;        // items per thread in the cell-count scan
 constexpr int kScanThreads = 1024;
 

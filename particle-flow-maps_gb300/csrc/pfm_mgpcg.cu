@@ -319,6 +319,19 @@ __device__ __forceinline__ void st8h(H* p, const float (&v)[8]) {
   for (int q = 0; q < 8; ++q) stv(h + q, v[q]);
   *reinterpret_cast<uint4*>(p) = u;
 }
+__device__ __forceinline__ void ld4(const float* p, float (&v)[4]) {
+  const float4 a = *reinterpret_cast<const float4*>(p);
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+}
+template <typename H>
+__device__ __forceinline__ void ld4h(const H* p, float (&v)[4]) {
+  const uint2 u = *reinterpret_cast<const uint2*>(p);
+  const H* h = reinterpret_cast<const H*>(&u);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) v[q] = ldv(h + q);
+}
+__device__ __forceinline__ void ld4(const __half* p, float (&v)[4]) { ld4h(p, v); }
+__device__ __forceinline__ void ld4(const __nv_bfloat16* p, float (&v)[4]) { ld4h(p, v); }
 __device__ __forceinline__ void ld8(const __half* p, float (&v)[8]) { ld8h(p, v); }
 __device__ __forceinline__ void ld8(const __nv_bfloat16* p, float (&v)[8]) { ld8h(p, v); }
 __device__ __forceinline__ void st8(__half* p, const float (&v)[8]) { st8h(p, v); }
@@ -410,7 +423,12 @@ struct OpSmooth8 {
 };
 
 template <typename S>
-__global__ void __launch_bounds__(256) k_smooth8(S* __restrict__ z, const S* __restrict__ r, Lvl L, BC bc,
+// Compiled for 4 resident blocks per SM (64 registers, a 16-byte spill) instead of the 3 that its
+// 71 registers allowed: 3.51 against 3.65 ms for a 3-iteration 256^3 FP16-level solve.
+#ifndef PFM_SMOOTH8_MINB
+#define PFM_SMOOTH8_MINB 4
+#endif
+__global__ void __launch_bounds__(256, PFM_SMOOTH8_MINB) k_smooth8(S* __restrict__ z, const S* __restrict__ r, Lvl L, BC bc,
                                                  int phase, const SolveState* st, int fresh) {
   smooth8_blk<S>(z, r, L, bc, phase, st, blockIdx.x, fresh != 0);
 }
@@ -536,6 +554,88 @@ __device__ __forceinline__ void restrict_blk(const S* __restrict__ zf, const S* 
   stv(rc + e, acc);
 }
 
+// The same restriction in 3D with one thread per run of four coarse cells along the last axis:
+// each of the 2 x 2 fine rows under them is read as whole 8-element vectors (z, r and the four
+// neighbouring rows) and its eight residuals are formed as stencil<3> forms them (the same
+// neighbour order); each coarse cell sums its eight in restrict_blk's order.  Needs Lf.n2 % 8 == 0.
+template <typename S>
+__device__ __forceinline__ void restrict8_blk(const S* __restrict__ zf, const S* __restrict__ rf, const Lvl& Lf,
+                                              S* __restrict__ rc, const Lvl& Lc, const BC& bc, const SolveState* st,
+                                              unsigned bid) {
+  if (st && st->done) return;
+  const int runs = Lc.n2 >> 2;
+  const unsigned e = bid * blockDim.x + threadIdx.x;
+  if ((int64_t)e >= (int64_t)Lc.n0 * Lc.n1 * runs) return;
+  const unsigned row = e / (unsigned)runs;
+  const int K0 = (int)(e - row * (unsigned)runs) * 4;
+  const unsigned I_ = udiv(row, Lc.d1);
+  const int I = (int)I_, J = (int)(row - I_ * (unsigned)Lc.n1);
+  const int k0 = 2 * K0;
+  const int64_t sx = (int64_t)Lf.n1 * Lf.n2, sy = Lf.n2;
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  const float den = 2.0f;
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+      const int i = 2 * I + a, j = 2 * J + b;
+      if (i >= Lf.n0 || j >= Lf.n1) continue;
+      const int64_t c0 = ((int64_t)i * Lf.n1 + j) * Lf.n2 + k0;
+      float zc[8], rr[8], xp[8], xm[8], yp[8], ym[8];
+      ld8(zf + c0, zc);
+      ld8(rf + c0, rr);
+      const bool hx = i < Lf.n0 - 1, lx = i > 0, hy = j < Lf.n1 - 1, ly = j > 0;
+      if (hx) ld8(zf + c0 + sx, xp);
+      if (lx) ld8(zf + c0 - sx, xm);
+      if (hy) ld8(zf + c0 + sy, yp);
+      if (ly) ld8(zf + c0 - sy, ym);
+      const float zl = k0 > 0 ? ldv(zf + c0 - 1) : 0.f;
+      const float zr = k0 + 8 < Lf.n2 ? ldv(zf + c0 + 8) : 0.f;
+      float base = 6.f;
+      if (i <= 0 && bc.lo[0] == 2) base -= 1.f;
+      if (i >= Lf.n0 - 1 && bc.hi[0] == 2) base -= 1.f;
+      if (j <= 0 && bc.lo[1] == 2) base -= 1.f;
+      if (j >= Lf.n1 - 1 && bc.hi[1] == 2) base -= 1.f;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int k = k0 + q;
+        float nb = 0.f;
+        if (hx) nb += xp[q];
+        if (lx) nb += xm[q];
+        if (hy) nb += yp[q];
+        if (ly) nb += ym[q];
+        if (k < Lf.n2 - 1) nb += (q < 7) ? zc[q + 1] : zr;
+        if (k > 0) nb += (q > 0) ? zc[q - 1] : zl;
+        float mult = base;
+        if (k <= 0 && bc.lo[2] == 2) mult -= 1.f;
+        if (k >= Lf.n2 - 1 && bc.hi[2] == 2) mult -= 1.f;
+        const float res = rr[q] - (mult * zc[q] - nb);
+        acc[q >> 1] += res * 1.0f / den;
+      }
+    }
+  const int64_t cc = ((int64_t)I * Lc.n1 + J) * Lc.n2 + K0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) stv(rc + cc + q, acc[q]);
+}
+
+template <typename S>
+struct OpRestrict8 {
+  const S* zf;
+  const S* rf;
+  Lvl Lf;
+  S* rc;
+  Lvl Lc;
+  BC bc;
+  const SolveState* st;
+  __device__ __forceinline__ void run(unsigned bid, unsigned) const { restrict8_blk<S>(zf, rf, Lf, rc, Lc, bc, st, bid); }
+};
+
+template <typename S>
+__global__ void __launch_bounds__(256) k_restrict8(const S* __restrict__ zf, const S* __restrict__ rf, Lvl Lf,
+                                                   S* __restrict__ rc, Lvl Lc, BC bc, const SolveState* st) {
+  restrict8_blk<S>(zf, rf, Lf, rc, Lc, bc, st, blockIdx.x);
+}
+
 template <int D, typename S>
 struct OpRestrict {
   const S* zf;
@@ -583,6 +683,46 @@ template <int D, typename S>
 __global__ void __launch_bounds__(256) k_prolong(S* __restrict__ zf, Lvl Lf, const S* __restrict__ zc,
                                                  Lvl Lc, const SolveState* st) {
   prolong_blk<D, S>(zf, Lf, zc, Lc, st, blockIdx.x);
+}
+
+// The same update in 3D with one thread per run of eight fine cells along the last axis (whole
+// 8-element vectors of z_l, the four coarse cells under them as one vector of z_{l+1}); needs
+// Lf.n2 % 8 == 0.  Element for element the sum of prolong_blk.
+template <typename S>
+__device__ __forceinline__ void prolong8_blk(S* __restrict__ zf, const Lvl& Lf, const S* __restrict__ zc,
+                                             const Lvl& Lc, const SolveState* st, unsigned bid) {
+  if (st && st->done) return;
+  const int runs = Lf.n2 >> 3;
+  const unsigned e = bid * blockDim.x + threadIdx.x;
+  if ((int64_t)e >= (int64_t)Lf.n0 * Lf.n1 * runs) return;
+  const unsigned row = e / (unsigned)runs;
+  const int k0 = (int)(e - row * (unsigned)runs) * 8;
+  const unsigned i_ = udiv(row, Lf.d1);
+  const int i = (int)i_, j = (int)(row - i_ * (unsigned)Lf.n1);
+  const int64_t c0 = ((int64_t)i * Lf.n1 + j) * Lf.n2 + k0;
+  const int64_t cc = ((int64_t)(i >> 1) * Lc.n1 + (j >> 1)) * Lc.n2 + (k0 >> 1);
+  float a[8], out[8], b[4];
+  ld8(zf + c0, a);
+  ld4(zc + cc, b);
+#pragma unroll
+  for (int q = 0; q < 8; ++q) out[q] = a[q] + b[q >> 1];
+  st8(zf + c0, out);
+}
+
+template <typename S>
+struct OpProlong8 {
+  S* zf;
+  Lvl Lf;
+  const S* zc;
+  Lvl Lc;
+  const SolveState* st;
+  __device__ __forceinline__ void run(unsigned bid, unsigned) const { prolong8_blk<S>(zf, Lf, zc, Lc, st, bid); }
+};
+
+template <typename S>
+__global__ void __launch_bounds__(256) k_prolong8(S* __restrict__ zf, Lvl Lf, const S* __restrict__ zc, Lvl Lc,
+                                                  const SolveState* st) {
+  prolong8_blk<S>(zf, Lf, zc, Lc, st, blockIdx.x);
 }
 
 // init(r, k) (3D/mgpcg.py:71-79): r0 = r * k
@@ -701,7 +841,7 @@ struct OpDot {
 };
 
 template <typename SA>
-__global__ void __launch_bounds__(kReduceThreads) k_dot(const SA* __restrict__ a, const float* __restrict__ b,
+__global__ void __launch_bounds__(kReduceThreads, kReduceResident) k_dot(const SA* __restrict__ a, const float* __restrict__ b,
                                                         int64_t n, RedBuf rb, int kind, double eps, double inv_n,
                                                         int max_iters, int f64) {
   dot_blk<SA>(a, b, n, rb, kind, eps, inv_n, max_iters, f64, blockIdx.x, gridDim.x);
@@ -802,7 +942,7 @@ struct OpApDot {
 };
 
 template <int D>
-__global__ void __launch_bounds__(kReduceThreads) k_Ap_dot(const float* __restrict__ p, float* __restrict__ Ap,
+__global__ void __launch_bounds__(kReduceThreads, kReduceResident) k_Ap_dot(const float* __restrict__ p, float* __restrict__ Ap,
                                                            Lvl L, BC bc, RedBuf rb, double eps, int f64) {
   Ap_dot_blk<D>(p, Ap, L, bc, rb, eps, f64, blockIdx.x, gridDim.x);
 }
@@ -860,7 +1000,7 @@ struct OpUpdateXr {
   }
 };
 
-__global__ void __launch_bounds__(kReduceThreads) k_update_xr(float* __restrict__ x, const float* __restrict__ p,
+__global__ void __launch_bounds__(kReduceThreads, kReduceResident) k_update_xr(float* __restrict__ x, const float* __restrict__ p,
                                                               float* __restrict__ r, const float* __restrict__ Ap,
                                                               int64_t n, RedBuf rb, double tol, int tol_mode,
                                                               int f64, double inv_n, double* x64) {
@@ -987,14 +1127,14 @@ struct OpTrueResidual {
 };
 
 template <int D>
-__global__ void __launch_bounds__(kReduceThreads) k_true_residual(const float* __restrict__ b,
+__global__ void __launch_bounds__(kReduceThreads, kReduceResident) k_true_residual(const float* __restrict__ b,
                                                                   const float* __restrict__ x, Lvl L, BC bc,
                                                                   RedBuf rb, int every) {
   true_residual_blk<D>(b, x, L, bc, rb, every, blockIdx.x, gridDim.x);
 }
 
 template <int D>
-__global__ void __launch_bounds__(kReduceThreads) k_true_residual_replace(const float* __restrict__ b,
+__global__ void __launch_bounds__(kReduceThreads, kReduceResident) k_true_residual_replace(const float* __restrict__ b,
                                                                           const double* __restrict__ x64,
                                                                           float* __restrict__ r, Lvl L, BC bc,
                                                                           RedBuf rb, int every, double tol,
@@ -1254,9 +1394,11 @@ static unsigned red_blocks(int64_t n) {
   return b > (unsigned)kReduceBlocks ? (unsigned)kReduceBlocks : b;
 }
 
+// Elementwise kernels: one wave of 8 resident 256-thread blocks per SM (every block loops over an
+// equal share, so no partial last wave idles most of the GPU).
 static unsigned stream_blocks(int64_t n) {
   unsigned b = grid_for(n, 256);
-  return b > 152u * 16u ? 152u * 16u : b;
+  return b > 152u * 8u ? 152u * 8u : b;
 }
 
 // Level l's z and r in storage S.  Level 0's r is the PCG residual in the FP32 solve; the mixed
@@ -1380,8 +1522,12 @@ static void vcycle(pfm_handle* h, const SolveState* st, cudaStream_t s) {
     flush(l);  // the restriction reads z_l
     if (l + 1 != l0) zero_first[l + 1] = true;
     Lvl Lf = lvl_of(h, l), Lc = lvl_of(h, l + 1);
-    launch(h, k_restrict<D, S>, grid_for(Lc.count, 256), 256, 0, s, (const S*)level_z<S>(h, l),
-           (const S*)level_r<S>(h, l), Lf, level_r<S>(h, l + 1), Lc, bc, st);
+    if (D == 3 && Lf.n2 % 8 == 0)
+      launch(h, k_restrict8<S>, grid_for((int64_t)Lc.n0 * Lc.n1 * (Lc.n2 / 4), 256), 256, 0, s,
+             (const S*)level_z<S>(h, l), (const S*)level_r<S>(h, l), Lf, level_r<S>(h, l + 1), Lc, bc, st);
+    else
+      launch(h, k_restrict<D, S>, grid_for(Lc.count, 256), 256, 0, s, (const S*)level_z<S>(h, l),
+             (const S*)level_r<S>(h, l), Lf, level_r<S>(h, l + 1), Lc, bc, st);
   }
   if (l0 < L) {
     TailPlan T{};
@@ -1409,8 +1555,12 @@ static void vcycle(pfm_handle* h, const SolveState* st, cudaStream_t s) {
     Lvl Lf = lvl_of(h, l), Lc = lvl_of(h, l + 1);
     flush(l);  // the prolongation reads z_l and z_{l+1}
     flush(l + 1);
-    launch(h, k_prolong<D, S>, grid_for(Lf.count, 256), 256, 0, s, level_z<S>(h, l), Lf, (const S*)level_z<S>(h, l + 1),
-           Lc, st);
+    if (D == 3 && Lf.n2 % 8 == 0)
+      launch(h, k_prolong8<S>, grid_for((int64_t)Lf.n0 * Lf.n1 * (Lf.n2 / 8), 256), 256, 0, s, level_z<S>(h, l), Lf,
+             (const S*)level_z<S>(h, l + 1), Lc, st);
+    else
+      launch(h, k_prolong<D, S>, grid_for(Lf.count, 256), 256, 0, s, level_z<S>(h, l), Lf,
+             (const S*)level_z<S>(h, l + 1), Lc, st);
     for (int i = 0; i < h->cfg.pre_post_smoothing; ++i) {
       smooth_launch<D, S>(h, l, 1, st, s);
       smooth_launch<D, S>(h, l, 0, st, s);
