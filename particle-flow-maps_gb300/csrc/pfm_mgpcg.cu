@@ -341,6 +341,21 @@ __device__ __forceinline__ void st8(__nv_bfloat16* p, const float (&v)[8]) { st8
 // and the four neighbouring runs are read as whole vectors (the cells of the other colour, which a
 // half-sweep never changes, are written back unchanged) and each cell of the colour is updated
 // with the same sum, in the same order, as stencil<3> -- bitwise the result of k_smooth.
+// Eight consecutive elements of a level vector as loaded (16-bit storage: one 16-byte word, four
+// registers; f32: eight), converted to f32 element by element where they are used.
+template <typename S>
+struct Raw8 {
+  uint4 u;
+  __device__ __forceinline__ void load(const S* p) { u = *reinterpret_cast<const uint4*>(p); }
+  __device__ __forceinline__ float operator[](int q) const { return ldv(reinterpret_cast<const S*>(&u) + q); }
+};
+template <>
+struct Raw8<float> {
+  float v[8];
+  __device__ __forceinline__ void load(const float* p) { ld8(p, v); }
+  __device__ __forceinline__ float operator[](int q) const { return v[q]; }
+};
+
 template <typename S>
 __device__ __forceinline__ void smooth8_blk(S* __restrict__ z, const S* __restrict__ r, const Lvl& L, const BC& bc,
                                             int phase, const SolveState* st, unsigned bid, bool fresh = false) {
@@ -354,16 +369,16 @@ __device__ __forceinline__ void smooth8_blk(S* __restrict__ z, const S* __restri
   const int i = (int)i_, j = (int)(row - i_ * (unsigned)L.n1);
   const int64_t sx = (int64_t)L.n1 * L.n2, sy = L.n2;
   const int64_t c0 = ((int64_t)i * L.n1 + j) * L.n2 + k0;
-  float zc[8], rr[8], xp[8], xm[8], yp[8], ym[8];
-  ld8(r + c0, rr);
+  Raw8<S> rr, zc, xp, xm, yp, ym;
+  rr.load(r + c0);
+  float base = 6.f;
+  if (i <= 0 && bc.lo[0] == 2) base -= 1.f;
+  if (i >= L.n0 - 1 && bc.hi[0] == 2) base -= 1.f;
+  if (j <= 0 && bc.lo[1] == 2) base -= 1.f;
+  if (j >= L.n1 - 1 && bc.hi[1] == 2) base -= 1.f;
+  const int first = (i + j + k0 + phase) & 1;  // run offset of the first cell of the colour
+  float out[8];
   if (fresh) {  // z starts at zero: the colour gets (r + 0) / mult, the other colour zero
-    float base = 6.f;
-    if (i <= 0 && bc.lo[0] == 2) base -= 1.f;
-    if (i >= L.n0 - 1 && bc.hi[0] == 2) base -= 1.f;
-    if (j <= 0 && bc.lo[1] == 2) base -= 1.f;
-    if (j >= L.n1 - 1 && bc.hi[1] == 2) base -= 1.f;
-    const int first = (i + j + k0 + phase) & 1;
-    float out[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
       const int k = k0 + q;
@@ -375,25 +390,17 @@ __device__ __forceinline__ void smooth8_blk(S* __restrict__ z, const S* __restri
     st8(z + c0, out);
     return;
   }
-  ld8(z + c0, zc);
+  zc.load(z + c0);
   const bool hx = i < L.n0 - 1, lx = i > 0, hy = j < L.n1 - 1, ly = j > 0;
-  if (hx) ld8(z + c0 + sx, xp);
-  if (lx) ld8(z + c0 - sx, xm);
-  if (hy) ld8(z + c0 + sy, yp);
-  if (ly) ld8(z + c0 - sy, ym);
+  if (hx) xp.load(z + c0 + sx);
+  if (lx) xm.load(z + c0 - sx);
+  if (hy) yp.load(z + c0 + sy);
+  if (ly) ym.load(z + c0 - sy);
   const float zl = k0 > 0 ? ldv(z + c0 - 1) : 0.f;
   const float zr = k0 + 8 < L.n2 ? ldv(z + c0 + 8) : 0.f;
-  float base = 6.f;
-  if (i <= 0 && bc.lo[0] == 2) base -= 1.f;
-  if (i >= L.n0 - 1 && bc.hi[0] == 2) base -= 1.f;
-  if (j <= 0 && bc.lo[1] == 2) base -= 1.f;
-  if (j >= L.n1 - 1 && bc.hi[1] == 2) base -= 1.f;
-  const int first = (i + j + k0 + phase) & 1;  // run offset of the first cell of the colour
-  float out[8];
-#pragma unroll
-  for (int q = 0; q < 8; ++q) out[q] = zc[q];
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
+    out[q] = zc[q];
     if ((q & 1) != first) continue;
     const int k = k0 + q;
     float ret = 0.f;
@@ -422,13 +429,16 @@ struct OpSmooth8 {
   __device__ __forceinline__ void run(unsigned bid, unsigned) const { smooth8_blk<S>(z, r, L, bc, phase, st, bid); }
 };
 
-template <typename S>
-// Compiled for 4 resident blocks per SM (64 registers, a 16-byte spill) instead of the 3 that its
-// 71 registers allowed: 3.51 against 3.65 ms for a 3-iteration 256^3 FP16-level solve.
-#ifndef PFM_SMOOTH8_MINB
-#define PFM_SMOOTH8_MINB 4
+// Resident blocks per SM the smoother is compiled for: f32 levels 3 (72 registers, no spill),
+// 16-bit levels PFM_SMOOTH8_MINB16.
+#ifndef PFM_SMOOTH8_MINB16
+#define PFM_SMOOTH8_MINB16 4
 #endif
-__global__ void __launch_bounds__(256, PFM_SMOOTH8_MINB) k_smooth8(S* __restrict__ z, const S* __restrict__ r, Lvl L, BC bc,
+template <typename S>
+constexpr int smooth8_min_blocks() { return sizeof(S) == 2 ? PFM_SMOOTH8_MINB16 : 3; }
+
+template <typename S>
+__global__ void __launch_bounds__(256, smooth8_min_blocks<S>()) k_smooth8(S* __restrict__ z, const S* __restrict__ r, Lvl L, BC bc,
                                                  int phase, const SolveState* st, int fresh) {
   smooth8_blk<S>(z, r, L, bc, phase, st, blockIdx.x, fresh != 0);
 }
