@@ -211,7 +211,7 @@ int pfm_create(const pfm_config* cfg, pfm_handle** out) {
   h->o_p = take(C * 4);
   h->o_Ap = take(C * 4);
   h->o_b = take(C * 4);  // recentred right-hand side (warm start, true residual, tol_mode 2)
-  h->o_partials = take(kReduceBlocks * sizeof(double));
+  h->o_partials = take(2 * kReduceBlocks * sizeof(double));  // two reductions in one pass (grid_sum2)
   h->o_state = take(sizeof(SolveState));
   h->o_maxpart = take(kReduceBlocks * sizeof(float) + 256);
   h->o_step = take(sizeof(StepCtl));

@@ -149,8 +149,65 @@ __device__ bool grid_sum(double v, double* partials, unsigned* ticket, double* t
   return true;
 }
 
+// Two sums of the same partition at once: each is reduced exactly as grid_sum reduces it (the
+// same warp trees, block order and final combination), the second through partials[nb ..).
+__device__ bool grid_sum2(double v0, double v1, double* partials, unsigned* ticket, double* total0, double* total1,
+                          unsigned bid, unsigned nb) {
+  __shared__ double ws[2][32];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  v0 = warp_sum(v0);
+  v1 = warp_sum(v1);
+  if (lane == 0) {
+    ws[0][wid] = v0;
+    ws[1][wid] = v1;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    double b0 = lane < (int)(blockDim.x >> 5) ? ws[0][lane] : 0.0;
+    double b1 = lane < (int)(blockDim.x >> 5) ? ws[1][lane] : 0.0;
+    b0 = warp_sum(b0);
+    b1 = warp_sum(b1);
+    if (lane == 0) {
+      partials[bid] = b0;
+      partials[nb + bid] = b1;
+      __threadfence();
+      unsigned t = atomicAdd(ticket, 1u);
+      last = (t == nb - 1);
+    }
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  double s0 = 0.0, s1 = 0.0;
+  for (int b = threadIdx.x; b < (int)nb; b += blockDim.x) {
+    s0 += ((volatile double*)partials)[b];
+    s1 += ((volatile double*)partials)[nb + b];
+  }
+  s0 = warp_sum(s0);
+  s1 = warp_sum(s1);
+  __syncthreads();  // every thread is done reading ws before it is reused
+  if (lane == 0) {
+    ws[0][wid] = s0;
+    ws[1][wid] = s1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t0 = 0.0, t1 = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      t0 += ws[0][w];
+      t1 += ws[1][w];
+    }
+    *total0 = t0;
+    *total1 = t1;
+    *ticket = 0u;
+  }
+  __syncthreads();
+  return true;
+}
+
 struct RedBuf {
-  double* partials;
+  double* partials;  // 2 x kReduceBlocks
   SolveState* st;
 };
 
@@ -960,15 +1017,17 @@ __global__ void __launch_bounds__(kReduceThreads, kReduceResident) k_Ap_dot(cons
 // update_x, update_r, reduce(r, r) and the convergence test (3D/mgpcg.py:243-258).  With x64
 // (the residual-replacement solve) x accumulates in FP64 and a passing test only marks the solve
 // for verification (done = 5): k_true_residual, next in the iteration, decides on the true residual.
+// With want_mean the pass also sums the new r for the next recenter (sum(r) / n into st->mean),
+// accumulated and reduced exactly as dot_blk's RED_MEAN pass over the same r would: the same mean.
 __device__ __forceinline__ void update_xr_blk(float* __restrict__ x, const float* __restrict__ p, float* __restrict__ r,
                                               const float* __restrict__ Ap, int64_t n, RedBuf rb, double tol,
                                               int tol_mode, int f64, double inv_n, unsigned bid, unsigned nb,
-                                              double* __restrict__ x64 = nullptr) {
+                                              double* __restrict__ x64 = nullptr, bool want_mean = false) {
   SolveState* st = rb.st;
   if (st->done) return;
   const float alpha = st->alpha;
-  float acc = 0.f;
-  CompSum cacc;
+  float acc = 0.f, macc = 0.f;
+  CompSum cacc, cmacc;
   for (int64_t e = (int64_t)bid * blockDim.x + threadIdx.x; e < n; e += (int64_t)nb * blockDim.x) {
     if (x64)
       x64[e] = fma((double)alpha, (double)p[e], x64[e]);
@@ -976,12 +1035,24 @@ __device__ __forceinline__ void update_xr_blk(float* __restrict__ x, const float
       x[e] += alpha * p[e];
     float re = r[e] - alpha * Ap[e];
     r[e] = re;
-    if (f64) cacc.add(re * re);
-    else acc += re * re;
+    if (f64) {
+      cacc.add(re * re);
+      if (want_mean) cmacc.add(re);
+    } else {
+      acc += re * re;
+      if (want_mean) macc += re;
+    }
   }
-  double total;
-  if (!grid_sum(f64 ? cacc.value() : (double)acc, rb.partials, &st->ticket, &total, bid, nb)) return;
+  double total, tmean = 0.0;
+  if (want_mean) {
+    if (!grid_sum2(f64 ? cacc.value() : (double)acc, f64 ? cmacc.value() * 1.0 : (double)macc, rb.partials,
+                   &st->ticket, &total, &tmean, bid, nb))
+      return;
+  } else if (!grid_sum(f64 ? cacc.value() : (double)acc, rb.partials, &st->ticket, &total, bid, nb)) {
+    return;
+  }
   if (threadIdx.x == 0) {
+    if (want_mean) st->mean = (float)(tmean * inv_n);
     st->rTr = total;
     if (total > 0.0) st->hscale = (float)(1.0 / sqrt(total * inv_n));
     if (!isfinite(total)) {
@@ -1013,8 +1084,8 @@ struct OpUpdateXr {
 __global__ void __launch_bounds__(kReduceThreads, kReduceResident) k_update_xr(float* __restrict__ x, const float* __restrict__ p,
                                                               float* __restrict__ r, const float* __restrict__ Ap,
                                                               int64_t n, RedBuf rb, double tol, int tol_mode,
-                                                              int f64, double inv_n, double* x64) {
-  update_xr_blk(x, p, r, Ap, n, rb, tol, tol_mode, f64, inv_n, blockIdx.x, gridDim.x, x64);
+                                                              int f64, double inv_n, double* x64, int want_mean) {
+  update_xr_blk(x, p, r, Ap, n, rb, tol, tol_mode, f64, inv_n, blockIdx.x, gridDim.x, x64, want_mean != 0);
 }
 
 // FP32 <-> FP64 copies of x for the residual-replacement solve
@@ -1642,6 +1713,9 @@ struct SolveKernels {
   pfm_handle* h;
   pfm_solve_opts o;
   bool mixed, warm, true_res, keep_b, neu, replace;
+  // the next recenter's mean is summed by k_update_xr (all-Neumann; not when the true-residual
+  // replacement rewrites r after it)
+  bool fuse_mean;
   int f64, chunk, mi;
   int64_t n;
   double inv_n;
@@ -1665,6 +1739,7 @@ struct SolveKernels {
     n = h->cells;
     inv_n = 1.0 / (double)n;
     neu = all_neumann(h);
+    fuse_mean = neu && !replace;
     st = ws_ptr<SolveState>(h, h->o_state);
     rb = RedBuf{ws_ptr<double>(h, h->o_partials), st};
     r0 = ws_ptr<float>(h, h->o_r[0]);
@@ -1679,12 +1754,13 @@ struct SolveKernels {
     bc = bc_of(h);
   }
   // recenter r0 (all-Neumann) and, in the mixed solve with `storage`, refresh its scaled
-  // level-storage copy
-  void recenter(cudaStream_t q, bool storage) {
+  // level-storage copy.  With mean_ready the mean was summed by the k_update_xr that wrote r0.
+  void recenter(cudaStream_t q, bool storage, bool mean_ready = false) {
     S* out = (mixed && storage) ? rh : nullptr;
     if (neu) {
-      launch(h, k_dot<float>, red_blocks(n), kReduceThreads, 0, q, (const float*)r0, (const float*)nullptr, n, rb,
-             (int)RED_MEAN, o.eps, inv_n, mi, f64);
+      if (!mean_ready)
+        launch(h, k_dot<float>, red_blocks(n), kReduceThreads, 0, q, (const float*)r0, (const float*)nullptr, n, rb,
+               (int)RED_MEAN, o.eps, inv_n, mi, f64);
       launch(h, k_sub_mean<S>, stream_blocks(n), 256, 0, q, r0, out, n, (const SolveState*)st);
     } else if (out) {
       launch(h, k_to_storage<S>, stream_blocks(n), 256, 0, q, out, (const float*)r0, n, (const SolveState*)st);
@@ -1693,7 +1769,7 @@ struct SolveKernels {
   void first_half(cudaStream_t q) {
     launch(h, k_Ap_dot<D>, red_blocks(n), kReduceThreads, 0, q, (const float*)p, Ap, L0, bc, rb, o.eps, f64);
     launch(h, k_update_xr, red_blocks(n), kReduceThreads, 0, q, x, (const float*)p, r0, (const float*)Ap, n, rb, o.tol,
-           o.tol_mode, f64, inv_n, x64);
+           o.tol_mode, f64, inv_n, x64, fuse_mean ? 1 : 0);
     if (replace)
       launch(h, k_true_residual_replace<D>, red_blocks(n), kReduceThreads, 0, q, (const float*)bvec,
              (const double*)x64, r0, L0, bc, rb, o.true_residual_every, o.tol, o.tol_mode, inv_n);
@@ -1726,7 +1802,7 @@ struct SolveKernels {
     first_half(q);
   }
   void body(cudaStream_t q, cudaGraphConditionalHandle cond) {
-    recenter(q, true);
+    recenter(q, true, fuse_mean);
     vcycle<D, S>(h, st, q);
     launch(h, k_dot<S>, red_blocks(n), kReduceThreads, 0, q, (const S*)z0, (const float*)r0, n, rb, (int)RED_ZTR, o.eps,
            inv_n, mi, f64);
