@@ -449,7 +449,8 @@ inline void with_cube(const pfm_handle* h, Fn&& f) {
 
 // P2G particle record and cell key (3D), shared by the payload pass and the fused RK4 + P2G:
 //   pos4[q]      = (pos/dx, 0)
-//   famrec[f][q] = (m_f, (T C T)_f row), m = T_gm^T-composed init_imp, T C T = T_gm^T init_C T_gm
+//   famrec[f][q] = (m_f, dx (T C T)_f row), m = T_gm^T-composed init_imp, T C T = T_gm^T init_C T_gm
+//                  (the row pre-scaled by dx: the tiles take face offsets in grid units)
 //                  (3D/run_3D.py:462-479)
 //   key[q]       = linear cell of int(pos/dx) clamped to the grid (3D/run_3D.py:348),
 //   slot[q]      = arrival index in its bin (atomic on the bin count; fixed later by the sort).
@@ -503,7 +504,8 @@ __device__ __forceinline__ void write_p2g_record3(const P2GRecords3& R, int64_t 
   for (int r = 0; r < 3; ++r) m[r] = TT[r][0] * m0[0] + TT[r][1] * m0[1] + TT[r][2] * m0[2];
   R.pos4[q] = make_float4(v[0], v[1], v[2], 0.f);
 #pragma unroll
-  for (int f = 0; f < 3; ++f) R.famrec[f * P + q] = make_float4(m[f], TCT[f][0], TCT[f][1], TCT[f][2]);
+  for (int f = 0; f < 3; ++f)
+    R.famrec[f * P + q] = make_float4(m[f], TCT[f][0] * g.dx, TCT[f][1] * g.dx, TCT[f][2] * g.dx);
 }
 
 // Launches RK4_T_forward (3D); with R non-null the kernel also writes the P2G records and keys

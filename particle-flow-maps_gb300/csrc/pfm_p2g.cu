@@ -257,9 +257,12 @@ __device__ __forceinline__ int ring_prologue(float4* ring, const float4* __restr
   return sb + kRing < se ? __ldg(order + sb + kRing) : 0;
 }
 
-// Weights and offsets of the window faces c-1 .. c-1+W-1 along one axis (N_2 of 3D/run_3D.py:486)
+// Weights and offsets of the window faces c-1 .. c-1+W-1 along one axis (N_2 of 3D/run_3D.py:486).
+// The offsets are face minus particle position in grid units: the records carry the affine rows
+// already multiplied by dx (write_p2g_record3), so c (x_face - x_p) is formed without a multiply by
+// dx per face (the same products when dx is a power of two, where both scalings are exact).
 template <bool OWN>
-__device__ __forceinline__ void tile_axis(float p, int c, float dx, float* w, float* d) {
+__device__ __forceinline__ void tile_axis(float p, int c, float* w, float* d) {
   constexpr int W = OWN ? 4 : 3;
   const float fz = p - (float)c;
   if (c >= 1 && fz >= 0.f && fz < 1.f) {  // closed form of the branches (exact subtractions)
@@ -289,18 +292,18 @@ __device__ __forceinline__ void tile_axis(float p, int c, float dx, float* w, fl
 #pragma unroll
   for (int o = 0; o < W; ++o) {
     const float t = (float)(c - 1 + o);
-    d[o] = (OWN ? (t - p) : ((t + 0.5f) - p)) * dx;
+    d[o] = OWN ? (t - p) : ((t + 0.5f) - p);
   }
 }
 
 // One family: the particle loop from the ring (whose prologue was issued earlier; qn is the index
 // of slot sb + kRing), the window store, and -- after the barrier -- the next family's ring
 // prologue (NEXT >= 0), the window merge and the face add-back.
-template <int FAM, int NEXT>
+template <int FAM, int NEXT, bool APIC>
 __device__ __forceinline__ int tile_family(float2* __restrict__ win, float4* ring, const float4* __restrict__ pos4,
                                            const float4* __restrict__ rec, const float4* __restrict__ rec_next,
                                            const int* __restrict__ order, int sb, int se, int qn, int ci, int cj,
-                                           int ck, int x0, int y0, int z0, const MacGeom& g, int use_apic,
+                                           int ck, int x0, int y0, int z0, const MacGeom& g,
                                            float* __restrict__ u, float* __restrict__ w) {
   constexpr int W0 = FAM == 0 ? 4 : 3, W1 = FAM == 1 ? 4 : 3, W2 = FAM == 2 ? 4 : 3;
   constexpr int E0 = kTX + W0 - 1, E1 = kTY + W1 - 1, E2 = kTZ + W2 - 1, NE = E0 * E1 * E2;
@@ -312,23 +315,22 @@ __device__ __forceinline__ int tile_family(float2* __restrict__ win, float4* rin
     for (int b = 0; b < W1; ++b)
 #pragma unroll
       for (int k = 0; k < W2; ++k) acc[a][b][k] = make_float2(0.f, 0.f);
-  const float dx = g.dx;
   int d = 0;
   for (int s = sb; s < se; ++s) {
     cp_async_wait<kRing - 1>();  // slot d (group s - sb of this family) has landed
     const float4 p = ring[(2 * d) * kTileThreads + threadIdx.x];
     const float4 fr = ring[(2 * d + 1) * kTileThreads + threadIdx.x];
     float w0[W0], d0[W0], w1[W1], d1[W1], w2[W2], d2[W2];
-    tile_axis<FAM == 0>(p.x, ci, dx, w0, d0);
-    tile_axis<FAM == 1>(p.y, cj, dx, w1, d1);
-    tile_axis<FAM == 2>(p.z, ck, dx, w2, d2);
+    tile_axis<FAM == 0>(p.x, ci, w0, d0);
+    tile_axis<FAM == 1>(p.y, cj, w1, d1);
+    tile_axis<FAM == 2>(p.z, ck, w2, d2);
     // Face (a, b, k) receives w0[a] w1[b] w2[k] (m + c1 d0[a] + c2 d1[b] + c3 d2[k]) with
     // (m, c1, c2, c3) the record (APIC: run_3D.py:486-528); factored per axis as
     // w2[k] P_ab + (w2[k] d2[k]) Q_ab, P_ab = w1[b] (m w0[a] + c1 w0[a] d0[a]) + c2 w0[a] (w1[b] d1[b]),
     // Q_ab = c3 w0[a] w1[b], the weight sum w0[a] w1[b] w2[k] riding in the same packed FMA:
     // two instructions per face instead of five (the same terms, associated differently).
     const float m = fr.x;
-    const float c1 = use_apic ? fr.y : 0.f, c2 = use_apic ? fr.z : 0.f, c3 = use_apic ? fr.w : 0.f;
+    const float c1 = APIC ? fr.y : 0.f, c2 = APIC ? fr.z : 0.f, c3 = APIC ? fr.w : 0.f;
     float e1[W1], e2[W2];
 #pragma unroll
     for (int b = 0; b < W1; ++b) e1[b] = w1[b] * d1[b];
@@ -345,7 +347,7 @@ __device__ __forceinline__ int tile_family(float2* __restrict__ win, float4* rin
 #pragma unroll
         for (int k = 0; k < W2; ++k) {
           acc[a][b][k] = __ffma2_rn(make_float2(w2[k], w2[k]), pw, acc[a][b][k]);
-          acc[a][b][k].x = fmaf(e2[k], Q, acc[a][b][k].x);
+          if (APIC) acc[a][b][k].x = fmaf(e2[k], Q, acc[a][b][k].x);  // without APIC Q = 0: adds 0
         }
       }
     }
@@ -415,10 +417,11 @@ __device__ __forceinline__ int tile_family(float2* __restrict__ win, float4* rin
 }
 
 // One parity class (px, py, pz) of tiles; grid = (tiles along z, y, x of that parity).
+template <bool APIC>
 __global__ void __launch_bounds__(kTileThreads, 1) k_tile3(const float4* __restrict__ pos4,
                                                            const float4* __restrict__ famrec,
                                                            const int* __restrict__ order,
-                                                           const int* __restrict__ start, MacGeom g, int use_apic,
+                                                           const int* __restrict__ start, MacGeom g,
                                                            int64_t P, int px, int py, int pz, FaceOut3 out) {
   extern __shared__ __align__(16) unsigned char tile_smem[];
   float2* win = reinterpret_cast<float2*>(tile_smem);  // kWinSlots x kTileThreads window values (num, den)
@@ -437,12 +440,12 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_tile3(const float4* __restr
   const float4* r1 = famrec + P;
   const float4* r2 = famrec + 2 * P;
   int qn = ring_prologue(ring, pos4, r0, order, sb, se);
-  qn = tile_family<0, 1>(win, ring, pos4, r0, r1, order, sb, se, qn, ci, cj, ck, x0, y0, z0, g, use_apic, out.u[0],
-                         out.w[0]);
-  qn = tile_family<1, 2>(win, ring, pos4, r1, r2, order, sb, se, qn, ci, cj, ck, x0, y0, z0, g, use_apic, out.u[1],
-                         out.w[1]);
-  tile_family<2, -1>(win, ring, pos4, r2, r2, order, sb, se, qn, ci, cj, ck, x0, y0, z0, g, use_apic, out.u[2],
-                     out.w[2]);
+  qn = tile_family<0, 1, APIC>(win, ring, pos4, r0, r1, order, sb, se, qn, ci, cj, ck, x0, y0, z0, g, out.u[0],
+                               out.w[0]);
+  qn = tile_family<1, 2, APIC>(win, ring, pos4, r1, r2, order, sb, se, qn, ci, cj, ck, x0, y0, z0, g, out.u[1],
+                               out.w[1]);
+  tile_family<2, -1, APIC>(win, ring, pos4, r2, r2, order, sb, se, qn, ci, cj, ck, x0, y0, z0, g, out.u[2],
+                           out.w[2]);
   cp_async_wait<0>();
 }
 
@@ -529,9 +532,15 @@ __device__ __forceinline__ void tile_smoke_channel(float2* __restrict__ win, con
     const float4 p = __ldg(pos4 + q);
     const float4 fr = __ldg(rec + q);
     float w0[3], d0[3], w1[3], d1[3], w2[3], d2[3];
-    tile_axis<false>(p.x, ci, dx, w0, d0);
-    tile_axis<false>(p.y, cj, dx, w1, d1);
-    tile_axis<false>(p.z, ck, dx, w2, d2);
+    tile_axis<false>(p.x, ci, w0, d0);
+    tile_axis<false>(p.y, cj, w1, d1);
+    tile_axis<false>(p.z, ck, w2, d2);
+#pragma unroll
+    for (int o = 0; o < 3; ++o) {  // the smoke records are not pre-scaled: offsets in world units
+      d0[o] *= dx;
+      d1[o] *= dx;
+      d2[o] *= dx;
+    }
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
@@ -839,7 +848,8 @@ int p2g3_from_records(pfm_handle* h, float* const* us, float* const* ws, cudaStr
   }
   if (h->P > 0) {
     static std::atomic<unsigned long long> attr{0};  // above the default 48 KB: opt in per device
-    rc = check_cuda(h, opt_in_smem(k_tile3, (int)kTileSmem, attr), "k_tile3 shared-memory attribute");
+    auto tile = h->cfg.use_apic ? k_tile3<true> : k_tile3<false>;
+    rc = check_cuda(h, opt_in_smem(tile, (int)kTileSmem, attr), "k_tile3 shared-memory attribute");
     if (rc) return rc;
     const int nt[3] = {(h->geom.N[0] + kTX - 1) / kTX, (h->geom.N[1] + kTY - 1) / kTY, (h->geom.N[2] + kTZ - 1) / kTZ};
     for (int px = 0; px < 2; ++px)
@@ -847,8 +857,8 @@ int p2g3_from_records(pfm_handle* h, float* const* us, float* const* ws, cudaStr
         for (int pz = 0; pz < 2; ++pz) {
           const unsigned bx = (nt[0] - px + 1) / 2, by = (nt[1] - py + 1) / 2, bz = (nt[2] - pz + 1) / 2;
           if (!bx || !by || !bz) continue;
-          launch(h, k_tile3, dim3(bz, by, bx), kTileThreads, kTileSmem, st, pos4, famrec, order, start, h->geom,
-                 h->cfg.use_apic, h->P, px, py, pz, out);
+          launch(h, tile, dim3(bz, by, bx), kTileThreads, kTileSmem, st, pos4, famrec, order, start, h->geom, h->P,
+                 px, py, pz, out);
         }
     launch(h, k_normalize3, grid_for(F[0] + F[1] + F[2], kBinThreads), kBinThreads, 0, st, out, F[0], F[1], F[2]);
   }
