@@ -180,16 +180,15 @@ __global__ void __launch_bounds__(kBinThreads) k_payload2(const int* __restrict_
 // Tiled P2G (3D).  Cells are grouped in kTX x kTY x kTZ tiles, one thread per cell.  For each
 // face family the thread sums its cell's particles (particle-index order) into a register window
 // of the 4 x 3 x 3 faces they can reach (4 along the family's own axis: faces c-1 .. c+2; 3 along
-// the others: c-1 .. c+1), every thread stores its window in shared memory (36 slots x 512 cells,
-// 147 KB), and after one barrier each face of the region around the tile sums the slots of the
-// cells that reach it, in slot order, and adds the sum into the face grids.  Tiles run in 8
-// launches by the parity of their tile coordinates: tiles of one parity are a tile apart and their
-// face regions (one face below, two above) never overlap, so no atomics are needed.  Each face
-// sums in a fixed order (launch, pass, particle index): the result is bitwise reproducible (the
-// same sums, in the same order, as merging the windows into a shared copy of the region in 36
-// passes with a barrier between passes).  Particles outside the grid sit in the clamped edge cell,
-// whose window still holds every in-grid face they reach; their weights come from their real
-// positions.
+// the others: c-1 .. c+1), every thread stores its window in shared memory (36 slots per cell),
+// and after one barrier each face of the region around the tile sums the slots of the cells that
+// reach it, in slot order, and adds the sum into the face grids.  Tiles run in 8 launches by the
+// parity of their tile coordinates: tiles of one parity are a tile apart and their face regions
+// (one face below, two above) never overlap, so no atomics are needed.  Each face sums in a fixed
+// order (launch, pass, particle index): the result is bitwise reproducible (the same sums, in the
+// same order, as merging the windows into a shared copy of the region in 36 passes with a barrier
+// between passes).  Particles outside the grid sit in the clamped edge cell, whose window still
+// holds every in-grid face they reach; their weights come from their real positions.
 //
 // Record staging: a cell's particles are gathered through the sorted order, so each one costs a
 // memory round trip.  Every thread keeps a ring of kRing particle slots in shared memory (pos4 and
@@ -197,28 +196,38 @@ __global__ void __launch_bounds__(kBinThreads) k_payload2(const int* __restrict_
 // kRing - 1 particles are in flight while one is summed; the next slot's particle index is read one
 // iteration ahead.  The first kRing copies of the next family are issued before the window merge
 // and face add-back of the current one, so that memory latency overlaps the merge.
-// Tile of 4 x 8 x 16 cells: 16 along the last axis, the length of the seeding order's cell groups
-// (pfm_seed_jittered), so the records of a group's particles are read by one tile in one launch
-// (with 8-cell tiles a group's 128-particle runs are split between tiles of different parity
-// launches and every record line is fetched twice).
+//
+// Tile of 4 x 4 x 16 cells (256 threads, 128 registers each): 16 along the last axis, the length
+// of the seeding order's cell groups (pfm_seed_jittered), so the records of a group's particles
+// are read by one tile in one launch (with 8-cell tiles a group's 128-particle runs are split
+// between tiles of different parity launches and every record line is fetched twice).  With a
+// ring of 2 a block holds 90 KB of shared memory, so two blocks share an SM and one block's
+// barriers and window merge overlap the other's particle loop.  Measured at 256^3 (the P2G phase:
+// sort, 8 tile launches, normalisation): 4 x 8 x 16 cells with a ring of 5 (one 224 KB block per
+// SM) 10.33 ms; 4 x 4 x 16 with rings of 4 / 3 / 2 / 1 (two blocks per SM) 9.65 / 9.37 / 9.25 /
+// 10.96 ms; 4 x 3 x 16 with rings of 5 / 4: 11.14 / 10.82 ms.
 #ifndef PFM_TILE_X
 #define PFM_TILE_X 4
 #endif
 #ifndef PFM_TILE_Y
-#define PFM_TILE_Y 8
+#define PFM_TILE_Y 4
 #endif
 #ifndef PFM_TILE_Z
 #define PFM_TILE_Z 16
 #endif
 constexpr int kTX = PFM_TILE_X, kTY = PFM_TILE_Y, kTZ = PFM_TILE_Z;
 constexpr int kTileThreads = kTX * kTY * kTZ;
-static_assert(kTileThreads == 512, "the P2G tiles are 512-cell blocks");
+static_assert(kTileThreads % 32 == 0 && kTileThreads <= 512, "the P2G tiles are whole warps, at most 512 cells");
 static_assert(kTX >= 3 && kTY >= 3 && kTZ >= 3, "same-parity tiles must be far enough apart for their face regions");
-constexpr int kWinSlots = 4 * 3 * 3;                                              // window faces per cell
-constexpr int kRing = 5;                                                          // staged particles per thread
-constexpr size_t kWinBytes = (size_t)kWinSlots * kTileThreads * sizeof(float2);  // 147,456 B
-constexpr size_t kRingBytes = (size_t)kRing * 2 * kTileThreads * sizeof(float4);  // 81,920 B
-constexpr size_t kTileSmem = kWinBytes + kRingBytes;                              // 229,376 B
+constexpr int kTileBlocksPerSM = 512 / kTileThreads;  // resident tile blocks per SM (128 registers a thread)
+constexpr int kWinSlots = 4 * 3 * 3;                   // window faces per cell
+#ifndef PFM_TILE_RING
+#define PFM_TILE_RING 2
+#endif
+constexpr int kRing = PFM_TILE_RING;                                              // staged particles per thread
+constexpr size_t kWinBytes = (size_t)kWinSlots * kTileThreads * sizeof(float2);  // 73,728 B
+constexpr size_t kRingBytes = (size_t)kRing * 2 * kTileThreads * sizeof(float4);  // 16,384 B
+constexpr size_t kTileSmem = kWinBytes + kRingBytes;                              // 92,160 B
 static_assert(kTileSmem <= 227 * 1024, "k_tile3 exceeds the 227 KB of shared memory of a block");
 
 struct FaceOut3 {
@@ -418,7 +427,7 @@ __device__ __forceinline__ int tile_family(float2* __restrict__ win, float4* rin
 
 // One parity class (px, py, pz) of tiles; grid = (tiles along z, y, x of that parity).
 template <bool APIC>
-__global__ void __launch_bounds__(kTileThreads, 1) k_tile3(const float4* __restrict__ pos4,
+__global__ void __launch_bounds__(kTileThreads, kTileBlocksPerSM) k_tile3(const float4* __restrict__ pos4,
                                                            const float4* __restrict__ famrec,
                                                            const int* __restrict__ order,
                                                            const int* __restrict__ start, MacGeom g,
@@ -608,9 +617,9 @@ __device__ __forceinline__ void tile_smoke_channel(float2* __restrict__ win, con
   __syncthreads();
 }
 
-constexpr size_t kSmokeTileSmem = (size_t)27 * kTileThreads * sizeof(float2);  // 110,592 B
+constexpr size_t kSmokeTileSmem = (size_t)27 * kTileThreads * sizeof(float2);  // 55,296 B
 
-__global__ void __launch_bounds__(kTileThreads, 1) k_tile_smoke3(const float4* __restrict__ pos4,
+__global__ void __launch_bounds__(kTileThreads, kTileBlocksPerSM) k_tile_smoke3(const float4* __restrict__ pos4,
                                                                  const float4* __restrict__ chrec,
                                                                  const int* __restrict__ order,
                                                                  const int* __restrict__ start, MacGeom g, int use_apic,
