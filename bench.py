@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--replace", type=int, default=0, choices=[0, 1],
                     help="mixed arm: the FP64 true residual replaces the recursive one every 5 iterations and "
                          "before convergence is accepted (1) or is only reported (0)")
+    ap.add_argument("--warm-start", type=int, default=3, choices=[1, 2, 3],
+                    help="mixed arm's initial guess: the previous pressure (1), its linear (2) or quadratic (3) "
+                         "extrapolation through the last pressures")
     ap.add_argument("--fp64-res", type=int, default=-1,
                     help="grid of the FP64-oracle check of each arm's projection (-1: the bench grid, 0: off)")
     ap.add_argument("--eager", action="store_true",
@@ -436,7 +439,7 @@ def main():
     # the two arms of the metric, at the same residual: MGPCG stops at |r| < tol |b| in both
     plain_opts = dict(tol=args.tol, tol_mode=args.tol_mode, max_iters=400, check_every=4)
     mixed_opts = dict(tol=args.tol, tol_mode=2, max_iters=400, check_every=4, precision=args.precision,
-                      warm_start=2, true_residual_every=5, true_residual_replace=bool(args.replace))
+                      warm_start=args.warm_start, true_residual_every=5, true_residual_replace=bool(args.replace))
     plain = None
     if args.arms in ("both", "plain"):
         plain = timed_arm(plain_opts)
@@ -524,7 +527,8 @@ def main():
         mixed = args.arms != "plain"
         arm = (f"mixed-precision MGPCG ({args.precision} multigrid levels, FP64 inner products, FP64 true residual "
                f"every 5 iterations {'replacing the recursive one' if args.replace else 'reported'}) warm-started "
-               f"from the extrapolation of the last two steps' pressures" if mixed else
+               + {1: "from the previous step's pressure", 2: "from the linear extrapolation of the last two steps' pressures",
+                  3: "from the quadratic extrapolation of the last three steps' pressures"}[args.warm_start] if mixed else
                "plain FP32 MGPCG from a zero initial guess")
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "step_form": ("eager phase calls (pfm3_* entry points)" if args.eager else

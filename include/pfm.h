@@ -70,9 +70,12 @@ typedef struct pfm_handle pfm_handle;
  * products and norms are compensated FP32 sums per thread combined in FP64.
  * warm_start 1 starts from the caller's current pressure (p_out of pfm3/pfm2_poisson, x_out of
  * pfm_mgpcg_solve) instead of zero; warm_start 2 starts from the linear extrapolation
- * 2 p - p_before of that pressure and the solution the same buffer received before it, which the
- * handle keeps in its workspace for up to two buffers (their pointers name the slots; a third
- * buffer is PFM_ERR_ARG); the first solve of a buffer starts from p alone.
+ * 2 p - p_before of that pressure and what the same buffer held at the start of its previous solve
+ * (in a step loop: the solution before it), and warm_start 3 from the quadratic extrapolation
+ * 3 (p - p_before) + p_before2 through the last three.  The handle keeps the two earlier values in
+ * its workspace for up to two buffers (their pointers name the slots; a third buffer is
+ * PFM_ERR_ARG); with fewer kept (a new history) the solve starts from the highest order they allow
+ * (p alone, then the linear form).
  * true_residual_every K > 0 recomputes the true residual |b - A x| every K iterations and after
  * the last one and reports it (stats.rTr_true); the stopping rule stays the reference's, on the
  * recursive residual (x is stored in f32, whose rounding alone leaves a true residual of about
@@ -89,7 +92,8 @@ typedef struct pfm_solve_opts {
                       host waits once per solve; with max_iters = -1 the host relaunches the
                       loop every check_every iterations (>= 1) until it converges */
   int precision;   /* 0 FP32 (reference), 1 FP16 multigrid levels, 2 BF16 multigrid levels */
-  int warm_start;  /* 1: initial guess = the caller's pressure buffer; 2: its extrapolation */
+  int warm_start;  /* 1: initial guess = the caller's pressure buffer; 2 / 3: its linear /
+                      quadratic extrapolation through the buffer's last solutions */
   int true_residual_every; /* 0: never (reference); K > 0: check every K iterations and at the end */
   int true_residual_replace; /* mixed solve with K > 0: 1 = x accumulates in FP64 and the true residual
                                 b - A x (FP64) replaces the recursive one every K iterations and before
@@ -361,7 +365,7 @@ int pfm2_step(pfm_handle* h, const pfm2_step_fields* f, const pfm_step_params* p
 /* Sets the step clock: the next step is i + 1; ik, sub_t and frame_idx as the reference's loop
  * variables (restart from a checkpoint).  pfm_step_reset(h, -1, 0, 0, 0) is a fresh start. */
 int pfm_step_reset(pfm_handle* h, int i, int ik, double sub_t, int frame_idx, void* stream);
-/* Forgets the previous solutions kept for warm_start 2 (a new simulation on the same handle and
+/* Forgets the previous solutions kept for warm_start 2 and 3 (a new simulation on the same handle and
  * pressure buffers); asynchronous on `stream`.  No counterpart in the reference, whose solves
  * start from zero (3D/mgpcg.py:63-79). */
 int pfm_reset_warm_history(pfm_handle* h, void* stream);

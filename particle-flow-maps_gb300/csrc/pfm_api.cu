@@ -216,7 +216,7 @@ int pfm_create(const pfm_config* cfg, pfm_handle** out) {
   h->o_maxpart = take(kReduceBlocks * sizeof(float) + 256);
   h->o_step = take(sizeof(StepCtl));
   h->o_x64 = take(C * 8);  // FP64 x of the residual-replacement solve
-  h->o_hist = take(2 * C * 4);
+  h->o_hist = take(4 * C * 4);  // per pressure buffer: its last two solutions
   h->o_hist_flag = take(2 * sizeof(int));
   h->hist_ptr[0] = h->hist_ptr[1] = nullptr;
 

@@ -1902,19 +1902,33 @@ static int solve_dispatch(pfm_handle* h, const pfm_solve_opts* opts, pfm_solve_s
   return solve_impl<D, float>(h, o, stats, s);
 }
 
-// x = 2 p - hist (the linear extrapolation of the last two solutions) where the slot holds a
-// previous solution, else x = p; the slot then takes p.  One thread sets the flag afterwards.
-__global__ void __launch_bounds__(256) k_warm_extrap(float* __restrict__ x, float* __restrict__ hist,
-                                                     const float* __restrict__ p, int64_t n, const int* flag) {
-  const bool have = *flag != 0;
+// The warm-start guess from the buffer's current pressure p and the slot's history (h1 the solution
+// before p, h2 the one before h1; `count` of them are valid): MODE 2 x = 2 p - h1, the linear
+// extrapolation; MODE 3 x = 3 (p - h1) + h2, the quadratic one through the three solutions (with
+// fewer solutions kept, the highest order they allow; with none, x = p).  The history then
+// shifts (h2 = h1, h1 = p) in both modes, so either may follow the other; k_bump_count counts it.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_warm_extrap(float* __restrict__ x, float* __restrict__ h1,
+                                                     float* __restrict__ h2, const float* __restrict__ p, int64_t n,
+                                                     const int* count) {
+  const int c = *count;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
     const float v = p[e];
-    x[e] = have ? __fsub_rn(2.f * v, hist[e]) : v;
-    hist[e] = v;
+    if (c == 0) {
+      x[e] = v;
+    } else {
+      const float a = h1[e];
+      if (MODE == 3 && c >= 2)
+        x[e] = __fadd_rn(__fmul_rn(3.f, __fsub_rn(v, a)), h2[e]);
+      else
+        x[e] = __fsub_rn(2.f * v, a);
+      h2[e] = a;
+    }
+    h1[e] = v;
   }
 }
 
-__global__ void k_set_flag(int* flag) { *flag = 1; }
+__global__ void k_bump_count(int* count) { *count = *count < 2 ? *count + 1 : 2; }
 
 int warm_start_init(pfm_handle* h, float* x, const float* p_io, int mode, cudaStream_t s) {
   if (!p_io) return set_error(h, PFM_ERR_NULL, "MGPCG: warm_start needs the pressure buffer");
@@ -1929,18 +1943,25 @@ int warm_start_init(pfm_handle* h, float* x, const float* p_io, int mode, cudaSt
       slot = k;
     }
   if (slot < 0)
-    return set_error(h, PFM_ERR_ARG, "MGPCG: warm_start 2 keeps the history of at most two pressure buffers per handle");
-  float* hist = ws_ptr<float>(h, h->o_hist) + (size_t)slot * h->cells;
-  int* flag = ws_ptr<int>(h, h->o_hist_flag) + slot;
-  launch(h, k_warm_extrap, stream_blocks(h->cells), 256, 0, s, x, hist, p_io, (int64_t)h->cells, (const int*)flag);
-  launch(h, k_set_flag, 1, 1, 0, s, flag);
+    return set_error(h, PFM_ERR_ARG,
+                     "MGPCG: warm_start 2 and 3 keep the history of at most two pressure buffers per handle");
+  float* h1 = ws_ptr<float>(h, h->o_hist) + (size_t)(2 * slot) * h->cells;
+  float* h2 = h1 + h->cells;
+  int* count = ws_ptr<int>(h, h->o_hist_flag) + slot;
+  if (mode == 3)
+    launch(h, k_warm_extrap<3>, stream_blocks(h->cells), 256, 0, s, x, h1, h2, p_io, (int64_t)h->cells,
+           (const int*)count);
+  else
+    launch(h, k_warm_extrap<2>, stream_blocks(h->cells), 256, 0, s, x, h1, h2, p_io, (int64_t)h->cells,
+           (const int*)count);
+  launch(h, k_bump_count, 1, 1, 0, s, count);
   return launch_check(h, "warm start");
 }
 
 int mgpcg_solve_in_place(pfm_handle* h, float* x_out, const pfm_solve_opts* opts, pfm_solve_stats* stats,
                          cudaStream_t s) {
-  if (opts && (opts->warm_start < 0 || opts->warm_start > 2))
-    return set_error(h, PFM_ERR_ARG, "MGPCG: warm_start must be 0, 1 or 2");
+  if (opts && (opts->warm_start < 0 || opts->warm_start > 3))
+    return set_error(h, PFM_ERR_ARG, "MGPCG: warm_start must be 0, 1, 2 or 3");
   if (opts && opts->warm_start) {  // the initial guess from the caller's current x_out
     int c = warm_start_init(h, ws_ptr<float>(h, h->o_x), x_out, opts->warm_start, s);
     if (c) return c;

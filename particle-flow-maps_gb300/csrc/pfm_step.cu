@@ -97,8 +97,8 @@ static int check_step_params(pfm_handle* h, const pfm_step_params* p) {
   if (p->poisson.max_iters < 0)
     return set_error(h, PFM_ERR_ARG, "step: the device solve needs a finite max_iters (the host does not relaunch it)");
   if (p->poisson.tol_mode < 0 || p->poisson.tol_mode > 2 || p->poisson.precision < 0 || p->poisson.precision > 2 ||
-      p->poisson.warm_start < 0 || p->poisson.warm_start > 2)
-    return set_error(h, PFM_ERR_ARG, "step: tol_mode, precision and warm_start must be 0..2");
+      p->poisson.warm_start < 0 || p->poisson.warm_start > 3)
+    return set_error(h, PFM_ERR_ARG, "step: tol_mode and precision must be 0..2, warm_start 0..3");
   return PFM_OK;
 }
 

@@ -324,9 +324,15 @@ class Scene:
         o.max_iters, o.eps, o.tol, o.tol_mode, o.check_every = int(max_iters), float(eps), float(tol), int(tol_mode), int(check_every)
         o.precision = {"fp32": 0, "fp16": 1, "bf16": 2}.get(precision, precision)
         o.precision = int(o.precision)
-        # False/True -> 0/1 (start from zero / from the caller's pressure); 2: extrapolate from the
-        # caller's pressure and the solution before it (the library keeps that one per buffer)
-        o.warm_start = 2 if (not isinstance(warm_start, bool) and warm_start == 2) else int(bool(warm_start))
+        # False/True -> 0/1 (start from zero / from the caller's pressure); 2 / 3: extrapolate
+        # linearly / quadratically from the caller's pressure and the solutions before it (the
+        # library keeps those per buffer)
+        if isinstance(warm_start, bool) or warm_start in (None, 0, 1):
+            o.warm_start = int(bool(warm_start))
+        elif warm_start in (2, 3):
+            o.warm_start = int(warm_start)
+        else:
+            raise PfmError(1, f"warm_start must be False/True, 0, 1, 2 or 3, not {warm_start!r}")
         o.true_residual_every = int(true_residual_every)
         o.true_residual_replace = int(bool(true_residual_replace))
         return o
@@ -337,8 +343,9 @@ class Scene:
 
         ``precision`` "fp32" (0, the reference), "fp16" (1) or "bf16" (2) multigrid level storage;
         ``warm_start`` starts from p_out's current pressure (``warm_start=2``: from the linear
-        extrapolation 2 p - p_before of it and the solution before it, which the library keeps per
-        p_out buffer, two buffers per scene); ``true_residual_every`` K > 0
+        extrapolation 2 p - p_before of it and the solution before it; ``warm_start=3``: from the
+        quadratic 3 (p - p_before) + p_before2 through the last three; the library keeps the
+        earlier solutions per p_out buffer, two buffers per scene); ``true_residual_every`` K > 0
         recomputes |b - A x| every K iterations and reports it; with ``true_residual_replace`` (FP16/BF16
         levels) x is kept in FP64 and that residual, formed in FP64, replaces the recursive one every K
         iterations and before convergence is accepted."""
@@ -459,8 +466,8 @@ class Scene:
         self._check(fn(self.h, ctypes.byref(fields), ctypes.byref(params), self._stream()))
 
     def reset_warm_history(self):
-        """Forgets the pressures kept for ``warm_start=2`` (the next solve of each buffer starts from
-        the buffer's pressure alone)."""
+        """Forgets the pressures kept for ``warm_start=2`` and ``3`` (the next solve of each buffer
+        starts from the buffer's pressure alone)."""
         self._check(self.lib.pfm_reset_warm_history(self.h, self._stream()))
 
     def step_reset(self, i=-1, ik=0, sub_t=0.0, frame_idx=0):

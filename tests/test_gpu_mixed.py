@@ -213,6 +213,68 @@ def test_extrapolated_warm_start_history_per_buffer():
     assert ia.iterations == ib.iterations and torch.equal(a, ps[0])
 
 
+def test_quadratic_warm_start_is_the_extrapolation():
+    """warm_start 3: the library keeps what the buffer held at the start of its two previous solves
+    (in a step loop, the two solutions before the current one) and starts from 3 (p - h1) + h2, the
+    quadratic through the three; with one kept value, from the linear 2 p - h1; with none (a fresh
+    history), from p.  Each solve is bitwise the warm_start 1 solve from that guess formed with
+    torch in the same rounding order."""
+    res = (32, 32, 32)
+    sc = pfm.Scene(3, res, 1 / 32, 0)
+    import __graft_entry__ as G
+    base = G._ring_velocity(res, 1 / 32)
+    kw = dict(tol=1e-6, tol_mode=2, max_iters=400, precision="fp16")
+    p = torch.zeros(res, device="cuda")
+    held = []  # the buffer's contents at the start of each solve
+    for k in range(4):  # slightly different fields, as successive steps give
+        fields = [a * (1.0 + 0.05 * k) for a in base]
+        if k == 0:
+            guess = p.clone()
+        elif k == 1:
+            guess = 2 * p - held[-1]
+        else:
+            guess = 3 * (p - held[-1]) + held[-2]
+        held.append(p.clone())
+        ia = sc.poisson([torch.from_numpy(f).cuda() for f in fields], p, warm_start=3, **kw)
+        ref = guess.clone()
+        ib = pfm.Scene(3, res, 1 / 32, 0).poisson([torch.from_numpy(f).cuda() for f in fields], ref,
+                                                  warm_start=True, **kw)
+        torch.cuda.synchronize()
+        assert ia.iterations == ib.iterations and torch.equal(p, ref), k
+
+
+def test_quadratic_warm_start_in_the_step():
+    """warm_start 3 in the whole-step graph: bitwise the eager phase calls; on the two-ring scene
+    its solves take no more iterations in total than with the linear extrapolation, and the results
+    stay within the solver tolerance of the warm_start 1 run."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    base = dict(tol=1e-6, tol_mode=2, max_iters=400, precision="fp16", true_residual_every=5)
+    runs = {}
+    for name, ws, graph in (("prev", True, True), ("lin", 2, True), ("quad", 3, True), ("quad_eager", 3, False)):
+        sim = bench.make_sim(64, 2, dict(base, warm_start=ws), graph=graph)
+        its = []
+        for _ in range(10):
+            sim.step()
+            if not graph:
+                its.append((sim.infos[-2].iterations, sim.infos[-1].iterations))
+        torch.cuda.synchronize()
+        if graph:
+            info = sim.step_info()
+            its = [tuple(info.history[s % 64]) for s in range(info.step - 9, info.step + 1)]
+        runs[name] = (its, [t.clone() for t in sim.u], sim.p.clone())
+        del sim
+    for a, b in zip(runs["quad"][1] + [runs["quad"][2]], runs["quad_eager"][1] + [runs["quad_eager"][2]]):
+        assert torch.equal(a, b)
+    assert runs["quad"][0] == runs["quad_eager"][0]
+    total = {k: sum(i[0] + i[1] for i in runs[k][0][3:]) for k in ("lin", "quad")}
+    assert total["quad"] <= total["lin"], (runs["lin"][0], runs["quad"][0])
+    for a, b in zip(runs["quad"][1], runs["prev"][1]):
+        assert (a - b).norm().item() <= 1e-5 * b.norm().item()
+
+
 @pytest.mark.parametrize("precision", ["fp16", "bf16"])
 def test_true_residual_replacement_against_fp64_oracle(ring64, precision):
     """true_residual_replace: x accumulates in FP64 and every 5 iterations, and before convergence
