@@ -89,23 +89,28 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int* total) {
   return prefix + x - v;
 }
 
-// one block: exclusive scan of nb block sums in place (nb <= kScanThreads * kScanItems)
+// one block: exclusive scan of nb block sums in place, kScanThreads * kScanItems at a time with the
+// running total carried between chunks (more than one chunk from 512^3 cells on)
 __global__ void __launch_bounds__(kScanThreads) k_scan_top(int* __restrict__ bsum, int nb) {
-  int vals[kScanItems];
-  int loc = 0;
+  int carry = 0;
+  for (int c0 = 0; c0 < nb; c0 += kScanThreads * kScanItems) {
+    int vals[kScanItems];
+    int loc = 0;
 #pragma unroll
-  for (int t = 0; t < kScanItems; ++t) {
-    int e = threadIdx.x * kScanItems + t;
-    vals[t] = e < nb ? bsum[e] : 0;
-    loc += vals[t];
-  }
-  int total;
-  int ex = block_exclusive_scan(loc, &total);
+    for (int t = 0; t < kScanItems; ++t) {
+      int e = c0 + threadIdx.x * kScanItems + t;
+      vals[t] = e < nb ? bsum[e] : 0;
+      loc += vals[t];
+    }
+    int total;
+    int ex = block_exclusive_scan(loc, &total) + carry;
 #pragma unroll
-  for (int t = 0; t < kScanItems; ++t) {
-    int e = threadIdx.x * kScanItems + t;
-    if (e < nb) bsum[e] = ex;
-    ex += vals[t];
+    for (int t = 0; t < kScanItems; ++t) {
+      int e = c0 + threadIdx.x * kScanItems + t;
+      if (e < nb) bsum[e] = ex;
+      ex += vals[t];
+    }
+    carry += total;
   }
 }
 
@@ -788,7 +793,6 @@ static int sort_from_keys(pfm_handle* h, cudaStream_t st) {
   int* bsum = ws_ptr<int>(h, h->o_blocksums);
   const int64_t per_block = (int64_t)kScanThreads * kScanItems;
   const int nb = (int)((C + per_block - 1) / per_block);
-  if (nb > kScanThreads * kScanItems) return set_error(h, PFM_ERR_SHAPE, "too many cells for the bin scan");
   launch(h, k_scan_blocksums, nb, kScanThreads, 0, st, (const int*)count, C, bsum);
   launch(h, k_scan_top, 1, kScanThreads, 0, st, bsum, nb);
   launch(h, k_scan_apply, nb, kScanThreads, 0, st, (const int*)count, C, (const int*)bsum, start, (int)P);

@@ -109,3 +109,39 @@ def test_cube_instances_equal_runtime_strides(n):
         outs.append([a[k] for k in ("pos", "T_gm", "T_init", "init_C")] + [b["pos"], b["T_gm"]] + list(mid))
     for x, y in zip(*outs):
         assert torch.equal(x, y)
+
+
+def test_cube_instance_512_equals_runtime_strides():
+    """The 512^3 instances (the largest extent compiled in; its row offsets reach 2 MB) against the
+    runtime-stride kernels: the RK4 with the gradient reinitialisation on 2^20 particles spread
+    over the whole grid, and the three midpoint launches over every face.  Bitwise equal."""
+    from pfm import _lib
+    n = 512
+    dx = 1.0 / n
+    P = 1 << 20
+    rng = np.random.default_rng(13)
+    dev = torch.device("cuda:0")
+    sc = pfm.Scene(3, (n, n, n), dx, P)
+    g = torch.Generator(device=dev).manual_seed(5)
+    u = [(0.3 * torch.randn(s, device=dev, generator=g)) for s in sc.face_shapes]
+    ua = [(0.3 * torch.randn(s, device=dev, generator=g)) for s in sc.face_shapes]
+    pos = torch.from_numpy(rng.uniform(0.0, 1.0, (3, P)).astype(np.float32)).to(dev)
+    eye = torch.eye(3, device=dev).reshape(3, 3, 1)
+    st = dict(pos=pos, T_gm=eye + 0.05 * torch.randn(3, 3, P, device=dev, generator=g),
+              T_init=eye + 0.05 * torch.randn(3, 3, P, device=dev, generator=g),
+              init_C=torch.randn(3, 3, P, device=dev, generator=g),
+              init_imp=torch.randn(3, P, device=dev, generator=g))
+    dt = 0.4 / n
+    outs = []
+    for cube in (1, 0):
+        sc.set_tuning(_lib.TUNE_CUBE_KERNELS, cube)
+        a = _clone(st)
+        sc.gradm_rk4_records3(a["pos"], a["T_gm"], a["T_init"], a["init_C"], a["init_imp"], u, ua, dt)
+        mid = sc.alloc_faces()
+        sc.midpoint(u, mid, 0.5 * dt)
+        torch.cuda.synchronize()
+        outs.append([a[k] for k in ("pos", "T_gm", "T_init", "init_C")] + list(mid))
+    for x, y in zip(*outs):
+        assert torch.equal(x, y)
+    del outs, u, ua, sc
+    torch.cuda.empty_cache()

@@ -422,3 +422,27 @@ def test_p2g2_collisions_and_edges():
     (ox, oy), (owx, owy), (opx, opy) = O.p2g2(imp, pos, C, psi, res, dx)
     for t, o in zip(u + w + psi_g, [ox, oy, owx, owy, opx, opy]):
         assert rel(host(t), o) < TOL
+
+
+def test_sort_bitexact_512_cube():
+    """A 512^3 grid: 134,217,728 cells, 16,384 block sums, so the one-block scan of the block sums
+    runs in two chunks with the total carried between them.  2^20 particles spread over the grid,
+    a fifth of them in the last eighth of the cells (whose starts the carry offsets): counts and
+    permutation bit for bit numpy's."""
+    rng = np.random.default_rng(31)
+    n = 512
+    res = (n, n, n)
+    P = 1 << 20
+    pos = rng.uniform(0.0, 1.0, (P, 3)).astype(np.float32)
+    pos[: P // 5, 0] = rng.uniform(0.875, 1.0, P // 5).astype(np.float32)
+    sc = pfm.Scene(3, res, 1.0 / n, P)
+    count, order = sc.sort_particles(pfm.soa(pos))
+    cells = np.clip((pos / np.float32(1.0 / n)).astype(np.int64), 0, n - 1)
+    key = (cells[:, 0] * n + cells[:, 1]) * n + cells[:, 2]
+    assert np.array_equal(host(order), np.argsort(key, kind="stable"))
+    c = host(count).ravel()
+    nz = np.nonzero(c)[0]
+    ref = np.bincount(key, minlength=n ** 3)
+    assert np.array_equal(nz, np.nonzero(ref)[0]) and np.array_equal(c[nz], ref[nz])
+    del sc, count, order
+    torch.cuda.empty_cache()
