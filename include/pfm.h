@@ -146,6 +146,9 @@ int pfm_measure_fp32_peak(float* sink, int blocks_per_sm, int iters, int reps, i
 #define PFM_TUNE_CUBE_KERNELS 4   /* 1: on cubic 64^3, 128^3, 256^3 and 512^3 grids the 3D RK4 and
                                      midpoint kernels run instances compiled for that extent (the
                                      face-field strides are constants); 0: strides read at run time (1) */
+#define PFM_TUNE_MIDPOINT_CENTRE 5 /* 1: the 3D midpoint's first RK stage, which samples the face centre,
+                                     uses its constant weights and leaves out the zero-weight taps
+                                     (interior faces, power-of-two dx); 0: the generic taps (1) */
 int pfm_set_tuning(pfm_handle* h, int key, int value);
 int pfm_get_tuning(const pfm_handle* h, int key, int* value);
 

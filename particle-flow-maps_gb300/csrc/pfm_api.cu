@@ -225,6 +225,7 @@ int pfm_create(const pfm_config* cfg, pfm_handle** out) {
   h->tail_cells = 4096;
   h->smooth_tma = 0;
   h->cube_kernels = 1;
+  h->mid_centre = 1;
   if (cudaHostAlloc((void**)&h->h_state, sizeof(SolveState), cudaHostAllocDefault) != cudaSuccess) {
     cudaGetLastError();
     delete h;
@@ -296,6 +297,9 @@ int pfm_set_tuning(pfm_handle* h, int key, int value) {
   } else if (key == PFM_TUNE_CUBE_KERNELS) {
     if (value != 0 && value != 1) return set_error(h, PFM_ERR_ARG, "cube kernels must be 0 or 1");
     h->cube_kernels = value;
+  } else if (key == PFM_TUNE_MIDPOINT_CENTRE) {
+    if (value != 0 && value != 1) return set_error(h, PFM_ERR_ARG, "midpoint face-centre form must be 0 or 1");
+    h->mid_centre = value;
   } else {
     return set_error(h, PFM_ERR_ARG, "unknown tuning key");
   }
@@ -316,6 +320,7 @@ int pfm_get_tuning(const pfm_handle* h, int key, int* value) {
   else if (key == PFM_TUNE_MG_TAIL_CELLS) *value = h->tail_cells;
   else if (key == PFM_TUNE_SMOOTH_TMA) *value = h->smooth_tma;
   else if (key == PFM_TUNE_CUBE_KERNELS) *value = h->cube_kernels;
+  else if (key == PFM_TUNE_MIDPOINT_CENTRE) *value = h->mid_centre;
   else return PFM_ERR_ARG;
   return PFM_OK;
 }

@@ -76,12 +76,113 @@ __global__ void __launch_bounds__(256) k_max_speed(const float* __restrict__ ux,
 // Midpoint for face family `fam` (3D/run_3D.py:106-120, 144-173, 296-312): psi starts at the face
 // centre X_fam (taichi_utils.py:33-46), T at the unit vector e_fam; RK4 over -dt_half with the
 // rows-form gradient (dT/dt = grad u . T); then u1 = T . u0(psi).
+// One component of interp_mac3_taps (value and gradient) at a sample on whole or half cells whose
+// clamp does not bind: per axis the three taps are the C set (s whole: t = 0, weights 1/8, 3/4,
+// 1/8, derivatives -1/2, -0, 1/2) or the H set (s half: t = -1/2, weights 1/2, 1/2, 0,
+// derivatives -1, 1, 0), the weights interp_mac3's closed form gives there.  The sums are
+// interp_mac3_taps' own, term for term and in its order, less the terms whose weight is zero
+// (which add a zero): the same results, with the zero-weight loads and FMAs left out (12 of the 27
+// rows and taps of a component with two H axes).  b: the component's first tap; sx, sy: its
+// strides along x and y.
+template <bool CX, bool CY, bool CZ>
+__device__ __forceinline__ void centre_component(const float* __restrict__ b, int sx, int sy, float& v, float& gx,
+                                                 float& gy, float& gz) {
+  constexpr int NA = CX ? 3 : 2, NB = CY ? 3 : 2;
+  float v_ = 0.f, x_ = 0.f, y_ = 0.f, z_ = 0.f;
+#pragma unroll
+  for (int a = 0; a < NA; ++a) {
+    float Aa = 0.f, Ba = 0.f, Ca = 0.f;
+#pragma unroll
+    for (int bb = 0; bb < NB; ++bb) {
+      const float* __restrict__ row = b + (a * sx + bb * sy);
+      const float v0 = __ldg(row), v1 = __ldg(row + 1);
+      float tn, td;
+      if (CZ) {
+        const float v2 = __ldg(row + 2);
+        tn = fmaf(v2, 0.125f, fmaf(v1, 0.75f, v0 * 0.125f));
+        td = fmaf(v2, 0.5f, v0 * -0.5f);
+      } else {
+        tn = fmaf(v1, 0.5f, v0 * 0.5f);
+        td = fmaf(v1, 1.f, v0 * -1.f);
+      }
+      const float wy = CY ? (bb == 1 ? 0.75f : 0.125f) : 0.5f;
+      Aa = fmaf(wy, tn, Aa);
+      if (!CY || bb != 1) Ba = fmaf(CY ? (bb == 0 ? -0.5f : 0.5f) : (bb == 0 ? -1.f : 1.f), tn, Ba);
+      Ca = fmaf(wy, td, Ca);
+    }
+    const float wx = CX ? (a == 1 ? 0.75f : 0.125f) : 0.5f;
+    v_ = fmaf(wx, Aa, v_);
+    if (!CX || a != 1) x_ = fmaf(CX ? (a == 0 ? -0.5f : 0.5f) : (a == 0 ? -1.f : 1.f), Aa, x_);
+    y_ = fmaf(wx, Ba, y_);
+    z_ = fmaf(wx, Ca, z_);
+  }
+  v = v_;
+  gx = x_;
+  gy = y_;
+  gz = z_;
+}
+
+// interp_mac3<NC>(want_grad) at the centre of face (i, j, k) of family fam, when the sample is
+// that face centre exactly (p / dx gives back the face's coordinates) and no clamp binds; else
+// false (the caller interpolates generically).  Component c samples axis a at s = X_a - BL(c, a),
+// X the face centre (whole on the family's axis, half elsewhere), BL = 0 on a = c, 1/2 elsewhere:
+// s is whole (C taps, first tap s - 1) when a is both or neither of fam and c, else half (H taps,
+// first tap s - 1/2).
+template <int fam, int NC>
+__device__ __forceinline__ bool interp_face_centre(const MacFields3& F, const MacGeom& g, const float p[3],
+                                                   const int I[3], float uo[3], float G[3][3]) {
+  bool ok = true;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float u = p[a] * g.inv_dx;
+    const float X = (float)I[a] + (a == fam ? 0.f : 0.5f);
+    ok = ok && (u == X);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float sv = (a == c) ? u - 0.0f : u - 0.5f;
+      ok = ok && sv >= 1.f && sv <= g.hi[c][a];
+    }
+  }
+  if (!ok) return false;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    int first[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) first[a] = (a == fam || a != c) ? I[a] - 1 : I[a];
+    const int m1 = NC ? (c == 1 ? NC + 1 : NC) : g.n[c][1], m2 = NC ? (c == 2 ? NC + 1 : NC) : g.n[c][2];
+    const float* __restrict__ base = F.u[c] + ((first[0] * m1 + first[1]) * m2 + first[2]);
+    const int sx = m1 * m2;
+    float v, gx, gy, gz;
+    // axis a takes the C set when (a == fam) == (a == c)
+    if (c == fam)
+      centre_component<true, true, true>(base, sx, m2, v, gx, gy, gz);
+    else if (fam == 0 && c == 1)
+      centre_component<false, false, true>(base, sx, m2, v, gx, gy, gz);
+    else if (fam == 0 && c == 2)
+      centre_component<false, true, false>(base, sx, m2, v, gx, gy, gz);
+    else if (fam == 1 && c == 0)
+      centre_component<false, false, true>(base, sx, m2, v, gx, gy, gz);
+    else if (fam == 1 && c == 2)
+      centre_component<true, false, false>(base, sx, m2, v, gx, gy, gz);
+    else if (fam == 2 && c == 0)
+      centre_component<false, true, false>(base, sx, m2, v, gx, gy, gz);
+    else
+      centre_component<true, false, false>(base, sx, m2, v, gx, gy, gz);
+    uo[c] = v;
+    G[c][0] = gx * g.inv_dx;
+    G[c][1] = gy * g.inv_dx;
+    G[c][2] = gz * g.inv_dx;
+  }
+  return true;
+}
+
 // NC: the grid's cube extent when the interpolation is compiled for it (interp_mac3_taps<NC>), else 0.
+// centre != 0: the first stage at the face centre in the constant-weight form (interp_face_centre).
 template <int fam, int NC>
 __global__ void __launch_bounds__(kGThreads, PFM_MID_MINB) k_midpoint3(MacFields3 F, MacGeom g, float dt_half,
                                                         float* __restrict__ u1, float* __restrict__ psi_out,
                                                         float* __restrict__ T_out,
-                                                        const float* __restrict__ dt_half_dev) {
+                                                        const float* __restrict__ dt_half_dev, int centre) {
   if (dt_half_dev) dt_half = *dt_half_dev;  // the whole-step graph keeps dt on the device
   const int n0 = g.n[fam][0], n1 = g.n[fam][1], n2 = g.n[fam][2];
   const int64_t nf = (int64_t)n0 * n1 * n2;
@@ -99,10 +200,12 @@ __global__ void __launch_bounds__(kGThreads, PFM_MID_MINB) k_midpoint3(MacFields
   const float half = 0.5f * neg_dt;
   float pk[3] = {p0[0], p0[1], p0[2]}, Tk[3] = {T0[0], T0[1], T0[2]};
   float su[3], sT[3];
+  const int I[3] = {i, j, k};
 #pragma unroll 1
   for (int s = 0; s < 4; ++s) {
     float u[3], G[3][3];
-    interp_mac3<NC>(F, g, pk, u, G, true);
+    // the first stage samples the face centre itself: constant weights, a third of the rows fewer
+    if (s > 0 || !centre || !interp_face_centre<fam, NC>(F, g, pk, I, u, G)) interp_mac3<NC>(F, g, pk, u, G, true);
     float dT[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) dT[c] = G[c][0] * Tk[0] + G[c][1] * Tk[1] + G[c][2] * Tk[2];
@@ -205,9 +308,13 @@ static void launch_midpoint3(pfm_handle* h, int fam, dim3 gr, cudaStream_t st, c
                              float* u1, float* psi_out, float* T_out, const float* dt_half_dev) {
   with_cube(h, [&](auto nc) {
     constexpr int NC = decltype(nc)::value;
-    if (fam == 0) launch(h, k_midpoint3<0, NC>, gr, kGThreads, 0, st, F, h->geom, dt_half, u1, psi_out, T_out, dt_half_dev);
-    if (fam == 1) launch(h, k_midpoint3<1, NC>, gr, kGThreads, 0, st, F, h->geom, dt_half, u1, psi_out, T_out, dt_half_dev);
-    if (fam == 2) launch(h, k_midpoint3<2, NC>, gr, kGThreads, 0, st, F, h->geom, dt_half, u1, psi_out, T_out, dt_half_dev);
+    const int c = h->mid_centre;
+    if (fam == 0)
+      launch(h, k_midpoint3<0, NC>, gr, kGThreads, 0, st, F, h->geom, dt_half, u1, psi_out, T_out, dt_half_dev, c);
+    if (fam == 1)
+      launch(h, k_midpoint3<1, NC>, gr, kGThreads, 0, st, F, h->geom, dt_half, u1, psi_out, T_out, dt_half_dev, c);
+    if (fam == 2)
+      launch(h, k_midpoint3<2, NC>, gr, kGThreads, 0, st, F, h->geom, dt_half, u1, psi_out, T_out, dt_half_dev, c);
   });
 }
 

@@ -146,6 +146,7 @@ struct pfm_handle {
   int tail_cells;
   int smooth_tma;  // 3D 16-bit MGPCG levels smoothed from TMA-staged tiles (same results)
   int cube_kernels;  // 3D interpolating kernels instantiated for the grid's cube extent (same results)
+  int mid_centre;    // 3D midpoint's first stage at the face centre in constant-weight form (same results)
   // whole-step graph (pfm3_step / pfm2_step), rebuilt when its fields or parameters change
   cudaGraphExec_t g_step;
   std::string step_key;

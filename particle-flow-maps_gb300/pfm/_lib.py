@@ -182,6 +182,7 @@ TUNE_P2G2_COLUMN = 1
 TUNE_MG_TAIL_CELLS = 2
 TUNE_SMOOTH_TMA = 3
 TUNE_CUBE_KERNELS = 4
+TUNE_MIDPOINT_CENTRE = 5
 # scratch limits of pfm_sort_particles_noalloc (include/pfm.h)
 NOALLOC_MAX_PARTICLES = 1 << 21
 NOALLOC_MAX_CELLS = 1 << 18

@@ -145,3 +145,27 @@ def test_cube_instance_512_equals_runtime_strides():
         assert torch.equal(x, y)
     del outs, u, ua, sc
     torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("res", [(64, 64, 64), (40, 32, 48)])
+def test_midpoint_face_centre_form_equals_generic_taps(res):
+    """PFM_TUNE_MIDPOINT_CENTRE: the midpoint's first RK stage samples the face centre, where every
+    axis' weights are the t = 0 or t = -1/2 constants; the constant-weight form leaves the
+    zero-weight taps out and is bitwise the generic interpolation (a cube instance and a grid with
+    the strides read at run time; boundary faces, where a clamp binds, take the generic taps)."""
+    from pfm import _lib
+    dx = 1.0 / 32
+    sc = pfm.Scene(3, res, dx, 0)
+    g = torch.Generator(device="cuda").manual_seed(17)
+    u = [0.3 * torch.randn(s, device="cuda", generator=g) for s in sc.face_shapes]
+    outs = []
+    for centre in (1, 0):
+        sc.set_tuning(_lib.TUNE_MIDPOINT_CENTRE, centre)
+        mid = sc.alloc_faces()
+        psi = [torch.zeros(s + (3,), device="cuda") for s in sc.face_shapes]
+        T = [torch.zeros(s + (3,), device="cuda") for s in sc.face_shapes]
+        sc.midpoint(u, mid, 0.7 * dx, psi_out=psi, T_out=T)
+        torch.cuda.synchronize()
+        outs.append(list(mid) + psi + T)
+    for x, y in zip(*outs):
+        assert torch.equal(x, y)
