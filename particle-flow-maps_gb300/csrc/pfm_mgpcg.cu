@@ -394,6 +394,58 @@ __device__ __forceinline__ void ld8(const __nv_bfloat16* p, float (&v)[8]) { ld8
 __device__ __forceinline__ void st8(__half* p, const float (&v)[8]) { st8h(p, v); }
 __device__ __forceinline__ void st8(__nv_bfloat16* p, const float (&v)[8]) { st8h(p, v); }
 
+// The same update in 3D for the x and y face families with one thread per run of eight faces
+// along the last axis (whole vectors of u and of the two pressure rows; the row index decides the
+// boundary terms for the whole run); needs N2 % 8 == 0.  Element for element k_subtract_grad_p.
+template <int fam>
+__global__ void __launch_bounds__(256) k_subtract_grad_p8(float* __restrict__ u, const float* __restrict__ p,
+                                                          MacGeom g, int lo_neu, int hi_neu) {
+  static_assert(fam == 0 || fam == 1, "runs along the last axis: the x and y faces");
+  const int N0 = g.N[0], N1 = g.N[1], N2 = g.N[2];
+  const int n1 = g.n[fam][1], runs = N2 >> 3;
+  const unsigned e = blockIdx.x * blockDim.x + threadIdx.x;
+  if ((int64_t)e >= (int64_t)g.n[fam][0] * n1 * runs) return;
+  const unsigned row = e / (unsigned)runs;
+  const int k0 = (int)(e - row * (unsigned)runs) * 8;
+  const unsigned i_ = udiv(row, g.dn[fam][1]);
+  const int i = (int)i_, j = (int)(row - i_ * (unsigned)n1);
+  const int a = fam == 0 ? i : j, Nf = fam == 0 ? N0 : N1;
+  auto clampi = [](int v, int n) { return v < 0 ? 0 : (v > n - 1 ? n - 1 : v); };
+  const int hi_a = clampi(a, Nf), lo_a = clampi(a - 1, Nf);
+  const int64_t pr_row = fam == 0 ? ((int64_t)hi_a * N1 + j) * N2 : ((int64_t)i * N1 + hi_a) * N2;
+  const int64_t pl_row = fam == 0 ? ((int64_t)lo_a * N1 + j) * N2 : ((int64_t)i * N1 + lo_a) * N2;
+  const int64_t c0 = ((int64_t)i * n1 + j) * N2 + k0;
+  float uv[8], pr[8], pl[8];
+  ld8(u + c0, uv);
+  ld8(p + pr_row + k0, pr);
+  ld8(p + pl_row + k0, pl);
+  const bool zl = a - 1 < 0, zr = a >= Nf, wall = (a == 0 && lo_neu) || (a == Nf && hi_neu);
+  float out[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const float r = zr ? 0.f : pr[q], l = zl ? 0.f : pl[q];
+    out[q] = wall ? 0.f : uv[q] - (r - l);
+  }
+  st8(u + c0, out);
+}
+
+// k_subtract_grad_p of face family f, as runs of eight faces where the family and grid allow
+template <int D>
+static void launch_subtract_grad_p(pfm_handle* h, int f, float* u, const float* p, int lo, int hi, cudaStream_t s) {
+  const MacGeom& g = h->geom;
+  const int64_t nf = (int64_t)g.n[f][0] * g.n[f][1] * g.n[f][2];
+  if (D == 3 && f < 2 && g.N[2] % 8 == 0) {
+    const unsigned nb = grid_for(nf / 8, 256);
+    if (f == 0) launch(h, k_subtract_grad_p8<0>, nb, 256, 0, s, u, p, g, lo, hi);
+    if (f == 1) launch(h, k_subtract_grad_p8<1>, nb, 256, 0, s, u, p, g, lo, hi);
+    return;
+  }
+  if (f == 0) launch(h, k_subtract_grad_p<D, 0>, grid_for(nf, 256), 256, 0, s, u, p, g, lo, hi);
+  if (f == 1) launch(h, k_subtract_grad_p<D, 1>, grid_for(nf, 256), 256, 0, s, u, p, g, lo, hi);
+  if (D == 3 && f == 2) launch(h, k_subtract_grad_p<3, 2>, grid_for(nf, 256), 256, 0, s, u, p, g, lo, hi);
+}
+
+
 // smooth(l, phase) in 3D with one thread per run of eight cells along the last axis: the run, r
 // and the four neighbouring runs are read as whole vectors (the cells of the other colour, which a
 // half-sweep never changes, are written back unchanged) and each cell of the colour is updated
@@ -1702,7 +1754,7 @@ static int append_solve_loop(GraphCursor& gc, K& k) {
 // The kernels of one MGPCG.solve (3D/mgpcg.py:202-280) with level storage S (float: the reference
 // solve; __half / __nv_bfloat16: the mixed solve, which also accumulates every inner product in
 // f64), grouped as the graphs use them:
-//   setup:  x (unless warm-started) = p = Ap = 0, recenter, [b = r0, b.b, r0 = b - A x for a warm
+//   setup:  x (unless warm-started) = p = 0, recenter, [b = r0, b.b, r0 = b - A x for a warm
 //           start], r0.r0, first V-cycle, p = z, z.r, and the first half of iteration 1 (Ap,
 //           alpha, x/r update, convergence test [, true residual]);
 //   body:   one WHILE iteration: the second half of iteration k and the first half of k+1, then
@@ -1778,11 +1830,11 @@ struct SolveKernels {
              o.true_residual_every);
   }
   void setup(cudaStream_t q) {
-    // init(): x = p = Ap = 0 (3D/mgpcg.py:63-79); z0 is zeroed by the V-cycle
+    // init(): x = p = Ap = 0 (3D/mgpcg.py:63-79); z0 is zeroed by the V-cycle, and Ap needs no
+    // zeroing: k_Ap_dot writes every element before k_update_xr reads it
     cudaMemsetAsync(st, 0, sizeof(SolveState), q);
     if (!warm) cudaMemsetAsync(x, 0, n * 4, q);
     cudaMemsetAsync(p, 0, n * 4, q);
-    cudaMemsetAsync(Ap, 0, n * 4, q);
     recenter(q, false);
     if (keep_b) {
       cudaMemcpyAsync(bvec, r0, n * 4, cudaMemcpyDeviceToDevice, q);
@@ -1997,11 +2049,8 @@ static int poisson_impl(pfm_handle* h, float* const* u, float* p_out, const pfm_
   const float* x = ws_ptr<float>(h, h->o_x);
   if (solve_rc != PFM_OK && solve_rc != PFM_ERR_NOT_CONVERGED) return solve_rc;
   for (int f = 0; f < D; ++f) {
-    int64_t nf = (int64_t)g.n[f][0] * g.n[f][1] * g.n[f][2];
     const int lo = h->cfg.boundary[f][0] == 2, hi = h->cfg.boundary[f][1] == 2;
-    if (f == 0) launch(h, k_subtract_grad_p<D, 0>, grid_for(nf, 256), 256, 0, s, u[f], x, g, lo, hi);
-    if (f == 1) launch(h, k_subtract_grad_p<D, 1>, grid_for(nf, 256), 256, 0, s, u[f], x, g, lo, hi);
-    if (f == 2) launch(h, k_subtract_grad_p<D, 2>, grid_for(nf, 256), 256, 0, s, u[f], x, g, lo, hi);
+    launch_subtract_grad_p<D>(h, f, u[f], x, lo, hi, s);
   }
   rc = launch_check(h, "subtract_grad_p");
   if (rc) return rc;
@@ -2088,18 +2137,13 @@ int append_poisson_post(GraphCursor& gc, float* const* u, float* p_io) {
   pfm_handle* h = gc.h;
   if (gc.rc) return gc.rc;
   const int D = h->cfg.dim;
-  const MacGeom& g = h->geom;
   float* x = ws_ptr<float>(h, h->o_x);
   cudaStream_t q = gc.seg();
   if (p_io) cudaMemcpyAsync(p_io, x, h->cells * 4, cudaMemcpyDeviceToDevice, q);
   for (int f = 0; f < D; ++f) {
-    const int64_t nf = (int64_t)g.n[f][0] * g.n[f][1] * g.n[f][2];
     const int lo = h->cfg.boundary[f][0] == 2, hi = h->cfg.boundary[f][1] == 2;
-    if (D == 3 && f == 0) launch(h, k_subtract_grad_p<3, 0>, grid_for(nf, 256), 256, 0, q, u[f], (const float*)x, g, lo, hi);
-    if (D == 3 && f == 1) launch(h, k_subtract_grad_p<3, 1>, grid_for(nf, 256), 256, 0, q, u[f], (const float*)x, g, lo, hi);
-    if (D == 3 && f == 2) launch(h, k_subtract_grad_p<3, 2>, grid_for(nf, 256), 256, 0, q, u[f], (const float*)x, g, lo, hi);
-    if (D == 2 && f == 0) launch(h, k_subtract_grad_p<2, 0>, grid_for(nf, 256), 256, 0, q, u[f], (const float*)x, g, lo, hi);
-    if (D == 2 && f == 1) launch(h, k_subtract_grad_p<2, 1>, grid_for(nf, 256), 256, 0, q, u[f], (const float*)x, g, lo, hi);
+    if (D == 3) launch_subtract_grad_p<3>(h, f, u[f], x, lo, hi, q);
+    else launch_subtract_grad_p<2>(h, f, u[f], x, lo, hi, q);
   }
   return gc.rc;
 }
@@ -2507,17 +2551,12 @@ int pfm_subtract_grad_p(pfm_handle* h, float* u_x, float* u_y, float* u_z, const
   if (!h) return PFM_ERR_NULL;
   const int D = h->cfg.dim;
   if (!u_x || !u_y || (D == 3 && !u_z) || !p) return set_error(h, PFM_ERR_NULL, "pfm_subtract_grad_p: null input");
-  const MacGeom& g = h->geom;
   cudaStream_t s = (cudaStream_t)stream;
   float* u[3] = {u_x, u_y, u_z};
   for (int f = 0; f < D; ++f) {
-    const unsigned nf = (unsigned)((int64_t)g.n[f][0] * g.n[f][1] * g.n[f][2]);
     // lo/hi = 0: the gradient subtraction alone; the boundary faces are left to pfm_apply_bc
-    if (D == 3 && f == 0) launch(h, k_subtract_grad_p<3, 0>, grid_for(nf, 256), 256, 0, s, u[f], p, g, 0, 0);
-    if (D == 3 && f == 1) launch(h, k_subtract_grad_p<3, 1>, grid_for(nf, 256), 256, 0, s, u[f], p, g, 0, 0);
-    if (D == 3 && f == 2) launch(h, k_subtract_grad_p<3, 2>, grid_for(nf, 256), 256, 0, s, u[f], p, g, 0, 0);
-    if (D == 2 && f == 0) launch(h, k_subtract_grad_p<2, 0>, grid_for(nf, 256), 256, 0, s, u[f], p, g, 0, 0);
-    if (D == 2 && f == 1) launch(h, k_subtract_grad_p<2, 1>, grid_for(nf, 256), 256, 0, s, u[f], p, g, 0, 0);
+    if (D == 3) launch_subtract_grad_p<3>(h, f, u[f], p, 0, 0, s);
+    else launch_subtract_grad_p<2>(h, f, u[f], p, 0, 0, s);
   }
   return launch_check(h, "pfm_subtract_grad_p");
 }
