@@ -686,6 +686,31 @@ __global__ void __launch_bounds__(kBinThreads) k_normalize3(FaceOut3 out, int64_
   if (wv > 0.f) u[e] = u[e] / wv;
 }
 
+// The same division four faces at a time (16-byte vectors of u and w; every family's face count a
+// multiple of 4 and the six arrays 16-byte aligned): element for element k_normalize3.
+__global__ void __launch_bounds__(kBinThreads) k_normalize3v(FaceOut3 out, int64_t Q0, int64_t Q1, int64_t Q2) {
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int f = 0;
+  if (e >= Q0) {
+    e -= Q0;
+    f = 1;
+    if (e >= Q1) {
+      e -= Q1;
+      f = 2;
+      if (e >= Q2) return;
+    }
+  }
+  float4* u = reinterpret_cast<float4*>(f == 0 ? out.u[0] : (f == 1 ? out.u[1] : out.u[2]));
+  const float4* w = reinterpret_cast<const float4*>(f == 0 ? out.w[0] : (f == 1 ? out.w[1] : out.w[2]));
+  const float4 wv = w[e];
+  float4 uv = u[e];
+  if (wv.x > 0.f) uv.x = uv.x / wv.x;
+  if (wv.y > 0.f) uv.y = uv.y / wv.y;
+  if (wv.z > 0.f) uv.z = uv.z / wv.z;
+  if (wv.w > 0.f) uv.w = uv.w / wv.w;
+  u[e] = uv;
+}
+
 // Column gather (2D): columns along j; 2D normalises with scale = 1/w (run_2D.py:599-611) and
 // also carries the reference map psi.
 template <int fam>
@@ -873,7 +898,14 @@ int p2g3_from_records(pfm_handle* h, float* const* us, float* const* ws, cudaStr
           launch(h, tile, dim3(bz, by, bx), kTileThreads, kTileSmem, st, pos4, famrec, order, start, h->geom, h->P,
                  px, py, pz, out);
         }
-    launch(h, k_normalize3, grid_for(F[0] + F[1] + F[2], kBinThreads), kBinThreads, 0, st, out, F[0], F[1], F[2]);
+    bool vec = true;
+    for (int f = 0; f < 3; ++f)
+      vec = vec && F[f] % 4 == 0 && ((uintptr_t)us[f] | (uintptr_t)ws[f]) % 16 == 0;
+    if (vec)
+      launch(h, k_normalize3v, grid_for((F[0] + F[1] + F[2]) / 4, kBinThreads), kBinThreads, 0, st, out, F[0] / 4,
+             F[1] / 4, F[2] / 4);
+    else
+      launch(h, k_normalize3, grid_for(F[0] + F[1] + F[2], kBinThreads), kBinThreads, 0, st, out, F[0], F[1], F[2]);
   }
   return launch_check(h, "p2g3");
 }
