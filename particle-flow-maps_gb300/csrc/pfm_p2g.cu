@@ -144,6 +144,23 @@ __global__ void __launch_bounds__(kBinThreads) k_scatter_order(const int* __rest
   order[start[key[q]] + slot[q]] = (int)q;
 }
 
+// The same scatter for four consecutive particles per thread (16-byte loads of their keys and
+// slots, the four bin-start lookups in flight together); needs P % 4 == 0.
+__global__ void __launch_bounds__(kBinThreads) k_scatter_order4(const int4* __restrict__ key4,
+                                                                const int4* __restrict__ slot4,
+                                                                const int* __restrict__ start, int64_t P4,
+                                                                int* __restrict__ order) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= P4) return;
+  const int4 k = key4[t], sl = slot4[t];
+  const int s0 = start[k.x], s1 = start[k.y], s2 = start[k.z], s3 = start[k.w];
+  const int q = (int)(4 * t);
+  order[s0 + sl.x] = q;
+  order[s1 + sl.y] = q + 1;
+  order[s2 + sl.z] = q + 2;
+  order[s3 + sl.w] = q + 3;
+}
+
 // each bin in ascending particle index: the stable order of a CPU counting sort.  Bins of up to
 // kSmallBin entries here, one thread per bin; larger ones in k_bin_sort_big (pfm_binsort.cuh).
 __global__ void __launch_bounds__(kBinThreads) k_cell_sort(const int* __restrict__ start, int64_t C,
@@ -822,7 +839,11 @@ static int sort_from_keys(pfm_handle* h, cudaStream_t st) {
   launch(h, k_scan_top, 1, kScanThreads, 0, st, bsum, nb);
   launch(h, k_scan_apply, nb, kScanThreads, 0, st, (const int*)count, C, (const int*)bsum, start, (int)P);
   if (P > 0) {
-    launch(h, k_scatter_order, grid_for(P, kBinThreads), kBinThreads, 0, st, key, slot, (const int*)start, P, order);
+    if (P % 4 == 0 && ((uintptr_t)key | (uintptr_t)slot) % 16 == 0)
+      launch(h, k_scatter_order4, grid_for(P / 4, kBinThreads), kBinThreads, 0, st, (const int4*)key,
+             (const int4*)slot, (const int*)start, P / 4, order);
+    else
+      launch(h, k_scatter_order, grid_for(P, kBinThreads), kBinThreads, 0, st, key, slot, (const int*)start, P, order);
     launch(h, k_cell_sort, grid_for(C, kBinThreads), kBinThreads, 0, st, (const int*)start, C, order);
     launch(h, k_bin_sort_big, grid_for(C, kBigThreads), kBigThreads, 0, st, (const int*)start, C, order);
   }
