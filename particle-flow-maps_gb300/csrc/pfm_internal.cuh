@@ -448,6 +448,13 @@ inline void with_cube(const pfm_handle* h, Fn&& f) {
   }
 }
 
+// Loads and stores of particle state that a thread touches once (the RK4's inputs and outputs):
+// the evict-first (streaming) cache operators, so that they do not displace the grid rows the
+// interpolations reuse (RK4 at 256^3: 14.83 against 15.12 ms with the default operators).
+__device__ __forceinline__ float ld_stream(const float* p) { return __ldcs(p); }
+template <class T>
+__device__ __forceinline__ void st_stream(T* p, T v) { __stcs(p, v); }
+
 // P2G particle record and cell key (3D), shared by the payload pass and the fused RK4 + P2G:
 //   pos4[q]      = (pos/dx, 0)
 //   famrec[f][q] = (m_f, dx (T C T)_f row), m = T_gm^T-composed init_imp, T C T = T_gm^T init_C T_gm
@@ -476,7 +483,7 @@ __device__ __forceinline__ void write_p2g_record3(const P2GRecords3& R, int64_t 
     c[a] = ci < 0 ? 0 : (ci > g.N[a] - 1 ? g.N[a] - 1 : ci);
   }
   const int k = (c[0] * g.N[1] + c[1]) * g.N[2] + c[2];
-  R.key[q] = k;
+  st_stream(R.key + q, k);
   R.slot[q] = atomicAdd(&R.count[k], 1);
   float Cm[3][3], N[3][3];
 #pragma unroll
@@ -499,14 +506,14 @@ __device__ __forceinline__ void write_p2g_record3(const P2GRecords3& R, int64_t 
       TCT[r][cc] = A[0][r] * CA[0][cc] + A[1][r] * CA[1][cc] + A[2][r] * CA[2][cc];
       TT[r][cc] = A[0][r] * N[0][cc] + A[1][r] * N[1][cc] + A[2][r] * N[2][cc];
     }
-  const float m0[3] = {R.imp0[q], R.imp0[P + q], R.imp0[2 * P + q]};
+  const float m0[3] = {ld_stream(R.imp0 + q), ld_stream(R.imp0 + P + q), ld_stream(R.imp0 + 2 * P + q)};
   float m[3];
 #pragma unroll
   for (int r = 0; r < 3; ++r) m[r] = TT[r][0] * m0[0] + TT[r][1] * m0[1] + TT[r][2] * m0[2];
-  R.pos4[q] = make_float4(v[0], v[1], v[2], 0.f);
+  st_stream(R.pos4 + q, make_float4(v[0], v[1], v[2], 0.f));
 #pragma unroll
   for (int f = 0; f < 3; ++f)
-    R.famrec[f * P + q] = make_float4(m[f], TCT[f][0] * g.dx, TCT[f][1] * g.dx, TCT[f][2] * g.dx);
+    st_stream(R.famrec + f * P + q, make_float4(m[f], TCT[f][0] * g.dx, TCT[f][1] * g.dx, TCT[f][2] * g.dx));
 }
 
 // Launches RK4_T_forward (3D); with R non-null the kernel also writes the P2G records and keys

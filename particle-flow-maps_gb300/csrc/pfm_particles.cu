@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(kRK4Threads, PFM_RK4_MINB) k_rk4_T_forward3(fl
   int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= P) return;
   if (dt_dev) dt = *dt_dev;  // the whole-step graph keeps dt on the device
-  float p0[3] = {pos[q], pos[P + q], pos[2 * P + q]};
+  float p0[3] = {ld_stream(pos + q), ld_stream(pos + P + q), ld_stream(pos + 2 * P + q)};
   float T0[3][3];
   float u[3], G[3][3];  // the RK4 stage's velocity and gradient
   if (GRADM) {
@@ -125,8 +125,8 @@ __global__ void __launch_bounds__(kRK4Threads, PFM_RK4_MINB) k_rk4_T_forward3(fl
     for (int v = 0; v < 3; ++v)
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        M[c][v] = T[(v * 3 + c) * P + q];   // M[r][k] = T_gm_k[r]
-        N[c][v] = Ti[(v * 3 + c) * P + q];  // N[k][c] = T_init_c[k]
+        M[c][v] = ld_stream(T + (v * 3 + c) * P + q);   // M[r][k] = T_gm_k[r]
+        N[c][v] = ld_stream(Ti + (v * 3 + c) * P + q);  // N[k][c] = T_init_c[k]
       }
 #pragma unroll
     for (int c = 0; c < 3; ++c)
@@ -141,7 +141,7 @@ __global__ void __launch_bounds__(kRK4Threads, PFM_RK4_MINB) k_rk4_T_forward3(fl
 #pragma unroll
     for (int v = 0; v < 3; ++v)
 #pragma unroll
-      for (int c = 0; c < 3; ++c) T0[v][c] = T[(v * 3 + c) * P + q];
+      for (int c = 0; c < 3; ++c) T0[v][c] = ld_stream(T + (v * 3 + c) * P + q);
   }
   float pk[3] = {p0[0], p0[1], p0[2]};
   float Tk[3][3];
@@ -185,14 +185,14 @@ __global__ void __launch_bounds__(kRK4Threads, PFM_RK4_MINB) k_rk4_T_forward3(fl
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     pn[c] = p0[c] + coef * su[c];
-    pos[c * P + q] = pn[c];
+    st_stream(pos + c * P + q, pn[c]);
   }
 #pragma unroll
   for (int v = 0; v < 3; ++v)
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       Tn[v][c] = T0[v][c] - coef * sT[v][c];
-      T[(v * 3 + c) * P + q] = Tn[v][c];
+      st_stream(T + (v * 3 + c) * P + q, Tn[v][c]);
     }
   if (PAY) {
     const float v[3] = {pn[0] / g.dx, pn[1] / g.dx, pn[2] / g.dx};
