@@ -23,7 +23,7 @@ namespace pfm {
 
 constexpr int kBinThreads = 256;
 
-// cell key + slot in the bin (slot order is arbitrary here; fixed by k_cell_sort)
+// cell key + slot in the bin (slot order is arbitrary here; fixed by k_cell_sort_staged)
 template <int D>
 __global__ void __launch_bounds__(kBinThreads) k_bin_keys(const float* __restrict__ pos, int64_t P, MacGeom g,
                                                           int* __restrict__ key, int* __restrict__ slot,
@@ -161,14 +161,29 @@ __global__ void __launch_bounds__(kBinThreads) k_scatter_order4(const int4* __re
   order[s3 + sl.w] = q + 3;
 }
 
-// each bin in ascending particle index: the stable order of a CPU counting sort.  Bins of up to
-// kSmallBin entries here, one thread per bin; larger ones in k_bin_sort_big (pfm_binsort.cuh).
-__global__ void __launch_bounds__(kBinThreads) k_cell_sort(const int* __restrict__ start, int64_t C,
-                                                           int* __restrict__ order) {
-  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= C) return;
-  const int b = start[c], e = start[c + 1];
-  sort_bin_by_thread(order, b, e - b);
+// Each bin in ascending particle index: the stable order of a CPU counting sort.  One thread per
+// bin of up to kSmallBin entries (larger ones are left to k_bin_sort_big, pfm_binsort.cuh), with
+// the block's span of `order` staged in shared memory: the 256 consecutive bins of a block are one
+// contiguous run of entries, read and written back with coalesced accesses, and each thread sorts
+// its bin there.  A block whose run exceeds the stage (large bins among its cells) sorts its bins
+// in global memory.
+constexpr int kSortStage = 4096;  // entries a block stages (16 KB; 8 per cell on average is 2,048)
+__global__ void __launch_bounds__(kBinThreads) k_cell_sort_staged(const int* __restrict__ start, int64_t C,
+                                                                  int* __restrict__ order) {
+  __shared__ int stage[kSortStage];
+  const int64_t c0 = (int64_t)blockIdx.x * kBinThreads, c = c0 + threadIdx.x;
+  const int64_t cend = C < c0 + kBinThreads ? C : c0 + kBinThreads;
+  const int base = start[c0], span = start[cend] - base;
+  const int b = c < C ? start[c] : 0, e = c < C ? start[c + 1] : 0;
+  if (span > kSortStage) {  // the same for the whole block
+    if (c < C) sort_bin_by_thread(order, b, e - b);
+    return;
+  }
+  for (int i = threadIdx.x; i < span; i += kBinThreads) stage[i] = order[base + i];
+  __syncthreads();
+  if (c < C) sort_bin_by_thread(stage, b - base, e - b);
+  __syncthreads();
+  for (int i = threadIdx.x; i < span; i += kBinThreads) order[base + i] = stage[i];
 }
 
 // Payload and cell keys (3D), one pass in particle order q (coalesced reads and writes); the
@@ -844,7 +859,7 @@ static int sort_from_keys(pfm_handle* h, cudaStream_t st) {
              (const int4*)slot, (const int*)start, P / 4, order);
     else
       launch(h, k_scatter_order, grid_for(P, kBinThreads), kBinThreads, 0, st, key, slot, (const int*)start, P, order);
-    launch(h, k_cell_sort, grid_for(C, kBinThreads), kBinThreads, 0, st, (const int*)start, C, order);
+    launch(h, k_cell_sort_staged, grid_for(C, kBinThreads), kBinThreads, 0, st, (const int*)start, C, order);
     launch(h, k_bin_sort_big, grid_for(C, kBigThreads), kBigThreads, 0, st, (const int*)start, C, order);
   }
   return launch_check(h, "sort_particles");
