@@ -394,6 +394,91 @@ __device__ __forceinline__ void ld8(const __nv_bfloat16* p, float (&v)[8]) { ld8
 __device__ __forceinline__ void st8(__half* p, const float (&v)[8]) { st8h(p, v); }
 __device__ __forceinline__ void st8(__nv_bfloat16* p, const float (&v)[8]) { st8h(p, v); }
 
+// k_divergence in 3D with one thread per run of eight cells along the last axis (Lv.n2 % 8 == 0):
+// whole vectors of the x and y faces on either side, the nine z faces of the run one by one (their
+// rows are n2 + 1 long).  The same sum, in the same order, per cell.
+__global__ void __launch_bounds__(256) k_divergence8(const float* __restrict__ ux, const float* __restrict__ uy,
+                                                     const float* __restrict__ uz, Lvl L, float* __restrict__ r0,
+                                                     float scale) {
+  const int runs = L.n2 >> 3;
+  const unsigned e = blockIdx.x * blockDim.x + threadIdx.x;
+  if ((int64_t)e >= (int64_t)L.n0 * L.n1 * runs) return;
+  const unsigned row = e / (unsigned)runs;
+  const int k0 = (int)(e - row * (unsigned)runs) * 8;
+  const unsigned i_ = udiv(row, L.d1);
+  const int i = (int)i_, j = (int)(row - i_ * (unsigned)L.n1);
+  float vl[8], vr[8], vb[8], vt[8], z[9], out[8];
+  ld8(ux + ((int64_t)i * L.n1 + j) * L.n2 + k0, vl);
+  ld8(ux + ((int64_t)(i + 1) * L.n1 + j) * L.n2 + k0, vr);
+  ld8(uy + ((int64_t)i * (L.n1 + 1) + j) * L.n2 + k0, vb);
+  ld8(uy + ((int64_t)i * (L.n1 + 1) + j + 1) * L.n2 + k0, vt);
+  const float* zr = uz + ((int64_t)i * L.n1 + j) * (L.n2 + 1) + k0;
+#pragma unroll
+  for (int q = 0; q < 9; ++q) z[q] = zr[q];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) out[q] = (vr[q] - vl[q] + vt[q] - vb[q] + z[q + 1] - z[q]) * scale;
+  st8(r0 + ((int64_t)i * L.n1 + j) * L.n2 + k0, out);
+}
+
+// k_residual in 3D with one thread per run of eight cells along the last axis (L.n2 % 8 == 0):
+// x, b and the four neighbouring runs of x as whole vectors, each cell's neighbour sum in
+// stencil<3>'s order.  The same residual per cell.
+__global__ void __launch_bounds__(256) k_residual8(float* __restrict__ r, const float* __restrict__ b,
+                                                   const float* __restrict__ x, Lvl L, BC bc) {
+  const int runs = L.n2 >> 3;
+  const unsigned e = blockIdx.x * blockDim.x + threadIdx.x;
+  if ((int64_t)e >= (int64_t)L.n0 * L.n1 * runs) return;
+  const unsigned row = e / (unsigned)runs;
+  const int k0 = (int)(e - row * (unsigned)runs) * 8;
+  const unsigned i_ = udiv(row, L.d1);
+  const int i = (int)i_, j = (int)(row - i_ * (unsigned)L.n1);
+  const int64_t sx = (int64_t)L.n1 * L.n2, sy = L.n2;
+  const int64_t c0 = ((int64_t)i * L.n1 + j) * L.n2 + k0;
+  float xc[8], bb[8], xp[8], xm[8], yp[8], ym[8], out[8];
+  ld8(x + c0, xc);
+  ld8(b + c0, bb);
+  const bool hx = i < L.n0 - 1, lx = i > 0, hy = j < L.n1 - 1, ly = j > 0;
+  if (hx) ld8(x + c0 + sx, xp);
+  if (lx) ld8(x + c0 - sx, xm);
+  if (hy) ld8(x + c0 + sy, yp);
+  if (ly) ld8(x + c0 - sy, ym);
+  const float zl = k0 > 0 ? x[c0 - 1] : 0.f;
+  const float zr = k0 + 8 < L.n2 ? x[c0 + 8] : 0.f;
+  float base = 6.f;
+  if (i <= 0 && bc.lo[0] == 2) base -= 1.f;
+  if (i >= L.n0 - 1 && bc.hi[0] == 2) base -= 1.f;
+  if (j <= 0 && bc.lo[1] == 2) base -= 1.f;
+  if (j >= L.n1 - 1 && bc.hi[1] == 2) base -= 1.f;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int k = k0 + q;
+    float nb = 0.f;
+    if (hx) nb += xp[q];
+    if (lx) nb += xm[q];
+    if (hy) nb += yp[q];
+    if (ly) nb += ym[q];
+    if (k < L.n2 - 1) nb += (q < 7) ? xc[q + 1] : zr;
+    if (k > 0) nb += (q > 0) ? xc[q - 1] : zl;
+    float mult = base;
+    if (k <= 0 && bc.lo[2] == 2) mult -= 1.f;
+    if (k >= L.n2 - 1 && bc.hi[2] == 2) mult -= 1.f;
+    out[q] = bb[q] - (mult * xc[q] - nb);
+  }
+  st8(r + c0, out);
+}
+
+// The divergence of the finest level times scale into out, as runs of eight cells where the grid
+// allows.
+template <int D>
+static void launch_divergence(pfm_handle* h, const float* ux, const float* uy, const float* uz, float* out,
+                              float scale, cudaStream_t s) {
+  const Lvl L = lvl_of(h, 0);
+  if (D == 3 && L.n2 % 8 == 0)
+    launch(h, k_divergence8, grid_for(L.count / 8, 256), 256, 0, s, ux, uy, uz, L, out, scale);
+  else
+    launch(h, k_divergence<D>, grid_for(h->cells, 256), 256, 0, s, ux, uy, uz, L, out, scale);
+}
+
 // The same update in 3D for the x and y face families with one thread per run of eight faces
 // along the last axis (whole vectors of u and of the two pressure rows; the row index decides the
 // boundary terms for the whole run); needs N2 % 8 == 0.  Element for element k_subtract_grad_p.
@@ -1841,7 +1926,12 @@ struct SolveKernels {
       launch(h, k_dot<float>, red_blocks(n), kReduceThreads, 0, q, (const float*)bvec, (const float*)bvec, n, rb,
              (int)RED_BTB, o.eps, inv_n, mi, 1);
     }
-    if (warm) launch(h, k_residual<D>, stream_blocks(n), 256, 0, q, r0, (const float*)bvec, (const float*)x, L0, bc);
+    if (warm) {
+      if (D == 3 && L0.n2 % 8 == 0)
+        launch(h, k_residual8, grid_for(n / 8, 256), 256, 0, q, r0, (const float*)bvec, (const float*)x, L0, bc);
+      else
+        launch(h, k_residual<D>, stream_blocks(n), 256, 0, q, r0, (const float*)bvec, (const float*)x, L0, bc);
+    }
     if (replace) launch(h, k_x_to64, stream_blocks(n), 256, 0, q, x64, (const float*)x, n, (const SolveState*)st);
     launch(h, k_dot<float>, red_blocks(n), kReduceThreads, 0, q, (const float*)r0, (const float*)r0, n, rb,
            (int)RED_RTR0, o.eps, inv_n, mi, f64);
@@ -2041,8 +2131,7 @@ static int poisson_impl(pfm_handle* h, float* const* u, float* p_out, const pfm_
                                                           h->cfg.boundary[f][1] == 2);
   }
   float* r0 = ws_ptr<float>(h, h->o_r[0]);
-  launch(h, k_divergence<D>, grid_for(h->cells, 256), 256, 0, s, u[0], u[1], D == 3 ? u[2] : nullptr, lvl_of(h, 0),
-         r0, -1.f);
+  launch_divergence<D>(h, u[0], u[1], D == 3 ? u[2] : nullptr, r0, -1.f, s);
   rc = launch_check(h, "divergence");
   if (rc) return rc;
   int solve_rc = mgpcg_solve_in_place(h, p_out, opts, stats, s);
@@ -2113,10 +2202,9 @@ int append_poisson_pre(GraphCursor& gc, float* const* u, float* p_io, const pfm_
   float* r0 = ws_ptr<float>(h, h->o_r[0]);
   float* x = ws_ptr<float>(h, h->o_x);
   if (D == 3)
-    launch(h, k_divergence<3>, grid_for(h->cells, 256), 256, 0, q, u[0], u[1], u[2], lvl_of(h, 0), r0, -1.f);
+    launch_divergence<3>(h, u[0], u[1], u[2], r0, -1.f, q);
   else
-    launch(h, k_divergence<2>, grid_for(h->cells, 256), 256, 0, q, u[0], u[1], (const float*)nullptr, lvl_of(h, 0), r0,
-           -1.f);
+    launch_divergence<2>(h, u[0], u[1], nullptr, r0, -1.f, q);
   if (o.warm_start && !gc.rc) gc.rc = warm_start_init(h, x, p_io, o.warm_start, q);
   dispatch_solve(D, o.precision, [&](auto dd, auto ss) {
     SolveKernels<decltype(dd)::value, decltype(ss)> K(h, o);
@@ -2540,10 +2628,9 @@ int pfm_divergence(pfm_handle* h, const float* u_x, const float* u_y, const floa
   if (!u_x || !u_y || (D == 3 && !u_z) || !div_out) return set_error(h, PFM_ERR_NULL, "pfm_divergence: null input");
   cudaStream_t s = (cudaStream_t)stream;
   if (D == 3)
-    launch(h, k_divergence<3>, grid_for(h->cells, 256), 256, 0, s, u_x, u_y, u_z, lvl_of(h, 0), div_out, 1.f);
+    launch_divergence<3>(h, u_x, u_y, u_z, div_out, 1.f, s);
   else
-    launch(h, k_divergence<2>, grid_for(h->cells, 256), 256, 0, s, u_x, u_y, (const float*)nullptr, lvl_of(h, 0),
-           div_out, 1.f);
+    launch_divergence<2>(h, u_x, u_y, nullptr, div_out, 1.f, s);
   return launch_check(h, "pfm_divergence");
 }
 
