@@ -92,3 +92,15 @@ def test_reinit_schedule_3d_vs_2d():
     assert [k for _, k in s3] == [(i % 2 == 0) for i in range(12)]
     s2 = sched(12, 5, 2, False)
     assert s2[5] == (True, True) and s2[6] == (False, False) and s2[7] == (False, True)
+
+
+def test_solve_option_warm_start_values():
+    """Scene._opts maps the Python warm_start values to the C field (False/True -> 0/1, 2 and 3 as
+    given) and rejects anything else on the host."""
+    import pfm
+    from pfm.core import Scene
+    for v, want in ((False, 0), (True, 1), (0, 0), (1, 1), (2, 2), (3, 3), (None, 0)):
+        assert Scene._opts(400, 1e-6, 2, 4, warm_start=v).warm_start == want, v
+    for bad in (4, -1, "quad"):
+        with pytest.raises(pfm.PfmError):
+            Scene._opts(400, 1e-6, 2, 4, warm_start=bad)
