@@ -40,12 +40,15 @@ def main():
     ap.add_argument("--at", type=int, nargs="+", default=[1, 10, 50])
     ap.add_argument("--oracle-tol", type=float, default=1e-8, help="relative residual of the FP64 oracle solve")
     ap.add_argument("--arms", nargs="+", default=["plain", "mixed"])
+    ap.add_argument("--warm-start", type=int, default=3, choices=[1, 2, 3],
+                    help="the mixed arm's initial guess (as bench.py): previous pressure, linear or quadratic "
+                         "extrapolation")
     args = ap.parse_args()
     import torch
     import bench
     import oracle as O
     arms = {"plain": dict(tol=1e-6, tol_mode=1, max_iters=400),
-            "mixed": dict(tol=1e-6, tol_mode=2, max_iters=400, precision="fp16", warm_start=True,
+            "mixed": dict(tol=1e-6, tol_mode=2, max_iters=400, precision="fp16", warm_start=args.warm_start,
                           true_residual_every=5)}
     for arm in args.arms:
         sim = bench.make_sim(args.res, 2, arms[arm], graph=False)  # eager steps: the solves are host calls
