@@ -463,10 +463,9 @@ def main():
     # pre-midpoint and midpoint velocity grids once each
     rk4_bytes = P * 288 + 2 * F3 * 4
     achieved = rk4_bytes / (rk4_ms / 1e3) / 1e9
-    # DRAM bytes of one launch: dram__bytes_read.sum + dram__bytes_write.sum of the ncu capture of
+    # DRAM bytes of one launch: dram__bytes_read.sum + dram__bytes_write.sum of an ncu capture of
     # k_rk4_T_forward3<true, true> at 128^3 (1,671,280,384 + 3,168,529,152 B for 16,777,216
-    # particles, profiles/k_rk4_T_forward3_128.md), scaled by the particle count (the grid scales
-    # with it at a fixed particle density)
+    # particles), scaled by the particle count (the grid scales with it at a fixed particle density)
     traffic = (1671280384 + 3168529152) / 16777216 * P
     roofline = {"bound": "hbm", "kernel": "k_rk4_T_forward3", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
