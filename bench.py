@@ -172,6 +172,42 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def host_round_trip_steps(sim, host_u, steps, down, up):
+    """``steps`` steps whose grid velocity makes a round trip through pinned host memory: each step's
+    input is uploaded from ``host_u`` and its result read back into ``host_u``, so every step starts
+    from the previous step's result as read back.  The read-back of a step and the upload of the
+    next are issued per velocity component on two streams (device->host on ``down``, host->device on
+    ``up``): the upload of a component waits only for that component's read-back, so the two copy
+    directions run at once (one 67 MB face grid each way at 256^3: 0.41 ms together against 0.32 +
+    0.35 ms one after the other).  The step itself runs on the current stream, after the last upload."""
+    import torch
+    cur = torch.cuda.current_stream()
+    for d, h in zip(sim.u, host_u):
+        d.copy_(h, non_blocking=True)
+    for k in range(steps):
+        sim.step()
+        done = torch.cuda.Event()
+        done.record(cur)
+        down.wait_event(done)
+        last = k + 1 == steps
+        for d, h in zip(sim.u, host_u):
+            with torch.cuda.stream(down):
+                h.copy_(d, non_blocking=True)
+            if not last:
+                e = torch.cuda.Event()
+                e.record(down)
+                up.wait_event(e)
+                with torch.cuda.stream(up):
+                    d.copy_(h, non_blocking=True)
+        if not last:
+            e = torch.cuda.Event()
+            e.record(up)
+            cur.wait_event(e)
+    e = torch.cuda.Event()
+    e.record(down)
+    cur.wait_event(e)
+
+
 def measured_peak():
     path = os.path.join(REPO, "MEASURED_PEAKS.json")
     try:
@@ -490,19 +526,15 @@ def main():
     if not args.no_e2e:
         # through the same C-ABI calls, with the step's grid velocity uploaded from pinned host memory
         # and the projected result read back into the same host buffers every step: the velocity makes
-        # a round trip through the host, so each step starts from the previous step's result (the
-        # stream orders the read-back before the next upload) and the solves do the same work as in
-        # the device-timed steps
+        # a round trip through the host, so each step starts from the previous step's result (events
+        # order each component's read-back before its next upload) and the solves do the same work as
+        # in the device-timed steps
         host_u = [t.cpu().pin_memory() for t in sim.u]
+        down, up = torch.cuda.Stream(), torch.cuda.Stream()
         barrier()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record()
-        for _ in range(args.steps):
-            for d, h in zip(sim.u, host_u):
-                d.copy_(h, non_blocking=True)
-            sim.step()
-            for h, d in zip(host_u, sim.u):
-                h.copy_(d, non_blocking=True)
+        host_round_trip_steps(sim, host_u, args.steps, down, up)
         b.record()
         torch.cuda.synchronize()
         e_rate, _ = job_rate(a.elapsed_time(b) / 1e3, args.steps, world, dist, "cuda")

@@ -227,3 +227,35 @@ def test_step3d_full_size_properties(n):
         torch.cuda.empty_cache()
     for a, b in zip(*outs):
         assert torch.equal(a, b)
+
+
+def test_host_round_trip_equals_device_steps():
+    """The bench's end-to-end loop (bench.host_round_trip_steps: each step's velocity uploaded from
+    pinned host memory and read back, read-backs and uploads overlapped on two streams) gives
+    bitwise the velocity of the same steps run on the device alone: the events order every
+    component's read-back after its step and its upload before the next."""
+    import sys
+    import os
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    opts = dict(tol=1e-6, tol_mode=2, max_iters=400, check_every=4, precision="fp16", warm_start=3,
+                true_residual_every=5)
+    outs = []
+    for trip in (False, True):
+        sim = bench.make_sim(32, 2, opts, graph=True)
+        for _ in range(3):
+            sim.step()
+        torch.cuda.synchronize()
+        if trip:
+            host_u = [t.cpu().pin_memory() for t in sim.u]
+            bench.host_round_trip_steps(sim, host_u, 5, torch.cuda.Stream(), torch.cuda.Stream())
+            torch.cuda.synchronize()
+            outs.append([h.clone() for h in host_u])
+        else:
+            for _ in range(5):
+                sim.step()
+            torch.cuda.synchronize()
+            outs.append([t.cpu() for t in sim.u])
+        del sim
+    for a, b in zip(*outs):
+        assert torch.equal(a, b)
