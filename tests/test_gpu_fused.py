@@ -111,12 +111,13 @@ def test_cube_instances_equal_runtime_strides(n):
         assert torch.equal(x, y)
 
 
-def test_cube_instance_512_equals_runtime_strides():
-    """The 512^3 instances (the largest extent compiled in; its row offsets reach 2 MB) against the
-    runtime-stride kernels: the RK4 with the gradient reinitialisation on 2^20 particles spread
-    over the whole grid, and the three midpoint launches over every face.  Bitwise equal."""
+@pytest.mark.parametrize("n", [256, 512])
+def test_cube_instance_large_equals_runtime_strides(n):
+    """The 256^3 instances (the ones the 256^3 workload runs) and the 512^3 ones (the largest extent
+    compiled in; its row offsets reach 2 MB) against the runtime-stride kernels: the RK4 with the
+    gradient reinitialisation on 2^20 particles spread over the whole grid, and the three midpoint
+    launches over every face.  Bitwise equal."""
     from pfm import _lib
-    n = 512
     dx = 1.0 / n
     P = 1 << 20
     rng = np.random.default_rng(13)
