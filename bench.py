@@ -36,8 +36,10 @@ FALLBACK_HBM_GBS = 6800.0
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
+    # 20 steps: one particle reinitialisation cycle (reinit every 20 steps), so the timed window
+    # always holds one reseeding step and the solves that follow it
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--res", type=int, default=256)
     ap.add_argument("--ppc-axis", type=int, default=2)
