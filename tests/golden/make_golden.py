@@ -10,6 +10,7 @@ Run where the reference is checked out, with its root directory (the one holding
     python tests/golden/make_golden.py REFERENCE_ROOT ref3d_fields    # smoke transport + curl, 16x12x8
     python tests/golden/make_golden.py REFERENCE_ROOT ref2d_fields    # advect_smoke + curl, 32x24
     python tests/golden/make_golden.py REFERENCE_ROOT ref3d_variants  # the "evolve m" kernels, 12x10x8
+    python tests/golden/make_golden.py REFERENCE_ROOT ref3d_mgpcg     # MGPCG_3.Poisson, 32^3, 3 levels
 
 Taichi 1.5.0 is not installable here, so the reference modules are executed through
 ``oracle/ref_shim`` (a restatement of the Taichi semantics the step uses: f32 arithmetic,
@@ -649,9 +650,32 @@ def ref3d_variants():
     return out
 
 
+# ------------------------------------------------------------------------------------------------
+# 3D MGPCG with a deeper hierarchy: 32^3 -> 3 levels (32, 16, 8)
+# ------------------------------------------------------------------------------------------------
+def ref3d_mgpcg():
+    n = 32
+    R = load3d(hp3d((n, n, n)))
+    import mgpcg as MG
+    import taichi as ti
+    rng = np.random.default_rng(7)
+    s = MG.MGPCG_3(boundary_types=R.boundary_types, N=[n, n, n], base_level=3)
+    fx = ti.field(float, shape=(n + 1, n, n)); fy = ti.field(float, shape=(n, n + 1, n))
+    fz = ti.field(float, shape=(n, n, n + 1))
+    a, b, c = (smooth_field(f.shape, rng, 0.3, 1 / n) for f in (fx, fy, fz))
+    fx.from_numpy(a); fy.from_numpy(b); fz.from_numpy(c)
+    out = {"in_x": a, "in_y": b, "in_z": c, "levels": np.int32(s.n_mg_levels)}
+    log = io.StringIO()
+    with contextlib.redirect_stdout(log):
+        s.Poisson(fx, fy, fz)
+    out.update(u_x=fx.to_numpy(), u_y=fy.to_numpy(), u_z=fz.to_numpy(), p=s.p.to_numpy(),
+               iters=np.int32(parse_iters(log.getvalue())[-1]))
+    return out
+
+
 CASES = dict(ref3d_kernels=ref3d_kernels, ref2d_kernels=ref2d_kernels, ref3d_steps=ref3d_steps,
              ref2d_steps=ref2d_steps, ref3d_fields=ref3d_fields, ref2d_fields=ref2d_fields,
-             ref3d_variants=ref3d_variants)
+             ref3d_variants=ref3d_variants, ref3d_mgpcg=ref3d_mgpcg)
 
 if __name__ == "__main__":
     if len(sys.argv) != 3 or sys.argv[2] not in CASES:

@@ -56,6 +56,19 @@ def test_oracle_poisson_3d_bitexact(golden, case):
     assert np.array_equal(p, g[f"{case}_p"])
 
 
+def test_oracle_poisson_3d_three_levels_bitexact(golden):
+    """MGPCG_3.Poisson on a 32^3 grid: a V-cycle of three levels (32, 16, 8; the 16^3 cases above
+    have two), the reference's recursion of restriction, bottom sweeps and prolongation one level
+    deeper.  Same stopping iteration, bitwise the same velocity and pressure."""
+    g = golden("ref3d_mgpcg")
+    assert int(g["levels"]) == 3
+    ux, uy, uz, p, it, _ = O.poisson3(g["in_x"], g["in_y"], g["in_z"])
+    assert it == int(g["iters"])
+    for a, n in zip((ux, uy, uz), "xyz"):
+        assert np.array_equal(a, g[f"u_{n}"]), n
+    assert np.array_equal(p, g["p"])
+
+
 def test_oracle_kernels_2d(golden):
     g = golden("ref2d_kernels")
     dx = 1.0 / int(g["res"][1])
