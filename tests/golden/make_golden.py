@@ -6,6 +6,7 @@ Run where the reference is checked out, with its root directory (the one holding
     python tests/golden/make_golden.py REFERENCE_ROOT ref3d_kernels   # per-kernel cases, 3D
     python tests/golden/make_golden.py REFERENCE_ROOT ref2d_kernels   # per-kernel cases, 2D
     python tests/golden/make_golden.py REFERENCE_ROOT ref3d_steps     # run_3D.main(): 10 steps at 8^3
+    python tests/golden/make_golden.py REFERENCE_ROOT ref3d_steps16   # run_3D.main(): 3 steps at 16^3
     python tests/golden/make_golden.py REFERENCE_ROOT ref2d_steps     # run_2D.main(): 20 steps at 32^2
     python tests/golden/make_golden.py REFERENCE_ROOT ref3d_fields    # smoke transport + curl, 16x12x8
     python tests/golden/make_golden.py REFERENCE_ROOT ref2d_fields    # advect_smoke + curl, 32x24
@@ -416,6 +417,17 @@ def ref3d_steps():
     return snaps
 
 
+def ref3d_steps16():
+    """run_3D.main() at 16^3 (a two-level MGPCG inside the loop), 3 steps."""
+    nsteps = 3
+    hp = hp3d((16, 16, 16), reinit_every=5, reinit_every_grad_m=2, total_steps=nsteps)
+    R = load3d(hp)
+    snaps = _run_main(R, nsteps, {nsteps}, ["particles_pos", "particles_init_imp"], ["u_x", "u_y", "u_z"])
+    snaps["res"] = np.array([16, 16, 16])
+    snaps["hp"] = np.array([hp["reinit_every"], hp["reinit_every_grad_m"]])
+    return snaps
+
+
 def ref2d_steps():
     nsteps = 20
     hp = hp2d((32, 32), total_steps=nsteps)
@@ -675,7 +687,7 @@ def ref3d_mgpcg():
 
 CASES = dict(ref3d_kernels=ref3d_kernels, ref2d_kernels=ref2d_kernels, ref3d_steps=ref3d_steps,
              ref2d_steps=ref2d_steps, ref3d_fields=ref3d_fields, ref2d_fields=ref2d_fields,
-             ref3d_variants=ref3d_variants, ref3d_mgpcg=ref3d_mgpcg)
+             ref3d_variants=ref3d_variants, ref3d_mgpcg=ref3d_mgpcg, ref3d_steps16=ref3d_steps16)
 
 if __name__ == "__main__":
     if len(sys.argv) != 3 or sys.argv[2] not in CASES:
