@@ -52,3 +52,23 @@ def test_reference_arm_other_ranks_exit_quietly():
                        capture_output=True, text=True, env=env, timeout=120)
     assert r.returncode == 0
     assert r.stdout.strip() == ""
+
+
+def test_reference_arm_line_on_rank0():
+    """The reference arm (the oracle's CPU step on the host cores) prints one JSON line with the
+    bench contract's keys; a tiny bounded sample (8^3 steps scaled to 16^3) keeps it quick."""
+    import json
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "0", "--res", "16", "--cpu-res", "8"],
+                       capture_output=True, text=True, env=dict(os.environ, RANK="0", WORLD_SIZE="1"), timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [x for x in r.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["unit"] == "steps/s" and d["higher_is_better"] is True
+    assert d["value"] > 0 and d["steps"] == 1 and d["warmup"] == 0 and d["n_gpus"] == 1
+    assert d["ms_per_step"] == pytest.approx(1e3 / d["value"])
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
+    assert d["cpu_baseline"]["cores"] >= 1
+    assert d["e2e"] == {"value": d["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert "16^3" in d["config"]["workload"]
