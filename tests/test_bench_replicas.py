@@ -57,7 +57,6 @@ def test_reference_arm_other_ranks_exit_quietly():
 def test_reference_arm_line_on_rank0():
     """The reference arm (the oracle's CPU step on the host cores) prints one JSON line with the
     bench contract's keys; a tiny bounded sample (8^3 steps scaled to 16^3) keeps it quick."""
-    import json
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
                         "--warmup", "0", "--res", "16", "--cpu-res", "8"],
                        capture_output=True, text=True, env=dict(os.environ, RANK="0", WORLD_SIZE="1"), timeout=300)
